@@ -1,0 +1,441 @@
+// rp_api.cu -- C ABI of libraypath: errors, parameters, resident scenes,
+// spectral tables, and the rp_simulate dispatch to the two forms.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "rp_internal.h"
+
+// ---------------------------------------------------------------- errors --
+static thread_local char g_err[1024] = "";
+thread_local int64_t g_launches = 0;
+
+void rp_set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int rp_cuda_fail(cudaError_t e, const char* what) {
+    rp_set_error("CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
+    return RP_ERR_CUDA;
+}
+
+int Arena::reserve(size_t bytes) {
+    if (bytes <= cap) return RP_OK;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    size_t want = bytes + bytes / 8 + (1 << 20);
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        rp_set_error("device scratch allocation of %zu bytes failed: %s", want, cudaGetErrorString(e));
+        return RP_ERR_NOMEM;
+    }
+    cap = want;
+    return RP_OK;
+}
+
+void Arena::release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    off = 0;
+}
+
+extern "C" const char* rp_version(void) { return "raypath-gb300 1.0 (sm_103a)"; }
+
+extern "C" int rp_last_error(char* buf, size_t len) {
+    if (!buf || len == 0) return RP_ERR_ARG;
+    snprintf(buf, len, "%s", g_err);
+    return RP_OK;
+}
+
+extern "C" int rp_last_launch_count(int64_t* n) {
+    if (!n) return RP_ERR_ARG;
+    *n = g_launches;
+    return RP_OK;
+}
+
+// ------------------------------------------------------------ parameters --
+// Derivations of parseSimulationParameters, src/CUDA/file_io.cu:167-213.
+extern "C" int rp_params_derive(rp_params* p) {
+    if (!p) { rp_set_error("rp_params_derive: null params"); return RP_ERR_ARG; }
+    if (!(p->frequency > 0) || !(p->bandwidth > 0) || !(p->rx_sample_rate > 0) ||
+        !(p->rx_window_m > 0) || !(p->eps_1 > 0) || !(p->eps_2 > 0) || !(p->fs > 0)) {
+        rp_set_error("rp_params_derive: frequency, bandwidth, rx_sample_rate, rx_window_m, "
+                     "eps_1, eps_2 and fs must be positive");
+        return RP_ERR_ARG;
+    }
+    const double c = 299792458.0;
+    p->c = c;
+    p->rng_res = c / p->bandwidth;
+    p->lam = c / p->frequency;
+    p->k = 2 * RP_PI_F / p->lam;
+    p->grefr_lin = std::pow(10.0, p->subsurface_gain / 10.0);
+    p->grefl_lin = std::pow(10.0, p->surface_gain / 10.0);
+    p->ks = p->k * p->rms_height;
+    p->c_1 = c / std::sqrt(p->eps_1);
+    p->c_2 = c / std::sqrt(p->eps_2);
+    p->nu_1 = 376.7 / std::sqrt(p->eps_1);
+    p->nu_2 = 376.7 / std::sqrt(p->eps_2);
+    auto alpha = [&](double sig, double eps) {
+        double epp = sig / (2 * RP_PI_FRIIS * p->frequency * 8.85e-12);
+        double a = std::sqrt(1 + (epp / eps) * (epp / eps)) - 1;
+        a = std::sqrt(0.5 * eps * a);
+        return (a * 2 * RP_PI_FRIIS) / p->lam;
+    };
+    p->alpha1 = alpha(p->sig_1, p->eps_1);
+    p->alpha2 = alpha(p->sig_2, p->eps_2);
+    // nr keeps the reference's float expression (file_io.cu:212) bit for bit.
+    float nrf = ((float)p->rx_window_m / 299792480.0f) * (float)p->rx_sample_rate;
+    if (!(nrf >= 2.0f) || nrf > 1.0e6f) {
+        rp_set_error("rp_params_derive: rx_window_m and rx_sample_rate give %g range bins", (double)nrf);
+        return RP_ERR_ARG;
+    }
+    p->nr = (int32_t)nrf;
+    p->dr = p->rx_window_m / (double)p->nr;
+    return RP_OK;
+}
+
+// loadAttenPrismFile's conductivity -> alpha, src/CUDA/file_io.cu:501-505.
+extern "C" int rp_prism_alpha(const rp_params* p, double sig, double* alpha) {
+    if (!p || !alpha) { rp_set_error("rp_prism_alpha: null argument"); return RP_ERR_ARG; }
+    double epp = sig / (2 * RP_PI_FRIIS * p->frequency * 8.85e-12);
+    double a = std::sqrt(1 + (epp / p->eps_2) * (epp / p->eps_2)) - 1;
+    a = std::sqrt(0.5 * p->eps_2 * a);
+    *alpha = (a * 2 * RP_PI_FRIIS) / p->lam;
+    return RP_OK;
+}
+
+// ----------------------------------------------------------- host tables --
+using cd = std::complex<double>;
+
+static void host_fft(std::vector<cd>& a, int sign) {
+    const int n = (int)a.size();
+    for (int i = 1, j = 0; i < n; ++i) {
+        int bit = n >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) std::swap(a[i], a[j]);
+    }
+    for (int len = 2; len <= n; len <<= 1) {
+        int half = len >> 1;
+        for (int k = 0; k < half; ++k) {
+            double ang = sign * 2.0 * RP_PI * k / len;
+            cd w(std::cos(ang), std::sin(ang));
+            for (int i = 0; i < n; i += len) {
+                cd u = a[i + k], v = a[i + k + half] * w;
+                a[i + k] = u + v;
+                a[i + k + half] = u - v;
+            }
+        }
+    }
+}
+
+static double host_sinc(double x) {
+    if (std::fabs(x) < 1e-6) return 1.0;
+    return std::sin(RP_PI * x) / (RP_PI * x);
+}
+
+template <class T>
+static int upload(T** dst, const void* src, size_t bytes, size_t* acc) {
+    if (bytes == 0) { *dst = nullptr; return RP_OK; }
+    RP_CUDA(cudaMalloc((void**)dst, bytes));
+    RP_CUDA(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+    if (acc) *acc += bytes;
+    return RP_OK;
+}
+
+static int upload_cplx(const std::vector<cd>& v, double** d64, float** d32, size_t* acc) {
+    std::vector<double> a(2 * v.size());
+    std::vector<float> b(2 * v.size());
+    for (size_t i = 0; i < v.size(); ++i) {
+        a[2 * i] = v[i].real(); a[2 * i + 1] = v[i].imag();
+        b[2 * i] = (float)v[i].real(); b[2 * i + 1] = (float)v[i].imag();
+    }
+    int rc = upload(d64, a.data(), a.size() * sizeof(double), acc);
+    if (rc) return rc;
+    return upload(d32, b.data(), b.size() * sizeof(float), acc);
+}
+
+static std::vector<cd> twiddles(int n) {
+    std::vector<cd> t(n / 2);
+    for (int k = 0; k < n / 2; ++k) {
+        double ang = -2.0 * RP_PI * k / n;
+        t[k] = cd(std::cos(ang), std::sin(ang));
+    }
+    return t;
+}
+
+static bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+// Bluestein chirp w_k = e^{-i pi k^2 / n} (angle reduced exactly mod 2 pi).
+static std::vector<cd> bluestein_chirp(int n) {
+    std::vector<cd> w(n);
+    for (int k = 0; k < n; ++k) {
+        long long kk = ((long long)k * k) % (2LL * n);
+        double ang = -RP_PI * (double)kk / n;
+        w[k] = cd(std::cos(ang), std::sin(ang));
+    }
+    return w;
+}
+
+static std::vector<cd> bluestein_kernel(const std::vector<cd>& w, int M) {
+    const int n = (int)w.size();
+    std::vector<cd> b(M, cd(0, 0));
+    for (int k = 0; k < n; ++k) {
+        b[k] = std::conj(w[k]);
+        if (k) b[M - k] = std::conj(w[k]);
+    }
+    host_fft(b, -1);
+    return b;
+}
+
+// Forward DFT of any length on the host (FP64), cuFFT sign convention.
+static std::vector<cd> host_dft(std::vector<cd> x) {
+    const int n = (int)x.size();
+    if (is_pow2(n)) { host_fft(x, -1); return x; }
+    int M = 1;
+    while (M < 2 * n - 1) M <<= 1;
+    std::vector<cd> w = bluestein_chirp(n), b = bluestein_kernel(w, M), y(M, cd(0, 0));
+    for (int k = 0; k < n; ++k) y[k] = x[k] * w[k];
+    host_fft(y, -1);
+    for (int k = 0; k < M; ++k) y[k] *= b[k];
+    host_fft(y, +1);
+    for (int k = 0; k < n; ++k) x[k] = y[k] * w[k] / (double)M;
+    return x;
+}
+
+static int build_plan(DftPlan& pl, int n, size_t* acc) {
+    pl.n = n;
+    pl.pow2 = is_pow2(n);
+    int M = 1;
+    if (pl.pow2) M = n;
+    else while (M < 2 * n - 1) M <<= 1;
+    int l = 0;
+    while ((1 << l) < M) ++l;
+    pl.log2M = l;
+    int rc = upload_cplx(twiddles(M), &pl.tw64, &pl.tw32, acc);
+    if (rc || pl.pow2) return rc;
+    std::vector<cd> w = bluestein_chirp(n);
+    if ((rc = upload_cplx(w, &pl.bw64, &pl.bw32, acc))) return rc;
+    return upload_cplx(bluestein_kernel(w, M), &pl.bW64, &pl.bW32, acc);
+}
+
+static void free_plan(DftPlan& pl) {
+    void* ptrs[] = {pl.tw64, pl.bw64, pl.bW64, pl.tw32, pl.bw32, pl.bW32};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    pl = DftPlan();
+}
+
+static int build_tables(rp_scene* s) {
+    const rp_params& p = s->p;
+    const int nr = p.nr;
+    s->nr = nr;
+    size_t acc = 0;
+    int rc;
+    if ((rc = build_plan(s->plan2, 2 * nr, &acc))) return rc;
+    if ((rc = build_plan(s->planN, 2 * nr - 1, &acc))) return rc;
+    // chirp spectra (genCenteredChirpPadded, radar_kernels.cu:489-503)
+    std::vector<cd> c1(2 * nr), c2(2 * nr);
+    for (int i = 0; i < 2 * nr; ++i) {
+        double off = (double)(i - nr / 2) * p.dr;
+        c1[i] = cd(host_sinc(off / p.rng_res), 0.0);
+        c2[i] = cd(host_sinc(off / (2 * p.rng_res)), 0.0);
+    }
+    if ((rc = upload_cplx(host_dft(c1), &s->d_C1_64, &s->d_C1_32, &acc))) return rc;
+    if ((rc = upload_cplx(host_dft(c2), &s->d_C2_64, &s->d_C2_32, &acc))) return rc;
+    // cropSpectrum (elementary_kernels.cu:258-278): keep |freq_k| <= B on the
+    // N-point grid; the kept set is min(k, N-k) <= K.
+    const int N = 2 * nr - 1;
+    int K = -1;
+    for (int m = 0; m <= N / 2; ++m)
+        if (!(std::fabs((double)m * p.rx_sample_rate / N) > p.bandwidth)) K = m;
+    s->crop_K = K;
+    s->crop_all = (K >= N / 2);
+    s->store_bytes += acc;
+    return RP_OK;
+}
+
+// Morton order of facet centres (spatial locality for the fast form).
+static uint64_t spread16(uint32_t v) {
+    uint64_t x = v & 0xffff;
+    x = (x | (x << 8)) & 0x00ff00ff;
+    x = (x | (x << 4)) & 0x0f0f0f0f;
+    x = (x | (x << 2)) & 0x33333333;
+    x = (x | (x << 1)) & 0x55555555;
+    return x;
+}
+
+extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t nf,
+                               const double* targets, int64_t nt, const double* prisms,
+                               int64_t np, int device, rp_scene** out) {
+    if (!p || !out || nf < 0 || nt < 0 || np < 0 || (nf > 0 && !facets) ||
+        (nt > 0 && !targets) || (np > 0 && !prisms)) {
+        rp_set_error("rp_scene_create: bad argument");
+        return RP_ERR_ARG;
+    }
+    if (nf > (int64_t)1 << 31) { rp_set_error("rp_scene_create: more than 2^31 facets"); return RP_ERR_ARG; }
+    if (p->nr <= 0 || !(p->lam > 0)) {
+        rp_set_error("rp_scene_create: parameters not derived (call rp_params_derive)");
+        return RP_ERR_ARG;
+    }
+    if (p->specular || !p->convolution || !p->convolution_linear) {
+        rp_set_error("rp_scene_create: only the default mode (specular=false, convolution=true, "
+                     "convolution_linear=true) is implemented");
+        return RP_ERR_UNSUPPORTED;
+    }
+    *out = nullptr;
+    RP_CUDA(cudaSetDevice(device));
+    rp_scene* s = new rp_scene();
+    s->p = *p;
+    s->device = device;
+    s->nf = nf; s->nt = nt; s->np = np;
+    DevParams& d = s->dp;
+    d.lam = p->lam; d.fs = p->fs; d.P = p->power; d.nidx = std::sqrt(p->eps_2);
+    d.eps1 = p->eps_1; d.eps2 = p->eps_2; d.nu1 = p->nu_1; d.nu2 = p->nu_2;
+    d.alpha1 = p->alpha1; d.alpha2 = p->alpha2; d.ks = p->ks; d.c1_over_c2 = p->c_1 / p->c_2;
+    d.dr = p->dr; d.smpl = p->rx_sample_rate; d.B = p->bandwidth; d.rng_res = p->rng_res;
+    d.ap_rad = p->aperture * (RP_PI / 180.0);
+    d.ap_cos = std::cos(d.ap_rad);
+    d.nr = p->nr; d.lossless = p->lossless; d.disable_surface = p->disable_surface;
+    d.rerad_funct = p->rerad_funct;
+    int rc;
+    auto fail = [&](int code) { rp_scene_destroy(s); return code; };
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return fail(rp_cuda_fail(cudaGetLastError(), "cudaGetDeviceProperties"));
+    s->sm_count = prop.multiProcessorCount;
+    if ((rc = upload(&s->d_facets, facets, sizeof(double) * 12 * nf, &s->store_bytes))) return fail(rc);
+    if ((rc = upload(&s->d_targets, targets, sizeof(double) * 7 * nt, &s->store_bytes))) return fail(rc);
+    if ((rc = upload(&s->d_prisms, prisms, sizeof(double) * 7 * np, &s->store_bytes))) return fail(rc);
+    for (int64_t t = 0; t < nt; ++t)
+        if (targets[6 * nt + t] == 0.0) { s->any_ttype0 = 1; break; }
+    // spatially sorted copy for the fast form
+    if (nf > 0) {
+        double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
+        for (int64_t i = 0; i < nf; ++i) {
+            xmin = std::min(xmin, facets[i]); xmax = std::max(xmax, facets[i]);
+            ymin = std::min(ymin, facets[nf + i]); ymax = std::max(ymax, facets[nf + i]);
+        }
+        double sx = (xmax > xmin) ? 65535.0 / (xmax - xmin) : 0.0;
+        double sy = (ymax > ymin) ? 65535.0 / (ymax - ymin) : 0.0;
+        std::vector<uint64_t> key(nf);
+        for (int64_t i = 0; i < nf; ++i) {
+            uint32_t qx = (uint32_t)std::lround((facets[i] - xmin) * sx);
+            uint32_t qy = (uint32_t)std::lround((facets[nf + i] - ymin) * sy);
+            key[i] = (spread16(qy) << 1) | spread16(qx);
+        }
+        std::vector<int64_t> order(nf);
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return key[a] < key[b]; });
+        std::vector<double> sorted((size_t)12 * nf);
+        for (int c = 0; c < 12; ++c)
+            for (int64_t i = 0; i < nf; ++i) sorted[(size_t)c * nf + i] = facets[(size_t)c * nf + order[i]];
+        if ((rc = upload(&s->d_order, order.data(), sizeof(int64_t) * nf, &s->store_bytes))) return fail(rc);
+        if ((rc = upload(&s->d_sorted, sorted.data(), sizeof(double) * 12 * nf, &s->store_bytes))) return fail(rc);
+    }
+    if ((rc = build_tables(s))) return fail(rc);
+    cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(rp_cuda_fail(e, "cudaStreamCreate"));
+    *out = s;
+    return RP_OK;
+}
+
+extern "C" int rp_scene_destroy(rp_scene* s) {
+    if (!s) return RP_OK;
+    cudaSetDevice(s->device);
+    if (s->own_stream) cudaStreamSynchronize(s->own_stream);
+    void* ptrs[] = {s->d_facets, s->d_targets, s->d_prisms, s->d_order, s->d_sorted,
+                    s->d_C1_64, s->d_C2_64, s->d_C1_32, s->d_C2_32};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    free_plan(s->plan2);
+    free_plan(s->planN);
+    s->arena.release();
+    if (s->own_stream) cudaStreamDestroy(s->own_stream);
+    delete s;
+    return RP_OK;
+}
+
+extern "C" int rp_scene_footprint(const rp_scene* s, int64_t* bytes) {
+    if (!s || !bytes) { rp_set_error("rp_scene_footprint: null argument"); return RP_ERR_ARG; }
+    *bytes = (int64_t)s->store_bytes;
+    return RP_OK;
+}
+
+extern "C" int rp_query_footprint(const rp_scene* s, int64_t ns, int form, int64_t* bytes) {
+    if (!s || !bytes || ns < 0) { rp_set_error("rp_query_footprint: bad argument"); return RP_ERR_ARG; }
+    int f = form & 0xff;
+    if (f == RP_FORM_PLAIN_F64) *bytes = (int64_t)rp_plain_scratch(s, ns);
+    else if (f == RP_FORM_FAST_F32) *bytes = (int64_t)rp_fast_scratch(s, ns);
+    else { rp_set_error("rp_query_footprint: unknown form %d", form); return RP_ERR_ARG; }
+    return RP_OK;
+}
+
+static int run_form(rp_scene* s, const double* d_traces, int64_t ns, int form, void* d_out,
+                    int64_t* counts, cudaStream_t st) {
+    int f = form & 0xff;
+    int out64 = (form & RP_OUT_COMPLEX128) ? 1 : 0;
+    if (f == RP_FORM_PLAIN_F64) return rp_plain_run(s, d_traces, ns, d_out, out64, counts, st);
+    if (f == RP_FORM_FAST_F32) return rp_fast_run(s, d_traces, ns, d_out, out64, counts, st);
+    rp_set_error("unknown form %d", form);
+    return RP_ERR_ARG;
+}
+
+extern "C" int rp_simulate_device(rp_scene* s, const double* d_traces, int64_t ns, int form,
+                                  void* d_out, int64_t* counts, void* stream) {
+    if (!s || ns < 0 || (ns > 0 && (!d_traces || !d_out))) {
+        rp_set_error("rp_simulate_device: bad argument");
+        return RP_ERR_ARG;
+    }
+    g_launches = 0;
+    RP_CUDA(cudaSetDevice(s->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->own_stream;
+    if (ns == 0) return RP_OK;
+    return run_form(s, d_traces, ns, form, d_out, counts, st);
+}
+
+extern "C" int rp_simulate(rp_scene* s, const double* traces, int64_t ns, int form, void* out,
+                           int out_on_device, int64_t* counts, void* stream) {
+    if (!s || ns < 0 || (ns > 0 && (!traces || !out))) {
+        rp_set_error("rp_simulate: bad argument");
+        return RP_ERR_ARG;
+    }
+    g_launches = 0;
+    RP_CUDA(cudaSetDevice(s->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->own_stream;
+    if (ns == 0) return RP_OK;
+    const size_t esz = (form & RP_OUT_COMPLEX128) ? 16 : 8;
+    const size_t out_bytes = esz * (size_t)s->nr * ns;
+    double* d_tr = nullptr;
+    void* d_out = out_on_device ? out : nullptr;
+    RP_CUDA(cudaMallocAsync((void**)&d_tr, sizeof(double) * 9 * ns, st));
+    if (!out_on_device) {
+        cudaError_t e = cudaMallocAsync(&d_out, out_bytes, st);
+        if (e != cudaSuccess) { cudaFreeAsync(d_tr, st); return rp_cuda_fail(e, "cudaMallocAsync(out)"); }
+    }
+    int rc = RP_OK;
+    cudaError_t e = cudaMemcpyAsync(d_tr, traces, sizeof(double) * 9 * ns, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) rc = rp_cuda_fail(e, "cudaMemcpyAsync(traces)");
+    if (rc == RP_OK) rc = run_form(s, d_tr, ns, form, d_out, counts, st);
+    if (rc == RP_OK && !out_on_device) {
+        e = cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) rc = rp_cuda_fail(e, "cudaMemcpyAsync(out)");
+    }
+    cudaFreeAsync(d_tr, st);
+    if (!out_on_device) cudaFreeAsync(d_out, st);
+    e = cudaStreamSynchronize(st);
+    if (rc == RP_OK && e != cudaSuccess) rc = rp_cuda_fail(e, "cudaStreamSynchronize");
+    return rc;
+}

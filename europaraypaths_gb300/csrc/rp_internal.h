@@ -1,0 +1,118 @@
+// rp_internal.h -- shared host/device definitions of libraypath.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/raypath.h"
+
+// Constants exactly as the reference spells them.
+#define RP_PI_F 3.14159265      // geometry_kernels.cu:45, radar_kernels.cu:682
+#define RP_PI_FRIIS 3.14159     // geometry_kernels.cu:411, file_io.cu:196
+#define RP_PI 3.14159265358979323846
+
+// Output flag OR'ed into `form`: write complex128 instead of complex64.
+#define RP_OUT_COMPLEX128 0x100
+
+// Fixed-point scale headroom for deterministic integer accumulation.
+#define RP_FIX_BITS 60
+
+void rp_set_error(const char* fmt, ...);
+int rp_cuda_fail(cudaError_t e, const char* what);
+
+#define RP_CUDA(call)                                                    \
+    do {                                                                 \
+        cudaError_t _e = (call);                                         \
+        if (_e != cudaSuccess) return rp_cuda_fail(_e, #call);           \
+    } while (0)
+
+// Device-side copy of the constants every kernel needs (FP64).
+struct DevParams {
+    double lam, fs, P, nidx, eps1, eps2, nu1, nu2, alpha1, alpha2, ks, c1_over_c2;
+    double dr, smpl, B, rng_res, ap_rad, ap_cos;
+    int nr, lossless, disable_surface, rerad_funct;
+};
+
+// Grow-only device arena for per-call scratch.
+struct Arena {
+    void* ptr = nullptr;
+    size_t cap = 0;
+    size_t off = 0;
+    int reserve(size_t bytes);          // make sure cap >= bytes (frees old)
+    void reset() { off = 0; }
+    template <class T>
+    T* take(size_t n) {
+        size_t a = (off + 255) & ~size_t(255);
+        off = a + n * sizeof(T);
+        return reinterpret_cast<T*>(static_cast<char*>(ptr) + a);
+    }
+    void release();
+};
+
+// Bytes a take<T>(n) sequence needs, for sizing an Arena.
+struct ArenaPlan {
+    size_t off = 0;
+    template <class T>
+    void take(size_t n) { off = ((off + 255) & ~size_t(255)) + n * sizeof(T); }
+};
+
+// A DFT of length n on the device: a radix-2 FFT when n is a power of two,
+// else Bluestein's chirp-z transform through a power-of-two length M.
+struct DftPlan {
+    int n = 0;
+    int pow2 = 0;          // n is a power of two
+    int log2M = 0;         // log2 of the FFT length actually run (n or M)
+    double* tw64 = nullptr;   // e^{-2 pi i k / M}, k < M/2
+    double* bw64 = nullptr;   // Bluestein w_k = e^{-i pi k^2 / n}, k < n
+    double* bW64 = nullptr;   // FFT_M of the conjugate chirp
+    float* tw32 = nullptr;
+    float* bw32 = nullptr;
+    float* bW32 = nullptr;
+    int M() const { return 1 << log2M; }
+};
+
+struct rp_scene {
+    rp_params p;
+    DevParams dp;
+    int device = 0;
+    int64_t nf = 0, nt = 0, np = 0;
+    int nr = 0;
+    // ---- plain store: original facet order, FP64 SoA [12][nf]
+    double* d_facets = nullptr;
+    // ---- targets FP64 SoA [7][nt], prisms FP64 SoA [7][np]
+    double* d_targets = nullptr;
+    double* d_prisms = nullptr;
+    int any_ttype0 = 0;
+    // ---- fast store: spatially sorted facets
+    int64_t* d_order = nullptr;          // sorted position -> original index
+    double* d_sorted = nullptr;          // FP64 SoA [12][nf] in sorted order
+    // ---- per-scene spectral tables
+    DftPlan plan2;                       // length 2 nr (linear chirp convolution)
+    DftPlan planN;                       // length N = 2 nr - 1 (convolveComplex)
+    double* d_C1_64 = nullptr;           // DFT_2nr of the surface chirp (complex)
+    double* d_C2_64 = nullptr;           // DFT_2nr of the target chirp (complex)
+    float* d_C1_32 = nullptr;
+    float* d_C2_32 = nullptr;
+    int crop_K = 0;                      // kept spectrum half-width on the N grid
+    int crop_all = 0;                    // crop keeps every bin
+    // ---- scratch
+    Arena arena;
+    cudaStream_t own_stream = nullptr;
+    int sm_count = 0;
+    size_t store_bytes = 0;
+};
+
+// Per-thread launch counter (rp_last_launch_count).
+extern thread_local int64_t g_launches;
+#define RP_LAUNCHED() (++g_launches)
+
+// Entry points of the two forms (rp_plain.cu, rp_fast.cu).
+int rp_plain_run(rp_scene* s, const double* d_traces, int64_t ns, void* d_out, int out64,
+                 int64_t* h_counts, cudaStream_t st);
+int rp_fast_run(rp_scene* s, const double* d_traces, int64_t ns, void* d_out, int out64,
+                int64_t* h_counts, cudaStream_t st);
+size_t rp_plain_scratch(const rp_scene* s, int64_t ns);
+size_t rp_fast_scratch(const rp_scene* s, int64_t ns);

@@ -1,0 +1,131 @@
+"""Resident-scene simulation API over the C ABI (libraypath.so).
+
+``Scene`` owns a device-resident facet store (created once, reused by every
+call), and ``Scene.simulate`` runs any number of traces in one call -- the
+trace loop of ``src/CUDA/sim.cu:615-1008`` without its per-trace files.
+``simulate(params, facets, targets)`` is the one-shot convenience form and
+returns a complex64 radargram shaped like ``compile_rdrgrm``'s (nr, ns).
+
+Forms: ``"fast"`` (fused FP32 split-precision kernels) and ``"plain"`` (the
+FP64 restatement of the reference trace loop).  There is no CPU fallback:
+without the library, or without a GPU, calls raise.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from . import param_gen
+from . import traces as _traces
+
+FORMS = {"plain": _abi.RP_FORM_PLAIN_F64, "fast": _abi.RP_FORM_FAST_F32}
+OUT_COMPLEX128 = 0x100
+
+
+def _as_params(params):
+    if isinstance(params, _abi.RpParams):
+        return params
+    return param_gen.to_rp_params(params)
+
+
+def prisms_from_conductivity(p, prisms_cond):
+    """(7, P) prisms with a conductivity row -> alpha row (rp_prism_alpha)."""
+    pr = np.array(prisms_cond, dtype=np.float64).reshape(7, -1).copy()
+    lib = _abi.lib()
+    for k in range(pr.shape[1]):
+        a = ctypes.c_double()
+        _abi.check("rp_prism_alpha", lib.rp_prism_alpha(ctypes.byref(p), float(pr[0, k]), ctypes.byref(a)))
+        pr[0, k] = a.value
+    return pr
+
+
+class Scene:
+    """A resident scene: facets (12, N), targets (7, T), prisms (7, P) with alpha."""
+
+    def __init__(self, params, facets, targets=None, prisms=None, device=0):
+        self.params = _as_params(params)
+        self.facets = np.ascontiguousarray(facets, dtype=np.float64).reshape(12, -1)
+        if targets is None:
+            targets = np.zeros((7, 0))
+        self.targets = np.ascontiguousarray(targets, dtype=np.float64).reshape(7, -1)
+        if prisms is None:
+            prisms = np.zeros((7, 0))
+        self.prisms = np.ascontiguousarray(prisms, dtype=np.float64).reshape(7, -1)
+        self.nr = int(self.params.nr)
+        self._h = ctypes.c_void_p()
+        lib = _abi.lib()
+        rc = lib.rp_scene_create(ctypes.byref(self.params), self.facets.ctypes.data,
+                                 self.facets.shape[1], self.targets.ctypes.data,
+                                 self.targets.shape[1], self.prisms.ctypes.data,
+                                 self.prisms.shape[1], int(device), ctypes.byref(self._h))
+        _abi.check("rp_scene_create", rc)
+
+    @property
+    def handle(self):
+        return self._h.value
+
+    def close(self):
+        if self._h and self._h.value:
+            _abi.lib().rp_scene_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def footprint(self):
+        b = ctypes.c_int64()
+        _abi.check("rp_scene_footprint", _abi.lib().rp_scene_footprint(self._h, ctypes.byref(b)))
+        return b.value
+
+    def scratch_bytes(self, ns, form="fast"):
+        b = ctypes.c_int64()
+        _abi.check("rp_query_footprint",
+                   _abi.lib().rp_query_footprint(self._h, int(ns), FORMS[form], ctypes.byref(b)))
+        return b.value
+
+    def default_traces(self):
+        return _traces.linear_track(self.params)
+
+    def simulate(self, traces=None, form="fast", complex128=False, return_counts=False):
+        """Simulate traces (ns, 9) on host memory; returns complex (ns, nr)."""
+        tr = self.default_traces() if traces is None else traces
+        tr = np.ascontiguousarray(tr, dtype=np.float64).reshape(-1, 9)
+        ns = tr.shape[0]
+        out = np.zeros((ns, self.nr), np.complex128 if complex128 else np.complex64)
+        counts = np.zeros((ns, 2), np.int64)
+        f = FORMS[form] | (OUT_COMPLEX128 if complex128 else 0)
+        rc = _abi.lib().rp_simulate(self._h, tr.ctypes.data, ns, f, out.ctypes.data, 0,
+                                    counts.ctypes.data, None)
+        _abi.check("rp_simulate", rc)
+        return (out, counts) if return_counts else out
+
+    def simulate_device(self, d_traces, d_out, form="fast", stream=None, complex128=False):
+        """Resident-input path: d_traces (ns, 9) float64 and d_out (ns, nr)
+        complex64 torch CUDA tensors; runs on ``stream`` (a torch stream)."""
+        ns = int(d_traces.shape[0])
+        f = FORMS[form] | (OUT_COMPLEX128 if complex128 else 0)
+        sp = None if stream is None else ctypes.c_void_p(stream.cuda_stream)
+        rc = _abi.lib().rp_simulate_device(self._h, ctypes.c_void_p(d_traces.data_ptr()), ns, f,
+                                           ctypes.c_void_p(d_out.data_ptr()), None, sp)
+        _abi.check("rp_simulate_device", rc)
+
+
+def last_launch_count():
+    n = ctypes.c_int64()
+    _abi.lib().rp_last_launch_count(ctypes.byref(n))
+    return n.value
+
+
+def simulate(params, facets, targets=None, traces=None, form="fast", prisms=None, device=0):
+    """One-shot simulation; returns the complex64 radargram (nr, ns)."""
+    with Scene(params, facets, targets, prisms, device) as sc:
+        return sc.simulate(traces, form=form).T

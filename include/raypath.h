@@ -1,0 +1,163 @@
+/*
+ * raypath.h -- C ABI of libraypath.so, the GB300 radar-sounder raypath engine.
+ *
+ * Every function returns an int status: RP_OK (0) or a negative RP_ERR_* code.
+ * rp_last_error() returns the text of the calling thread's last error.  No
+ * function calls exit(); no function throws across the ABI.
+ *
+ * Array layouts (all row-major, host pointers unless stated otherwise):
+ *   facets   double[12][n]   SoA: x,y,z, nx,ny,nz, ux,uy,uz, vx,vy,vz
+ *            (the twelve arrays of loadFacetFile, src/CUDA/file_io.cu:337-362)
+ *   targets  double[7][nt]   SoA: x,y,z, nx,ny,nz, ttype
+ *            (loadTargetFile, src/CUDA/file_io.cu:365-426)
+ *   prisms   double[7][np]   SoA: alpha[Np/m], xmin,ymin,zmin, xmax,ymax,zmax
+ *            (loadAttenPrismFile, src/CUDA/file_io.cu:477-517, conductivity
+ *            already turned into alpha by rp_prism_alpha)
+ *   traces   double[ns][9]   per trace: sx,sy,sz, snx,sny,snz, rst,
+ *            grefl_lin, grefr_lin (the per-trace state of the trace loop,
+ *            src/CUDA/sim.cu:621-651; the source normal already multiplied by
+ *            source_normal_multiplier)
+ *   out      float2[ns][nr]  complex64 radargram columns (what
+ *            saveSignalToFile writes per trace, src/CUDA/file_io.cu:284-296)
+ */
+#ifndef RAYPATH_H
+#define RAYPATH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    RP_OK = 0,
+    RP_ERR_ARG = -1,         /* bad argument or size                           */
+    RP_ERR_IO = -2,          /* file missing / unreadable / not a directory    */
+    RP_ERR_PARSE = -3,       /* malformed JSON or text record                  */
+    RP_ERR_CUDA = -4,        /* CUDA runtime error (text in rp_last_error)     */
+    RP_ERR_NOMEM = -5,       /* host or device allocation failed               */
+    RP_ERR_UNSUPPORTED = -6, /* mode not implemented by the requested form     */
+    RP_ERR_BUDGET = -7,      /* request exceeds the admission memory budget    */
+    RP_ERR_TIMEOUT = -8,     /* a bounded wait ran out                         */
+    RP_ERR_INTERNAL = -9     /* invariant violated (bin window overflow, ...)  */
+};
+
+/* Simulation form. */
+enum {
+    RP_FORM_PLAIN_F64 = 0,   /* FP64 restatement of the reference trace loop    */
+    RP_FORM_FAST_F32 = 1     /* fused FP32 split-precision form                 */
+};
+
+/*
+ * Simulation parameters: the JSON keys read by parseSimulationParameters
+ * (src/CUDA/file_io.cu:122-249) plus the constants it derives
+ * (file_io.cu:168-213).  Fill the inputs, then call rp_params_derive().
+ */
+typedef struct rp_params {
+    /* ---- inputs (JSON keys) ---- */
+    double frequency;            /* "frequency"  [Hz]                         */
+    double bandwidth;            /* "bandwidth"  [Hz]                         */
+    double power;                /* "power"      [W]                          */
+    double aperture;             /* "aperture"   [deg]                        */
+    double surface_gain;         /* "surface_gain"    [dB]                    */
+    double subsurface_gain;      /* "subsurface_gain" [dB]                    */
+    double rms_height;           /* "rms_height" [m]                          */
+    double buff;                 /* "buff"                                    */
+    double eps_1, eps_2;         /* "eps_1", "eps_2"                          */
+    double sig_1, sig_2;         /* "sig_1", "sig_2" [S/m]                    */
+    double rx_sample_rate;       /* "rx_sample_rate" [Hz]                     */
+    double rx_window_m;          /* "rx_window_m" [m]                         */
+    double rx_window_offset_m;   /* "rx_window_offset_m" [m] (static rst)     */
+    double fs;                   /* "fs" facet size [m]                       */
+    double source_normal_multiplier; /* "source_normal_multiplier" (1)        */
+    double altitude;             /* "altitude" (0)                            */
+    double sx0, sdx, sy, sz;     /* linear source track                       */
+    int32_t ns;                  /* "ns"                                      */
+    int32_t rerad_funct;         /* "rerad_funct"                             */
+    int32_t convolution;         /* "convolution"        (bool)               */
+    int32_t convolution_linear;  /* "convolution_linear" (bool)               */
+    int32_t specular;            /* "specular"           (bool)               */
+    int32_t lossless;            /* "lossless"           (bool)               */
+    int32_t incoherent;          /* "incoherent"         (bool, false)        */
+    int32_t disable_surface;     /* "disable_surface"    (bool, false)        */
+    int32_t debug_surface;       /* "debug_surface"      (bool, false)        */
+    int32_t pol;                 /* polarisation: 0 = H (never parsed, 0)     */
+    /* ---- derived by rp_params_derive ---- */
+    double c;                    /* speed of light                            */
+    double lam, k;               /* wavelength, wavenumber                    */
+    double rng_res;              /* c / bandwidth                             */
+    double grefl_lin, grefr_lin; /* 10^(gain/10)                              */
+    double ks;                   /* k * rms_height                            */
+    double c_1, c_2;             /* c / sqrt(eps)                             */
+    double nu_1, nu_2;           /* 376.7 / sqrt(eps)                         */
+    double alpha1, alpha2;       /* attenuation constants [Np/m]              */
+    double dr;                   /* rx_window_m / nr                          */
+    int32_t nr;                  /* range bins (float expression file_io.cu:212) */
+    int32_t reserved;
+} rp_params;
+
+/* Opaque resident scene (facet store, targets, prisms on the device). */
+typedef struct rp_scene rp_scene;
+
+/* Library version string, e.g. "raypath-gb300 1.0". */
+const char* rp_version(void);
+
+/* Copy the calling thread's last error text into buf (always terminated). */
+int rp_last_error(char* buf, size_t len);
+
+/* Fill the derived fields of p.  Replaces the derivations of
+ * parseSimulationParameters, src/CUDA/file_io.cu:167-213. */
+int rp_params_derive(rp_params* p);
+
+/* Conductivity [S/m] of an attenuation prism to alpha [Np/m].  Replaces the
+ * conversion inside loadAttenPrismFile, src/CUDA/file_io.cu:501-505. */
+int rp_prism_alpha(const rp_params* p, double conductivity, double* alpha);
+
+/*
+ * Create a resident scene: the facet store is laid out on the device once
+ * and reused by every rp_simulate call.  Replaces the facet/target/prism
+ * loading and H2D copies of src/CUDA/sim.cu:185-311 and :477-531.
+ * device: CUDA device ordinal.
+ */
+int rp_scene_create(const rp_params* p,
+                    const double* facets, int64_t n_facets,
+                    const double* targets, int64_t n_targets,
+                    const double* prisms, int64_t n_prisms,
+                    int device, rp_scene** out);
+
+int rp_scene_destroy(rp_scene* s);
+
+/* Device bytes held by the scene's resident stores. */
+int rp_scene_footprint(const rp_scene* s, int64_t* bytes);
+
+/* Device bytes a rp_simulate call of ns traces needs as scratch, per form. */
+int rp_query_footprint(const rp_scene* s, int64_t ns, int form, int64_t* bytes);
+
+/*
+ * Simulate ns traces (one radargram column each).  Replaces the trace loop
+ * of src/CUDA/sim.cu:615-1008 (one call covers many iterations of it).
+ *   traces  host double[ns][9] (see above)
+ *   out     float2[ns][nr]; host memory when out_on_device == 0, else device
+ *   counts  optional host int64[ns][2]: illuminated facets and in-aperture
+ *           targets per trace (the N_ill and N_t of the pair count); may be NULL
+ *   stream  cudaStream_t to run on (NULL = the library's own stream)
+ * A trace with no illuminated facet yields a zero column (the reference
+ * skips writing its file, src/CUDA/sim.cu:693-697; counts report N_ill = 0).
+ */
+int rp_simulate(rp_scene* s, const double* traces, int64_t ns, int form,
+                void* out, int out_on_device, int64_t* counts, void* stream);
+
+/* Same as rp_simulate with the trace table already in device memory
+ * (double[ns][9]) -- the resident-input path used for throughput runs. */
+int rp_simulate_device(rp_scene* s, const double* d_traces, int64_t ns, int form,
+                       void* d_out, int64_t* counts, void* stream);
+
+/* Number of kernel launches issued by this thread's last rp_simulate*. */
+int rp_last_launch_count(int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RAYPATH_H */
