@@ -309,6 +309,7 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
     d.dr = p->dr; d.smpl = p->rx_sample_rate; d.B = p->bandwidth; d.rng_res = p->rng_res;
     d.ap_rad = p->aperture * (RP_PI / 180.0);
     d.ap_cos = std::cos(d.ap_rad);
+    d.turn = RP_PI_F / (RP_PI * p->lam);
     d.nr = p->nr; d.lossless = p->lossless; d.disable_surface = p->disable_surface;
     d.rerad_funct = p->rerad_funct;
     int rc;

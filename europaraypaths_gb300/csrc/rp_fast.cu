@@ -130,7 +130,8 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
         double Ps = d_friis(Pf, G, t.grefr, dp.lam, d);
         if (!dp.lossless) Ps *= fre;
         double amp = sqrt(Ps);
-        double tt = 2.0 * d / dp.lam;                 // phase in turns: exp(-j 2 pi tt)
+        // phase in turns: phasor(2 Itd) = exp(-j (2 pi_F/lam) 2 Itd) = exp(-j 2 pi tt)
+        double tt = 2.0 * d * dp.turn;
         double ft = tt - floor(tt);
         double sn, cs;
         sincospi(-2.0 * ft, &sn, &cs);
@@ -143,7 +144,7 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
         double Kf = sqrt(dp.P * t.grefr * G * (dp.lossless ? 1.0 : frc) * dp.nidx) * dp.lam *
                     dp.lam * Dmax / (f4 * d);
         xI = (float)((d - t.rst) / dp.dr);
-        double ti = d / dp.lam;
+        double ti = d * dp.turn;
         float tauI = (float)(ti - floor(ti));
         float ddx = (float)(fx - cx), ddy = (float)(fy - cy), ddz = (float)(fz - cz);
         rr = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
@@ -275,7 +276,7 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
 
 __device__ __forceinline__ void tma_bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
     asm volatile(
-        "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
             smem_u32(dst)),
         "l"(src), "r"(bytes), "r"(smem_u32(bar))
         : "memory");
@@ -324,7 +325,7 @@ struct PairArgs {
     float pik;          // pi * (pi_F * fs / lam): sinc arguments in radians
     float ealpha;       // -2 alpha2 log2(e)
     float eks;          // -2 ks^2 log2(e)
-    double nidx, inv_dr, inv_lam;
+    double nidx, inv_dr, inv_lam;   // inv_lam: turns per metre, pi_F / (pi lam)
     int lossless;
 };
 
@@ -739,12 +740,8 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
     std::vector<int> ub = host_target_bounds32(sc, tr, ns, tg);
     PlanV<float> p2 = plan_view32(sc->plan2), pN = plan_view32(sc->planN);
     const DevParams& dp = sc->dp;
-    static int smem_set = 0;
     const size_t pair_smem = 2 * RP_CHUNK * sizeof(FacetRec) + (size_t)RP_WIN * RP_PAIR_THREADS * sizeof(float2);
-    if (!smem_set) {
-        RP_CUDA(cudaFuncSetAttribute(k_pairs32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem));
-        smem_set = 1;
-    }
+    RP_CUDA(cudaFuncSetAttribute(k_pairs32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem));
     int occ = 0;
     RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pairs32, RP_PAIR_THREADS, pair_smem));
     occ = std::max(occ, 1);
@@ -849,11 +846,11 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
             P.err = reinterpret_cast<unsigned int*>(misc + 2);
             P.nr_f = (float)nr; P.nr = nr;
             P.kb = (float)(dp.nidx / dp.dr);
-            P.kt = (float)(dp.nidx / dp.lam);
+            P.kt = (float)(dp.nidx * dp.turn);
             P.pik = (float)(RP_PI * (RP_PI_F * dp.fs / dp.lam));
             P.ealpha = (float)(-2.0 * dp.alpha2 * 1.4426950408889634);
             P.eks = (float)(-2.0 * dp.ks * dp.ks * 1.4426950408889634);
-            P.nidx = dp.nidx; P.inv_dr = 1.0 / dp.dr; P.inv_lam = 1.0 / dp.lam;
+            P.nidx = dp.nidx; P.inv_dr = 1.0 / dp.dr; P.inv_lam = dp.turn;
             P.lossless = dp.lossless;
             int grid = std::min(occ * sc->sm_count, nb * P.tblocks * RP_PARTS);
             k_pairs32<<<grid, RP_PAIR_THREADS, pair_smem, st>>>(P);

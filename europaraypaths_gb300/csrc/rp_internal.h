@@ -33,6 +33,8 @@ int rp_cuda_fail(cudaError_t e, const char* what);
 struct DevParams {
     double lam, fs, P, nidx, eps1, eps2, nu1, nu2, alpha1, alpha2, ks, c1_over_c2;
     double dr, smpl, B, rng_res, ap_rad, ap_cos;
+    double turn;   // phase turns per metre of range: pi_F / (pi lam), so that
+                   // exp(-j (2 pi_F / lam) r) = exp(-j 2 pi r turn) (radar_kernels.cu:682)
     int nr, lossless, disable_surface, rerad_funct;
 };
 

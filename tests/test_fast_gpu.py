@@ -1,0 +1,75 @@
+"""Fused FP32 split-precision form vs the FP64 CPU oracle (through the C ABI).
+
+Tolerances (the accuracy bar of the fast form): relative L2 <= 1e-3 of the
+complex radargram, max phase error <= 0.01 rad at bins above -40 dB of the
+peak, and an exact match of every trace's peak range bin.
+"""
+import numpy as np
+import pytest
+
+from helpers import peak_bins, phase_err_max, rel_l2, tiny_scene
+
+pytestmark = pytest.mark.gpu
+
+REL_L2 = 1e-3
+PHASE = 0.01
+
+
+def fast_vs_oracle(sc, oracle, traces=None, prisms=None):
+    from europaraypaths_gb300 import simulator, traces as tr_mod
+    scene = simulator.Scene(sc["params"], sc["facets"], sc["targets"], prisms=prisms)
+    tr = tr_mod.linear_track(scene.params) if traces is None else traces
+    got, cnt = scene.simulate(tr, form="fast", return_counts=True)
+    ref, rcnt = oracle.simulate(scene.params, sc["facets"], sc["targets"], tr, prisms_soa=prisms)
+    scene.close()
+    return got, ref, cnt, rcnt
+
+
+def check(got, ref):
+    assert rel_l2(got, ref) <= REL_L2, rel_l2(got, ref)
+    assert phase_err_max(got, ref) <= PHASE, phase_err_max(got, ref)
+    assert np.array_equal(peak_bins(got), peak_bins(ref))
+
+
+def test_fast_matches_oracle_tiny(built_lib, oracle):
+    sc = tiny_scene()
+    got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle)
+    assert np.array_equal(cnt, rcnt)
+    check(got, ref)
+
+
+def test_fast_small_plain_scene_subset(built_lib, oracle):
+    # the full small plain-form scene (40k facets, 1600 targets), 3 traces
+    from europaraypaths_gb300 import scenes, traces as tr_mod, param_gen
+    sc = scenes.small_plain()
+    p = param_gen.to_rp_params(sc["params"])
+    tr = tr_mod.linear_track(p)[[0, 50, 99]]
+    got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle, traces=tr)
+    assert np.array_equal(cnt, rcnt)
+    check(got, ref)
+
+
+def test_fast_non_pow2_bins_and_lossless(built_lib, oracle):
+    from europaraypaths_gb300 import scenes
+    sc = tiny_scene(rx_window_m=scenes.rx_window_for_bins(250, 4e6), rx_window_offset_m=24000.0,
+                    lossless=True)
+    got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle)
+    assert got.shape[1] == 250
+    check(got, ref)
+
+
+def test_fast_prisms(built_lib, oracle):
+    sc = tiny_scene()
+    prisms = np.array([[2e-3], [-500.0], [-500.0], [-1200.0], [300.0], [400.0], [-100.0]])
+    got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle, prisms=prisms)
+    check(got, ref)
+
+
+def test_fast_deterministic(built_lib):
+    from europaraypaths_gb300 import simulator
+    sc = tiny_scene(nside=60, ntside=8, ns=4)
+    scene = simulator.Scene(sc["params"], sc["facets"], sc["targets"])
+    a = scene.simulate(form="fast")
+    b = scene.simulate(form="fast")
+    scene.close()
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
