@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Throughput benchmark: facet-trace pairs/s of the raypath engine.
+
+Workload (``large_scene``): 2000x2000 facets at 5 m (4M, seeded fractal
+surface, Hurst 0.8, RMS 5 m), a rough interface 1.5 km deep sampled as
+200x200 targets at 50 m, 2000 traces at 50 km altitude with 5 m spacing,
+9 MHz / 1 MHz chirp sampled at 4 MHz into 4096 range bins, aperture 3 deg.
+All inputs are seeded synthetic data (no public dataset is involved).
+
+A step is one call over a batch of consecutive flyby traces (default 8); the
+K timed steps walk along the track.  ``value`` is pairs/s with the scene and
+trace tables already resident on the device (pairs = sum over traces of
+N_ill * (1 + 2 N_t), counted exactly by the kernels); ``e2e`` is the same
+metric through the public C ABI call ``rp_simulate`` with pinned host trace
+tables in and the host radargram out, copies inside the timed region.
+
+``--impl reference`` times the CPU implementation of the path (the FP64
+oracle, a restatement of the reference's trace loop) on the host cores, each
+step a bounded sample (one trace, a capped number of in-aperture targets).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "facet-trace pairs/s at <=1e-3 rel L2 vs FP64 oracle"
+UNIT = "pairs/s"
+WORKLOAD = ("large_scene: 2000x2000 facets at 5 m (4M), fractal H=0.8 RMS 5 m; rough interface "
+            "1.5 km deep as 200x200 targets at 50 m (eps 3.15); 2000 traces at 50 km, 5 m spacing; "
+            "9 MHz/1 MHz, 4 MHz sampling, 4096 bins; aperture 3 deg; seeded synthetic")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def shard_steps(total_traces, traces_per_step, steps, warmup, rank, world):
+    """Weak scaling: each rank walks its own stretch of the track.
+
+    Returns the list of (start, count) trace batches for warm-up + timed steps
+    of this rank; batches wrap around the track."""
+    out = []
+    per_rank = steps + warmup
+    for k in range(per_rank):
+        start = ((rank * per_rank + k) * traces_per_step) % max(total_traces - traces_per_step + 1, 1)
+        out.append((start, traces_per_step))
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def build_scene(device):
+    from europaraypaths_gb300 import scenes, simulator, traces
+    sc = scenes.large_scene()
+    scene = simulator.Scene(sc["params"], sc["facets"], sc["targets"], device=device)
+    track = traces.linear_track(scene.params)
+    return sc, scene, track
+
+
+def cpu_baseline(sc, scene, track, max_targets, trace_index):
+    """FP64 oracle on one trace of the workload with a capped target count."""
+    from oracle import loader
+    loader.lib()
+    nthreads = os.cpu_count() or 1
+    tr = track[trace_index:trace_index + 1]
+    t0 = time.perf_counter()
+    _, counts = loader.simulate(scene.params, sc["facets"], sc["targets"], tr,
+                                nthreads=nthreads, max_targets=max_targets)
+    dt = time.perf_counter() - t0
+    from europaraypaths_gb300 import opcount
+    p = opcount.pairs(counts)
+    return {"value": p / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"1 trace (index {trace_index}) of the workload, first {max_targets} in-aperture "
+                      f"targets: {p} pairs in {dt:.2f} s (FP64 C++ oracle, OpenMP over targets)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from europaraypaths_gb300 import scenes, param_gen, traces, opcount
+    from oracle import loader
+    loader.lib()
+    sc = scenes.large_scene()
+    p = param_gen.to_rp_params(sc["params"], derive=False)
+    loader.derive(p)
+    track = traces.linear_track(p)
+    nthreads = os.cpu_count() or 1
+    times, pairs = [], []
+    for k in range(args.warmup + args.steps):
+        tr = track[(k * 97) % p.ns:(k * 97) % p.ns + 1]
+        t0 = time.perf_counter()
+        _, counts = loader.simulate(p, sc["facets"], sc["targets"], tr, nthreads=nthreads,
+                                    max_targets=args.ref_targets)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+            pairs.append(opcount.pairs(counts))
+    total = float(sum(times))
+    value = sum(pairs) / total
+    sample = (f"each step: 1 trace of the workload, first {args.ref_targets} in-aperture targets "
+              f"(FP64 C++ oracle restating the reference trace loop, {nthreads} threads)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--traces-per-step", type=int, default=8)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--plain-traces", type=int, default=1, help="traces for the plain FP64 form (0 = skip)")
+    ap.add_argument("--cpu-targets", type=int, default=48, help="target cap of the CPU baseline sample")
+    ap.add_argument("--ref-targets", type=int, default=24, help="target cap per --impl reference step")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from europaraypaths_gb300 import simulator, opcount
+    sc, scene, track = build_scene(local)
+    nr = scene.nr
+    tps = args.traces_per_step
+    batches = shard_steps(track.shape[0], tps, args.steps, args.warmup, rank, world)
+    d_tracks = [torch.from_numpy(np.ascontiguousarray(track[s:s + n])).cuda() for s, n in batches]
+    d_out = torch.empty((tps, nr), dtype=torch.complex64, device="cuda")
+    stream = torch.cuda.Stream()
+    counts = [np.zeros((tps, 2), np.int64) for _ in batches]
+
+    simulator.set_timing(True)
+    # warm-up
+    for k in range(args.warmup):
+        scene.simulate_device(d_tracks[k], d_out, form="fast", stream=stream, counts=counts[k])
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    stage = {"setup_ms": 0.0, "pairs_ms": 0.0, "compress_ms": 0.0, "tail_ms": 0.0, "pair_launches": 0}
+    launches = 0
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for k in range(args.warmup, args.warmup + args.steps):
+        scene.simulate_device(d_tracks[k], d_out, form="fast", stream=stream, counts=counts[k])
+        t = simulator.last_timing()
+        for key in stage:
+            stage[key] += t[key]
+        launches += simulator.last_launch_count()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clocks = sampler.stop()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    timed_counts = np.concatenate(counts[args.warmup:])
+    my_pairs = opcount.pairs(timed_counts)
+    my_evals = opcount.target_evals(timed_counts)
+    if dist is not None:
+        t = torch.tensor([elapsed_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+        pt = torch.tensor([float(my_pairs)], dtype=torch.float64, device="cuda")
+        dist.all_reduce(pt, op=dist.ReduceOp.SUM)
+        total_pairs = float(pt.item())
+    else:
+        total_pairs = float(my_pairs)
+    value = total_pairs / (elapsed_ms / 1e3)
+
+    # ---- end to end through rp_simulate (pinned host buffers) ----
+    h_tr = torch.empty((tps, 9), dtype=torch.float64).pin_memory()
+    h_out = torch.empty((tps, nr), dtype=torch.complex64).pin_memory()
+    e2e_pairs = 0
+    t0 = time.perf_counter()
+    for k in range(args.e2e_steps):
+        s, n = batches[(args.warmup + k) % len(batches)]
+        h_tr.copy_(torch.from_numpy(track[s:s + n]))
+        c = np.zeros((tps, 2), np.int64)
+        scene.simulate_host_ptrs(h_tr.data_ptr(), n, h_out.data_ptr(), form="fast", stream=stream, counts=c)
+        e2e_pairs += opcount.pairs(c)
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+        pt = torch.tensor([float(e2e_pairs)], dtype=torch.float64, device="cuda")
+        dist.all_reduce(pt, op=dist.ReduceOp.SUM)
+        e2e_pairs = float(pt.item())
+    e2e = {"value": e2e_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(9 * 8 * tps),
+           "d2h_bytes_per_step": int(8 * nr * tps), "steps": args.e2e_steps,
+           "call": "rp_simulate (C ABI), pinned host trace table in, host complex64 radargram out"}
+
+    line = None
+    if rank == 0:
+        peaks = measured_peaks()
+        sm_mhz = clocks.get("sm_mhz") or peaks.get("clocks_under_load", {}).get("sm_mhz_median") or 1455.0
+        n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+        pairs_s = stage["pairs_ms"] / 1e3
+        mufu_rate = opcount.MUFU_PER_EVAL * my_evals / pairs_s if pairs_s > 0 else 0.0
+        mufu_peak = opcount.MUFU_PER_CLK_PER_SM * n_sm * sm_mhz * 1e6
+        roof = {"bound": "sfu", "kernel": "k_pairs32",
+                "achieved": mufu_rate / 1e12, "peak": mufu_peak / 1e12, "unit": "Tmufu/s",
+                "frac": mufu_rate / mufu_peak if mufu_peak else None,
+                "traffic": None,
+                "peak_source": (f"nominal {opcount.MUFU_PER_CLK_PER_SM} MUFU results/clk/SM x {n_sm} SMs x "
+                                f"{sm_mhz:.0f} MHz median SM clock under load (not in MEASURED_PEAKS.json, "
+                                "which holds HBM and bf16 only)"),
+                "ops_per_eval": opcount.MUFU_PER_EVAL,
+                "pair_kernel_ms_per_launch": stage["pairs_ms"] / max(stage["pair_launches"], 1),
+                "pair_evals_per_s": my_evals / pairs_s if pairs_s > 0 else None,
+                "stage_ms": {k: stage[k] for k in ("setup_ms", "pairs_ms", "compress_ms", "tail_ms")},
+                "hbm_peak_gbs": peaks.get("hbm_gbs")}
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "traces_per_step": tps, "form": "fast (FP32 split precision)",
+                           "l2": "inputs larger than L2: 384 MB resident facet store, ~55 MB of facet "
+                                 "records per trace per step",
+                           "parallelism": f"replicas over trace ranges x{world}"},
+                "e2e": e2e, "roofline": roof, "clocks": clocks, "gpu_launches": launches}
+        if args.plain_traces > 0 and world == 1:
+            ptr = torch.from_numpy(np.ascontiguousarray(track[1000:1000 + args.plain_traces])).cuda()
+            pout = torch.empty((args.plain_traces, nr), dtype=torch.complex64, device="cuda")
+            pc = np.zeros((args.plain_traces, 2), np.int64)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            scene.simulate_device(ptr, pout, form="plain", stream=stream, counts=pc)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            pv = opcount.pairs(pc) / (e0.elapsed_time(e1) / 1e3)
+            line["plain_form"] = {"value": pv, "unit": UNIT, "traces": args.plain_traces,
+                                  "fast_over_plain": value / pv if pv else None}
+        if not args.no_cpu_baseline and world == 1:
+            line["cpu_baseline"] = cpu_baseline(sc, scene, track, args.cpu_targets, 1000)
+        print(json.dumps(line), flush=True)
+    scene.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

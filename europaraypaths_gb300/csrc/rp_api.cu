@@ -16,6 +16,24 @@
 // ---------------------------------------------------------------- errors --
 static thread_local char g_err[1024] = "";
 thread_local int64_t g_launches = 0;
+thread_local StageTimer g_timer;
+
+void StageTimer::mark(int i, cudaStream_t st) {
+    if (!enabled) return;
+    if (!have_events) {
+        for (int k = 0; k <= RP_NSTAGE; ++k) cudaEventCreate(&ev[k]);
+        have_events = 1;
+    }
+    cudaEventRecord(ev[i], st);
+}
+
+void StageTimer::collect(int first, int last) {
+    if (!enabled || !have_events) return;
+    for (int k = first; k < last; ++k) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, ev[k], ev[k + 1]) == cudaSuccess) ms[k] += t;
+    }
+}
 
 void rp_set_error(const char* fmt, ...) {
     va_list ap;
@@ -57,6 +75,18 @@ extern "C" const char* rp_version(void) { return "raypath-gb300 1.0 (sm_103a)"; 
 extern "C" int rp_last_error(char* buf, size_t len) {
     if (!buf || len == 0) return RP_ERR_ARG;
     snprintf(buf, len, "%s", g_err);
+    return RP_OK;
+}
+
+extern "C" int rp_set_timing(int enable) {
+    g_timer.enabled = enable ? 1 : 0;
+    return RP_OK;
+}
+
+extern "C" int rp_last_timing(double* ms, int n) {
+    if (!ms || n < 0) return RP_ERR_ARG;
+    for (int i = 0; i < n && i < RP_NSTAGE; ++i) ms[i] = g_timer.ms[i];
+    if (n > RP_NSTAGE) ms[RP_NSTAGE] = (double)g_timer.pair_launches;
     return RP_OK;
 }
 
@@ -401,6 +431,7 @@ extern "C" int rp_simulate_device(rp_scene* s, const double* d_traces, int64_t n
         return RP_ERR_ARG;
     }
     g_launches = 0;
+    g_timer.reset();
     RP_CUDA(cudaSetDevice(s->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : s->own_stream;
     if (ns == 0) return RP_OK;
@@ -414,6 +445,7 @@ extern "C" int rp_simulate(rp_scene* s, const double* traces, int64_t ns, int fo
         return RP_ERR_ARG;
     }
     g_launches = 0;
+    g_timer.reset();
     RP_CUDA(cudaSetDevice(s->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : s->own_stream;
     if (ns == 0) return RP_OK;

@@ -794,6 +794,7 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
         C32* sscr = a.take<C32>((size_t)nb * Lw.surf_slot);
         const double* trb = d_traces + 9 * s0;
 
+        g_timer.mark(0, st);
         RP_CUDA(cudaMemsetAsync(vmax, 0, sizeof(unsigned long long) * nb, st));
         RP_CUDA(cudaMemsetAsync(dmin, 0xff, sizeof(unsigned long long) * nb, st));
         RP_CUDA(cudaMemsetAsync(acc, 0, sizeof(long long) * nb * nr * 2, st));
@@ -828,14 +829,17 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
         }
         int h_maxw = 0;
         RP_CUDA(cudaMemcpyAsync(&h_maxw, misc, sizeof(int), cudaMemcpyDeviceToHost, st));
+        g_timer.mark(1, st);
         RP_CUDA(cudaStreamSynchronize(st));
+        g_timer.collect(0, 1);
         const int Wt = std::max(1, std::min(nr, (h_maxw + 3) & ~3));
         FastLayout L = fast_layout(sc, nb, tmax, Wt);
         C32* T = a.take<C32>((size_t)RP_PARTS * nb * L.tstride * Wt);
         C32* Z = a.take<C32>((size_t)nb * L.tstride * nr);
         C32* cscr = a.take<C32>((size_t)L.slots * L.slot);
+        RP_CUDA(cudaMemsetAsync(T, 0, sizeof(C32) * RP_PARTS * nb * L.tstride * Wt, st));
+        g_timer.mark(1, st);
         if (nt > 0 && nf > 0 && tmax > 0) {
-            RP_CUDA(cudaMemsetAsync(T, 0, sizeof(C32) * RP_PARTS * nb * L.tstride * Wt, st));
             PairArgs P;
             P.rec = rec; P.meta = meta; P.rstride = Lw.rstride; P.mstride = Lw.mstride;
             P.nill = d_nill; P.ntl = d_ntl; P.tlist = tlist; P.tstride = L.tstride;
@@ -855,17 +859,22 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
             int grid = std::min(occ * sc->sm_count, nb * P.tblocks * RP_PARTS);
             k_pairs32<<<grid, RP_PAIR_THREADS, pair_smem, st>>>(P);
             RP_LAUNCHED();
+            ++g_timer.pair_launches;
+            g_timer.mark(2, st);
             const float sig_scale = (float)(-1.0 / std::sqrt(dp.P));
             k_conv32<<<L.slots, 256, 0, st>>>(d_ntl, L.tstride, nb, bt0, T, Wt, Z, (const C32*)sc->d_C2_32,
                                              p2, pN, sc->crop_K, sc->crop_all, nr, sig_scale, cscr, L.slot);
             RP_LAUNCHED();
         }
+        if (!(nt > 0 && nf > 0 && tmax > 0)) g_timer.mark(2, st);
+        g_timer.mark(3, st);
         k_surf_conv32<<<nb, 256, 0, st>>>(acc, d_nill, vmax, dp.disable_surface, nr, (const C32*)sc->d_C1_32, p2,
                                          refl, sscr, Lw.surf_slot);
         RP_LAUNCHED();
         k_sum32<<<dim3((nr + 255) / 256, nb), 256, 0, st>>>(d_nill, d_ntl, L.tstride, refl, Z, nr, d_out, out64,
                                                            (int)s0);
         RP_LAUNCHED();
+        g_timer.mark(4, st);
         RP_CUDA(cudaGetLastError());
         unsigned int herr[2] = {0, 0};
         std::vector<int> a1(nb), a2(nb);
@@ -873,6 +882,7 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
         RP_CUDA(cudaMemcpyAsync(a1.data(), d_nill, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
         RP_CUDA(cudaMemcpyAsync(a2.data(), d_ntl, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
         RP_CUDA(cudaStreamSynchronize(st));
+        g_timer.collect(1, 4);
         if (herr[1]) { rp_set_error("fast form: a shared-memory stage wait timed out"); return RP_ERR_TIMEOUT; }
         if (herr[0]) { rp_set_error("fast form: a pair fell outside its target's bin window"); return RP_ERR_INTERNAL; }
         if (h_counts)

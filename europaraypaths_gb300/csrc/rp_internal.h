@@ -111,6 +111,25 @@ struct rp_scene {
 extern thread_local int64_t g_launches;
 #define RP_LAUNCHED() (++g_launches)
 
+// Per-thread stage timing with CUDA events on the launching stream
+// (rp_set_timing / rp_last_timing).  Stages: 0 cull + per-facet setup,
+// 1 pair kernel, 2 per-target range compression, 3 surface + final sum.
+#define RP_NSTAGE 4
+struct StageTimer {
+    int enabled = 0;
+    double ms[RP_NSTAGE] = {0, 0, 0, 0};
+    int64_t pair_launches = 0;
+    cudaEvent_t ev[RP_NSTAGE + 1] = {};
+    int have_events = 0;
+    void reset() {
+        for (int i = 0; i < RP_NSTAGE; ++i) ms[i] = 0;
+        pair_launches = 0;
+    }
+    void mark(int i, cudaStream_t st);          // record boundary event i
+    void collect(int first, int last);          // add elapsed of stages first..last-1 (after sync)
+};
+extern thread_local StageTimer g_timer;
+
 // Entry points of the two forms (rp_plain.cu, rp_fast.cu).
 int rp_plain_run(rp_scene* s, const double* d_traces, int64_t ns, void* d_out, int out64,
                  int64_t* h_counts, cudaStream_t st);

@@ -396,6 +396,7 @@ int rp_plain_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, 
         C64* sscr = a.take<C64>((size_t)nb * L.surf_slot);
         const double* trb = d_traces + 9 * s0;
 
+        g_timer.mark(0, st);
         RP_CUDA(cudaMemsetAsync(vmax, 0, sizeof(unsigned long long) * nb, st));
         RP_CUDA(cudaMemsetAsync(dmin, 0xff, sizeof(unsigned long long) * nb, st));
         RP_CUDA(cudaMemsetAsync(acc, 0, sizeof(long long) * nb * nr * 2, st));
@@ -427,23 +428,33 @@ int rp_plain_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, 
                 nfa, d_nill, sxv, sv, vmax, nr, acc);
             RP_LAUNCHED();
         }
+        g_timer.mark(1, st);
         if (nt > 0 && nf > 0 && tmax > 0) {
             k_pairs64<<<dim3((unsigned)((L.tstride + 63) / 64), nb), 64, 0, st>>>(
                 sc->d_facets, nfa, idx, d_nill, sc->d_targets, nt, tlist, d_ntl, L.tstride,
                 sc->d_prisms, np, trb, sc->dp, Itd, Gi, frc, PT, PS);
             RP_LAUNCHED();
+            ++g_timer.pair_launches;
+            g_timer.mark(2, st);
             k_conv64<<<L.slots, 256, 0, st>>>(d_ntl, L.tstride, nb, sc->d_targets, nt, tlist, PT, PS,
                                              (const C64*)sc->d_C2_64, p2, pN, sc->crop_K,
                                              sc->crop_all, nr, cscr, L.slot);
             RP_LAUNCHED();
         }
+        if (!(nt > 0 && nf > 0 && tmax > 0)) g_timer.mark(2, st);
+        g_timer.mark(3, st);
         k_surf_conv64<<<nb, 256, 0, st>>>(acc, d_nill, vmax, sc->dp.disable_surface, nr,
                                          (const C64*)sc->d_C1_64, p2, refl, sscr, L.surf_slot);
         RP_LAUNCHED();
         k_sum64<<<dim3((nr + 255) / 256, nb), 256, 0, st>>>(d_nill, d_ntl, L.tstride, refl, PT, nr,
                                                            d_out, out64, (int)s0);
         RP_LAUNCHED();
+        g_timer.mark(4, st);
         RP_CUDA(cudaGetLastError());
+        if (g_timer.enabled) {
+            RP_CUDA(cudaStreamSynchronize(st));
+            g_timer.collect(0, 4);
+        }
         if (h_counts) {
             std::vector<int> a1(nb), a2(nb);
             RP_CUDA(cudaMemcpyAsync(a1.data(), d_nill, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));

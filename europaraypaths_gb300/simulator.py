@@ -108,15 +108,41 @@ class Scene:
         _abi.check("rp_simulate", rc)
         return (out, counts) if return_counts else out
 
-    def simulate_device(self, d_traces, d_out, form="fast", stream=None, complex128=False):
+    def simulate_device(self, d_traces, d_out, form="fast", stream=None, complex128=False,
+                        counts=None):
         """Resident-input path: d_traces (ns, 9) float64 and d_out (ns, nr)
-        complex64 torch CUDA tensors; runs on ``stream`` (a torch stream)."""
+        complex64 torch CUDA tensors; runs on ``stream`` (a torch stream).
+        ``counts``: optional int64 numpy array (ns, 2) filled with N_ill, N_t."""
         ns = int(d_traces.shape[0])
         f = FORMS[form] | (OUT_COMPLEX128 if complex128 else 0)
         sp = None if stream is None else ctypes.c_void_p(stream.cuda_stream)
+        cp = None if counts is None else counts.ctypes.data
         rc = _abi.lib().rp_simulate_device(self._h, ctypes.c_void_p(d_traces.data_ptr()), ns, f,
-                                           ctypes.c_void_p(d_out.data_ptr()), None, sp)
+                                           ctypes.c_void_p(d_out.data_ptr()), cp, sp)
         _abi.check("rp_simulate_device", rc)
+
+    def simulate_host_ptrs(self, traces_ptr, ns, out_ptr, form="fast", stream=None, counts=None):
+        """rp_simulate on raw host pointers (e.g. pinned torch tensors)."""
+        f = FORMS[form]
+        sp = None if stream is None else ctypes.c_void_p(stream.cuda_stream)
+        cp = None if counts is None else counts.ctypes.data
+        rc = _abi.lib().rp_simulate(self._h, ctypes.c_void_p(traces_ptr), int(ns), f,
+                                    ctypes.c_void_p(out_ptr), 0, cp, sp)
+        _abi.check("rp_simulate", rc)
+
+
+def set_timing(enable=True):
+    """Per-stage CUDA-event timing of this thread's calls (rp_set_timing)."""
+    _abi.lib().rp_set_timing(1 if enable else 0)
+
+
+def last_timing():
+    """Stage times (ms) of this thread's last call: setup, pairs, compression,
+    surface+sum, and the pair-kernel launch count."""
+    buf = (ctypes.c_double * 5)()
+    _abi.lib().rp_last_timing(buf, 5)
+    return {"setup_ms": buf[0], "pairs_ms": buf[1], "compress_ms": buf[2], "tail_ms": buf[3],
+            "pair_launches": int(buf[4])}
 
 
 def last_launch_count():

@@ -156,6 +156,17 @@ int rp_simulate_device(rp_scene* s, const double* d_traces, int64_t ns, int form
 /* Number of kernel launches issued by this thread's last rp_simulate*. */
 int rp_last_launch_count(int64_t* launches);
 
+/* Enable (1) / disable (0) per-stage CUDA-event timing of this thread's
+ * rp_simulate* calls (events recorded on the launching stream).  Replaces
+ * the gettimeofday phase timers of src/CUDA/sim.cu:43-58. */
+int rp_set_timing(int enable);
+
+/* Stage times in ms of this thread's last rp_simulate* call:
+ *   ms[0] cull + per-facet setup, ms[1] pair kernel, ms[2] per-target range
+ *   compression, ms[3] surface compression + final sum; ms[4] (if n > 4) the
+ *   number of pair-kernel launches. */
+int rp_last_timing(double* ms, int n);
+
 #ifdef __cplusplus
 }
 #endif
