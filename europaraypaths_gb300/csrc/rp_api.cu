@@ -7,11 +7,13 @@
 #include <complex>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <vector>
 
 #include "rp_internal.h"
+#include "rp_fft.cuh"
 
 // ---------------------------------------------------------------- errors --
 static thread_local char g_err[1024] = "";
@@ -294,6 +296,45 @@ static int build_tables(rp_scene* s) {
         if (!(std::fabs((double)m * p.rx_sample_rate / N) > p.bandwidth)) K = m;
     s->crop_K = K;
     s->crop_all = (K >= N / 2);
+    // shared-memory path tables: nr a power of two, M = 4 nr
+    if (is_pow2(nr) && nr >= 4) {
+        const int n2 = 2 * nr, M = 4 * nr;
+        int lM = 0;
+        while ((1 << lM) < M) ++lM;
+        std::vector<Cplx<double>> tw(M);
+        for (int k = 0; k < M; ++k) {
+            double ang = -2.0 * RP_PI * k / M;
+            tw[k] = Cplx<double>{std::cos(ang), std::sin(ang)};
+        }
+        struct TWH {
+            const std::vector<Cplx<double>>* t;
+            Cplx<double> operator()(int k) const { return (*t)[k]; }
+        } f{&tw};
+        auto to32 = [](const std::vector<Cplx<double>>& v, float** d, size_t* a) {
+            std::vector<float> b(2 * v.size());
+            for (size_t i = 0; i < v.size(); ++i) { b[2 * i] = (float)v[i].x; b[2 * i + 1] = (float)v[i].y; }
+            return upload(d, b.data(), b.size() * sizeof(float), a);
+        };
+        std::vector<Cplx<double>> c2(n2), b(M, Cplx<double>{0, 0}), bi(M, Cplx<double>{0, 0});
+        for (int i = 0; i < n2; ++i) c2[i] = Cplx<double>{host_sinc((double)(i - nr / 2) * p.dr / (2 * p.rng_res)), 0.0};
+        host_dif(c2.data(), n2, f, lM);
+        std::vector<cd> w = bluestein_chirp(N);
+        for (int k = 0; k < N; ++k) {
+            Cplx<double> cw{w[k].real(), -w[k].imag()}, ww{w[k].real(), w[k].imag()};
+            b[k] = cw;
+            bi[k] = ww;
+            if (k) { b[M - k] = cw; bi[M - k] = ww; }
+        }
+        host_dif(b.data(), M, f, lM);
+        host_dif(bi.data(), M, f, lM);
+        if ((rc = to32(tw, &s->d_twS, &acc))) return rc;
+        if ((rc = to32(c2, &s->d_C2S, &acc))) return rc;
+        if ((rc = to32(b, &s->d_bWS, &acc))) return rc;
+        if ((rc = to32(bi, &s->d_bWiS, &acc))) return rc;
+        s->mS = M;
+        s->log2mS = lM;
+        s->smem_conv = 1;
+    }
     s->store_bytes += acc;
     return RP_OK;
 }
@@ -377,6 +418,7 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
         if ((rc = upload(&s->d_sorted, sorted.data(), sizeof(double) * 12 * nf, &s->store_bytes))) return fail(rc);
     }
     if ((rc = build_tables(s))) return fail(rc);
+    if (const char* v = getenv("RP_PAIR_VARIANT")) s->pair_variant = atoi(v) == 2 ? 2 : 3;
     cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return fail(rp_cuda_fail(e, "cudaStreamCreate"));
     *out = s;
@@ -388,7 +430,8 @@ extern "C" int rp_scene_destroy(rp_scene* s) {
     cudaSetDevice(s->device);
     if (s->own_stream) cudaStreamSynchronize(s->own_stream);
     void* ptrs[] = {s->d_facets, s->d_targets, s->d_prisms, s->d_order, s->d_sorted,
-                    s->d_C1_64, s->d_C2_64, s->d_C1_32, s->d_C2_32};
+                    s->d_C1_64, s->d_C2_64, s->d_C1_32, s->d_C2_32, s->d_twS, s->d_C2S,
+                    s->d_bWS, s->d_bWiS};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     free_plan(s->plan2);

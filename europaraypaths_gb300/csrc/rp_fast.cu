@@ -27,12 +27,16 @@
 
 #include "rp_common.cuh"
 #include "rp_conv.cuh"
+#include "rp_fft.cuh"
 
 #define RP_CHUNK 256          // facets per chunk (one record tile)
 #define RP_PAIR_THREADS 256   // targets per pair-kernel block
 #define RP_WIN 16             // bins in a thread's per-chunk window
 #define RP_PARTS 4            // facet-range splits per (trace, target block)
 #define RP_SPIN_LIMIT (1 << 22)
+#define RP_CONV_SPLIT 64       // targets per range-compression work item (fixed:
+                               // a trace's sum order never depends on the batch)
+#define RP_CONV_THREADS 512
 
 namespace {
 
@@ -329,12 +333,141 @@ struct PairArgs {
     int lossless;
 };
 
-__device__ __forceinline__ float sinc_rad(float a) {
-    // sin(a)/a with a = pi x; 1 when |x| < 1e-6 (elementary_kernels.cu:50-53)
-    return (fabsf(a) < 3.14159265e-6f) ? 1.0f : __sinf(a) / a;
+// Per-(chunk, target) anchors of the split-precision evaluation.
+struct Anchor {
+    float Dx, Dy, Dz;     // target - chunk centre (FP32 of an FP64 difference)
+    float T0, T0sq;       // |target - chunk centre| (FP64 -> FP32)
+    float tau0;           // frac(n T0 turn): phase of the anchor in turns
+    float xbase;          // n T0 / dr - blo (bins, relative to the window start)
+    float tnx, tny, tnz;  // target normal
+};
+
+// One (facet, target) evaluation of the target leg (compTargetRays,
+// compRefrEnergyIn, accumulateTarget; geometry_kernels.cu:272-350, 520-554,
+// radar_kernels.cu:767-830).  Returns the phasor and x - blo, the bin
+// coordinate relative to the window start.  sinc(x) = sin(pi x)/(pi x) is
+// evaluated as sin(a)/a with a = pi x; the four quotients share one
+// reciprocal, and |x| < 1e-6 counts as sinc = 1 (elementary_kernels.cu:50-53).
+__device__ __forceinline__ void pair_eval(const FacetRec& r, const Anchor& an, const PairArgs& A,
+                                          float& xr, float& vre, float& vim) {
+    const float dd = fmaf(an.Dx, r.a.x, fmaf(an.Dy, r.a.y, an.Dz * r.a.z));
+    const float qd = fmaf(-2.f, dd, r.a.w);             // Ttd^2 - T0^2
+    const float d2 = an.T0sq + qd;
+    const float rinv = rsqrtf(d2);
+    const float Ttd = d2 * rinv;
+    const float dT = __fdividef(qd, Ttd + an.T0);       // Ttd - T0 without cancellation
+    const float jx = (an.Dx - r.a.x) * rinv;
+    const float jy = (an.Dy - r.a.y) * rinv;
+    const float jz = (an.Dz - r.a.z) * rinv;
+    const float cT = fminf(1.f, fmaxf(-1.f, -fmaf(jx, r.b.x, fmaf(jy, r.b.y, jz * r.b.z))));
+    const float cD = fminf(1.f, fmaxf(-1.f, -fmaf(jx, an.tnx, fmaf(jy, an.tny, jz * an.tnz))));
+    const float yu = fmaf(jx, r.c.x, fmaf(jy, r.c.y, jz * r.c.z));
+    const float xv = fmaf(jx, r.d.x, fmaf(jy, r.d.y, jz * r.d.z));
+    const float h2 = fmaf(xv, xv, yu * yu);
+    const float aT = fmaf(-cT, cT, 1.f);
+    const float aD = fmaf(-cD, cD, 1.f);
+    // sin(th) cos(ph) = sqrt(a) xv / sqrt(h2); atan2(0, 0) = 0 gives (sqrt(a), 0)
+    const bool hz = !(h2 > 0.f);
+    const float pT = aT * h2, pD = aD * h2;
+    const float gT = (pT > 0.f) ? aT * rsqrtf(pT) : 0.f;
+    const float gD = (pD > 0.f) ? aD * rsqrtf(pD) : 0.f;
+    const float a1 = A.pik * (hz ? sqrtf(aT) : gT * xv);
+    const float a2 = A.pik * (hz ? 0.f : gT * yu);
+    const float a3 = A.pik * (hz ? sqrtf(aD) : gD * xv);
+    const float a4 = A.pik * (hz ? 0.f : gD * yu);
+    const float eps = 3.14159265e-6f;
+    const bool z1 = fabsf(a1) < eps, z2 = fabsf(a2) < eps, z3 = fabsf(a3) < eps, z4 = fabsf(a4) < eps;
+    const float num = (z1 ? 1.f : __sinf(a1)) * (z2 ? 1.f : __sinf(a2)) * (z3 ? 1.f : __sinf(a3)) *
+                      (z4 ? 1.f : __sinf(a4));
+    const float den = (z1 ? 1.f : a1) * (z2 ? 1.f : a2) * (z3 ? 1.f : a3) * (z4 ? 1.f : a4);
+    const float S = __fdividef(num, den);
+    float e2 = 0.f;
+    if (!A.lossless) {
+        float ea = A.ealpha * Ttd;
+        e2 = fmaf(A.eks, cT * cT, ea);
+    }
+    const float amp = r.d.w * fabsf(S) * rinv * exp2f(e2);
+    float tau = r.c.w + an.tau0 + A.kt * dT;
+    tau -= rintf(tau);
+    float sn, cs;
+    __sincosf(-6.28318530717958647f * tau, &sn, &cs);
+    vre = amp * cs;
+    vim = amp * sn;
+    xr = r.b.w + an.xbase + A.kb * dT;
 }
 
-__global__ void __launch_bounds__(RP_PAIR_THREADS)
+// Attenuation-prism factor for one pair (compTargetRays, geometry_kernels.cu:
+// 317-342): exp2 of the change of the exponent from alpha2 * Ttd to
+// sum(alpha_p d_p) + alpha2 (Ttd - sum d_p).
+__device__ __noinline__ float prism_factor(float4 ra, double cx, double cy, double cz, float Dx,
+                                           float Dy, float Dz, float T0sq, const double* PR,
+                                           int64_t np, float ealpha) {
+    const float dd = fmaf(Dx, ra.x, fmaf(Dy, ra.y, Dz * ra.z));
+    const float d2 = T0sq + fmaf(-2.f, dd, ra.w);
+    const float rinv = rsqrtf(d2);
+    const float Ttd = d2 * rinv;
+    const double fx = cx + ra.x, fy = cy + ra.y, fz = cz + ra.z;
+    const double jx = (Dx - ra.x) * rinv, jy = (Dy - ra.y) * rinv, jz = (Dz - ra.z) * rinv;
+    double tot = 0.0, ex = 0.0;
+    for (int64_t p = 0; p < np; ++p) {
+        double box[6] = {PR[np + p], PR[2 * np + p], PR[3 * np + p],
+                         PR[4 * np + p], PR[5 * np + p], PR[6 * np + p]};
+        double ad = d_prism_dist(fx, fy, fz, jx, jy, jz, box, Ttd);
+        tot += ad;
+        ex += PR[p] * ad;
+    }
+    // ealpha = -2 alpha2 log2(e): replace alpha2 * tot by the prisms' sum
+    return exp2f(-ealpha * (float)tot - 2.f * 1.44269504f * (float)ex);
+}
+
+// Add one phasor into the thread's window (or, outside it, directly into the
+// thread's own trace row).  Truncating bin as the reference's (short) cast.
+__device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo, int b0,
+                                        float2* win, int tid, C32* Trow, const PairArgs& A) {
+    const float xabs = xr + (float)blo;
+    if (!(xabs > -1.f && xabs < A.nr_f)) return;
+    const int b = (int)xabs;
+    const float w = xabs - (float)b;
+    const int sl = b - blo;
+    const bool two = (b + 1) < A.nr;
+    if (sl >= 0 && sl + 1 < RP_WIN) {
+        float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
+        float2 v0 = *p0;
+        v0.x = fmaf(vre, 1.f - w, v0.x);
+        v0.y = fmaf(vim, 1.f - w, v0.y);
+        *p0 = v0;
+        if (two) {
+            float2* p1 = p0 + RP_PAIR_THREADS;
+            float2 v1 = *p1;
+            v1.x = fmaf(vre, w, v1.x);
+            v1.y = fmaf(vim, w, v1.y);
+            *p1 = v1;
+        }
+        return;
+    }
+    const int o0 = b - b0;
+    if (o0 >= 0 && o0 < A.Wt) {
+        C32 t0 = Trow[o0];
+        t0.x = fmaf(vre, 1.f - w, t0.x);
+        t0.y = fmaf(vim, 1.f - w, t0.y);
+        Trow[o0] = t0;
+    } else {
+        atomicOr(A.err, 1u);
+    }
+    if (two) {
+        if (o0 + 1 >= 0 && o0 + 1 < A.Wt) {
+            C32 t1 = Trow[o0 + 1];
+            t1.x = fmaf(vre, w, t1.x);
+            t1.y = fmaf(vim, w, t1.y);
+            Trow[o0 + 1] = t1;
+        } else {
+            atomicOr(A.err, 1u);
+        }
+    }
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(RP_PAIR_THREADS, MINB)
 k_pairs32(PairArgs A) {
     extern __shared__ __align__(128) unsigned char smem[];
     FacetRec* srec = reinterpret_cast<FacetRec*>(smem);                     // [2][RP_CHUNK]
@@ -411,116 +544,44 @@ k_pairs32(PairArgs A) {
                 const double T0 = sqrt(Dx * Dx + Dy * Dy + Dz * Dz);
                 const double xt = A.nidx * T0 * A.inv_dr;
                 const double tt = A.nidx * T0 * A.inv_lam;
-                const float tau0 = (float)(tt - floor(tt));
-                const float Dxf = (float)Dx, Dyf = (float)Dy, Dzf = (float)Dz;
-                const float T0f = (float)T0;
-                const float T0sq = (float)(T0 * T0);
-                const double lo = (double)m.xmin + A.nidx * ((double)T0 - (double)m.R) * A.inv_dr;
+                const double lo = (double)m.xmin + A.nidx * (T0 - (double)m.R) * A.inv_dr;
                 const int blo = (int)floor(lo) - 1;
-                const float xbase = (float)(xt - (double)blo);     // x - blo = xI + xbase + kb dT
+                Anchor an;
+                an.Dx = (float)Dx; an.Dy = (float)Dy; an.Dz = (float)Dz;
+                an.T0 = (float)T0; an.T0sq = (float)(T0 * T0);
+                an.tau0 = (float)(tt - floor(tt));
+                an.xbase = (float)(xt - (double)blo);
+                an.tnx = tnx; an.tny = tny; an.tnz = tnz;
                 for (int w = 0; w < RP_WIN; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
                 const int cnt = m.n;
-                for (int jj = 0; jj < cnt; ++jj) {
-                    const FacetRec r = R[jj];
-                    // d = target - facet = D - delta;  Ttd^2 - T0^2 = -2 D.delta + |delta|^2
-                    const float dd = fmaf(Dxf, r.a.x, fmaf(Dyf, r.a.y, Dzf * r.a.z));
-                    const float qd = fmaf(-2.f, dd, r.a.w);
-                    const float d2 = T0sq + qd;
-                    const float rinv = rsqrtf(d2);
-                    const float Ttd = d2 * rinv;
-                    const float dT = __fdividef(qd, Ttd + T0f);
-                    const float jx = (Dxf - r.a.x) * rinv;
-                    const float jy = (Dyf - r.a.y) * rinv;
-                    const float jz = (Dzf - r.a.z) * rinv;
-                    float cT = -fmaf(jx, r.b.x, fmaf(jy, r.b.y, jz * r.b.z));
-                    float cD = -fmaf(jx, tnx, fmaf(jy, tny, jz * tnz));
-                    cT = fminf(1.f, fmaxf(-1.f, cT));
-                    cD = fminf(1.f, fmaxf(-1.f, cD));
-                    const float yu = fmaf(jx, r.c.x, fmaf(jy, r.c.y, jz * r.c.z));
-                    const float xv = fmaf(jx, r.d.x, fmaf(jy, r.d.y, jz * r.d.z));
-                    const float h2 = fmaf(xv, xv, yu * yu);
-                    const float aT = fmaf(-cT, cT, 1.f);
-                    const float aD = fmaf(-cD, cD, 1.f);
-                    // sin(th)cos(ph) = sqrt(a) xv / sqrt(h2); atan2(0,0) = 0 -> (sqrt(a), 0)
-                    float g1, g2, g3, g4;
-                    if (h2 > 0.f) {
-                        const float gT = (aT > 0.f) ? aT * rsqrtf(aT * h2) : 0.f;
-                        const float gD = (aD > 0.f) ? aD * rsqrtf(aD * h2) : 0.f;
-                        g1 = gT * xv; g2 = gT * yu; g3 = gD * xv; g4 = gD * yu;
-                    } else {
-                        g1 = sqrtf(aT); g2 = 0.f; g3 = sqrtf(aD); g4 = 0.f;
+                const bool prisms = (A.np > 0) && !A.lossless;
+                int jj = 0;
+                for (; jj + 1 < cnt; jj += 2) {
+                    const FacetRec r0 = R[jj];
+                    const FacetRec r1 = R[jj + 1];
+                    float x0, re0, im0, x1, re1, im1;
+                    pair_eval(r0, an, A, x0, re0, im0);
+                    pair_eval(r1, an, A, x1, re1, im1);
+                    if (prisms) {
+                        const float f0 = prism_factor(r0.a, m.cx, m.cy, m.cz, an.Dx, an.Dy, an.Dz, an.T0sq,
+                                                      A.PR, A.np, A.ealpha);
+                        const float f1 = prism_factor(r1.a, m.cx, m.cy, m.cz, an.Dx, an.Dy, an.Dz, an.T0sq,
+                                                      A.PR, A.np, A.ealpha);
+                        re0 *= f0; im0 *= f0; re1 *= f1; im1 *= f1;
                     }
-                    const float S = sinc_rad(A.pik * g1) * sinc_rad(A.pik * g2) *
-                                    sinc_rad(A.pik * g3) * sinc_rad(A.pik * g4);
-                    float e2 = 0.f;
-                    if (!A.lossless) {
-                        float ea = A.ealpha * Ttd;
-                        if (A.np > 0) {
-                            // attenuation prisms (compTargetRays, geometry_kernels.cu:317-342)
-                            const double fx = m.cx + r.a.x, fy = m.cy + r.a.y, fz = m.cz + r.a.z;
-                            double tot = 0.0, ex = 0.0;
-                            for (int64_t p = 0; p < A.np; ++p) {
-                                double box[6] = {A.PR[A.np + p], A.PR[2 * A.np + p], A.PR[3 * A.np + p],
-                                                 A.PR[4 * A.np + p], A.PR[5 * A.np + p], A.PR[6 * A.np + p]};
-                                double ad = d_prism_dist(fx, fy, fz, jx, jy, jz, box, Ttd);
-                                tot += ad;
-                                ex += A.PR[p] * ad;
-                            }
-                            // ealpha = -2 alpha2 log2 e; the prism part replaces alpha2 there
-                            ea = A.ealpha * (Ttd - (float)tot) - 2.f * 1.44269504f * (float)ex;
-                        }
-                        e2 = fmaf(A.eks, cT * cT, ea);
+                    bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
+                    bin_add(x1, re1, im1, blo, b0, win, tid, Trow, A);
+                }
+                if (jj < cnt) {
+                    const FacetRec r0 = R[jj];
+                    float x0, re0, im0;
+                    pair_eval(r0, an, A, x0, re0, im0);
+                    if (prisms) {
+                        const float f0 = prism_factor(r0.a, m.cx, m.cy, m.cz, an.Dx, an.Dy, an.Dz, an.T0sq,
+                                                      A.PR, A.np, A.ealpha);
+                        re0 *= f0; im0 *= f0;
                     }
-                    const float amp = r.d.w * fabsf(S) * rinv * exp2f(e2);
-                    float tau = r.c.w + tau0 + A.kt * dT;
-                    tau -= rintf(tau);
-                    float sn, cs;
-                    __sincosf(-6.28318530717958647f * tau, &sn, &cs);
-                    const float vre = amp * cs, vim = amp * sn;
-                    // bin of rngt: x = (Itd + n Ttd - rst)/dr, relative to blo
-                    const float xr = r.b.w + xbase + A.kb * dT;     // x - blo
-                    const float xabs = xr + (float)blo;
-                    if (xabs > -1.f && xabs < A.nr_f) {
-                        int b = (int)xabs;                            // truncation (short cast)
-                        const float w = xabs - (float)b;
-                        const int sl = b - blo;
-                        const bool two = (b + 1) < A.nr;
-                        if (sl >= 0 && sl + 1 < RP_WIN) {
-                            float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
-                            float2 v0 = *p0;
-                            v0.x = fmaf(vre, 1.f - w, v0.x);
-                            v0.y = fmaf(vim, 1.f - w, v0.y);
-                            *p0 = v0;
-                            if (two) {
-                                float2* p1 = p0 + RP_PAIR_THREADS;
-                                float2 v1 = *p1;
-                                v1.x = fmaf(vre, w, v1.x);
-                                v1.y = fmaf(vim, w, v1.y);
-                                *p1 = v1;
-                            }
-                        } else {
-                            // outside the chunk window: direct update of the owned trace
-                            const int o0 = b - b0;
-                            if (o0 >= 0 && o0 < A.Wt) {
-                                C32 t0 = Trow[o0];
-                                t0.x = fmaf(vre, 1.f - w, t0.x);
-                                t0.y = fmaf(vim, 1.f - w, t0.y);
-                                Trow[o0] = t0;
-                            } else {
-                                atomicOr(A.err, 1u);
-                            }
-                            if (two) {
-                                if (o0 + 1 >= 0 && o0 + 1 < A.Wt) {
-                                    C32 t1 = Trow[o0 + 1];
-                                    t1.x = fmaf(vre, w, t1.x);
-                                    t1.y = fmaf(vim, w, t1.y);
-                                    Trow[o0 + 1] = t1;
-                                } else {
-                                    atomicOr(A.err, 1u);
-                                }
-                            }
-                        }
-                    }
+                    bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
                 }
                 // flush the window into the owned trace
                 for (int w = 0; w < RP_WIN; ++w) {
@@ -587,6 +648,187 @@ __global__ void k_conv32(const int* __restrict__ ntl, int64_t tstride, int nb, c
         conv_complex_block<float>(tr, ptarg, pN, nr, crop_K, crop_all, A, B, wa, wb,
                                   Z + ((size_t)s * tstride + q) * nr, sig_scale);
     }
+}
+
+// Shared-memory range compression (nr a power of two, 6 nr complex values of
+// shared memory).  One work item = RP_CONV_SPLIT consecutive targets of one
+// trace; their contributions are summed in target order in registers and
+// written as one partial trace.  Per target (X: 2nr, W: M = 4nr):
+//   X = DIF(pad T)                         T = sum of the facet-range parts
+//   W = DIT(X * C2)[nr/2 ..] / 2nr         Ptarg (convolvePhasorChirpLinear)
+//   W = DIT(X * DIF(pad Ptarg)) * s / 2nr  u = Psour (*) Ptarg, Psour = s T
+//   X = crop(Bluestein_N(u))               DFT on the N = 2nr - 1 grid, cropSpectrum
+//   out[j] += Bluestein_N^-1(X)[2j] / N    takeEveryOtherComplex
+// (radar_kernels.cu:554-649, elementary_kernels.cu:258-353).
+struct ConvArgs {
+    const int* ntl;
+    int64_t tstride;
+    int nb;
+    const int* bt0;
+    const C32* T;
+    int Wt;
+    const Cplx<float>* tw;
+    int log2M;
+    const Cplx<float>* C2s;
+    const Cplx<float>* bWs;
+    const Cplx<float>* bWis;
+    const Cplx<float>* bw;
+    int nr, n2, N, M, crop_K, crop_all;
+    float sig_scale;
+    C32* part;          // [nb][nsplit][nr]
+    int nsplit;
+    unsigned int* work;
+};
+
+struct TW32 {
+    const Cplx<float>* t;
+    __device__ __forceinline__ Cplx<float> operator()(int k) const {
+        const float2 v = __ldg(reinterpret_cast<const float2*>(t) + k);
+        return Cplx<float>{v.x, v.y};
+    }
+};
+
+template <int KPT>
+__global__ void __launch_bounds__(RP_CONV_THREADS)
+k_conv32s(ConvArgs A) {
+    extern __shared__ __align__(16) unsigned char csm[];
+    Cplx<float>* X = reinterpret_cast<Cplx<float>*>(csm);
+    Cplx<float>* W = X + A.n2;
+    __shared__ unsigned int s_item;
+    const TW32 tw{A.tw};
+    const int tid = threadIdx.x;
+    const int nr = A.nr, n2 = A.n2, N = A.N, M = A.M;
+    const unsigned int items = (unsigned)A.nb * A.nsplit;
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(A.work, 1u);
+        __syncthreads();
+        const unsigned int item = s_item;
+        __syncthreads();
+        if (item >= items) break;
+        const int s = item / A.nsplit;
+        const int sp = item % A.nsplit;
+        const int nq = A.ntl[s];
+        const int q0 = sp * RP_CONV_SPLIT;
+        if (q0 >= nq) continue;
+        const int q1 = min(q0 + RP_CONV_SPLIT, nq);
+        float accr[KPT], acci[KPT];
+#pragma unroll
+        for (int i = 0; i < KPT; ++i) { accr[i] = 0.f; acci[i] = 0.f; }
+        for (int q = q0; q < q1; ++q) {
+            const int b0 = A.bt0[(size_t)s * A.tstride + q];
+            for (int k = tid; k < n2; k += RP_CONV_THREADS) {
+                Cplx<float> v{0.f, 0.f};
+                const int o = k - b0;
+                if (k < nr && o >= 0 && o < A.Wt) {
+                    for (int p = 0; p < RP_PARTS; ++p) {
+                        const C32 u = A.T[(((size_t)p * A.nb + s) * A.tstride + q) * A.Wt + o];
+                        v.x += u.x;
+                        v.y += u.y;
+                    }
+                }
+                X[k] = v;
+            }
+            __syncthreads();
+            block_dif(X, n2, tw, A.log2M);
+            for (int k = tid; k < n2; k += RP_CONV_THREADS) W[k] = c_mul(X[k], A.C2s[k]);
+            __syncthreads();
+            block_dit(W, n2, tw, A.log2M);
+            {   // Ptarg = W[nr/2 + k] / n2 moved to the front, zero padded
+                const float inv = 1.f / (float)n2;
+                Cplx<float> keep[KPT];
+#pragma unroll
+                for (int c = 0; c < KPT; ++c) {
+                    const int k = tid + c * RP_CONV_THREADS;
+                    if (k < nr) keep[c] = W[nr / 2 + k];
+                }
+                __syncthreads();
+#pragma unroll
+                for (int c = 0; c < KPT; ++c) {
+                    const int k = tid + c * RP_CONV_THREADS;
+                    if (k < nr) W[k] = Cplx<float>{keep[c].x * inv, keep[c].y * inv};
+                }
+                for (int k = nr + tid; k < n2; k += RP_CONV_THREADS) W[k] = Cplx<float>{0.f, 0.f};
+                __syncthreads();
+            }
+            block_dif(W, n2, tw, A.log2M);
+            {
+                const float sc = A.sig_scale / (float)n2;
+                for (int k = tid; k < n2; k += RP_CONV_THREADS) {
+                    Cplx<float> v = c_mul(X[k], W[k]);
+                    W[k] = Cplx<float>{v.x * sc, v.y * sc};
+                }
+            }
+            __syncthreads();
+            block_dit(W, n2, tw, A.log2M);                 // u (natural, N values)
+            for (int k = tid; k < M; k += RP_CONV_THREADS)
+                W[k] = (k < N) ? c_mul(W[k], A.bw[k]) : Cplx<float>{0.f, 0.f};
+            __syncthreads();
+            block_dif(W, M, tw, A.log2M);
+            for (int k = tid; k < M; k += RP_CONV_THREADS) W[k] = c_mul(W[k], A.bWs[k]);
+            __syncthreads();
+            block_dit(W, M, tw, A.log2M);
+            {
+                const float invM = 1.f / (float)M;
+                for (int k = tid; k < N; k += RP_CONV_THREADS) {
+                    const int m = k < N - k ? k : N - k;
+                    const bool kept = A.crop_all || m <= A.crop_K;
+                    Cplx<float> v = c_mul(W[k], A.bw[k]);
+                    X[k] = kept ? Cplx<float>{v.x * invM, v.y * invM} : Cplx<float>{0.f, 0.f};
+                }
+            }
+            __syncthreads();
+            for (int k = tid; k < M; k += RP_CONV_THREADS)
+                W[k] = (k < N) ? c_mulc(X[k], A.bw[k]) : Cplx<float>{0.f, 0.f};
+            __syncthreads();
+            block_dif(W, M, tw, A.log2M);
+            for (int k = tid; k < M; k += RP_CONV_THREADS) W[k] = c_mul(W[k], A.bWis[k]);
+            __syncthreads();
+            block_dit(W, M, tw, A.log2M);
+            {
+                const float sc = 1.f / ((float)M * (float)N);
+#pragma unroll
+                for (int i = 0; i < KPT; ++i) {
+                    const int j = tid + i * RP_CONV_THREADS;
+                    if (j < nr) {
+                        Cplx<float> v = c_mulc(W[2 * j], A.bw[2 * j]);
+                        accr[i] = fmaf(v.x, sc, accr[i]);
+                        acci[i] = fmaf(v.y, sc, acci[i]);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        C32* out = A.part + ((size_t)s * A.nsplit + sp) * nr;
+#pragma unroll
+        for (int i = 0; i < KPT; ++i) {
+            const int j = tid + i * RP_CONV_THREADS;
+            if (j < nr) out[j] = C32{accr[i], acci[i]};
+        }
+    }
+}
+
+// sig = refl + sum of the per-split partial traces (split order), FP64.
+__global__ void k_sum32s(const int* __restrict__ nill, const int* __restrict__ ntl,
+                         const C32* __restrict__ refl, const C32* __restrict__ part, int nsplit, int nr,
+                         void* __restrict__ out, int out64, int s0) {
+    const int s = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nr) return;
+    double vr = 0.0, vi = 0.0;
+    if (nill[s] > 0) {
+        C32 r = refl[(size_t)s * nr + i];
+        vr = r.x; vi = r.y;
+        const int ns = (ntl[s] + RP_CONV_SPLIT - 1) / RP_CONV_SPLIT;
+        const C32* z = part + (size_t)s * nsplit * nr + i;
+        for (int q = 0; q < ns; ++q) {
+            C32 u = z[(size_t)q * nr];
+            vr += u.x;
+            vi += u.y;
+        }
+    }
+    const size_t o = (size_t)(s0 + s) * nr + i;
+    if (out64) reinterpret_cast<C64*>(out)[o] = C64{vr, vi};
+    else reinterpret_cast<float2*>(out)[o] = make_float2((float)vr, (float)vi);
 }
 
 __global__ void k_surf_conv32(const long long* __restrict__ acc, const int* __restrict__ nill,
@@ -665,17 +907,25 @@ void fast_take_setup(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<uint8_t>((size_t)L.nb * nt);            // target flags
     a.template take<int>((size_t)L.nb * nt);                // tlist
     a.template take<int>((size_t)L.nb * L.tstride);         // bt0
-    a.template take<int>(4);                                // maxw, work, err[2]
+    a.template take<int>(8);                                // maxw, work, err[2], conv work
     a.template take<long long>((size_t)L.nb * nr * 2);      // surface fixed point
     a.template take<C32>((size_t)L.nb * nr);                // refl
     a.template take<C32>((size_t)L.nb * L.surf_slot);       // surface conv scratch
 }
 
+bool use_smem_conv(const rp_scene* sc) { return sc->smem_conv && sc->nr <= 4096; }
+
+int64_t conv_splits(int64_t tstride) { return (tstride + RP_CONV_SPLIT - 1) / RP_CONV_SPLIT; }
+
 template <class Aa>
 void fast_take_pairs(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<C32>((size_t)RP_PARTS * L.nb * L.tstride * L.Wt);   // T parts
-    a.template take<C32>((size_t)L.nb * L.tstride * sc->nr);            // Z
-    a.template take<C32>((size_t)L.slots * L.slot);                      // conv scratch
+    if (use_smem_conv(sc)) {
+        a.template take<C32>((size_t)L.nb * conv_splits(L.tstride) * sc->nr);   // partial traces
+    } else {
+        a.template take<C32>((size_t)L.nb * L.tstride * sc->nr);        // Z
+        a.template take<C32>((size_t)L.slots * L.slot);                  // conv scratch
+    }
 }
 
 FastLayout fast_layout(const rp_scene* sc, int nb, int64_t tstride, int Wt) {
@@ -714,6 +964,25 @@ std::vector<int> host_target_bounds32(const rp_scene* sc, const std::vector<doub
     return ub;
 }
 
+template <int KPT>
+int launch_conv_k(const ConvArgs& C, size_t csm, int sms, int items, cudaStream_t st) {
+    RP_CUDA(cudaFuncSetAttribute(k_conv32s<KPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+    int occ = 0;
+    RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv32s<KPT>, RP_CONV_THREADS, csm));
+    int grid = std::max(1, std::min(std::max(occ, 1) * sms, items));
+    k_conv32s<KPT><<<grid, RP_CONV_THREADS, csm, st>>>(C);
+    RP_LAUNCHED();
+    return RP_OK;
+}
+
+int launch_conv32s(const ConvArgs& C, size_t csm, int sms, int items, cudaStream_t st) {
+    const int kpt = (C.nr + RP_CONV_THREADS - 1) / RP_CONV_THREADS;
+    if (kpt <= 1) return launch_conv_k<1>(C, csm, sms, items, st);
+    if (kpt <= 2) return launch_conv_k<2>(C, csm, sms, items, st);
+    if (kpt <= 4) return launch_conv_k<4>(C, csm, sms, items, st);
+    return launch_conv_k<8>(C, csm, sms, items, st);
+}
+
 }  // namespace
 
 size_t rp_fast_scratch(const rp_scene* sc, int64_t ns) {
@@ -741,9 +1010,12 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
     PlanV<float> p2 = plan_view32(sc->plan2), pN = plan_view32(sc->planN);
     const DevParams& dp = sc->dp;
     const size_t pair_smem = 2 * RP_CHUNK * sizeof(FacetRec) + (size_t)RP_WIN * RP_PAIR_THREADS * sizeof(float2);
-    RP_CUDA(cudaFuncSetAttribute(k_pairs32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem));
+    // register/occupancy variant of the pair kernel: 2 or 3 resident blocks per SM
+    const int variant = sc->pair_variant;
+    void (*pk)(PairArgs) = (variant == 3) ? k_pairs32<3> : k_pairs32<2>;
+    RP_CUDA(cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem));
     int occ = 0;
-    RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pairs32, RP_PAIR_THREADS, pair_smem));
+    RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, RP_PAIR_THREADS, pair_smem));
     occ = std::max(occ, 1);
     for (int64_t s0 = 0; s0 < ns;) {
         int nb = 0;
@@ -788,7 +1060,7 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
         uint8_t* tflags = a.take<uint8_t>((size_t)nb * nta);
         int* tlist = a.take<int>((size_t)nb * nta);
         int* bt0 = a.take<int>((size_t)nb * Lw.tstride);
-        int* misc = a.take<int>(4);
+        int* misc = a.take<int>(8);
         long long* acc = a.take<long long>((size_t)nb * nr * 2);
         C32* refl = a.take<C32>((size_t)nb * nr);
         C32* sscr = a.take<C32>((size_t)nb * Lw.surf_slot);
@@ -798,7 +1070,7 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
         RP_CUDA(cudaMemsetAsync(vmax, 0, sizeof(unsigned long long) * nb, st));
         RP_CUDA(cudaMemsetAsync(dmin, 0xff, sizeof(unsigned long long) * nb, st));
         RP_CUDA(cudaMemsetAsync(acc, 0, sizeof(long long) * nb * nr * 2, st));
-        RP_CUDA(cudaMemsetAsync(misc, 0, sizeof(int) * 4, st));
+        RP_CUDA(cudaMemsetAsync(misc, 0, sizeof(int) * 8, st));
         if (nf > 0) {
             k_cull_count<<<dim3((unsigned)((nf + RP_TILE - 1) / RP_TILE), nb), RP_TILE_THREADS, 0, st>>>(
                 sc->d_sorted, nf, trb, dp.ap_rad, fflags, tcnt, dmin);
@@ -834,9 +1106,18 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
         g_timer.collect(0, 1);
         const int Wt = std::max(1, std::min(nr, (h_maxw + 3) & ~3));
         FastLayout L = fast_layout(sc, nb, tmax, Wt);
+        const bool smem_conv = use_smem_conv(sc);
+        const int nsplit = (int)conv_splits(L.tstride);
         C32* T = a.take<C32>((size_t)RP_PARTS * nb * L.tstride * Wt);
-        C32* Z = a.take<C32>((size_t)nb * L.tstride * nr);
-        C32* cscr = a.take<C32>((size_t)L.slots * L.slot);
+        C32* Z = nullptr;
+        C32* cscr = nullptr;
+        C32* part = nullptr;
+        if (smem_conv) {
+            part = a.take<C32>((size_t)nb * nsplit * nr);
+        } else {
+            Z = a.take<C32>((size_t)nb * L.tstride * nr);
+            cscr = a.take<C32>((size_t)L.slots * L.slot);
+        }
         RP_CUDA(cudaMemsetAsync(T, 0, sizeof(C32) * RP_PARTS * nb * L.tstride * Wt, st));
         g_timer.mark(1, st);
         if (nt > 0 && nf > 0 && tmax > 0) {
@@ -857,22 +1138,42 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
             P.nidx = dp.nidx; P.inv_dr = 1.0 / dp.dr; P.inv_lam = dp.turn;
             P.lossless = dp.lossless;
             int grid = std::min(occ * sc->sm_count, nb * P.tblocks * RP_PARTS);
-            k_pairs32<<<grid, RP_PAIR_THREADS, pair_smem, st>>>(P);
+            pk<<<grid, RP_PAIR_THREADS, pair_smem, st>>>(P);
             RP_LAUNCHED();
             ++g_timer.pair_launches;
             g_timer.mark(2, st);
             const float sig_scale = (float)(-1.0 / std::sqrt(dp.P));
-            k_conv32<<<L.slots, 256, 0, st>>>(d_ntl, L.tstride, nb, bt0, T, Wt, Z, (const C32*)sc->d_C2_32,
-                                             p2, pN, sc->crop_K, sc->crop_all, nr, sig_scale, cscr, L.slot);
-            RP_LAUNCHED();
+            if (smem_conv) {
+                ConvArgs C;
+                C.ntl = d_ntl; C.tstride = L.tstride; C.nb = nb; C.bt0 = bt0; C.T = T; C.Wt = Wt;
+                C.tw = (const Cplx<float>*)sc->d_twS; C.log2M = sc->log2mS;
+                C.C2s = (const Cplx<float>*)sc->d_C2S; C.bWs = (const Cplx<float>*)sc->d_bWS;
+                C.bWis = (const Cplx<float>*)sc->d_bWiS; C.bw = (const Cplx<float>*)sc->planN.bw32;
+                C.nr = nr; C.n2 = 2 * nr; C.N = 2 * nr - 1; C.M = sc->mS;
+                C.crop_K = sc->crop_K; C.crop_all = sc->crop_all; C.sig_scale = sig_scale;
+                C.part = part; C.nsplit = nsplit; C.work = reinterpret_cast<unsigned int*>(misc + 4);
+                const size_t csm = (size_t)(C.n2 + C.M) * sizeof(Cplx<float>);
+                int rc2 = launch_conv32s(C, csm, sc->sm_count, nb * nsplit, st);
+                if (rc2) return rc2;
+            } else {
+                k_conv32<<<L.slots, 256, 0, st>>>(d_ntl, L.tstride, nb, bt0, T, Wt, Z, (const C32*)sc->d_C2_32,
+                                                 p2, pN, sc->crop_K, sc->crop_all, nr, sig_scale, cscr, L.slot);
+                RP_LAUNCHED();
+            }
         }
         if (!(nt > 0 && nf > 0 && tmax > 0)) g_timer.mark(2, st);
         g_timer.mark(3, st);
         k_surf_conv32<<<nb, 256, 0, st>>>(acc, d_nill, vmax, dp.disable_surface, nr, (const C32*)sc->d_C1_32, p2,
                                          refl, sscr, Lw.surf_slot);
         RP_LAUNCHED();
-        k_sum32<<<dim3((nr + 255) / 256, nb), 256, 0, st>>>(d_nill, d_ntl, L.tstride, refl, Z, nr, d_out, out64,
-                                                           (int)s0);
+        if (smem_conv) {
+            if (!(nt > 0 && nf > 0 && tmax > 0)) RP_CUDA(cudaMemsetAsync(part, 0, sizeof(C32) * nb * nsplit * nr, st));
+            k_sum32s<<<dim3((nr + 255) / 256, nb), 256, 0, st>>>(d_nill, d_ntl, refl, part, nsplit, nr, d_out,
+                                                                out64, (int)s0);
+        } else {
+            k_sum32<<<dim3((nr + 255) / 256, nb), 256, 0, st>>>(d_nill, d_ntl, L.tstride, refl, Z, nr, d_out,
+                                                               out64, (int)s0);
+        }
         RP_LAUNCHED();
         g_timer.mark(4, st);
         RP_CUDA(cudaGetLastError());

@@ -1,0 +1,166 @@
+// rp_fft.cuh -- in-place power-of-two FFT stages shared by the host (table
+// preparation) and the device (block-level transforms in shared memory).
+//
+// Forward transforms are decimation-in-frequency: natural order in,
+// digit-reversed order out.  Inverse transforms are the mirrored
+// decimation-in-time stages: digit-reversed in, natural out, unscaled
+// (DIT(DIF(x)) = n x, the cuFFT convention of the reference).  Pointwise
+// products between two DIF outputs of the same length are therefore valid in
+// the scrambled order, and no permutation pass is ever needed.  Spectral
+// tables (chirp and Bluestein kernels) are prepared on the host with these
+// same stage functions, so they come out in the device's order.
+//
+// Stage schedule for n = 2^m: DIF runs radix-4 stages of span L = n, n/4,
+// ... while L >= 4, then one radix-2 stage (L = 2) if m is odd; DIT runs the
+// same stages in reverse.  Twiddles come from a table tw[k] = e^{-2 pi i k/M}
+// of a power of two M >= n (k < M): e^{-2 pi i j/L} = tw[j * (M / L)].
+#pragma once
+
+#include <cuda_runtime.h>
+
+template <class T> struct Cplx { T x, y; };
+
+template <class T> __host__ __device__ __forceinline__ Cplx<T> c_mul(Cplx<T> a, Cplx<T> b) {
+    return Cplx<T>{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+template <class T> __host__ __device__ __forceinline__ Cplx<T> c_mulc(Cplx<T> a, Cplx<T> b) {
+    // a * conj(b)
+    return Cplx<T>{a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y};
+}
+template <class T> __host__ __device__ __forceinline__ Cplx<T> c_add(Cplx<T> a, Cplx<T> b) { return Cplx<T>{a.x + b.x, a.y + b.y}; }
+template <class T> __host__ __device__ __forceinline__ Cplx<T> c_sub(Cplx<T> a, Cplx<T> b) { return Cplx<T>{a.x - b.x, a.y - b.y}; }
+
+__host__ __device__ __forceinline__ int fft_log2(int n) {
+    int l = 0;
+    while ((1 << l) < n) ++l;
+    return l;
+}
+
+// One radix-4 DIF butterfly, t in [0, n/4), stage span L (L >= 4).
+template <class T, class TW>
+__host__ __device__ __forceinline__ void dif4(Cplx<T>* a, int L, int lq, int t, const TW& tw, int mshift) {
+    const int q4 = L >> 2;
+    const int j = t & (q4 - 1);
+    const int b = (t >> lq) * L + j;       // lq = log2(q4)
+    Cplx<T> x0 = a[b], x1 = a[b + q4], x2 = a[b + 2 * q4], x3 = a[b + 3 * q4];
+    Cplx<T> t0 = c_add(x0, x2), t1 = c_sub(x0, x2), t2 = c_add(x1, x3), t3 = c_sub(x1, x3);
+    Cplx<T> y0 = c_add(t0, t2), y2 = c_sub(t0, t2);
+    Cplx<T> y1 = Cplx<T>{t1.x + t3.y, t1.y - t3.x};   // t1 - i t3
+    Cplx<T> y3 = Cplx<T>{t1.x - t3.y, t1.y + t3.x};   // t1 + i t3
+    a[b] = y0;
+    if (j == 0) {
+        a[b + q4] = y1; a[b + 2 * q4] = y2; a[b + 3 * q4] = y3;
+    } else {
+        Cplx<T> w1 = tw(j << mshift);              // e^{-2 pi i j / L}
+        Cplx<T> w2 = c_mul(w1, w1);
+        Cplx<T> w3 = c_mul(w1, w2);
+        a[b + q4] = c_mul(y1, w1);
+        a[b + 2 * q4] = c_mul(y2, w2);
+        a[b + 3 * q4] = c_mul(y3, w3);
+    }
+}
+
+// One radix-4 DIT butterfly (inverse direction), mirror of dif4.
+template <class T, class TW>
+__host__ __device__ __forceinline__ void dit4(Cplx<T>* a, int L, int lq, int t, const TW& tw, int mshift) {
+    const int q4 = L >> 2;
+    const int j = t & (q4 - 1);
+    const int b = (t >> lq) * L + j;
+    Cplx<T> x0 = a[b], x1 = a[b + q4], x2 = a[b + 2 * q4], x3 = a[b + 3 * q4];
+    if (j != 0) {
+        Cplx<T> w1 = tw(j << mshift);
+        Cplx<T> w2 = c_mul(w1, w1);
+        Cplx<T> w3 = c_mul(w1, w2);
+        x1 = c_mulc(x1, w1);
+        x2 = c_mulc(x2, w2);
+        x3 = c_mulc(x3, w3);
+    }
+    Cplx<T> t0 = c_add(x0, x2), t1 = c_sub(x0, x2), t2 = c_add(x1, x3), t3 = c_sub(x1, x3);
+    a[b] = c_add(t0, t2);
+    a[b + 2 * q4] = c_sub(t0, t2);
+    a[b + q4] = Cplx<T>{t1.x - t3.y, t1.y + t3.x};       // t1 + i t3
+    a[b + 3 * q4] = Cplx<T>{t1.x + t3.y, t1.y - t3.x};   // t1 - i t3
+}
+
+// Radix-2 stages of span L (t in [0, n/2)).
+template <class T, class TW>
+__host__ __device__ __forceinline__ void dif2(Cplx<T>* a, int L, int lh, int t, const TW& tw, int mshift) {
+    const int h = L >> 1;
+    const int j = t & (h - 1);
+    const int b = (t >> lh) * L + j;
+    Cplx<T> x0 = a[b], x1 = a[b + h];
+    a[b] = c_add(x0, x1);
+    Cplx<T> d = c_sub(x0, x1);
+    a[b + h] = (j == 0) ? d : c_mul(d, tw(j << mshift));
+}
+
+template <class T, class TW>
+__host__ __device__ __forceinline__ void dit2(Cplx<T>* a, int L, int lh, int t, const TW& tw, int mshift) {
+    const int h = L >> 1;
+    const int j = t & (h - 1);
+    const int b = (t >> lh) * L + j;
+    Cplx<T> x0 = a[b], x1 = a[b + h];
+    if (j != 0) x1 = c_mulc(x1, tw(j << mshift));
+    a[b] = c_add(x0, x1);
+    a[b + h] = c_sub(x0, x1);
+}
+
+// Host: full transforms (serial), used to prepare device-order tables.
+template <class T, class TW>
+void host_dif(Cplx<T>* a, int n, const TW& tw, int log2M) {
+    const int m = fft_log2(n);
+    int L = n, lL = m;
+    for (; L >= 4; L >>= 2, lL -= 2)
+        for (int t = 0; t < n / 4; ++t) dif4(a, L, lL - 2, t, tw, log2M - lL);
+    if (L == 2)
+        for (int t = 0; t < n / 2; ++t) dif2(a, 2, 0, t, tw, log2M - 1);
+}
+
+template <class T, class TW>
+void host_dit(Cplx<T>* a, int n, const TW& tw, int log2M) {
+    const int m = fft_log2(n);
+    int L, lL;
+    if (m & 1) {
+        for (int t = 0; t < n / 2; ++t) dit2(a, 2, 0, t, tw, log2M - 1);
+        L = 8; lL = 3;
+    } else {
+        L = 4; lL = 2;
+    }
+    for (; L <= n; L <<= 2, lL += 2)
+        for (int t = 0; t < n / 4; ++t) dit4(a, L, lL - 2, t, tw, log2M - lL);
+}
+
+#ifdef __CUDACC__
+// Device: block-cooperative transforms on shared memory; every thread of the
+// block must call them.  tw reads the global twiddle table of length M.
+template <class T, class TW>
+__device__ void block_dif(Cplx<T>* a, int n, const TW& tw, int log2M) {
+    const int m = fft_log2(n);
+    int L = n, lL = m;
+    for (; L >= 4; L >>= 2, lL -= 2) {
+        for (int t = threadIdx.x; t < n / 4; t += blockDim.x) dif4(a, L, lL - 2, t, tw, log2M - lL);
+        __syncthreads();
+    }
+    if (L == 2) {
+        for (int t = threadIdx.x; t < n / 2; t += blockDim.x) dif2(a, 2, 0, t, tw, log2M - 1);
+        __syncthreads();
+    }
+}
+
+template <class T, class TW>
+__device__ void block_dit(Cplx<T>* a, int n, const TW& tw, int log2M) {
+    const int m = fft_log2(n);
+    int L, lL;
+    if (m & 1) {
+        for (int t = threadIdx.x; t < n / 2; t += blockDim.x) dit2(a, 2, 0, t, tw, log2M - 1);
+        __syncthreads();
+        L = 8; lL = 3;
+    } else {
+        L = 4; lL = 2;
+    }
+    for (; L <= n; L <<= 2, lL += 2) {
+        for (int t = threadIdx.x; t < n / 4; t += blockDim.x) dit4(a, L, lL - 2, t, tw, log2M - lL);
+        __syncthreads();
+    }
+}
+#endif

@@ -100,6 +100,16 @@ struct rp_scene {
     float* d_C2_32 = nullptr;
     int crop_K = 0;                      // kept spectrum half-width on the N grid
     int crop_all = 0;                    // crop keeps every bin
+    // shared-memory compression tables (nr a power of two): FP32, spectra in
+    // the digit-reversed order of the in-place DIF stages (rp_fft.cuh)
+    int smem_conv = 0;                   // tables present
+    int mS = 0, log2mS = 0;              // M = 4 nr
+    float* d_twS = nullptr;              // e^{-2 pi i k / M}, k < M
+    float* d_C2S = nullptr;              // DIF_2nr(target chirp)
+    float* d_bWS = nullptr;              // DIF_M(conj Bluestein chirp)
+    float* d_bWiS = nullptr;             // DIF_M(Bluestein chirp)
+    // ---- tuning
+    int pair_variant = 3;                // resident pair-kernel blocks per SM (2 or 3)
     // ---- scratch
     Arena arena;
     cudaStream_t own_stream = nullptr;

@@ -11,12 +11,13 @@ the inbound one times -1/sqrt(P) in the non-specular mode; so one k_pairs32
 evaluation covers two metric pairs.
 
 MUFU (special-function unit) instructions per k_pairs32 evaluation, read off
-the source: rsqrt (1/Ttd), the fast division for dT (1), two rsqrt for the
-azimuth/inclination projections (2), four sin for the sinc factors (4), four
-sinc divisions (4, each a reciprocal), exp2 (1) and sin+cos of the phase (2).
+the source (pair_eval): rsqrt (1/Ttd), the fast division for dT (1), two
+rsqrt for the azimuth/inclination projections (2), four sin for the sinc
+factors (4), one reciprocal shared by the four sinc quotients (1), exp2 (1)
+and sin + cos of the phase (2).
 """
 
-MUFU_PER_EVAL = 15
+MUFU_PER_EVAL = 12
 EVALS_PER_TARGET_PAIR_METRIC = 0.5     # one evaluation covers two metric pairs
 
 # Nominal special-function throughput of a Blackwell SM (results per clock).
