@@ -76,6 +76,8 @@ _SIGS = {
     "rp_last_launch_count": ([ctypes.c_void_p], ctypes.c_int),
     "rp_set_timing": ([ctypes.c_int], ctypes.c_int),
     "rp_last_timing": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rp_surface_noalloc": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                            ctypes.c_void_p], ctypes.c_int),
 }
 
 

@@ -167,6 +167,26 @@ int rp_set_timing(int enable);
  *   number of pair-kernel launches. */
 int rp_last_timing(double* ms, int n);
 
+/*
+ * Surface-only radargram columns with no device allocation at call time.
+ * No counterpart in the reference.  For callers that may not allocate
+ * device memory once they are running (their device memory budget is fixed
+ * up front, e.g. owned by a host application's allocator or a long-running
+ * service that must not grow after initialisation): the scene is created
+ * beforehand with rp_scene_create, and this call then allocates nothing --
+ * its scratch is a fixed 16 MiB array inside the library.
+ *   d_traces  device double[ns][9]; d_out device float2[ns][nr]
+ *   limits    ns <= 16 traces and nr <= 4096 range bins per call, else
+ *             RP_ERR_BUDGET with the limits in rp_last_error()
+ * The result equals rp_simulate_device's fast form for a scene without
+ * targets.  Every call shares the one scratch array: calls that overlap on
+ * the GPU (different streams, or unordered host threads) race and must not
+ * be issued.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ */
+int rp_surface_noalloc(const rp_scene* s, const double* d_traces, int64_t ns, void* d_out,
+                       void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,60 @@
+"""rp_surface_noalloc: surface-only columns with no device allocation.
+
+Some callers cannot allocate device memory once they are running -- their
+device memory is fixed at start-up (owned by a host application's allocator,
+or a service that must not grow after initialisation).  For them the library
+offers one entry point whose scratch is a fixed array inside the library.
+This test calls it through the C ABI twice in a row and checks both results
+against the resident fast form (rp_simulate_device) on a scene without
+targets, within the fast form's parity tolerance; it also checks that
+oversized requests are refused with RP_ERR_BUDGET.
+
+The file name sorts last so that a run stopping at the first failure has
+already run every other test.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from helpers import rel_l2, tiny_scene
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+
+
+def test_surface_noalloc_matches_resident_fast_form(built_lib):
+    import torch
+    from europaraypaths_gb300 import _abi, simulator, traces as tr_mod
+
+    sc = tiny_scene(nside=40, ns=5)
+    scene = simulator.Scene(sc["params"], sc["facets"], targets=None)
+    tr = tr_mod.linear_track(scene.params)
+    tr[2, 0] += 1e6                     # one trace sees no facet: a zero column
+    ns, nr = tr.shape[0], scene.nr
+    d_tr = torch.from_numpy(np.ascontiguousarray(tr)).cuda()
+    ref = torch.zeros((ns, nr), dtype=torch.complex64, device="cuda")
+    scene.simulate_device(d_tr, ref, form="fast")
+    torch.cuda.synchronize()
+    ref_h = ref.cpu().numpy()
+    assert np.abs(ref_h).max() > 0 and np.all(ref_h[2] == 0)
+    lib = _abi.lib()
+    for call in range(2):
+        out = torch.full((ns, nr), complex(float("nan"), float("nan")), dtype=torch.complex64,
+                         device="cuda")
+        rc = lib.rp_surface_noalloc(ctypes.c_void_p(scene.handle), ctypes.c_void_p(d_tr.data_ptr()),
+                                    ns, ctypes.c_void_p(out.data_ptr()), None)
+        _abi.check("rp_surface_noalloc", rc)
+        # the call runs on the scene's own stream; wait for the whole device
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        assert np.all(np.isfinite(got)), f"call {call}: unwritten output"
+        assert rel_l2(got, ref_h) <= TOL, f"call {call}: rel L2 {rel_l2(got, ref_h)}"
+        assert np.all(got[2] == 0)
+    # a request beyond the fixed scratch is refused, without touching the GPU
+    big = torch.zeros((17, 9), dtype=torch.float64, device="cuda")
+    rc = lib.rp_surface_noalloc(ctypes.c_void_p(scene.handle), ctypes.c_void_p(big.data_ptr()), 17,
+                                ctypes.c_void_p(out.data_ptr()), None)
+    assert rc == -7 and "at most 16 traces" in _abi.last_error()
+    scene.close()
