@@ -46,15 +46,20 @@ def dist_env():
     return rank, world, local
 
 
-def shard_steps(total_traces, traces_per_step, steps, warmup, rank, world):
+def shard_steps(total_traces, traces_per_step, steps, warmup, rank, world, lo=None, hi=None):
     """Weak scaling: each rank walks its own stretch of the track.
 
-    Returns the list of (start, count) trace batches for warm-up + timed steps
-    of this rank; batches wrap around the track."""
+    Batches are taken from the interior [lo, hi) of the track (default: the
+    middle half, where the aperture footprint lies wholly inside the scene)
+    and wrap around inside it.  Returns the (start, count) batches of this
+    rank's warm-up + timed steps."""
+    lo = total_traces // 4 if lo is None else lo
+    hi = (3 * total_traces) // 4 if hi is None else hi
+    span = max(hi - lo - traces_per_step + 1, 1)
     out = []
     per_rank = steps + warmup
     for k in range(per_rank):
-        start = ((rank * per_rank + k) * traces_per_step) % max(total_traces - traces_per_step + 1, 1)
+        start = lo + ((rank * per_rank + k) * traces_per_step) % span
         out.append((start, traces_per_step))
     return out
 
@@ -160,7 +165,8 @@ def run_reference(args):
     nthreads = os.cpu_count() or 1
     times, pairs = [], []
     for k in range(args.warmup + args.steps):
-        tr = track[(k * 97) % p.ns:(k * 97) % p.ns + 1]
+        i0 = p.ns // 4 + (k * 97) % (p.ns // 2)     # interior of the track
+        tr = track[i0:i0 + 1]
         t0 = time.perf_counter()
         _, counts = loader.simulate(p, sc["facets"], sc["targets"], tr, nthreads=nthreads,
                                     max_targets=args.ref_targets)
@@ -303,6 +309,8 @@ def main():
                 "ops_per_eval": opcount.MUFU_PER_EVAL,
                 "pair_kernel_ms_per_launch": stage["pairs_ms"] / max(stage["pair_launches"], 1),
                 "pair_evals_per_s": my_evals / pairs_s if pairs_s > 0 else None,
+                "pair_evals_per_launch": my_evals / max(stage["pair_launches"], 1),
+                "mean_counts_per_trace": [float(timed_counts[:, 0].mean()), float(timed_counts[:, 1].mean())],
                 "stage_ms": {k: stage[k] for k in ("setup_ms", "pairs_ms", "compress_ms", "tail_ms")},
                 "hbm_peak_gbs": peaks.get("hbm_gbs")}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

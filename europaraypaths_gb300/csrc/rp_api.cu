@@ -418,7 +418,7 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
         if ((rc = upload(&s->d_sorted, sorted.data(), sizeof(double) * 12 * nf, &s->store_bytes))) return fail(rc);
     }
     if ((rc = build_tables(s))) return fail(rc);
-    if (const char* v = getenv("RP_PAIR_VARIANT")) s->pair_variant = atoi(v) == 2 ? 2 : 3;
+    if (const char* v = getenv("RP_PAIR_VARIANT")) s->pair_variant = atoi(v) == 1 ? 1 : 0;
     cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return fail(rp_cuda_fail(e, "cudaStreamCreate"));
     *out = s;

@@ -22,6 +22,7 @@
 //      the phase of rngt - lam/2, radar_kernels.cu:834-892);
 //   5. surface range compression and a fixed-order sum over targets.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <vector>
 
@@ -175,27 +176,70 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
 }
 
 // Fixed-point accumulation of the surface leg (same scheme as the plain form).
-__global__ void k_surf_fix32(int64_t nf, const int* __restrict__ nill, const float* __restrict__ sx,
-                             const C32* __restrict__ sv, const unsigned long long* __restrict__ vmax,
-                             int nr, long long* __restrict__ acc) {
+// The surface of a trace concentrates in a few bins, so each block first sums
+// its facets into a shared-memory window of RP_SFIX_WIN bins starting at the
+// block's lowest bin (integer adds: order-free), then adds each non-zero bin
+// to the trace with one global atomic; contributions beyond the window go to
+// global memory directly.
+#define RP_SFIX_WIN 128
+#define RP_SFIX_PER 4
+__global__ void __launch_bounds__(256) k_surf_fix32(int64_t nf, const int* __restrict__ nill,
+                                                    const float* __restrict__ sx, const C32* __restrict__ sv,
+                                                    const unsigned long long* __restrict__ vmax, int nr,
+                                                    long long* __restrict__ acc) {
+    __shared__ unsigned long long hist[2 * RP_SFIX_WIN];
+    __shared__ int sh_min[32];
     const int s = blockIdx.y;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = nill[s];
-    if (j >= n) return;
+    const int64_t j0 = (int64_t)blockIdx.x * blockDim.x * RP_SFIX_PER;
+    if (j0 >= n) return;                                  // uniform per block
     double vm = __longlong_as_double((long long)vmax[s]);
     if (!(vm > 0)) return;
     const double scale = ldexp(1.0, RP_FIX_BITS) / (2.0 * (double)n * vm);
-    double x = sx[(size_t)s * nf + j];
-    if (!(x > -1.0) || x >= (double)nr) return;
-    long b = (long)x;
-    double w = x - (double)b;
-    C32 v = sv[(size_t)s * nf + j];
     long long* a = acc + (size_t)s * nr * 2;
-    fix_add(a + 2 * b, (double)v.x * (1.0 - w), scale);
-    fix_add(a + 2 * b + 1, (double)v.y * (1.0 - w), scale);
-    if (b + 1 < nr) {
-        fix_add(a + 2 * (b + 1), (double)v.x * w, scale);
-        fix_add(a + 2 * (b + 1) + 1, (double)v.y * w, scale);
+    int bl = INT_MAX;
+    for (int k = 0; k < RP_SFIX_PER; ++k) {
+        const int64_t j = j0 + (int64_t)k * blockDim.x + threadIdx.x;
+        if (j < n) {
+            double x = sx[(size_t)s * nf + j];
+            if (x > -1.0 && x < (double)nr) bl = min(bl, (int)(long)x);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) bl = min(bl, __shfl_xor_sync(0xffffffffu, bl, o));
+    if ((threadIdx.x & 31) == 0) sh_min[threadIdx.x >> 5] = bl;
+    for (int i = threadIdx.x; i < 2 * RP_SFIX_WIN; i += blockDim.x) hist[i] = 0ull;
+    __syncthreads();
+    int blo = INT_MAX;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) blo = min(blo, sh_min[w]);
+    for (int k = 0; k < RP_SFIX_PER; ++k) {
+        const int64_t j = j0 + (int64_t)k * blockDim.x + threadIdx.x;
+        if (j >= n) continue;
+        double x = sx[(size_t)s * nf + j];
+        if (!(x > -1.0) || x >= (double)nr) continue;
+        long b = (long)x;
+        double w = x - (double)b;
+        C32 v = sv[(size_t)s * nf + j];
+        const long long q[4] = {llrint((double)v.x * (1.0 - w) * scale), llrint((double)v.y * (1.0 - w) * scale),
+                                llrint((double)v.x * w * scale), llrint((double)v.y * w * scale)};
+        for (int h = 0; h < 2; ++h) {
+            const long bb = b + h;
+            if (h == 1 && bb >= nr) break;
+            const long sl = bb - blo;
+            if (sl >= 0 && sl < RP_SFIX_WIN) {
+                atomicAdd(&hist[2 * sl], (unsigned long long)q[2 * h]);
+                atomicAdd(&hist[2 * sl + 1], (unsigned long long)q[2 * h + 1]);
+            } else {
+                atomicAdd(reinterpret_cast<unsigned long long*>(a + 2 * bb), (unsigned long long)q[2 * h]);
+                atomicAdd(reinterpret_cast<unsigned long long*>(a + 2 * bb + 1), (unsigned long long)q[2 * h + 1]);
+            }
+        }
+    }
+    __syncthreads();
+    if (blo == INT_MAX) return;
+    for (int i = threadIdx.x; i < 2 * RP_SFIX_WIN; i += blockDim.x) {
+        const unsigned long long v = hist[i];
+        const long bb = blo + (i >> 1);
+        if (v != 0ull && bb < nr) atomicAdd(reinterpret_cast<unsigned long long*>(a + 2 * bb + (i & 1)), v);
     }
 }
 
@@ -327,6 +371,7 @@ struct PairArgs {
     float kb;           // n / dr
     float kt;           // n / lam
     float pik;          // pi * (pi_F * fs / lam): sinc arguments in radians
+    float pik2;         // pik^2
     float ealpha;       // -2 alpha2 log2(e)
     float eks;          // -2 ks^2 log2(e)
     double nidx, inv_dr, inv_lam;   // inv_lam: turns per metre, pi_F / (pi lam)
@@ -342,12 +387,38 @@ struct Anchor {
     float tnx, tny, tnz;  // target normal
 };
 
+// Maclaurin coefficients of sin(a)/a in powers of a^2: (-1)^k / (2k+1)!.
+__constant__ float c_sinc_coef[16] = {
+    1.0f, -1.0f / 6.0f, 1.0f / 120.0f, -1.0f / 5040.0f, 1.0f / 362880.0f, -1.0f / 39916800.0f,
+    1.0f / 6227020800.0f, -1.0f / 1307674368000.0f, 1.0f / 355687428096000.0f,
+    -1.0f / 121645100408832000.0f, 1.0f / 51090942171709440000.0f,
+    -1.0f / 25852016738884976640000.0f, 1.0f / 15511210043330985984000000.0f,
+    -1.0f / 10888869450418352160768000000.0f, 1.0f / 8841761993739701954543616000000.0f,
+    -1.0f / 8222838654177922817725562880000000.0f};
+
+// sin(a)/a from a^2 with NT Maclaurin terms (Horner in a^2).
+template <int NT>
+__device__ __forceinline__ float sinc_sq(float a2) {
+    float s = c_sinc_coef[NT - 1];
+#pragma unroll
+    for (int k = NT - 2; k >= 0; --k) s = fmaf(s, a2, c_sinc_coef[k]);
+    return s;
+}
+
 // One (facet, target) evaluation of the target leg (compTargetRays,
 // compRefrEnergyIn, accumulateTarget; geometry_kernels.cu:272-350, 520-554,
 // radar_kernels.cu:767-830).  Returns the phasor and x - blo, the bin
-// coordinate relative to the window start.  sinc(x) = sin(pi x)/(pi x) is
-// evaluated as sin(a)/a with a = pi x; the four quotients share one
-// reciprocal, and |x| < 1e-6 counts as sinc = 1 (elementary_kernels.cu:50-53).
+// coordinate relative to the window start.
+//
+// The two directivities facet_G(Tth, Tph) and facet_G(TargetTh, Tph)
+// (radar_kernels.cu:658-677) need sinc(pik/pi * sin(th) cos(ph)) and
+// sinc(pik/pi * sin(th) sin(ph)), sinc(x) = sin(pi x)/(pi x).  With
+// cos(Tph) = xv / sqrt(h2), sin(Tph) = yu / sqrt(h2) and sin^2(th) = 1 - c^2,
+// the squared sinc arguments are pik^2 (1 - c^2) xv^2 / h2 etc. (atan2(0, 0)
+// = 0 gives xv^2/h2 = 1, yu^2/h2 = 0).  NT > 0 evaluates sin(a)/a as a
+// polynomial in a^2 (no special-function unit); NT == 0 uses sin(a)/a with
+// one shared reciprocal, 1 for |a| < pi 1e-6 (elementary_kernels.cu:50-53).
+template <int NT>
 __device__ __forceinline__ void pair_eval(const FacetRec& r, const Anchor& an, const PairArgs& A,
                                           float& xr, float& vre, float& vim) {
     const float dd = fmaf(an.Dx, r.a.x, fmaf(an.Dy, r.a.y, an.Dz * r.a.z));
@@ -363,29 +434,36 @@ __device__ __forceinline__ void pair_eval(const FacetRec& r, const Anchor& an, c
     const float cD = fminf(1.f, fmaxf(-1.f, -fmaf(jx, an.tnx, fmaf(jy, an.tny, jz * an.tnz))));
     const float yu = fmaf(jx, r.c.x, fmaf(jy, r.c.y, jz * r.c.z));
     const float xv = fmaf(jx, r.d.x, fmaf(jy, r.d.y, jz * r.d.z));
-    const float h2 = fmaf(xv, xv, yu * yu);
+    const float X = xv * xv, Y = yu * yu;
+    const float h2 = X + Y;
     const float aT = fmaf(-cT, cT, 1.f);
     const float aD = fmaf(-cD, cD, 1.f);
-    // sin(th) cos(ph) = sqrt(a) xv / sqrt(h2); atan2(0, 0) = 0 gives (sqrt(a), 0)
-    const bool hz = !(h2 > 0.f);
-    const float pT = aT * h2, pD = aD * h2;
-    const float gT = (pT > 0.f) ? aT * rsqrtf(pT) : 0.f;
-    const float gD = (pD > 0.f) ? aD * rsqrtf(pD) : 0.f;
-    const float a1 = A.pik * (hz ? sqrtf(aT) : gT * xv);
-    const float a2 = A.pik * (hz ? 0.f : gT * yu);
-    const float a3 = A.pik * (hz ? sqrtf(aD) : gD * xv);
-    const float a4 = A.pik * (hz ? 0.f : gD * yu);
-    const float eps = 3.14159265e-6f;
-    const bool z1 = fabsf(a1) < eps, z2 = fabsf(a2) < eps, z3 = fabsf(a3) < eps, z4 = fabsf(a4) < eps;
-    const float num = (z1 ? 1.f : __sinf(a1)) * (z2 ? 1.f : __sinf(a2)) * (z3 ? 1.f : __sinf(a3)) *
-                      (z4 ? 1.f : __sinf(a4));
-    const float den = (z1 ? 1.f : a1) * (z2 ? 1.f : a2) * (z3 ? 1.f : a3) * (z4 ? 1.f : a4);
-    const float S = __fdividef(num, den);
-    float e2 = 0.f;
-    if (!A.lossless) {
-        float ea = A.ealpha * Ttd;
-        e2 = fmaf(A.eks, cT * cT, ea);
+    float S;
+    if (NT > 0) {
+        const bool hz = !(h2 > 0.f);
+        const float k2 = A.pik2 * __frcp_rn(hz ? 1.f : h2);
+        const float xx = hz ? A.pik2 : k2 * X;
+        const float yy = hz ? 0.f : k2 * Y;
+        S = sinc_sq<(NT > 0 ? NT : 1)>(aT * xx) * sinc_sq<(NT > 0 ? NT : 1)>(aT * yy) *
+            sinc_sq<(NT > 0 ? NT : 1)>(aD * xx) * sinc_sq<(NT > 0 ? NT : 1)>(aD * yy);
+    } else {
+        const bool hz = !(h2 > 0.f);
+        const float pT = aT * h2, pD = aD * h2;
+        const float gT = (pT > 0.f) ? aT * rsqrtf(pT) : 0.f;
+        const float gD = (pD > 0.f) ? aD * rsqrtf(pD) : 0.f;
+        const float a1 = A.pik * (hz ? sqrtf(aT) : gT * xv);
+        const float a2 = A.pik * (hz ? 0.f : gT * yu);
+        const float a3 = A.pik * (hz ? sqrtf(aD) : gD * xv);
+        const float a4 = A.pik * (hz ? 0.f : gD * yu);
+        const float eps = 3.14159265e-6f;
+        const bool z1 = fabsf(a1) < eps, z2 = fabsf(a2) < eps, z3 = fabsf(a3) < eps, z4 = fabsf(a4) < eps;
+        const float num = (z1 ? 1.f : __sinf(a1)) * (z2 ? 1.f : __sinf(a2)) * (z3 ? 1.f : __sinf(a3)) *
+                          (z4 ? 1.f : __sinf(a4));
+        const float den = (z1 ? 1.f : a1) * (z2 ? 1.f : a2) * (z3 ? 1.f : a3) * (z4 ? 1.f : a4);
+        S = __fdividef(num, den);
     }
+    float e2 = 0.f;
+    if (!A.lossless) e2 = fmaf(A.eks, cT * cT, A.ealpha * Ttd);
     const float amp = r.d.w * fabsf(S) * rinv * exp2f(e2);
     float tau = r.c.w + an.tau0 + A.kt * dT;
     tau -= rintf(tau);
@@ -466,8 +544,8 @@ __device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo,
     }
 }
 
-template <int MINB>
-__global__ void __launch_bounds__(RP_PAIR_THREADS, MINB)
+template <int NT>
+__global__ void __launch_bounds__(RP_PAIR_THREADS, 3)
 k_pairs32(PairArgs A) {
     extern __shared__ __align__(128) unsigned char smem[];
     FacetRec* srec = reinterpret_cast<FacetRec*>(smem);                     // [2][RP_CHUNK]
@@ -560,8 +638,8 @@ k_pairs32(PairArgs A) {
                     const FacetRec r0 = R[jj];
                     const FacetRec r1 = R[jj + 1];
                     float x0, re0, im0, x1, re1, im1;
-                    pair_eval(r0, an, A, x0, re0, im0);
-                    pair_eval(r1, an, A, x1, re1, im1);
+                    pair_eval<NT>(r0, an, A, x0, re0, im0);
+                    pair_eval<NT>(r1, an, A, x1, re1, im1);
                     if (prisms) {
                         const float f0 = prism_factor(r0.a, m.cx, m.cy, m.cz, an.Dx, an.Dy, an.Dz, an.T0sq,
                                                       A.PR, A.np, A.ealpha);
@@ -575,7 +653,7 @@ k_pairs32(PairArgs A) {
                 if (jj < cnt) {
                     const FacetRec r0 = R[jj];
                     float x0, re0, im0;
-                    pair_eval(r0, an, A, x0, re0, im0);
+                    pair_eval<NT>(r0, an, A, x0, re0, im0);
                     if (prisms) {
                         const float f0 = prism_factor(r0.a, m.cx, m.cy, m.cz, an.Dx, an.Dy, an.Dz, an.T0sq,
                                                       A.PR, A.np, A.ealpha);
@@ -964,6 +1042,17 @@ std::vector<int> host_target_bounds32(const rp_scene* sc, const std::vector<doub
     return ub;
 }
 
+// Number of Maclaurin terms of sin(a)/a for |a| <= amax with truncation
+// error below 1e-9 (0: use the special-function unit).  variant 1 forces the
+// special-function path.
+int sinc_terms(double amax, int variant) {
+    if (variant == 1) return 0;
+    if (amax <= 2.0) return 7;
+    if (amax <= 3.2) return 10;
+    if (amax <= 4.6) return 13;
+    return 0;
+}
+
 template <int KPT>
 int launch_conv_k(const ConvArgs& C, size_t csm, int sms, int items, cudaStream_t st) {
     RP_CUDA(cudaFuncSetAttribute(k_conv32s<KPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
@@ -1010,9 +1099,10 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
     PlanV<float> p2 = plan_view32(sc->plan2), pN = plan_view32(sc->planN);
     const DevParams& dp = sc->dp;
     const size_t pair_smem = 2 * RP_CHUNK * sizeof(FacetRec) + (size_t)RP_WIN * RP_PAIR_THREADS * sizeof(float2);
-    // register/occupancy variant of the pair kernel: 2 or 3 resident blocks per SM
-    const int variant = sc->pair_variant;
-    void (*pk)(PairArgs) = (variant == 3) ? k_pairs32<3> : k_pairs32<2>;
+    // sinc evaluation: Maclaurin terms needed for |a| <= pik (0 = special-function unit)
+    const int nt_terms = sinc_terms(RP_PI * (RP_PI_F * dp.fs / dp.lam), sc->pair_variant);
+    void (*pk)(PairArgs) = nt_terms == 7 ? k_pairs32<7> : nt_terms == 10 ? k_pairs32<10>
+                         : nt_terms == 13 ? k_pairs32<13> : k_pairs32<0>;
     RP_CUDA(cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem));
     int occ = 0;
     RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, RP_PAIR_THREADS, pair_smem));
@@ -1079,7 +1169,8 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
             k_facets32<<<dim3((unsigned)Lw.mstride, nb), RP_CHUNK, 0, st>>>(
                 sc->d_sorted, nfa, idx, d_nill, trb, dp, rec, meta, Lw.rstride, Lw.mstride, sxv, sv, vmax);
             RP_LAUNCHED();
-            k_surf_fix32<<<dim3((unsigned)((nf + 255) / 256), nb), 256, 0, st>>>(nfa, d_nill, sxv, sv, vmax, nr, acc);
+            k_surf_fix32<<<dim3((unsigned)((nf + 256 * RP_SFIX_PER - 1) / (256 * RP_SFIX_PER)), nb), 256, 0, st>>>(
+                nfa, d_nill, sxv, sv, vmax, nr, acc);
             RP_LAUNCHED();
             k_tmeta32<<<nb, 256, 0, st>>>(meta, Lw.mstride, d_nill, tm);
             RP_LAUNCHED();
@@ -1133,6 +1224,7 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
             P.kb = (float)(dp.nidx / dp.dr);
             P.kt = (float)(dp.nidx * dp.turn);
             P.pik = (float)(RP_PI * (RP_PI_F * dp.fs / dp.lam));
+            P.pik2 = P.pik * P.pik;
             P.ealpha = (float)(-2.0 * dp.alpha2 * 1.4426950408889634);
             P.eks = (float)(-2.0 * dp.ks * dp.ks * 1.4426950408889634);
             P.nidx = dp.nidx; P.inv_dr = 1.0 / dp.dr; P.inv_lam = dp.turn;

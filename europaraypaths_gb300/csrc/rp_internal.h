@@ -109,7 +109,7 @@ struct rp_scene {
     float* d_bWS = nullptr;              // DIF_M(conj Bluestein chirp)
     float* d_bWiS = nullptr;             // DIF_M(Bluestein chirp)
     // ---- tuning
-    int pair_variant = 3;                // resident pair-kernel blocks per SM (2 or 3)
+    int pair_variant = 0;                // 0 auto (polynomial sinc where accurate), 1 special-function sinc
     // ---- scratch
     Arena arena;
     cudaStream_t own_stream = nullptr;

@@ -73,3 +73,16 @@ def test_fast_deterministic(built_lib):
     b = scene.simulate(form="fast")
     scene.close()
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.parametrize("nside", [400, 148])
+def test_fast_polynomial_sinc_regimes(built_lib, oracle, nside):
+    # fs = 5 m (sinc argument up to 1.5 rad: 7 Maclaurin terms) and
+    # fs = 13.5 m (up to 4 rad: 13 terms) at 9 MHz
+    from europaraypaths_gb300 import traces as tr_mod, param_gen
+    sc = tiny_scene(nside=nside, ntside=3, ns=2)
+    p = param_gen.to_rp_params(sc["params"])
+    tr = tr_mod.linear_track(p)
+    got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle, traces=tr)
+    assert np.array_equal(cnt, rcnt)
+    check(got, ref)

@@ -140,7 +140,14 @@ def test_kat_subsurface_target_gpu(built_lib, form):
 @pytest.mark.gpu
 def test_kat_subsurface_layer_gpu(built_lib):
     """subsurface_layer/code/params.py: vacuum, 20 km deep layer of 300x300
-    targets under 300x300 facets of 13.3 m; P of a mirror at 2(h+d)."""
+    targets under 300x300 facets of 13.3 m, source at altitude h, receive
+    window tracking the layer; P of a mirror at 2(h+d) (output.py:32-45, 72).
+
+    Checked at h = 40 and 20 km, where the 4 km wide layer spans several
+    Fresnel radii of the two-way path.  Towards h = 100 km (the top of the
+    reference's altitude range) it spans only about two, and the reference's
+    model -- in the FP64 plain form as in the fast form -- falls below the
+    infinite-layer formula (0.70 of it at h = 100 km)."""
     depth = 20e3
     with quiet():
         dom = {"ox": -2e3, "oy": -2e3, "oz": 0, "fs": 20 / 1.5, "nx": 300, "ny": 300}
@@ -154,11 +161,10 @@ def test_kat_subsurface_layer_gpu(built_lib):
     G = 10 ** (prm["surface_gain"] / 10)
     lam = prm["lam"]
     with simulator.Scene(prm, fac, tg) as sc:
-        for h in (100e3, 40e3):
+        for h in (40e3, 20e3):
             tr = tr_mod.linear_track(sc.params, 1)
-            tr[0, 2] = h + depth
-            tr[0, 6] = h + depth + depth - 500.0   # rx window tracks the layer (n = 1)
+            tr[0, 2] = h
+            tr[0, 6] = h + depth - 500.0           # track_Z_rxwin(sz, -d sqrt(eps2) + 500), eps2 = 1
             out = sc.simulate(tr, form="fast")
-            hh = h + depth
-            Pr = prm["power"] * G ** 2 * lam ** 2 / ((4 * np.pi) ** 2 * (2 * (hh + depth)) ** 2)
+            Pr = prm["power"] * G ** 2 * lam ** 2 / ((4 * np.pi) ** 2 * (2 * (h + depth)) ** 2)
             _check_power(out, Pr, 10.0)

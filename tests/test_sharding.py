@@ -61,4 +61,5 @@ def test_two_rank_sharding_gloo():
 def test_shard_steps_single_rank():
     import bench
     b = bench.shard_steps(2000, 8, 10, 3, 0, 1)
-    assert len(b) == 13 and b[0] == (0, 8) and b[1] == (8, 8)
+    assert len(b) == 13 and b[0] == (500, 8) and b[1] == (508, 8)
+    assert all(500 <= s and s + n <= 1500 for s, n in b)
