@@ -419,6 +419,7 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
     }
     if ((rc = build_tables(s))) return fail(rc);
     if (const char* v = getenv("RP_PAIR_VARIANT")) s->pair_variant = atoi(v) == 1 ? 1 : 0;
+    if (const char* v = getenv("RP_PAIR_CFG")) s->pair_cfg = std::max(0, std::min(3, atoi(v)));
     cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return fail(rp_cuda_fail(e, "cudaStreamCreate"));
     *out = s;
@@ -437,6 +438,7 @@ extern "C" int rp_scene_destroy(rp_scene* s) {
     free_plan(s->plan2);
     free_plan(s->planN);
     s->arena.release();
+    s->arena2.release();
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;
     return RP_OK;

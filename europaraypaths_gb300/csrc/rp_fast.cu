@@ -368,10 +368,12 @@ struct PairArgs {
     // constants
     float nr_f;
     int nr;
+    int nr1;            // nr - 1: both split bins are inside the trace when b < nr - 1
     float kb;           // n / dr
     float kt;           // n / lam
     float pik;          // pi * (pi_F * fs / lam): sinc arguments in radians
     float pik2;         // pik^2
+    float sc[8];        // sinc polynomial coefficients in t = a^2 (sinc_poly)
     float ealpha;       // -2 alpha2 log2(e)
     float eks;          // -2 ks^2 log2(e)
     double nidx, inv_dr, inv_lam;   // inv_lam: turns per metre, pi_F / (pi lam)
@@ -387,21 +389,31 @@ struct Anchor {
     float tnx, tny, tnz;  // target normal
 };
 
-// Maclaurin coefficients of sin(a)/a in powers of a^2: (-1)^k / (2k+1)!.
-__constant__ float c_sinc_coef[16] = {
-    1.0f, -1.0f / 6.0f, 1.0f / 120.0f, -1.0f / 5040.0f, 1.0f / 362880.0f, -1.0f / 39916800.0f,
-    1.0f / 6227020800.0f, -1.0f / 1307674368000.0f, 1.0f / 355687428096000.0f,
-    -1.0f / 121645100408832000.0f, 1.0f / 51090942171709440000.0f,
-    -1.0f / 25852016738884976640000.0f, 1.0f / 15511210043330985984000000.0f,
-    -1.0f / 10888869450418352160768000000.0f, 1.0f / 8841761993739701954543616000000.0f,
-    -1.0f / 8222838654177922817725562880000000.0f};
+// Hardware approximations (PTX rsqrt/rcp/ex2 .approx.ftz): single
+// special-function-unit instructions, relative error ~2^-22.
+__device__ __forceinline__ float rsqrt_a(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_a(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float ex2_a(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 
-// sin(a)/a from a^2 with NT Maclaurin terms (Horner in a^2).
-template <int NT>
-__device__ __forceinline__ float sinc_sq(float a2) {
-    float s = c_sinc_coef[NT - 1];
+// sin(a)/a as a degree-D polynomial in t = a^2 (coefficients fitted per
+// scene on [0, amax^2], see sinc_poly), Horner form.
+template <int D>
+__device__ __forceinline__ float sinc_poly_eval(const float* c, float t) {
+    float s = c[D];
 #pragma unroll
-    for (int k = NT - 2; k >= 0; --k) s = fmaf(s, a2, c_sinc_coef[k]);
+    for (int k = D - 1; k >= 0; --k) s = fmaf(s, t, c[k]);
     return s;
 }
 
@@ -424,29 +436,34 @@ __device__ __forceinline__ void pair_eval(const FacetRec& r, const Anchor& an, c
     const float dd = fmaf(an.Dx, r.a.x, fmaf(an.Dy, r.a.y, an.Dz * r.a.z));
     const float qd = fmaf(-2.f, dd, r.a.w);             // Ttd^2 - T0^2
     const float d2 = an.T0sq + qd;
-    const float rinv = rsqrtf(d2);
+    const float rinv = rsqrt_a(d2);
     const float Ttd = d2 * rinv;
-    const float dT = __fdividef(qd, Ttd + an.T0);       // Ttd - T0 without cancellation
+    const float dT = qd * rcp_a(Ttd + an.T0);           // Ttd - T0 without cancellation
     const float jx = (an.Dx - r.a.x) * rinv;
     const float jy = (an.Dy - r.a.y) * rinv;
     const float jz = (an.Dz - r.a.z) * rinv;
-    const float cT = fminf(1.f, fmaxf(-1.f, -fmaf(jx, r.b.x, fmaf(jy, r.b.y, jz * r.b.z))));
-    const float cD = fminf(1.f, fmaxf(-1.f, -fmaf(jx, an.tnx, fmaf(jy, an.tny, jz * an.tnz))));
+    float cT = -fmaf(jx, r.b.x, fmaf(jy, r.b.y, jz * r.b.z));
+    float cD = -fmaf(jx, an.tnx, fmaf(jy, an.tny, jz * an.tnz));
     const float yu = fmaf(jx, r.c.x, fmaf(jy, r.c.y, jz * r.c.z));
     const float xv = fmaf(jx, r.d.x, fmaf(jy, r.d.y, jz * r.d.z));
     const float X = xv * xv, Y = yu * yu;
     const float h2 = X + Y;
-    const float aT = fmaf(-cT, cT, 1.f);
-    const float aD = fmaf(-cD, cD, 1.f);
     float S;
     if (NT > 0) {
+        // 1 - c^2 may round a hair below 0 for |c| ~ 1: harmless in the polynomial
+        const float aT = fmaf(-cT, cT, 1.f);
+        const float aD = fmaf(-cD, cD, 1.f);
         const bool hz = !(h2 > 0.f);
-        const float k2 = A.pik2 * __frcp_rn(hz ? 1.f : h2);
+        const float k2 = A.pik2 * rcp_a(h2);
         const float xx = hz ? A.pik2 : k2 * X;
         const float yy = hz ? 0.f : k2 * Y;
-        S = sinc_sq<(NT > 0 ? NT : 1)>(aT * xx) * sinc_sq<(NT > 0 ? NT : 1)>(aT * yy) *
-            sinc_sq<(NT > 0 ? NT : 1)>(aD * xx) * sinc_sq<(NT > 0 ? NT : 1)>(aD * yy);
+        S = sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aT * xx) * sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aT * yy) *
+            sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aD * xx) * sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aD * yy);
     } else {
+        cT = fminf(1.f, fmaxf(-1.f, cT));
+        cD = fminf(1.f, fmaxf(-1.f, cD));
+        const float aT = fmaf(-cT, cT, 1.f);
+        const float aD = fmaf(-cD, cD, 1.f);
         const bool hz = !(h2 > 0.f);
         const float pT = aT * h2, pD = aD * h2;
         const float gT = (pT > 0.f) ? aT * rsqrtf(pT) : 0.f;
@@ -462,10 +479,10 @@ __device__ __forceinline__ void pair_eval(const FacetRec& r, const Anchor& an, c
         const float den = (z1 ? 1.f : a1) * (z2 ? 1.f : a2) * (z3 ? 1.f : a3) * (z4 ? 1.f : a4);
         S = __fdividef(num, den);
     }
-    float e2 = 0.f;
-    if (!A.lossless) e2 = fmaf(A.eks, cT * cT, A.ealpha * Ttd);
-    const float amp = r.d.w * fabsf(S) * rinv * exp2f(e2);
-    float tau = r.c.w + an.tau0 + A.kt * dT;
+    // attenuation and roughness (zero constants when lossless)
+    const float e2 = fmaf(A.eks, cT * cT, A.ealpha * Ttd);
+    const float amp = r.d.w * fabsf(S) * rinv * ex2_a(e2);
+    float tau = (r.c.w + an.tau0) + A.kt * dT;
     tau -= rintf(tau);
     float sn, cs;
     __sincosf(-6.28318530717958647f * tau, &sn, &cs);
@@ -499,20 +516,29 @@ __device__ __noinline__ float prism_factor(float4 ra, double cx, double cy, doub
 }
 
 // Add one phasor into the thread's window (or, outside it, directly into the
-// thread's own trace row).  Truncating bin as the reference's (short) cast.
-__device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo, int b0,
-                                        float2* win, int tid, C32* Trow, const PairArgs& A) {
-    const float xabs = xr + (float)blo;
-    if (!(xabs > -1.f && xabs < A.nr_f)) return;
-    const int b = (int)xabs;
-    const float w = xabs - (float)b;
+// thread's own trace row).  Bin and weight follow the reference's two-bin
+// split: b = (short)x (truncation), w = x - b (radar_kernels.cu:736-760).
+// floor(xr) comes from rounding xr - 1/2 with the 1.5 * 2^23 magic number
+// (an exact half rounds either way; the split is continuous there, so both
+// give the same contributions); x in (-1, 0) is truncated to bin 0 as the
+// reference does.
+__device__ __noinline__ void bin_add_edge(int b, float w, float vre, float vim, int blo, int b0,
+                                          float2* win, int tid, C32* Trow, int nr, int Wt,
+                                          unsigned int* err) {
+    if (b < 0) {
+        if (b != -1) return;
+        b = 0;              // x in (-1, 0): truncation gives bin 0 and w = x
+        w -= 1.f;
+    }
+    if (b >= nr) return;
+    const float w0 = 1.f - w;
+    const bool two = (b + 1) < nr;
     const int sl = b - blo;
-    const bool two = (b + 1) < A.nr;
-    if (sl >= 0 && sl + 1 < RP_WIN) {
+    if ((unsigned)sl < (unsigned)(RP_WIN - 1)) {
         float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
         float2 v0 = *p0;
-        v0.x = fmaf(vre, 1.f - w, v0.x);
-        v0.y = fmaf(vim, 1.f - w, v0.y);
+        v0.x = fmaf(vre, w0, v0.x);
+        v0.y = fmaf(vim, w0, v0.y);
         *p0 = v0;
         if (two) {
             float2* p1 = p0 + RP_PAIR_THREADS;
@@ -524,34 +550,59 @@ __device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo,
         return;
     }
     const int o0 = b - b0;
-    if (o0 >= 0 && o0 < A.Wt) {
+    if (o0 >= 0 && o0 < Wt) {
         C32 t0 = Trow[o0];
-        t0.x = fmaf(vre, 1.f - w, t0.x);
-        t0.y = fmaf(vim, 1.f - w, t0.y);
+        t0.x = fmaf(vre, w0, t0.x);
+        t0.y = fmaf(vim, w0, t0.y);
         Trow[o0] = t0;
     } else {
-        atomicOr(A.err, 1u);
+        atomicOr(err, 1u);
     }
     if (two) {
-        if (o0 + 1 >= 0 && o0 + 1 < A.Wt) {
+        if (o0 + 1 >= 0 && o0 + 1 < Wt) {
             C32 t1 = Trow[o0 + 1];
             t1.x = fmaf(vre, w, t1.x);
             t1.y = fmaf(vim, w, t1.y);
             Trow[o0 + 1] = t1;
         } else {
-            atomicOr(A.err, 1u);
+            atomicOr(err, 1u);
         }
     }
 }
 
-template <int NT>
-__global__ void __launch_bounds__(RP_PAIR_THREADS, 3)
+// Common case inline (both bins inside the window and the trace); the rest
+// (window spill, x < 0, the last bin) in bin_add_edge.
+__device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo, int b0,
+                                        float2* win, int tid, C32* Trow, const PairArgs& A) {
+    const float t = (xr - 0.5f) + 12582912.0f;
+    const int sl = __float_as_int(t) - 0x4B400000;
+    const float w = xr - (t - 12582912.0f);
+    const int b = blo + sl;
+    if ((unsigned)sl < (unsigned)(RP_WIN - 1) && (unsigned)b < (unsigned)A.nr1) {
+        float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
+        float2* p1 = p0 + RP_PAIR_THREADS;
+        float2 v0 = *p0, v1 = *p1;
+        const float w0 = 1.f - w;
+        v0.x = fmaf(vre, w0, v0.x);
+        v0.y = fmaf(vim, w0, v0.y);
+        v1.x = fmaf(vre, w, v1.x);
+        v1.y = fmaf(vim, w, v1.y);
+        *p0 = v0;
+        *p1 = v1;
+    } else {
+        bin_add_edge(b, w, vre, vim, blo, b0, win, tid, Trow, A.nr, A.Wt, A.err);
+    }
+}
+
+template <int NT, int ILP, int MINB>
+__global__ void __launch_bounds__(RP_PAIR_THREADS, MINB)
 k_pairs32(PairArgs A) {
     extern __shared__ __align__(128) unsigned char smem[];
     FacetRec* srec = reinterpret_cast<FacetRec*>(smem);                     // [2][RP_CHUNK]
     float2* win = reinterpret_cast<float2*>(smem + 2 * RP_CHUNK * sizeof(FacetRec));  // [RP_WIN][threads]
     __shared__ uint64_t bars[2];
     __shared__ unsigned int s_item;
+    __shared__ double s_tpos[3][RP_PAIR_THREADS];   // this thread's target position (FP64)
     const int tid = threadIdx.x;
     if (tid == 0) {
         mbar_init(&bars[0], 1);
@@ -579,13 +630,14 @@ k_pairs32(PairArgs A) {
         if (k0 >= k1) continue;
         const int q = tb * RP_PAIR_THREADS + tid;
         const bool active = q < nq;
-        double tx = 0, ty = 0, tz = 0;
         float tnx = 0, tny = 0, tnz = 1;
         int b0 = 0;
         C32* Trow = nullptr;
         if (active) {
             const int64_t ti = A.tlist[(size_t)s * A.tstride + q];
-            tx = A.TG[ti]; ty = A.TG[A.nt + ti]; tz = A.TG[2 * A.nt + ti];
+            s_tpos[0][tid] = A.TG[ti];
+            s_tpos[1][tid] = A.TG[A.nt + ti];
+            s_tpos[2][tid] = A.TG[2 * A.nt + ti];
             tnx = (float)A.TG[3 * A.nt + ti]; tny = (float)A.TG[4 * A.nt + ti];
             tnz = (float)A.TG[5 * A.nt + ti];
             b0 = A.bt0[(size_t)s * A.tstride + q];
@@ -610,7 +662,7 @@ k_pairs32(PairArgs A) {
                 tma_bulk_g2s(srec + (buf ^ 1) * RP_CHUNK, rbase + (size_t)(k + 1) * RP_CHUNK, bytes,
                              &bars[buf ^ 1]);
             }
-            const ChunkMeta m = A.meta[(size_t)s * A.mstride + k];
+            const ChunkMeta* mp = A.meta + (size_t)s * A.mstride + k;
             if (!mbar_wait(&bars[buf], phase[buf])) {
                 if (tid == 0) atomicOr(A.err + 1, 1u);
             }
@@ -618,11 +670,12 @@ k_pairs32(PairArgs A) {
             const FacetRec* R = srec + buf * RP_CHUNK;
             if (active) {
                 // FP64 anchors of this (chunk, target)
-                const double Dx = tx - m.cx, Dy = ty - m.cy, Dz = tz - m.cz;
+                const double mcx = mp->cx, mcy = mp->cy, mcz = mp->cz;
+                const double Dx = s_tpos[0][tid] - mcx, Dy = s_tpos[1][tid] - mcy, Dz = s_tpos[2][tid] - mcz;
                 const double T0 = sqrt(Dx * Dx + Dy * Dy + Dz * Dz);
                 const double xt = A.nidx * T0 * A.inv_dr;
                 const double tt = A.nidx * T0 * A.inv_lam;
-                const double lo = (double)m.xmin + A.nidx * (T0 - (double)m.R) * A.inv_dr;
+                const double lo = (double)mp->xmin + A.nidx * (T0 - (double)mp->R) * A.inv_dr;
                 const int blo = (int)floor(lo) - 1;
                 Anchor an;
                 an.Dx = (float)Dx; an.Dy = (float)Dy; an.Dz = (float)Dz;
@@ -631,9 +684,10 @@ k_pairs32(PairArgs A) {
                 an.xbase = (float)(xt - (double)blo);
                 an.tnx = tnx; an.tny = tny; an.tnz = tnz;
                 for (int w = 0; w < RP_WIN; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
-                const int cnt = m.n;
+                const int cnt = mp->n;
                 const bool prisms = (A.np > 0) && !A.lossless;
                 int jj = 0;
+                if (ILP == 2)
                 for (; jj + 1 < cnt; jj += 2) {
                     const FacetRec r0 = R[jj];
                     const FacetRec r1 = R[jj + 1];
@@ -641,21 +695,21 @@ k_pairs32(PairArgs A) {
                     pair_eval<NT>(r0, an, A, x0, re0, im0);
                     pair_eval<NT>(r1, an, A, x1, re1, im1);
                     if (prisms) {
-                        const float f0 = prism_factor(r0.a, m.cx, m.cy, m.cz, an.Dx, an.Dy, an.Dz, an.T0sq,
+                        const float f0 = prism_factor(r0.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
                                                       A.PR, A.np, A.ealpha);
-                        const float f1 = prism_factor(r1.a, m.cx, m.cy, m.cz, an.Dx, an.Dy, an.Dz, an.T0sq,
+                        const float f1 = prism_factor(r1.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
                                                       A.PR, A.np, A.ealpha);
                         re0 *= f0; im0 *= f0; re1 *= f1; im1 *= f1;
                     }
                     bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
                     bin_add(x1, re1, im1, blo, b0, win, tid, Trow, A);
                 }
-                if (jj < cnt) {
+                for (; jj < cnt; ++jj) {
                     const FacetRec r0 = R[jj];
                     float x0, re0, im0;
                     pair_eval<NT>(r0, an, A, x0, re0, im0);
                     if (prisms) {
-                        const float f0 = prism_factor(r0.a, m.cx, m.cy, m.cz, an.Dx, an.Dy, an.Dz, an.T0sq,
+                        const float f0 = prism_factor(r0.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
                                                       A.PR, A.np, A.ealpha);
                         re0 *= f0; im0 *= f0;
                     }
@@ -767,15 +821,18 @@ struct TW32 {
 };
 
 template <int KPT>
-__global__ void __launch_bounds__(RP_CONV_THREADS)
+__global__ void __launch_bounds__(RP_CONV_THREADS, 1)
 k_conv32s(ConvArgs A) {
     extern __shared__ __align__(16) unsigned char csm[];
     Cplx<float>* X = reinterpret_cast<Cplx<float>*>(csm);
     Cplx<float>* W = X + A.n2;
+    Cplx<float>* TWs = W + A.M;          // first quarter of the twiddle circle
     __shared__ unsigned int s_item;
-    const TW32 tw{A.tw};
     const int tid = threadIdx.x;
     const int nr = A.nr, n2 = A.n2, N = A.N, M = A.M;
+    #pragma unroll 8
+    for (int k = tid; k < M / 4; k += RP_CONV_THREADS) TWs[k] = A.tw[k];
+    __syncthreads();
     const unsigned int items = (unsigned)A.nb * A.nsplit;
     for (;;) {
         if (tid == 0) s_item = atomicAdd(A.work, 1u);
@@ -794,6 +851,7 @@ k_conv32s(ConvArgs A) {
         for (int i = 0; i < KPT; ++i) { accr[i] = 0.f; acci[i] = 0.f; }
         for (int q = q0; q < q1; ++q) {
             const int b0 = A.bt0[(size_t)s * A.tstride + q];
+            #pragma unroll 8
             for (int k = tid; k < n2; k += RP_CONV_THREADS) {
                 Cplx<float> v{0.f, 0.f};
                 const int o = k - b0;
@@ -807,10 +865,11 @@ k_conv32s(ConvArgs A) {
                 X[k] = v;
             }
             __syncthreads();
-            block_dif(X, n2, tw, A.log2M);
+            block_dif_u<float, 4>(X, n2, TWs, A.log2M);
+            #pragma unroll 8
             for (int k = tid; k < n2; k += RP_CONV_THREADS) W[k] = c_mul(X[k], A.C2s[k]);
             __syncthreads();
-            block_dit(W, n2, tw, A.log2M);
+            block_dit_u<float, 4>(W, n2, TWs, A.log2M);
             {   // Ptarg = W[nr/2 + k] / n2 moved to the front, zero padded
                 const float inv = 1.f / (float)n2;
                 Cplx<float> keep[KPT];
@@ -825,28 +884,33 @@ k_conv32s(ConvArgs A) {
                     const int k = tid + c * RP_CONV_THREADS;
                     if (k < nr) W[k] = Cplx<float>{keep[c].x * inv, keep[c].y * inv};
                 }
+                #pragma unroll 8
                 for (int k = nr + tid; k < n2; k += RP_CONV_THREADS) W[k] = Cplx<float>{0.f, 0.f};
                 __syncthreads();
             }
-            block_dif(W, n2, tw, A.log2M);
+            block_dif_u<float, 4>(W, n2, TWs, A.log2M);
             {
                 const float sc = A.sig_scale / (float)n2;
+                #pragma unroll 8
                 for (int k = tid; k < n2; k += RP_CONV_THREADS) {
                     Cplx<float> v = c_mul(X[k], W[k]);
                     W[k] = Cplx<float>{v.x * sc, v.y * sc};
                 }
             }
             __syncthreads();
-            block_dit(W, n2, tw, A.log2M);                 // u (natural, N values)
+            block_dit_u<float, 4>(W, n2, TWs, A.log2M);                 // u (natural, N values)
+            #pragma unroll 8
             for (int k = tid; k < M; k += RP_CONV_THREADS)
                 W[k] = (k < N) ? c_mul(W[k], A.bw[k]) : Cplx<float>{0.f, 0.f};
             __syncthreads();
-            block_dif(W, M, tw, A.log2M);
+            block_dif_u<float, 4>(W, M, TWs, A.log2M);
+            #pragma unroll 8
             for (int k = tid; k < M; k += RP_CONV_THREADS) W[k] = c_mul(W[k], A.bWs[k]);
             __syncthreads();
-            block_dit(W, M, tw, A.log2M);
+            block_dit_u<float, 4>(W, M, TWs, A.log2M);
             {
                 const float invM = 1.f / (float)M;
+                #pragma unroll 8
                 for (int k = tid; k < N; k += RP_CONV_THREADS) {
                     const int m = k < N - k ? k : N - k;
                     const bool kept = A.crop_all || m <= A.crop_K;
@@ -855,13 +919,15 @@ k_conv32s(ConvArgs A) {
                 }
             }
             __syncthreads();
+            #pragma unroll 8
             for (int k = tid; k < M; k += RP_CONV_THREADS)
                 W[k] = (k < N) ? c_mulc(X[k], A.bw[k]) : Cplx<float>{0.f, 0.f};
             __syncthreads();
-            block_dif(W, M, tw, A.log2M);
+            block_dif_u<float, 4>(W, M, TWs, A.log2M);
+            #pragma unroll 8
             for (int k = tid; k < M; k += RP_CONV_THREADS) W[k] = c_mul(W[k], A.bWis[k]);
             __syncthreads();
-            block_dit(W, M, tw, A.log2M);
+            block_dit_u<float, 4>(W, M, TWs, A.log2M);
             {
                 const float sc = 1.f / ((float)M * (float)N);
 #pragma unroll
@@ -991,6 +1057,7 @@ void fast_take_setup(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<C32>((size_t)L.nb * L.surf_slot);       // surface conv scratch
 }
 
+// 2nr + 4nr + nr complex64 = 56 nr bytes of shared memory per block (224 KiB at nr = 4096).
 bool use_smem_conv(const rp_scene* sc) { return sc->smem_conv && sc->nr <= 4096; }
 
 int64_t conv_splits(int64_t tstride) { return (tstride + RP_CONV_SPLIT - 1) / RP_CONV_SPLIT; }
@@ -1042,15 +1109,74 @@ std::vector<int> host_target_bounds32(const rp_scene* sc, const std::vector<doub
     return ub;
 }
 
-// Number of Maclaurin terms of sin(a)/a for |a| <= amax with truncation
-// error below 1e-9 (0: use the special-function unit).  variant 1 forces the
+// Pair-kernel instantiation: sinc degree x (ILP facets per step, resident
+// blocks per SM).  cfg 0: 2 x 3, 1: 2 x 2, 2: 1 x 4, 3: 1 x 3.
+template <int NT>
+void (*pick_cfg(int cfg))(PairArgs) {
+    switch (cfg) {
+        case 1: return k_pairs32<NT, 2, 2>;
+        case 2: return k_pairs32<NT, 1, 4>;
+        case 3: return k_pairs32<NT, 1, 3>;
+        default: return k_pairs32<NT, 2, 3>;
+    }
+}
+
+void (*pick_pair_kernel(int deg, int cfg))(PairArgs) {
+    switch (deg) {
+        case 4: return pick_cfg<4>(cfg);
+        case 5: return pick_cfg<5>(cfg);
+        case 6: return pick_cfg<6>(cfg);
+        default: return pick_cfg<0>(cfg);
+    }
+}
+
+// Degree of the polynomial in t = a^2 that approximates sin(a)/a to ~1e-7
+// for |a| <= amax (0: use the special-function unit).  variant 1 forces the
 // special-function path.
-int sinc_terms(double amax, int variant) {
+int sinc_degree(double amax, int variant) {
     if (variant == 1) return 0;
-    if (amax <= 2.0) return 7;
-    if (amax <= 3.2) return 10;
-    if (amax <= 4.6) return 13;
+    if (amax <= 2.0) return 4;
+    if (amax <= 3.2) return 5;
+    if (amax <= 5.0) return 6;
     return 0;
+}
+
+// Chebyshev projection of s(t) = sin(sqrt t)/sqrt t on [0, T] (64 nodes,
+// degree D), converted to monomial coefficients in t: near-minimax, own
+// construction from the Chebyshev expansion of a smooth function.
+void sinc_poly(double T, int D, double* mono) {
+    const int N = 64;
+    double c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < N; ++k) {
+        const double th = RP_PI * (k + 0.5) / N;
+        const double u = std::cos(th);
+        const double t = 0.5 * T * (u + 1.0);
+        const double a = std::sqrt(t);
+        const double f = (a > 1e-12) ? std::sin(a) / a : 1.0;
+        for (int j = 0; j <= D; ++j) c[j] += f * std::cos(j * th);
+    }
+    for (int j = 0; j <= D; ++j) c[j] *= 2.0 / N;
+    c[0] *= 0.5;
+    // sum_j c_j T_j(u) -> monomials in u (T_{j+1} = 2u T_j - T_{j-1})
+    double Tm[8][8] = {};
+    Tm[0][0] = 1.0;
+    if (D >= 1) Tm[1][1] = 1.0;
+    for (int j = 2; j <= D; ++j)
+        for (int i = 0; i <= j; ++i) Tm[j][i] = (i ? 2.0 * Tm[j - 1][i - 1] : 0.0) - Tm[j - 2][i];
+    double pu[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int j = 0; j <= D; ++j)
+        for (int i = 0; i <= j; ++i) pu[i] += c[j] * Tm[j][i];
+    // u = 2t/T - 1 = alpha t + beta -> monomials in t (binomial expansion)
+    const double al = 2.0 / T, be = -1.0;
+    for (int i = 0; i < 8; ++i) mono[i] = 0.0;
+    for (int i = 0; i <= D; ++i) {
+        double binom = 1.0;
+        for (int k = 0; k <= i; ++k) {
+            // C(i,k) al^k be^(i-k)
+            mono[k] += pu[i] * binom * std::pow(al, k) * std::pow(be, i - k);
+            binom = binom * (i - k) / (k + 1);
+        }
+    }
 }
 
 template <int KPT>
@@ -1099,10 +1225,12 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
     PlanV<float> p2 = plan_view32(sc->plan2), pN = plan_view32(sc->planN);
     const DevParams& dp = sc->dp;
     const size_t pair_smem = 2 * RP_CHUNK * sizeof(FacetRec) + (size_t)RP_WIN * RP_PAIR_THREADS * sizeof(float2);
-    // sinc evaluation: Maclaurin terms needed for |a| <= pik (0 = special-function unit)
-    const int nt_terms = sinc_terms(RP_PI * (RP_PI_F * dp.fs / dp.lam), sc->pair_variant);
-    void (*pk)(PairArgs) = nt_terms == 7 ? k_pairs32<7> : nt_terms == 10 ? k_pairs32<10>
-                         : nt_terms == 13 ? k_pairs32<13> : k_pairs32<0>;
+    // sinc evaluation: polynomial degree for |a| <= pik (0 = special-function unit)
+    const double pik_d = RP_PI * (RP_PI_F * dp.fs / dp.lam);
+    const int deg = sinc_degree(pik_d, sc->pair_variant);
+    double coef[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (deg > 0) sinc_poly(pik_d * pik_d, deg, coef);
+    void (*pk)(PairArgs) = pick_pair_kernel(deg, sc->pair_cfg);
     RP_CUDA(cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem));
     int occ = 0;
     RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, RP_PAIR_THREADS, pair_smem));
@@ -1122,12 +1250,10 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
             ++nb;
             if (nb >= 64) break;
         }
-        // reserve for the worst window (Wt = nr) so no reallocation is needed
         FastLayout Lw = fast_layout(sc, nb, tmax, nr);
         {
             ArenaPlan a;
             fast_take_setup(a, sc, Lw);
-            fast_take_pairs(a, sc, Lw);
             int rc = sc->arena.reserve(a.off);
             if (rc) return rc;
         }
@@ -1197,17 +1323,25 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
         g_timer.collect(0, 1);
         const int Wt = std::max(1, std::min(nr, (h_maxw + 3) & ~3));
         FastLayout L = fast_layout(sc, nb, tmax, Wt);
+        {
+            ArenaPlan a2;
+            fast_take_pairs(a2, sc, L);
+            int rc = sc->arena2.reserve(a2.off);
+            if (rc) return rc;
+        }
+        Arena& b = sc->arena2;
+        b.reset();
         const bool smem_conv = use_smem_conv(sc);
         const int nsplit = (int)conv_splits(L.tstride);
-        C32* T = a.take<C32>((size_t)RP_PARTS * nb * L.tstride * Wt);
+        C32* T = b.take<C32>((size_t)RP_PARTS * nb * L.tstride * Wt);
         C32* Z = nullptr;
         C32* cscr = nullptr;
         C32* part = nullptr;
         if (smem_conv) {
-            part = a.take<C32>((size_t)nb * nsplit * nr);
+            part = b.take<C32>((size_t)nb * nsplit * nr);
         } else {
-            Z = a.take<C32>((size_t)nb * L.tstride * nr);
-            cscr = a.take<C32>((size_t)L.slots * L.slot);
+            Z = b.take<C32>((size_t)nb * L.tstride * nr);
+            cscr = b.take<C32>((size_t)L.slots * L.slot);
         }
         RP_CUDA(cudaMemsetAsync(T, 0, sizeof(C32) * RP_PARTS * nb * L.tstride * Wt, st));
         g_timer.mark(1, st);
@@ -1220,13 +1354,14 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
             P.tblocks = (int)((L.tstride + RP_PAIR_THREADS - 1) / RP_PAIR_THREADS);
             P.work = reinterpret_cast<unsigned int*>(misc + 1);
             P.err = reinterpret_cast<unsigned int*>(misc + 2);
-            P.nr_f = (float)nr; P.nr = nr;
+            P.nr_f = (float)nr; P.nr = nr; P.nr1 = nr - 1;
             P.kb = (float)(dp.nidx / dp.dr);
             P.kt = (float)(dp.nidx * dp.turn);
             P.pik = (float)(RP_PI * (RP_PI_F * dp.fs / dp.lam));
             P.pik2 = P.pik * P.pik;
-            P.ealpha = (float)(-2.0 * dp.alpha2 * 1.4426950408889634);
-            P.eks = (float)(-2.0 * dp.ks * dp.ks * 1.4426950408889634);
+            for (int k = 0; k < 8; ++k) P.sc[k] = (float)coef[k];
+            P.ealpha = dp.lossless ? 0.f : (float)(-2.0 * dp.alpha2 * 1.4426950408889634);
+            P.eks = dp.lossless ? 0.f : (float)(-2.0 * dp.ks * dp.ks * 1.4426950408889634);
             P.nidx = dp.nidx; P.inv_dr = 1.0 / dp.dr; P.inv_lam = dp.turn;
             P.lossless = dp.lossless;
             int grid = std::min(occ * sc->sm_count, nb * P.tblocks * RP_PARTS);
@@ -1244,7 +1379,7 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
                 C.nr = nr; C.n2 = 2 * nr; C.N = 2 * nr - 1; C.M = sc->mS;
                 C.crop_K = sc->crop_K; C.crop_all = sc->crop_all; C.sig_scale = sig_scale;
                 C.part = part; C.nsplit = nsplit; C.work = reinterpret_cast<unsigned int*>(misc + 4);
-                const size_t csm = (size_t)(C.n2 + C.M) * sizeof(Cplx<float>);
+                const size_t csm = (size_t)(C.n2 + C.M + C.M / 4) * sizeof(Cplx<float>);
                 int rc2 = launch_conv32s(C, csm, sc->sm_count, nb * nsplit, st);
                 if (rc2) return rc2;
             } else {

@@ -163,4 +163,122 @@ __device__ void block_dit(Cplx<T>* a, int n, const TW& tw, int log2M) {
         __syncthreads();
     }
 }
+
+// Shared-memory variants for the hot range-compression kernel: twiddles come
+// from a shared table of M/4 entries (every index j * (M/L) used above is
+// below M/4 because j < L/4 in radix-4 stages and j = 0 in the radix-2
+// stage), and each thread first loads the inputs of U butterflies, then
+// computes and stores them, so the loads of a stage overlap.
+template <class T>
+struct SmemTw {
+    const Cplx<T>* t;
+    __device__ __forceinline__ Cplx<T> operator()(int k) const { return t[k]; }
+};
+
+template <class T, int U>
+__device__ __noinline__ void block_dif_u(Cplx<T>* a, int n, const Cplx<T>* tws, int log2M) {
+    const SmemTw<T> tw{tws};
+    const int m = fft_log2(n);
+    const int nb = n >> 2;
+    int L = n, lL = m;
+    for (; L >= 4; L >>= 2, lL -= 2) {
+        const int q4 = L >> 2, lq = lL - 2, msh = log2M - lL;
+        for (int t0 = threadIdx.x; t0 < nb; t0 += blockDim.x * U) {
+            Cplx<T> x[U][4];
+            int bb[U], jj[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int t = t0 + u * blockDim.x;
+                const int j = t & (q4 - 1);
+                jj[u] = j;
+                bb[u] = (t >> lq) * L + j;
+                if (t < nb) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) x[u][q] = a[bb[u] + q * q4];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int t = t0 + u * blockDim.x;
+                if (t >= nb) continue;
+                Cplx<T> t0c = c_add(x[u][0], x[u][2]), t1 = c_sub(x[u][0], x[u][2]);
+                Cplx<T> t2 = c_add(x[u][1], x[u][3]), t3 = c_sub(x[u][1], x[u][3]);
+                Cplx<T> y1 = Cplx<T>{t1.x + t3.y, t1.y - t3.x};
+                Cplx<T> y3 = Cplx<T>{t1.x - t3.y, t1.y + t3.x};
+                const int b = bb[u];
+                a[b] = c_add(t0c, t2);
+                Cplx<T> y2 = c_sub(t0c, t2);
+                if (jj[u] == 0) {
+                    a[b + q4] = y1; a[b + 2 * q4] = y2; a[b + 3 * q4] = y3;
+                } else {
+                    Cplx<T> w1 = tw(jj[u] << msh);
+                    Cplx<T> w2 = c_mul(w1, w1);
+                    Cplx<T> w3 = c_mul(w1, w2);
+                    a[b + q4] = c_mul(y1, w1);
+                    a[b + 2 * q4] = c_mul(y2, w2);
+                    a[b + 3 * q4] = c_mul(y3, w3);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (L == 2) {
+        for (int t = threadIdx.x; t < n / 2; t += blockDim.x) dif2(a, 2, 0, t, tw, log2M - 1);
+        __syncthreads();
+    }
+}
+
+template <class T, int U>
+__device__ __noinline__ void block_dit_u(Cplx<T>* a, int n, const Cplx<T>* tws, int log2M) {
+    const SmemTw<T> tw{tws};
+    const int m = fft_log2(n);
+    const int nb = n >> 2;
+    int L, lL;
+    if (m & 1) {
+        for (int t = threadIdx.x; t < n / 2; t += blockDim.x) dit2(a, 2, 0, t, tw, log2M - 1);
+        __syncthreads();
+        L = 8; lL = 3;
+    } else {
+        L = 4; lL = 2;
+    }
+    for (; L <= n; L <<= 2, lL += 2) {
+        const int q4 = L >> 2, lq = lL - 2, msh = log2M - lL;
+        for (int t0 = threadIdx.x; t0 < nb; t0 += blockDim.x * U) {
+            Cplx<T> x[U][4];
+            int bb[U], jj[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int t = t0 + u * blockDim.x;
+                const int j = t & (q4 - 1);
+                jj[u] = j;
+                bb[u] = (t >> lq) * L + j;
+                if (t < nb) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) x[u][q] = a[bb[u] + q * q4];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int t = t0 + u * blockDim.x;
+                if (t >= nb) continue;
+                Cplx<T> x1 = x[u][1], x2 = x[u][2], x3 = x[u][3];
+                if (jj[u] != 0) {
+                    Cplx<T> w1 = tw(jj[u] << msh);
+                    Cplx<T> w2 = c_mul(w1, w1);
+                    Cplx<T> w3 = c_mul(w1, w2);
+                    x1 = c_mulc(x1, w1);
+                    x2 = c_mulc(x2, w2);
+                    x3 = c_mulc(x3, w3);
+                }
+                Cplx<T> t0c = c_add(x[u][0], x2), t1 = c_sub(x[u][0], x2), t2 = c_add(x1, x3), t3 = c_sub(x1, x3);
+                const int b = bb[u];
+                a[b] = c_add(t0c, t2);
+                a[b + 2 * q4] = c_sub(t0c, t2);
+                a[b + q4] = Cplx<T>{t1.x - t3.y, t1.y + t3.x};
+                a[b + 3 * q4] = Cplx<T>{t1.x + t3.y, t1.y - t3.x};
+            }
+        }
+        __syncthreads();
+    }
+}
 #endif

@@ -110,8 +110,11 @@ struct rp_scene {
     float* d_bWiS = nullptr;             // DIF_M(Bluestein chirp)
     // ---- tuning
     int pair_variant = 0;                // 0 auto (polynomial sinc where accurate), 1 special-function sinc
-    // ---- scratch
+    int pair_cfg = 0;                    // pair-kernel (ILP, blocks/SM) configuration
+    // ---- scratch: per-call setup buffers, and the pair-stage buffers sized
+    // once the real target-window width is known
     Arena arena;
+    Arena arena2;
     cudaStream_t own_stream = nullptr;
     int sm_count = 0;
     size_t store_bytes = 0;
