@@ -297,18 +297,29 @@ def main():
         sm_mhz = clocks.get("sm_mhz") or peaks.get("clocks_under_load", {}).get("sm_mhz_median") or 1455.0
         n_sm = torch.cuda.get_device_properties(local).multi_processor_count
         pairs_s = stage["pairs_ms"] / 1e3
-        mufu_rate = opcount.MUFU_PER_EVAL * my_evals / pairs_s if pairs_s > 0 else 0.0
-        mufu_peak = opcount.MUFU_PER_CLK_PER_SM * n_sm * sm_mhz * 1e6
-        roof = {"bound": "sfu", "kernel": "k_pairs32",
-                "achieved": mufu_rate / 1e12, "peak": mufu_peak / 1e12, "unit": "Tmufu/s",
-                "frac": mufu_rate / mufu_peak if mufu_peak else None,
-                "traffic": None,
-                "peak_source": (f"nominal {opcount.MUFU_PER_CLK_PER_SM} MUFU results/clk/SM x {n_sm} SMs x "
-                                f"{sm_mhz:.0f} MHz median SM clock under load (not in MEASURED_PEAKS.json, "
-                                "which holds HBM and bf16 only)"),
-                "ops_per_eval": opcount.MUFU_PER_EVAL,
+        evals_rate = my_evals / pairs_s if pairs_s > 0 else 0.0
+        clk = sm_mhz * 1e6
+        fp32_peak = opcount.FP32_FMA_PER_CLK_PER_SM * n_sm * clk
+        mufu_peak = opcount.MUFU_PER_CLK_PER_SM * n_sm * clk
+        fp32_rate = opcount.FP32_OPS_PER_EVAL * evals_rate
+        mufu_rate = opcount.MUFU_PER_EVAL * evals_rate
+        roof = {"bound": "fp32", "kernel": "k_pairs32",
+                "achieved": fp32_rate / 1e12, "peak": fp32_peak / 1e12,
+                "unit": "T FP32-pipe instructions/s",
+                "frac": fp32_rate / fp32_peak if fp32_peak else None,
+                # DRAM read+write of one launch from the committed ncu capture (4 traces: 753 + 140 MB),
+                # scaled by the traces per launch; the kernel is compute-bound (DRAM < 0.1 % of peak)
+                "traffic": 893e6 * tps / 4.0,
+                "traffic_unit": "bytes per launch (ncu, profiles/k_pairs32_large_scene.md, scaled)",
+                "peak_source": (f"nominal {opcount.FP32_FMA_PER_CLK_PER_SM} FP32 lanes/clk/SM x {n_sm} SMs x "
+                                f"{sm_mhz:.0f} MHz median SM clock under load; MEASURED_PEAKS.json holds HBM "
+                                "and bf16 tensor peaks only, and this kernel uses neither"),
+                "ops_per_eval": opcount.FP32_OPS_PER_EVAL,
+                "sfu": {"achieved": mufu_rate / 1e12, "peak": mufu_peak / 1e12, "unit": "T MUFU/s",
+                        "frac": mufu_rate / mufu_peak if mufu_peak else None,
+                        "ops_per_eval": opcount.MUFU_PER_EVAL},
                 "pair_kernel_ms_per_launch": stage["pairs_ms"] / max(stage["pair_launches"], 1),
-                "pair_evals_per_s": my_evals / pairs_s if pairs_s > 0 else None,
+                "pair_evals_per_s": evals_rate,
                 "pair_evals_per_launch": my_evals / max(stage["pair_launches"], 1),
                 "mean_counts_per_trace": [float(timed_counts[:, 0].mean()), float(timed_counts[:, 1].mean())],
                 "stage_ms": {k: stage[k] for k in ("setup_ms", "pairs_ms", "compress_ms", "tail_ms")},

@@ -110,7 +110,7 @@ struct rp_scene {
     float* d_bWiS = nullptr;             // DIF_M(Bluestein chirp)
     // ---- tuning
     int pair_variant = 0;                // 0 auto (polynomial sinc where accurate), 1 special-function sinc
-    int pair_cfg = 0;                    // pair-kernel (ILP, blocks/SM) configuration
+    int pair_cfg = 1;                    // pair-kernel (ILP, blocks/SM) configuration (1: 2 x 2)
     // ---- scratch: per-call setup buffers, and the pair-stage buffers sized
     // once the real target-window width is known
     Arena arena;

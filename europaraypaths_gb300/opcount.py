@@ -10,14 +10,20 @@ The fused FP32 kernel (csrc/rp_fast.cu, k_pairs32) evaluates one
 the inbound one times -1/sqrt(P) in the non-specular mode; so one k_pairs32
 evaluation covers two metric pairs.
 
-MUFU (special-function unit) instructions per k_pairs32 evaluation, read off
-the source (pair_eval): rsqrt (1/Ttd), the fast division for dT (1), two
-rsqrt for the azimuth/inclination projections (2), four sin for the sinc
-factors (4), one reciprocal shared by the four sinc quotients (1), exp2 (1)
-and sin + cos of the phase (2).
+Counts per k_pairs32 evaluation with the polynomial sinc (degree 4, the
+large-scene case), read off the source (pair_eval, bin_add fast path):
+
+* FP32 FMA-pipe instructions (FADD/FMUL/FFMA): 82 -- 3+1+1 distance, 1 Ttd,
+  2 dT, 6 direction, 3+3 cosines, 6 tangent projections, 3 h^2, 2 (1 - c^2),
+  3 squared sinc arguments scale, 4 arguments, 16 polynomials (4 x 4), 3 sinc
+  product, 3 exponent, 3 amplitude, 3 phase turns, 1 phase scale, 2 phasor,
+  2 bin coordinate, 11 bin split and window update.
+* MUFU (special-function) instructions: 6 -- rsqrt (1/Ttd), rcp (dT), rcp
+  (1/h^2), ex2, sin and cos of the phase.
 """
 
-MUFU_PER_EVAL = 12
+FP32_OPS_PER_EVAL = 82
+MUFU_PER_EVAL = 6
 EVALS_PER_TARGET_PAIR_METRIC = 0.5     # one evaluation covers two metric pairs
 
 # Nominal special-function throughput of a Blackwell SM (results per clock).
