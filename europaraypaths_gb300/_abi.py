@@ -78,6 +78,17 @@ _SIGS = {
     "rp_last_timing": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rp_surface_noalloc": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                             ctypes.c_void_p], ctypes.c_int),
+    "rp_count_records": ([ctypes.c_char_p, ctypes.c_void_p], ctypes.c_int),
+    "rp_read_facets": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
+    "rp_read_targets": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
+    "rp_read_sources": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
+    "rp_read_gains": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
+    "rp_read_rx_window": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
+    "rp_read_prisms": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p],
+                       ctypes.c_int),
+    "rp_write_trace": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
+    "rp_check_directory": ([ctypes.c_char_p], ctypes.c_int),
+    "rp_clear_traces": ([ctypes.c_char_p, ctypes.c_void_p], ctypes.c_int),
 }
 
 

@@ -167,6 +167,49 @@ int rp_set_timing(int enable);
  *   number of pair-kernel launches. */
 int rp_last_timing(double* ms, int n);
 
+/* ---- the reference's text formats (host only; see rp_io.cu) ---- */
+
+/* Non-blank lines of a text file.  Replaces count_lines,
+ * src/CUDA/file_io.cu:314-335. */
+int rp_count_records(const char* path, int64_t* n);
+
+/* Facet file "x,y,z:nx,ny,nz:ux,uy,uz:vx,vy,vz" -> double[12][cap].
+ * Replaces loadFacetFile, src/CUDA/file_io.cu:337-362. */
+int rp_read_facets(const char* path, double* soa, int64_t cap, int64_t* n);
+
+/* Target file, 3/4/6/7 columns (default normal +z, ttype 0) -> double[7][cap].
+ * Replaces loadTargetFile, src/CUDA/file_io.cu:365-426. */
+int rp_read_targets(const char* path, double* soa, int64_t cap, int64_t* n);
+
+/* Source-path file, 3 or 6 columns -> rows x,y,z,nx,ny,nz.
+ * Replaces loadSourceFile, src/CUDA/file_io.cu:429-474. */
+int rp_read_sources(const char* path, double* rows, int64_t cap, int64_t* n);
+
+/* Gain-pattern file "surface_dB,subsurface_dB" per line -> rows of 2.
+ * Replaces loadGainFile, src/CUDA/file_io.cu:597-624. */
+int rp_read_gains(const char* path, double* rows, int64_t cap, int64_t* n);
+
+/* Receive-window starts, exactly ns lines.  Replaces
+ * loadRxWindowPositions, src/CUDA/file_io.cu:520-551 (RP_ERR_PARSE instead
+ * of exit()). */
+int rp_read_rx_window(const char* path, double* out, int64_t ns);
+
+/* Attenuation prisms "sigma,xmin,ymin,zmin,xmax,ymax,zmax" -> double[7][cap]
+ * with alpha in row 0.  Replaces loadAttenPrismFile, file_io.cu:477-517. */
+int rp_read_prisms(const char* path, const rp_params* p, double* soa, int64_t cap, int64_t* n);
+
+/* Write one trace as "%e %e\n" per bin (re_im: nr complex64 values).
+ * Replaces saveSignalToFile, src/CUDA/file_io.cu:284-296. */
+int rp_write_trace(const char* path, const float* re_im, int64_t nr);
+
+/* The output directory must exist.  Replaces checkDirectoryExists,
+ * src/CUDA/file_io.cu:266-281. */
+int rp_check_directory(const char* path);
+
+/* Remove s*.txt from dir.  Replaces remove_s_txt_files,
+ * src/CUDA/file_io.cu:554-593. */
+int rp_clear_traces(const char* dir, int64_t* removed);
+
 /*
  * Surface-only radargram columns with no device allocation at call time.
  * No counterpart in the reference.  For callers that may not allocate
