@@ -78,6 +78,11 @@ _SIGS = {
     "rp_last_timing": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rp_surface_noalloc": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                             ctypes.c_void_p], ctypes.c_int),
+    "rp_workspace_create": ([ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
+    "rp_workspace_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "rp_workspace_bytes": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rp_simulate_ws": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
+                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rp_count_records": ([ctypes.c_char_p, ctypes.c_void_p], ctypes.c_int),
     "rp_read_facets": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
     "rp_read_targets": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),

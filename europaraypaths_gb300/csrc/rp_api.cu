@@ -437,8 +437,8 @@ extern "C" int rp_scene_destroy(rp_scene* s) {
         if (q) cudaFree(q);
     free_plan(s->plan2);
     free_plan(s->planN);
-    s->arena.release();
-    s->arena2.release();
+    s->ws.arena.release();
+    s->ws.arena2.release();
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;
     return RP_OK;
@@ -459,12 +459,12 @@ extern "C" int rp_query_footprint(const rp_scene* s, int64_t ns, int form, int64
     return RP_OK;
 }
 
-static int run_form(rp_scene* s, const double* d_traces, int64_t ns, int form, void* d_out,
-                    int64_t* counts, cudaStream_t st) {
+static int run_form(rp_scene* s, rp_workspace* ws, const double* d_traces, int64_t ns, int form,
+                    void* d_out, int64_t* counts, cudaStream_t st) {
     int f = form & 0xff;
     int out64 = (form & RP_OUT_COMPLEX128) ? 1 : 0;
-    if (f == RP_FORM_PLAIN_F64) return rp_plain_run(s, d_traces, ns, d_out, out64, counts, st);
-    if (f == RP_FORM_FAST_F32) return rp_fast_run(s, d_traces, ns, d_out, out64, counts, st);
+    if (f == RP_FORM_PLAIN_F64) return rp_plain_run(s, ws, d_traces, ns, d_out, out64, counts, st);
+    if (f == RP_FORM_FAST_F32) return rp_fast_run(s, ws, d_traces, ns, d_out, out64, counts, st);
     rp_set_error("unknown form %d", form);
     return RP_ERR_ARG;
 }
@@ -480,7 +480,44 @@ extern "C" int rp_simulate_device(rp_scene* s, const double* d_traces, int64_t n
     RP_CUDA(cudaSetDevice(s->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : s->own_stream;
     if (ns == 0) return RP_OK;
-    return run_form(s, d_traces, ns, form, d_out, counts, st);
+    return run_form(s, &s->ws, d_traces, ns, form, d_out, counts, st);
+}
+
+extern "C" int rp_workspace_create(int device, rp_workspace** out) {
+    if (!out) { rp_set_error("rp_workspace_create: null argument"); return RP_ERR_ARG; }
+    *out = new rp_workspace();
+    (*out)->device = device;
+    return RP_OK;
+}
+
+extern "C" int rp_workspace_destroy(rp_workspace* ws) {
+    if (!ws) return RP_OK;
+    cudaSetDevice(ws->device);
+    cudaDeviceSynchronize();
+    ws->arena.release();
+    ws->arena2.release();
+    delete ws;
+    return RP_OK;
+}
+
+extern "C" int rp_workspace_bytes(const rp_workspace* ws, int64_t* bytes) {
+    if (!ws || !bytes) { rp_set_error("rp_workspace_bytes: null argument"); return RP_ERR_ARG; }
+    *bytes = (int64_t)(ws->arena.cap + ws->arena2.cap);
+    return RP_OK;
+}
+
+extern "C" int rp_simulate_ws(rp_scene* s, rp_workspace* ws, const double* d_traces, int64_t ns, int form,
+                              void* d_out, int64_t* counts, void* stream) {
+    if (!s || !ws || ns < 0 || (ns > 0 && (!d_traces || !d_out)) || ws->device != s->device) {
+        rp_set_error("rp_simulate_ws: bad argument (scene and workspace must share a device)");
+        return RP_ERR_ARG;
+    }
+    g_launches = 0;
+    g_timer.reset();
+    RP_CUDA(cudaSetDevice(s->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->own_stream;
+    if (ns == 0) return RP_OK;
+    return run_form(s, ws, d_traces, ns, form, d_out, counts, st);
 }
 
 extern "C" int rp_simulate(rp_scene* s, const double* traces, int64_t ns, int form, void* out,
@@ -506,7 +543,7 @@ extern "C" int rp_simulate(rp_scene* s, const double* traces, int64_t ns, int fo
     int rc = RP_OK;
     cudaError_t e = cudaMemcpyAsync(d_tr, traces, sizeof(double) * 9 * ns, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) rc = rp_cuda_fail(e, "cudaMemcpyAsync(traces)");
-    if (rc == RP_OK) rc = run_form(s, d_tr, ns, form, d_out, counts, st);
+    if (rc == RP_OK) rc = run_form(s, &s->ws, d_tr, ns, form, d_out, counts, st);
     if (rc == RP_OK && !out_on_device) {
         e = cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, st);
         if (e != cudaSuccess) rc = rp_cuda_fail(e, "cudaMemcpyAsync(out)");

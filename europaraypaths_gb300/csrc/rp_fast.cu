@@ -1208,7 +1208,7 @@ size_t rp_fast_scratch(const rp_scene* sc, int64_t ns) {
     return a.off;
 }
 
-int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, int out64,
+int rp_fast_run(rp_scene* sc, rp_workspace* ws, const double* d_traces, int64_t ns, void* d_out, int out64,
                 int64_t* h_counts, cudaStream_t st) {
     const int64_t nf = sc->nf, nt = sc->nt;
     const int nr = sc->nr;
@@ -1254,10 +1254,10 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
         {
             ArenaPlan a;
             fast_take_setup(a, sc, Lw);
-            int rc = sc->arena.reserve(a.off);
+            int rc = ws->arena.reserve(a.off);
             if (rc) return rc;
         }
-        Arena& a = sc->arena;
+        Arena& a = ws->arena;
         a.reset();
         const int64_t nfa = std::max<int64_t>(nf, 1), nta = std::max<int64_t>(nt, 1);
         const int tiles = (int)((std::max(nfa, nta) + RP_TILE - 1) / RP_TILE);
@@ -1326,10 +1326,10 @@ int rp_fast_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, i
         {
             ArenaPlan a2;
             fast_take_pairs(a2, sc, L);
-            int rc = sc->arena2.reserve(a2.off);
+            int rc = ws->arena2.reserve(a2.off);
             if (rc) return rc;
         }
-        Arena& b = sc->arena2;
+        Arena& b = ws->arena2;
         b.reset();
         const bool smem_conv = use_smem_conv(sc);
         const int nsplit = (int)conv_splits(L.tstride);

@@ -76,6 +76,14 @@ struct DftPlan {
     int M() const { return 1 << log2M; }
 };
 
+// Per-call scratch of one stream of work: scenes are shared and read-only
+// during a simulation; everything a call writes lives here.
+struct rp_workspace {
+    int device = 0;
+    Arena arena;     // setup buffers
+    Arena arena2;    // pair-stage buffers, sized once the target-window width is known
+};
+
 struct rp_scene {
     rp_params p;
     DevParams dp;
@@ -111,10 +119,8 @@ struct rp_scene {
     // ---- tuning
     int pair_variant = 0;                // 0 auto (polynomial sinc where accurate), 1 special-function sinc
     int pair_cfg = 1;                    // pair-kernel (ILP, blocks/SM) configuration (1: 2 x 2)
-    // ---- scratch: per-call setup buffers, and the pair-stage buffers sized
-    // once the real target-window width is known
-    Arena arena;
-    Arena arena2;
+    // ---- the scene's own workspace (rp_simulate / rp_simulate_device)
+    rp_workspace ws;
     cudaStream_t own_stream = nullptr;
     int sm_count = 0;
     size_t store_bytes = 0;
@@ -144,9 +150,9 @@ struct StageTimer {
 extern thread_local StageTimer g_timer;
 
 // Entry points of the two forms (rp_plain.cu, rp_fast.cu).
-int rp_plain_run(rp_scene* s, const double* d_traces, int64_t ns, void* d_out, int out64,
-                 int64_t* h_counts, cudaStream_t st);
-int rp_fast_run(rp_scene* s, const double* d_traces, int64_t ns, void* d_out, int out64,
-                int64_t* h_counts, cudaStream_t st);
+int rp_plain_run(rp_scene* s, rp_workspace* ws, const double* d_traces, int64_t ns, void* d_out,
+                 int out64, int64_t* h_counts, cudaStream_t st);
+int rp_fast_run(rp_scene* s, rp_workspace* ws, const double* d_traces, int64_t ns, void* d_out,
+                int out64, int64_t* h_counts, cudaStream_t st);
 size_t rp_plain_scratch(const rp_scene* s, int64_t ns);
 size_t rp_fast_scratch(const rp_scene* s, int64_t ns);

@@ -337,7 +337,7 @@ size_t rp_plain_scratch(const rp_scene* sc, int64_t ns) {
     return a.off;
 }
 
-int rp_plain_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, int out64,
+int rp_plain_run(rp_scene* sc, rp_workspace* ws, const double* d_traces, int64_t ns, void* d_out, int out64,
                  int64_t* h_counts, cudaStream_t st) {
     const int64_t nf = sc->nf, nt = sc->nt, np = sc->np;
     const int nr = sc->nr;
@@ -368,9 +368,9 @@ int rp_plain_run(rp_scene* sc, const double* d_traces, int64_t ns, void* d_out, 
         PlainLayout L = plain_layout(sc, nb, tmax);
         ArenaPlan plan;
         plain_take(plan, sc, L);
-        int rc = sc->arena.reserve(plan.off);
+        int rc = ws->arena.reserve(plan.off);
         if (rc) return rc;
-        Arena& a = sc->arena;
+        Arena& a = ws->arena;
         a.reset();
         const int64_t nfa = std::max<int64_t>(nf, 1), nta = std::max<int64_t>(nt, 1);
         const int tiles = (int)((std::max(nfa, nta) + RP_TILE - 1) / RP_TILE);

@@ -153,6 +153,24 @@ int rp_simulate(rp_scene* s, const double* traces, int64_t ns, int form,
 int rp_simulate_device(rp_scene* s, const double* d_traces, int64_t ns, int form,
                        void* d_out, int64_t* counts, void* stream);
 
+/* Opaque per-stream scratch.  A scene is read-only while it simulates, so
+ * several workspaces (one per concurrent stream or host thread) can run the
+ * same resident scene at once; rp_simulate / rp_simulate_device use the
+ * scene's own workspace.  New: the reference runs one trace loop at a time
+ * (src/CUDA/sim.cu:615). */
+typedef struct rp_workspace rp_workspace;
+
+int rp_workspace_create(int device, rp_workspace** out);
+int rp_workspace_destroy(rp_workspace* ws);
+
+/* Device bytes currently held by the workspace's scratch. */
+int rp_workspace_bytes(const rp_workspace* ws, int64_t* bytes);
+
+/* rp_simulate_device with an explicit workspace (trace table and output in
+ * device memory).  Calls sharing a workspace must be ordered on one stream. */
+int rp_simulate_ws(rp_scene* s, rp_workspace* ws, const double* d_traces, int64_t ns, int form,
+                   void* d_out, int64_t* counts, void* stream);
+
 /* Number of kernel launches issued by this thread's last rp_simulate*. */
 int rp_last_launch_count(int64_t* launches);
 
