@@ -151,6 +151,118 @@ def cpu_baseline(sc, scene, track, max_targets, trace_index):
                       f"targets: {p} pairs in {dt:.2f} s (FP64 C++ oracle, OpenMP over targets)"}
 
 
+def batch_workload(args, device):
+    """The uneven-scenes workload: resident scenes and, per step, a few
+    interior traces of every scene (the traces of one step are consecutive)."""
+    from europaraypaths_gb300 import scenes, simulator, traces
+    t0 = time.perf_counter()
+    specs = scenes.uneven_batch(n_scenes=args.batch_scenes)
+    objs = [simulator.Scene(s["params"], s["facets"], s["targets"], device=device) for s in specs]
+    tracks = [traces.linear_track(o.params) for o in objs]
+    return specs, objs, tracks, time.perf_counter() - t0
+
+
+def run_batch(args, objs, tracks, stream):
+    """Pairs/s of one rp_simulate_batch call over every scene (the pair stage
+    of all scenes in one persistent launch) vs the same traces scene by scene
+    (rp_simulate_ws per scene on one stream)."""
+    import ctypes
+    import torch
+    from europaraypaths_gb300 import _abi, opcount, simulator
+    K = args.batch_traces
+    steps = args.batch_steps + 1                    # first call warms up (and tunes)
+    ws = simulator.Workspace(objs[0].device)
+    lib = _abi.lib()
+    d_tr, d_out = [], []
+    for k in range(steps):
+        row_t, row_o = [], []
+        for o, tr in zip(objs, tracks):
+            ns = tr.shape[0]
+            lo = ns // 4 + (k * K) % max(ns // 2 - K, 1)
+            row_t.append(torch.from_numpy(np.ascontiguousarray(tr[lo:lo + K])).cuda())
+            row_o.append(torch.empty((K, o.nr), dtype=torch.complex64, device="cuda"))
+        d_tr.append(row_t)
+        d_out.append(row_o)
+    counts = [[np.zeros((K, 2), np.int64) for _ in objs] for _ in range(steps)]
+
+    def jobs(k):
+        arr = (_abi.RpJob * len(objs))()
+        for i, o in enumerate(objs):
+            arr[i] = _abi.RpJob(o.handle, d_tr[k][i].data_ptr(), K, d_out[k][i].data_ptr(),
+                                counts[k][i].ctypes.data)
+        return arr
+
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    torch.cuda.synchronize()
+    _abi.check("rp_simulate_batch", lib.rp_simulate_batch(jobs(0), len(objs), ws.handle, sp))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    launches = 0
+    for k in range(1, steps):
+        _abi.check("rp_simulate_batch", lib.rp_simulate_batch(jobs(k), len(objs), ws.handle, sp))
+        launches += simulator.last_launch_count()
+    torch.cuda.synchronize()
+    tb = time.perf_counter() - t0
+    pairs = sum(opcount.pairs(np.concatenate(counts[k])) for k in range(1, steps))
+    # the same traces, one scene per call
+    seq_counts = [[np.zeros((K, 2), np.int64) for _ in objs] for _ in range(steps)]
+    t0 = time.perf_counter()
+    for k in range(1, steps):
+        for i, o in enumerate(objs):
+            rc = lib.rp_simulate_ws(ctypes.c_void_p(o.handle), ws.handle, ctypes.c_void_p(d_tr[k][i].data_ptr()),
+                                    K, simulator.FORMS["fast"], ctypes.c_void_p(d_out[k][i].data_ptr()),
+                                    seq_counts[k][i].ctypes.data, sp)
+            _abi.check("rp_simulate_ws", rc)
+    torch.cuda.synchronize()
+    ts = time.perf_counter() - t0
+    ws.close()
+    bands = {}
+    for o in objs:
+        key = f"{o.params.frequency / 1e6:g} MHz/{o.nr} bins"
+        bands[key] = bands.get(key, 0) + 1
+    return {"value": pairs / tb, "unit": UNIT, "scenes": len(objs), "traces_per_scene_per_step": K,
+            "steps": steps - 1, "ms_per_step": 1e3 * tb / (steps - 1), "pairs_per_step": pairs / (steps - 1),
+            "gpu_launches_per_step": launches / (steps - 1),
+            "one_scene_per_call": {"value": pairs / ts, "ms_per_step": 1e3 * ts / (steps - 1)},
+            "batched_over_one_at_a_time": ts / tb,
+            "tuned_multi_cfg": simulator.autotune_query(True),
+            "mix": bands}
+
+
+def run_serving(args, objs, tracks, plain_value):
+    """The serving loop: Poisson arrivals of flyby requests over the resident
+    scenes (a scene drawn uniformly, 1-8 consecutive interior traces), served
+    concurrently with footprint admission; latency is submit to result."""
+    from europaraypaths_gb300 import serving
+    rng = np.random.default_rng(4)
+    srv = serving.Server(workers=4, device=objs[0].device)
+    sids = [srv.adopt_scene(o) for o in objs]
+    n_req = int(args.serve_rate * args.serve_seconds)
+    gaps = rng.exponential(1.0 / args.serve_rate, n_req)
+    reqs = []
+    t_start = time.perf_counter()
+    t_next = t_start
+    for g in gaps:
+        t_next += g
+        dt = t_next - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        i = int(rng.integers(0, len(objs)))
+        ns = tracks[i].shape[0]
+        n = int(rng.integers(1, 9))
+        lo = ns // 4 + int(rng.integers(0, max(ns // 2 - n, 1)))
+        reqs.append(srv.submit(sids[i], tracks[i][lo:lo + n]))
+    for r in reqs:
+        r.result(timeout=600)
+    st = srv.stats()
+    srv.close(keep_scenes=True)
+    st.update({"requests": n_req, "rate_req_s": args.serve_rate, "arrival_window_s": args.serve_seconds,
+               "workers": 4, "request": "uniform scene of the uneven-scenes workload, 1-8 interior traces",
+               "vs_plain_form": (st["pairs_per_s"] / plain_value) if (plain_value and st.get("pairs_per_s"))
+               else None})
+    return st
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -202,6 +314,11 @@ def main():
     ap.add_argument("--cpu-targets", type=int, default=48, help="target cap of the CPU baseline sample")
     ap.add_argument("--ref-targets", type=int, default=24, help="target cap per --impl reference step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-scenes", type=int, default=64, help="scenes of the batched workload (0 = skip)")
+    ap.add_argument("--batch-traces", type=int, default=2, help="interior traces per scene per batched step")
+    ap.add_argument("--batch-steps", type=int, default=3)
+    ap.add_argument("--serve-seconds", type=float, default=15.0, help="serving-loop arrivals window (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson request rate, requests/s")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -346,8 +463,21 @@ def main():
             pv = opcount.pairs(pc) / (e0.elapsed_time(e1) / 1e3)
             line["plain_form"] = {"value": pv, "unit": UNIT, "traces": args.plain_traces,
                                   "fast_over_plain": value / pv if pv else None}
+        roof["pair_cfg"] = {f"degree_{d}": simulator.autotune_query(False, d) for d in (0, 4, 5, 6)
+                            if simulator.autotune_query(False, d) >= 0}
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(sc, scene, track, args.cpu_targets, 1000)
+        if world == 1 and (args.batch_scenes > 0 or args.serve_seconds > 0):
+            scene.close()
+            specs, objs, tracks, t_build = batch_workload(args, local)
+            if args.batch_scenes > 0:
+                line["batch"] = run_batch(args, objs, tracks, stream)
+                line["batch"]["setup_s"] = t_build
+            if args.serve_seconds > 0:
+                plain = line.get("plain_form", {}).get("value")
+                line["serving"] = run_serving(args, objs, tracks, plain)
+            for o in objs:
+                o.close()
         print(json.dumps(line), flush=True)
     scene.close()
     if dist is not None:

@@ -24,6 +24,12 @@ _D = ctypes.c_double
 _I = ctypes.c_int32
 
 
+class RpJob(ctypes.Structure):
+    """struct rp_job (include/raypath.h)."""
+    _fields_ = [("scene", ctypes.c_void_p), ("d_traces", ctypes.c_void_p), ("ns", ctypes.c_int64),
+                ("d_out", ctypes.c_void_p), ("counts", ctypes.c_void_p)]
+
+
 class RpParams(ctypes.Structure):
     """struct rp_params (include/raypath.h); field order must match."""
     _fields_ = [
@@ -83,6 +89,9 @@ _SIGS = {
     "rp_workspace_bytes": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rp_simulate_ws": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rp_simulate_batch": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rp_autotune": ([ctypes.c_int], ctypes.c_int),
+    "rp_autotune_query": ([ctypes.c_int, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
     "rp_count_records": ([ctypes.c_char_p, ctypes.c_void_p], ctypes.c_int),
     "rp_read_facets": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
     "rp_read_targets": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),

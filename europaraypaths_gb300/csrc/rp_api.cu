@@ -315,22 +315,28 @@ static int build_tables(rp_scene* s) {
             for (size_t i = 0; i < v.size(); ++i) { b[2 * i] = (float)v[i].x; b[2 * i + 1] = (float)v[i].y; }
             return upload(d, b.data(), b.size() * sizeof(float), a);
         };
-        std::vector<Cplx<double>> c2(n2), b(M, Cplx<double>{0, 0}), bi(M, Cplx<double>{0, 0});
+        std::vector<Cplx<double>> c2(n2), h(M, Cplx<double>{0, 0});
         for (int i = 0; i < n2; ++i) c2[i] = Cplx<double>{host_sinc((double)(i - nr / 2) * p.dr / (2 * p.rng_res)), 0.0};
         host_dif(c2.data(), n2, f, lM);
-        std::vector<cd> w = bluestein_chirp(N);
-        for (int k = 0; k < N; ++k) {
-            Cplx<double> cw{w[k].real(), -w[k].imag()}, ww{w[k].real(), w[k].imag()};
-            b[k] = cw;
-            bi[k] = ww;
-            if (k) { b[M - k] = cw; bi[M - k] = ww; }
+        // cropSpectrum followed by the inverse N-point DFT is a circular
+        // convolution with h[n] = (1/N) sum_{min(k,N-k) <= K} e^{2 pi i k n / N}
+        // = sin(pi (2K+1) n / N) / (N sin(pi n / N)) (the Dirichlet kernel of
+        // the kept band; a delta when nothing is cropped).  Its M-point
+        // spectrum, with the 1/M of the unnormalised inverse, in DIF order.
+        for (int n = 0; n < N; ++n) {
+            double v;
+            if (s->crop_all) v = (n == 0) ? 1.0 : 0.0;
+            else if (n == 0) v = (double)(2 * K + 1) / N;
+            else {
+                const long long r = ((long long)(2 * K + 1) * n) % (2LL * N);
+                v = std::sin(RP_PI * (double)r / N) / ((double)N * std::sin(RP_PI * (double)n / N));
+            }
+            h[n] = Cplx<double>{v / M, 0.0};
         }
-        host_dif(b.data(), M, f, lM);
-        host_dif(bi.data(), M, f, lM);
+        host_dif(h.data(), M, f, lM);
         if ((rc = to32(tw, &s->d_twS, &acc))) return rc;
         if ((rc = to32(c2, &s->d_C2S, &acc))) return rc;
-        if ((rc = to32(b, &s->d_bWS, &acc))) return rc;
-        if ((rc = to32(bi, &s->d_bWiS, &acc))) return rc;
+        if ((rc = to32(h, &s->d_HS, &acc))) return rc;
         s->mS = M;
         s->log2mS = lM;
         s->smem_conv = 1;
@@ -391,6 +397,7 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
     if ((rc = upload(&s->d_facets, facets, sizeof(double) * 12 * nf, &s->store_bytes))) return fail(rc);
     if ((rc = upload(&s->d_targets, targets, sizeof(double) * 7 * nt, &s->store_bytes))) return fail(rc);
     if ((rc = upload(&s->d_prisms, prisms, sizeof(double) * 7 * np, &s->store_bytes))) return fail(rc);
+    if (nt > 0) s->h_targets.assign(targets, targets + 7 * nt);
     for (int64_t t = 0; t < nt; ++t)
         if (targets[6 * nt + t] == 0.0) { s->any_ttype0 = 1; break; }
     // spatially sorted copy for the fast form
@@ -432,7 +439,7 @@ extern "C" int rp_scene_destroy(rp_scene* s) {
     if (s->own_stream) cudaStreamSynchronize(s->own_stream);
     void* ptrs[] = {s->d_facets, s->d_targets, s->d_prisms, s->d_order, s->d_sorted,
                     s->d_C1_64, s->d_C2_64, s->d_C1_32, s->d_C2_32, s->d_twS, s->d_C2S,
-                    s->d_bWS, s->d_bWiS};
+                    s->d_HS};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     free_plan(s->plan2);
@@ -518,6 +525,28 @@ extern "C" int rp_simulate_ws(rp_scene* s, rp_workspace* ws, const double* d_tra
     cudaStream_t st = stream ? (cudaStream_t)stream : s->own_stream;
     if (ns == 0) return RP_OK;
     return run_form(s, ws, d_traces, ns, form, d_out, counts, st);
+}
+
+extern "C" int rp_simulate_batch(const rp_job* jobs, int njobs, rp_workspace* ws, void* stream) {
+    if (!ws || njobs < 0 || (njobs > 0 && !jobs)) {
+        rp_set_error("rp_simulate_batch: bad argument");
+        return RP_ERR_ARG;
+    }
+    g_launches = 0;
+    g_timer.reset();
+    std::vector<rp_job> live;
+    for (int j = 0; j < njobs; ++j) {
+        const rp_job& b = jobs[j];
+        if (!b.scene || b.ns < 0 || (b.ns > 0 && (!b.d_traces || !b.d_out)) || b.scene->device != ws->device) {
+            rp_set_error("rp_simulate_batch: job %d: bad scene, trace table, output or device", j);
+            return RP_ERR_ARG;
+        }
+        if (b.ns > 0) live.push_back(b);
+    }
+    RP_CUDA(cudaSetDevice(ws->device));
+    if (live.empty()) return RP_OK;
+    cudaStream_t st = stream ? (cudaStream_t)stream : live[0].scene->own_stream;
+    return rp_fast_batch(live.data(), (int)live.size(), ws, st);
 }
 
 extern "C" int rp_simulate(rp_scene* s, const double* traces, int64_t ns, int form, void* out,

@@ -24,6 +24,8 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "rp_common.cuh"
@@ -378,6 +380,7 @@ struct PairArgs {
     float eks;          // -2 ks^2 log2(e)
     double nidx, inv_dr, inv_lam;   // inv_lam: turns per metre, pi_F / (pi lam)
     int lossless;
+    int deg;            // sinc polynomial degree (0: special-function unit)
 };
 
 // Per-(chunk, target) anchors of the split-precision evaluation.
@@ -594,23 +597,157 @@ __device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo,
     }
 }
 
+// One work item of the pair stage: target block tb of trace s of a batch,
+// facet chunks [k0, k1) of part `part`.  srec: two chunk buffers, win: the
+// per-thread bin windows, bars/phase: the two stage barriers and their
+// parities (carried across items), s_tpos: the threads' target positions.
+template <int NT, int ILP, class PA>
+__device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, FacetRec* srec, float2* win,
+                                          uint64_t* bars, uint32_t* phase, double (*s_tpos)[RP_PAIR_THREADS]) {
+    const int tid = threadIdx.x;
+    const int nq = A.ntl[s];
+    const int n = A.nill[s];
+    if (tb * RP_PAIR_THREADS >= nq || n == 0) return;
+    const int nchunks = (n + RP_CHUNK - 1) / RP_CHUNK;
+    const int k0 = (int)((int64_t)nchunks * part / RP_PARTS);
+    const int k1 = (int)((int64_t)nchunks * (part + 1) / RP_PARTS);
+    if (k0 >= k1) return;
+    const int q = tb * RP_PAIR_THREADS + tid;
+    const bool active = q < nq;
+    float tnx = 0, tny = 0, tnz = 1;
+    int b0 = 0;
+    C32* Trow = nullptr;
+    if (active) {
+        const int64_t ti = A.tlist[(size_t)s * A.tstride + q];
+        s_tpos[0][tid] = A.TG[ti];
+        s_tpos[1][tid] = A.TG[A.nt + ti];
+        s_tpos[2][tid] = A.TG[2 * A.nt + ti];
+        tnx = (float)A.TG[3 * A.nt + ti]; tny = (float)A.TG[4 * A.nt + ti];
+        tnz = (float)A.TG[5 * A.nt + ti];
+        b0 = A.bt0[(size_t)s * A.tstride + q];
+        Trow = A.T + (((size_t)part * A.nb + s) * A.tstride + q) * A.Wt;
+    }
+    const FacetRec* rbase = A.rec + (size_t)s * A.rstride;
+    // prologue: stage chunk k0
+    if (tid == 0) {
+        int cnt = min(RP_CHUNK, n - k0 * RP_CHUNK);
+        uint32_t bytes = (uint32_t)(cnt * sizeof(FacetRec));
+        mbar_expect_tx(&bars[0], bytes);
+        tma_bulk_g2s(srec, rbase + (size_t)k0 * RP_CHUNK, bytes, &bars[0]);
+    }
+    for (int k = k0; k < k1; ++k) {
+        const int buf = (k - k0) & 1;
+        // prefetch the next chunk into the other buffer (its readers
+        // finished at the trailing __syncthreads of the previous step)
+        if (tid == 0 && k + 1 < k1) {
+            int cnt = min(RP_CHUNK, n - (k + 1) * RP_CHUNK);
+            uint32_t bytes = (uint32_t)(cnt * sizeof(FacetRec));
+            mbar_expect_tx(&bars[buf ^ 1], bytes);
+            tma_bulk_g2s(srec + (buf ^ 1) * RP_CHUNK, rbase + (size_t)(k + 1) * RP_CHUNK, bytes,
+                         &bars[buf ^ 1]);
+        }
+        const ChunkMeta* mp = A.meta + (size_t)s * A.mstride + k;
+        if (!mbar_wait(&bars[buf], phase[buf])) {
+            if (tid == 0) atomicOr(A.err + 1, 1u);
+        }
+        phase[buf] ^= 1u;
+        const FacetRec* R = srec + buf * RP_CHUNK;
+        if (active) {
+            // FP64 anchors of this (chunk, target)
+            const double mcx = mp->cx, mcy = mp->cy, mcz = mp->cz;
+            const double Dx = s_tpos[0][tid] - mcx, Dy = s_tpos[1][tid] - mcy, Dz = s_tpos[2][tid] - mcz;
+            const double T0 = sqrt(Dx * Dx + Dy * Dy + Dz * Dz);
+            const double xt = A.nidx * T0 * A.inv_dr;
+            const double tt = A.nidx * T0 * A.inv_lam;
+            const double lo = (double)mp->xmin + A.nidx * (T0 - (double)mp->R) * A.inv_dr;
+            const int blo = (int)floor(lo) - 1;
+            Anchor an;
+            an.Dx = (float)Dx; an.Dy = (float)Dy; an.Dz = (float)Dz;
+            an.T0 = (float)T0; an.T0sq = (float)(T0 * T0);
+            an.tau0 = (float)(tt - floor(tt));
+            an.xbase = (float)(xt - (double)blo);
+            an.tnx = tnx; an.tny = tny; an.tnz = tnz;
+            for (int w = 0; w < RP_WIN; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
+            const int cnt = mp->n;
+            const bool prisms = (A.np > 0) && !A.lossless;
+            int jj = 0;
+            if (ILP == 2)
+            for (; jj + 1 < cnt; jj += 2) {
+                const FacetRec r0 = R[jj];
+                const FacetRec r1 = R[jj + 1];
+                float x0, re0, im0, x1, re1, im1;
+                pair_eval<NT>(r0, an, A, x0, re0, im0);
+                pair_eval<NT>(r1, an, A, x1, re1, im1);
+                if (prisms) {
+                    const float f0 = prism_factor(r0.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
+                                                  A.PR, A.np, A.ealpha);
+                    const float f1 = prism_factor(r1.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
+                                                  A.PR, A.np, A.ealpha);
+                    re0 *= f0; im0 *= f0; re1 *= f1; im1 *= f1;
+                }
+                bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
+                bin_add(x1, re1, im1, blo, b0, win, tid, Trow, A);
+            }
+            for (; jj < cnt; ++jj) {
+                const FacetRec r0 = R[jj];
+                float x0, re0, im0;
+                pair_eval<NT>(r0, an, A, x0, re0, im0);
+                if (prisms) {
+                    const float f0 = prism_factor(r0.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
+                                                  A.PR, A.np, A.ealpha);
+                    re0 *= f0; im0 *= f0;
+                }
+                bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
+            }
+            // flush the window into the owned trace
+            for (int w = 0; w < RP_WIN; ++w) {
+                const float2 v = win[w * RP_PAIR_THREADS + tid];
+                if (v.x != 0.f || v.y != 0.f) {
+                    const int o = blo + w - b0;
+                    if (o >= 0 && o < A.Wt) {
+                        C32 t0 = Trow[o];
+                        t0.x += v.x;
+                        t0.y += v.y;
+                        Trow[o] = t0;
+                    } else {
+                        atomicOr(A.err, 1u);
+                    }
+                }
+            }
+        }
+        __syncthreads();   // everyone done with buffer `buf` before it is refilled
+    }
+}
+
+#define RP_PAIR_SMEM_DECL                                                                       \
+    extern __shared__ __align__(128) unsigned char smem[];                                      \
+    FacetRec* srec = reinterpret_cast<FacetRec*>(smem);                     /* [2][RP_CHUNK] */ \
+    float2* win = reinterpret_cast<float2*>(smem + 2 * RP_CHUNK * sizeof(FacetRec));            \
+    __shared__ uint64_t bars[2];                                                                \
+    __shared__ unsigned int s_item;                                                             \
+    __shared__ double s_tpos[3][RP_PAIR_THREADS];                                               \
+    const int tid = threadIdx.x;                                                                \
+    if (tid == 0) {                                                                             \
+        mbar_init(&bars[0], 1);                                                                 \
+        mbar_init(&bars[1], 1);                                                                 \
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");                     \
+    }                                                                                           \
+    __syncthreads();                                                                            \
+    uint32_t phase[2] = {0u, 0u};
+
+#define RP_PAIR_SMEM_END                                                    \
+    if (tid == 0) {                                                         \
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bars[0]))); \
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bars[1]))); \
+    }
+
+// Single-batch pair kernel: the batch's constants live in the parameter
+// bank.  Persistent: blocks take (trace, target block, part) items from a
+// work counter until all are done.
 template <int NT, int ILP, int MINB>
 __global__ void __launch_bounds__(RP_PAIR_THREADS, MINB)
 k_pairs32(PairArgs A) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    FacetRec* srec = reinterpret_cast<FacetRec*>(smem);                     // [2][RP_CHUNK]
-    float2* win = reinterpret_cast<float2*>(smem + 2 * RP_CHUNK * sizeof(FacetRec));  // [RP_WIN][threads]
-    __shared__ uint64_t bars[2];
-    __shared__ unsigned int s_item;
-    __shared__ double s_tpos[3][RP_PAIR_THREADS];   // this thread's target position (FP64)
-    const int tid = threadIdx.x;
-    if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    uint32_t phase[2] = {0u, 0u};
+    RP_PAIR_SMEM_DECL
     const unsigned int items = (unsigned)A.nb * A.tblocks * RP_PARTS;
     for (;;) {
         if (tid == 0) s_item = atomicAdd(A.work, 1u);
@@ -621,123 +758,51 @@ k_pairs32(PairArgs A) {
         const int part = item % RP_PARTS;
         const int tb = (item / RP_PARTS) % A.tblocks;
         const int s = item / (RP_PARTS * A.tblocks);
-        const int nq = A.ntl[s];
-        const int n = A.nill[s];
-        if (tb * RP_PAIR_THREADS >= nq || n == 0) continue;
-        const int nchunks = (n + RP_CHUNK - 1) / RP_CHUNK;
-        const int k0 = (int)((int64_t)nchunks * part / RP_PARTS);
-        const int k1 = (int)((int64_t)nchunks * (part + 1) / RP_PARTS);
-        if (k0 >= k1) continue;
-        const int q = tb * RP_PAIR_THREADS + tid;
-        const bool active = q < nq;
-        float tnx = 0, tny = 0, tnz = 1;
-        int b0 = 0;
-        C32* Trow = nullptr;
-        if (active) {
-            const int64_t ti = A.tlist[(size_t)s * A.tstride + q];
-            s_tpos[0][tid] = A.TG[ti];
-            s_tpos[1][tid] = A.TG[A.nt + ti];
-            s_tpos[2][tid] = A.TG[2 * A.nt + ti];
-            tnx = (float)A.TG[3 * A.nt + ti]; tny = (float)A.TG[4 * A.nt + ti];
-            tnz = (float)A.TG[5 * A.nt + ti];
-            b0 = A.bt0[(size_t)s * A.tstride + q];
-            Trow = A.T + (((size_t)part * A.nb + s) * A.tstride + q) * A.Wt;
-        }
-        const FacetRec* rbase = A.rec + (size_t)s * A.rstride;
-        // prologue: stage chunk k0
+        pair_item<NT, ILP>(A, s, tb, part, srec, win, bars, phase, s_tpos);
+    }
+    RP_PAIR_SMEM_END
+}
+
+// Multi-job pair kernel: one persistent launch over the items of many
+// batches (scenes of different sizes, bin counts and sinc degrees).  Job j
+// owns items [start[j], start[j + 1]); a block copies the job's constants
+// into registers and dispatches on its sinc degree.
+template <int ILP, int MINB>
+__global__ void __launch_bounds__(RP_PAIR_THREADS, MINB)
+k_pairs32m(const PairArgs* __restrict__ jobs, const unsigned int* __restrict__ start, int njobs,
+           unsigned int* work) {
+    RP_PAIR_SMEM_DECL
+    __shared__ int s_job;
+    const unsigned int total = start[njobs];
+    for (;;) {
         if (tid == 0) {
-            int cnt = min(RP_CHUNK, n - k0 * RP_CHUNK);
-            uint32_t bytes = (uint32_t)(cnt * sizeof(FacetRec));
-            mbar_expect_tx(&bars[0], bytes);
-            tma_bulk_g2s(srec, rbase + (size_t)k0 * RP_CHUNK, bytes, &bars[0]);
+            const unsigned int it = atomicAdd(work, 1u);
+            int lo = 0, hi = njobs - 1;          // last j with start[j] <= it
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (start[mid] <= it) lo = mid; else hi = mid - 1;
+            }
+            s_item = it;
+            s_job = lo;
         }
-        for (int k = k0; k < k1; ++k) {
-            const int buf = (k - k0) & 1;
-            // prefetch the next chunk into the other buffer (its readers
-            // finished at the trailing __syncthreads of the previous step)
-            if (tid == 0 && k + 1 < k1) {
-                int cnt = min(RP_CHUNK, n - (k + 1) * RP_CHUNK);
-                uint32_t bytes = (uint32_t)(cnt * sizeof(FacetRec));
-                mbar_expect_tx(&bars[buf ^ 1], bytes);
-                tma_bulk_g2s(srec + (buf ^ 1) * RP_CHUNK, rbase + (size_t)(k + 1) * RP_CHUNK, bytes,
-                             &bars[buf ^ 1]);
-            }
-            const ChunkMeta* mp = A.meta + (size_t)s * A.mstride + k;
-            if (!mbar_wait(&bars[buf], phase[buf])) {
-                if (tid == 0) atomicOr(A.err + 1, 1u);
-            }
-            phase[buf] ^= 1u;
-            const FacetRec* R = srec + buf * RP_CHUNK;
-            if (active) {
-                // FP64 anchors of this (chunk, target)
-                const double mcx = mp->cx, mcy = mp->cy, mcz = mp->cz;
-                const double Dx = s_tpos[0][tid] - mcx, Dy = s_tpos[1][tid] - mcy, Dz = s_tpos[2][tid] - mcz;
-                const double T0 = sqrt(Dx * Dx + Dy * Dy + Dz * Dz);
-                const double xt = A.nidx * T0 * A.inv_dr;
-                const double tt = A.nidx * T0 * A.inv_lam;
-                const double lo = (double)mp->xmin + A.nidx * (T0 - (double)mp->R) * A.inv_dr;
-                const int blo = (int)floor(lo) - 1;
-                Anchor an;
-                an.Dx = (float)Dx; an.Dy = (float)Dy; an.Dz = (float)Dz;
-                an.T0 = (float)T0; an.T0sq = (float)(T0 * T0);
-                an.tau0 = (float)(tt - floor(tt));
-                an.xbase = (float)(xt - (double)blo);
-                an.tnx = tnx; an.tny = tny; an.tnz = tnz;
-                for (int w = 0; w < RP_WIN; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
-                const int cnt = mp->n;
-                const bool prisms = (A.np > 0) && !A.lossless;
-                int jj = 0;
-                if (ILP == 2)
-                for (; jj + 1 < cnt; jj += 2) {
-                    const FacetRec r0 = R[jj];
-                    const FacetRec r1 = R[jj + 1];
-                    float x0, re0, im0, x1, re1, im1;
-                    pair_eval<NT>(r0, an, A, x0, re0, im0);
-                    pair_eval<NT>(r1, an, A, x1, re1, im1);
-                    if (prisms) {
-                        const float f0 = prism_factor(r0.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
-                                                      A.PR, A.np, A.ealpha);
-                        const float f1 = prism_factor(r1.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
-                                                      A.PR, A.np, A.ealpha);
-                        re0 *= f0; im0 *= f0; re1 *= f1; im1 *= f1;
-                    }
-                    bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
-                    bin_add(x1, re1, im1, blo, b0, win, tid, Trow, A);
-                }
-                for (; jj < cnt; ++jj) {
-                    const FacetRec r0 = R[jj];
-                    float x0, re0, im0;
-                    pair_eval<NT>(r0, an, A, x0, re0, im0);
-                    if (prisms) {
-                        const float f0 = prism_factor(r0.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
-                                                      A.PR, A.np, A.ealpha);
-                        re0 *= f0; im0 *= f0;
-                    }
-                    bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
-                }
-                // flush the window into the owned trace
-                for (int w = 0; w < RP_WIN; ++w) {
-                    const float2 v = win[w * RP_PAIR_THREADS + tid];
-                    if (v.x != 0.f || v.y != 0.f) {
-                        const int o = blo + w - b0;
-                        if (o >= 0 && o < A.Wt) {
-                            C32 t0 = Trow[o];
-                            t0.x += v.x;
-                            t0.y += v.y;
-                            Trow[o] = t0;
-                        } else {
-                            atomicOr(A.err, 1u);
-                        }
-                    }
-                }
-            }
-            __syncthreads();   // everyone done with buffer `buf` before it is refilled
+        __syncthreads();
+        const unsigned int item = s_item;
+        const int j = s_job;
+        __syncthreads();
+        if (item >= total) break;
+        const PairArgs A = jobs[j];
+        const unsigned int li = item - start[j];
+        const int part = li % RP_PARTS;
+        const int tb = (li / RP_PARTS) % A.tblocks;
+        const int s = li / (RP_PARTS * A.tblocks);
+        switch (A.deg) {
+            case 4: pair_item<4, ILP>(A, s, tb, part, srec, win, bars, phase, s_tpos); break;
+            case 5: pair_item<5, ILP>(A, s, tb, part, srec, win, bars, phase, s_tpos); break;
+            case 6: pair_item<6, ILP>(A, s, tb, part, srec, win, bars, phase, s_tpos); break;
+            default: pair_item<0, ILP>(A, s, tb, part, srec, win, bars, phase, s_tpos); break;
         }
     }
-    if (tid == 0) {
-        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bars[0])));
-        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bars[1])));
-    }
+    RP_PAIR_SMEM_END
 }
 
 // ---------------------------------------------------------- compression --
@@ -789,9 +854,14 @@ __global__ void k_conv32(const int* __restrict__ ntl, int64_t tstride, int nb, c
 //   X = DIF(pad T)                         T = sum of the facet-range parts
 //   W = DIT(X * C2)[nr/2 ..] / 2nr         Ptarg (convolvePhasorChirpLinear)
 //   W = DIT(X * DIF(pad Ptarg)) * s / 2nr  u = Psour (*) Ptarg, Psour = s T
-//   X = crop(Bluestein_N(u))               DFT on the N = 2nr - 1 grid, cropSpectrum
-//   out[j] += Bluestein_N^-1(X)[2j] / N    takeEveryOtherComplex
-// (radar_kernels.cu:554-649, elementary_kernels.cu:258-353).
+//                                          (length N = 2nr - 1: the N-point
+//                                          circular product has no wrap)
+//   W = DIT_M(DIF_M(pad u) * H)            u (*) h, h = IDFT_N(crop mask)
+//   out[j] += W[2j] + W[2j + N]            circular on N, takeEveryOtherComplex
+// cropSpectrum + IDFT_N is the fixed circular convolution with h, so the two
+// N-point Bluestein transforms of convolveComplex reduce to one linear
+// convolution at M >= 2N - 1 (radar_kernels.cu:554-649,
+// elementary_kernels.cu:258-353).
 struct ConvArgs {
     const int* ntl;
     int64_t tstride;
@@ -802,9 +872,7 @@ struct ConvArgs {
     const Cplx<float>* tw;
     int log2M;
     const Cplx<float>* C2s;
-    const Cplx<float>* bWs;
-    const Cplx<float>* bWis;
-    const Cplx<float>* bw;
+    const Cplx<float>* Hs;  // DIF_M(crop kernel) / M
     int nr, n2, N, M, crop_K, crop_all;
     float sig_scale;
     C32* part;          // [nb][nsplit][nr]
@@ -820,26 +888,49 @@ struct TW32 {
     }
 };
 
+// Persistent over the items of one or more batches (job j owns items
+// [start[j], start[j + 1])); shared memory: the twiddle quarter for the
+// job's M (reloaded when M changes), then X and W.
 template <int KPT>
 __global__ void __launch_bounds__(RP_CONV_THREADS, 1)
-k_conv32s(ConvArgs A) {
+k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ start, int njobs,
+          int maxM, unsigned int* work) {
     extern __shared__ __align__(16) unsigned char csm[];
-    Cplx<float>* X = reinterpret_cast<Cplx<float>*>(csm);
-    Cplx<float>* W = X + A.n2;
-    Cplx<float>* TWs = W + A.M;          // first quarter of the twiddle circle
+    Cplx<float>* TWs = reinterpret_cast<Cplx<float>*>(csm);   // first quarter of the twiddle circle
+    Cplx<float>* X = TWs + maxM / 4;
     __shared__ unsigned int s_item;
+    __shared__ int s_job;
+    __shared__ ConvArgs A;                  // the current item's job (off the FFT hot path)
     const int tid = threadIdx.x;
-    const int nr = A.nr, n2 = A.n2, N = A.N, M = A.M;
-    #pragma unroll 8
-    for (int k = tid; k < M / 4; k += RP_CONV_THREADS) TWs[k] = A.tw[k];
-    __syncthreads();
-    const unsigned int items = (unsigned)A.nb * A.nsplit;
+    const unsigned int total = start[njobs];
+    int curM = 0, curJ = -1;
     for (;;) {
-        if (tid == 0) s_item = atomicAdd(A.work, 1u);
+        if (tid == 0) {
+            const unsigned int it = atomicAdd(work, 1u);
+            int lo = 0, hi = njobs - 1;          // last j with start[j] <= it
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (start[mid] <= it) lo = mid; else hi = mid - 1;
+            }
+            s_item = it;
+            s_job = lo;
+        }
+        __syncthreads();        // every thread is done with the previous item's A
+        const unsigned int item0 = s_item;
+        const int jb = s_job;
+        if (tid == 0 && item0 < total && jb != curJ) A = jobs[jb];
         __syncthreads();
-        const unsigned int item = s_item;
-        __syncthreads();
-        if (item >= items) break;
+        if (item0 >= total) break;
+        curJ = jb;
+        const unsigned int item = item0 - start[jb];
+        const int nr = A.nr, n2 = A.n2, N = A.N, M = A.M;
+        Cplx<float>* W = X + n2;
+        if (M != curM) {
+            #pragma unroll 8
+            for (int k = tid; k < M / 4; k += RP_CONV_THREADS) TWs[k] = A.tw[k];
+            __syncthreads();
+            curM = M;
+        }
         const int s = item / A.nsplit;
         const int sp = item % A.nsplit;
         const int nq = A.ntl[s];
@@ -900,44 +991,23 @@ k_conv32s(ConvArgs A) {
             __syncthreads();
             block_dit_u<float, 4>(W, n2, TWs, A.log2M);                 // u (natural, N values)
             #pragma unroll 8
-            for (int k = tid; k < M; k += RP_CONV_THREADS)
-                W[k] = (k < N) ? c_mul(W[k], A.bw[k]) : Cplx<float>{0.f, 0.f};
+            for (int k = N + tid; k < M; k += RP_CONV_THREADS) W[k] = Cplx<float>{0.f, 0.f};
             __syncthreads();
+            // cropSpectrum + inverse DFT on the N grid = circular convolution
+            // with the crop kernel h: linear convolution at M >= 2N - 1, then
+            // circ[n] = lin[n] + lin[n + N]
             block_dif_u<float, 4>(W, M, TWs, A.log2M);
             #pragma unroll 8
-            for (int k = tid; k < M; k += RP_CONV_THREADS) W[k] = c_mul(W[k], A.bWs[k]);
+            for (int k = tid; k < M; k += RP_CONV_THREADS) W[k] = c_mul(W[k], A.Hs[k]);
             __syncthreads();
             block_dit_u<float, 4>(W, M, TWs, A.log2M);
-            {
-                const float invM = 1.f / (float)M;
-                #pragma unroll 8
-                for (int k = tid; k < N; k += RP_CONV_THREADS) {
-                    const int m = k < N - k ? k : N - k;
-                    const bool kept = A.crop_all || m <= A.crop_K;
-                    Cplx<float> v = c_mul(W[k], A.bw[k]);
-                    X[k] = kept ? Cplx<float>{v.x * invM, v.y * invM} : Cplx<float>{0.f, 0.f};
-                }
-            }
-            __syncthreads();
-            #pragma unroll 8
-            for (int k = tid; k < M; k += RP_CONV_THREADS)
-                W[k] = (k < N) ? c_mulc(X[k], A.bw[k]) : Cplx<float>{0.f, 0.f};
-            __syncthreads();
-            block_dif_u<float, 4>(W, M, TWs, A.log2M);
-            #pragma unroll 8
-            for (int k = tid; k < M; k += RP_CONV_THREADS) W[k] = c_mul(W[k], A.bWis[k]);
-            __syncthreads();
-            block_dit_u<float, 4>(W, M, TWs, A.log2M);
-            {
-                const float sc = 1.f / ((float)M * (float)N);
 #pragma unroll
-                for (int i = 0; i < KPT; ++i) {
-                    const int j = tid + i * RP_CONV_THREADS;
-                    if (j < nr) {
-                        Cplx<float> v = c_mulc(W[2 * j], A.bw[2 * j]);
-                        accr[i] = fmaf(v.x, sc, accr[i]);
-                        acci[i] = fmaf(v.y, sc, acci[i]);
-                    }
+            for (int i = 0; i < KPT; ++i) {
+                const int j = tid + i * RP_CONV_THREADS;
+                if (j < nr) {     // takeEveryOtherComplex: circ[2j]
+                    const Cplx<float> a = W[2 * j], b = W[2 * j + N];
+                    accr[i] += a.x + b.x;
+                    acci[i] += a.y + b.y;
                 }
             }
             __syncthreads();
@@ -1089,25 +1159,6 @@ FastLayout fast_layout(const rp_scene* sc, int nb, int64_t tstride, int Wt) {
 
 const size_t kFastBudget = (size_t)32 << 30;
 
-std::vector<int> host_target_bounds32(const rp_scene* sc, const std::vector<double>& tr, int64_t ns,
-                                      const std::vector<double>& tg) {
-    std::vector<int> ub(ns, 0);
-    const int64_t nt = sc->nt;
-    const double ap = sc->dp.ap_rad + 1e-9;
-    for (int64_t s = 0; s < ns; ++s) {
-        const double* r = &tr[9 * s];
-        int c = 0;
-        for (int64_t i = 0; i < nt; ++i) {
-            double vx = tg[i] - r[0], vy = tg[nt + i] - r[1], vz = tg[2 * nt + i] - r[2];
-            double m = std::sqrt(vx * vx + vy * vy + vz * vz);
-            double cs = -r[3] * vx / m - r[4] * vy / m - r[5] * vz / m;
-            cs = std::max(-1.0, std::min(1.0, cs));
-            if (!(std::acos(cs) > ap)) ++c;
-        }
-        ub[s] = c;
-    }
-    return ub;
-}
 
 // Pair-kernel instantiation: sinc degree x (ILP facets per step, resident
 // blocks per SM).  cfg 0: 2 x 3, 1: 2 x 2, 2: 1 x 4, 3: 1 x 3.
@@ -1180,245 +1231,607 @@ void sinc_poly(double T, int D, double* mono) {
 }
 
 template <int KPT>
-int launch_conv_k(const ConvArgs& C, size_t csm, int sms, int items, cudaStream_t st) {
+int launch_conv_k(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, int maxM, size_t csm, int sms,
+                  unsigned int items, unsigned int* work, cudaStream_t st) {
     RP_CUDA(cudaFuncSetAttribute(k_conv32s<KPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
     int occ = 0;
     RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv32s<KPT>, RP_CONV_THREADS, csm));
-    int grid = std::max(1, std::min(std::max(occ, 1) * sms, items));
-    k_conv32s<KPT><<<grid, RP_CONV_THREADS, csm, st>>>(C);
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(occ, 1) * sms, items));
+    k_conv32s<KPT><<<grid, RP_CONV_THREADS, csm, st>>>(d_jobs, d_start, njobs, maxM, work);
     RP_LAUNCHED();
     return RP_OK;
 }
 
-int launch_conv32s(const ConvArgs& C, size_t csm, int sms, int items, cudaStream_t st) {
-    const int kpt = (C.nr + RP_CONV_THREADS - 1) / RP_CONV_THREADS;
-    if (kpt <= 1) return launch_conv_k<1>(C, csm, sms, items, st);
-    if (kpt <= 2) return launch_conv_k<2>(C, csm, sms, items, st);
-    if (kpt <= 4) return launch_conv_k<4>(C, csm, sms, items, st);
-    return launch_conv_k<8>(C, csm, sms, items, st);
+int launch_conv32s(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, int max_nr, int maxM,
+                   size_t csm, int sms, unsigned int items, unsigned int* work, cudaStream_t st) {
+    const int kpt = (max_nr + RP_CONV_THREADS - 1) / RP_CONV_THREADS;
+    if (kpt <= 1) return launch_conv_k<1>(d_jobs, d_start, njobs, maxM, csm, sms, items, work, st);
+    if (kpt <= 2) return launch_conv_k<2>(d_jobs, d_start, njobs, maxM, csm, sms, items, work, st);
+    if (kpt <= 4) return launch_conv_k<4>(d_jobs, d_start, njobs, maxM, csm, sms, items, work, st);
+    return launch_conv_k<8>(d_jobs, d_start, njobs, maxM, csm, sms, items, work, st);
+}
+
+// Multi-job pair kernel per configuration (same (ILP, blocks/SM) table as
+// pick_cfg).
+void (*pick_multi(int cfg))(const PairArgs*, const unsigned int*, int, unsigned int*) {
+    switch (cfg) {
+        case 1: return k_pairs32m<2, 2>;
+        case 2: return k_pairs32m<1, 4>;
+        case 3: return k_pairs32m<1, 3>;
+        default: return k_pairs32m<2, 3>;
+    }
+}
+
+// ---------------------------------------------------------- autotuner ----
+// (multi, degree) -> configuration, for the process.  Probing launches the
+// candidate kernels on the real inputs (results are discarded and the
+// outputs re-zeroed), so only timing depends on the choice.
+std::mutex g_tune_mu;
+std::map<std::pair<int, int>, int> g_tuned;
+int g_autotune = -1;    // -1: not decided yet (env), 0 off, 1 on
+
+bool autotune_on() {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    if (g_autotune < 0) g_autotune = getenv("RP_PAIR_CFG") ? 0 : 1;
+    return g_autotune == 1;
+}
+
+int tuned_lookup(int multi, int deg) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find({multi, deg});
+    return it == g_tuned.end() ? -1 : it->second;
+}
+
+void tuned_store(int multi, int deg, int cfg) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[{multi, deg}] = cfg;
+}
+
+// ------------------------------------------------------------- segments ----
+// A segment is up to 64 traces of one scene processed as one batch; a wave
+// is a set of segments (possibly of different scenes) whose scratch fits the
+// budget and whose pair stage runs as one launch.
+struct Seg {
+    rp_scene* sc = nullptr;
+    const double* trb = nullptr;   // device trace rows of this segment
+    int64_t s0 = 0;                // first row in the job's output
+    int nb = 0;
+    int64_t tmax = 0;
+    void* d_out = nullptr;
+    int out64 = 0;
+    int64_t* h_counts = nullptr;
+    int deg = 0;
+    const double* coef = nullptr;
+    FastLayout Lw, L;
+    // setup stage
+    uint8_t* fflags; int* tcnt; int* nill; int* ntl; unsigned long long* vmax; unsigned long long* dmin;
+    int* idx; FacetRec* rec; ChunkMeta* meta; float* sxv; C32* sv; TraceMeta* tm; uint8_t* tflags;
+    int* tlist; int* bt0; int* misc; long long* acc; C32* refl; C32* sscr;
+    // pair stage
+    int Wt = 1;
+    int nsplit = 0;
+    bool smem = false;
+    bool pairs = false;
+    C32* T = nullptr; C32* Z = nullptr; C32* cscr = nullptr; C32* part = nullptr;
+};
+
+struct SceneConst {
+    int deg = 0;
+    double coef[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+SceneConst scene_const(const rp_scene* sc) {
+    SceneConst k;
+    const double pik_d = RP_PI * (RP_PI_F * sc->dp.fs / sc->dp.lam);
+    k.deg = sinc_degree(pik_d, sc->pair_variant);
+    if (k.deg > 0) sinc_poly(pik_d * pik_d, k.deg, k.coef);
+    return k;
+}
+
+size_t seg_setup_bytes(const rp_scene* sc, const FastLayout& L) {
+    ArenaPlan a;
+    fast_take_setup(a, sc, L);
+    return a.off + 256;
+}
+
+size_t seg_pair_bytes(const rp_scene* sc, const FastLayout& L) {
+    ArenaPlan a;
+    fast_take_pairs(a, sc, L);
+    return a.off + 256;
+}
+
+// Setup stage of one segment: cull and compact facets, facet records and
+// chunk metadata, surface bins, target list, target windows (maxw in misc[0]).
+void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
+    rp_scene* sc = g.sc;
+    const int64_t nf = sc->nf, nt = sc->nt;
+    const int nr = sc->nr, nb = g.nb;
+    const DevParams& dp = sc->dp;
+    const FastLayout& Lw = g.Lw;
+    const int64_t nfa = std::max<int64_t>(nf, 1), nta = std::max<int64_t>(nt, 1);
+    const int tiles = (int)((std::max(nfa, nta) + RP_TILE - 1) / RP_TILE);
+    g.fflags = a.take<uint8_t>((size_t)nb * nfa);
+    g.tcnt = a.take<int>((size_t)nb * tiles);
+    g.nill = a.take<int>(nb);
+    g.ntl = a.take<int>(nb);
+    g.vmax = a.take<unsigned long long>(nb);
+    g.dmin = a.take<unsigned long long>(nb);
+    g.idx = a.take<int>((size_t)nb * nfa);
+    g.rec = a.take<FacetRec>((size_t)nb * Lw.rstride);
+    g.meta = a.take<ChunkMeta>((size_t)nb * Lw.mstride);
+    g.sxv = a.take<float>((size_t)nb * nfa);
+    g.sv = a.take<C32>((size_t)nb * nfa);
+    g.tm = a.take<TraceMeta>(nb);
+    g.tflags = a.take<uint8_t>((size_t)nb * nta);
+    g.tlist = a.take<int>((size_t)nb * nta);
+    g.bt0 = a.take<int>((size_t)nb * Lw.tstride);
+    a.take<int>(8);
+    g.acc = a.take<long long>((size_t)nb * nr * 2);
+    g.refl = a.take<C32>((size_t)nb * nr);
+    g.sscr = a.take<C32>((size_t)nb * Lw.surf_slot);
+    const double* trb = g.trb;
+    cudaMemsetAsync(g.vmax, 0, sizeof(unsigned long long) * nb, st);
+    cudaMemsetAsync(g.dmin, 0xff, sizeof(unsigned long long) * nb, st);
+    cudaMemsetAsync(g.acc, 0, sizeof(long long) * nb * nr * 2, st);
+    if (nf > 0) {
+        k_cull_count<<<dim3((unsigned)((nf + RP_TILE - 1) / RP_TILE), nb), RP_TILE_THREADS, 0, st>>>(
+            sc->d_sorted, nf, trb, dp.ap_rad, g.fflags, g.tcnt, g.dmin);
+        RP_LAUNCHED();
+        compact_flags(g.fflags, nf, nb, g.tcnt, g.nill, g.idx, nfa, true, st);
+        k_facets32<<<dim3((unsigned)Lw.mstride, nb), RP_CHUNK, 0, st>>>(
+            sc->d_sorted, nfa, g.idx, g.nill, trb, dp, g.rec, g.meta, Lw.rstride, Lw.mstride, g.sxv, g.sv, g.vmax);
+        RP_LAUNCHED();
+        k_surf_fix32<<<dim3((unsigned)((nf + 256 * RP_SFIX_PER - 1) / (256 * RP_SFIX_PER)), nb), 256, 0, st>>>(
+            nfa, g.nill, g.sxv, g.sv, g.vmax, nr, g.acc);
+        RP_LAUNCHED();
+        k_tmeta32<<<nb, 256, 0, st>>>(g.meta, Lw.mstride, g.nill, g.tm);
+        RP_LAUNCHED();
+    } else {
+        cudaMemsetAsync(g.nill, 0, sizeof(int) * nb, st);
+    }
+    if (nt > 0) {
+        k_target_flags<<<dim3((unsigned)((nt + 255) / 256), nb), 256, 0, st>>>(sc->d_targets, nt, trb, dp.ap_rad,
+                                                                            g.tflags);
+        RP_LAUNCHED();
+        compact_flags(g.tflags, nt, nb, g.tcnt, g.ntl, g.tlist, Lw.tstride, false, st);
+        if (nf > 0) {
+            k_tsetup32<<<dim3((unsigned)((Lw.tstride + 255) / 256), nb), 256, 0, st>>>(
+                sc->d_targets, nt, g.tlist, g.ntl, Lw.tstride, g.tm, g.nill, dp, g.bt0, g.misc);
+            RP_LAUNCHED();
+        }
+    } else {
+        cudaMemsetAsync(g.ntl, 0, sizeof(int) * nb, st);
+    }
+}
+
+PairArgs seg_pair_args(const Seg& g) {
+    const rp_scene* sc = g.sc;
+    const DevParams& dp = sc->dp;
+    const int nr = sc->nr;
+    PairArgs P;
+    P.rec = g.rec; P.meta = g.meta; P.rstride = g.Lw.rstride; P.mstride = g.Lw.mstride;
+    P.nill = g.nill; P.ntl = g.ntl; P.tlist = g.tlist; P.tstride = g.L.tstride;
+    P.TG = sc->d_targets; P.nt = sc->nt; P.PR = sc->d_prisms; P.np = sc->np;
+    P.bt0 = g.bt0; P.T = g.T; P.Wt = g.Wt; P.nb = g.nb;
+    P.tblocks = (int)((g.L.tstride + RP_PAIR_THREADS - 1) / RP_PAIR_THREADS);
+    P.work = reinterpret_cast<unsigned int*>(g.misc + 1);
+    P.err = reinterpret_cast<unsigned int*>(g.misc + 2);
+    P.nr_f = (float)nr; P.nr = nr; P.nr1 = nr - 1;
+    P.kb = (float)(dp.nidx / dp.dr);
+    P.kt = (float)(dp.nidx * dp.turn);
+    P.pik = (float)(RP_PI * (RP_PI_F * dp.fs / dp.lam));
+    P.pik2 = P.pik * P.pik;
+    for (int k = 0; k < 8; ++k) P.sc[k] = (float)g.coef[k];
+    P.ealpha = dp.lossless ? 0.f : (float)(-2.0 * dp.alpha2 * 1.4426950408889634);
+    P.eks = dp.lossless ? 0.f : (float)(-2.0 * dp.ks * dp.ks * 1.4426950408889634);
+    P.nidx = dp.nidx; P.inv_dr = 1.0 / dp.dr; P.inv_lam = dp.turn;
+    P.lossless = dp.lossless;
+    P.deg = g.deg;
+    return P;
+}
+
+ConvArgs seg_conv_args(const Seg& g) {
+    const rp_scene* sc = g.sc;
+    const int nr = sc->nr;
+    ConvArgs C;
+    C.ntl = g.ntl; C.tstride = g.L.tstride; C.nb = g.nb; C.bt0 = g.bt0; C.T = g.T; C.Wt = g.Wt;
+    C.tw = (const Cplx<float>*)sc->d_twS; C.log2M = sc->log2mS;
+    C.C2s = (const Cplx<float>*)sc->d_C2S; C.Hs = (const Cplx<float>*)sc->d_HS;
+    C.nr = nr; C.n2 = 2 * nr; C.N = 2 * nr - 1; C.M = sc->mS;
+    C.crop_K = sc->crop_K; C.crop_all = sc->crop_all;
+    C.sig_scale = (float)(-1.0 / std::sqrt(sc->dp.P));
+    C.part = g.part; C.nsplit = g.nsplit; C.work = nullptr;
+    return C;
+}
+
+// Pair launch of a wave: the single-batch kernel (constants in the parameter
+// bank) for one segment, the multi-job kernel otherwise.  cap bounds the
+// items taken (autotuner probes); UINT_MAX runs everything.
+int launch_pairs(const std::vector<Seg*>& ps, const PairArgs* d_jobs, const unsigned int* d_start,
+                 unsigned int* d_work, int cfg, int sms, cudaStream_t st) {
+    const size_t pair_smem = 2 * RP_CHUNK * sizeof(FacetRec) + (size_t)RP_WIN * RP_PAIR_THREADS * sizeof(float2);
+    if (ps.size() == 1) {
+        const Seg& g = *ps[0];
+        PairArgs P = seg_pair_args(g);
+        P.work = d_work;
+        void (*pk)(PairArgs) = pick_pair_kernel(g.deg, cfg);
+        RP_CUDA(cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem));
+        int occ = 0;
+        RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, RP_PAIR_THREADS, pair_smem));
+        const int64_t items = (int64_t)g.nb * P.tblocks * RP_PARTS;
+        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(occ, 1) * sms, items));
+        pk<<<grid, RP_PAIR_THREADS, pair_smem, st>>>(P);
+    } else {
+        auto mk = pick_multi(cfg);
+        RP_CUDA(cudaFuncSetAttribute(mk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem));
+        int occ = 0;
+        RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mk, RP_PAIR_THREADS, pair_smem));
+        int64_t items = 0;
+        for (const Seg* g : ps) items += (int64_t)g->nb * ((g->L.tstride + RP_PAIR_THREADS - 1) / RP_PAIR_THREADS) * RP_PARTS;
+        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(occ, 1) * sms, items));
+        mk<<<grid, RP_PAIR_THREADS, pair_smem, st>>>(d_jobs, d_start, (int)ps.size(), d_work);
+    }
+    RP_LAUNCHED();
+    return RP_OK;
+}
+
+// Zero the pair-stage outputs of a wave (T windows, work counter, flags).
+int zero_pairs(const std::vector<Seg*>& ps, unsigned int* d_work, cudaStream_t st) {
+    for (const Seg* g : ps) {
+        RP_CUDA(cudaMemsetAsync(g->T, 0, sizeof(C32) * RP_PARTS * g->nb * g->L.tstride * g->Wt, st));
+        RP_CUDA(cudaMemsetAsync(g->misc + 1, 0, sizeof(int) * 3, st));
+    }
+    RP_CUDA(cudaMemsetAsync(d_work, 0, sizeof(unsigned int), st));
+    return RP_OK;
+}
+
+// Choose the pair configuration of a wave: the tuned one, or probe all four
+// (each a full launch on this wave's items, outputs re-zeroed after).
+int choose_cfg(const std::vector<Seg*>& ps, const PairArgs* d_jobs, const unsigned int* d_start,
+               unsigned int* d_work, int sms, cudaStream_t st, int* cfg_out) {
+    const int multi = ps.size() > 1 ? 1 : 0;
+    const int deg = multi ? -1 : ps[0]->deg;
+    if (!autotune_on()) { *cfg_out = ps[0]->sc->pair_cfg; return RP_OK; }
+    int c = tuned_lookup(multi, deg);
+    if (c >= 0) { *cfg_out = c; return RP_OK; }
+    cudaEvent_t e0, e1;
+    RP_CUDA(cudaEventCreate(&e0));
+    RP_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bestc = ps[0]->sc->pair_cfg;
+    for (int k = 0; k < 4; ++k) {
+        int rc = zero_pairs(ps, d_work, st);
+        if (rc) return rc;
+        RP_CUDA(cudaEventRecord(e0, st));
+        rc = launch_pairs(ps, d_jobs, d_start, d_work, k, sms, st);
+        if (rc) return rc;
+        RP_CUDA(cudaEventRecord(e1, st));
+        RP_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        RP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) { best = ms; bestc = k; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    tuned_store(multi, deg, bestc);
+    *cfg_out = bestc;
+    return zero_pairs(ps, d_work, st);
+}
+
+int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
+    const int nseg = (int)segs.size();
+    const int sms = segs[0].sc->sm_count;
+    // ---- setup stage for every segment
+    {
+        ArenaPlan pl;
+        pl.take<int>(8 * (size_t)nseg);
+        size_t need = pl.off;
+        for (Seg& g : segs) need += seg_setup_bytes(g.sc, g.Lw);
+        int rc = ws->arena.reserve(need);
+        if (rc) return rc;
+    }
+    Arena& a = ws->arena;
+    a.reset();
+    int* misc_all = a.take<int>(8 * (size_t)nseg);
+    for (int i = 0; i < nseg; ++i) segs[i].misc = misc_all + 8 * i;
+    g_timer.mark(0, st);
+    RP_CUDA(cudaMemsetAsync(misc_all, 0, sizeof(int) * 8 * nseg, st));
+    for (Seg& g : segs) seg_setup(g, a, st);
+    RP_CUDA(cudaGetLastError());
+    std::vector<int> h_misc(8 * (size_t)nseg);
+    RP_CUDA(cudaMemcpyAsync(h_misc.data(), misc_all, sizeof(int) * 8 * nseg, cudaMemcpyDeviceToHost, st));
+    g_timer.mark(1, st);
+    RP_CUDA(cudaStreamSynchronize(st));
+    g_timer.collect(0, 1);
+    // ---- pair-stage buffers and job tables
+    std::vector<Seg*> ps, cs;
+    for (int i = 0; i < nseg; ++i) {
+        Seg& g = segs[i];
+        g.Wt = std::max(1, std::min(g.sc->nr, (h_misc[8 * i] + 3) & ~3));
+        g.L = fast_layout(g.sc, g.nb, g.tmax, g.Wt);
+        g.smem = use_smem_conv(g.sc);
+        g.nsplit = (int)conv_splits(g.L.tstride);
+        g.pairs = g.sc->nt > 0 && g.sc->nf > 0 && g.tmax > 0;
+        if (g.pairs) ps.push_back(&g);
+        if (g.pairs && g.smem) cs.push_back(&g);
+    }
+    {
+        size_t need = 1024 + (ps.size() + cs.size()) * (sizeof(PairArgs) + sizeof(ConvArgs) + 64);
+        for (Seg& g : segs) need += seg_pair_bytes(g.sc, g.L);
+        int rc = ws->arena2.reserve(need);
+        if (rc) return rc;
+    }
+    Arena& b = ws->arena2;
+    b.reset();
+    unsigned int* d_work = b.take<unsigned int>(4);
+    PairArgs* d_pjobs = b.take<PairArgs>(std::max<size_t>(ps.size(), 1));
+    unsigned int* d_pstart = b.take<unsigned int>(ps.size() + 1);
+    ConvArgs* d_cjobs = b.take<ConvArgs>(std::max<size_t>(cs.size(), 1));
+    unsigned int* d_cstart = b.take<unsigned int>(cs.size() + 1);
+    for (Seg& g : segs) {
+        g.T = b.take<C32>((size_t)RP_PARTS * g.nb * g.L.tstride * g.Wt);
+        if (g.smem) {
+            g.part = b.take<C32>((size_t)g.nb * g.nsplit * g.sc->nr);
+        } else {
+            g.Z = b.take<C32>((size_t)g.nb * g.L.tstride * g.sc->nr);
+            g.cscr = b.take<C32>((size_t)g.L.slots * g.L.slot);
+        }
+    }
+    RP_CUDA(cudaMemsetAsync(d_work, 0, sizeof(unsigned int) * 4, st));
+    for (Seg& g : segs)
+        RP_CUDA(cudaMemsetAsync(g.T, 0, sizeof(C32) * RP_PARTS * g.nb * g.L.tstride * g.Wt, st));
+    std::vector<PairArgs> hp;
+    std::vector<unsigned int> hps(1, 0u);
+    for (Seg* g : ps) {
+        hp.push_back(seg_pair_args(*g));
+        hps.push_back(hps.back() + (unsigned)(g->nb * hp.back().tblocks * RP_PARTS));
+    }
+    std::vector<ConvArgs> hc;
+    std::vector<unsigned int> hcs(1, 0u);
+    int max_nr = 1, maxM = 4;
+    size_t csm = 0;
+    for (Seg* g : cs) {
+        hc.push_back(seg_conv_args(*g));
+        hcs.push_back(hcs.back() + (unsigned)(g->nb * g->nsplit));
+        max_nr = std::max(max_nr, g->sc->nr);
+        maxM = std::max(maxM, g->sc->mS);
+        csm = std::max(csm, (size_t)(2 * g->sc->nr + g->sc->mS) * sizeof(Cplx<float>));
+    }
+    csm += (size_t)(maxM / 4) * sizeof(Cplx<float>);
+    if (!hp.empty()) {
+        RP_CUDA(cudaMemcpyAsync(d_pjobs, hp.data(), sizeof(PairArgs) * hp.size(), cudaMemcpyHostToDevice, st));
+        RP_CUDA(cudaMemcpyAsync(d_pstart, hps.data(), sizeof(unsigned int) * hps.size(), cudaMemcpyHostToDevice, st));
+    }
+    if (!hc.empty()) {
+        RP_CUDA(cudaMemcpyAsync(d_cjobs, hc.data(), sizeof(ConvArgs) * hc.size(), cudaMemcpyHostToDevice, st));
+        RP_CUDA(cudaMemcpyAsync(d_cstart, hcs.data(), sizeof(unsigned int) * hcs.size(), cudaMemcpyHostToDevice, st));
+    }
+    // ---- pair stage: one launch for the wave
+    if (!ps.empty()) {
+        int cfg = 0;
+        int rc = choose_cfg(ps, d_pjobs, d_pstart, d_work, sms, st, &cfg);
+        if (rc) return rc;
+        g_timer.mark(1, st);
+        rc = launch_pairs(ps, d_pjobs, d_pstart, d_work, cfg, sms, st);
+        if (rc) return rc;
+        ++g_timer.pair_launches;
+    } else {
+        g_timer.mark(1, st);
+    }
+    g_timer.mark(2, st);
+    // ---- range compression: one launch for the shared-memory segments, the
+    // global-scratch kernel per remaining segment
+    if (!cs.empty()) {
+        int rc = launch_conv32s(d_cjobs, d_cstart, (int)cs.size(), max_nr, maxM, csm, sms, hcs.back(),
+                                d_work + 1, st);
+        if (rc) return rc;
+    }
+    for (Seg* g : ps) {
+        if (g->smem) continue;
+        const rp_scene* sc = g->sc;
+        k_conv32<<<g->L.slots, 256, 0, st>>>(g->ntl, g->L.tstride, g->nb, g->bt0, g->T, g->Wt, g->Z,
+                                            (const C32*)sc->d_C2_32, plan_view32(sc->plan2), plan_view32(sc->planN),
+                                            sc->crop_K, sc->crop_all, sc->nr, (float)(-1.0 / std::sqrt(sc->dp.P)),
+                                            g->cscr, g->L.slot);
+        RP_LAUNCHED();
+    }
+    g_timer.mark(3, st);
+    // ---- surface compression and the final sums
+    for (Seg& g : segs) {
+        const rp_scene* sc = g.sc;
+        const int nr = sc->nr;
+        k_surf_conv32<<<g.nb, 256, 0, st>>>(g.acc, g.nill, g.vmax, sc->dp.disable_surface, nr,
+                                            (const C32*)sc->d_C1_32, plan_view32(sc->plan2), g.refl, g.sscr,
+                                            g.Lw.surf_slot);
+        RP_LAUNCHED();
+        if (g.smem) {
+            if (!g.pairs) RP_CUDA(cudaMemsetAsync(g.part, 0, sizeof(C32) * g.nb * g.nsplit * nr, st));
+            k_sum32s<<<dim3((nr + 255) / 256, g.nb), 256, 0, st>>>(g.nill, g.ntl, g.refl, g.part, g.nsplit, nr,
+                                                                  g.d_out, g.out64, (int)g.s0);
+        } else {
+            if (!g.pairs) RP_CUDA(cudaMemsetAsync(g.Z, 0, sizeof(C32) * g.nb * g.L.tstride * nr, st));
+            k_sum32<<<dim3((nr + 255) / 256, g.nb), 256, 0, st>>>(g.nill, g.ntl, g.L.tstride, g.refl, g.Z, nr,
+                                                                 g.d_out, g.out64, (int)g.s0);
+        }
+        RP_LAUNCHED();
+    }
+    g_timer.mark(4, st);
+    RP_CUDA(cudaGetLastError());
+    std::vector<std::vector<int>> cnt(nseg);
+    RP_CUDA(cudaMemcpyAsync(h_misc.data(), misc_all, sizeof(int) * 8 * nseg, cudaMemcpyDeviceToHost, st));
+    for (int i = 0; i < nseg; ++i) {
+        if (!segs[i].h_counts) continue;
+        cnt[i].resize(2 * (size_t)segs[i].nb);
+        RP_CUDA(cudaMemcpyAsync(cnt[i].data(), segs[i].nill, sizeof(int) * segs[i].nb, cudaMemcpyDeviceToHost, st));
+        RP_CUDA(cudaMemcpyAsync(cnt[i].data() + segs[i].nb, segs[i].ntl, sizeof(int) * segs[i].nb,
+                                cudaMemcpyDeviceToHost, st));
+    }
+    RP_CUDA(cudaStreamSynchronize(st));
+    g_timer.collect(1, 4);
+    for (int i = 0; i < nseg; ++i) {
+        if (h_misc[8 * i + 3]) { rp_set_error("fast form: a shared-memory stage wait timed out"); return RP_ERR_TIMEOUT; }
+        if (h_misc[8 * i + 2]) { rp_set_error("fast form: a pair fell outside its target's bin window"); return RP_ERR_INTERNAL; }
+    }
+    for (int i = 0; i < nseg; ++i) {
+        const Seg& g = segs[i];
+        if (!g.h_counts) continue;
+        for (int k = 0; k < g.nb; ++k) {
+            g.h_counts[2 * (g.s0 + k)] = cnt[i][k];
+            g.h_counts[2 * (g.s0 + k) + 1] = cnt[i][g.nb + k];
+        }
+    }
+    return RP_OK;
+}
+
+std::vector<int> host_target_bounds(const rp_scene* sc, const double* tr, int64_t ns) {
+    std::vector<int> ub(ns, 0);
+    const int64_t nt = sc->nt;
+    const double* tg = sc->h_targets.data();
+    const double ap = sc->dp.ap_rad + 1e-9;
+    for (int64_t s = 0; s < ns; ++s) {
+        const double* r = tr + 9 * s;
+        int c = 0;
+        for (int64_t i = 0; i < nt; ++i) {
+            double vx = tg[i] - r[0], vy = tg[nt + i] - r[1], vz = tg[2 * nt + i] - r[2];
+            double m = std::sqrt(vx * vx + vy * vy + vz * vz);
+            double cs = -r[3] * vx / m - r[4] * vy / m - r[5] * vz / m;
+            cs = std::max(-1.0, std::min(1.0, cs));
+            if (!(std::acos(cs) > ap)) ++c;
+        }
+        ub[s] = c;
+    }
+    return ub;
+}
+
+int check_scene(const rp_scene* sc) {
+    if (sc->any_ttype0) {
+        rp_set_error("fast form: ttype-0 targets are handled by the plain form only");
+        return RP_ERR_UNSUPPORTED;
+    }
+    if (sc->planN.pow2) { rp_set_error("internal: N = 2 nr - 1 is a power of two"); return RP_ERR_INTERNAL; }
+    return RP_OK;
 }
 
 }  // namespace
 
 size_t rp_fast_scratch(const rp_scene* sc, int64_t ns) {
     FastLayout L = fast_layout(sc, (int)std::max<int64_t>(1, std::min<int64_t>(ns, 16)), sc->nt, sc->nr);
-    ArenaPlan a;
-    fast_take_setup(a, sc, L);
-    fast_take_pairs(a, sc, L);
-    return a.off;
+    return seg_setup_bytes(sc, L) + seg_pair_bytes(sc, L) + 4096;
+}
+
+// Splits every job into segments (<= 64 traces, scratch within the budget)
+// and packs consecutive segments into waves under the same budget.
+int rp_fast_batch(const rp_job* jobs, int njobs, rp_workspace* ws, cudaStream_t st) {
+    std::vector<SceneConst> kc(njobs);
+    std::vector<std::vector<double>> tr(njobs);
+    for (int j = 0; j < njobs; ++j) {
+        int rc = check_scene(jobs[j].scene);
+        if (rc) return rc;
+        kc[j] = scene_const(jobs[j].scene);
+        tr[j].resize(9 * (size_t)jobs[j].ns);
+        if (jobs[j].ns)
+            RP_CUDA(cudaMemcpyAsync(tr[j].data(), jobs[j].d_traces, sizeof(double) * 9 * jobs[j].ns,
+                                    cudaMemcpyDeviceToHost, st));
+    }
+    RP_CUDA(cudaStreamSynchronize(st));
+    std::vector<Seg> wave;
+    size_t wave_bytes = 0;
+    for (int j = 0; j < njobs; ++j) {
+        rp_scene* sc = jobs[j].scene;
+        const int64_t ns = jobs[j].ns;
+        const int nr = sc->nr;
+        std::vector<int> ub = host_target_bounds(sc, tr[j].data(), ns);
+        for (int64_t s0 = 0; s0 < ns;) {
+            int nb = 0;
+            int64_t tmax = 0;
+            size_t bytes = 0;
+            for (;;) {
+                if (s0 + nb >= ns) break;
+                const int64_t t2 = std::max<int64_t>(tmax, ub[s0 + nb]);
+                const FastLayout L = fast_layout(sc, nb + 1, t2, nr);
+                const size_t b2 = seg_setup_bytes(sc, L) + seg_pair_bytes(sc, L);
+                if (nb > 0 && b2 > kFastBudget) break;
+                tmax = t2;
+                bytes = b2;
+                ++nb;
+                if (nb >= 64) break;
+            }
+            if (!wave.empty() && wave_bytes + bytes > kFastBudget) {
+                int rc = run_wave(wave, ws, st);
+                if (rc) return rc;
+                wave.clear();
+                wave_bytes = 0;
+            }
+            Seg g;
+            g.sc = sc;
+            g.trb = jobs[j].d_traces + 9 * s0;
+            g.s0 = s0;
+            g.nb = nb;
+            g.tmax = tmax;
+            g.d_out = jobs[j].d_out;
+            g.out64 = 0;
+            g.h_counts = jobs[j].counts;
+            g.deg = kc[j].deg;
+            g.coef = kc[j].coef;
+            g.Lw = fast_layout(sc, nb, tmax, nr);
+            wave.push_back(g);
+            wave_bytes += bytes;
+            s0 += nb;
+        }
+    }
+    if (!wave.empty()) {
+        int rc = run_wave(wave, ws, st);
+        if (rc) return rc;
+    }
+    return RP_OK;
 }
 
 int rp_fast_run(rp_scene* sc, rp_workspace* ws, const double* d_traces, int64_t ns, void* d_out, int out64,
                 int64_t* h_counts, cudaStream_t st) {
-    const int64_t nf = sc->nf, nt = sc->nt;
-    const int nr = sc->nr;
-    if (sc->any_ttype0) {
-        rp_set_error("fast form: ttype-0 targets are handled by the plain form only");
-        return RP_ERR_UNSUPPORTED;
+    int rc = check_scene(sc);
+    if (rc) return rc;
+    if (!out64) {
+        rp_job j{sc, d_traces, ns, d_out, h_counts};
+        return rp_fast_batch(&j, 1, ws, st);
     }
-    if (sc->planN.pow2) { rp_set_error("internal: N = 2 nr - 1 is a power of two"); return RP_ERR_INTERNAL; }
-    std::vector<double> tr(9 * ns), tg(7 * nt);
+    // complex128 output: same batches, out64 set on every segment
+    std::vector<double> tr(9 * (size_t)ns);
     RP_CUDA(cudaMemcpyAsync(tr.data(), d_traces, sizeof(double) * 9 * ns, cudaMemcpyDeviceToHost, st));
-    if (nt) RP_CUDA(cudaMemcpyAsync(tg.data(), sc->d_targets, sizeof(double) * 7 * nt, cudaMemcpyDeviceToHost, st));
     RP_CUDA(cudaStreamSynchronize(st));
-    std::vector<int> ub = host_target_bounds32(sc, tr, ns, tg);
-    PlanV<float> p2 = plan_view32(sc->plan2), pN = plan_view32(sc->planN);
-    const DevParams& dp = sc->dp;
-    const size_t pair_smem = 2 * RP_CHUNK * sizeof(FacetRec) + (size_t)RP_WIN * RP_PAIR_THREADS * sizeof(float2);
-    // sinc evaluation: polynomial degree for |a| <= pik (0 = special-function unit)
-    const double pik_d = RP_PI * (RP_PI_F * dp.fs / dp.lam);
-    const int deg = sinc_degree(pik_d, sc->pair_variant);
-    double coef[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    if (deg > 0) sinc_poly(pik_d * pik_d, deg, coef);
-    void (*pk)(PairArgs) = pick_pair_kernel(deg, sc->pair_cfg);
-    RP_CUDA(cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem));
-    int occ = 0;
-    RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, RP_PAIR_THREADS, pair_smem));
-    occ = std::max(occ, 1);
+    std::vector<int> ub = host_target_bounds(sc, tr.data(), ns);
+    const SceneConst kc = scene_const(sc);
     for (int64_t s0 = 0; s0 < ns;) {
         int nb = 0;
         int64_t tmax = 0;
         for (;;) {
             if (s0 + nb >= ns) break;
-            int64_t t2 = std::max<int64_t>(tmax, ub[s0 + nb]);
-            FastLayout L = fast_layout(sc, nb + 1, t2, nr);
-            ArenaPlan a;
-            fast_take_setup(a, sc, L);
-            fast_take_pairs(a, sc, L);
-            if (nb > 0 && a.off > kFastBudget) break;
+            const int64_t t2 = std::max<int64_t>(tmax, ub[s0 + nb]);
+            const FastLayout L = fast_layout(sc, nb + 1, t2, sc->nr);
+            if (nb > 0 && seg_setup_bytes(sc, L) + seg_pair_bytes(sc, L) > kFastBudget) break;
             tmax = t2;
             ++nb;
             if (nb >= 64) break;
         }
-        FastLayout Lw = fast_layout(sc, nb, tmax, nr);
-        {
-            ArenaPlan a;
-            fast_take_setup(a, sc, Lw);
-            int rc = ws->arena.reserve(a.off);
-            if (rc) return rc;
-        }
-        Arena& a = ws->arena;
-        a.reset();
-        const int64_t nfa = std::max<int64_t>(nf, 1), nta = std::max<int64_t>(nt, 1);
-        const int tiles = (int)((std::max(nfa, nta) + RP_TILE - 1) / RP_TILE);
-        uint8_t* fflags = a.take<uint8_t>((size_t)nb * nfa);
-        int* tcnt = a.take<int>((size_t)nb * tiles);
-        int* d_nill = a.take<int>(nb);
-        int* d_ntl = a.take<int>(nb);
-        unsigned long long* vmax = a.take<unsigned long long>(nb);
-        unsigned long long* dmin = a.take<unsigned long long>(nb);
-        int* idx = a.take<int>((size_t)nb * nfa);
-        FacetRec* rec = a.take<FacetRec>((size_t)nb * Lw.rstride);
-        ChunkMeta* meta = a.take<ChunkMeta>((size_t)nb * Lw.mstride);
-        float* sxv = a.take<float>((size_t)nb * nfa);
-        C32* sv = a.take<C32>((size_t)nb * nfa);
-        TraceMeta* tm = a.take<TraceMeta>(nb);
-        uint8_t* tflags = a.take<uint8_t>((size_t)nb * nta);
-        int* tlist = a.take<int>((size_t)nb * nta);
-        int* bt0 = a.take<int>((size_t)nb * Lw.tstride);
-        int* misc = a.take<int>(8);
-        long long* acc = a.take<long long>((size_t)nb * nr * 2);
-        C32* refl = a.take<C32>((size_t)nb * nr);
-        C32* sscr = a.take<C32>((size_t)nb * Lw.surf_slot);
-        const double* trb = d_traces + 9 * s0;
-
-        g_timer.mark(0, st);
-        RP_CUDA(cudaMemsetAsync(vmax, 0, sizeof(unsigned long long) * nb, st));
-        RP_CUDA(cudaMemsetAsync(dmin, 0xff, sizeof(unsigned long long) * nb, st));
-        RP_CUDA(cudaMemsetAsync(acc, 0, sizeof(long long) * nb * nr * 2, st));
-        RP_CUDA(cudaMemsetAsync(misc, 0, sizeof(int) * 8, st));
-        if (nf > 0) {
-            k_cull_count<<<dim3((unsigned)((nf + RP_TILE - 1) / RP_TILE), nb), RP_TILE_THREADS, 0, st>>>(
-                sc->d_sorted, nf, trb, dp.ap_rad, fflags, tcnt, dmin);
-            RP_LAUNCHED();
-            compact_flags(fflags, nf, nb, tcnt, d_nill, idx, nfa, true, st);
-            k_facets32<<<dim3((unsigned)Lw.mstride, nb), RP_CHUNK, 0, st>>>(
-                sc->d_sorted, nfa, idx, d_nill, trb, dp, rec, meta, Lw.rstride, Lw.mstride, sxv, sv, vmax);
-            RP_LAUNCHED();
-            k_surf_fix32<<<dim3((unsigned)((nf + 256 * RP_SFIX_PER - 1) / (256 * RP_SFIX_PER)), nb), 256, 0, st>>>(
-                nfa, d_nill, sxv, sv, vmax, nr, acc);
-            RP_LAUNCHED();
-            k_tmeta32<<<nb, 256, 0, st>>>(meta, Lw.mstride, d_nill, tm);
-            RP_LAUNCHED();
-        } else {
-            RP_CUDA(cudaMemsetAsync(d_nill, 0, sizeof(int) * nb, st));
-        }
-        if (nt > 0) {
-            k_target_flags<<<dim3((unsigned)((nt + 255) / 256), nb), 256, 0, st>>>(sc->d_targets, nt, trb,
-                                                                                dp.ap_rad, tflags);
-            RP_LAUNCHED();
-            compact_flags(tflags, nt, nb, tcnt, d_ntl, tlist, Lw.tstride, false, st);
-            if (nf > 0) {
-                k_tsetup32<<<dim3((unsigned)((Lw.tstride + 255) / 256), nb), 256, 0, st>>>(
-                    sc->d_targets, nt, tlist, d_ntl, Lw.tstride, tm, d_nill, dp, bt0, misc);
-                RP_LAUNCHED();
-            }
-        } else {
-            RP_CUDA(cudaMemsetAsync(d_ntl, 0, sizeof(int) * nb, st));
-        }
-        int h_maxw = 0;
-        RP_CUDA(cudaMemcpyAsync(&h_maxw, misc, sizeof(int), cudaMemcpyDeviceToHost, st));
-        g_timer.mark(1, st);
-        RP_CUDA(cudaStreamSynchronize(st));
-        g_timer.collect(0, 1);
-        const int Wt = std::max(1, std::min(nr, (h_maxw + 3) & ~3));
-        FastLayout L = fast_layout(sc, nb, tmax, Wt);
-        {
-            ArenaPlan a2;
-            fast_take_pairs(a2, sc, L);
-            int rc = ws->arena2.reserve(a2.off);
-            if (rc) return rc;
-        }
-        Arena& b = ws->arena2;
-        b.reset();
-        const bool smem_conv = use_smem_conv(sc);
-        const int nsplit = (int)conv_splits(L.tstride);
-        C32* T = b.take<C32>((size_t)RP_PARTS * nb * L.tstride * Wt);
-        C32* Z = nullptr;
-        C32* cscr = nullptr;
-        C32* part = nullptr;
-        if (smem_conv) {
-            part = b.take<C32>((size_t)nb * nsplit * nr);
-        } else {
-            Z = b.take<C32>((size_t)nb * L.tstride * nr);
-            cscr = b.take<C32>((size_t)L.slots * L.slot);
-        }
-        RP_CUDA(cudaMemsetAsync(T, 0, sizeof(C32) * RP_PARTS * nb * L.tstride * Wt, st));
-        g_timer.mark(1, st);
-        if (nt > 0 && nf > 0 && tmax > 0) {
-            PairArgs P;
-            P.rec = rec; P.meta = meta; P.rstride = Lw.rstride; P.mstride = Lw.mstride;
-            P.nill = d_nill; P.ntl = d_ntl; P.tlist = tlist; P.tstride = L.tstride;
-            P.TG = sc->d_targets; P.nt = nt; P.PR = sc->d_prisms; P.np = sc->np;
-            P.bt0 = bt0; P.T = T; P.Wt = Wt; P.nb = nb;
-            P.tblocks = (int)((L.tstride + RP_PAIR_THREADS - 1) / RP_PAIR_THREADS);
-            P.work = reinterpret_cast<unsigned int*>(misc + 1);
-            P.err = reinterpret_cast<unsigned int*>(misc + 2);
-            P.nr_f = (float)nr; P.nr = nr; P.nr1 = nr - 1;
-            P.kb = (float)(dp.nidx / dp.dr);
-            P.kt = (float)(dp.nidx * dp.turn);
-            P.pik = (float)(RP_PI * (RP_PI_F * dp.fs / dp.lam));
-            P.pik2 = P.pik * P.pik;
-            for (int k = 0; k < 8; ++k) P.sc[k] = (float)coef[k];
-            P.ealpha = dp.lossless ? 0.f : (float)(-2.0 * dp.alpha2 * 1.4426950408889634);
-            P.eks = dp.lossless ? 0.f : (float)(-2.0 * dp.ks * dp.ks * 1.4426950408889634);
-            P.nidx = dp.nidx; P.inv_dr = 1.0 / dp.dr; P.inv_lam = dp.turn;
-            P.lossless = dp.lossless;
-            int grid = std::min(occ * sc->sm_count, nb * P.tblocks * RP_PARTS);
-            pk<<<grid, RP_PAIR_THREADS, pair_smem, st>>>(P);
-            RP_LAUNCHED();
-            ++g_timer.pair_launches;
-            g_timer.mark(2, st);
-            const float sig_scale = (float)(-1.0 / std::sqrt(dp.P));
-            if (smem_conv) {
-                ConvArgs C;
-                C.ntl = d_ntl; C.tstride = L.tstride; C.nb = nb; C.bt0 = bt0; C.T = T; C.Wt = Wt;
-                C.tw = (const Cplx<float>*)sc->d_twS; C.log2M = sc->log2mS;
-                C.C2s = (const Cplx<float>*)sc->d_C2S; C.bWs = (const Cplx<float>*)sc->d_bWS;
-                C.bWis = (const Cplx<float>*)sc->d_bWiS; C.bw = (const Cplx<float>*)sc->planN.bw32;
-                C.nr = nr; C.n2 = 2 * nr; C.N = 2 * nr - 1; C.M = sc->mS;
-                C.crop_K = sc->crop_K; C.crop_all = sc->crop_all; C.sig_scale = sig_scale;
-                C.part = part; C.nsplit = nsplit; C.work = reinterpret_cast<unsigned int*>(misc + 4);
-                const size_t csm = (size_t)(C.n2 + C.M + C.M / 4) * sizeof(Cplx<float>);
-                int rc2 = launch_conv32s(C, csm, sc->sm_count, nb * nsplit, st);
-                if (rc2) return rc2;
-            } else {
-                k_conv32<<<L.slots, 256, 0, st>>>(d_ntl, L.tstride, nb, bt0, T, Wt, Z, (const C32*)sc->d_C2_32,
-                                                 p2, pN, sc->crop_K, sc->crop_all, nr, sig_scale, cscr, L.slot);
-                RP_LAUNCHED();
-            }
-        }
-        if (!(nt > 0 && nf > 0 && tmax > 0)) g_timer.mark(2, st);
-        g_timer.mark(3, st);
-        k_surf_conv32<<<nb, 256, 0, st>>>(acc, d_nill, vmax, dp.disable_surface, nr, (const C32*)sc->d_C1_32, p2,
-                                         refl, sscr, Lw.surf_slot);
-        RP_LAUNCHED();
-        if (smem_conv) {
-            if (!(nt > 0 && nf > 0 && tmax > 0)) RP_CUDA(cudaMemsetAsync(part, 0, sizeof(C32) * nb * nsplit * nr, st));
-            k_sum32s<<<dim3((nr + 255) / 256, nb), 256, 0, st>>>(d_nill, d_ntl, refl, part, nsplit, nr, d_out,
-                                                                out64, (int)s0);
-        } else {
-            k_sum32<<<dim3((nr + 255) / 256, nb), 256, 0, st>>>(d_nill, d_ntl, L.tstride, refl, Z, nr, d_out,
-                                                               out64, (int)s0);
-        }
-        RP_LAUNCHED();
-        g_timer.mark(4, st);
-        RP_CUDA(cudaGetLastError());
-        unsigned int herr[2] = {0, 0};
-        std::vector<int> a1(nb), a2(nb);
-        RP_CUDA(cudaMemcpyAsync(herr, misc + 2, sizeof(herr), cudaMemcpyDeviceToHost, st));
-        RP_CUDA(cudaMemcpyAsync(a1.data(), d_nill, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
-        RP_CUDA(cudaMemcpyAsync(a2.data(), d_ntl, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
-        RP_CUDA(cudaStreamSynchronize(st));
-        g_timer.collect(1, 4);
-        if (herr[1]) { rp_set_error("fast form: a shared-memory stage wait timed out"); return RP_ERR_TIMEOUT; }
-        if (herr[0]) { rp_set_error("fast form: a pair fell outside its target's bin window"); return RP_ERR_INTERNAL; }
-        if (h_counts)
-            for (int k = 0; k < nb; ++k) {
-                h_counts[2 * (s0 + k)] = a1[k];
-                h_counts[2 * (s0 + k) + 1] = a2[k];
-            }
+        std::vector<Seg> w(1);
+        Seg& g = w[0];
+        g.sc = sc; g.trb = d_traces + 9 * s0; g.s0 = s0; g.nb = nb; g.tmax = tmax;
+        g.d_out = d_out; g.out64 = 1; g.h_counts = h_counts; g.deg = kc.deg; g.coef = kc.coef;
+        g.Lw = fast_layout(sc, nb, tmax, sc->nr);
+        rc = run_wave(w, ws, st);
+        if (rc) return rc;
         s0 += nb;
     }
+    return RP_OK;
+}
+
+extern "C" int rp_autotune(int enable) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_autotune = enable ? 1 : 0;
+    return RP_OK;
+}
+
+extern "C" int rp_autotune_query(int multi, int degree, int* cfg) {
+    if (!cfg) { rp_set_error("rp_autotune_query: null cfg"); return RP_ERR_ARG; }
+    *cfg = tuned_lookup(multi ? 1 : 0, multi ? -1 : degree);
     return RP_OK;
 }

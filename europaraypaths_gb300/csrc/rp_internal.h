@@ -95,6 +95,7 @@ struct rp_scene {
     // ---- targets FP64 SoA [7][nt], prisms FP64 SoA [7][np]
     double* d_targets = nullptr;
     double* d_prisms = nullptr;
+    std::vector<double> h_targets;       // host copy of the targets (aperture bounds)
     int any_ttype0 = 0;
     // ---- fast store: spatially sorted facets
     int64_t* d_order = nullptr;          // sorted position -> original index
@@ -114,8 +115,7 @@ struct rp_scene {
     int mS = 0, log2mS = 0;              // M = 4 nr
     float* d_twS = nullptr;              // e^{-2 pi i k / M}, k < M
     float* d_C2S = nullptr;              // DIF_2nr(target chirp)
-    float* d_bWS = nullptr;              // DIF_M(conj Bluestein chirp)
-    float* d_bWiS = nullptr;             // DIF_M(Bluestein chirp)
+    float* d_HS = nullptr;               // DIF_M(crop kernel h) / M
     // ---- tuning
     int pair_variant = 0;                // 0 auto (polynomial sinc where accurate), 1 special-function sinc
     int pair_cfg = 1;                    // pair-kernel (ILP, blocks/SM) configuration (1: 2 x 2)
@@ -154,5 +154,6 @@ int rp_plain_run(rp_scene* s, rp_workspace* ws, const double* d_traces, int64_t 
                  int out64, int64_t* h_counts, cudaStream_t st);
 int rp_fast_run(rp_scene* s, rp_workspace* ws, const double* d_traces, int64_t ns, void* d_out,
                 int out64, int64_t* h_counts, cudaStream_t st);
+int rp_fast_batch(const rp_job* jobs, int njobs, rp_workspace* ws, cudaStream_t st);
 size_t rp_plain_scratch(const rp_scene* s, int64_t ns);
 size_t rp_fast_scratch(const rp_scene* s, int64_t ns);

@@ -135,3 +135,47 @@ def large_scene(seed=2, n_facets_side=2000, n_targets_side=200, ns=2000):
     th = gaussian_field(n_targets_side, n_targets_side, tfs, 10.0, 200.0, seed + 1000)
     targets = ss.target_arrays(tdom, "flat", zoffset=-1500.0, heights=th)
     return {"name": "large_scene", "params": p, "facets": facets, "targets": targets}
+
+
+def uneven_batch(seed=3, n_scenes=64, min_facets=10_000, max_facets=4_000_000, alt=25e3):
+    """Many independent scenes of uneven size (the batched-scenes workload).
+
+    Per scene (all drawn from ``default_rng(seed)``):
+    * facet count log-uniform in [min_facets, max_facets] (a square grid);
+    * band: 9 MHz / 1 MHz chirp sampled at 4 MHz with fs = 10 m, or 60 MHz /
+      10 MHz sampled at 24 MHz with fs = 2.5 m (equal odds);
+    * bins: 2048, 4096 or 8192;
+    * surface: Gaussian field, RMS U(1, 10) m, l = 50 m;
+    * one or two target layers at U(0.5, 3) km depth, 50 m sampling, each a
+      Gaussian interface (RMS 5 m, l = 200 m), eps 3.15, sigma 1e-6;
+    * trace count U{50..2000}, linear along x across the scene at 25 km,
+      aperture 3 deg.
+    Returns a list of scene dictionaries (name, params, facets, targets)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_scenes):
+        nfac = float(np.exp(rng.uniform(np.log(min_facets), np.log(max_facets))))
+        n_side = max(8, int(round(np.sqrt(nfac))))
+        vhf = bool(rng.integers(0, 2))
+        f0, B, smpl, fs, gain = (60e6, 10e6, 24e6, 2.5, 7.3) if vhf else (9e6, 1e6, 4e6, 10.0, 4.0)
+        nr = int(rng.choice([2048, 4096, 8192]))
+        rms = float(rng.uniform(1.0, 10.0))
+        nlay = int(rng.integers(1, 3))
+        depths = sorted(float(d) for d in rng.uniform(500.0, 3000.0, nlay))
+        ns = int(rng.integers(50, 2001))
+        side = n_side * fs
+        sdx = side / ns
+        p = base_params(f0, B, smpl, nr, 3.0, 3.15, 1e-6, rms, fs, alt, ns, sdx, gain)
+        dom = {"fs": fs, "nx": n_side, "ny": n_side, "ox": -side / 2, "oy": -side / 2}
+        h = gaussian_field(n_side, n_side, fs, rms, 50.0, seed * 1000 + i)
+        facets = ss.surface_arrays(dom, "flat", heights=h)
+        tn = max(1, int(side // 50.0))
+        tdom = {"fs": 50.0, "nx": tn, "ny": tn, "ox": -tn * 25.0, "oy": -tn * 25.0}
+        layers = []
+        for k, d in enumerate(depths):
+            th = gaussian_field(tn, tn, 50.0, 5.0, 200.0, seed * 1000 + 500 + 2 * i + k)
+            layers.append(ss.target_arrays(tdom, "flat", zoffset=-d, heights=th))
+        targets = np.concatenate(layers, axis=1)
+        out.append({"name": f"uneven_{i}", "params": p, "facets": facets, "targets": targets,
+                    "band": "60/10 MHz" if vhf else "9/1 MHz", "layers": nlay})
+    return out

@@ -82,6 +82,9 @@ class GpuEngine:
         self.scenes[sid] = Scene(params, facets, targets, prisms=prisms, device=self.device)
         return self.scenes[sid].footprint()
 
+    def adopt_scene(self, sid, scene):
+        self.scenes[sid] = scene
+
     def remove_scene(self, sid):
         self.scenes.pop(sid).close()
 
@@ -147,6 +150,14 @@ class Server:
             sid = self.next_scene
             self.next_scene += 1
         self.engine.add_scene(sid, params, facets, targets, prisms)
+        return sid
+
+    def adopt_scene(self, scene):
+        """Serve an existing resident Scene (the caller keeps ownership)."""
+        with self.cv:
+            sid = self.next_scene
+            self.next_scene += 1
+        self.engine.adopt_scene(sid, scene)
         return sid
 
     def remove_scene(self, sid):
@@ -239,7 +250,9 @@ class Server:
                     raise TimeoutError("drain timed out")
                 self.cv.wait(0.05 if left is None else min(0.05, left))
 
-    def close(self):
+    def close(self, keep_scenes=False):
+        """Drain, stop the dispatcher and free the slots (and, unless
+        keep_scenes, the scenes)."""
         self.drain()
         with self.cv:
             self.closed = True
@@ -247,5 +260,6 @@ class Server:
         self.dispatcher.join(timeout=5)
         for s in self.slots:
             self.engine.close_slot(s)
-        for sid in list(getattr(self.engine, "scenes", {}).keys()):
-            self.engine.remove_scene(sid)
+        if not keep_scenes:
+            for sid in list(getattr(self.engine, "scenes", {}).keys()):
+                self.engine.remove_scene(sid)

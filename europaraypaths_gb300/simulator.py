@@ -52,6 +52,7 @@ class Scene:
             prisms = np.zeros((7, 0))
         self.prisms = np.ascontiguousarray(prisms, dtype=np.float64).reshape(7, -1)
         self.nr = int(self.params.nr)
+        self.device = int(device)
         self._h = ctypes.c_void_p()
         lib = _abi.lib()
         rc = lib.rp_scene_create(ctypes.byref(self.params), self.facets.ctypes.data,
@@ -155,3 +156,75 @@ def simulate(params, facets, targets=None, traces=None, form="fast", prisms=None
     """One-shot simulation; returns the complex64 radargram (nr, ns)."""
     with Scene(params, facets, targets, prisms, device) as sc:
         return sc.simulate(traces, form=form).T
+
+
+class Workspace:
+    """Device scratch for calls on one stream (rp_workspace)."""
+
+    def __init__(self, device=0):
+        self.device = device
+        self._h = ctypes.c_void_p()
+        _abi.check("rp_workspace_create", _abi.lib().rp_workspace_create(int(device), ctypes.byref(self._h)))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def bytes(self):
+        b = ctypes.c_int64()
+        _abi.check("rp_workspace_bytes", _abi.lib().rp_workspace_bytes(self._h, ctypes.byref(b)))
+        return b.value
+
+    def close(self):
+        if self._h and self._h.value:
+            _abi.lib().rp_workspace_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def simulate_batch(jobs, workspace=None, stream=None, return_counts=False):
+    """Fast form over many scenes in one call (rp_simulate_batch).
+
+    ``jobs``: a list of (Scene, traces (ns, 9)) pairs, scenes of any sizes and
+    bands on one device.  The pair stage of all of them runs as one persistent
+    launch.  Returns one complex64 (ns, nr) array per job (and the (ns, 2)
+    counts per job with ``return_counts``)."""
+    import torch
+    if not jobs:
+        return []
+    dev = jobs[0][0].device
+    ws = workspace if workspace is not None else Workspace(dev)
+    d_tr, d_out, counts = [], [], []
+    arr = (_abi.RpJob * len(jobs))()
+    for i, (sc, tr) in enumerate(jobs):
+        tr = np.ascontiguousarray(tr, dtype=np.float64).reshape(-1, 9)
+        t = torch.from_numpy(tr).to(f"cuda:{dev}")
+        o = torch.empty((tr.shape[0], sc.nr), dtype=torch.complex64, device=f"cuda:{dev}")
+        c = np.zeros((tr.shape[0], 2), np.int64)
+        d_tr.append(t)
+        d_out.append(o)
+        counts.append(c)
+        arr[i] = _abi.RpJob(sc.handle, t.data_ptr(), tr.shape[0], o.data_ptr(), c.ctypes.data)
+    st = torch.cuda.current_stream(dev) if stream is None else stream
+    torch.cuda.synchronize(dev)
+    rc = _abi.lib().rp_simulate_batch(arr, len(jobs), ws.handle, ctypes.c_void_p(st.cuda_stream))
+    _abi.check("rp_simulate_batch", rc)
+    outs = [o.cpu().numpy() for o in d_out]
+    return (outs, counts) if return_counts else outs
+
+
+def autotune(enable=True):
+    """Switch the pair-kernel autotuner on or off (rp_autotune)."""
+    _abi.lib().rp_autotune(1 if enable else 0)
+
+
+def autotune_query(multi, degree=0):
+    """The tuned pair-kernel configuration (0-3) or -1 when not tuned yet."""
+    c = ctypes.c_int()
+    _abi.check("rp_autotune_query", _abi.lib().rp_autotune_query(int(bool(multi)), int(degree), ctypes.byref(c)))
+    return c.value

@@ -171,6 +171,35 @@ int rp_workspace_bytes(const rp_workspace* ws, int64_t* bytes);
 int rp_simulate_ws(rp_scene* s, rp_workspace* ws, const double* d_traces, int64_t ns, int form,
                    void* d_out, int64_t* counts, void* stream);
 
+/* One scene's share of a batch: its trace table and radargram in device
+ * memory, counts (ns x 2: N_ill, N_t) in host memory or NULL. */
+typedef struct rp_job {
+    rp_scene* scene;
+    const double* d_traces;   /* ns x 9 float64 */
+    int64_t ns;
+    void* d_out;              /* ns x nr complex64 */
+    int64_t* counts;
+} rp_job;
+
+/* Fast form over many scenes at once (uneven facet, target, trace and bin
+ * counts, different radar bands): the pair stage of every scene runs in ONE
+ * persistent kernel launch (a job table over all scenes' work items), range
+ * compression in one launch per bin-count class.  No counterpart in the
+ * reference, which runs one scene per process (sim.cu:615-1008); each
+ * trace's result is bitwise the one rp_simulate_ws gives.  Every scene must
+ * live on the workspace's device. */
+int rp_simulate_batch(const rp_job* jobs, int njobs, rp_workspace* ws, void* stream);
+
+/* Pair-kernel autotuner.  With tuning on (the default unless RP_PAIR_CFG
+ * fixes a configuration), the first pair launch of each kind (single-scene
+ * kernel per sinc degree, or the multi-scene kernel) times the kernel's
+ * configurations (facets per step x resident blocks per SM) on a bounded
+ * sample of its work items and keeps the fastest for the process.  The
+ * configurations give bitwise identical results. */
+int rp_autotune(int enable);
+/* The tuned configuration for (multi, degree), or -1 when not tuned yet. */
+int rp_autotune_query(int multi, int degree, int* cfg);
+
 /* Number of kernel launches issued by this thread's last rp_simulate*. */
 int rp_last_launch_count(int64_t* launches);
 

@@ -32,6 +32,9 @@ class FakeEngine:
     def add_scene(self, sid, params, facets, targets, prisms):
         self.scenes[sid] = int(params["nr"])
 
+    def adopt_scene(self, sid, scene):
+        self.scenes[sid] = int(scene["nr"])
+
     def remove_scene(self, sid):
         self.scenes.pop(sid)
 
@@ -167,6 +170,16 @@ def test_cancel_queued():
     first.result(timeout=5)
     srv.close()
     assert second.id not in eng.started
+
+
+def test_adopted_scene_survives_close():
+    from europaraypaths_gb300.serving import Server
+    eng = FakeEngine(delay=0.001)
+    srv = Server(engine=eng, workers=2, mem_budget=10 ** 6)
+    sid = srv.adopt_scene({"nr": 6})
+    assert srv.submit(sid, _traces(2, 5)).result(timeout=5).shape == (2, 6)
+    srv.close(keep_scenes=True)
+    assert sid in eng.scenes
 
 
 @pytest.mark.gpu
