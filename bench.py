@@ -471,11 +471,17 @@ def main():
             scene.close()
             specs, objs, tracks, t_build = batch_workload(args, local)
             if args.batch_scenes > 0:
-                line["batch"] = run_batch(args, objs, tracks, stream)
-                line["batch"]["setup_s"] = t_build
+                try:
+                    line["batch"] = run_batch(args, objs, tracks, stream)
+                    line["batch"]["setup_s"] = t_build
+                except Exception as e:       # reported in the line; the headline stands
+                    line["batch"] = {"error": f"{type(e).__name__}: {e}"}
             if args.serve_seconds > 0:
                 plain = line.get("plain_form", {}).get("value")
-                line["serving"] = run_serving(args, objs, tracks, plain)
+                try:
+                    line["serving"] = run_serving(args, objs, tracks, plain)
+                except Exception as e:
+                    line["serving"] = {"error": f"{type(e).__name__}: {e}"}
             for o in objs:
                 o.close()
         print(json.dumps(line), flush=True)

@@ -17,7 +17,7 @@ RP_FORM_FAST_F32 = 1
 ERRORS = {
     -1: "RP_ERR_ARG", -2: "RP_ERR_IO", -3: "RP_ERR_PARSE", -4: "RP_ERR_CUDA",
     -5: "RP_ERR_NOMEM", -6: "RP_ERR_UNSUPPORTED", -7: "RP_ERR_BUDGET",
-    -8: "RP_ERR_TIMEOUT", -9: "RP_ERR_INTERNAL",
+    -8: "RP_ERR_TIMEOUT", -9: "RP_ERR_INTERNAL", -10: "RP_ERR_CANCELLED",
 }
 
 _D = ctypes.c_double
@@ -72,6 +72,8 @@ _SIGS = {
                          ctypes.c_void_p], ctypes.c_int),
     "rp_scene_destroy": ([ctypes.c_void_p], ctypes.c_int),
     "rp_scene_footprint": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rp_query_footprint_traces": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
+                                   ctypes.c_void_p], ctypes.c_int),
     "rp_query_footprint": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p],
                            ctypes.c_int),
     "rp_simulate": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
@@ -92,6 +94,15 @@ _SIGS = {
     "rp_simulate_batch": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rp_autotune": ([ctypes.c_int], ctypes.c_int),
     "rp_autotune_query": ([ctypes.c_int, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
+    "rp_server_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p,
+                          ctypes.c_void_p], ctypes.c_int),
+    "rp_server_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "rp_submit": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
+                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rp_poll": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int], ctypes.c_int),
+    "rp_cancel": ([ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
+    "rp_server_drain": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rp_server_stats": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rp_count_records": ([ctypes.c_char_p, ctypes.c_void_p], ctypes.c_int),
     "rp_read_facets": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),
     "rp_read_targets": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p], ctypes.c_int),

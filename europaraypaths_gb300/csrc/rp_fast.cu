@@ -1703,6 +1703,29 @@ std::vector<int> host_target_bounds(const rp_scene* sc, const double* tr, int64_
     return ub;
 }
 
+// Size the next segment of a scene's traces starting at s0: up to 64 traces
+// whose scratch (target windows bounded by nr) fits the budget.
+void next_segment(const rp_scene* sc, const std::vector<int>& ub, int64_t s0, int64_t ns, int* nb_out,
+                  int64_t* tmax_out, size_t* bytes_out) {
+    int nb = 0;
+    int64_t tmax = 0;
+    size_t bytes = 0;
+    for (;;) {
+        if (s0 + nb >= ns) break;
+        const int64_t t2 = std::max<int64_t>(tmax, ub[s0 + nb]);
+        const FastLayout L = fast_layout(sc, nb + 1, t2, sc->nr);
+        const size_t b2 = seg_setup_bytes(sc, L) + seg_pair_bytes(sc, L);
+        if (nb > 0 && b2 > kFastBudget) break;
+        tmax = t2;
+        bytes = b2;
+        ++nb;
+        if (nb >= 64) break;
+    }
+    *nb_out = nb;
+    *tmax_out = tmax;
+    *bytes_out = bytes;
+}
+
 int check_scene(const rp_scene* sc) {
     if (sc->any_ttype0) {
         rp_set_error("fast form: ttype-0 targets are handled by the plain form only");
@@ -1714,10 +1737,28 @@ int check_scene(const rp_scene* sc) {
 
 }  // namespace
 
-size_t rp_fast_scratch(const rp_scene* sc, int64_t ns) {
-    FastLayout L = fast_layout(sc, (int)std::max<int64_t>(1, std::min<int64_t>(ns, 16)), sc->nt, sc->nr);
-    return seg_setup_bytes(sc, L) + seg_pair_bytes(sc, L) + 4096;
+// Peak scratch of a call: the largest wave of the same segment/wave plan the
+// run makes (in-aperture target counts from the traces when given, else every
+// target of the scene).
+size_t rp_fast_plan_bytes(const rp_scene* sc, const double* h_traces, int64_t ns) {
+    std::vector<int> ub = h_traces ? host_target_bounds(sc, h_traces, ns) : std::vector<int>(ns, (int)sc->nt);
+    size_t peak = 0, wave = 0;
+    for (int64_t s0 = 0; s0 < ns;) {
+        int nb;
+        int64_t tmax;
+        size_t bytes;
+        next_segment(sc, ub, s0, ns, &nb, &tmax, &bytes);
+        if (wave > 0 && wave + bytes > kFastBudget) {
+            peak = std::max(peak, wave);
+            wave = 0;
+        }
+        wave += bytes;
+        s0 += nb;
+    }
+    return std::max(peak, wave) + 4096;
 }
+
+size_t rp_fast_scratch(const rp_scene* sc, int64_t ns) { return rp_fast_plan_bytes(sc, nullptr, ns); }
 
 // Splits every job into segments (<= 64 traces, scratch within the budget)
 // and packs consecutive segments into waves under the same budget.
@@ -1742,20 +1783,10 @@ int rp_fast_batch(const rp_job* jobs, int njobs, rp_workspace* ws, cudaStream_t 
         const int nr = sc->nr;
         std::vector<int> ub = host_target_bounds(sc, tr[j].data(), ns);
         for (int64_t s0 = 0; s0 < ns;) {
-            int nb = 0;
-            int64_t tmax = 0;
-            size_t bytes = 0;
-            for (;;) {
-                if (s0 + nb >= ns) break;
-                const int64_t t2 = std::max<int64_t>(tmax, ub[s0 + nb]);
-                const FastLayout L = fast_layout(sc, nb + 1, t2, nr);
-                const size_t b2 = seg_setup_bytes(sc, L) + seg_pair_bytes(sc, L);
-                if (nb > 0 && b2 > kFastBudget) break;
-                tmax = t2;
-                bytes = b2;
-                ++nb;
-                if (nb >= 64) break;
-            }
+            int nb;
+            int64_t tmax;
+            size_t bytes;
+            next_segment(sc, ub, s0, ns, &nb, &tmax, &bytes);
             if (!wave.empty() && wave_bytes + bytes > kFastBudget) {
                 int rc = run_wave(wave, ws, st);
                 if (rc) return rc;
@@ -1801,17 +1832,10 @@ int rp_fast_run(rp_scene* sc, rp_workspace* ws, const double* d_traces, int64_t 
     std::vector<int> ub = host_target_bounds(sc, tr.data(), ns);
     const SceneConst kc = scene_const(sc);
     for (int64_t s0 = 0; s0 < ns;) {
-        int nb = 0;
-        int64_t tmax = 0;
-        for (;;) {
-            if (s0 + nb >= ns) break;
-            const int64_t t2 = std::max<int64_t>(tmax, ub[s0 + nb]);
-            const FastLayout L = fast_layout(sc, nb + 1, t2, sc->nr);
-            if (nb > 0 && seg_setup_bytes(sc, L) + seg_pair_bytes(sc, L) > kFastBudget) break;
-            tmax = t2;
-            ++nb;
-            if (nb >= 64) break;
-        }
+        int nb;
+        int64_t tmax;
+        size_t bytes;
+        next_segment(sc, ub, s0, ns, &nb, &tmax, &bytes);
         std::vector<Seg> w(1);
         Seg& g = w[0];
         g.sc = sc; g.trb = d_traces + 9 * s0; g.s0 = s0; g.nb = nb; g.tmax = tmax;
@@ -1833,5 +1857,16 @@ extern "C" int rp_autotune(int enable) {
 extern "C" int rp_autotune_query(int multi, int degree, int* cfg) {
     if (!cfg) { rp_set_error("rp_autotune_query: null cfg"); return RP_ERR_ARG; }
     *cfg = tuned_lookup(multi ? 1 : 0, multi ? -1 : degree);
+    return RP_OK;
+}
+
+extern "C" int rp_query_footprint_traces(const rp_scene* s, const double* traces, int64_t ns, int form,
+                                         int64_t* bytes) {
+    if (!s || !bytes || ns < 0 || (ns > 0 && !traces)) {
+        rp_set_error("rp_query_footprint_traces: bad argument");
+        return RP_ERR_ARG;
+    }
+    if ((form & 0xff) != RP_FORM_FAST_F32) return rp_query_footprint(s, ns, form, bytes);
+    *bytes = (int64_t)rp_fast_plan_bytes(s, traces, ns);
     return RP_OK;
 }

@@ -40,8 +40,11 @@ enum {
     RP_ERR_UNSUPPORTED = -6, /* mode not implemented by the requested form     */
     RP_ERR_BUDGET = -7,      /* request exceeds the admission memory budget    */
     RP_ERR_TIMEOUT = -8,     /* a bounded wait ran out                         */
-    RP_ERR_INTERNAL = -9     /* invariant violated (bin window overflow, ...)  */
+    RP_ERR_INTERNAL = -9,    /* invariant violated (bin window overflow, ...)  */
+    RP_ERR_CANCELLED = -10   /* the request was cancelled before it started     */
 };
+
+#define RP_PENDING 1         /* rp_poll: the request is queued or running      */
 
 /* Simulation form. */
 enum {
@@ -131,8 +134,13 @@ int rp_scene_destroy(rp_scene* s);
 /* Device bytes held by the scene's resident stores. */
 int rp_scene_footprint(const rp_scene* s, int64_t* bytes);
 
-/* Device bytes a rp_simulate call of ns traces needs as scratch, per form. */
+/* Device bytes a rp_simulate call of ns traces needs as scratch, per form
+ * (an upper bound: every target of the scene taken as in aperture). */
 int rp_query_footprint(const rp_scene* s, int64_t ns, int form, int64_t* bytes);
+
+/* The same for a given host trace table (ns x 9): in-aperture target counts
+ * from the traces, so the bound is close to what the call reserves. */
+int rp_query_footprint_traces(const rp_scene* s, const double* traces, int64_t ns, int form, int64_t* bytes);
 
 /*
  * Simulate ns traces (one radargram column each).  Replaces the trace loop
@@ -199,6 +207,59 @@ int rp_simulate_batch(const rp_job* jobs, int njobs, rp_workspace* ws, void* str
 int rp_autotune(int enable);
 /* The tuned configuration for (multi, degree), or -1 when not tuned yet. */
 int rp_autotune_query(int multi, int degree, int* cfg);
+
+/*
+ * Serving: a resident request loop on one device.  No counterpart in the
+ * reference, which runs one flyby per process (sim.cu:16-1008).
+ *
+ * Requests name a resident scene and carry a host trace table (copied at
+ * submit) and a caller-owned host output (ns x nr complex64, written before
+ * the request completes).  A request is admitted when a worker is free and its
+ * device footprint (rp_query_footprint plus its trace table and output) fits
+ * the memory budget next to everything running; requests wait in FIFO order.
+ * A free worker takes the queue head and, for fast-form requests, every
+ * following queued fast-form request that also fits (up to max_batch), and
+ * runs them as one rp_simulate_batch call on its own stream and workspace --
+ * continuous batching: requests arriving while others run are admitted as
+ * workers and memory free up, and their work overlaps on the device.  A
+ * request's result does not depend on what it was batched or overlapped with.
+ * The queue is internally locked; every function may be called from any
+ * thread.
+ */
+typedef struct rp_server rp_server;
+
+/* Optional executor: run() and footprint() replace the GPU path and
+ * rp_query_footprint (the server then makes no CUDA call).  For embedding the
+ * queue in front of another engine and for testing the scheduler. */
+typedef struct rp_executor {
+    int (*run)(void* user, rp_scene* scene, const double* traces, int64_t ns, int form, void* out,
+               int64_t* counts);
+    int64_t (*footprint)(void* user, rp_scene* scene, int64_t ns, int form);
+    void* user;
+} rp_executor;
+
+/* workers >= 1; mem_budget <= 0: 60% of the device's free memory;
+ * max_batch >= 1 requests per worker call; ex may be NULL. */
+int rp_server_create(int device, int workers, int64_t mem_budget, int max_batch, const rp_executor* ex,
+                     rp_server** out);
+/* Drains the queue, then stops the workers. */
+int rp_server_destroy(rp_server* srv);
+/* Queue a request; *ticket identifies it.  RP_ERR_BUDGET when its footprint
+ * alone exceeds the budget (it could never be admitted). */
+int rp_submit(rp_server* srv, rp_scene* scene, const double* traces, int64_t ns, int form, void* out,
+              int64_t* counts, int64_t* ticket);
+/* RP_PENDING while queued or running; once finished, the request's status
+ * (RP_OK, an error, RP_ERR_CANCELLED) and the ticket is released.
+ * timeout_ms: 0 polls, < 0 waits until the request finishes. */
+int rp_poll(rp_server* srv, int64_t ticket, int timeout_ms);
+/* Cancel a request that has not started (RP_ERR_ARG if it has). */
+int rp_cancel(rp_server* srv, int64_t ticket);
+/* Wait until nothing is queued or running (timeout_ms < 0: no limit). */
+int rp_server_drain(rp_server* srv, int timeout_ms);
+/* stats[0..n): completed, failed, rejected, cancelled, p50 ms, p99 ms,
+ * mean ms (submit to completion), mean queue wait ms, pairs, pairs/s (first
+ * submit to last completion), worker calls, largest batch, requests in flight. */
+int rp_server_stats(rp_server* srv, double* stats, int n);
 
 /* Number of kernel launches issued by this thread's last rp_simulate*. */
 int rp_last_launch_count(int64_t* launches);

@@ -11,14 +11,15 @@ from helpers import tiny_scene
 
 
 class FakeEngine:
-    """Stands in for the GPU: footprint = bytes_per_trace * ns, run() sleeps
-    and returns a radargram that is a pure function of the traces."""
+    """Stands in for the GPU behind the native scheduler: footprint =
+    bytes_per_trace * ns; run() sleeps and returns a radargram that is a pure
+    function of the traces."""
 
-    def __init__(self, bytes_per_trace=1000, delay=0.02, fail_on=None):
+    def __init__(self, bytes_per_trace=1000, delay=0.02, fail_on_base=None):
         self.bpt = bytes_per_trace
         self.delay = delay
-        self.fail_on = fail_on
-        self.scenes = {}
+        self.fail_on_base = fail_on_base
+        self.nrs = {}
         self.lock = threading.Lock()
         self.live = 0
         self.live_bytes = 0
@@ -26,47 +27,37 @@ class FakeEngine:
         self.peak_bytes = 0
         self.started = []
 
-    def free_memory(self):
-        return 10 ** 9
-
-    def add_scene(self, sid, params, facets, targets, prisms):
-        self.scenes[sid] = int(params["nr"])
-
-    def adopt_scene(self, sid, scene):
-        self.scenes[sid] = int(scene["nr"])
-
-    def remove_scene(self, sid):
-        self.scenes.pop(sid)
-
     def footprint(self, sid, ns, form):
         return self.bpt * ns
 
-    def make_slot(self):
-        return {}
-
-    def close_slot(self, slot):
-        pass
-
-    def run(self, slot, req):
-        fp = self.footprint(req.scene_id, req.traces.shape[0], req.form)
+    def run(self, sid, traces, form):
+        fp = self.footprint(sid, traces.shape[0], form)
         with self.lock:
-            self.started.append(req.id)
+            self.started.append(float(traces[0, 0]))
             self.live += 1
             self.live_bytes += fp
             self.peak_live = max(self.peak_live, self.live)
             self.peak_bytes = max(self.peak_bytes, self.live_bytes)
         try:
             time.sleep(self.delay)
-            if self.fail_on is not None and req.id == self.fail_on:
+            if self.fail_on_base is not None and traces[0, 0] == self.fail_on_base:
                 raise RuntimeError("planted failure")
-            nr = self.scenes[req.scene_id]
-            out = np.outer(req.traces[:, 0], np.arange(nr)).astype(np.complex64)
-            counts = np.ones((req.traces.shape[0], 2), np.int64)
+            nr = self.nrs[sid]
+            out = np.outer(traces[:, 0], np.arange(nr)).astype(np.complex64)
+            counts = np.ones((traces.shape[0], 2), np.int64)
             return out, counts
         finally:
             with self.lock:
                 self.live -= 1
                 self.live_bytes -= fp
+
+
+def _server(eng, nr=4, **kw):
+    from europaraypaths_gb300.serving import Server
+    srv = Server(executor=eng, **kw)
+    sid = srv.add_scene({"nr": nr})
+    eng.nrs[sid] = nr
+    return srv, sid
 
 
 def _traces(n, base):
@@ -76,10 +67,8 @@ def _traces(n, base):
 
 
 def test_results_and_stats():
-    from europaraypaths_gb300.serving import Server
     eng = FakeEngine()
-    srv = Server(engine=eng, workers=3, mem_budget=10 ** 6)
-    sid = srv.add_scene({"nr": 8}, None)
+    srv, sid = _server(eng, nr=8, workers=3, mem_budget=10 ** 6, max_batch=1)
     reqs = [srv.submit(sid, _traces(1 + i % 3, 10 * i)) for i in range(12)]
     for i, r in enumerate(reqs):
         out = r.result(timeout=10)
@@ -87,15 +76,14 @@ def test_results_and_stats():
         assert np.array_equal(out[:, 1].real, 10 * i + np.arange(1 + i % 3))
     st = srv.stats()
     assert st["completed"] == 12 and st["p99_ms"] >= st["p50_ms"] > 0
+    assert st["pairs"] == sum(3 * (1 + i % 3) for i in range(12))
     assert eng.peak_live > 1          # requests overlapped
     srv.close()
 
 
 def test_admission_respects_budget():
-    from europaraypaths_gb300.serving import Server
     eng = FakeEngine(bytes_per_trace=1000, delay=0.03)
-    srv = Server(engine=eng, workers=8, mem_budget=2500)
-    sid = srv.add_scene({"nr": 4}, None)
+    srv, sid = _server(eng, workers=8, mem_budget=2500, max_batch=1)
     reqs = [srv.submit(sid, _traces(1, i)) for i in range(10)]
     for r in reqs:
         r.result(timeout=10)
@@ -105,9 +93,8 @@ def test_admission_respects_budget():
 
 
 def test_request_over_budget_refused():
-    from europaraypaths_gb300.serving import BudgetError, Server
-    srv = Server(engine=FakeEngine(), workers=2, mem_budget=1500)
-    sid = srv.add_scene({"nr": 4}, None)
+    from europaraypaths_gb300.serving import BudgetError
+    srv, sid = _server(FakeEngine(), workers=2, mem_budget=1500)
     with pytest.raises(BudgetError):
         srv.submit(sid, _traces(2, 0))
     assert srv.stats()["rejected"] == 1
@@ -115,71 +102,83 @@ def test_request_over_budget_refused():
 
 
 def test_fifo_order_single_worker():
-    from europaraypaths_gb300.serving import Server
     eng = FakeEngine(delay=0.005)
-    srv = Server(engine=eng, workers=1, mem_budget=10 ** 6)
-    sid = srv.add_scene({"nr": 4}, None)
-    reqs = [srv.submit(sid, _traces(1, i)) for i in range(8)]
+    srv, sid = _server(eng, workers=1, mem_budget=10 ** 6, max_batch=1)
+    for i in range(8):
+        srv.submit(sid, _traces(1, i))
     srv.drain(timeout=10)
-    assert eng.started == [r.id for r in reqs]
+    assert eng.started == [float(i) for i in range(8)]
     srv.close()
 
 
 def test_head_of_line_waits_for_budget():
     # a big request at the head is not overtaken by smaller ones behind it
-    from europaraypaths_gb300.serving import Server
     eng = FakeEngine(bytes_per_trace=1000, delay=0.03)
-    srv = Server(engine=eng, workers=4, mem_budget=3000)
-    sid = srv.add_scene({"nr": 4}, None)
+    srv, sid = _server(eng, workers=4, mem_budget=3000, max_batch=1)
     a = srv.submit(sid, _traces(2, 0))
     big = srv.submit(sid, _traces(3, 10))
     small = srv.submit(sid, _traces(1, 20))
     srv.drain(timeout=10)
-    assert eng.started.index(big.id) < eng.started.index(small.id)
+    assert eng.started.index(10.0) < eng.started.index(20.0)
     assert a.done() and big.done() and small.done()
     srv.close()
 
 
 def test_failure_is_isolated():
-    from europaraypaths_gb300.serving import Server
-    eng = FakeEngine(fail_on=2)
-    srv = Server(engine=eng, workers=2, mem_budget=10 ** 6)
-    sid = srv.add_scene({"nr": 4}, None)
+    eng = FakeEngine(fail_on_base=2.0)
+    srv, sid = _server(eng, workers=2, mem_budget=10 ** 6, max_batch=1)
     reqs = [srv.submit(sid, _traces(1, i)) for i in range(5)]
-    for r in reqs:
-        if r.id == 2:
-            with pytest.raises(RuntimeError, match="planted"):
+    for i, r in enumerate(reqs):
+        if i == 2:
+            with pytest.raises(RuntimeError, match="failed"):
                 r.result(timeout=10)
         else:
             r.result(timeout=10)
-    assert srv.stats()["completed"] == 4
+    st = srv.stats()
+    assert st["completed"] == 4 and st["failed"] == 1
     srv.close()
 
 
 def test_cancel_queued():
-    from europaraypaths_gb300.serving import Server
-    eng = FakeEngine(delay=0.05)
-    srv = Server(engine=eng, workers=1, mem_budget=10 ** 6)
-    sid = srv.add_scene({"nr": 4}, None)
+    from europaraypaths_gb300.serving import CancelledError
+    eng = FakeEngine(delay=0.2)
+    srv, sid = _server(eng, workers=1, mem_budget=10 ** 6, max_batch=1)
     first = srv.submit(sid, _traces(1, 0))
+    time.sleep(0.05)
     second = srv.submit(sid, _traces(1, 1))
-    time.sleep(0.01)
     assert srv.cancel(second)
-    with pytest.raises(RuntimeError, match="cancelled"):
+    with pytest.raises(CancelledError):
         second.result(timeout=5)
     first.result(timeout=5)
     srv.close()
-    assert second.id not in eng.started
+    assert 1.0 not in eng.started
+    assert srv.stats is not None
+
+
+def test_continuous_batching_takes_queued_requests():
+    # one worker busy with a slow request; requests queued meanwhile are
+    # taken together by its next call
+    eng = FakeEngine(delay=0.1)
+    srv, sid = _server(eng, workers=1, mem_budget=10 ** 6, max_batch=8)
+    reqs = [srv.submit(sid, _traces(1, 0))]
+    time.sleep(0.03)
+    reqs += [srv.submit(sid, _traces(2, 10 * k)) for k in range(1, 6)]
+    for k, r in enumerate(reqs):
+        assert r.result(timeout=10)[0, 1].real == 10 * k
+    st = srv.stats()
+    assert st["worker_calls"] == 2 and st["max_batch_seen"] == 5
+    srv.close()
 
 
 def test_adopted_scene_survives_close():
     from europaraypaths_gb300.serving import Server
     eng = FakeEngine(delay=0.001)
-    srv = Server(engine=eng, workers=2, mem_budget=10 ** 6)
+    srv = Server(executor=eng, workers=2, mem_budget=10 ** 6)
     sid = srv.adopt_scene({"nr": 6})
+    eng.nrs[sid] = 6
     assert srv.submit(sid, _traces(2, 5)).result(timeout=5).shape == (2, 6)
     srv.close(keep_scenes=True)
-    assert sid in eng.scenes
+    assert sid in srv.scenes
 
 
 @pytest.mark.gpu
