@@ -31,35 +31,17 @@
 #include "rp_common.cuh"
 #include "rp_conv.cuh"
 #include "rp_fft.cuh"
+#include "rp_pair.cuh"
 
-#define RP_CHUNK 256          // facets per chunk (one record tile)
-#define RP_PAIR_THREADS 256   // targets per pair-kernel block
-#define RP_WIN 16             // bins in a thread's per-chunk window
-#define RP_PARTS 4            // facet-range splits per (trace, target block)
-#define RP_SPIN_LIMIT (1 << 22)
 #define RP_CONV_SPLIT 64       // targets per range-compression work item (fixed:
                                // a trace's sum order never depends on the batch)
 #define RP_CONV_THREADS 512
 
+using namespace rpk;
+
 namespace {
 
-using C32 = Cx<float>;
 using C64 = Cx<double>;
-
-struct __align__(16) FacetRec {
-    float4 a;   // dx, dy, dz (facet - chunk centre), |d|^2
-    float4 b;   // nx, ny, nz, xI = (Itd - rst) / dr
-    float4 c;   // ux, uy, uz, tauI = frac(Itd / lam)
-    float4 d;   // vx, vy, vz, K = amplitude factor
-};
-
-struct __align__(16) ChunkMeta {
-    double cx, cy, cz;     // chunk centre
-    float R;               // max |facet - centre|
-    float xmin, xmax;      // range of (Itd - rst)/dr
-    int n;                 // facets in the chunk
-    double bbmin[3], bbmax[3];
-};
 
 // --------------------------------------------------------- block reduce --
 template <class T, class Op>
@@ -310,443 +292,12 @@ __global__ void k_tsetup32(const double* __restrict__ TG, int64_t nt, const int*
     atomicMax(maxw, b1 - b0);
 }
 
-// ------------------------------------------------------------ TMA bulk --
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ void tma_bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
-}
-
-// Bounded wait on an mbarrier phase; returns false if the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
-    for (int it = 0; it < RP_SPIN_LIMIT; ++it) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-            " selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(smem_u32(bar)), "r"(phase)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-// ----------------------------------------------------------- pair kernel --
-struct PairArgs {
-    const FacetRec* rec;
-    const ChunkMeta* meta;
-    int64_t rstride, mstride;
-    const int* nill;
-    const int* ntl;
-    const int* tlist;
-    int64_t tstride;
-    const double* TG;
-    int64_t nt;
-    const double* PR;   // prisms (alpha, box) FP64 SoA
-    int64_t np;
-    const int* bt0;
-    C32* T;             // [RP_PARTS][nb][tstride][Wt]
-    int Wt;
-    int nb;
-    int tblocks;        // target blocks per trace
-    unsigned int* work; // work counter
-    unsigned int* err;  // error flags: [0] window overflow, [1] wait timeout
-    // constants
-    float nr_f;
-    int nr;
-    int nr1;            // nr - 1: both split bins are inside the trace when b < nr - 1
-    float kb;           // n / dr
-    float kt;           // n / lam
-    float pik;          // pi * (pi_F * fs / lam): sinc arguments in radians
-    float pik2;         // pik^2
-    float sc[8];        // sinc polynomial coefficients in t = a^2 (sinc_poly)
-    float ealpha;       // -2 alpha2 log2(e)
-    float eks;          // -2 ks^2 log2(e)
-    double nidx, inv_dr, inv_lam;   // inv_lam: turns per metre, pi_F / (pi lam)
-    int lossless;
-    int deg;            // sinc polynomial degree (0: special-function unit)
-};
-
-// Per-(chunk, target) anchors of the split-precision evaluation.
-struct Anchor {
-    float Dx, Dy, Dz;     // target - chunk centre (FP32 of an FP64 difference)
-    float T0, T0sq;       // |target - chunk centre| (FP64 -> FP32)
-    float tau0;           // frac(n T0 turn): phase of the anchor in turns
-    float xbase;          // n T0 / dr - blo (bins, relative to the window start)
-    float tnx, tny, tnz;  // target normal
-};
-
-// Hardware approximations (PTX rsqrt/rcp/ex2 .approx.ftz): single
-// special-function-unit instructions, relative error ~2^-22.
-__device__ __forceinline__ float rsqrt_a(float x) {
-    float y;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-__device__ __forceinline__ float rcp_a(float x) {
-    float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-__device__ __forceinline__ float ex2_a(float x) {
-    float y;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-// sin(a)/a as a degree-D polynomial in t = a^2 (coefficients fitted per
-// scene on [0, amax^2], see sinc_poly), Horner form.
-template <int D>
-__device__ __forceinline__ float sinc_poly_eval(const float* c, float t) {
-    float s = c[D];
-#pragma unroll
-    for (int k = D - 1; k >= 0; --k) s = fmaf(s, t, c[k]);
-    return s;
-}
-
-// One (facet, target) evaluation of the target leg (compTargetRays,
-// compRefrEnergyIn, accumulateTarget; geometry_kernels.cu:272-350, 520-554,
-// radar_kernels.cu:767-830).  Returns the phasor and x - blo, the bin
-// coordinate relative to the window start.
-//
-// The two directivities facet_G(Tth, Tph) and facet_G(TargetTh, Tph)
-// (radar_kernels.cu:658-677) need sinc(pik/pi * sin(th) cos(ph)) and
-// sinc(pik/pi * sin(th) sin(ph)), sinc(x) = sin(pi x)/(pi x).  With
-// cos(Tph) = xv / sqrt(h2), sin(Tph) = yu / sqrt(h2) and sin^2(th) = 1 - c^2,
-// the squared sinc arguments are pik^2 (1 - c^2) xv^2 / h2 etc. (atan2(0, 0)
-// = 0 gives xv^2/h2 = 1, yu^2/h2 = 0).  NT > 0 evaluates sin(a)/a as a
-// polynomial in a^2 (no special-function unit); NT == 0 uses sin(a)/a with
-// one shared reciprocal, 1 for |a| < pi 1e-6 (elementary_kernels.cu:50-53).
-template <int NT>
-__device__ __forceinline__ void pair_eval(const FacetRec& r, const Anchor& an, const PairArgs& A,
-                                          float& xr, float& vre, float& vim) {
-    const float dd = fmaf(an.Dx, r.a.x, fmaf(an.Dy, r.a.y, an.Dz * r.a.z));
-    const float qd = fmaf(-2.f, dd, r.a.w);             // Ttd^2 - T0^2
-    const float d2 = an.T0sq + qd;
-    const float rinv = rsqrt_a(d2);
-    const float Ttd = d2 * rinv;
-    const float dT = qd * rcp_a(Ttd + an.T0);           // Ttd - T0 without cancellation
-    const float jx = (an.Dx - r.a.x) * rinv;
-    const float jy = (an.Dy - r.a.y) * rinv;
-    const float jz = (an.Dz - r.a.z) * rinv;
-    float cT = -fmaf(jx, r.b.x, fmaf(jy, r.b.y, jz * r.b.z));
-    float cD = -fmaf(jx, an.tnx, fmaf(jy, an.tny, jz * an.tnz));
-    const float yu = fmaf(jx, r.c.x, fmaf(jy, r.c.y, jz * r.c.z));
-    const float xv = fmaf(jx, r.d.x, fmaf(jy, r.d.y, jz * r.d.z));
-    const float X = xv * xv, Y = yu * yu;
-    const float h2 = X + Y;
-    float S;
-    if (NT > 0) {
-        // 1 - c^2 may round a hair below 0 for |c| ~ 1: harmless in the polynomial
-        const float aT = fmaf(-cT, cT, 1.f);
-        const float aD = fmaf(-cD, cD, 1.f);
-        const bool hz = !(h2 > 0.f);
-        const float k2 = A.pik2 * rcp_a(h2);
-        const float xx = hz ? A.pik2 : k2 * X;
-        const float yy = hz ? 0.f : k2 * Y;
-        S = sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aT * xx) * sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aT * yy) *
-            sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aD * xx) * sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aD * yy);
-    } else {
-        cT = fminf(1.f, fmaxf(-1.f, cT));
-        cD = fminf(1.f, fmaxf(-1.f, cD));
-        const float aT = fmaf(-cT, cT, 1.f);
-        const float aD = fmaf(-cD, cD, 1.f);
-        const bool hz = !(h2 > 0.f);
-        const float pT = aT * h2, pD = aD * h2;
-        const float gT = (pT > 0.f) ? aT * rsqrtf(pT) : 0.f;
-        const float gD = (pD > 0.f) ? aD * rsqrtf(pD) : 0.f;
-        const float a1 = A.pik * (hz ? sqrtf(aT) : gT * xv);
-        const float a2 = A.pik * (hz ? 0.f : gT * yu);
-        const float a3 = A.pik * (hz ? sqrtf(aD) : gD * xv);
-        const float a4 = A.pik * (hz ? 0.f : gD * yu);
-        const float eps = 3.14159265e-6f;
-        const bool z1 = fabsf(a1) < eps, z2 = fabsf(a2) < eps, z3 = fabsf(a3) < eps, z4 = fabsf(a4) < eps;
-        const float num = (z1 ? 1.f : __sinf(a1)) * (z2 ? 1.f : __sinf(a2)) * (z3 ? 1.f : __sinf(a3)) *
-                          (z4 ? 1.f : __sinf(a4));
-        const float den = (z1 ? 1.f : a1) * (z2 ? 1.f : a2) * (z3 ? 1.f : a3) * (z4 ? 1.f : a4);
-        S = __fdividef(num, den);
-    }
-    // attenuation and roughness (zero constants when lossless)
-    const float e2 = fmaf(A.eks, cT * cT, A.ealpha * Ttd);
-    const float amp = r.d.w * fabsf(S) * rinv * ex2_a(e2);
-    float tau = (r.c.w + an.tau0) + A.kt * dT;
-    tau -= rintf(tau);
-    float sn, cs;
-    __sincosf(-6.28318530717958647f * tau, &sn, &cs);
-    vre = amp * cs;
-    vim = amp * sn;
-    xr = r.b.w + an.xbase + A.kb * dT;
-}
-
-// Attenuation-prism factor for one pair (compTargetRays, geometry_kernels.cu:
-// 317-342): exp2 of the change of the exponent from alpha2 * Ttd to
-// sum(alpha_p d_p) + alpha2 (Ttd - sum d_p).
-__device__ __noinline__ float prism_factor(float4 ra, double cx, double cy, double cz, float Dx,
-                                           float Dy, float Dz, float T0sq, const double* PR,
-                                           int64_t np, float ealpha) {
-    const float dd = fmaf(Dx, ra.x, fmaf(Dy, ra.y, Dz * ra.z));
-    const float d2 = T0sq + fmaf(-2.f, dd, ra.w);
-    const float rinv = rsqrtf(d2);
-    const float Ttd = d2 * rinv;
-    const double fx = cx + ra.x, fy = cy + ra.y, fz = cz + ra.z;
-    const double jx = (Dx - ra.x) * rinv, jy = (Dy - ra.y) * rinv, jz = (Dz - ra.z) * rinv;
-    double tot = 0.0, ex = 0.0;
-    for (int64_t p = 0; p < np; ++p) {
-        double box[6] = {PR[np + p], PR[2 * np + p], PR[3 * np + p],
-                         PR[4 * np + p], PR[5 * np + p], PR[6 * np + p]};
-        double ad = d_prism_dist(fx, fy, fz, jx, jy, jz, box, Ttd);
-        tot += ad;
-        ex += PR[p] * ad;
-    }
-    // ealpha = -2 alpha2 log2(e): replace alpha2 * tot by the prisms' sum
-    return exp2f(-ealpha * (float)tot - 2.f * 1.44269504f * (float)ex);
-}
-
-// Add one phasor into the thread's window (or, outside it, directly into the
-// thread's own trace row).  Bin and weight follow the reference's two-bin
-// split: b = (short)x (truncation), w = x - b (radar_kernels.cu:736-760).
-// floor(xr) comes from rounding xr - 1/2 with the 1.5 * 2^23 magic number
-// (an exact half rounds either way; the split is continuous there, so both
-// give the same contributions); x in (-1, 0) is truncated to bin 0 as the
-// reference does.
-__device__ __noinline__ void bin_add_edge(int b, float w, float vre, float vim, int blo, int b0,
-                                          float2* win, int tid, C32* Trow, int nr, int Wt,
-                                          unsigned int* err) {
-    if (b < 0) {
-        if (b != -1) return;
-        b = 0;              // x in (-1, 0): truncation gives bin 0 and w = x
-        w -= 1.f;
-    }
-    if (b >= nr) return;
-    const float w0 = 1.f - w;
-    const bool two = (b + 1) < nr;
-    const int sl = b - blo;
-    if ((unsigned)sl < (unsigned)(RP_WIN - 1)) {
-        float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
-        float2 v0 = *p0;
-        v0.x = fmaf(vre, w0, v0.x);
-        v0.y = fmaf(vim, w0, v0.y);
-        *p0 = v0;
-        if (two) {
-            float2* p1 = p0 + RP_PAIR_THREADS;
-            float2 v1 = *p1;
-            v1.x = fmaf(vre, w, v1.x);
-            v1.y = fmaf(vim, w, v1.y);
-            *p1 = v1;
-        }
-        return;
-    }
-    const int o0 = b - b0;
-    if (o0 >= 0 && o0 < Wt) {
-        C32 t0 = Trow[o0];
-        t0.x = fmaf(vre, w0, t0.x);
-        t0.y = fmaf(vim, w0, t0.y);
-        Trow[o0] = t0;
-    } else {
-        atomicOr(err, 1u);
-    }
-    if (two) {
-        if (o0 + 1 >= 0 && o0 + 1 < Wt) {
-            C32 t1 = Trow[o0 + 1];
-            t1.x = fmaf(vre, w, t1.x);
-            t1.y = fmaf(vim, w, t1.y);
-            Trow[o0 + 1] = t1;
-        } else {
-            atomicOr(err, 1u);
-        }
-    }
-}
-
-// Common case inline (both bins inside the window and the trace); the rest
-// (window spill, x < 0, the last bin) in bin_add_edge.
-__device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo, int b0,
-                                        float2* win, int tid, C32* Trow, const PairArgs& A) {
-    const float t = (xr - 0.5f) + 12582912.0f;
-    const int sl = __float_as_int(t) - 0x4B400000;
-    const float w = xr - (t - 12582912.0f);
-    const int b = blo + sl;
-    if ((unsigned)sl < (unsigned)(RP_WIN - 1) && (unsigned)b < (unsigned)A.nr1) {
-        float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
-        float2* p1 = p0 + RP_PAIR_THREADS;
-        float2 v0 = *p0, v1 = *p1;
-        const float w0 = 1.f - w;
-        v0.x = fmaf(vre, w0, v0.x);
-        v0.y = fmaf(vim, w0, v0.y);
-        v1.x = fmaf(vre, w, v1.x);
-        v1.y = fmaf(vim, w, v1.y);
-        *p0 = v0;
-        *p1 = v1;
-    } else {
-        bin_add_edge(b, w, vre, vim, blo, b0, win, tid, Trow, A.nr, A.Wt, A.err);
-    }
-}
-
-// One work item of the pair stage: target block tb of trace s of a batch,
-// facet chunks [k0, k1) of part `part`.  srec: two chunk buffers, win: the
-// per-thread bin windows, bars/phase: the two stage barriers and their
-// parities (carried across items), s_tpos: the threads' target positions.
-template <int NT, int ILP, class PA>
-__device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, FacetRec* srec, float2* win,
-                                          uint64_t* bars, uint32_t* phase, double (*s_tpos)[RP_PAIR_THREADS]) {
-    const int tid = threadIdx.x;
-    const int nq = A.ntl[s];
-    const int n = A.nill[s];
-    if (tb * RP_PAIR_THREADS >= nq || n == 0) return;
-    const int nchunks = (n + RP_CHUNK - 1) / RP_CHUNK;
-    const int k0 = (int)((int64_t)nchunks * part / RP_PARTS);
-    const int k1 = (int)((int64_t)nchunks * (part + 1) / RP_PARTS);
-    if (k0 >= k1) return;
-    const int q = tb * RP_PAIR_THREADS + tid;
-    const bool active = q < nq;
-    float tnx = 0, tny = 0, tnz = 1;
-    int b0 = 0;
-    C32* Trow = nullptr;
-    if (active) {
-        const int64_t ti = A.tlist[(size_t)s * A.tstride + q];
-        s_tpos[0][tid] = A.TG[ti];
-        s_tpos[1][tid] = A.TG[A.nt + ti];
-        s_tpos[2][tid] = A.TG[2 * A.nt + ti];
-        tnx = (float)A.TG[3 * A.nt + ti]; tny = (float)A.TG[4 * A.nt + ti];
-        tnz = (float)A.TG[5 * A.nt + ti];
-        b0 = A.bt0[(size_t)s * A.tstride + q];
-        Trow = A.T + (((size_t)part * A.nb + s) * A.tstride + q) * A.Wt;
-    }
-    const FacetRec* rbase = A.rec + (size_t)s * A.rstride;
-    // prologue: stage chunk k0
-    if (tid == 0) {
-        int cnt = min(RP_CHUNK, n - k0 * RP_CHUNK);
-        uint32_t bytes = (uint32_t)(cnt * sizeof(FacetRec));
-        mbar_expect_tx(&bars[0], bytes);
-        tma_bulk_g2s(srec, rbase + (size_t)k0 * RP_CHUNK, bytes, &bars[0]);
-    }
-    for (int k = k0; k < k1; ++k) {
-        const int buf = (k - k0) & 1;
-        // prefetch the next chunk into the other buffer (its readers
-        // finished at the trailing __syncthreads of the previous step)
-        if (tid == 0 && k + 1 < k1) {
-            int cnt = min(RP_CHUNK, n - (k + 1) * RP_CHUNK);
-            uint32_t bytes = (uint32_t)(cnt * sizeof(FacetRec));
-            mbar_expect_tx(&bars[buf ^ 1], bytes);
-            tma_bulk_g2s(srec + (buf ^ 1) * RP_CHUNK, rbase + (size_t)(k + 1) * RP_CHUNK, bytes,
-                         &bars[buf ^ 1]);
-        }
-        const ChunkMeta* mp = A.meta + (size_t)s * A.mstride + k;
-        if (!mbar_wait(&bars[buf], phase[buf])) {
-            if (tid == 0) atomicOr(A.err + 1, 1u);
-        }
-        phase[buf] ^= 1u;
-        const FacetRec* R = srec + buf * RP_CHUNK;
-        if (active) {
-            // FP64 anchors of this (chunk, target)
-            const double mcx = mp->cx, mcy = mp->cy, mcz = mp->cz;
-            const double Dx = s_tpos[0][tid] - mcx, Dy = s_tpos[1][tid] - mcy, Dz = s_tpos[2][tid] - mcz;
-            const double T0 = sqrt(Dx * Dx + Dy * Dy + Dz * Dz);
-            const double xt = A.nidx * T0 * A.inv_dr;
-            const double tt = A.nidx * T0 * A.inv_lam;
-            const double lo = (double)mp->xmin + A.nidx * (T0 - (double)mp->R) * A.inv_dr;
-            const int blo = (int)floor(lo) - 1;
-            Anchor an;
-            an.Dx = (float)Dx; an.Dy = (float)Dy; an.Dz = (float)Dz;
-            an.T0 = (float)T0; an.T0sq = (float)(T0 * T0);
-            an.tau0 = (float)(tt - floor(tt));
-            an.xbase = (float)(xt - (double)blo);
-            an.tnx = tnx; an.tny = tny; an.tnz = tnz;
-            for (int w = 0; w < RP_WIN; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
-            const int cnt = mp->n;
-            const bool prisms = (A.np > 0) && !A.lossless;
-            int jj = 0;
-            if (ILP == 2)
-            for (; jj + 1 < cnt; jj += 2) {
-                const FacetRec r0 = R[jj];
-                const FacetRec r1 = R[jj + 1];
-                float x0, re0, im0, x1, re1, im1;
-                pair_eval<NT>(r0, an, A, x0, re0, im0);
-                pair_eval<NT>(r1, an, A, x1, re1, im1);
-                if (prisms) {
-                    const float f0 = prism_factor(r0.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
-                                                  A.PR, A.np, A.ealpha);
-                    const float f1 = prism_factor(r1.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
-                                                  A.PR, A.np, A.ealpha);
-                    re0 *= f0; im0 *= f0; re1 *= f1; im1 *= f1;
-                }
-                bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
-                bin_add(x1, re1, im1, blo, b0, win, tid, Trow, A);
-            }
-            for (; jj < cnt; ++jj) {
-                const FacetRec r0 = R[jj];
-                float x0, re0, im0;
-                pair_eval<NT>(r0, an, A, x0, re0, im0);
-                if (prisms) {
-                    const float f0 = prism_factor(r0.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
-                                                  A.PR, A.np, A.ealpha);
-                    re0 *= f0; im0 *= f0;
-                }
-                bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
-            }
-            // flush the window into the owned trace
-            for (int w = 0; w < RP_WIN; ++w) {
-                const float2 v = win[w * RP_PAIR_THREADS + tid];
-                if (v.x != 0.f || v.y != 0.f) {
-                    const int o = blo + w - b0;
-                    if (o >= 0 && o < A.Wt) {
-                        C32 t0 = Trow[o];
-                        t0.x += v.x;
-                        t0.y += v.y;
-                        Trow[o] = t0;
-                    } else {
-                        atomicOr(A.err, 1u);
-                    }
-                }
-            }
-        }
-        __syncthreads();   // everyone done with buffer `buf` before it is refilled
-    }
-}
-
-#define RP_PAIR_SMEM_DECL                                                                       \
-    extern __shared__ __align__(128) unsigned char smem[];                                      \
-    FacetRec* srec = reinterpret_cast<FacetRec*>(smem);                     /* [2][RP_CHUNK] */ \
-    float2* win = reinterpret_cast<float2*>(smem + 2 * RP_CHUNK * sizeof(FacetRec));            \
-    __shared__ uint64_t bars[2];                                                                \
-    __shared__ unsigned int s_item;                                                             \
-    __shared__ double s_tpos[3][RP_PAIR_THREADS];                                               \
-    const int tid = threadIdx.x;                                                                \
-    if (tid == 0) {                                                                             \
-        mbar_init(&bars[0], 1);                                                                 \
-        mbar_init(&bars[1], 1);                                                                 \
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");                     \
-    }                                                                                           \
-    __syncthreads();                                                                            \
-    uint32_t phase[2] = {0u, 0u};
-
-#define RP_PAIR_SMEM_END                                                    \
-    if (tid == 0) {                                                         \
-        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bars[0]))); \
-        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bars[1]))); \
-    }
-
 // Single-batch pair kernel: the batch's constants live in the parameter
 // bank.  Persistent: blocks take (trace, target block, part) items from a
 // work counter until all are done.
 template <int NT, int ILP, int MINB>
 __global__ void __launch_bounds__(RP_PAIR_THREADS, MINB)
-k_pairs32(PairArgs A) {
+k_pairs32(const __grid_constant__ PairArgs A) {
     RP_PAIR_SMEM_DECL
     const unsigned int items = (unsigned)A.nb * A.tblocks * RP_PARTS;
     for (;;) {
@@ -758,49 +309,7 @@ k_pairs32(PairArgs A) {
         const int part = item % RP_PARTS;
         const int tb = (item / RP_PARTS) % A.tblocks;
         const int s = item / (RP_PARTS * A.tblocks);
-        pair_item<NT, ILP>(A, s, tb, part, srec, win, bars, phase, s_tpos);
-    }
-    RP_PAIR_SMEM_END
-}
-
-// Multi-job pair kernel: one persistent launch over the items of many
-// batches (scenes of different sizes, bin counts and sinc degrees).  Job j
-// owns items [start[j], start[j + 1]); a block copies the job's constants
-// into registers and dispatches on its sinc degree.
-template <int ILP, int MINB>
-__global__ void __launch_bounds__(RP_PAIR_THREADS, MINB)
-k_pairs32m(const PairArgs* __restrict__ jobs, const unsigned int* __restrict__ start, int njobs,
-           unsigned int* work) {
-    RP_PAIR_SMEM_DECL
-    __shared__ int s_job;
-    const unsigned int total = start[njobs];
-    for (;;) {
-        if (tid == 0) {
-            const unsigned int it = atomicAdd(work, 1u);
-            int lo = 0, hi = njobs - 1;          // last j with start[j] <= it
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (start[mid] <= it) lo = mid; else hi = mid - 1;
-            }
-            s_item = it;
-            s_job = lo;
-        }
-        __syncthreads();
-        const unsigned int item = s_item;
-        const int j = s_job;
-        __syncthreads();
-        if (item >= total) break;
-        const PairArgs A = jobs[j];
-        const unsigned int li = item - start[j];
-        const int part = li % RP_PARTS;
-        const int tb = (li / RP_PARTS) % A.tblocks;
-        const int s = li / (RP_PARTS * A.tblocks);
-        switch (A.deg) {
-            case 4: pair_item<4, ILP>(A, s, tb, part, srec, win, bars, phase, s_tpos); break;
-            case 5: pair_item<5, ILP>(A, s, tb, part, srec, win, bars, phase, s_tpos); break;
-            case 6: pair_item<6, ILP>(A, s, tb, part, srec, win, bars, phase, s_tpos); break;
-            default: pair_item<0, ILP>(A, s, tb, part, srec, win, bars, phase, s_tpos); break;
-        }
+        pair_item<NT, ILP>(A, s, tb, part, bars, phase);
     }
     RP_PAIR_SMEM_END
 }
@@ -1163,7 +672,7 @@ const size_t kFastBudget = (size_t)32 << 30;
 // Pair-kernel instantiation: sinc degree x (ILP facets per step, resident
 // blocks per SM).  cfg 0: 2 x 3, 1: 2 x 2, 2: 1 x 4, 3: 1 x 3.
 template <int NT>
-void (*pick_cfg(int cfg))(PairArgs) {
+void (*pick_cfg(int cfg))(const PairArgs) {
     switch (cfg) {
         case 1: return k_pairs32<NT, 2, 2>;
         case 2: return k_pairs32<NT, 1, 4>;
@@ -1172,7 +681,7 @@ void (*pick_cfg(int cfg))(PairArgs) {
     }
 }
 
-void (*pick_pair_kernel(int deg, int cfg))(PairArgs) {
+void (*pick_pair_kernel(int deg, int cfg))(const PairArgs) {
     switch (deg) {
         case 4: return pick_cfg<4>(cfg);
         case 5: return pick_cfg<5>(cfg);
@@ -1249,17 +758,6 @@ int launch_conv32s(const ConvArgs* d_jobs, const unsigned int* d_start, int njob
     if (kpt <= 2) return launch_conv_k<2>(d_jobs, d_start, njobs, maxM, csm, sms, items, work, st);
     if (kpt <= 4) return launch_conv_k<4>(d_jobs, d_start, njobs, maxM, csm, sms, items, work, st);
     return launch_conv_k<8>(d_jobs, d_start, njobs, maxM, csm, sms, items, work, st);
-}
-
-// Multi-job pair kernel per configuration (same (ILP, blocks/SM) table as
-// pick_cfg).
-void (*pick_multi(int cfg))(const PairArgs*, const unsigned int*, int, unsigned int*) {
-    switch (cfg) {
-        case 1: return k_pairs32m<2, 2>;
-        case 2: return k_pairs32m<1, 4>;
-        case 3: return k_pairs32m<1, 3>;
-        default: return k_pairs32m<2, 3>;
-    }
 }
 
 // ---------------------------------------------------------- autotuner ----
@@ -1365,13 +863,14 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
     g.tflags = a.take<uint8_t>((size_t)nb * nta);
     g.tlist = a.take<int>((size_t)nb * nta);
     g.bt0 = a.take<int>((size_t)nb * Lw.tstride);
-    a.take<int>(8);
+    g.misc = a.take<int>(8);
     g.acc = a.take<long long>((size_t)nb * nr * 2);
     g.refl = a.take<C32>((size_t)nb * nr);
     g.sscr = a.take<C32>((size_t)nb * Lw.surf_slot);
     const double* trb = g.trb;
     cudaMemsetAsync(g.vmax, 0, sizeof(unsigned long long) * nb, st);
     cudaMemsetAsync(g.dmin, 0xff, sizeof(unsigned long long) * nb, st);
+    cudaMemsetAsync(g.misc, 0, sizeof(int) * 8, st);
     cudaMemsetAsync(g.acc, 0, sizeof(long long) * nb * nr * 2, st);
     if (nf > 0) {
         k_cull_count<<<dim3((unsigned)((nf + RP_TILE - 1) / RP_TILE), nb), RP_TILE_THREADS, 0, st>>>(
@@ -1426,7 +925,6 @@ PairArgs seg_pair_args(const Seg& g) {
     P.eks = dp.lossless ? 0.f : (float)(-2.0 * dp.ks * dp.ks * 1.4426950408889634);
     P.nidx = dp.nidx; P.inv_dr = 1.0 / dp.dr; P.inv_lam = dp.turn;
     P.lossless = dp.lossless;
-    P.deg = g.deg;
     return P;
 }
 
@@ -1447,14 +945,14 @@ ConvArgs seg_conv_args(const Seg& g) {
 // Pair launch of a wave: the single-batch kernel (constants in the parameter
 // bank) for one segment, the multi-job kernel otherwise.  cap bounds the
 // items taken (autotuner probes); UINT_MAX runs everything.
-int launch_pairs(const std::vector<Seg*>& ps, const PairArgs* d_jobs, const unsigned int* d_start,
+int launch_pairs(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsigned int* d_start,
                  unsigned int* d_work, int cfg, int sms, cudaStream_t st) {
-    const size_t pair_smem = 2 * RP_CHUNK * sizeof(FacetRec) + (size_t)RP_WIN * RP_PAIR_THREADS * sizeof(float2);
+    const size_t pair_smem = RP_PAIR_SMEM_BYTES;
     if (ps.size() == 1) {
         const Seg& g = *ps[0];
         PairArgs P = seg_pair_args(g);
         P.work = d_work;
-        void (*pk)(PairArgs) = pick_pair_kernel(g.deg, cfg);
+        void (*pk)(const PairArgs) = pick_pair_kernel(g.deg, cfg);
         RP_CUDA(cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem));
         int occ = 0;
         RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, RP_PAIR_THREADS, pair_smem));
@@ -1462,14 +960,10 @@ int launch_pairs(const std::vector<Seg*>& ps, const PairArgs* d_jobs, const unsi
         const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(occ, 1) * sms, items));
         pk<<<grid, RP_PAIR_THREADS, pair_smem, st>>>(P);
     } else {
-        auto mk = pick_multi(cfg);
-        RP_CUDA(cudaFuncSetAttribute(mk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem));
-        int occ = 0;
-        RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mk, RP_PAIR_THREADS, pair_smem));
         int64_t items = 0;
         for (const Seg* g : ps) items += (int64_t)g->nb * ((g->L.tstride + RP_PAIR_THREADS - 1) / RP_PAIR_THREADS) * RP_PARTS;
-        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(occ, 1) * sms, items));
-        mk<<<grid, RP_PAIR_THREADS, pair_smem, st>>>(d_jobs, d_start, (int)ps.size(), d_work);
+        const int rc = launch_pairs_multi(cfg, d_jobs, d_start, (int)ps.size(), d_work, items, sms, st);
+        if (rc) return rc;
     }
     RP_LAUNCHED();
     return RP_OK;
@@ -1487,7 +981,7 @@ int zero_pairs(const std::vector<Seg*>& ps, unsigned int* d_work, cudaStream_t s
 
 // Choose the pair configuration of a wave: the tuned one, or probe all four
 // (each a full launch on this wave's items, outputs re-zeroed after).
-int choose_cfg(const std::vector<Seg*>& ps, const PairArgs* d_jobs, const unsigned int* d_start,
+int choose_cfg(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsigned int* d_start,
                unsigned int* d_work, int sms, cudaStream_t st, int* cfg_out) {
     const int multi = ps.size() > 1 ? 1 : 0;
     const int deg = multi ? -1 : ps[0]->deg;
@@ -1523,23 +1017,19 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     const int sms = segs[0].sc->sm_count;
     // ---- setup stage for every segment
     {
-        ArenaPlan pl;
-        pl.take<int>(8 * (size_t)nseg);
-        size_t need = pl.off;
+        size_t need = 0;
         for (Seg& g : segs) need += seg_setup_bytes(g.sc, g.Lw);
         int rc = ws->arena.reserve(need);
         if (rc) return rc;
     }
     Arena& a = ws->arena;
     a.reset();
-    int* misc_all = a.take<int>(8 * (size_t)nseg);
-    for (int i = 0; i < nseg; ++i) segs[i].misc = misc_all + 8 * i;
     g_timer.mark(0, st);
-    RP_CUDA(cudaMemsetAsync(misc_all, 0, sizeof(int) * 8 * nseg, st));
     for (Seg& g : segs) seg_setup(g, a, st);
     RP_CUDA(cudaGetLastError());
     std::vector<int> h_misc(8 * (size_t)nseg);
-    RP_CUDA(cudaMemcpyAsync(h_misc.data(), misc_all, sizeof(int) * 8 * nseg, cudaMemcpyDeviceToHost, st));
+    for (int i = 0; i < nseg; ++i)
+        RP_CUDA(cudaMemcpyAsync(&h_misc[8 * i], segs[i].misc, sizeof(int) * 8, cudaMemcpyDeviceToHost, st));
     g_timer.mark(1, st);
     RP_CUDA(cudaStreamSynchronize(st));
     g_timer.collect(0, 1);
@@ -1556,18 +1046,13 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         if (g.pairs && g.smem) cs.push_back(&g);
     }
     {
-        size_t need = 1024 + (ps.size() + cs.size()) * (sizeof(PairArgs) + sizeof(ConvArgs) + 64);
+        size_t need = 1024 + (ps.size() + cs.size()) * (sizeof(PairJob) + sizeof(ConvArgs) + 64);
         for (Seg& g : segs) need += seg_pair_bytes(g.sc, g.L);
         int rc = ws->arena2.reserve(need);
         if (rc) return rc;
     }
     Arena& b = ws->arena2;
     b.reset();
-    unsigned int* d_work = b.take<unsigned int>(4);
-    PairArgs* d_pjobs = b.take<PairArgs>(std::max<size_t>(ps.size(), 1));
-    unsigned int* d_pstart = b.take<unsigned int>(ps.size() + 1);
-    ConvArgs* d_cjobs = b.take<ConvArgs>(std::max<size_t>(cs.size(), 1));
-    unsigned int* d_cstart = b.take<unsigned int>(cs.size() + 1);
     for (Seg& g : segs) {
         g.T = b.take<C32>((size_t)RP_PARTS * g.nb * g.L.tstride * g.Wt);
         if (g.smem) {
@@ -1577,14 +1062,19 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
             g.cscr = b.take<C32>((size_t)g.L.slots * g.L.slot);
         }
     }
+    unsigned int* d_work = b.take<unsigned int>(4);
+    PairJob* d_pjobs = b.take<PairJob>(std::max<size_t>(ps.size(), 1));
+    unsigned int* d_pstart = b.take<unsigned int>(ps.size() + 1);
+    ConvArgs* d_cjobs = b.take<ConvArgs>(std::max<size_t>(cs.size(), 1));
+    unsigned int* d_cstart = b.take<unsigned int>(cs.size() + 1);
     RP_CUDA(cudaMemsetAsync(d_work, 0, sizeof(unsigned int) * 4, st));
     for (Seg& g : segs)
         RP_CUDA(cudaMemsetAsync(g.T, 0, sizeof(C32) * RP_PARTS * g.nb * g.L.tstride * g.Wt, st));
-    std::vector<PairArgs> hp;
+    std::vector<PairJob> hp;
     std::vector<unsigned int> hps(1, 0u);
     for (Seg* g : ps) {
-        hp.push_back(seg_pair_args(*g));
-        hps.push_back(hps.back() + (unsigned)(g->nb * hp.back().tblocks * RP_PARTS));
+        hp.push_back(PairJob{seg_pair_args(*g), g->deg});
+        hps.push_back(hps.back() + (unsigned)(g->nb * hp.back().a.tblocks * RP_PARTS));
     }
     std::vector<ConvArgs> hc;
     std::vector<unsigned int> hcs(1, 0u);
@@ -1599,7 +1089,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     }
     csm += (size_t)(maxM / 4) * sizeof(Cplx<float>);
     if (!hp.empty()) {
-        RP_CUDA(cudaMemcpyAsync(d_pjobs, hp.data(), sizeof(PairArgs) * hp.size(), cudaMemcpyHostToDevice, st));
+        RP_CUDA(cudaMemcpyAsync(d_pjobs, hp.data(), sizeof(PairJob) * hp.size(), cudaMemcpyHostToDevice, st));
         RP_CUDA(cudaMemcpyAsync(d_pstart, hps.data(), sizeof(unsigned int) * hps.size(), cudaMemcpyHostToDevice, st));
     }
     if (!hc.empty()) {
@@ -1658,7 +1148,8 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     g_timer.mark(4, st);
     RP_CUDA(cudaGetLastError());
     std::vector<std::vector<int>> cnt(nseg);
-    RP_CUDA(cudaMemcpyAsync(h_misc.data(), misc_all, sizeof(int) * 8 * nseg, cudaMemcpyDeviceToHost, st));
+    for (int i = 0; i < nseg; ++i)
+        RP_CUDA(cudaMemcpyAsync(&h_misc[8 * i], segs[i].misc, sizeof(int) * 8, cudaMemcpyDeviceToHost, st));
     for (int i = 0; i < nseg; ++i) {
         if (!segs[i].h_counts) continue;
         cnt[i].resize(2 * (size_t)segs[i].nb);

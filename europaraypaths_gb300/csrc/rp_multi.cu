@@ -1,0 +1,75 @@
+// rp_multi.cu -- the multi-job pair kernel: one persistent launch over the
+// work items of many batches (scenes of different sizes, bands, bin counts
+// and sinc degrees).  Its own translation unit (see rp_pair.cuh).
+#include <algorithm>
+
+#include "rp_internal.h"
+#include "rp_pair.cuh"
+
+namespace rpk {
+
+// Multi-job pair kernel: one persistent launch over the items of many
+// batches (scenes of different sizes, bin counts and sinc degrees).  Job j
+// owns items [start[j], start[j + 1]); a block copies the job's constants
+// into registers and dispatches on its sinc degree.
+template <int ILP, int MINB>
+__global__ void __launch_bounds__(RP_PAIR_THREADS, MINB)
+k_pairs32m(const PairJob* __restrict__ jobs, const unsigned int* __restrict__ start, int njobs,
+           unsigned int* work) {
+    RP_PAIR_SMEM_DECL
+    __shared__ int s_job;
+    const unsigned int total = start[njobs];
+    for (;;) {
+        if (tid == 0) {
+            const unsigned int it = atomicAdd(work, 1u);
+            int lo = 0, hi = njobs - 1;          // last j with start[j] <= it
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (start[mid] <= it) lo = mid; else hi = mid - 1;
+            }
+            s_item = it;
+            s_job = lo;
+        }
+        __syncthreads();
+        const unsigned int item = s_item;
+        const int j = s_job;
+        __syncthreads();
+        if (item >= total) break;
+        const PairArgs A = jobs[j].a;
+        const int deg = jobs[j].deg;
+        const unsigned int li = item - start[j];
+        const int part = li % RP_PARTS;
+        const int tb = (li / RP_PARTS) % A.tblocks;
+        const int s = li / (RP_PARTS * A.tblocks);
+        switch (deg) {
+            case 4: pair_item<4, ILP>(A, s, tb, part, bars, phase); break;
+            case 5: pair_item<5, ILP>(A, s, tb, part, bars, phase); break;
+            case 6: pair_item<6, ILP>(A, s, tb, part, bars, phase); break;
+            default: pair_item<0, ILP>(A, s, tb, part, bars, phase); break;
+        }
+    }
+    RP_PAIR_SMEM_END
+}
+
+void (*pick_multi(int cfg))(const PairJob*, const unsigned int*, int, unsigned int*) {
+    switch (cfg) {
+        case 1: return k_pairs32m<2, 2>;
+        case 2: return k_pairs32m<1, 4>;
+        case 3: return k_pairs32m<1, 3>;
+        default: return k_pairs32m<2, 3>;
+    }
+}
+
+int launch_pairs_multi(int cfg, const PairJob* d_jobs, const unsigned int* d_start, int njobs,
+                       unsigned int* d_work, int64_t items, int sms, cudaStream_t st) {
+    const size_t smem = RP_PAIR_SMEM_BYTES;
+    auto mk = pick_multi(cfg);
+    RP_CUDA(cudaFuncSetAttribute(mk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mk, RP_PAIR_THREADS, smem));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(occ, 1) * sms, items));
+    mk<<<grid, RP_PAIR_THREADS, smem, st>>>(d_jobs, d_start, njobs, d_work);
+    return RP_OK;
+}
+
+}  // namespace rpk
