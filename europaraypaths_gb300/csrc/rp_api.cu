@@ -288,6 +288,14 @@ static int build_tables(rp_scene* s) {
     }
     if ((rc = upload_cplx(host_dft(c1), &s->d_C1_64, &s->d_C1_32, &acc))) return rc;
     if ((rc = upload_cplx(host_dft(c2), &s->d_C2_64, &s->d_C2_32, &acc))) return rc;
+    if (s->dp.cmode == 1) {
+        // genChirp (radar_kernels.cu:454-466): sinc(i dr / res) + its wrap at nr
+        if ((rc = build_plan(s->planR, nr, &acc))) return rc;
+        std::vector<cd> cr(nr);
+        for (int i = 0; i < nr; ++i)
+            cr[i] = cd(host_sinc((double)i * p.dr / p.rng_res) + host_sinc((double)(i - nr) * p.dr / p.rng_res), 0.0);
+        if ((rc = upload_cplx(host_dft(cr), &s->d_CR_64, &s->d_CR_32, &acc))) return rc;
+    }
     // cropSpectrum (elementary_kernels.cu:258-278): keep |freq_k| <= B on the
     // N-point grid; the kept set is min(k, N-k) <= K.
     const int N = 2 * nr - 1;
@@ -368,11 +376,30 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
         rp_set_error("rp_scene_create: parameters not derived (call rp_params_derive)");
         return RP_ERR_ARG;
     }
-    if (p->specular || !p->convolution || !p->convolution_linear) {
-        rp_set_error("rp_scene_create: only the default mode (specular=false, convolution=true, "
-                     "convolution_linear=true) is implemented");
+    // Modes (sim.cu:733-986).  The reference defines: the default
+    // (non-specular, linear convolution); specular with linear convolution;
+    // specular without convolution or with circular convolution for ttype-0
+    // targets only.  Non-specular without linear convolution writes a 2nr
+    // chirp into an nr (or unallocated) buffer (sim.cu:411-438, 851-856), and
+    // ttype-1 targets without linear convolution use an unallocated chirp and
+    // temp buffer (sim.cu:864-872, 912): refused.  incoherent draws its
+    // phases from clock64() and is not reproducible: refused.
+    const bool lin = p->convolution && p->convolution_linear;
+    if (p->incoherent) {
+        rp_set_error("rp_scene_create: incoherent mode is not implemented (clock64 phases)");
         return RP_ERR_UNSUPPORTED;
     }
+    if (!p->specular && !lin) {
+        rp_set_error("rp_scene_create: non-specular mode needs convolution=true, convolution_linear=true");
+        return RP_ERR_UNSUPPORTED;
+    }
+    if (p->specular && !lin)
+        for (int64_t t = 0; t < nt; ++t)
+            if (targets[6 * nt + t] != 0.0) {
+                rp_set_error("rp_scene_create: specular mode without linear convolution supports ttype-0 "
+                             "targets only");
+                return RP_ERR_UNSUPPORTED;
+            }
     *out = nullptr;
     RP_CUDA(cudaSetDevice(device));
     rp_scene* s = new rp_scene();
@@ -389,6 +416,9 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
     d.turn = RP_PI_F / (RP_PI * p->lam);
     d.nr = p->nr; d.lossless = p->lossless; d.disable_surface = p->disable_surface;
     d.rerad_funct = p->rerad_funct;
+    d.specular = p->specular ? 1 : 0;
+    d.cmode = !p->convolution ? 2 : (p->convolution_linear ? 0 : 1);
+    d.c_over_c2 = p->c / p->c_2;
     int rc;
     auto fail = [&](int code) { rp_scene_destroy(s); return code; };
     cudaDeviceProp prop;
@@ -439,11 +469,12 @@ extern "C" int rp_scene_destroy(rp_scene* s) {
     if (s->own_stream) cudaStreamSynchronize(s->own_stream);
     void* ptrs[] = {s->d_facets, s->d_targets, s->d_prisms, s->d_order, s->d_sorted,
                     s->d_C1_64, s->d_C2_64, s->d_C1_32, s->d_C2_32, s->d_twS, s->d_C2S,
-                    s->d_HS};
+                    s->d_HS, s->d_CR_64, s->d_CR_32};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     free_plan(s->plan2);
     free_plan(s->planN);
+    free_plan(s->planR);
     s->ws.arena.release();
     s->ws.arena2.release();
     if (s->own_stream) cudaStreamDestroy(s->own_stream);

@@ -53,3 +53,23 @@ __device__ void conv_complex_block(const Cx<R>* sig, const Cx<R>* ker, const Pla
     for (int k = threadIdx.x; k < nr; k += blockDim.x) out[k] = cscale(A[2 * k], sc);
     __syncthreads();
 }
+
+// out[i] = (1/nr) IDFT_nr( DFT_nr(in) * C )[i]: the circular convolution of
+// convolvePhasorChirp (radar_kernels.cu:516-552).  x, wa, wb: scratch of
+// pl.M() values each.  `in` may alias `out`.
+template <class R>
+__device__ void conv_circular_block(const Cx<R>* in, const Cx<R>* C, const PlanV<R>& pl, int nr,
+                                    Cx<R>* x, Cx<R>* wa, Cx<R>* wb, Cx<R>* out) {
+    const int M = 1 << pl.log2M;
+    for (int k = threadIdx.x; k < M; k += blockDim.x)
+        x[k] = (k < nr) ? in[k] : Cx<R>{R(0), R(0)};
+    __syncthreads();
+    Cx<R>* r = block_dft<R>(x, wa, wb, pl, -1);
+    for (int k = threadIdx.x; k < nr; k += blockDim.x) r[k] = cmul(r[k], C[k]);
+    __syncthreads();
+    Cx<R>* a2 = (r == x) ? wa : x;
+    Cx<R>* r2 = block_dft<R>(r, a2, wb, pl, +1);
+    const R sc = R(1) / R(nr);
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) out[i] = cscale(r2[i], sc);
+    __syncthreads();
+}

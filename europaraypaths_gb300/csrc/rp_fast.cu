@@ -1218,6 +1218,11 @@ void next_segment(const rp_scene* sc, const std::vector<int>& ub, int64_t s0, in
 }
 
 int check_scene(const rp_scene* sc) {
+    if (sc->dp.specular || sc->dp.cmode != 0) {
+        rp_set_error("fast form: only the default mode (non-specular, linear convolution); the plain form "
+                     "runs the specular variants");
+        return RP_ERR_UNSUPPORTED;
+    }
     if (sc->any_ttype0) {
         rp_set_error("fast form: ttype-0 targets are handled by the plain form only");
         return RP_ERR_UNSUPPORTED;

@@ -36,6 +36,9 @@ struct DevParams {
     double turn;   // phase turns per metre of range: pi_F / (pi lam), so that
                    // exp(-j (2 pi_F / lam) r) = exp(-j 2 pi r turn) (radar_kernels.cu:682)
     int nr, lossless, disable_surface, rerad_funct;
+    int specular;        // specular mode (geometry_kernels.cu:434-446, 527-537, 563-570)
+    int cmode;           // 0 linear convolution, 1 circular, 2 none (sim.cu:733-986)
+    double c_over_c2;    // c / c_2 of refrRadarSignal's range (radar_kernels.cu:245)
 };
 
 // Grow-only device arena for per-call scratch.
@@ -103,6 +106,9 @@ struct rp_scene {
     // ---- per-scene spectral tables
     DftPlan plan2;                       // length 2 nr (linear chirp convolution)
     DftPlan planN;                       // length N = 2 nr - 1 (convolveComplex)
+    DftPlan planR;                       // length nr (circular convolution mode only)
+    double* d_CR_64 = nullptr;           // DFT_nr of genChirp's wrapped chirp (circular mode)
+    float* d_CR_32 = nullptr;
     double* d_C1_64 = nullptr;           // DFT_2nr of the surface chirp (complex)
     double* d_C2_64 = nullptr;           // DFT_2nr of the target chirp (complex)
     float* d_C1_32 = nullptr;

@@ -42,6 +42,21 @@ __device__ __forceinline__ double d_friis(double P, double Gt, double Gr, double
 }
 
 // geometry_kernels.cu:384-393
+// facetReradiation, geometry_kernels.cu:353-381 (sinc arguments without pi).
+__device__ __forceinline__ double d_facet_rerad(double th, double ph, double lam, double fs) {
+    double st = sin(th);
+    double s1 = d_sinc((fs / lam) * st * cos(ph));
+    double s2 = d_sinc((fs / lam) * st * sin(ph));
+    double v = (fs * fs / lam) * s1 * s2;
+    return v * v;
+}
+
+// snellsLaw, geometry_kernels.cu:490-501 (1e4 flags total internal reflection).
+__device__ __forceinline__ double d_snells(double th, double e1, double e2) {
+    double sR = sqrt(e1 / e2) * sin(th);
+    return sR > 1.0 ? 1e4 : asin(sR);
+}
+
 __device__ __forceinline__ double d_radar_eq(double P, double G, double fs, double lam, double d, double nf) {
     double num = P * G * G * fs * fs * fs * fs;
     double den = (4 * RP_PI_FRIIS) * (4 * RP_PI_FRIIS) * d * d * d * d;

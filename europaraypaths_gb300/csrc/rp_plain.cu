@@ -15,14 +15,18 @@ namespace {
 
 using C64 = Cx<double>;
 
-// compIncidentRays + snellsLaw + compReflectedEnergy (non-specular) + the
-// surface leg of surfacePT, per (trace, illuminated facet).
-// geometry_kernels.cu:103-140, 426-517; radar_kernels.cu:714-764.
+// compIncidentRays + snellsLaw + compReflectedEnergy + the surface leg, per
+// (trace, illuminated facet).  geometry_kernels.cu:103-140, 426-517.  The
+// surface leg: surfacePT's two-bin phasor (non-specular, radar_kernels.cu:
+// 714-764), genReflPhasor's one-bin phasor (specular with linear convolution,
+// :314-346); the other specular modes keep (Itd, fRe) for reflRadarSignal.
 __global__ void k_incident64(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx,
                              const int* __restrict__ nill, const double* __restrict__ traces,
                              DevParams dp, double* __restrict__ Itd_o, double* __restrict__ Gi_o,
                              double* __restrict__ frc_o, double* __restrict__ sx_o,
-                             C64* __restrict__ sv_o, unsigned long long* __restrict__ vmax) {
+                             C64* __restrict__ sv_o, unsigned long long* __restrict__ vmax,
+                             double* __restrict__ Rth_o, double* __restrict__ Iph_o,
+                             double* __restrict__ fre_o) {
     const int s = blockIdx.y;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nill[s]) return;
@@ -40,7 +44,12 @@ __global__ void k_incident64(const double* __restrict__ F, int64_t nf, const int
     double cI = cos(th), cR = cos(rth);
     double rho = (dp.nu2 * cI - dp.nu1 * cR) / (dp.nu2 * cI + dp.nu1 * cR);
     double frc = 1.0 - rho * rho;
-    double fre = rho * rho;
+    // specular: facetReradiation at twice the inclination times the radar
+    // equation (geometry_kernels.cu:434-446); non-specular: 1
+    double fre = dp.specular ? d_facet_rerad(2 * th, -ph, dp.lam, dp.fs) *
+                                   d_radar_eq(dp.P, t.grefl, dp.fs, dp.lam, d, (double)nill[s])
+                             : 1.0;
+    fre *= rho * rho;
     if (rth > 1e3) frc = 0.0;
     double atm = exp(-4.0 * dp.alpha1 * d);
     fre *= atm;
@@ -50,6 +59,23 @@ __global__ void k_incident64(const double* __restrict__ F, int64_t nf, const int
     Itd_o[o] = d;
     Gi_o[o] = G;
     frc_o[o] = frc;
+    Rth_o[o] = rth;
+    Iph_o[o] = ph;
+    fre_o[o] = fre;
+    if (dp.specular) {
+        if (dp.cmode == 0) {
+            // genReflPhasor: fRe e^{+j 4 pi_F Itd / lam} at bin (short)((Itd - rst)/dr)
+            double sn, cs;
+            sincos((4.0 * RP_PI_F / dp.lam) * d, &sn, &cs);
+            sx_o[o] = (d - t.rst) / dp.dr;
+            sv_o[o] = C64{fre * cs, fre * sn};
+            atomic_max_pos(vmax + s, fabs(fre));
+        } else {
+            sx_o[o] = -2.0;          // no binned surface trace in these modes
+            sv_o[o] = C64{0.0, 0.0};
+        }
+        return;
+    }
     // surfacePT: two Friis hops with the subsurface gain (radar_kernels.cu:722-733)
     double Pf = d_friis(dp.P, t.grefr, G, dp.lam, d);
     double Ps = d_friis(Pf, G, t.grefr, dp.lam, d);
@@ -64,9 +90,10 @@ __global__ void k_incident64(const double* __restrict__ F, int64_t nf, const int
 }
 
 // Fixed-point accumulation of the surface leg into acc[s][nr][2].
+// single: one truncated bin per facet (genPhasorTrace) instead of the split.
 __global__ void k_surf_fix64(int64_t nf, const int* __restrict__ nill, const double* __restrict__ sx,
                              const C64* __restrict__ sv, const unsigned long long* __restrict__ vmax,
-                             int nr, long long* __restrict__ acc) {
+                             int nr, long long* __restrict__ acc, int single) {
     const int s = blockIdx.y;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = nill[s];
@@ -81,6 +108,11 @@ __global__ void k_surf_fix64(int64_t nf, const int* __restrict__ nill, const dou
     double w = x - (double)b;
     C64 v = sv[o];
     long long* a = acc + (size_t)s * nr * 2;
+    if (single) {
+        fix_add(a + 2 * b, v.x, scale);
+        fix_add(a + 2 * b + 1, v.y, scale);
+        return;
+    }
     fix_add(a + 2 * b, v.x * (1.0 - w), scale);
     fix_add(a + 2 * b + 1, v.y * (1.0 - w), scale);
     if (b + 1 < nr) {
@@ -100,7 +132,8 @@ __global__ void k_pairs64(const double* __restrict__ F, int64_t nf, const int* _
                           const double* __restrict__ traces, DevParams dp,
                           const double* __restrict__ Itd, const double* __restrict__ Gi,
                           const double* __restrict__ frc, C64* __restrict__ PT,
-                          C64* __restrict__ PS) {
+                          C64* __restrict__ PS, const double* __restrict__ Rth,
+                          const double* __restrict__ Iph, double2* __restrict__ PD) {
     const int s = blockIdx.y;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= ntl[s]) return;
@@ -137,8 +170,16 @@ __global__ void k_pairs64(const double* __restrict__ F, int64_t nf, const int* _
         double att = exp(-4 * expo);
         double cT = cos(Tth);
         double rough = exp(-4 * ((dp.ks * cT) * (dp.ks * cT)));
-        double fEI = att * frc[o] * rough;
-        double fEO = fEI;   // compRefrEnergyOut applies the same factors
+        double fEI = att, fEO = att;
+        if (dp.specular) {
+            // compRefrEnergyIn / compRefrEnergyOut facet reradiation
+            // (geometry_kernels.cu:527-537, 563-570)
+            fEI *= d_facet_rerad(Rth[o] - Tth, Iph[o] - Tph, lam, fs);
+            double RrTh = d_snells(RP_PI_F - Tth, dp.eps2, dp.eps1);
+            fEO *= d_facet_rerad(RrTh, Tph - Iph[o], lam, fs);
+        }
+        fEI = fEI * frc[o] * rough;
+        fEO = fEO * frc[o] * rough;
         const double itd = Itd[o];
         if (ttype != 0) {
             double Gd = d_facet_G(TarTh, Tph, lam, fs);
@@ -165,6 +206,13 @@ __global__ void k_pairs64(const double* __restrict__ F, int64_t nf, const int* _
                     ps[b + 1] = cadd(ps[b + 1], cscale(u, w));
                 }
             }
+        } else if (dp.cmode == 2) {
+            // refrRadarSignal's per-facet amplitude and range: rerad of the
+            // facet-frame angle Tth and c / c2 (radar_kernels.cu:232-245)
+            double rr = d_rerad(dp.rerad_funct, Tth) * fEI * fEO;
+            double fSR = itd + Ttd;
+            rr *= d_radar_eq(dp.P, grefr, fs, lam, fSR, (double)nv);
+            PD[((size_t)s * tstride + q) * nf + j] = make_double2(rr, (fSR - Ttd) + Ttd * dp.c_over_c2);
         } else {
             double rr = d_rerad(dp.rerad_funct, TarTh) * fEI * fEO;
             double fSR = itd + Ttd;
@@ -184,11 +232,15 @@ __global__ void k_pairs64(const double* __restrict__ F, int64_t nf, const int* _
 // Range compression per target: Ptarg = linconv(PTtarg, chirp2); the
 // target's contribution = convolveComplex(Psour, Ptarg) (sim.cu:872, 912);
 // ttype 0: linconv(phasor trace, chirp2) (sim.cu:963).  Result -> PT row.
+// CT: the chirp spectrum of the target legs (chirp2; chirp1 in specular
+// mode, which never regenerates it, sim.cu:851-856); CR, pR: the wrapped
+// chirp of circular mode.
 __global__ void k_conv64(const int* __restrict__ ntl, int64_t tstride, int nb,
                          const double* __restrict__ TG, int64_t nt, const int* __restrict__ tlist,
                          C64* __restrict__ PT, const C64* __restrict__ PS, const C64* __restrict__ C2,
                          PlanV<double> p2, PlanV<double> pN, int crop_K, int crop_all, int nr,
-                         C64* __restrict__ scratch, size_t slot) {
+                         C64* __restrict__ scratch, size_t slot, int cmode, const C64* __restrict__ CR,
+                         PlanV<double> pR) {
     C64* base = scratch + (size_t)blockIdx.x * slot;
     const int M = max(1 << p2.log2M, 1 << pN.log2M);
     C64* x = base;
@@ -209,19 +261,29 @@ __global__ void k_conv64(const int* __restrict__ ntl, int64_t tstride, int nb,
         if (ttype != 0) {
             conv_linear_block<double>(pt, C2, p2, nr, x, wa, wb, ptarg, 1.0);
             conv_complex_block<double>(ps, ptarg, pN, nr, crop_K, crop_all, A, B, wa, wb, pt, 1.0);
-        } else {
+        } else if (cmode == 0) {
             conv_linear_block<double>(ps, C2, p2, nr, x, wa, wb, pt, 1.0);
+        } else if (cmode == 1) {
+            conv_circular_block<double>(ps, CR, pR, nr, x, wa, wb, pt);       // sim.cu:959
         }
     }
 }
 
 // Surface: fixed point -> complex, disable_surface, linconv with chirp1
 // (sim.cu:777-797).  One block per trace.
+// mode: 0 non-specular (disable_surface applies), 1 specular linear (it does
+// not, sim.cu:740-772), 2 zero (specular circular: the reference's surface
+// convolution is commented out, sim.cu:765-767).
 __global__ void k_surf_conv64(const long long* __restrict__ acc, const int* __restrict__ nill,
                               const unsigned long long* __restrict__ vmax, int disable, int nr,
                               const C64* __restrict__ C1, PlanV<double> p2,
-                              C64* __restrict__ refl, C64* __restrict__ scratch, size_t slot) {
+                              C64* __restrict__ refl, C64* __restrict__ scratch, size_t slot, int mode) {
     const int s = blockIdx.x;
+    if (mode == 2) {
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) refl[(size_t)s * nr + i] = C64{0.0, 0.0};
+        return;
+    }
+    if (mode == 1) disable = 0;
     C64* base = scratch + (size_t)s * slot;
     const int M = 1 << p2.log2M;
     C64* x = base;
@@ -236,6 +298,58 @@ __global__ void k_surf_conv64(const long long* __restrict__ acc, const int* __re
         in[i] = disable ? C64{0.0, 0.0} : C64{(double)a[2 * i] * inv, (double)a[2 * i + 1] * inv};
     __syncthreads();
     conv_linear_block<double>(in, C1, p2, nr, x, wa, wb, refl + (size_t)s * nr, 1.0);
+}
+
+// reflRadarSignal (radar_kernels.cu:58-160): per (trace, bin) the sum over the
+// illuminated facets (facet order) of fRe sinc((rst + ir dr - Itd)/res)
+// e^{+j 4 pi_F Itd / lam}.  Specular mode without convolution.
+__global__ void k_direct_refl64(const int* __restrict__ nill, const double* __restrict__ Itd,
+                                const double* __restrict__ fre, int64_t nf, const double* __restrict__ traces,
+                                DevParams dp, C64* __restrict__ refl) {
+    const int s = blockIdx.y;
+    const int ir = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ir >= dp.nr) return;
+    const TraceRow t = load_trace(traces, s);
+    const double r = t.rst + ir * dp.dr;
+    const int n = nill[s];
+    C64 acc{0.0, 0.0};
+    for (int j = 0; j < n; ++j) {
+        const size_t o = (size_t)s * nf + j;
+        const double d = Itd[o];
+        double sn, cs;
+        sincos((4.0 * RP_PI_F / dp.lam) * d, &sn, &cs);
+        const double a = d_sinc((r - d) / dp.rng_res) * fre[o];
+        acc.x += a * cs;
+        acc.y += a * sn;
+    }
+    refl[(size_t)s * dp.nr + ir] = acc;
+}
+
+// refrRadarSignal (radar_kernels.cu:201-300): per (trace, target, bin) the sum
+// over facets of rr sinc((rst + ir dr - rngt)/res) e^{+j 4 pi_F rngt / lam}
+// from the (rr, rngt) pairs k_pairs64 left in PD.  Result: the target's row of Z.
+__global__ void k_direct_refr64(const int* __restrict__ nill, const int* __restrict__ ntl, int64_t tstride,
+                                int64_t nf, const double2* __restrict__ PD, const double* __restrict__ traces,
+                                DevParams dp, C64* __restrict__ Z) {
+    const int s = blockIdx.z;
+    const int ir = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ir >= dp.nr) return;
+    const TraceRow t = load_trace(traces, s);
+    const double r = t.rst + ir * dp.dr;
+    const int n = nill[s];
+    for (int q = blockIdx.y; q < ntl[s]; q += gridDim.y) {
+        const double2* pd = PD + ((size_t)s * tstride + q) * nf;
+        C64 acc{0.0, 0.0};
+        for (int j = 0; j < n; ++j) {
+            const double2 v = pd[j];
+            double sn, cs;
+            sincos((4.0 * RP_PI_F / dp.lam) * v.y, &sn, &cs);
+            const double a = d_sinc((r - v.y) / dp.rng_res) * v.x;
+            acc.x += a * cs;
+            acc.y += a * sn;
+        }
+        Z[((size_t)s * tstride + q) * dp.nr + ir] = acc;
+    }
 }
 
 // sig = refl + sum_q refr_q in target order (sim.cu:980, 989).
@@ -291,6 +405,10 @@ void plain_take(A& a, const rp_scene* sc, const PlainLayout& L) {
     a.template take<C64>((size_t)L.nb * nr);               // refl
     a.template take<C64>((size_t)L.slots * L.slot);        // conv scratch
     a.template take<C64>((size_t)L.nb * L.surf_slot);      // surface conv scratch
+    a.template take<double>((size_t)L.nb * nf);            // Rth
+    a.template take<double>((size_t)L.nb * nf);            // Iph
+    a.template take<double>((size_t)L.nb * nf);            // fRe
+    if (sc->dp.cmode == 2) a.template take<double2>((size_t)L.nb * L.tstride * nf);   // (rr, rngt) per pair
 }
 
 PlainLayout plain_layout(const rp_scene* sc, int nb, int64_t tstride) {
@@ -394,6 +512,11 @@ int rp_plain_run(rp_scene* sc, rp_workspace* ws, const double* d_traces, int64_t
         C64* refl = a.take<C64>((size_t)nb * nr);
         C64* cscr = a.take<C64>((size_t)L.slots * L.slot);
         C64* sscr = a.take<C64>((size_t)nb * L.surf_slot);
+        double* Rth = a.take<double>((size_t)nb * nfa);
+        double* Iph = a.take<double>((size_t)nb * nfa);
+        double* fre = a.take<double>((size_t)nb * nfa);
+        double2* PD = (sc->dp.cmode == 2) ? a.take<double2>((size_t)nb * L.tstride * nfa) : nullptr;
+        const DevParams& dp = sc->dp;
         const double* trb = d_traces + 9 * s0;
 
         g_timer.mark(0, st);
@@ -422,29 +545,45 @@ int rp_plain_run(rp_scene* sc, rp_workspace* ws, const double* d_traces, int64_t
         }
         if (nf > 0) {
             k_incident64<<<dim3((unsigned)((nf + 255) / 256), nb), 256, 0, st>>>(
-                sc->d_facets, nf, idx, d_nill, trb, sc->dp, Itd, Gi, frc, sxv, sv, vmax);
+                sc->d_facets, nf, idx, d_nill, trb, sc->dp, Itd, Gi, frc, sxv, sv, vmax, Rth, Iph, fre);
             RP_LAUNCHED();
-            k_surf_fix64<<<dim3((unsigned)((nf + 255) / 256), nb), 256, 0, st>>>(
-                nfa, d_nill, sxv, sv, vmax, nr, acc);
-            RP_LAUNCHED();
+            if (!dp.specular || dp.cmode == 0) {
+                k_surf_fix64<<<dim3((unsigned)((nf + 255) / 256), nb), 256, 0, st>>>(
+                    nfa, d_nill, sxv, sv, vmax, nr, acc, dp.specular);
+                RP_LAUNCHED();
+            }
         }
         g_timer.mark(1, st);
         if (nt > 0 && nf > 0 && tmax > 0) {
             k_pairs64<<<dim3((unsigned)((L.tstride + 63) / 64), nb), 64, 0, st>>>(
                 sc->d_facets, nfa, idx, d_nill, sc->d_targets, nt, tlist, d_ntl, L.tstride,
-                sc->d_prisms, np, trb, sc->dp, Itd, Gi, frc, PT, PS);
+                sc->d_prisms, np, trb, sc->dp, Itd, Gi, frc, PT, PS, Rth, Iph, PD);
             RP_LAUNCHED();
             ++g_timer.pair_launches;
             g_timer.mark(2, st);
-            k_conv64<<<L.slots, 256, 0, st>>>(d_ntl, L.tstride, nb, sc->d_targets, nt, tlist, PT, PS,
-                                             (const C64*)sc->d_C2_64, p2, pN, sc->crop_K,
-                                             sc->crop_all, nr, cscr, L.slot);
+            if (dp.cmode == 2) {
+                k_direct_refr64<<<dim3((unsigned)((nr + 127) / 128), (unsigned)std::min<int64_t>(L.tstride, 65535), nb),
+                                  128, 0, st>>>(
+                    d_nill, d_ntl, L.tstride, nfa, PD, trb, dp, PT);
+            } else {
+                const C64* CT = (const C64*)(dp.specular ? sc->d_C1_64 : sc->d_C2_64);
+                k_conv64<<<L.slots, 256, 0, st>>>(d_ntl, L.tstride, nb, sc->d_targets, nt, tlist, PT, PS,
+                                                 CT, p2, pN, sc->crop_K, sc->crop_all, nr, cscr, L.slot,
+                                                 dp.cmode, (const C64*)sc->d_CR_64,
+                                                 dp.cmode == 1 ? plan_view64(sc->planR) : p2);
+            }
             RP_LAUNCHED();
         }
         if (!(nt > 0 && nf > 0 && tmax > 0)) g_timer.mark(2, st);
         g_timer.mark(3, st);
-        k_surf_conv64<<<nb, 256, 0, st>>>(acc, d_nill, vmax, sc->dp.disable_surface, nr,
-                                         (const C64*)sc->d_C1_64, p2, refl, sscr, L.surf_slot);
+        if (dp.specular && dp.cmode == 2) {
+            k_direct_refl64<<<dim3((unsigned)((nr + 127) / 128), nb), 128, 0, st>>>(d_nill, Itd, fre, nfa, trb,
+                                                                                  dp, refl);
+        } else {
+            const int smode = !dp.specular ? 0 : (dp.cmode == 0 ? 1 : 2);
+            k_surf_conv64<<<nb, 256, 0, st>>>(acc, d_nill, vmax, sc->dp.disable_surface, nr,
+                                             (const C64*)sc->d_C1_64, p2, refl, sscr, L.surf_slot, smode);
+        }
         RP_LAUNCHED();
         k_sum64<<<dim3((nr + 255) / 256, nb), 256, 0, st>>>(d_nill, d_ntl, L.tstride, refl, PT, nr,
                                                            d_out, out64, (int)s0);

@@ -1,6 +1,6 @@
 """Command-line drop-in for the reference's ``sim`` program.
 
-    python -m europaraypaths_gb300.sim params.json facets.fct targets.txt outdir [--form fast|plain]
+    python -m europaraypaths_gb300.sim params.json facets.fct targets.txt outdir [--form auto|fast|plain]
 
 Same arguments, JSON keys and input files as ``src/CUDA/sim.cu`` (main,
 sim.cu:92-1052): the parameter file (parseSimulationParameters), the facet
@@ -68,10 +68,21 @@ def load_inputs(params_path, facets_path, targets_path):
     return p, facets, targets, prisms, tr
 
 
-def run(params_path, facets_path, targets_path, outdir, form="fast", batch=64, quiet=False):
+def pick_form(p, targets):
+    """``auto``: the fast form for the default mode (non-specular, linear
+    convolution) without ttype-0 targets, else the plain FP64 form, which runs
+    every mode the reference defines."""
+    default_mode = (not p.specular) and p.convolution and p.convolution_linear
+    ttype0 = targets.shape[1] > 0 and bool(np.any(targets[6] == 0.0))
+    return "fast" if default_mode and not ttype0 else "plain"
+
+
+def run(params_path, facets_path, targets_path, outdir, form="auto", batch=64, quiet=False):
     t0 = time.perf_counter()
     fileio.check_directory(outdir)
     p, facets, targets, prisms, tr = load_inputs(params_path, facets_path, targets_path)
+    if form == "auto":
+        form = pick_form(p, np.asarray(targets).reshape(7, -1))
     from .simulator import Scene
     scene = Scene(p, facets, targets, prisms=prisms)
     fileio.clear_traces(outdir)
@@ -103,7 +114,7 @@ def main(argv=None):
     ap.add_argument("facets")
     ap.add_argument("targets")
     ap.add_argument("outdir")
-    ap.add_argument("--form", default="fast", choices=["fast", "plain"])
+    ap.add_argument("--form", default="auto", choices=["auto", "fast", "plain"])
     ap.add_argument("--batch", type=int, default=64, help="traces per engine call")
     a = ap.parse_args(argv)
     try:

@@ -9,9 +9,11 @@ It follows the reference line by line, vectorised over facets, for tiny scenes
 (``oracle/oracle.cpp``) is checked against it; both are checked against the
 analytic known-answer formulas of the reference's validation scenes.
 
-Mode covered: ``convolution=true, convolution_linear=true, specular=false``
+Modes covered: ``convolution=true, convolution_linear=true, specular=false``
 (the default written by ``param_gen.gen_params``), with ``lossless``,
-``disable_surface``, attenuation prisms and ``ttype`` 0/1 targets.
+``disable_surface``, attenuation prisms and ``ttype`` 0/1 targets; and the
+specular variants the reference defines: linear convolution (all targets),
+no convolution and circular convolution (``ttype`` 0 targets only).
 
 Reference citations are ``file:line`` inside the reference project.
 """
@@ -68,6 +70,44 @@ def rerad_funct(funcnum, th1):
         sigma = PI_F / 180
         return np.exp(-0.5 * th1 ** 2 / (sigma * sigma))
     return np.ones_like(th1)
+
+
+def facet_rerad(th, ph, lam, fs):
+    """facetReradiation, geometry_kernels.cu:353-381."""
+    s1 = sinc((fs / lam) * np.sin(th) * np.cos(ph))
+    s2 = sinc((fs / lam) * np.sin(th) * np.sin(ph))
+    return ((fs * fs / lam) * s1 * s2) ** 2
+
+
+def snells(th, e1, e2):
+    """snellsLaw, geometry_kernels.cu:490-501 (1e4 on total internal reflection)."""
+    sR = np.sqrt(e1 / e2) * np.sin(th)
+    return np.where(sR > 1.0, 1e4, np.arcsin(np.minimum(sR, 1.0)))
+
+
+def single_bin_trace(nr, x, ph):
+    """genReflPhasor/genRefrPhasor + genPhasorTrace: one truncated bin per
+    facet, out-of-range facets dropped (radar_kernels.cu:314-451)."""
+    b = np.trunc(x).astype(np.int64)
+    bad = (b < 0) | (b >= nr)
+    b[bad] = 0
+    ph = np.where(bad, 0.0, ph)
+    tr = np.zeros(nr, np.complex128)
+    np.add.at(tr, b, ph)
+    return tr
+
+
+def direct_sum(nr, rst, dr, res, rng, amp, lam):
+    """reflRadarSignal / refrRadarSignal: sum_f amp sinc((r - rng)/res) e^{j 4 pi rng / lam}
+    over every bin r = rst + ir dr (radar_kernels.cu:58-160, 201-300)."""
+    r = rst + np.arange(nr) * dr
+    ph = np.exp(1j * (4.0 * PI_F / lam) * rng) * amp
+    return (sinc((r[:, None] - rng[None, :]) / res) * ph[None, :]).sum(axis=1)
+
+
+def conv_circular(trace, chirp, nr):
+    """convolvePhasorChirp, radar_kernels.cu:516-552."""
+    return np.fft.ifft(np.fft.fft(trace) * np.fft.fft(chirp.astype(np.complex128)))
 
 
 def trunc_bin(x):
@@ -164,11 +204,17 @@ def simulate(p, facets, targets, traces, prisms=None):
     F = facets
     chirp1 = chirp_padded(nr, dr, p["rng_res"])
     chirp2 = chirp_padded(nr, dr, 2 * p["rng_res"])
+    spec = bool(p.get("specular", False))
+    cmode = 2 if not p.get("convolution", True) else (0 if p.get("convolution_linear", True) else 1)
+    chirpT = chirp1 if spec else chirp2            # specular never regenerates the chirp
+    ii = np.arange(nr)
+    chirpR = sinc(ii * dr / p["rng_res"]) + sinc((ii - nr) * dr / p["rng_res"])   # genChirp
     n_idx = np.sqrt(p["eps_2"])
     for s in range(traces.shape[0]):
         S = traces[s, 0:3]
         sn = traces[s, 3:6]
         rst = traces[s, 6]
+        grefl = traces[s, 7]
         grefr = traces[s, 8]
         # compSourceInclination + cropByAperture (geometry_kernels.cu:75-204)
         d = F[:, 0:3] - S
@@ -195,6 +241,8 @@ def simulate(p, facets, targets, traces, prisms=None):
         rho = (p["nu_2"] * cI - p["nu_1"] * cR) / (p["nu_2"] * cI + p["nu_1"] * cR)
         fRfrC = 1.0 - rho * rho
         fRe = rho * rho
+        if spec:
+            fRe = facet_rerad(2 * Ith, -Iph, lam, fs) * radar_eq(p["P"], grefl, fs, lam, Itd, nv) * fRe
         fRfrC = np.where(Rth > 1e3, 0.0, fRfrC)
         atm = np.exp(-4.0 * p["alpha1"] * Itd)
         fRe = fRe * atm
@@ -206,11 +254,19 @@ def simulate(p, facets, targets, traces, prisms=None):
         Ps = friis(Pf, G, grefr, lam, Itd)
         if not p["lossless"]:
             Ps = Ps * fRe
-        psurf = np.zeros(nr, np.complex128)
-        bin_split_add(psurf, nr, (Itd - rst) / dr, phasor(2 * Itd, lam) * np.sqrt(Ps))
-        if p["disable_surface"]:
-            psurf[:] = 0.0
-        refl = conv_linear(psurf, chirp1, nr)
+        if not spec:
+            psurf = np.zeros(nr, np.complex128)
+            bin_split_add(psurf, nr, (Itd - rst) / dr, phasor(2 * Itd, lam) * np.sqrt(Ps))
+            if p["disable_surface"]:
+                psurf[:] = 0.0
+            refl = conv_linear(psurf, chirp1, nr)
+        elif cmode == 0:
+            tr = single_bin_trace(nr, (Itd - rst) / dr, np.exp(1j * (4.0 * PI_F / lam) * Itd) * fRe)
+            refl = conv_linear(tr, chirp1, nr)
+        elif cmode == 2:
+            refl = direct_sum(nr, rst, dr, p["rng_res"], Itd, fRe, lam)
+        else:
+            refl = np.zeros(nr, np.complex128)
         # target loop (sim.cu:801-986)
         refr = np.zeros(nr, np.complex128)
         nt_in = 0
@@ -242,8 +298,13 @@ def simulate(p, facets, targets, traces, prisms=None):
             att = np.exp(-4 * expo)
             rough_t = np.exp(-4 * (p["ks"] * np.cos(Tth)) ** 2)
             # compRefrEnergyIn / compRefrEnergyOut (geometry_kernels.cu:520-584)
-            fEI = att * fRfrC * rough_t
-            fEO = att * fRfrC * rough_t
+            fEI = att.copy()
+            fEO = att.copy()
+            if spec:
+                fEI = fEI * facet_rerad(Rth - Tth, Iph - Tph, lam, fs)
+                fEO = fEO * facet_rerad(snells(PI_F - Tth, p["eps_2"], p["eps_1"]), Tph - Iph, lam, fs)
+            fEI = fEI * fRfrC * rough_t
+            fEO = fEO * fRfrC * rough_t
             fSR = Itd + Ttd
             if ttype != 0:
                 # accumulateTarget (radar_kernels.cu:767-830)
@@ -258,12 +319,18 @@ def simulate(p, facets, targets, traces, prisms=None):
                 rngt = Itd + Ttd * n_idx
                 pt = np.zeros(nr, np.complex128)
                 bin_split_add(pt, nr, (rngt - rst) / dr, phasor(rngt, lam) * np.sqrt(Pin * n_idx))
-                ptarg = conv_linear(pt, chirp2, nr)
+                ptarg = conv_linear(pt, chirpT, nr)
                 # radiateTarget (radar_kernels.cu:834-892)
                 ps = np.zeros(nr, np.complex128)
                 bin_split_add(ps, nr, (rngt - rst) / dr,
                               phasor(rngt - lam / 2.0, lam) * np.sqrt(Pout * n_idx))
                 refr += conv_complex(ps, ptarg, nr, p["smpl"], p["B"])
+            elif cmode == 2:
+                # refrRadarSignal: rerad of Tth, c / c2 (radar_kernels.cu:201-300)
+                rr = rerad_funct(p["rerad_funct"], Tth) * fEI * fEO
+                rr = rr * radar_eq(p["P"], grefr, fs, lam, fSR, nv)
+                rngt = (fSR - Ttd) + Ttd * (p["c"] / p["c_2"])
+                refr += direct_sum(nr, rst, dr, p["rng_res"], rngt, rr, lam)
             else:
                 # genRefrPhasor + genPhasorTrace + linear conv (radar_kernels.cu:351-448)
                 rr = rerad_funct(p["rerad_funct"], TarTh) * fEI * fEO
@@ -276,7 +343,7 @@ def simulate(p, facets, targets, traces, prisms=None):
                 ph[bad] = 0.0
                 tr = np.zeros(nr, np.complex128)
                 np.add.at(tr, b, ph)
-                refr += conv_linear(tr, chirp2, nr)
+                refr += conv_linear(tr, chirpT, nr) if cmode == 0 else conv_circular(tr, chirpR, nr)
         counts[s, 1] = nt_in
         out[s] = refl + refr
     return out, counts
@@ -325,6 +392,9 @@ def derive(j):
     p["rerad_funct"] = int(j.get("rerad_funct", 1))
     p["lossless"] = bool(j.get("lossless", False))
     p["disable_surface"] = bool(j.get("disable_surface", False))
+    p["specular"] = bool(j.get("specular", False))
+    p["convolution"] = bool(j.get("convolution", True))
+    p["convolution_linear"] = bool(j.get("convolution_linear", True))
     return p
 
 

@@ -8,7 +8,11 @@
  * It follows the reference (Nacnud04/EuropaRaypaths, src/CUDA/) line by line
  * for the default mode written by param_gen.gen_params (non-specular,
  * convolution, linear convolution), including attenuation prisms, lossless,
- * disable_surface and ttype 0 targets.  Each function cites the reference
+ * disable_surface and ttype 0 targets, and for the specular variants the
+ * reference defines: specular with linear convolution (all target types),
+ * specular without convolution and specular with circular convolution (ttype
+ * 0 targets only: for other targets the reference uses buffers it never
+ * allocates, sim.cu:411-445, 864-872).  Each function cites the reference
  * file:line it restates.  Deviations, all documented in the design notes:
  *   * the aperture test clamps the cosine to [-1, 1] before acos (the
  *     reference's unclamped acosf turns rounding above 1 into NaN and drops
@@ -90,6 +94,20 @@ inline double rerad(int f, double th1) {
 }
 
 inline double clamp1(double x) { return std::max(-1.0, std::min(1.0, x)); }
+
+// facetReradiation, geometry_kernels.cu:353-381 (sinc arguments without pi)
+inline double facet_rerad(double th, double ph, double lam, double fs) {
+    double s1 = sinc((fs / lam) * std::sin(th) * std::cos(ph));
+    double s2 = sinc((fs / lam) * std::sin(th) * std::sin(ph));
+    double v = (fs * fs / lam) * s1 * s2;
+    return v * v;
+}
+
+// snellsLaw, geometry_kernels.cu:490-501 (1e4 flags total internal reflection)
+inline double snells(double th, double e1, double e2) {
+    double sR = std::sqrt(e1 / e2) * std::sin(th);
+    return sR > 1.0 ? 1e4 : std::asin(sR);
+}
 
 // Two-bin linear split of surfacePT / accumulateTarget / radiateTarget,
 // radar_kernels.cu:736-760: bin = (short)x (truncation), w = x - bin.
@@ -221,6 +239,28 @@ std::vector<cd> chirp_spectrum(int nr, double dr, double res) {
     return c;
 }
 
+// genChirp, radar_kernels.cu:454-466: the sinc at the window start plus its
+// wrap at rst + nr dr, i.e. sinc(i dr / res) + sinc((i - nr) dr / res),
+// already transformed: returns DFT_nr of the real chirp.
+std::vector<cd> chirp_wrapped_spectrum(int nr, double dr, double res) {
+    std::vector<cd> c(nr), work;
+    for (int i = 0; i < nr; ++i)
+        c[i] = cd(sinc((double)i * dr / res) + sinc((double)(i - nr) * dr / res), 0.0);
+    dft(c.data(), nr, -1, work);
+    return c;
+}
+
+// convolvePhasorChirp, radar_kernels.cu:516-552: circular convolution of
+// length nr, scaled 1/nr.
+void conv_circular(const cd* tr, const std::vector<cd>& C, int nr, cd* out, std::vector<cd>& buf,
+                   std::vector<cd>& work) {
+    buf.assign(tr, tr + nr);
+    dft(buf.data(), nr, -1, work);
+    for (int i = 0; i < nr; ++i) buf[i] *= C[i];
+    dft(buf.data(), nr, +1, work);
+    for (int i = 0; i < nr; ++i) out[i] = buf[i] / (double)nr;
+}
+
 // convolvePhasorChirpLinear, radar_kernels.cu:554-649:
 // pad to 2nr, multiply spectra, inverse, scale 1/(2nr), window at nr/2.
 void conv_linear(const cd* tr, const std::vector<cd>& C, int nr, cd* out, std::vector<cd>& buf,
@@ -306,6 +346,14 @@ int oracle_simulate(const rp_params* P, const double* facets, int64_t nf,
     const double ap = p.aperture * (M_PI / 180.0);
     const double nidx = std::sqrt(p.eps_2);
     if (nr <= 0 || nf < 0 || nt < 0 || ns < 0) return RP_ERR_ARG;
+    // mode (sim.cu:733-986): conv mode 0 linear, 1 circular, 2 none
+    const bool spec = p.specular != 0;
+    const int cmode = !p.convolution ? 2 : (p.convolution_linear ? 0 : 1);
+    if (p.incoherent) return RP_ERR_UNSUPPORTED;
+    if (!spec && cmode != 0) return RP_ERR_UNSUPPORTED;   // chirp written past its buffer (sim.cu:431-438, 851-856)
+    if (spec && cmode != 0)
+        for (int64_t t = 0; t < nt; ++t)
+            if (targets[6 * nt + t] != 0.0) return RP_ERR_UNSUPPORTED;   // unallocated chirp / temp buffer
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
@@ -316,6 +364,10 @@ int oracle_simulate(const rp_params* P, const double* facets, int64_t nf,
 
     std::vector<cd> C1 = chirp_spectrum(nr, dr, p.rng_res);
     std::vector<cd> C2 = chirp_spectrum(nr, dr, 2 * p.rng_res);
+    // specular mode never regenerates the chirp: targets use C1 (sim.cu:851-856)
+    const std::vector<cd>& CT = spec ? C1 : C2;
+    std::vector<cd> CR;
+    if (cmode == 1) CR = chirp_wrapped_spectrum(nr, dr, p.rng_res);
     std::memset(out, 0, sizeof(double) * 2 * nr * ns);
 
     std::vector<int64_t> ill;
@@ -324,7 +376,7 @@ int oracle_simulate(const rp_params* P, const double* facets, int64_t nf,
         const double* tr = traces + 9 * s;
         const double sx = tr[0], sy = tr[1], sz = tr[2];
         const double snx = tr[3], sny = tr[4], snz = tr[5];
-        const double rst = tr[6], grefr = tr[8];
+        const double rst = tr[6], grefl = tr[7], grefr = tr[8];
         // compSourceInclination + cropByAperture, geometry_kernels.cu:75-204
         ill.clear();
         for (int64_t i = 0; i < nf; ++i) {
@@ -356,7 +408,11 @@ int oracle_simulate(const rp_params* P, const double* facets, int64_t nf,
             double cI = std::cos(th), cR = std::cos(rth);
             double rho = (p.nu_2 * cI - p.nu_1 * cR) / (p.nu_2 * cI + p.nu_1 * cR);
             double frc = 1.0 - rho * rho;
-            double fre = rho * rho;
+            // specular: facetReradiation at twice the inclination times the
+            // radar equation (geometry_kernels.cu:434-446); else 1
+            double fre = spec ? facet_rerad(2 * th, -ph, lam, fs) * radar_eq(p.power, grefl, fs, lam, d, (double)nv)
+                              : 1.0;
+            fre *= rho * rho;
             if (rth > 1e3) frc = 0.0;
             double atm = std::exp(-4.0 * p.alpha1 * d);
             fre *= atm; frc *= atm;
@@ -365,17 +421,40 @@ int oracle_simulate(const rp_params* P, const double* facets, int64_t nf,
             Gi[j] = facet_G(th, ph, lam, fs);
             fx[j] = F(0, i); fy[j] = F(1, i); fz[j] = F(2, i);
         }
-        // surfacePT, radar_kernels.cu:714-764 (facet order)
-        std::vector<cd> psurf(nr, cd(0, 0));
-        for (int64_t j = 0; j < nv; ++j) {
-            double Pf = friis(p.power, grefr, Gi[j], lam, Itd[j]);
-            double Ps = friis(Pf, Gi[j], grefr, lam, Itd[j]);
-            if (!p.lossless) Ps *= fRe[j];
-            split_add(psurf.data(), nr, (Itd[j] - rst) / dr, phasor(2 * Itd[j], lam) * std::sqrt(Ps));
-        }
-        if (p.disable_surface) std::fill(psurf.begin(), psurf.end(), cd(0, 0));
-        std::vector<cd> refl(nr), buf, wk;
-        conv_linear(psurf.data(), C1, nr, refl.data(), buf, wk);
+        std::vector<cd> refl(nr, cd(0, 0)), buf, wk;
+        if (!spec) {
+            // surfacePT, radar_kernels.cu:714-764 (facet order)
+            std::vector<cd> psurf(nr, cd(0, 0));
+            for (int64_t j = 0; j < nv; ++j) {
+                double Pf = friis(p.power, grefr, Gi[j], lam, Itd[j]);
+                double Ps = friis(Pf, Gi[j], grefr, lam, Itd[j]);
+                if (!p.lossless) Ps *= fRe[j];
+                split_add(psurf.data(), nr, (Itd[j] - rst) / dr, phasor(2 * Itd[j], lam) * std::sqrt(Ps));
+            }
+            if (p.disable_surface) std::fill(psurf.begin(), psurf.end(), cd(0, 0));
+            conv_linear(psurf.data(), C1, nr, refl.data(), buf, wk);
+        } else if (cmode == 0) {
+            // genReflPhasor + genPhasorTrace (radar_kernels.cu:314-346, 407-451):
+            // one truncated bin per facet, summed in facet order
+            std::vector<cd> ptr(nr, cd(0, 0));
+            for (int64_t j = 0; j < nv; ++j) {
+                double x = (Itd[j] - rst) / dr;
+                if (!(x > -1.0) || x >= (double)nr) continue;
+                double ph4 = (4.0 * PI_F / lam) * Itd[j];
+                ptr[(long)x] += cd(std::cos(ph4), std::sin(ph4)) * fRe[j];
+            }
+            conv_linear(ptr.data(), C1, nr, refl.data(), buf, wk);                     // sim.cu:770
+        } else if (cmode == 2) {
+            // reflRadarSignal, radar_kernels.cu:58-160 (facet order per bin)
+            for (int ir = 0; ir < nr; ++ir) {
+                cd acc(0, 0);
+                for (int64_t j = 0; j < nv; ++j) {
+                    double ph4 = (4.0 * PI_F / lam) * Itd[j];
+                    acc += cd(std::cos(ph4), std::sin(ph4)) * (sinc((rst + ir * dr - Itd[j]) / p.rng_res) * fRe[j]);
+                }
+                refl[ir] = acc;
+            }
+        }   // circular: the reference's surface convolution is commented out (sim.cu:765-767)
 
         // target loop, sim.cu:801-986: aperture test on the host (:808-826)
         std::vector<int64_t> tl;
@@ -393,6 +472,7 @@ int oracle_simulate(const rp_params* P, const double* facets, int64_t nf,
 #pragma omp parallel
         {
             std::vector<cd> pt(nr), ps(nr), ptarg(nr), b1, a2, b2, work;
+            std::vector<double> drr, drg;     // direct-sum phasors (no convolution)
 #pragma omp for schedule(dynamic, 1)
             for (int64_t q = 0; q < ntl; ++q) {
                 int64_t t = tl[q];
@@ -401,6 +481,8 @@ int oracle_simulate(const rp_params* P, const double* facets, int64_t nf,
                 int ttype = (int)TG(6, t);
                 std::fill(pt.begin(), pt.end(), cd(0, 0));
                 std::fill(ps.begin(), ps.end(), cd(0, 0));
+                drr.clear();
+                drg.clear();
                 for (int64_t j = 0; j < nv; ++j) {
                     int64_t i = ill[j];
                     // compTargetRays, geometry_kernels.cu:272-350
@@ -426,8 +508,14 @@ int oracle_simulate(const rp_params* P, const double* facets, int64_t nf,
                     // compRefrEnergyIn / compRefrEnergyOut, geometry_kernels.cu:520-584
                     double cT = std::cos(Tth);
                     double rough = std::exp(-4 * ((p.ks * cT) * (p.ks * cT)));
-                    double fEI = att * fRfrC[j] * rough;
-                    double fEO = att * fRfrC[j] * rough;
+                    double fEI = att, fEO = att;
+                    if (spec) {
+                        fEI *= facet_rerad(Rth[j] - Tth, Iph[j] - Tph, lam, fs);          // :528-537
+                        double RrTh = snells(PI_F - Tth, p.eps_2, p.eps_1);                // :565-570
+                        fEO *= facet_rerad(RrTh, Tph - Iph[j], lam, fs);
+                    }
+                    fEI = fEI * fRfrC[j] * rough;
+                    fEO = fEO * fRfrC[j] * rough;
                     double fSR = Itd[j] + Ttd;
                     if (ttype != 0) {
                         // accumulateTarget, radar_kernels.cu:767-830
@@ -442,6 +530,13 @@ int oracle_simulate(const rp_params* P, const double* facets, int64_t nf,
                         double Pout = friis(friis(1.0, grefr, Gi[j], lam, Itd[j]), Gt, Gd, lam, Ttd);
                         if (!p.lossless) Pout *= fEO;
                         split_add(ps.data(), nr, x, phasor(rngt - lam / 2.0, lam) * std::sqrt(Pout * nidx));
+                    } else if (cmode == 2) {
+                        // refrRadarSignal, radar_kernels.cu:201-300: rerad of the
+                        // facet-frame angle Tth and c / c2 (the reference's arguments)
+                        double rr = rerad(p.rerad_funct, Tth) * fEI * fEO;
+                        rr *= radar_eq(p.power, grefr, fs, lam, fSR, (double)nv);
+                        drr.push_back(rr);
+                        drg.push_back((fSR - Ttd) + Ttd * (p.c / p.c_2));
                     } else {
                         // genRefrPhasor, radar_kernels.cu:351-398 (binned into ps)
                         double rr = rerad(p.rerad_funct, TarTh) * fEI * fEO;
@@ -457,11 +552,23 @@ int oracle_simulate(const rp_params* P, const double* facets, int64_t nf,
                 }
                 cd* dst = refr_all.data() + (size_t)q * nr;
                 if (ttype != 0) {
-                    conv_linear(pt.data(), C2, nr, ptarg.data(), b1, work);                 // sim.cu:872
+                    conv_linear(pt.data(), CT, nr, ptarg.data(), b1, work);                 // sim.cu:872
                     conv_complex(ps.data(), ptarg.data(), nr, p.rx_sample_rate, p.bandwidth,
                                  dst, a2, b2, work);                                    // sim.cu:912
+                } else if (cmode == 0) {
+                    conv_linear(ps.data(), CT, nr, dst, b1, work);                          // sim.cu:963
+                } else if (cmode == 1) {
+                    conv_circular(ps.data(), CR, nr, dst, b1, work);                        // sim.cu:959
                 } else {
-                    conv_linear(ps.data(), C2, nr, dst, b1, work);                          // sim.cu:963
+                    for (int ir = 0; ir < nr; ++ir) {                                    // sim.cu:928-936
+                        cd acc(0, 0);
+                        for (size_t k = 0; k < drr.size(); ++k) {
+                            double ph4 = (4.0 * PI_F / lam) * drg[k];
+                            acc += cd(std::cos(ph4), std::sin(ph4)) *
+                                   (sinc((rst + ir * dr - drg[k]) / p.rng_res) * drr[k]);
+                        }
+                        dst[ir] = acc;
+                    }
                 }
             }
         }

@@ -87,8 +87,28 @@ def test_scene_create_rejects_bad_arguments(built_lib):
     h = ctypes.c_void_p()
     assert built_lib.rp_scene_create(ctypes.byref(p), None, 10, None, 0, None, 0, 0, ctypes.byref(h)) == -1
     assert built_lib.rp_scene_create(None, None, 0, None, 0, None, 0, 0, ctypes.byref(h)) == -1
-    q = param_gen.to_rp_params(dict(sc["params"], specular=True))
+    q = param_gen.to_rp_params(dict(sc["params"], convolution=False))
     f = np.ascontiguousarray(sc["facets"])
     assert built_lib.rp_scene_create(ctypes.byref(q), f.ctypes.data, f.shape[1], None, 0, None, 0, 0,
                                      ctypes.byref(h)) == -6
     assert built_lib.rp_simulate(None, None, 1, 1, None, 0, None, None) == -1
+
+
+@pytest.mark.parametrize("over,ttype", [({"convolution": False}, 1), ({"convolution_linear": False}, 1),
+                                        ({"specular": True, "convolution": False}, 1),
+                                        ({"specular": True, "convolution_linear": False}, 1),
+                                        ({"incoherent": True}, 1)])
+def test_scene_create_refuses_undefined_modes(built_lib, over, ttype):
+    # checked before any CUDA call: runs without a GPU
+    import ctypes
+    from europaraypaths_gb300 import _abi, param_gen, scenes
+    sc = scenes.small_plain(n_facets_side=8, n_targets_side=2, ns=1)
+    sc["params"].update(over)
+    p = param_gen.to_rp_params(sc["params"])
+    t = np.ascontiguousarray(sc["targets"])
+    t[6, :] = ttype
+    f = np.ascontiguousarray(sc["facets"])
+    h = ctypes.c_void_p()
+    rc = built_lib.rp_scene_create(ctypes.byref(p), f.ctypes.data, f.shape[1], t.ctypes.data, t.shape[1],
+                                   None, 0, 0, ctypes.byref(h))
+    assert rc == -6, _abi.last_error()

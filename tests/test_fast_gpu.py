@@ -86,3 +86,29 @@ def test_fast_polynomial_sinc_regimes(built_lib, oracle, nside):
     got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle, traces=tr)
     assert np.array_equal(cnt, rcnt)
     check(got, ref)
+
+
+def _vhf_scene(nr, n_side=120, fs=2.5, nt_side=4, ns=2, seed=5):
+    # 60 MHz / 10 MHz chirp sampled at 24 MHz, 2.5 m facets (the VHF band of
+    # the batched and flyby workloads), a rough layer 1 km deep
+    from europaraypaths_gb300 import scenes, simple_surfaces as ss
+    p = scenes.base_params(60e6, 10e6, 24e6, nr, 3.0, 3.15, 1e-6, 1.0, fs, 25e3, ns, 20.0, 7.3)
+    side = n_side * fs
+    dom = {"fs": fs, "nx": n_side, "ny": n_side, "ox": -side / 2, "oy": -side / 2}
+    h = scenes.gaussian_field(n_side, n_side, fs, 1.0, 20.0, seed)
+    facets = ss.surface_arrays(dom, "flat", heights=h)
+    tfs = side / nt_side
+    tdom = {"fs": tfs, "nx": nt_side, "ny": nt_side, "ox": -side / 2, "oy": -side / 2}
+    th = scenes.gaussian_field(nt_side, nt_side, tfs, 2.0, 50.0, seed + 1)
+    targets = ss.target_arrays(tdom, "flat", zoffset=-1000.0, heights=th)
+    return {"params": p, "facets": facets, "targets": targets}
+
+
+@pytest.mark.parametrize("nr", [4096, 8192])
+def test_fast_vhf_band(built_lib, oracle, nr):
+    # 4096 bins: shared-memory compression; 8192 bins: the global-scratch path
+    sc = _vhf_scene(nr)
+    got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle)
+    assert got.shape[1] == nr
+    assert np.array_equal(cnt, rcnt)
+    check(got, ref)

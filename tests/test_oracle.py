@@ -92,3 +92,42 @@ def test_oracle_target_cap(oracle):
     tr = tr_mod.linear_track(p)
     _, cnt = oracle.simulate(p, sc["facets"], sc["targets"], tr, max_targets=3)
     assert cnt[0, 1] == 3
+
+
+def _ttype0(sc):
+    sc["targets"][6, :] = 0.0
+    return sc
+
+
+@pytest.mark.parametrize("mode", ["specular_linear", "specular_none", "specular_circular"])
+def test_oracle_matches_numpy_specular_modes(oracle, mode):
+    # the specular variants the reference defines (sim.cu:733-986): linear
+    # convolution with every target type; no convolution and circular
+    # convolution with ttype 0 targets
+    over = {"specular": True, "rerad_funct": 0}
+    if mode == "specular_none":
+        over["convolution"] = False
+    if mode == "specular_circular":
+        over["convolution_linear"] = False
+    sc = tiny_scene(nside=24, ntside=3, ns=2, **over)
+    if mode == "specular_linear":
+        sc["targets"][6, ::2] = 0.0
+    else:
+        _ttype0(sc)
+    got, ref, cnt, rcnt = both(sc, oracle)
+    assert np.array_equal(cnt, rcnt)
+    assert np.abs(ref).max() > 0
+    assert rel_l2(got, ref) < 1e-11
+
+
+@pytest.mark.parametrize("over", [{"convolution": False}, {"convolution_linear": False},
+                                  {"specular": True, "convolution": False},
+                                  {"specular": True, "convolution_linear": False}])
+def test_oracle_rejects_undefined_modes(oracle, over):
+    # non-specular without linear convolution, and specular without linear
+    # convolution for ttype-1 targets, use buffers the reference never sized
+    # or allocated: the oracle refuses them (RP_ERR_UNSUPPORTED)
+    sc = tiny_scene(nside=12, ntside=2, ns=1, **over)
+    p, _ = prep(sc, oracle)
+    with pytest.raises(RuntimeError, match="-6"):
+        oracle.simulate(p, sc["facets"], sc["targets"], tr_mod.linear_track(p))

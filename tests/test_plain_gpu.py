@@ -53,3 +53,32 @@ def test_plain_disable_surface_and_empty_trace(built_lib, oracle):
     got, ref, cnt, rcnt = run_both(sc, oracle, traces=tr)
     assert cnt[1, 0] == 0 and np.all(got[1] == 0)
     assert rel_l2(got, ref) < 1e-10
+
+
+@pytest.mark.parametrize("mode", ["specular_linear", "specular_none", "specular_circular"])
+def test_plain_specular_modes(built_lib, oracle, mode):
+    # the specular variants of the reference trace loop (sim.cu:733-986):
+    # genReflPhasor/genRefrPhasor + linear convolution with every target type;
+    # reflRadarSignal/refrRadarSignal direct sums; circular convolution
+    over = {"specular": True, "rerad_funct": 0}
+    if mode == "specular_none":
+        over["convolution"] = False
+    if mode == "specular_circular":
+        over["convolution_linear"] = False
+    sc = tiny_scene(nside=24, ntside=3, ns=2, **over)
+    if mode == "specular_linear":
+        sc["targets"][6, ::2] = 0.0
+    else:
+        sc["targets"][6, :] = 0.0
+    got, ref, cnt, rcnt = run_both(sc, oracle)
+    assert np.array_equal(cnt, rcnt)
+    assert np.abs(ref).max() > 0
+    assert rel_l2(got, ref) < 1e-10
+
+
+def test_fast_form_refuses_specular(built_lib):
+    from europaraypaths_gb300 import simulator
+    sc = tiny_scene(nside=12, ntside=2, ns=1, specular=True)
+    with simulator.Scene(sc["params"], sc["facets"], sc["targets"]) as scene:
+        with pytest.raises(RuntimeError, match="RP_ERR_UNSUPPORTED|-6"):
+            scene.simulate(form="fast")
