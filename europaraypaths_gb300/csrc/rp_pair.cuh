@@ -127,6 +127,7 @@ struct Anchor {
     float tau0;           // frac(n T0 turn): phase of the anchor in turns
     float xbase;          // n T0 / dr - blo (bins, relative to the window start)
     float tnx, tny, tnz;  // target normal
+    float eaT0;           // ealpha T0: the attenuation exponent at the anchor
 };
 
 // Hardware approximations (PTX rsqrt/rcp/ex2 .approx.ftz): single
@@ -177,8 +178,7 @@ __device__ __forceinline__ void pair_eval(const FacetRec& r, const Anchor& an, c
     const float qd = fmaf(-2.f, dd, r.a.w);             // Ttd^2 - T0^2
     const float d2 = an.T0sq + qd;
     const float rinv = rsqrt_a(d2);
-    const float Ttd = d2 * rinv;
-    const float dT = qd * rcp_a(Ttd + an.T0);           // Ttd - T0 without cancellation
+    const float dT = qd * rcp_a(fmaf(d2, rinv, an.T0));  // Ttd - T0 without cancellation
     const float jx = (an.Dx - r.a.x) * rinv;
     const float jy = (an.Dy - r.a.y) * rinv;
     const float jz = (an.Dz - r.a.z) * rinv;
@@ -219,8 +219,9 @@ __device__ __forceinline__ void pair_eval(const FacetRec& r, const Anchor& an, c
         const float den = (z1 ? 1.f : a1) * (z2 ? 1.f : a2) * (z3 ? 1.f : a3) * (z4 ? 1.f : a4);
         S = __fdividef(num, den);
     }
-    // attenuation and roughness (zero constants when lossless)
-    const float e2 = fmaf(A.eks, cT * cT, A.ealpha * Ttd);
+    // attenuation and roughness (zero constants when lossless); ealpha Ttd
+    // = ealpha T0 + ealpha (Ttd - T0)
+    const float e2 = fmaf(A.eks, cT * cT, fmaf(A.ealpha, dT, an.eaT0));
     const float amp = r.d.w * fabsf(S) * rinv * ex2_a(e2);
     float tau = (r.c.w + an.tau0) + A.kt * dT;
     tau -= rintf(tau);
@@ -312,11 +313,17 @@ static __device__ __noinline__ void bin_add_edge(int b, float w, float vre, floa
 
 // Common case inline (both bins inside the window and the trace); the rest
 // (window spill, x < 0, the last bin) in bin_add_edge.
+// floor(x) as an integer (cvt.rmi: the conversion unit, not the FP32 pipe).
+__device__ __forceinline__ int floor_i(float x) {
+    int r;
+    asm("cvt.rmi.s32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
 __device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo, int b0,
                                         float2* win, int tid, C32* Trow, const PairArgs& A) {
-    const float t = (xr - 0.5f) + 12582912.0f;
-    const int sl = __float_as_int(t) - 0x4B400000;
-    const float w = xr - (t - 12582912.0f);
+    const int sl = floor_i(xr);
+    const float w = xr - (float)sl;
     const int b = blo + sl;
     if ((unsigned)sl < (unsigned)(RP_WIN - 1) && (unsigned)b < (unsigned)A.nr1) {
         float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
@@ -332,6 +339,25 @@ __device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo,
     } else {
         bin_add_edge(b, w, vre, vim, blo, b0, win, tid, Trow, A.nr, A.Wt, A.err);
     }
+}
+
+// bin_add for a chunk whose pairs all fall inside the window and the trace
+// (pair_item checks that per chunk and warp): no range tests, no edge path.
+// The clamp only keeps a (never expected) stray bin inside the window.
+__device__ __forceinline__ void bin_add_fast(float xr, float vre, float vim, float2* win, int tid) {
+    const int f = floor_i(xr);
+    const float w = xr - (float)f;
+    const unsigned sl = min((unsigned)f, (unsigned)(RP_WIN - 2));
+    float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
+    float2* p1 = p0 + RP_PAIR_THREADS;
+    float2 v0 = *p0, v1 = *p1;
+    const float w0 = 1.f - w;
+    v0.x = fmaf(vre, w0, v0.x);
+    v0.y = fmaf(vim, w0, v0.y);
+    v1.x = fmaf(vre, w, v1.x);
+    v1.y = fmaf(vim, w, v1.y);
+    *p0 = v0;
+    *p1 = v1;
 }
 
 // Dynamic shared memory of the pair kernels: two record buffers, the
@@ -395,6 +421,9 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         }
         phase[buf] ^= 1u;
         const FacetRec* R = srec + buf * RP_CHUNK;
+        Anchor an;
+        int blo = 0;
+        bool fits = true;
         if (active) {
             // FP64 anchors of this (chunk, target)
             const double mcx = mp->cx, mcy = mp->cy, mcz = mp->cz;
@@ -404,44 +433,71 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
             const double xt = A.nidx * T0 * A.inv_dr;
             const double tt = A.nidx * T0 * A.inv_lam;
             const double lo = (double)mp->xmin + A.nidx * (T0 - (double)mp->R) * A.inv_dr;
-            const int blo = (int)floor(lo) - 1;
-            Anchor an;
+            const double hi = (double)mp->xmax + A.nidx * (T0 + (double)mp->R) * A.inv_dr;
+            blo = (int)floor(lo) - 1;
+            // every pair's bin x lies in [lo, hi] (triangle inequality on the
+            // chunk's bounding radius); with half a bin of margin for FP32
+            // rounding, both split bins stay inside the window and the trace
+            fits = blo >= 0 && blo + RP_WIN <= A.nr1 && hi + 0.5 < (double)(blo + RP_WIN - 1);
             an.Dx = (float)Dx; an.Dy = (float)Dy; an.Dz = (float)Dz;
             an.T0 = (float)T0; an.T0sq = (float)(T0 * T0);
             an.tau0 = (float)(tt - floor(tt));
             an.xbase = (float)(xt - (double)blo);
             an.tnx = tnx; an.tny = tny; an.tnz = tnz;
+            an.eaT0 = (float)((double)A.ealpha * T0);
+        }
+        const bool all_fit = __all_sync(0xffffffffu, fits);
+        if (active) {
             for (int w = 0; w < RP_WIN; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
             const int cnt = mp->n;
             const bool prisms = (A.np > 0) && !A.lossless;
             int jj = 0;
-            if (ILP == 2)
-            for (; jj + 1 < cnt; jj += 2) {
-                const FacetRec r0 = R[jj];
-                const FacetRec r1 = R[jj + 1];
-                float x0, re0, im0, x1, re1, im1;
-                pair_eval<NT>(r0, an, A, x0, re0, im0);
-                pair_eval<NT>(r1, an, A, x1, re1, im1);
-                if (prisms) {
-                    const float f0 = prism_factor(r0.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
-                                                  A.PR, A.np, A.ealpha);
-                    const float f1 = prism_factor(r1.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
-                                                  A.PR, A.np, A.ealpha);
-                    re0 *= f0; im0 *= f0; re1 *= f1; im1 *= f1;
+            if (all_fit && !prisms) {
+                if (ILP == 2)
+                for (; jj + 1 < cnt; jj += 2) {
+                    const FacetRec r0 = R[jj];
+                    const FacetRec r1 = R[jj + 1];
+                    float x0, re0, im0, x1, re1, im1;
+                    pair_eval<NT>(r0, an, A, x0, re0, im0);
+                    pair_eval<NT>(r1, an, A, x1, re1, im1);
+                    bin_add_fast(x0, re0, im0, win, tid);
+                    bin_add_fast(x1, re1, im1, win, tid);
                 }
-                bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
-                bin_add(x1, re1, im1, blo, b0, win, tid, Trow, A);
-            }
-            for (; jj < cnt; ++jj) {
-                const FacetRec r0 = R[jj];
-                float x0, re0, im0;
-                pair_eval<NT>(r0, an, A, x0, re0, im0);
-                if (prisms) {
-                    const float f0 = prism_factor(r0.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
-                                                  A.PR, A.np, A.ealpha);
-                    re0 *= f0; im0 *= f0;
+                for (; jj < cnt; ++jj) {
+                    const FacetRec r0 = R[jj];
+                    float x0, re0, im0;
+                    pair_eval<NT>(r0, an, A, x0, re0, im0);
+                    bin_add_fast(x0, re0, im0, win, tid);
                 }
-                bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
+            } else {
+                if (ILP == 2)
+                for (; jj + 1 < cnt; jj += 2) {
+                    const FacetRec r0 = R[jj];
+                    const FacetRec r1 = R[jj + 1];
+                    float x0, re0, im0, x1, re1, im1;
+                    pair_eval<NT>(r0, an, A, x0, re0, im0);
+                    pair_eval<NT>(r1, an, A, x1, re1, im1);
+                    if (prisms) {
+                        const float f0 = prism_factor(r0.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
+                                                      A.PR, A.np, A.ealpha);
+                        const float f1 = prism_factor(r1.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
+                                                      A.PR, A.np, A.ealpha);
+                        re0 *= f0; im0 *= f0; re1 *= f1; im1 *= f1;
+                    }
+                    bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
+                    bin_add(x1, re1, im1, blo, b0, win, tid, Trow, A);
+                }
+                for (; jj < cnt; ++jj) {
+                    const FacetRec r0 = R[jj];
+                    float x0, re0, im0;
+                    pair_eval<NT>(r0, an, A, x0, re0, im0);
+                    if (prisms) {
+                        const float f0 = prism_factor(r0.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
+                                                      A.PR, A.np, A.ealpha);
+                        re0 *= f0; im0 *= f0;
+                    }
+                    bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
+                }
             }
             // flush the window into the owned trace
             for (int w = 0; w < RP_WIN; ++w) {
