@@ -440,8 +440,18 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
             __syncthreads();
             curM = M;
         }
-        const int s = item / A.nsplit;
-        const int sp = item % A.nsplit;
+        // the job's arguments in registers (the loops below store to shared
+        // memory, which would otherwise force re-reads of A)
+        const Cplx<float>* __restrict__ C2s = A.C2s;
+        const Cplx<float>* __restrict__ Hs = A.Hs;
+        const C32* __restrict__ T = A.T;
+        const int Wt = A.Wt, nbA = A.nb, log2M = A.log2M, nsplit = A.nsplit;
+        const int64_t tstride = A.tstride;
+        const float sig_scale = A.sig_scale;
+        const int* __restrict__ bt0 = A.bt0;
+        C32* __restrict__ part = A.part;
+        const int s = item / nsplit;
+        const int sp = item % nsplit;
         const int nq = A.ntl[s];
         const int q0 = sp * RP_CONV_SPLIT;
         if (q0 >= nq) continue;
@@ -450,14 +460,14 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
 #pragma unroll
         for (int i = 0; i < KPT; ++i) { accr[i] = 0.f; acci[i] = 0.f; }
         for (int q = q0; q < q1; ++q) {
-            const int b0 = A.bt0[(size_t)s * A.tstride + q];
+            const int b0 = bt0[(size_t)s * tstride + q];
             #pragma unroll 8
             for (int k = tid; k < n2; k += RP_CONV_THREADS) {
                 Cplx<float> v{0.f, 0.f};
                 const int o = k - b0;
-                if (k < nr && o >= 0 && o < A.Wt) {
+                if (k < nr && o >= 0 && o < Wt) {
                     for (int p = 0; p < RP_PARTS; ++p) {
-                        const C32 u = A.T[(((size_t)p * A.nb + s) * A.tstride + q) * A.Wt + o];
+                        const C32 u = T[(((size_t)p * nbA + s) * tstride + q) * Wt + o];
                         v.x += u.x;
                         v.y += u.y;
                     }
@@ -465,11 +475,11 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
                 X[k] = v;
             }
             __syncthreads();
-            block_dif_u<float, 4>(X, n2, TWs, A.log2M);
+            block_dif_u<float, 4>(X, n2, TWs, log2M);
             #pragma unroll 8
-            for (int k = tid; k < n2; k += RP_CONV_THREADS) W[k] = c_mul(X[k], A.C2s[k]);
+            for (int k = tid; k < n2; k += RP_CONV_THREADS) W[k] = c_mul(X[k], C2s[k]);
             __syncthreads();
-            block_dit_u<float, 4>(W, n2, TWs, A.log2M);
+            block_dit_u<float, 4>(W, n2, TWs, log2M);
             {   // Ptarg = W[nr/2 + k] / n2 moved to the front, zero padded
                 const float inv = 1.f / (float)n2;
                 Cplx<float> keep[KPT];
@@ -488,9 +498,9 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
                 for (int k = nr + tid; k < n2; k += RP_CONV_THREADS) W[k] = Cplx<float>{0.f, 0.f};
                 __syncthreads();
             }
-            block_dif_u<float, 4>(W, n2, TWs, A.log2M);
+            block_dif_u<float, 4>(W, n2, TWs, log2M);
             {
-                const float sc = A.sig_scale / (float)n2;
+                const float sc = sig_scale / (float)n2;
                 #pragma unroll 8
                 for (int k = tid; k < n2; k += RP_CONV_THREADS) {
                     Cplx<float> v = c_mul(X[k], W[k]);
@@ -498,18 +508,18 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
                 }
             }
             __syncthreads();
-            block_dit_u<float, 4>(W, n2, TWs, A.log2M);                 // u (natural, N values)
+            block_dit_u<float, 4>(W, n2, TWs, log2M);                 // u (natural, N values)
             #pragma unroll 8
             for (int k = N + tid; k < M; k += RP_CONV_THREADS) W[k] = Cplx<float>{0.f, 0.f};
             __syncthreads();
             // cropSpectrum + inverse DFT on the N grid = circular convolution
             // with the crop kernel h: linear convolution at M >= 2N - 1, then
             // circ[n] = lin[n] + lin[n + N]
-            block_dif_u<float, 4>(W, M, TWs, A.log2M);
+            block_dif_u<float, 4>(W, M, TWs, log2M);
             #pragma unroll 8
-            for (int k = tid; k < M; k += RP_CONV_THREADS) W[k] = c_mul(W[k], A.Hs[k]);
+            for (int k = tid; k < M; k += RP_CONV_THREADS) W[k] = c_mul(W[k], Hs[k]);
             __syncthreads();
-            block_dit_u<float, 4>(W, M, TWs, A.log2M);
+            block_dit_u<float, 4>(W, M, TWs, log2M);
 #pragma unroll
             for (int i = 0; i < KPT; ++i) {
                 const int j = tid + i * RP_CONV_THREADS;
@@ -521,7 +531,7 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
             }
             __syncthreads();
         }
-        C32* out = A.part + ((size_t)s * A.nsplit + sp) * nr;
+        C32* out = part + ((size_t)s * nsplit + sp) * nr;
 #pragma unroll
         for (int i = 0; i < KPT; ++i) {
             const int j = tid + i * RP_CONV_THREADS;

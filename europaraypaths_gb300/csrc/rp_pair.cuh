@@ -179,29 +179,44 @@ __device__ __forceinline__ void pair_eval(const FacetRec& r, const Anchor& an, c
     const float d2 = an.T0sq + qd;
     const float rinv = rsqrt_a(d2);
     const float dT = qd * rcp_a(fmaf(d2, rinv, an.T0));  // Ttd - T0 without cancellation
-    const float jx = (an.Dx - r.a.x) * rinv;
-    const float jy = (an.Dy - r.a.y) * rinv;
-    const float jz = (an.Dz - r.a.z) * rinv;
-    float cT = -fmaf(jx, r.b.x, fmaf(jy, r.b.y, jz * r.b.z));
-    float cD = -fmaf(jx, an.tnx, fmaf(jy, an.tny, jz * an.tnz));
-    const float yu = fmaf(jx, r.c.x, fmaf(jy, r.c.y, jz * r.c.z));
-    const float xv = fmaf(jx, r.d.x, fmaf(jy, r.d.y, jz * r.d.z));
-    const float X = xv * xv, Y = yu * yu;
-    const float h2 = X + Y;
-    float S;
+    float S, cT2;
     if (NT > 0) {
-        // 1 - c^2 may round a hair below 0 for |c| ~ 1: harmless in the polynomial
-        const float aT = fmaf(-cT, cT, 1.f);
-        const float aD = fmaf(-cD, cD, 1.f);
+        // The polynomial sinc needs only ratios of the direction's dot
+        // products, so the direction e = target - facet is not normalised:
+        // cos^2(Tth) = (e.n)^2 / |e|^2, 1 - cos^2 per angle, and the squared
+        // in-plane split xx = pik^2 (e.v)^2 / ((e.u)^2 + (e.v)^2), yy =
+        // pik^2 - xx (atan2(0, 0) = 0 gives xx = pik^2, yy = 0).  1 - c^2 may
+        // round a hair below 0 for |c| ~ 1: harmless in the polynomial.
+        const float ex = an.Dx - r.a.x, ey = an.Dy - r.a.y, ez = an.Dz - r.a.z;
+        const float pb = fmaf(ex, r.b.x, fmaf(ey, r.b.y, ez * r.b.z));
+        const float pt = fmaf(ex, an.tnx, fmaf(ey, an.tny, ez * an.tnz));
+        const float pc = fmaf(ex, r.c.x, fmaf(ey, r.c.y, ez * r.c.z));
+        const float pd = fmaf(ex, r.d.x, fmaf(ey, r.d.y, ez * r.d.z));
+        const float inv_d2 = rcp_a(d2);
+        const float pb2 = pb * pb;
+        cT2 = pb2 * inv_d2;
+        const float aT = 1.f - cT2;
+        const float aD = fmaf(-pt * pt, inv_d2, 1.f);
+        const float X = pd * pd;
+        const float h2 = fmaf(pc, pc, X);
         const bool hz = !(h2 > 0.f);
         const float k2 = A.pik2 * rcp_a(h2);
         const float xx = hz ? A.pik2 : k2 * X;
-        const float yy = hz ? 0.f : k2 * Y;
+        const float yy = A.pik2 - xx;
         S = sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aT * xx) * sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aT * yy) *
             sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aD * xx) * sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aD * yy);
     } else {
+        const float jx = (an.Dx - r.a.x) * rinv;
+        const float jy = (an.Dy - r.a.y) * rinv;
+        const float jz = (an.Dz - r.a.z) * rinv;
+        float cT = -fmaf(jx, r.b.x, fmaf(jy, r.b.y, jz * r.b.z));
+        float cD = -fmaf(jx, an.tnx, fmaf(jy, an.tny, jz * an.tnz));
+        const float yu = fmaf(jx, r.c.x, fmaf(jy, r.c.y, jz * r.c.z));
+        const float xv = fmaf(jx, r.d.x, fmaf(jy, r.d.y, jz * r.d.z));
+        const float h2 = fmaf(yu, yu, xv * xv);
         cT = fminf(1.f, fmaxf(-1.f, cT));
         cD = fminf(1.f, fmaxf(-1.f, cD));
+        cT2 = cT * cT;
         const float aT = fmaf(-cT, cT, 1.f);
         const float aD = fmaf(-cD, cD, 1.f);
         const bool hz = !(h2 > 0.f);
@@ -221,7 +236,7 @@ __device__ __forceinline__ void pair_eval(const FacetRec& r, const Anchor& an, c
     }
     // attenuation and roughness (zero constants when lossless); ealpha Ttd
     // = ealpha T0 + ealpha (Ttd - T0)
-    const float e2 = fmaf(A.eks, cT * cT, fmaf(A.ealpha, dT, an.eaT0));
+    const float e2 = fmaf(A.eks, cT2, fmaf(A.ealpha, dT, an.eaT0));
     const float amp = r.d.w * fabsf(S) * rinv * ex2_a(e2);
     float tau = (r.c.w + an.tau0) + A.kt * dT;
     tau -= rintf(tau);
