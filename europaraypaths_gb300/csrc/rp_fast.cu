@@ -475,11 +475,11 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
                 X[k] = v;
             }
             __syncthreads();
-            block_dif_u<float, 4>(X, n2, TWs, log2M);
+            block_dif_f<float>(X, n2, TWs, log2M);
             #pragma unroll 8
             for (int k = tid; k < n2; k += RP_CONV_THREADS) W[k] = c_mul(X[k], C2s[k]);
             __syncthreads();
-            block_dit_u<float, 4>(W, n2, TWs, log2M);
+            block_dit_f<float>(W, n2, TWs, log2M);
             {   // Ptarg = W[nr/2 + k] / n2 moved to the front, zero padded
                 const float inv = 1.f / (float)n2;
                 Cplx<float> keep[KPT];
@@ -498,7 +498,7 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
                 for (int k = nr + tid; k < n2; k += RP_CONV_THREADS) W[k] = Cplx<float>{0.f, 0.f};
                 __syncthreads();
             }
-            block_dif_u<float, 4>(W, n2, TWs, log2M);
+            block_dif_f<float>(W, n2, TWs, log2M);
             {
                 const float sc = sig_scale / (float)n2;
                 #pragma unroll 8
@@ -508,18 +508,18 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
                 }
             }
             __syncthreads();
-            block_dit_u<float, 4>(W, n2, TWs, log2M);                 // u (natural, N values)
+            block_dit_f<float>(W, n2, TWs, log2M);                 // u (natural, N values)
             #pragma unroll 8
             for (int k = N + tid; k < M; k += RP_CONV_THREADS) W[k] = Cplx<float>{0.f, 0.f};
             __syncthreads();
             // cropSpectrum + inverse DFT on the N grid = circular convolution
             // with the crop kernel h: linear convolution at M >= 2N - 1, then
             // circ[n] = lin[n] + lin[n + N]
-            block_dif_u<float, 4>(W, M, TWs, log2M);
+            block_dif_f<float>(W, M, TWs, log2M);
             #pragma unroll 8
             for (int k = tid; k < M; k += RP_CONV_THREADS) W[k] = c_mul(W[k], Hs[k]);
             __syncthreads();
-            block_dit_u<float, 4>(W, M, TWs, log2M);
+            block_dit_f<float>(W, M, TWs, log2M);
 #pragma unroll
             for (int i = 0; i < KPT; ++i) {
                 const int j = tid + i * RP_CONV_THREADS;

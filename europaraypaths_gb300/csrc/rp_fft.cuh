@@ -281,4 +281,108 @@ __device__ __noinline__ void block_dit_u(Cplx<T>* a, int n, const Cplx<T>* tws, 
         __syncthreads();
     }
 }
+// Fused radix-4 stage pairs ("radix 16"): the 16 elements a[base + i*S],
+// i < 16, are closed under two consecutive radix-4 stages (DIF spans L, L/4
+// with S = L/16; DIT spans L, 4L with S = L/4), so one thread keeps them in
+// registers across both and a transform makes about half the passes over
+// shared memory (and half the barriers).  The stage schedule is the one
+// above, so outputs keep the same digit-reversed order.  Twiddles are
+// applied unconditionally (tw(0) = 1 exactly).
+template <class T>
+__device__ __forceinline__ void r4_dif_reg(Cplx<T>& x0, Cplx<T>& x1, Cplx<T>& x2, Cplx<T>& x3, Cplx<T> w1) {
+    const Cplx<T> t0 = c_add(x0, x2), t1 = c_sub(x0, x2), t2 = c_add(x1, x3), t3 = c_sub(x1, x3);
+    const Cplx<T> y1 = Cplx<T>{t1.x + t3.y, t1.y - t3.x};
+    const Cplx<T> y3 = Cplx<T>{t1.x - t3.y, t1.y + t3.x};
+    const Cplx<T> w2 = c_mul(w1, w1), w3 = c_mul(w1, w2);
+    x0 = c_add(t0, t2);
+    x1 = c_mul(y1, w1);
+    x2 = c_mul(c_sub(t0, t2), w2);
+    x3 = c_mul(y3, w3);
+}
+
+template <class T>
+__device__ __forceinline__ void r4_dit_reg(Cplx<T>& x0, Cplx<T>& x1, Cplx<T>& x2, Cplx<T>& x3, Cplx<T> w1) {
+    const Cplx<T> w2 = c_mul(w1, w1), w3 = c_mul(w1, w2);
+    const Cplx<T> v1 = c_mulc(x1, w1), v2 = c_mulc(x2, w2), v3 = c_mulc(x3, w3);
+    const Cplx<T> t0 = c_add(x0, v2), t1 = c_sub(x0, v2), t2 = c_add(v1, v3), t3 = c_sub(v1, v3);
+    x0 = c_add(t0, t2);
+    x2 = c_sub(t0, t2);
+    x1 = Cplx<T>{t1.x - t3.y, t1.y + t3.x};
+    x3 = Cplx<T>{t1.x + t3.y, t1.y - t3.x};
+}
+
+template <class T>
+__device__ __noinline__ void block_dif_f(Cplx<T>* a, int n, const Cplx<T>* tws, int log2M) {
+    const int m = fft_log2(n);
+    int L = n, lL = m;
+    for (; L >= 16; L >>= 4, lL -= 4) {
+        const int lS = lL - 4, S = 1 << lS;           // element stride L/16
+        const int msh1 = log2M - lL, msh2 = log2M - (lL - 2);
+        for (int g = threadIdx.x; g < (n >> 4); g += blockDim.x) {
+            const int b = g & (S - 1);
+            const int base = (g >> lS) * L + b;
+            Cplx<T> x[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) x[i] = a[base + i * S];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) r4_dif_reg(x[i], x[i + 4], x[i + 8], x[i + 12], tws[(b + i * S) << msh1]);
+            const Cplx<T> w = tws[b << msh2];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) r4_dif_reg(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3], w);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) a[base + i * S] = x[i];
+        }
+        __syncthreads();
+    }
+    const SmemTw<T> tw{tws};
+    if (L >= 4) {   // one remaining radix-4 stage (L = 4 or 8)
+        for (int t = threadIdx.x; t < n / 4; t += blockDim.x) dif4(a, L, lL - 2, t, tw, log2M - lL);
+        __syncthreads();
+        L >>= 2;
+        lL -= 2;
+    }
+    if (L == 2) {
+        for (int t = threadIdx.x; t < n / 2; t += blockDim.x) dif2(a, 2, 0, t, tw, log2M - 1);
+        __syncthreads();
+    }
+}
+
+template <class T>
+__device__ __noinline__ void block_dit_f(Cplx<T>* a, int n, const Cplx<T>* tws, int log2M) {
+    const SmemTw<T> tw{tws};
+    const int m = fft_log2(n);
+    int L, lL;
+    if (m & 1) {
+        for (int t = threadIdx.x; t < n / 2; t += blockDim.x) dit2(a, 2, 0, t, tw, log2M - 1);
+        __syncthreads();
+        L = 8; lL = 3;
+    } else {
+        L = 4; lL = 2;
+    }
+    if ((m >> 1) & 1) {   // an odd number of radix-4 stages: the smallest runs alone
+        for (int t = threadIdx.x; t < n / 4; t += blockDim.x) dit4(a, L, lL - 2, t, tw, log2M - lL);
+        __syncthreads();
+        L <<= 2;
+        lL += 2;
+    }
+    for (; L <= n / 4; L <<= 4, lL += 4) {
+        const int lS = lL - 2, S = 1 << lS;           // element stride L/4
+        const int msh1 = log2M - lL, msh2 = log2M - (lL + 2);
+        for (int g = threadIdx.x; g < (n >> 4); g += blockDim.x) {
+            const int b = g & (S - 1);
+            const int base = (g >> lS) * (4 * L) + b;
+            Cplx<T> x[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) x[i] = a[base + i * S];
+            const Cplx<T> w = tws[b << msh1];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) r4_dit_reg(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3], w);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) r4_dit_reg(x[k], x[k + 4], x[k + 8], x[k + 12], tws[(b + k * S) << msh2]);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) a[base + i * S] = x[i];
+        }
+        __syncthreads();
+    }
+}
 #endif
