@@ -342,7 +342,6 @@ static int build_tables(rp_scene* s) {
             h[n] = Cplx<double>{v / M, 0.0};
         }
         host_dif(h.data(), M, f, lM);
-        if ((rc = to32(tw, &s->d_twS, &acc))) return rc;
         if ((rc = to32(c2, &s->d_C2S, &acc))) return rc;
         if ((rc = to32(h, &s->d_HS, &acc))) return rc;
         s->mS = M;
@@ -468,7 +467,7 @@ extern "C" int rp_scene_destroy(rp_scene* s) {
     cudaSetDevice(s->device);
     if (s->own_stream) cudaStreamSynchronize(s->own_stream);
     void* ptrs[] = {s->d_facets, s->d_targets, s->d_prisms, s->d_order, s->d_sorted,
-                    s->d_C1_64, s->d_C2_64, s->d_C1_32, s->d_C2_32, s->d_twS, s->d_C2S,
+                    s->d_C1_64, s->d_C2_64, s->d_C1_32, s->d_C2_32, s->d_C2S,
                     s->d_HS, s->d_CR_64, s->d_CR_32};
     for (void* q : ptrs)
         if (q) cudaFree(q);

@@ -378,8 +378,6 @@ struct ConvArgs {
     const int* bt0;
     const C32* T;
     int Wt;
-    const Cplx<float>* tw;
-    int log2M;
     const Cplx<float>* C2s;
     const Cplx<float>* Hs;  // DIF_M(crop kernel) / M
     int nr, n2, N, M, crop_K, crop_all;
@@ -389,30 +387,22 @@ struct ConvArgs {
     unsigned int* work;
 };
 
-struct TW32 {
-    const Cplx<float>* t;
-    __device__ __forceinline__ Cplx<float> operator()(int k) const {
-        const float2 v = __ldg(reinterpret_cast<const float2*>(t) + k);
-        return Cplx<float>{v.x, v.y};
-    }
-};
-
 // Persistent over the items of one or more batches (job j owns items
-// [start[j], start[j + 1])); shared memory: the twiddle quarter for the
-// job's M (reloaded when M changes), then X and W.
+// [start[j], start[j + 1])); shared memory: X (2nr) and W (M), every element
+// at its swizzled position (swz, rp_fft.cuh) so no access pattern of the
+// transforms conflicts in the banks; twiddles come from the SFU.
 template <int KPT>
 __global__ void __launch_bounds__(RP_CONV_THREADS, 1)
 k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ start, int njobs,
-          int maxM, unsigned int* work) {
+          unsigned int* work) {
     extern __shared__ __align__(16) unsigned char csm[];
-    Cplx<float>* TWs = reinterpret_cast<Cplx<float>*>(csm);   // first quarter of the twiddle circle
-    Cplx<float>* X = TWs + maxM / 4;
+    Cplx<float>* X = reinterpret_cast<Cplx<float>*>(csm);
     __shared__ unsigned int s_item;
     __shared__ int s_job;
     __shared__ ConvArgs A;                  // the current item's job (off the FFT hot path)
     const int tid = threadIdx.x;
     const unsigned int total = start[njobs];
-    int curM = 0, curJ = -1;
+    int curJ = -1;
     for (;;) {
         if (tid == 0) {
             const unsigned int it = atomicAdd(work, 1u);
@@ -434,18 +424,12 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
         const unsigned int item = item0 - start[jb];
         const int nr = A.nr, n2 = A.n2, N = A.N, M = A.M;
         Cplx<float>* W = X + n2;
-        if (M != curM) {
-            #pragma unroll 8
-            for (int k = tid; k < M / 4; k += RP_CONV_THREADS) TWs[k] = A.tw[k];
-            __syncthreads();
-            curM = M;
-        }
         // the job's arguments in registers (the loops below store to shared
         // memory, which would otherwise force re-reads of A)
         const Cplx<float>* __restrict__ C2s = A.C2s;
         const Cplx<float>* __restrict__ Hs = A.Hs;
         const C32* __restrict__ T = A.T;
-        const int Wt = A.Wt, nbA = A.nb, log2M = A.log2M, nsplit = A.nsplit;
+        const int Wt = A.Wt, nbA = A.nb, nsplit = A.nsplit;
         const int64_t tstride = A.tstride;
         const float sig_scale = A.sig_scale;
         const int* __restrict__ bt0 = A.bt0;
@@ -472,59 +456,59 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
                         v.y += u.y;
                     }
                 }
-                X[k] = v;
+                X[swz(k)] = v;
             }
             __syncthreads();
-            block_dif_f<float>(X, n2, TWs, log2M);
+            block_dif_s<float>(X, n2);
             #pragma unroll 8
-            for (int k = tid; k < n2; k += RP_CONV_THREADS) W[k] = c_mul(X[k], C2s[k]);
+            for (int k = tid; k < n2; k += RP_CONV_THREADS) W[swz(k)] = c_mul(X[swz(k)], C2s[k]);
             __syncthreads();
-            block_dit_f<float>(W, n2, TWs, log2M);
+            block_dit_s<float>(W, n2);
             {   // Ptarg = W[nr/2 + k] / n2 moved to the front, zero padded
                 const float inv = 1.f / (float)n2;
                 Cplx<float> keep[KPT];
 #pragma unroll
                 for (int c = 0; c < KPT; ++c) {
                     const int k = tid + c * RP_CONV_THREADS;
-                    if (k < nr) keep[c] = W[nr / 2 + k];
+                    if (k < nr) keep[c] = W[swz(nr / 2 + k)];
                 }
                 __syncthreads();
 #pragma unroll
                 for (int c = 0; c < KPT; ++c) {
                     const int k = tid + c * RP_CONV_THREADS;
-                    if (k < nr) W[k] = Cplx<float>{keep[c].x * inv, keep[c].y * inv};
+                    if (k < nr) W[swz(k)] = Cplx<float>{keep[c].x * inv, keep[c].y * inv};
                 }
                 #pragma unroll 8
-                for (int k = nr + tid; k < n2; k += RP_CONV_THREADS) W[k] = Cplx<float>{0.f, 0.f};
+                for (int k = nr + tid; k < n2; k += RP_CONV_THREADS) W[swz(k)] = Cplx<float>{0.f, 0.f};
                 __syncthreads();
             }
-            block_dif_f<float>(W, n2, TWs, log2M);
+            block_dif_s<float>(W, n2);
             {
                 const float sc = sig_scale / (float)n2;
                 #pragma unroll 8
                 for (int k = tid; k < n2; k += RP_CONV_THREADS) {
-                    Cplx<float> v = c_mul(X[k], W[k]);
-                    W[k] = Cplx<float>{v.x * sc, v.y * sc};
+                    Cplx<float> v = c_mul(X[swz(k)], W[swz(k)]);
+                    W[swz(k)] = Cplx<float>{v.x * sc, v.y * sc};
                 }
             }
             __syncthreads();
-            block_dit_f<float>(W, n2, TWs, log2M);                 // u (natural, N values)
+            block_dit_s<float>(W, n2);                                // u (natural, N values)
             #pragma unroll 8
-            for (int k = N + tid; k < M; k += RP_CONV_THREADS) W[k] = Cplx<float>{0.f, 0.f};
+            for (int k = N + tid; k < M; k += RP_CONV_THREADS) W[swz(k)] = Cplx<float>{0.f, 0.f};
             __syncthreads();
             // cropSpectrum + inverse DFT on the N grid = circular convolution
             // with the crop kernel h: linear convolution at M >= 2N - 1, then
             // circ[n] = lin[n] + lin[n + N]
-            block_dif_f<float>(W, M, TWs, log2M);
+            block_dif_s<float>(W, M);
             #pragma unroll 8
-            for (int k = tid; k < M; k += RP_CONV_THREADS) W[k] = c_mul(W[k], Hs[k]);
+            for (int k = tid; k < M; k += RP_CONV_THREADS) W[swz(k)] = c_mul(W[swz(k)], Hs[k]);
             __syncthreads();
-            block_dit_f<float>(W, M, TWs, log2M);
+            block_dit_s<float>(W, M);
 #pragma unroll
             for (int i = 0; i < KPT; ++i) {
                 const int j = tid + i * RP_CONV_THREADS;
                 if (j < nr) {     // takeEveryOtherComplex: circ[2j]
-                    const Cplx<float> a = W[2 * j], b = W[2 * j + N];
+                    const Cplx<float> a = W[swz(2 * j)], b = W[swz(2 * j + N)];
                     accr[i] += a.x + b.x;
                     acci[i] += a.y + b.y;
                 }
@@ -750,24 +734,24 @@ void sinc_poly(double T, int D, double* mono) {
 }
 
 template <int KPT>
-int launch_conv_k(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, int maxM, size_t csm, int sms,
+int launch_conv_k(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, size_t csm, int sms,
                   unsigned int items, unsigned int* work, cudaStream_t st) {
     RP_CUDA(cudaFuncSetAttribute(k_conv32s<KPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
     int occ = 0;
     RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv32s<KPT>, RP_CONV_THREADS, csm));
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(occ, 1) * sms, items));
-    k_conv32s<KPT><<<grid, RP_CONV_THREADS, csm, st>>>(d_jobs, d_start, njobs, maxM, work);
+    k_conv32s<KPT><<<grid, RP_CONV_THREADS, csm, st>>>(d_jobs, d_start, njobs, work);
     RP_LAUNCHED();
     return RP_OK;
 }
 
-int launch_conv32s(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, int max_nr, int maxM,
+int launch_conv32s(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, int max_nr,
                    size_t csm, int sms, unsigned int items, unsigned int* work, cudaStream_t st) {
     const int kpt = (max_nr + RP_CONV_THREADS - 1) / RP_CONV_THREADS;
-    if (kpt <= 1) return launch_conv_k<1>(d_jobs, d_start, njobs, maxM, csm, sms, items, work, st);
-    if (kpt <= 2) return launch_conv_k<2>(d_jobs, d_start, njobs, maxM, csm, sms, items, work, st);
-    if (kpt <= 4) return launch_conv_k<4>(d_jobs, d_start, njobs, maxM, csm, sms, items, work, st);
-    return launch_conv_k<8>(d_jobs, d_start, njobs, maxM, csm, sms, items, work, st);
+    if (kpt <= 1) return launch_conv_k<1>(d_jobs, d_start, njobs, csm, sms, items, work, st);
+    if (kpt <= 2) return launch_conv_k<2>(d_jobs, d_start, njobs, csm, sms, items, work, st);
+    if (kpt <= 4) return launch_conv_k<4>(d_jobs, d_start, njobs, csm, sms, items, work, st);
+    return launch_conv_k<8>(d_jobs, d_start, njobs, csm, sms, items, work, st);
 }
 
 // ---------------------------------------------------------- autotuner ----
@@ -943,7 +927,6 @@ ConvArgs seg_conv_args(const Seg& g) {
     const int nr = sc->nr;
     ConvArgs C;
     C.ntl = g.ntl; C.tstride = g.L.tstride; C.nb = g.nb; C.bt0 = g.bt0; C.T = g.T; C.Wt = g.Wt;
-    C.tw = (const Cplx<float>*)sc->d_twS; C.log2M = sc->log2mS;
     C.C2s = (const Cplx<float>*)sc->d_C2S; C.Hs = (const Cplx<float>*)sc->d_HS;
     C.nr = nr; C.n2 = 2 * nr; C.N = 2 * nr - 1; C.M = sc->mS;
     C.crop_K = sc->crop_K; C.crop_all = sc->crop_all;
@@ -1088,16 +1071,14 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     }
     std::vector<ConvArgs> hc;
     std::vector<unsigned int> hcs(1, 0u);
-    int max_nr = 1, maxM = 4;
+    int max_nr = 1;
     size_t csm = 0;
     for (Seg* g : cs) {
         hc.push_back(seg_conv_args(*g));
         hcs.push_back(hcs.back() + (unsigned)(g->nb * g->nsplit));
         max_nr = std::max(max_nr, g->sc->nr);
-        maxM = std::max(maxM, g->sc->mS);
         csm = std::max(csm, (size_t)(2 * g->sc->nr + g->sc->mS) * sizeof(Cplx<float>));
     }
-    csm += (size_t)(maxM / 4) * sizeof(Cplx<float>);
     if (!hp.empty()) {
         RP_CUDA(cudaMemcpyAsync(d_pjobs, hp.data(), sizeof(PairJob) * hp.size(), cudaMemcpyHostToDevice, st));
         RP_CUDA(cudaMemcpyAsync(d_pstart, hps.data(), sizeof(unsigned int) * hps.size(), cudaMemcpyHostToDevice, st));
@@ -1122,8 +1103,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     // ---- range compression: one launch for the shared-memory segments, the
     // global-scratch kernel per remaining segment
     if (!cs.empty()) {
-        int rc = launch_conv32s(d_cjobs, d_cstart, (int)cs.size(), max_nr, maxM, csm, sms, hcs.back(),
-                                d_work + 1, st);
+        int rc = launch_conv32s(d_cjobs, d_cstart, (int)cs.size(), max_nr, csm, sms, hcs.back(), d_work + 1, st);
         if (rc) return rc;
     }
     for (Seg* g : ps) {

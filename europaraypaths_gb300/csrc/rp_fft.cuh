@@ -386,3 +386,117 @@ __device__ __noinline__ void block_dit_f(Cplx<T>* a, int n, const Cplx<T>* tws, 
     }
 }
 #endif
+
+#ifdef __CUDACC__
+// Bank-conflict-free variants for the compression kernel.  Element e of a
+// shared array lives at swz(e) = e ^ ((e >> 5) & 31): a permutation inside
+// each row of 32 complex values, so every access pattern of the stages below
+// (consecutive elements, or one element per row at any power-of-two stride)
+// reaches 32 distinct bank pairs.  Twiddles e^{-2 pi i j / L} come from the
+// special-function unit (__sincosf, |angle| <= pi / 2, absolute error below
+// 1e-6) instead of a table.
+__device__ __forceinline__ int swz(int e) { return e ^ ((e >> 5) & 31); }
+
+template <class T>
+__device__ __forceinline__ Cplx<T> tw_sfu(int j, float step) {   // e^{-i j step}
+    float sn, cs;
+    __sincosf((float)j * step, &sn, &cs);
+    return Cplx<T>{(T)cs, (T)-sn};
+}
+
+template <class T>
+__device__ __noinline__ void block_dif_s(Cplx<T>* a, int n) {
+    const int m = fft_log2(n);
+    int L = n, lL = m;
+    for (; L >= 16; L >>= 4, lL -= 4) {
+        const int lS = lL - 4, S = 1 << lS;
+        const float st1 = 6.28318530717958647f / (float)L, st2 = 4.f * st1;
+        for (int g = threadIdx.x; g < (n >> 4); g += blockDim.x) {
+            const int b = g & (S - 1);
+            const int base = (g >> lS) * L + b;
+            Cplx<T> x[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) x[i] = a[swz(base + i * S)];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) r4_dif_reg(x[i], x[i + 4], x[i + 8], x[i + 12], tw_sfu<T>(b + i * S, st1));
+            const Cplx<T> w = tw_sfu<T>(b, st2);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) r4_dif_reg(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3], w);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) a[swz(base + i * S)] = x[i];
+        }
+        __syncthreads();
+    }
+    if (L >= 4) {   // one remaining radix-4 stage (L = 4 or 8)
+        const int q4 = L >> 2, lq = lL - 2;
+        const float st = 6.28318530717958647f / (float)L;
+        for (int t = threadIdx.x; t < n / 4; t += blockDim.x) {
+            const int j = t & (q4 - 1);
+            const int b = (t >> lq) * L + j;
+            Cplx<T> x0 = a[swz(b)], x1 = a[swz(b + q4)], x2 = a[swz(b + 2 * q4)], x3 = a[swz(b + 3 * q4)];
+            r4_dif_reg(x0, x1, x2, x3, tw_sfu<T>(j, st));
+            a[swz(b)] = x0; a[swz(b + q4)] = x1; a[swz(b + 2 * q4)] = x2; a[swz(b + 3 * q4)] = x3;
+        }
+        __syncthreads();
+        L >>= 2;
+    }
+    if (L == 2) {
+        for (int t = threadIdx.x; t < n / 2; t += blockDim.x) {
+            const Cplx<T> x0 = a[swz(2 * t)], x1 = a[swz(2 * t + 1)];
+            a[swz(2 * t)] = c_add(x0, x1);
+            a[swz(2 * t + 1)] = c_sub(x0, x1);
+        }
+        __syncthreads();
+    }
+}
+
+template <class T>
+__device__ __noinline__ void block_dit_s(Cplx<T>* a, int n) {
+    const int m = fft_log2(n);
+    int L, lL;
+    if (m & 1) {
+        for (int t = threadIdx.x; t < n / 2; t += blockDim.x) {
+            const Cplx<T> x0 = a[swz(2 * t)], x1 = a[swz(2 * t + 1)];
+            a[swz(2 * t)] = c_add(x0, x1);
+            a[swz(2 * t + 1)] = c_sub(x0, x1);
+        }
+        __syncthreads();
+        L = 8; lL = 3;
+    } else {
+        L = 4; lL = 2;
+    }
+    if ((m >> 1) & 1) {   // an odd number of radix-4 stages: the smallest runs alone
+        const int q4 = L >> 2, lq = lL - 2;
+        const float st = 6.28318530717958647f / (float)L;
+        for (int t = threadIdx.x; t < n / 4; t += blockDim.x) {
+            const int j = t & (q4 - 1);
+            const int b = (t >> lq) * L + j;
+            Cplx<T> x0 = a[swz(b)], x1 = a[swz(b + q4)], x2 = a[swz(b + 2 * q4)], x3 = a[swz(b + 3 * q4)];
+            r4_dit_reg(x0, x1, x2, x3, tw_sfu<T>(j, st));
+            a[swz(b)] = x0; a[swz(b + q4)] = x1; a[swz(b + 2 * q4)] = x2; a[swz(b + 3 * q4)] = x3;
+        }
+        __syncthreads();
+        L <<= 2;
+        lL += 2;
+    }
+    for (; L <= n / 4; L <<= 4, lL += 4) {
+        const int lS = lL - 2, S = 1 << lS;
+        const float st1 = 6.28318530717958647f / (float)L, st2 = 0.25f * st1;
+        for (int g = threadIdx.x; g < (n >> 4); g += blockDim.x) {
+            const int b = g & (S - 1);
+            const int base = (g >> lS) * (4 * L) + b;
+            Cplx<T> x[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) x[i] = a[swz(base + i * S)];
+            const Cplx<T> w = tw_sfu<T>(b, st1);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) r4_dit_reg(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3], w);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) r4_dit_reg(x[k], x[k + 4], x[k + 8], x[k + 12], tw_sfu<T>(b + k * S, st2));
+#pragma unroll
+            for (int i = 0; i < 16; ++i) a[swz(base + i * S)] = x[i];
+        }
+        __syncthreads();
+    }
+}
+#endif

@@ -119,7 +119,6 @@ struct rp_scene {
     // the digit-reversed order of the in-place DIF stages (rp_fft.cuh)
     int smem_conv = 0;                   // tables present
     int mS = 0, log2mS = 0;              // M = 4 nr
-    float* d_twS = nullptr;              // e^{-2 pi i k / M}, k < M
     float* d_C2S = nullptr;              // DIF_2nr(target chirp)
     float* d_HS = nullptr;               // DIF_M(crop kernel h) / M
     // ---- tuning
