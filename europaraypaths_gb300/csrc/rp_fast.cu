@@ -94,44 +94,65 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
     const double cx = 0.5 * (mnx + mxx), cy = 0.5 * (mny + mxy), cz = 0.5 * (mnz + mxz);
     float xI = 0.f, rr = 0.f;
     if (ok) {
-        double dx = fx - t.sx, dy = fy - t.sy, dz = fz - t.sz;
-        double d = sqrt(dx * dx + dy * dy + dz * dz);
-        double Ix = dx / d, Iy = dy / d, Iz = dz / d;
-        double nx = F[3 * nf + i], ny = F[4 * nf + i], nz = F[5 * nf + i];
-        double ux = F[6 * nf + i], uy = F[7 * nf + i], uz = F[8 * nf + i];
-        double vx = F[9 * nf + i], vy = F[10 * nf + i], vz = F[11 * nf + i];
-        double th = acos(clamp1(-Ix * nx - Iy * ny - Iz * nz));
-        double ph = atan2(Ix * ux + Iy * uy + Iz * uz, Ix * vx + Iy * vy + Iz * vz);
-        double sR = sqrt(dp.eps1 / dp.eps2) * sin(th);
-        double rth = sR > 1.0 ? 1e4 : asin(sR);
-        double cI = cos(th), cR = cos(rth);
-        double rho = (dp.nu2 * cI - dp.nu1 * cR) / (dp.nu2 * cI + dp.nu1 * cR);
-        double frc = 1.0 - rho * rho;
-        double fre = rho * rho;
-        if (rth > 1e3) frc = 0.0;
-        double atm = exp(-4.0 * dp.alpha1 * d);
-        fre *= atm;
-        frc *= atm;
-        fre *= exp(-4 * ((dp.ks * cI) * (dp.ks * cI)));
-        double G = d_facet_G(th, ph, dp.lam, dp.fs);
-        // surface leg (surfacePT, radar_kernels.cu:714-764)
-        double Pf = d_friis(dp.P, t.grefr, G, dp.lam, d);
-        double Ps = d_friis(Pf, G, t.grefr, dp.lam, d);
+        // FP64: the range and everything that becomes a phase or a bin
+        // offset; FP32: the angles and amplitudes (relative error ~1e-6).
+        // Angles enter only through their cosines and sines, formed from dot
+        // and cross products: cos th = -I.n, sin th = |I x n| (accurate near
+        // nadir), cos ph / sin ph = (I.v, I.u) / |(I.v, I.u)| (atan2(0, 0) =
+        // 0), Snell's cos = sqrt(1 - sR^2) (cos(1e4) on total internal
+        // reflection, as the reference's flag value gives).
+        const double dxd = fx - t.sx, dyd = fy - t.sy, dzd = fz - t.sz;
+        const double d = sqrt(dxd * dxd + dyd * dyd + dzd * dzd);
+        const float inv_d = (float)(1.0 / d);
+        const float Ix = (float)dxd * inv_d, Iy = (float)dyd * inv_d, Iz = (float)dzd * inv_d;
+        const double nx = F[3 * nf + i], ny = F[4 * nf + i], nz = F[5 * nf + i];
+        const double ux = F[6 * nf + i], uy = F[7 * nf + i], uz = F[8 * nf + i];
+        const double vx = F[9 * nf + i], vy = F[10 * nf + i], vz = F[11 * nf + i];
+        const float nxf = (float)nx, nyf = (float)ny, nzf = (float)nz;
+        const float cI = fminf(1.f, fmaxf(-1.f, -(Ix * nxf + Iy * nyf + Iz * nzf)));
+        const float crx = Iy * nzf - Iz * nyf, cry = Iz * nxf - Ix * nzf, crz = Ix * nyf - Iy * nxf;
+        const float sI = fminf(1.f, sqrtf(crx * crx + cry * cry + crz * crz));
+        const float pu = Ix * (float)ux + Iy * (float)uy + Iz * (float)uz;
+        const float pv = Ix * (float)vx + Iy * (float)vy + Iz * (float)vz;
+        const float hh = sqrtf(pu * pu + pv * pv);
+        const float cph = hh > 0.f ? pv / hh : 1.f, sph = hh > 0.f ? pu / hh : 0.f;
+        const float sR = (float)sqrt(dp.eps1 / dp.eps2) * sI;
+        const bool tir = sR > 1.f;
+        const float cR = tir ? cosf(1e4f) : sqrtf(fmaxf(0.f, 1.f - sR * sR));
+        const float nu1 = (float)dp.nu1, nu2 = (float)dp.nu2;
+        const float rho = (nu2 * cI - nu1 * cR) / (nu2 * cI + nu1 * cR);
+        const float df = (float)d;
+        const float atm = expf(-4.0f * (float)dp.alpha1 * df);
+        const float frc = tir ? 0.f : (1.f - rho * rho) * atm;
+        const float ksc = (float)dp.ks * cI;
+        const float fre = rho * rho * atm * expf(-4.f * ksc * ksc);
+        // facet_G (radar_kernels.cu:658-677), sinc(x) = sin(pi x)/(pi x)
+        const float lamf = (float)dp.lam, fsf = (float)dp.fs;
+        const float piLlam = (float)RP_PI_F * fsf / lamf;
+        const float a1 = (float)RP_PI * piLlam * sI * cph, a2 = (float)RP_PI * piLlam * sI * sph;
+        const float s1 = fabsf(a1) < 3.14159265e-6f ? 1.f : sinf(a1) / a1;
+        const float s2 = fabsf(a2) < 3.14159265e-6f ? 1.f : sinf(a2) / a2;
+        const float D = (s1 * s2) * (s1 * s2);
+        const float G = D * (4.f * (float)RP_PI_F * fsf * fsf) / (lamf * lamf);
+        // surface leg (surfacePT, radar_kernels.cu:714-764): two Friis hops
+        const float f4 = (4.f * (float)RP_PI_FRIIS) * (4.f * (float)RP_PI_FRIIS);
+        const float grefr = (float)t.grefr;
+        const float hop = lamf * lamf * G * grefr / (f4 * df * df);
+        float Ps = (float)dp.P * hop * hop;
         if (!dp.lossless) Ps *= fre;
-        double amp = sqrt(Ps);
+        const float amp = sqrtf(Ps);
         // phase in turns: phasor(2 Itd) = exp(-j (2 pi_F/lam) 2 Itd) = exp(-j 2 pi tt)
-        double tt = 2.0 * d * dp.turn;
-        double ft = tt - floor(tt);
-        double sn, cs;
-        sincospi(-2.0 * ft, &sn, &cs);
+        const double tt = 2.0 * d * dp.turn;
+        const float ft = (float)(tt - floor(tt));
+        float sn, cs;
+        sincospif(-2.f * ft, &sn, &cs);
         sx_o[(size_t)s * nf + j] = (float)((d - t.rst) / dp.dr);
-        sv_o[(size_t)s * nf + j] = C32{(float)(amp * cs), (float)(amp * sn)};
-        atomic_max_pos(vmax + s, amp);
+        sv_o[(size_t)s * nf + j] = C32{amp * cs, amp * sn};
+        atomic_max_pos(vmax + s, (double)amp);
         // hoisted target-leg amplitude: sqrt(P Gr G frc n) lam^2 Dmax / ((4 pi)^2 Itd)
-        const double f4 = (4 * RP_PI_FRIIS) * (4 * RP_PI_FRIIS);
-        const double Dmax = (4 * RP_PI_F * dp.fs * dp.fs) / (dp.lam * dp.lam);
-        double Kf = sqrt(dp.P * t.grefr * G * (dp.lossless ? 1.0 : frc) * dp.nidx) * dp.lam *
-                    dp.lam * Dmax / (f4 * d);
+        const float Dmax = (4.f * (float)RP_PI_F * fsf * fsf) / (lamf * lamf);
+        const float Kf = sqrtf((float)dp.P * grefr * G * (dp.lossless ? 1.f : frc) * (float)dp.nidx) * lamf *
+                         lamf * Dmax / (f4 * df);
         xI = (float)((d - t.rst) / dp.dr);
         double ti = d * dp.turn;
         float tauI = (float)(ti - floor(ti));

@@ -41,7 +41,6 @@ __device__ __forceinline__ double d_friis(double P, double Gt, double Gr, double
     return (P * lam * lam * Gt * Gr) / ((4 * RP_PI_FRIIS) * (4 * RP_PI_FRIIS) * d * d);
 }
 
-// geometry_kernels.cu:384-393
 // facetReradiation, geometry_kernels.cu:353-381 (sinc arguments without pi).
 __device__ __forceinline__ double d_facet_rerad(double th, double ph, double lam, double fs) {
     double st = sin(th);
@@ -57,6 +56,7 @@ __device__ __forceinline__ double d_snells(double th, double e1, double e2) {
     return sR > 1.0 ? 1e4 : asin(sR);
 }
 
+// geometry_kernels.cu:384-393
 __device__ __forceinline__ double d_radar_eq(double P, double G, double fs, double lam, double d, double nf) {
     double num = P * G * G * fs * fs * fs * fs;
     double den = (4 * RP_PI_FRIIS) * (4 * RP_PI_FRIIS) * d * d * d * d;
