@@ -463,7 +463,7 @@ def main():
             pv = opcount.pairs(pc) / (e0.elapsed_time(e1) / 1e3)
             line["plain_form"] = {"value": pv, "unit": UNIT, "traces": args.plain_traces,
                                   "fast_over_plain": value / pv if pv else None}
-        roof["pair_cfg"] = {f"degree_{d}": simulator.autotune_query(False, d) for d in (0, 4, 5, 6)
+        roof["pair_cfg"] = {f"degree_{d}": simulator.autotune_query(False, d) for d in (0, 3, 4, 5, 6)
                             if simulator.autotune_query(False, d) >= 0}
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(sc, scene, track, args.cpu_targets, 1000)

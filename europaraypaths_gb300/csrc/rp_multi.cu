@@ -42,6 +42,7 @@ k_pairs32m(const PairJob* __restrict__ jobs, const unsigned int* __restrict__ st
         const int tb = (li / RP_PARTS) % A.tblocks;
         const int s = li / (RP_PARTS * A.tblocks);
         switch (deg) {
+            case 3: pair_item<3, ILP>(A, s, tb, part, bars, phase); break;
             case 4: pair_item<4, ILP>(A, s, tb, part, bars, phase); break;
             case 5: pair_item<5, ILP>(A, s, tb, part, bars, phase); break;
             case 6: pair_item<6, ILP>(A, s, tb, part, bars, phase); break;

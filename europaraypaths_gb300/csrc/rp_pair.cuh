@@ -171,7 +171,10 @@ __device__ __forceinline__ float sinc_poly_eval(const float* c, float t) {
 // = 0 gives xv^2/h2 = 1, yu^2/h2 = 0).  NT > 0 evaluates sin(a)/a as a
 // polynomial in a^2 (no special-function unit); NT == 0 uses sin(a)/a with
 // one shared reciprocal, 1 for |a| < pi 1e-6 (elementary_kernels.cu:50-53).
-template <int NT>
+// RED: reduce the phase to [-1/2, 1/2] turns before the special-function
+// sine and cosine; the fast path skips it when the chunk keeps |tau| below
+// 42 turns (sin/cos.approx hold their accuracy over +-100 pi radians).
+template <int NT, bool RED = true>
 __device__ __forceinline__ void pair_eval(const FacetRec& r, const Anchor& an, const PairArgs& A,
                                           float& xr, float& vre, float& vim) {
     const float dd = fmaf(an.Dx, r.a.x, fmaf(an.Dy, r.a.y, an.Dz * r.a.z));
@@ -239,7 +242,7 @@ __device__ __forceinline__ void pair_eval(const FacetRec& r, const Anchor& an, c
     const float e2 = fmaf(A.eks, cT2, fmaf(A.ealpha, dT, an.eaT0));
     const float amp = r.d.w * fabsf(S) * rinv * ex2_a(e2);
     float tau = (r.c.w + an.tau0) + A.kt * dT;
-    tau -= rintf(tau);
+    if (RED) tau -= rintf(tau);
     float sn, cs;
     __sincosf(-6.28318530717958647f * tau, &sn, &cs);
     vre = amp * cs;
@@ -453,7 +456,8 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
             // every pair's bin x lies in [lo, hi] (triangle inequality on the
             // chunk's bounding radius); with half a bin of margin for FP32
             // rounding, both split bins stay inside the window and the trace
-            fits = blo >= 0 && blo + RP_WIN <= A.nr1 && hi + 0.5 < (double)(blo + RP_WIN - 1);
+            fits = blo >= 0 && blo + RP_WIN <= A.nr1 && hi + 0.5 < (double)(blo + RP_WIN - 1) &&
+                   (double)A.kt * (double)mp->R < 40.0;     // |kt dT| <= kt R: the phase bound
             an.Dx = (float)Dx; an.Dy = (float)Dy; an.Dz = (float)Dz;
             an.T0 = (float)T0; an.T0sq = (float)(T0 * T0);
             an.tau0 = (float)(tt - floor(tt));
@@ -473,15 +477,15 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
                     const FacetRec r0 = R[jj];
                     const FacetRec r1 = R[jj + 1];
                     float x0, re0, im0, x1, re1, im1;
-                    pair_eval<NT>(r0, an, A, x0, re0, im0);
-                    pair_eval<NT>(r1, an, A, x1, re1, im1);
+                    pair_eval<NT, false>(r0, an, A, x0, re0, im0);
+                    pair_eval<NT, false>(r1, an, A, x1, re1, im1);
                     bin_add_fast(x0, re0, im0, win, tid);
                     bin_add_fast(x1, re1, im1, win, tid);
                 }
                 for (; jj < cnt; ++jj) {
                     const FacetRec r0 = R[jj];
                     float x0, re0, im0;
-                    pair_eval<NT>(r0, an, A, x0, re0, im0);
+                    pair_eval<NT, false>(r0, an, A, x0, re0, im0);
                     bin_add_fast(x0, re0, im0, win, tid);
                 }
             } else {

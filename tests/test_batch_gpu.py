@@ -91,5 +91,5 @@ def test_autotuner_records_choice(built_lib):
     s = tiny_scene(nside=30, ntside=3, ns=2)
     with simulator.Scene(s["params"], s["facets"], s["targets"]) as sc:
         sc.simulate(tr_mod.linear_track(sc.params))
-    tuned = [simulator.autotune_query(False, d) for d in (0, 4, 5, 6)]
+    tuned = [simulator.autotune_query(False, d) for d in (0, 3, 4, 5, 6)]
     assert any(0 <= c <= 3 for c in tuned)

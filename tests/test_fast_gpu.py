@@ -75,10 +75,11 @@ def test_fast_deterministic(built_lib):
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
-@pytest.mark.parametrize("nside", [400, 148])
+@pytest.mark.parametrize("nside", [400, 285, 200, 148, 30])
 def test_fast_polynomial_sinc_regimes(built_lib, oracle, nside):
-    # fs = 5 m (sinc argument up to 1.5 rad: 7 Maclaurin terms) and
-    # fs = 13.5 m (up to 4 rad: 13 terms) at 9 MHz
+    # at 9 MHz the largest sinc argument pik = pi^2 fs / lam picks the sinc
+    # evaluation: fs 5 m (1.48 rad, degree 3), 7 m (2.08, degree 4), 10 m
+    # (2.96, degree 5), 13.5 m (4.0, degree 6), 67 m (special-function path)
     from europaraypaths_gb300 import traces as tr_mod, param_gen
     sc = tiny_scene(nside=nside, ntside=3, ns=2)
     p = param_gen.to_rp_params(sc["params"])
