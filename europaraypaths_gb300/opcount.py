@@ -10,25 +10,34 @@ The fused FP32 kernel (csrc/rp_fast.cu, k_pairs32) evaluates one
 the inbound one times -1/sqrt(P) in the non-specular mode; so one k_pairs32
 evaluation covers two metric pairs.
 
-Counts per k_pairs32 evaluation with the polynomial sinc (degree 4, the
-large-scene case), read off the source (pair_eval, bin_add fast path):
+Counts per k_pairs32 evaluation on the large scene (sinc polynomial of
+degree 3, the fast window path), measured from the kernel's executed
+instruction mix (ncu sass__inst_executed_per_opcode over one launch, divided
+by the evaluations of that launch); a higher sinc degree adds 4 FFMA per
+degree:
 
-* FP32 FMA-pipe instructions (FADD/FMUL/FFMA): 82 -- 3+1+1 distance, 1 Ttd,
-  2 dT, 6 direction, 3+3 cosines, 6 tangent projections, 3 h^2, 2 (1 - c^2),
-  3 squared sinc arguments scale, 4 arguments, 16 polynomials (4 x 4), 3 sinc
-  product, 3 exponent, 3 amplitude, 3 phase turns, 1 phase scale, 2 phasor,
-  2 bin coordinate, 11 bin split and window update.
-* MUFU (special-function) instructions: 6 -- rsqrt (1/Ttd), rcp (dT), rcp
-  (1/h^2), ex2, sin and cos of the phase.
+* FP32-pipe instructions: 72 -- 34 FFMA, 26 FMUL, 10 FADD, 2 compare and
+  select.  The terms: distance and Ttd - T0 from the anchor, the four
+  direction dot products, 1 - cos^2 of both angles, the in-plane sinc split,
+  four degree-3 polynomials and their product, the attenuation exponent,
+  amplitude, phase and its scaling, phasor, bin coordinate, and the two-bin
+  window update.
+* MUFU (special-function) instructions: 7 -- rsqrt (1/Ttd), rcp (dT), rcp
+  (1/Ttd^2), rcp (1/h^2), ex2, sin and cos of the phase.
+* All instructions (the issue rate that bounds the kernel): 97.5 -- the
+  above plus 6 shared-memory accesses (record and window), the floor
+  conversion pair, address arithmetic and the loop.
 """
 
-FP32_OPS_PER_EVAL = 82
-MUFU_PER_EVAL = 6
+FP32_OPS_PER_EVAL = 72
+MUFU_PER_EVAL = 7
+INSTR_PER_EVAL = 97.5
 EVALS_PER_TARGET_PAIR_METRIC = 0.5     # one evaluation covers two metric pairs
 
 # Nominal special-function throughput of a Blackwell SM (results per clock).
 MUFU_PER_CLK_PER_SM = 16
 FP32_FMA_PER_CLK_PER_SM = 128
+ISSUE_PER_CLK_PER_SM = 128      # 4 schedulers x one 32-thread instruction per clock
 
 
 def pairs(counts):
