@@ -409,15 +409,22 @@ struct ConvArgs {
 };
 
 // Persistent over the items of one or more batches (job j owns items
-// [start[j], start[j + 1])); shared memory: X (2nr) and W (M), every element
-// at its swizzled position (swz, rp_fft.cuh) so no access pattern of the
-// transforms conflicts in the banks; twiddles come from the SFU.
-template <int KPT>
+// [start[j], start[j + 1])).  X (2nr) and W (M = 4nr) hold every element at
+// its swizzled position (swz, rp_fft.cuh: conflict-free in shared memory,
+// within one 256-byte row in global memory); twiddles come from the SFU.
+// MODE 0: X and W in shared memory (nr <= 4096), the targets summed in
+// registers.  MODE 1: X in shared memory, W in this block's slot of the
+// global scratch (nr = 8192, where W no longer fits).  MODE 2: both in the
+// slot (nr >= 16384).  Modes 1 and 2 sum the targets in the item's partial
+// trace in global memory (same thread, same element, same target order as
+// the registers of mode 0, so every mode gives the same sums).
+template <int KPT, int MODE>
 __global__ void __launch_bounds__(RP_CONV_THREADS, 1)
 k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ start, int njobs,
-          unsigned int* work) {
+          unsigned int* work, Cplx<float>* __restrict__ gscr, size_t gslot) {
     extern __shared__ __align__(16) unsigned char csm[];
-    Cplx<float>* X = reinterpret_cast<Cplx<float>*>(csm);
+    Cplx<float>* const sbase = reinterpret_cast<Cplx<float>*>(csm);
+    Cplx<float>* const gbase = gscr + (size_t)blockIdx.x * gslot;
     __shared__ unsigned int s_item;
     __shared__ int s_job;
     __shared__ ConvArgs A;                  // the current item's job (off the FFT hot path)
@@ -444,7 +451,8 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
         curJ = jb;
         const unsigned int item = item0 - start[jb];
         const int nr = A.nr, n2 = A.n2, N = A.N, M = A.M;
-        Cplx<float>* W = X + n2;
+        Cplx<float>* const X = (MODE == 2) ? gbase : sbase;
+        Cplx<float>* const W = (MODE == 0) ? sbase + n2 : (MODE == 1 ? gbase : gbase + n2);
         // the job's arguments in registers (the loops below store to shared
         // memory, which would otherwise force re-reads of A)
         const Cplx<float>* __restrict__ C2s = A.C2s;
@@ -461,9 +469,12 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
         const int q0 = sp * RP_CONV_SPLIT;
         if (q0 >= nq) continue;
         const int q1 = min(q0 + RP_CONV_SPLIT, nq);
+        C32* const out = part + ((size_t)s * nsplit + sp) * nr;
         float accr[KPT], acci[KPT];
 #pragma unroll
         for (int i = 0; i < KPT; ++i) { accr[i] = 0.f; acci[i] = 0.f; }
+        if (MODE != 0)
+            for (int j = tid; j < nr; j += RP_CONV_THREADS) out[j] = C32{0.f, 0.f};
         for (int q = q0; q < q1; ++q) {
             const int b0 = bt0[(size_t)s * tstride + q];
             #pragma unroll 8
@@ -487,17 +498,26 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
             block_dit_s<float>(W, n2);
             {   // Ptarg = W[nr/2 + k] / n2 moved to the front, zero padded
                 const float inv = 1.f / (float)n2;
-                Cplx<float> keep[KPT];
+                if (MODE == 0) {    // through registers
+                    Cplx<float> keep[KPT];
 #pragma unroll
-                for (int c = 0; c < KPT; ++c) {
-                    const int k = tid + c * RP_CONV_THREADS;
-                    if (k < nr) keep[c] = W[swz(nr / 2 + k)];
-                }
-                __syncthreads();
+                    for (int c = 0; c < KPT; ++c) {
+                        const int k = tid + c * RP_CONV_THREADS;
+                        if (k < nr) keep[c] = W[swz(nr / 2 + k)];
+                    }
+                    __syncthreads();
 #pragma unroll
-                for (int c = 0; c < KPT; ++c) {
-                    const int k = tid + c * RP_CONV_THREADS;
-                    if (k < nr) W[swz(k)] = Cplx<float>{keep[c].x * inv, keep[c].y * inv};
+                    for (int c = 0; c < KPT; ++c) {
+                        const int k = tid + c * RP_CONV_THREADS;
+                        if (k < nr) W[swz(k)] = Cplx<float>{keep[c].x * inv, keep[c].y * inv};
+                    }
+                } else {            // through W's unused upper part [n2, n2 + nr)
+                    for (int k = tid; k < nr; k += RP_CONV_THREADS) W[swz(n2 + k)] = W[swz(nr / 2 + k)];
+                    __syncthreads();
+                    for (int k = tid; k < nr; k += RP_CONV_THREADS) {
+                        const Cplx<float> v = W[swz(n2 + k)];
+                        W[swz(k)] = Cplx<float>{v.x * inv, v.y * inv};
+                    }
                 }
                 #pragma unroll 8
                 for (int k = nr + tid; k < n2; k += RP_CONV_THREADS) W[swz(k)] = Cplx<float>{0.f, 0.f};
@@ -525,22 +545,33 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
             for (int k = tid; k < M; k += RP_CONV_THREADS) W[swz(k)] = c_mul(W[swz(k)], Hs[k]);
             __syncthreads();
             block_dit_s<float>(W, M);
+            if (MODE == 0) {
 #pragma unroll
-            for (int i = 0; i < KPT; ++i) {
-                const int j = tid + i * RP_CONV_THREADS;
-                if (j < nr) {     // takeEveryOtherComplex: circ[2j]
+                for (int i = 0; i < KPT; ++i) {
+                    const int j = tid + i * RP_CONV_THREADS;
+                    if (j < nr) {     // takeEveryOtherComplex: circ[2j]
+                        const Cplx<float> a = W[swz(2 * j)], b = W[swz(2 * j + N)];
+                        accr[i] += a.x + b.x;
+                        acci[i] += a.y + b.y;
+                    }
+                }
+            } else {
+                for (int j = tid; j < nr; j += RP_CONV_THREADS) {
                     const Cplx<float> a = W[swz(2 * j)], b = W[swz(2 * j + N)];
-                    accr[i] += a.x + b.x;
-                    acci[i] += a.y + b.y;
+                    C32 o = out[j];
+                    o.x += a.x + b.x;
+                    o.y += a.y + b.y;
+                    out[j] = o;
                 }
             }
             __syncthreads();
         }
-        C32* out = part + ((size_t)s * nsplit + sp) * nr;
+        if (MODE == 0) {
 #pragma unroll
-        for (int i = 0; i < KPT; ++i) {
-            const int j = tid + i * RP_CONV_THREADS;
-            if (j < nr) out[j] = C32{accr[i], acci[i]};
+            for (int i = 0; i < KPT; ++i) {
+                const int j = tid + i * RP_CONV_THREADS;
+                if (j < nr) out[j] = C32{accr[i], acci[i]};
+            }
         }
     }
 }
@@ -651,16 +682,34 @@ void fast_take_setup(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<C32>((size_t)L.nb * L.surf_slot);       // surface conv scratch
 }
 
-// 2nr + 4nr + nr complex64 = 56 nr bytes of shared memory per block (224 KiB at nr = 4096).
-bool use_smem_conv(const rp_scene* sc) { return sc->smem_conv && sc->nr <= 4096; }
+// Storage mode of the range compression (k_conv32s): 0 X and W in shared
+// memory (2nr + 4nr complex64 = 48 nr bytes, 192 KiB at nr = 4096), 1 X in
+// shared memory and W in global scratch (nr = 8192), 2 both in global
+// scratch (nr >= 16384), 3 the Bluestein kernel k_conv32 (nr not a power of
+// two).
+int conv_mode(const rp_scene* sc) {
+    if (!sc->smem_conv) return 3;
+    if (sc->nr <= 4096) return 0;
+    if (sc->nr <= 8192) return 1;
+    return 2;
+}
+
+// Complex values in one block's slot of the global compression scratch.
+size_t conv_gslot(const rp_scene* sc) {
+    const int m = conv_mode(sc);
+    return m == 1 ? (size_t)sc->mS : (m == 2 ? (size_t)(2 * sc->nr + sc->mS) : 0);
+}
 
 int64_t conv_splits(int64_t tstride) { return (tstride + RP_CONV_SPLIT - 1) / RP_CONV_SPLIT; }
 
 template <class Aa>
 void fast_take_pairs(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<C32>((size_t)RP_PARTS * L.nb * L.tstride * L.Wt);   // T parts
-    if (use_smem_conv(sc)) {
+    if (conv_mode(sc) <= 2) {
         a.template take<C32>((size_t)L.nb * conv_splits(L.tstride) * sc->nr);   // partial traces
+        // global compression scratch: one slot per SM (a wave takes one region
+        // for all its segments, sized here per segment as an upper bound)
+        if (conv_mode(sc) >= 1) a.template take<C32>((size_t)sc->sm_count * conv_gslot(sc));
     } else {
         a.template take<C32>((size_t)L.nb * L.tstride * sc->nr);        // Z
         a.template take<C32>((size_t)L.slots * L.slot);                  // conv scratch
@@ -759,25 +808,35 @@ void sinc_poly(double T, int D, double* mono) {
     }
 }
 
-template <int KPT>
-int launch_conv_k(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, size_t csm, int sms,
-                  unsigned int items, unsigned int* work, cudaStream_t st) {
-    RP_CUDA(cudaFuncSetAttribute(k_conv32s<KPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+template <int KPT, int MODE>
+int launch_conv_k(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, size_t csm, int sms, int slots,
+                  unsigned int items, unsigned int* work, C32* gscr, size_t gslot, cudaStream_t st) {
+    RP_CUDA(cudaFuncSetAttribute(k_conv32s<KPT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
     int occ = 0;
-    RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv32s<KPT>, RP_CONV_THREADS, csm));
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(occ, 1) * sms, items));
-    k_conv32s<KPT><<<grid, RP_CONV_THREADS, csm, st>>>(d_jobs, d_start, njobs, work);
+    RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv32s<KPT, MODE>, RP_CONV_THREADS, csm));
+    int64_t gmax = (int64_t)std::max(occ, 1) * sms;
+    if (MODE != 0) gmax = std::min<int64_t>(gmax, slots);      // one scratch slot per block
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(gmax, items));
+    k_conv32s<KPT, MODE><<<grid, RP_CONV_THREADS, csm, st>>>(d_jobs, d_start, njobs, work,
+                                                              reinterpret_cast<Cplx<float>*>(gscr), gslot);
     RP_LAUNCHED();
     return RP_OK;
 }
 
-int launch_conv32s(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, int max_nr,
-                   size_t csm, int sms, unsigned int items, unsigned int* work, cudaStream_t st) {
+// One compression launch over a job table of one storage mode (modes 1 and
+// 2: at most `slots` blocks, one per slot of the global scratch).
+int launch_conv32s(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, int mode, int max_nr,
+                   size_t csm, int sms, int slots, unsigned int items, unsigned int* work, C32* gscr,
+                   size_t gslot, cudaStream_t st) {
+#define RP_CONV_ARGS d_jobs, d_start, njobs, csm, sms, slots, items, work, gscr, gslot, st
+    if (mode == 1) return launch_conv_k<1, 1>(RP_CONV_ARGS);
+    if (mode == 2) return launch_conv_k<1, 2>(RP_CONV_ARGS);
     const int kpt = (max_nr + RP_CONV_THREADS - 1) / RP_CONV_THREADS;
-    if (kpt <= 1) return launch_conv_k<1>(d_jobs, d_start, njobs, csm, sms, items, work, st);
-    if (kpt <= 2) return launch_conv_k<2>(d_jobs, d_start, njobs, csm, sms, items, work, st);
-    if (kpt <= 4) return launch_conv_k<4>(d_jobs, d_start, njobs, csm, sms, items, work, st);
-    return launch_conv_k<8>(d_jobs, d_start, njobs, csm, sms, items, work, st);
+    if (kpt <= 1) return launch_conv_k<1, 0>(RP_CONV_ARGS);
+    if (kpt <= 2) return launch_conv_k<2, 0>(RP_CONV_ARGS);
+    if (kpt <= 4) return launch_conv_k<4, 0>(RP_CONV_ARGS);
+    return launch_conv_k<8, 0>(RP_CONV_ARGS);
+#undef RP_CONV_ARGS
 }
 
 // ---------------------------------------------------------- autotuner ----
@@ -828,7 +887,7 @@ struct Seg {
     // pair stage
     int Wt = 1;
     int nsplit = 0;
-    bool smem = false;
+    int cmode = 0;          // compression storage mode (conv_mode)
     bool pairs = false;
     C32* T = nullptr; C32* Z = nullptr; C32* cscr = nullptr; C32* part = nullptr;
 };
@@ -1053,19 +1112,27 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     RP_CUDA(cudaStreamSynchronize(st));
     g_timer.collect(0, 1);
     // ---- pair-stage buffers and job tables
-    std::vector<Seg*> ps, cs;
+    std::vector<Seg*> ps, cs[3];
+    size_t gslot[3] = {0, 0, 0};
     for (int i = 0; i < nseg; ++i) {
         Seg& g = segs[i];
         g.Wt = std::max(1, std::min(g.sc->nr, (h_misc[8 * i] + 3) & ~3));
         g.L = fast_layout(g.sc, g.nb, g.tmax, g.Wt);
-        g.smem = use_smem_conv(g.sc);
+        g.cmode = conv_mode(g.sc);
         g.nsplit = (int)conv_splits(g.L.tstride);
         g.pairs = g.sc->nt > 0 && g.sc->nf > 0 && g.tmax > 0;
         if (g.pairs) ps.push_back(&g);
-        if (g.pairs && g.smem) cs.push_back(&g);
+        if (g.pairs && g.cmode <= 2) {
+            cs[g.cmode].push_back(&g);
+            gslot[g.cmode] = std::max(gslot[g.cmode], conv_gslot(g.sc));
+        }
     }
+    // one global compression scratch region per wave, shared by the mode-1
+    // and mode-2 launches (they run one after the other on the stream)
+    const size_t gscr_n = (size_t)sms * std::max(gslot[1], gslot[2]);
+    const size_t ncs = cs[0].size() + cs[1].size() + cs[2].size();
     {
-        size_t need = 1024 + (ps.size() + cs.size()) * (sizeof(PairJob) + sizeof(ConvArgs) + 64);
+        size_t need = 4096 + (ps.size() + ncs) * (sizeof(PairJob) + sizeof(ConvArgs) + 64) + gscr_n * sizeof(C32);
         for (Seg& g : segs) need += seg_pair_bytes(g.sc, g.L);
         int rc = ws->arena2.reserve(need);
         if (rc) return rc;
@@ -1074,18 +1141,23 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     b.reset();
     for (Seg& g : segs) {
         g.T = b.take<C32>((size_t)RP_PARTS * g.nb * g.L.tstride * g.Wt);
-        if (g.smem) {
+        if (g.cmode <= 2) {
             g.part = b.take<C32>((size_t)g.nb * g.nsplit * g.sc->nr);
         } else {
             g.Z = b.take<C32>((size_t)g.nb * g.L.tstride * g.sc->nr);
             g.cscr = b.take<C32>((size_t)g.L.slots * g.L.slot);
         }
     }
+    C32* gscr = gscr_n ? b.take<C32>(gscr_n) : nullptr;
     unsigned int* d_work = b.take<unsigned int>(4);
     PairJob* d_pjobs = b.take<PairJob>(std::max<size_t>(ps.size(), 1));
     unsigned int* d_pstart = b.take<unsigned int>(ps.size() + 1);
-    ConvArgs* d_cjobs = b.take<ConvArgs>(std::max<size_t>(cs.size(), 1));
-    unsigned int* d_cstart = b.take<unsigned int>(cs.size() + 1);
+    ConvArgs* d_cjobs[3];
+    unsigned int* d_cstart[3];
+    for (int m = 0; m < 3; ++m) {
+        d_cjobs[m] = b.take<ConvArgs>(std::max<size_t>(cs[m].size(), 1));
+        d_cstart[m] = b.take<unsigned int>(cs[m].size() + 1);
+    }
     RP_CUDA(cudaMemsetAsync(d_work, 0, sizeof(unsigned int) * 4, st));
     for (Seg& g : segs)
         RP_CUDA(cudaMemsetAsync(g.T, 0, sizeof(C32) * RP_PARTS * g.nb * g.L.tstride * g.Wt, st));
@@ -1095,23 +1167,31 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         hp.push_back(PairJob{seg_pair_args(*g), g->deg});
         hps.push_back(hps.back() + (unsigned)(g->nb * hp.back().a.tblocks * RP_PARTS));
     }
-    std::vector<ConvArgs> hc;
-    std::vector<unsigned int> hcs(1, 0u);
-    int max_nr = 1;
-    size_t csm = 0;
-    for (Seg* g : cs) {
-        hc.push_back(seg_conv_args(*g));
-        hcs.push_back(hcs.back() + (unsigned)(g->nb * g->nsplit));
-        max_nr = std::max(max_nr, g->sc->nr);
-        csm = std::max(csm, (size_t)(2 * g->sc->nr + g->sc->mS) * sizeof(Cplx<float>));
+    std::vector<ConvArgs> hc[3];
+    std::vector<unsigned int> hcs[3];
+    int max_nr[3] = {1, 1, 1};
+    size_t csm[3] = {0, 0, 0};
+    for (int m = 0; m < 3; ++m) {
+        hcs[m].assign(1, 0u);
+        for (Seg* g : cs[m]) {
+            hc[m].push_back(seg_conv_args(*g));
+            hcs[m].push_back(hcs[m].back() + (unsigned)(g->nb * g->nsplit));
+            max_nr[m] = std::max(max_nr[m], g->sc->nr);
+            // shared memory: X and W (mode 0), X (mode 1), nothing (mode 2)
+            const size_t sx = m == 0 ? (size_t)(2 * g->sc->nr + g->sc->mS) : (m == 1 ? (size_t)(2 * g->sc->nr) : 0);
+            csm[m] = std::max(csm[m], sx * sizeof(Cplx<float>));
+        }
     }
     if (!hp.empty()) {
         RP_CUDA(cudaMemcpyAsync(d_pjobs, hp.data(), sizeof(PairJob) * hp.size(), cudaMemcpyHostToDevice, st));
         RP_CUDA(cudaMemcpyAsync(d_pstart, hps.data(), sizeof(unsigned int) * hps.size(), cudaMemcpyHostToDevice, st));
     }
-    if (!hc.empty()) {
-        RP_CUDA(cudaMemcpyAsync(d_cjobs, hc.data(), sizeof(ConvArgs) * hc.size(), cudaMemcpyHostToDevice, st));
-        RP_CUDA(cudaMemcpyAsync(d_cstart, hcs.data(), sizeof(unsigned int) * hcs.size(), cudaMemcpyHostToDevice, st));
+    for (int m = 0; m < 3; ++m) {
+        if (hc[m].empty()) continue;
+        RP_CUDA(cudaMemcpyAsync(d_cjobs[m], hc[m].data(), sizeof(ConvArgs) * hc[m].size(), cudaMemcpyHostToDevice,
+                                st));
+        RP_CUDA(cudaMemcpyAsync(d_cstart[m], hcs[m].data(), sizeof(unsigned int) * hcs[m].size(),
+                                cudaMemcpyHostToDevice, st));
     }
     // ---- pair stage: one launch for the wave
     if (!ps.empty()) {
@@ -1126,14 +1206,16 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         g_timer.mark(1, st);
     }
     g_timer.mark(2, st);
-    // ---- range compression: one launch for the shared-memory segments, the
-    // global-scratch kernel per remaining segment
-    if (!cs.empty()) {
-        int rc = launch_conv32s(d_cjobs, d_cstart, (int)cs.size(), max_nr, csm, sms, hcs.back(), d_work + 1, st);
+    // ---- range compression: one launch per storage mode over its job
+    // table, the Bluestein kernel per segment whose nr is not a power of two
+    for (int m = 0; m < 3; ++m) {
+        if (cs[m].empty()) continue;
+        int rc = launch_conv32s(d_cjobs[m], d_cstart[m], (int)cs[m].size(), m, max_nr[m], csm[m], sms, sms,
+                                hcs[m].back(), d_work + 1 + m, gscr, gslot[m], st);
         if (rc) return rc;
     }
     for (Seg* g : ps) {
-        if (g->smem) continue;
+        if (g->cmode <= 2) continue;
         const rp_scene* sc = g->sc;
         k_conv32<<<g->L.slots, 256, 0, st>>>(g->ntl, g->L.tstride, g->nb, g->bt0, g->T, g->Wt, g->Z,
                                             (const C32*)sc->d_C2_32, plan_view32(sc->plan2), plan_view32(sc->planN),
@@ -1150,7 +1232,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
                                             (const C32*)sc->d_C1_32, plan_view32(sc->plan2), g.refl, g.sscr,
                                             g.Lw.surf_slot);
         RP_LAUNCHED();
-        if (g.smem) {
+        if (g.cmode <= 2) {
             if (!g.pairs) RP_CUDA(cudaMemsetAsync(g.part, 0, sizeof(C32) * g.nb * g.nsplit * nr, st));
             k_sum32s<<<dim3((nr + 255) / 256, g.nb), 256, 0, st>>>(g.nill, g.ntl, g.refl, g.part, g.nsplit, nr,
                                                                   g.d_out, g.out64, (int)g.s0);

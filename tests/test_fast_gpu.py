@@ -105,9 +105,11 @@ def _vhf_scene(nr, n_side=120, fs=2.5, nt_side=4, ns=2, seed=5):
     return {"params": p, "facets": facets, "targets": targets}
 
 
-@pytest.mark.parametrize("nr", [4096, 8192])
+@pytest.mark.parametrize("nr", [4096, 8192, 16384, 6000])
 def test_fast_vhf_band(built_lib, oracle, nr):
-    # 4096 bins: shared-memory compression; 8192 bins: the global-scratch path
+    # compression storage modes: 4096 bins all in shared memory, 8192 the
+    # product spectrum in global scratch, 16384 both buffers in global
+    # scratch, 6000 (not a power of two) the Bluestein kernel
     sc = _vhf_scene(nr)
     got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle)
     assert got.shape[1] == nr
