@@ -66,7 +66,7 @@ struct MaxOpF { __device__ float operator()(float a, float b) const { return fma
 __global__ void __launch_bounds__(RP_CHUNK)
 k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx,
            const int* __restrict__ nill, const double* __restrict__ traces, DevParams dp,
-           FacetRec* __restrict__ rec, ChunkMeta* __restrict__ meta, int64_t rstride,
+           FacetPair* __restrict__ rec, ChunkMeta* __restrict__ meta, int64_t rstride,
            int64_t mstride, float* __restrict__ sx_o, C32* __restrict__ sv_o,
            unsigned long long* __restrict__ vmax) {
     __shared__ double shd[32];
@@ -93,6 +93,9 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
     double mxz = block_reduce(ok ? fz : -1e300, MaxOp(), shd);
     const double cx = 0.5 * (mnx + mxx), cy = 0.5 * (mny + mxy), cz = 0.5 * (mnz + mxz);
     float xI = 0.f, rr = 0.f;
+    float fv[RP_NFIELD];            // this facet's record fields (FacetField order)
+#pragma unroll
+    for (int f = 0; f < RP_NFIELD; ++f) fv[f] = 0.f;
     if (ok) {
         // FP64: the range and everything that becomes a phase or a bin
         // offset; FP32: the angles and amplitudes (relative error ~1e-6).
@@ -154,16 +157,41 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
         const float Kf = sqrtf((float)dp.P * grefr * G * (dp.lossless ? 1.f : frc) * (float)dp.nidx) * lamf *
                          lamf * Dmax / (f4 * df);
         xI = (float)((d - t.rst) / dp.dr);
-        double ti = d * dp.turn;
-        float tauI = (float)(ti - floor(ti));
+        const double ti = d * dp.turn;
         float ddx = (float)(fx - cx), ddy = (float)(fy - cy), ddz = (float)(fz - cz);
         rr = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
-        FacetRec r;
-        r.a = make_float4(ddx, ddy, ddz, ddx * ddx + ddy * ddy + ddz * ddz);
-        r.b = make_float4((float)nx, (float)ny, (float)nz, xI);
-        r.c = make_float4((float)ux, (float)uy, (float)uz, tauI);
-        r.d = make_float4((float)vx, (float)vy, (float)vz, (float)Kf);
-        rec[(size_t)s * rstride + j] = r;
+        fv[F_DX] = ddx; fv[F_DY] = ddy; fv[F_DZ] = ddz; fv[F_Q] = ddx * ddx + ddy * ddy + ddz * ddz;
+        fv[F_NX] = (float)nx; fv[F_NY] = (float)ny; fv[F_NZ] = (float)nz; fv[F_XI] = xI;
+        fv[F_UX] = (float)ux; fv[F_UY] = (float)uy; fv[F_UZ] = (float)uz;
+        fv[F_PH] = (float)(-2.0 * RP_PI * (ti - floor(ti)));
+        fv[F_VX] = (float)vx; fv[F_VY] = (float)vy; fv[F_VZ] = (float)vz; fv[F_K] = (float)Kf;
+    }
+    // interleave with the partner facet j ^ 1 (FacetPair): the even lane
+    // writes fields 0-7 of the pair, the odd lane fields 8-15; a missing odd
+    // partner is the even facet with K = 0
+    {
+        const int lane1 = threadIdx.x & 1;
+        const bool pok = __shfl_xor_sync(0xffffffffu, ok ? 1 : 0, 1) != 0;
+        float pv[RP_NFIELD];
+#pragma unroll
+        for (int f = 0; f < RP_NFIELD; ++f) pv[f] = __shfl_xor_sync(0xffffffffu, fv[f], 1);
+        const bool pair_ok = lane1 ? pok : ok;      // the pair's even facet exists
+        if (pair_ok) {
+            float e[RP_NFIELD], o[RP_NFIELD];        // even and odd facet of the pair
+#pragma unroll
+            for (int f = 0; f < RP_NFIELD; ++f) {
+                e[f] = lane1 ? pv[f] : fv[f];
+                const bool odd_ok = lane1 ? ok : pok;
+                o[f] = odd_ok ? (lane1 ? fv[f] : pv[f]) : (f == F_K ? 0.f : e[f]);
+            }
+            FacetPair* pr = rec + ((size_t)s * rstride + j) / 2;
+            const int h = lane1 * (RP_NFIELD / 4);  // first float4 this lane writes
+#pragma unroll
+            for (int i = 0; i < RP_NFIELD / 4; ++i) {
+                const int f = 2 * (h + i);
+                pr->v[h + i] = make_float4(e[f], o[f], e[f + 1], o[f + 1]);
+            }
+        }
     }
     float R = block_reduce(ok ? rr : 0.f, MaxOpF(), shf);
     float xmn = block_reduce(ok ? xI : 3e38f, MinOpF(), shf);
@@ -668,7 +696,7 @@ void fast_take_setup(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<unsigned long long>(L.nb);              // vmax
     a.template take<unsigned long long>(L.nb);              // dmin
     a.template take<int>((size_t)L.nb * nf);                // idx
-    a.template take<FacetRec>((size_t)L.nb * L.rstride);    // records
+    a.template take<FacetPair>((size_t)L.nb * L.rstride / 2);    // records (facet pairs)
     a.template take<ChunkMeta>((size_t)L.nb * L.mstride);   // chunk meta
     a.template take<float>((size_t)L.nb * nf);              // surface x
     a.template take<C32>((size_t)L.nb * nf);                // surface v
@@ -882,7 +910,7 @@ struct Seg {
     FastLayout Lw, L;
     // setup stage
     uint8_t* fflags; int* tcnt; int* nill; int* ntl; unsigned long long* vmax; unsigned long long* dmin;
-    int* idx; FacetRec* rec; ChunkMeta* meta; float* sxv; C32* sv; TraceMeta* tm; uint8_t* tflags;
+    int* idx; FacetPair* rec; ChunkMeta* meta; float* sxv; C32* sv; TraceMeta* tm; uint8_t* tflags;
     int* tlist; int* bt0; int* misc; long long* acc; C32* refl; C32* sscr;
     // pair stage
     int Wt = 1;
@@ -934,7 +962,7 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
     g.vmax = a.take<unsigned long long>(nb);
     g.dmin = a.take<unsigned long long>(nb);
     g.idx = a.take<int>((size_t)nb * nfa);
-    g.rec = a.take<FacetRec>((size_t)nb * Lw.rstride);
+    g.rec = a.take<FacetPair>((size_t)nb * Lw.rstride / 2);
     g.meta = a.take<ChunkMeta>((size_t)nb * Lw.mstride);
     g.sxv = a.take<float>((size_t)nb * nfa);
     g.sv = a.take<C32>((size_t)nb * nfa);
@@ -997,9 +1025,12 @@ PairArgs seg_pair_args(const Seg& g) {
     P.nr_f = (float)nr; P.nr = nr; P.nr1 = nr - 1;
     P.kb = (float)(dp.nidx / dp.dr);
     P.kt = (float)(dp.nidx * dp.turn);
-    P.pik = (float)(RP_PI * (RP_PI_F * dp.fs / dp.lam));
-    P.pik2 = P.pik * P.pik;
-    for (int k = 0; k < 8; ++k) P.sc[k] = (float)g.coef[k];
+    P.kr = (float)(-2.0 * RP_PI * dp.nidx * dp.turn);
+    const double pik_d = RP_PI * (RP_PI_F * dp.fs / dp.lam);
+    P.pik = (float)pik_d;
+    P.pik2 = (float)(pik_d * pik_d);
+    // the kernel's polynomial argument is t' = a^2 / pik^2 in [0, 1]
+    for (int k = 0; k < 8; ++k) P.sc[k] = (float)(g.coef[k] * std::pow(pik_d * pik_d, k));
     P.ealpha = dp.lossless ? 0.f : (float)(-2.0 * dp.alpha2 * 1.4426950408889634);
     P.eks = dp.lossless ? 0.f : (float)(-2.0 * dp.ks * dp.ks * 1.4426950408889634);
     P.nidx = dp.nidx; P.inv_dr = 1.0 / dp.dr; P.inv_lam = dp.turn;

@@ -1,10 +1,10 @@
 // rp_pair.cuh -- the pair stage of the fast form, shared by the single-batch
-// kernel (rp_fast.cu) and the multi-job kernel (rp_multi.cu): the per-facet
+// kernel (rp_fast.cu) and the multi-job kernel (rp_multi.cu): the facet-pair
 // record, the TMA bulk staging helpers, the FP32 split-precision evaluation of
-// one (facet, target) pair (compTargetRays, compRefrEnergyIn,
-// accumulateTarget: geometry_kernels.cu:272-350, 520-554,
-// radar_kernels.cu:767-830), the deterministic window binning and the body
-// of one work item.
+// two (facet, target) pairs at once in packed two-lane FP32 instructions
+// (compTargetRays, compRefrEnergyIn, accumulateTarget: geometry_kernels.cu:
+// 272-350, 520-554, radar_kernels.cu:767-830), the deterministic window
+// binning and the body of one work item.
 //
 // The two kernels live in separate translation units: compiled together, the
 // multi-job kernel's call sites of the out-of-line helpers changed the code
@@ -26,12 +26,38 @@ namespace rpk {
 
 using C32 = Cx<float>;
 
-struct __align__(16) FacetRec {
-    float4 a;   // dx, dy, dz (facet - chunk centre), |d|^2
-    float4 b;   // nx, ny, nz, xI = (Itd - rst) / dr
-    float4 c;   // ux, uy, uz, tauI = frac(Itd / lam)
-    float4 d;   // vx, vy, vz, K = amplitude factor
+// Records of two consecutive facets of a chunk, interleaved field by field:
+// v[i] = {field 2i of facet 0, field 2i of facet 1, field 2i+1 of facet 0,
+// field 2i+1 of facet 1}.  One 128-bit shared-memory load then leaves a
+// field of both facets in adjacent registers, the operand of one packed
+// two-lane FP32 instruction.  A chunk with an odd count ends with a pair
+// whose second facet repeats the first with K = 0 (it adds exact zeros).
+enum FacetField {
+    F_DX, F_DY, F_DZ, F_Q,      // facet - chunk centre, |facet - chunk centre|^2
+    F_NX, F_NY, F_NZ, F_XI,     // normal, xI = (Itd - rst) / dr
+    F_UX, F_UY, F_UZ, F_PH,     // u tangent, -2 pi frac(Itd / lam) (radians)
+    F_VX, F_VY, F_VZ, F_K,      // v tangent, K = hoisted amplitude factor
+    RP_NFIELD
 };
+struct __align__(16) FacetPair {
+    float4 v[RP_NFIELD / 2];
+};
+#define RP_CHUNK_PAIRS (RP_CHUNK / 2)
+
+// Field f of both facets of a pair.
+template <int F>
+__device__ __forceinline__ float2 fld(const FacetPair& p) {
+    const float4& q = p.v[F >> 1];
+    return (F & 1) ? make_float2(q.z, q.w) : make_float2(q.x, q.y);
+}
+
+// Packed two-lane FP32 arithmetic (sm_100 and later: one instruction for
+// both lanes, each lane rounded exactly as fmaf / __fmul_rn / __fadd_rn).
+using f2 = float2;
+__device__ __forceinline__ f2 bc(float a) { return make_float2(a, a); }
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ f2 add2(f2 a, f2 b) { return __fadd2_rn(a, b); }
 
 struct __align__(16) ChunkMeta {
     double cx, cy, cz;     // chunk centre
@@ -80,7 +106,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
 
 // ----------------------------------------------------------- pair kernel --
 struct PairArgs {
-    const FacetRec* rec;
+    const FacetPair* rec;   // [nb][rstride / 2] facet pairs
     const ChunkMeta* meta;
     int64_t rstride, mstride;
     const int* nill;
@@ -103,10 +129,11 @@ struct PairArgs {
     int nr;
     int nr1;            // nr - 1: both split bins are inside the trace when b < nr - 1
     float kb;           // n / dr
-    float kt;           // n / lam
+    float kt;           // n / lam (turns per metre)
+    float kr;           // -2 pi n / lam (radians per metre)
     float pik;          // pi * (pi_F * fs / lam): sinc arguments in radians
     float pik2;         // pik^2
-    float sc[8];        // sinc polynomial coefficients in t = a^2 (sinc_poly)
+    float sc[8];        // sinc polynomial in t' = a^2 / pik^2 (sinc_poly, scaled)
     float ealpha;       // -2 alpha2 log2(e)
     float eks;          // -2 ks^2 log2(e)
     double nidx, inv_dr, inv_lam;   // inv_lam: turns per metre, pi_F / (pi lam)
@@ -124,7 +151,7 @@ struct PairJob {
 struct Anchor {
     float Dx, Dy, Dz;     // target - chunk centre (FP32 of an FP64 difference)
     float T0, T0sq;       // |target - chunk centre| (FP64 -> FP32)
-    float tau0;           // frac(n T0 turn): phase of the anchor in turns
+    float ph0;            // -2 pi frac(n T0 / lam): phase of the anchor (radians)
     float xbase;          // n T0 / dr - blo (bins, relative to the window start)
     float tnx, tny, tnz;  // target normal
     float eaT0;           // ealpha T0: the attenuation exponent at the anchor
@@ -148,106 +175,104 @@ __device__ __forceinline__ float ex2_a(float x) {
     return y;
 }
 
-// sin(a)/a as a degree-D polynomial in t = a^2 (coefficients fitted per
-// scene on [0, amax^2], see sinc_poly), Horner form.
+// sin(a)/a as a degree-D polynomial in t' = a^2 / pik^2 (coefficients
+// fitted per scene on a in [0, amax] and scaled, see sinc_poly), Horner
+// form, both lanes at once.
 template <int D>
-__device__ __forceinline__ float sinc_poly_eval(const float* c, float t) {
-    float s = c[D];
+__device__ __forceinline__ f2 sinc_poly2(const float* c, f2 t) {
+    f2 s = fma2(bc(c[D]), t, bc(c[D - 1]));
 #pragma unroll
-    for (int k = D - 1; k >= 0; --k) s = fmaf(s, t, c[k]);
+    for (int k = D - 2; k >= 0; --k) s = fma2(s, t, bc(c[k]));
     return s;
 }
 
-// One (facet, target) evaluation of the target leg (compTargetRays,
+// sin(a)/a for a^2 = u through the special-function unit; 1 for |a| < pi
+// 1e-6 (elementary_kernels.cu:50-53).  Returns the sine and the divisor
+// separately so four factors share one division.
+__device__ __forceinline__ void sinc_sfu(float u, float& num, float& den) {
+    const float a = u > 0.f ? u * rsqrt_a(u) : 0.f;
+    const bool z = a < 3.14159265e-6f;
+    num *= z ? 1.f : __sinf(a);
+    den *= z ? 1.f : a;
+}
+
+// Two (facet, target) evaluations of the target leg (compTargetRays,
 // compRefrEnergyIn, accumulateTarget; geometry_kernels.cu:272-350, 520-554,
-// radar_kernels.cu:767-830).  Returns the phasor and x - blo, the bin
-// coordinate relative to the window start.
+// radar_kernels.cu:767-830): the two facets of pair record r against one
+// target, in packed two-lane FP32.  Returns per lane the phasor and x - blo,
+// the bin coordinate relative to the window start.
 //
 // The two directivities facet_G(Tth, Tph) and facet_G(TargetTh, Tph)
 // (radar_kernels.cu:658-677) need sinc(pik/pi * sin(th) cos(ph)) and
-// sinc(pik/pi * sin(th) sin(ph)), sinc(x) = sin(pi x)/(pi x).  With
-// cos(Tph) = xv / sqrt(h2), sin(Tph) = yu / sqrt(h2) and sin^2(th) = 1 - c^2,
-// the squared sinc arguments are pik^2 (1 - c^2) xv^2 / h2 etc. (atan2(0, 0)
-// = 0 gives xv^2/h2 = 1, yu^2/h2 = 0).  NT > 0 evaluates sin(a)/a as a
-// polynomial in a^2 (no special-function unit); NT == 0 uses sin(a)/a with
-// one shared reciprocal, 1 for |a| < pi 1e-6 (elementary_kernels.cu:50-53).
-// RED: reduce the phase to [-1/2, 1/2] turns before the special-function
-// sine and cosine; the fast path skips it when the chunk keeps |tau| below
-// 42 turns (sin/cos.approx hold their accuracy over +-100 pi radians).
+// sinc(pik/pi * sin(th) sin(ph)), sinc(x) = sin(pi x)/(pi x).  The direction
+// e = facet - target is not normalised: with its dot products pb = e.n,
+// pt = e.n_target, pc = e.u, pd = e.v and d2 = |e|^2, sin^2(th) = 1 -
+// pb^2/d2 (likewise with pt) and cos^2(ph) = xs = pd^2 / (pc^2 + pd^2),
+// sin^2(ph) = 1 - xs, so the four squared arguments over pik^2 are
+// sin^2(th) xs and sin^2(th) (1 - xs) per angle.  A tiny constant in both
+// sums of xs gives xs = 1 when pc = pd = 0 (atan2(0, 0) = 0: cos = 1), and
+// changes nothing measurable otherwise.  1 - c^2 may round a hair below 0
+// for |c| ~ 1: harmless in the polynomial, clamped for the SFU path.  NT > 0
+// evaluates sin(a)/a as a polynomial in a^2; NT == 0 uses the SFU.
+// RED: reduce the phase to [-pi, pi] before the special-function sine and
+// cosine; the fast path skips it when the chunk keeps |phase| below 84 pi
+// (sin/cos.approx hold their accuracy over +-100 pi radians).
 template <int NT, bool RED = true>
-__device__ __forceinline__ void pair_eval(const FacetRec& r, const Anchor& an, const PairArgs& A,
-                                          float& xr, float& vre, float& vim) {
-    const float dd = fmaf(an.Dx, r.a.x, fmaf(an.Dy, r.a.y, an.Dz * r.a.z));
-    const float qd = fmaf(-2.f, dd, r.a.w);             // Ttd^2 - T0^2
-    const float d2 = an.T0sq + qd;
-    const float rinv = rsqrt_a(d2);
-    const float dT = qd * rcp_a(fmaf(d2, rinv, an.T0));  // Ttd - T0 without cancellation
-    float S, cT2;
+__device__ __forceinline__ void pair_eval2(const FacetPair& r, const Anchor& an, const PairArgs& A, f2& xr,
+                                           f2& vre, f2& vim) {
+    const f2 ONE = bc(1.f), M1 = bc(-1.f);
+    const f2 dx = fld<F_DX>(r), dy = fld<F_DY>(r), dz = fld<F_DZ>(r);
+    const f2 Dx = bc(an.Dx), Dy = bc(an.Dy), Dz = bc(an.Dz);
+    const f2 dd = fma2(Dx, dx, fma2(Dy, dy, mul2(Dz, dz)));
+    const f2 qd = fma2(bc(-2.f), dd, fld<F_Q>(r));              // Ttd^2 - T0^2
+    const f2 d2 = add2(bc(an.T0sq), qd);
+    const f2 rinv = make_float2(rsqrt_a(d2.x), rsqrt_a(d2.y));
+    const f2 sT = fma2(d2, rinv, bc(an.T0));                     // Ttd + T0
+    const f2 dT = mul2(qd, make_float2(rcp_a(sT.x), rcp_a(sT.y)));   // Ttd - T0 without cancellation
+    // e = facet - target; only squares of its dot products enter
+    const f2 ex = fma2(Dx, M1, dx), ey = fma2(Dy, M1, dy), ez = fma2(Dz, M1, dz);
+    const f2 pb = fma2(ex, fld<F_NX>(r), fma2(ey, fld<F_NY>(r), mul2(ez, fld<F_NZ>(r))));
+    const f2 pt = fma2(ex, bc(an.tnx), fma2(ey, bc(an.tny), mul2(ez, bc(an.tnz))));
+    const f2 pc = fma2(ex, fld<F_UX>(r), fma2(ey, fld<F_UY>(r), mul2(ez, fld<F_UZ>(r))));
+    const f2 pd = fma2(ex, fld<F_VX>(r), fma2(ey, fld<F_VY>(r), mul2(ez, fld<F_VZ>(r))));
+    const f2 inv_d2 = mul2(rinv, rinv);
+    const f2 cT2 = mul2(mul2(pb, pb), inv_d2);
+    const f2 aT = fma2(cT2, M1, ONE);
+    const f2 aD = fma2(mul2(mul2(pt, pt), inv_d2), M1, ONE);
+    const f2 X = fma2(pd, pd, bc(1e-30f));
+    const f2 h2 = fma2(pc, pc, X);
+    const f2 xs = mul2(X, make_float2(rcp_a(h2.x), rcp_a(h2.y)));
+    const f2 t1 = mul2(aT, xs), t3 = mul2(aD, xs);
+    const f2 t2 = fma2(t1, M1, aT), t4 = fma2(t3, M1, aD);
+    f2 S;
     if (NT > 0) {
-        // The polynomial sinc needs only ratios of the direction's dot
-        // products, so the direction e = target - facet is not normalised:
-        // cos^2(Tth) = (e.n)^2 / |e|^2, 1 - cos^2 per angle, and the squared
-        // in-plane split xx = pik^2 (e.v)^2 / ((e.u)^2 + (e.v)^2), yy =
-        // pik^2 - xx (atan2(0, 0) = 0 gives xx = pik^2, yy = 0).  1 - c^2 may
-        // round a hair below 0 for |c| ~ 1: harmless in the polynomial.
-        const float ex = an.Dx - r.a.x, ey = an.Dy - r.a.y, ez = an.Dz - r.a.z;
-        const float pb = fmaf(ex, r.b.x, fmaf(ey, r.b.y, ez * r.b.z));
-        const float pt = fmaf(ex, an.tnx, fmaf(ey, an.tny, ez * an.tnz));
-        const float pc = fmaf(ex, r.c.x, fmaf(ey, r.c.y, ez * r.c.z));
-        const float pd = fmaf(ex, r.d.x, fmaf(ey, r.d.y, ez * r.d.z));
-        const float inv_d2 = rcp_a(d2);
-        const float pb2 = pb * pb;
-        cT2 = pb2 * inv_d2;
-        const float aT = 1.f - cT2;
-        const float aD = fmaf(-pt * pt, inv_d2, 1.f);
-        const float X = pd * pd;
-        const float h2 = fmaf(pc, pc, X);
-        const bool hz = !(h2 > 0.f);
-        const float k2 = A.pik2 * rcp_a(h2);
-        const float xx = hz ? A.pik2 : k2 * X;
-        const float yy = A.pik2 - xx;
-        S = sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aT * xx) * sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aT * yy) *
-            sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aD * xx) * sinc_poly_eval<(NT > 0 ? NT : 1)>(A.sc, aD * yy);
+        constexpr int D = NT > 0 ? NT : 1;
+        S = mul2(mul2(sinc_poly2<D>(A.sc, t1), sinc_poly2<D>(A.sc, t2)),
+                 mul2(sinc_poly2<D>(A.sc, t3), sinc_poly2<D>(A.sc, t4)));
+        if (NT >= 5) S = make_float2(fabsf(S.x), fabsf(S.y));   // sinc changes sign beyond a = pi
     } else {
-        const float jx = (an.Dx - r.a.x) * rinv;
-        const float jy = (an.Dy - r.a.y) * rinv;
-        const float jz = (an.Dz - r.a.z) * rinv;
-        float cT = -fmaf(jx, r.b.x, fmaf(jy, r.b.y, jz * r.b.z));
-        float cD = -fmaf(jx, an.tnx, fmaf(jy, an.tny, jz * an.tnz));
-        const float yu = fmaf(jx, r.c.x, fmaf(jy, r.c.y, jz * r.c.z));
-        const float xv = fmaf(jx, r.d.x, fmaf(jy, r.d.y, jz * r.d.z));
-        const float h2 = fmaf(yu, yu, xv * xv);
-        cT = fminf(1.f, fmaxf(-1.f, cT));
-        cD = fminf(1.f, fmaxf(-1.f, cD));
-        cT2 = cT * cT;
-        const float aT = fmaf(-cT, cT, 1.f);
-        const float aD = fmaf(-cD, cD, 1.f);
-        const bool hz = !(h2 > 0.f);
-        const float pT = aT * h2, pD = aD * h2;
-        const float gT = (pT > 0.f) ? aT * rsqrtf(pT) : 0.f;
-        const float gD = (pD > 0.f) ? aD * rsqrtf(pD) : 0.f;
-        const float a1 = A.pik * (hz ? sqrtf(aT) : gT * xv);
-        const float a2 = A.pik * (hz ? 0.f : gT * yu);
-        const float a3 = A.pik * (hz ? sqrtf(aD) : gD * xv);
-        const float a4 = A.pik * (hz ? 0.f : gD * yu);
-        const float eps = 3.14159265e-6f;
-        const bool z1 = fabsf(a1) < eps, z2 = fabsf(a2) < eps, z3 = fabsf(a3) < eps, z4 = fabsf(a4) < eps;
-        const float num = (z1 ? 1.f : __sinf(a1)) * (z2 ? 1.f : __sinf(a2)) * (z3 ? 1.f : __sinf(a3)) *
-                          (z4 ? 1.f : __sinf(a4));
-        const float den = (z1 ? 1.f : a1) * (z2 ? 1.f : a2) * (z3 ? 1.f : a3) * (z4 ? 1.f : a4);
-        S = __fdividef(num, den);
+        const f2 P2 = bc(A.pik2);
+        const f2 u1 = mul2(t1, P2), u2 = mul2(t2, P2), u3 = mul2(t3, P2), u4 = mul2(t4, P2);
+        float n0 = 1.f, e0 = 1.f, n1 = 1.f, e1 = 1.f;
+        sinc_sfu(u1.x, n0, e0); sinc_sfu(u2.x, n0, e0); sinc_sfu(u3.x, n0, e0); sinc_sfu(u4.x, n0, e0);
+        sinc_sfu(u1.y, n1, e1); sinc_sfu(u2.y, n1, e1); sinc_sfu(u3.y, n1, e1); sinc_sfu(u4.y, n1, e1);
+        S = make_float2(fabsf(__fdividef(n0, e0)), fabsf(__fdividef(n1, e1)));
     }
     // attenuation and roughness (zero constants when lossless); ealpha Ttd
     // = ealpha T0 + ealpha (Ttd - T0)
-    const float e2 = fmaf(A.eks, cT2, fmaf(A.ealpha, dT, an.eaT0));
-    const float amp = r.d.w * fabsf(S) * rinv * ex2_a(e2);
-    float tau = (r.c.w + an.tau0) + A.kt * dT;
-    if (RED) tau -= rintf(tau);
-    float sn, cs;
-    __sincosf(-6.28318530717958647f * tau, &sn, &cs);
-    vre = amp * cs;
-    vim = amp * sn;
-    xr = r.b.w + an.xbase + A.kb * dT;
+    const f2 e2 = fma2(bc(A.eks), cT2, fma2(bc(A.ealpha), dT, bc(an.eaT0)));
+    const f2 amp = mul2(mul2(fld<F_K>(r), S), mul2(rinv, make_float2(ex2_a(e2.x), ex2_a(e2.y))));
+    f2 ph = fma2(bc(A.kr), dT, add2(fld<F_PH>(r), bc(an.ph0)));
+    if (RED) {
+        const f2 k = mul2(ph, bc(0.159154943091895336f));
+        ph = fma2(make_float2(rintf(k.x), rintf(k.y)), bc(-6.28318530717958647f), ph);
+    }
+    f2 sn, cs;
+    __sincosf(ph.x, &sn.x, &cs.x);
+    __sincosf(ph.y, &sn.y, &cs.y);
+    vre = mul2(amp, cs);
+    vim = mul2(amp, sn);
+    xr = fma2(bc(A.kb), dT, add2(fld<F_XI>(r), bc(an.xbase)));
 }
 
 // Attenuation-prism factor for one pair (compTargetRays, geometry_kernels.cu:
@@ -359,36 +384,51 @@ __device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo,
     }
 }
 
-// bin_add for a chunk whose pairs all fall inside the window and the trace
-// (pair_item checks that per chunk and warp): no range tests, no edge path.
-// The clamp only keeps a (never expected) stray bin inside the window.
-__device__ __forceinline__ void bin_add_fast(float xr, float vre, float vim, float2* win, int tid) {
-    const int f = floor_i(xr);
-    const float w = xr - (float)f;
-    const unsigned sl = min((unsigned)f, (unsigned)(RP_WIN - 2));
-    float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
-    float2* p1 = p0 + RP_PAIR_THREADS;
-    float2 v0 = *p0, v1 = *p1;
-    const float w0 = 1.f - w;
-    v0.x = fmaf(vre, w0, v0.x);
-    v0.y = fmaf(vim, w0, v0.y);
-    v1.x = fmaf(vre, w, v1.x);
-    v1.y = fmaf(vim, w, v1.y);
-    *p0 = v0;
-    *p1 = v1;
+// bin_add for the two lanes of a pair evaluation in a chunk whose pairs all
+// fall inside the window and the trace (pair_item checks that per chunk and
+// warp): no range tests, no edge path, lane 0 before lane 1.  The clamp only
+// keeps a (never expected) stray bin inside the window.
+__device__ __forceinline__ void bin_add_fast2(f2 xr, f2 vre, f2 vim, float2* win, int tid) {
+    const int f0 = floor_i(xr.x), f1 = floor_i(xr.y);
+    const f2 w = fma2(make_float2((float)f0, (float)f1), bc(-1.f), xr);
+    const f2 w0 = fma2(w, bc(-1.f), bc(1.f));
+    {
+        const unsigned sl = min((unsigned)f0, (unsigned)(RP_WIN - 2));
+        float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
+        float2* p1 = p0 + RP_PAIR_THREADS;
+        float2 v0 = *p0, v1 = *p1;
+        v0.x = fmaf(vre.x, w0.x, v0.x);
+        v0.y = fmaf(vim.x, w0.x, v0.y);
+        v1.x = fmaf(vre.x, w.x, v1.x);
+        v1.y = fmaf(vim.x, w.x, v1.y);
+        *p0 = v0;
+        *p1 = v1;
+    }
+    {
+        const unsigned sl = min((unsigned)f1, (unsigned)(RP_WIN - 2));
+        float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
+        float2* p1 = p0 + RP_PAIR_THREADS;
+        float2 v0 = *p0, v1 = *p1;
+        v0.x = fmaf(vre.y, w0.y, v0.x);
+        v0.y = fmaf(vim.y, w0.y, v0.y);
+        v1.x = fmaf(vre.y, w.y, v1.x);
+        v1.y = fmaf(vim.y, w.y, v1.y);
+        *p0 = v0;
+        *p1 = v1;
+    }
 }
 
 // Dynamic shared memory of the pair kernels: two record buffers, the
 // per-thread bin windows, the threads' FP64 target positions.
 extern __shared__ __align__(128) unsigned char pair_smem[];
-#define RP_PAIR_WIN_OFF (2 * RP_CHUNK * sizeof(FacetRec))
+#define RP_PAIR_WIN_OFF (2 * RP_CHUNK_PAIRS * sizeof(FacetPair))
 #define RP_PAIR_TPOS_OFF (RP_PAIR_WIN_OFF + (size_t)RP_WIN * RP_PAIR_THREADS * sizeof(float2))
 #define RP_PAIR_SMEM_BYTES (RP_PAIR_TPOS_OFF + 3 * RP_PAIR_THREADS * sizeof(double))
 
 template <int NT, int ILP, class PA>
 __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, uint64_t* bars, uint32_t* phase) {
     // every hot shared array is derived here from the shared symbol itself
-    FacetRec* srec = reinterpret_cast<FacetRec*>(pair_smem);                       // [2][RP_CHUNK]
+    FacetPair* srec = reinterpret_cast<FacetPair*>(pair_smem);                     // [2][RP_CHUNK_PAIRS]
     float2* win = reinterpret_cast<float2*>(pair_smem + RP_PAIR_WIN_OFF);          // [RP_WIN][threads]
     double* s_tpos = reinterpret_cast<double*>(pair_smem + RP_PAIR_TPOS_OFF);      // [3][threads]
     const int tid = threadIdx.x;
@@ -414,13 +454,13 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         b0 = A.bt0[(size_t)s * A.tstride + q];
         Trow = A.T + (((size_t)part * A.nb + s) * A.tstride + q) * A.Wt;
     }
-    const FacetRec* rbase = A.rec + (size_t)s * A.rstride;
-    // prologue: stage chunk k0
+    const FacetPair* rbase = A.rec + (size_t)s * (A.rstride / 2);
+    // prologue: stage chunk k0 (whole pairs: an odd count ends with a padded pair)
     if (tid == 0) {
         int cnt = min(RP_CHUNK, n - k0 * RP_CHUNK);
-        uint32_t bytes = (uint32_t)(cnt * sizeof(FacetRec));
+        uint32_t bytes = (uint32_t)(((cnt + 1) >> 1) * sizeof(FacetPair));
         mbar_expect_tx(&bars[0], bytes);
-        tma_bulk_g2s(srec, rbase + (size_t)k0 * RP_CHUNK, bytes, &bars[0]);
+        tma_bulk_g2s(srec, rbase + (size_t)k0 * RP_CHUNK_PAIRS, bytes, &bars[0]);
     }
     for (int k = k0; k < k1; ++k) {
         const int buf = (k - k0) & 1;
@@ -428,9 +468,9 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         // finished at the trailing __syncthreads of the previous step)
         if (tid == 0 && k + 1 < k1) {
             int cnt = min(RP_CHUNK, n - (k + 1) * RP_CHUNK);
-            uint32_t bytes = (uint32_t)(cnt * sizeof(FacetRec));
+            uint32_t bytes = (uint32_t)(((cnt + 1) >> 1) * sizeof(FacetPair));
             mbar_expect_tx(&bars[buf ^ 1], bytes);
-            tma_bulk_g2s(srec + (buf ^ 1) * RP_CHUNK, rbase + (size_t)(k + 1) * RP_CHUNK, bytes,
+            tma_bulk_g2s(srec + (buf ^ 1) * RP_CHUNK_PAIRS, rbase + (size_t)(k + 1) * RP_CHUNK_PAIRS, bytes,
                          &bars[buf ^ 1]);
         }
         const ChunkMeta* mp = A.meta + (size_t)s * A.mstride + k;
@@ -438,7 +478,7 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
             if (tid == 0) atomicOr(A.err + 1, 1u);
         }
         phase[buf] ^= 1u;
-        const FacetRec* R = srec + buf * RP_CHUNK;
+        const FacetPair* R = srec + buf * RP_CHUNK_PAIRS;
         Anchor an;
         int blo = 0;
         bool fits = true;
@@ -449,7 +489,7 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
                          Dz = s_tpos[2 * RP_PAIR_THREADS + tid] - mcz;
             const double T0 = sqrt(Dx * Dx + Dy * Dy + Dz * Dz);
             const double xt = A.nidx * T0 * A.inv_dr;
-            const double tt = A.nidx * T0 * A.inv_lam;
+            const double tt = A.nidx * T0 * A.inv_lam;      // turns
             const double lo = (double)mp->xmin + A.nidx * (T0 - (double)mp->R) * A.inv_dr;
             const double hi = (double)mp->xmax + A.nidx * (T0 + (double)mp->R) * A.inv_dr;
             blo = (int)floor(lo) - 1;
@@ -460,7 +500,7 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
                    (double)A.kt * (double)mp->R < 40.0;     // |kt dT| <= kt R: the phase bound
             an.Dx = (float)Dx; an.Dy = (float)Dy; an.Dz = (float)Dz;
             an.T0 = (float)T0; an.T0sq = (float)(T0 * T0);
-            an.tau0 = (float)(tt - floor(tt));
+            an.ph0 = (float)(-2.0 * 3.14159265358979323846 * (tt - floor(tt)));
             an.xbase = (float)(xt - (double)blo);
             an.tnx = tnx; an.tny = tny; an.tnz = tnz;
             an.eaT0 = (float)((double)A.ealpha * T0);
@@ -469,53 +509,44 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         if (active) {
             for (int w = 0; w < RP_WIN; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
             const int cnt = mp->n;
+            const int npairs = (cnt + 1) >> 1;
             const bool prisms = (A.np > 0) && !A.lossless;
-            int jj = 0;
+            int jp = 0;
             if (all_fit && !prisms) {
                 if (ILP == 2)
-                for (; jj + 1 < cnt; jj += 2) {
-                    const FacetRec r0 = R[jj];
-                    const FacetRec r1 = R[jj + 1];
-                    float x0, re0, im0, x1, re1, im1;
-                    pair_eval<NT, false>(r0, an, A, x0, re0, im0);
-                    pair_eval<NT, false>(r1, an, A, x1, re1, im1);
-                    bin_add_fast(x0, re0, im0, win, tid);
-                    bin_add_fast(x1, re1, im1, win, tid);
+                for (; jp + 1 < npairs; jp += 2) {
+                    const FacetPair r0 = R[jp];
+                    const FacetPair r1 = R[jp + 1];
+                    f2 x0, re0, im0, x1, re1, im1;
+                    pair_eval2<NT, false>(r0, an, A, x0, re0, im0);
+                    pair_eval2<NT, false>(r1, an, A, x1, re1, im1);
+                    bin_add_fast2(x0, re0, im0, win, tid);
+                    bin_add_fast2(x1, re1, im1, win, tid);
                 }
-                for (; jj < cnt; ++jj) {
-                    const FacetRec r0 = R[jj];
-                    float x0, re0, im0;
-                    pair_eval<NT, false>(r0, an, A, x0, re0, im0);
-                    bin_add_fast(x0, re0, im0, win, tid);
+                for (; jp < npairs; ++jp) {
+                    const FacetPair r0 = R[jp];
+                    f2 x0, re0, im0;
+                    pair_eval2<NT, false>(r0, an, A, x0, re0, im0);
+                    bin_add_fast2(x0, re0, im0, win, tid);
                 }
             } else {
-                if (ILP == 2)
-                for (; jj + 1 < cnt; jj += 2) {
-                    const FacetRec r0 = R[jj];
-                    const FacetRec r1 = R[jj + 1];
-                    float x0, re0, im0, x1, re1, im1;
-                    pair_eval<NT>(r0, an, A, x0, re0, im0);
-                    pair_eval<NT>(r1, an, A, x1, re1, im1);
+                for (; jp < npairs; ++jp) {
+                    const FacetPair r0 = R[jp];
+                    f2 x0, re0, im0;
+                    pair_eval2<NT>(r0, an, A, x0, re0, im0);
+                    const bool two = 2 * jp + 1 < cnt;      // the second facet is not padding
                     if (prisms) {
-                        const float f0 = prism_factor(r0.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
-                                                      A.PR, A.np, A.ealpha);
-                        const float f1 = prism_factor(r1.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
-                                                      A.PR, A.np, A.ealpha);
-                        re0 *= f0; im0 *= f0; re1 *= f1; im1 *= f1;
+                        const f2 dx = fld<F_DX>(r0), dy = fld<F_DY>(r0), dz = fld<F_DZ>(r0), q = fld<F_Q>(r0);
+                        const float f0 = prism_factor(make_float4(dx.x, dy.x, dz.x, q.x), mp->cx, mp->cy, mp->cz,
+                                                      an.Dx, an.Dy, an.Dz, an.T0sq, A.PR, A.np, A.ealpha);
+                        const float f1 = two ? prism_factor(make_float4(dx.y, dy.y, dz.y, q.y), mp->cx, mp->cy,
+                                                            mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq, A.PR, A.np,
+                                                            A.ealpha)
+                                             : 0.f;
+                        re0.x *= f0; im0.x *= f0; re0.y *= f1; im0.y *= f1;
                     }
-                    bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
-                    bin_add(x1, re1, im1, blo, b0, win, tid, Trow, A);
-                }
-                for (; jj < cnt; ++jj) {
-                    const FacetRec r0 = R[jj];
-                    float x0, re0, im0;
-                    pair_eval<NT>(r0, an, A, x0, re0, im0);
-                    if (prisms) {
-                        const float f0 = prism_factor(r0.a, mp->cx, mp->cy, mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq,
-                                                      A.PR, A.np, A.ealpha);
-                        re0 *= f0; im0 *= f0;
-                    }
-                    bin_add(x0, re0, im0, blo, b0, win, tid, Trow, A);
+                    bin_add(x0.x, re0.x, im0.x, blo, b0, win, tid, Trow, A);
+                    if (two) bin_add(x0.y, re0.y, im0.y, blo, b0, win, tid, Trow, A);
                 }
             }
             // flush the window into the owned trace
