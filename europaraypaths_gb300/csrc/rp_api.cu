@@ -352,6 +352,26 @@ static int build_tables(rp_scene* s) {
     return RP_OK;
 }
 
+// Whether every facet's frame (n, u, v) is orthonormal to 1e-5 (unit
+// lengths, pairwise dot products): the fast form then forms the incidence
+// angle from the tangent components alone.  The generators that build u and
+// v by cross products give such frames; frames with independently
+// normalised slope tangents do not.
+static int frames_orthonormal(const double* F, int64_t nf) {
+    const double tol = 1e-5;
+    for (int64_t i = 0; i < nf; ++i) {
+        const double n[3] = {F[3 * nf + i], F[4 * nf + i], F[5 * nf + i]};
+        const double u[3] = {F[6 * nf + i], F[7 * nf + i], F[8 * nf + i]};
+        const double v[3] = {F[9 * nf + i], F[10 * nf + i], F[11 * nf + i]};
+        auto dot = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+        if (!(std::fabs(dot(n, n) - 1.0) <= tol && std::fabs(dot(u, u) - 1.0) <= tol &&
+              std::fabs(dot(v, v) - 1.0) <= tol && std::fabs(dot(n, u)) <= tol && std::fabs(dot(n, v)) <= tol &&
+              std::fabs(dot(u, v)) <= tol))
+            return 0;
+    }
+    return 1;
+}
+
 // Morton order of facet centres (spatial locality for the fast form).
 static uint64_t spread16(uint32_t v) {
     uint64_t x = v & 0xffff;
@@ -454,6 +474,9 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
         if ((rc = upload(&s->d_sorted, sorted.data(), sizeof(double) * 12 * nf, &s->store_bytes))) return fail(rc);
     }
     if ((rc = build_tables(s))) return fail(rc);
+    s->ortho = nf > 0 ? frames_orthonormal(facets, nf) : 0;
+    if (const char* v = getenv("RP_PAIR_ORTHO")) s->ortho = s->ortho && atoi(v) != 0;   // 0: general frames
+    s->dp.ortho = s->ortho;
     if (const char* v = getenv("RP_PAIR_VARIANT")) s->pair_variant = atoi(v) == 1 ? 1 : 0;
     if (const char* v = getenv("RP_PAIR_CFG")) s->pair_cfg = std::max(0, std::min(3, atoi(v)));
     cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);

@@ -68,7 +68,7 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
            const int* __restrict__ nill, const double* __restrict__ traces, DevParams dp,
            FacetPair* __restrict__ rec, ChunkMeta* __restrict__ meta, int64_t rstride,
            int64_t mstride, float* __restrict__ sx_o, C32* __restrict__ sv_o,
-           unsigned long long* __restrict__ vmax) {
+           unsigned long long* __restrict__ vmax, double* __restrict__ org) {
     __shared__ double shd[32];
     __shared__ float shf[32];
     const int s = blockIdx.y;
@@ -91,7 +91,17 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
     double mxx = block_reduce(ok ? fx : -1e300, MaxOp(), shd);
     double mxy = block_reduce(ok ? fy : -1e300, MaxOp(), shd);
     double mxz = block_reduce(ok ? fz : -1e300, MaxOp(), shd);
-    const double cx = 0.5 * (mnx + mxx), cy = 0.5 * (mny + mxy), cz = 0.5 * (mnz + mxz);
+    // the trace origin is its first illuminated facet; the chunk centre is
+    // the origin plus the FP32 rounding of (bounding-box centre - origin), so
+    // its offset cf from the origin is exact in FP32
+    const int64_t i0 = idx[(size_t)s * nf];
+    const double ox = F[i0], oy = F[nf + i0], oz = F[2 * nf + i0];
+    const float cfx = (float)(0.5 * (mnx + mxx) - ox), cfy = (float)(0.5 * (mny + mxy) - oy),
+                cfz = (float)(0.5 * (mnz + mxz) - oz);
+    const double cx = ox + (double)cfx, cy = oy + (double)cfy, cz = oz + (double)cfz;
+    if (k == 0 && threadIdx.x == 0) {
+        org[4 * s] = ox; org[4 * s + 1] = oy; org[4 * s + 2] = oz; org[4 * s + 3] = 0.0;
+    }
     float xI = 0.f, rr = 0.f;
     float fv[RP_NFIELD];            // this facet's record fields (FacetField order)
 #pragma unroll
@@ -161,7 +171,14 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
         float ddx = (float)(fx - cx), ddy = (float)(fy - cy), ddz = (float)(fz - cz);
         rr = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
         fv[F_DX] = ddx; fv[F_DY] = ddy; fv[F_DZ] = ddz; fv[F_Q] = ddx * ddx + ddy * ddy + ddz * ddz;
-        fv[F_NX] = (float)nx; fv[F_NY] = (float)ny; fv[F_NZ] = (float)nz; fv[F_XI] = xI;
+        if (dp.ortho) {         // a.u and a.v in place of the normal (exact products, one rounding)
+            fv[F_AU] = (float)((double)ddx * (float)ux + (double)ddy * (float)uy + (double)ddz * (float)uz);
+            fv[F_AV] = (float)((double)ddx * (float)vx + (double)ddy * (float)vy + (double)ddz * (float)vz);
+            fv[F_NZ] = 0.f;
+        } else {
+            fv[F_NX] = (float)nx; fv[F_NY] = (float)ny; fv[F_NZ] = (float)nz;
+        }
+        fv[F_XI] = xI;
         fv[F_UX] = (float)ux; fv[F_UY] = (float)uy; fv[F_UZ] = (float)uz;
         fv[F_PH] = (float)(-2.0 * RP_PI * (ti - floor(ti)));
         fv[F_VX] = (float)vx; fv[F_VY] = (float)vy; fv[F_VZ] = (float)vz; fv[F_K] = (float)Kf;
@@ -202,6 +219,14 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
         m.R = R * (1.0f + 1e-6f) + 1e-4f;
         m.xmin = xmn; m.xmax = xmx;
         m.n = min(RP_CHUNK, n - k * RP_CHUNK);
+        m.cfx = cfx; m.cfy = cfy; m.cfz = cfz;
+        const double cc = (double)cfx * cfx + (double)cfy * cfy + (double)cfz * cfz;
+        m.cch = (float)cc;
+        m.ccl = (float)(cc - (double)m.cch);
+        const double kb = dp.nidx / dp.dr;
+        m.lo_off = (float)((double)xmn - kb * (double)m.R);
+        m.hi_off = (float)((double)xmx + kb * (double)m.R);
+        m.phase_ok = dp.nidx * dp.turn * (double)m.R < 40.0;    // |kt dT| <= kt R
         m.bbmin[0] = mnx; m.bbmin[1] = mny; m.bbmin[2] = mnz;
         m.bbmax[0] = mxx; m.bbmax[1] = mxy; m.bbmax[2] = mxz;
         meta[(size_t)s * mstride + k] = m;
@@ -344,7 +369,7 @@ __global__ void k_tsetup32(const double* __restrict__ TG, int64_t nt, const int*
 // Single-batch pair kernel: the batch's constants live in the parameter
 // bank.  Persistent: blocks take (trace, target block, part) items from a
 // work counter until all are done.
-template <int NT, int ILP, int MINB>
+template <int NT, int ILP, int MINB, bool ORTHO>
 __global__ void __launch_bounds__(RP_PAIR_THREADS, MINB)
 k_pairs32(const __grid_constant__ PairArgs A) {
     RP_PAIR_SMEM_DECL
@@ -358,7 +383,7 @@ k_pairs32(const __grid_constant__ PairArgs A) {
         const int part = item % RP_PARTS;
         const int tb = (item / RP_PARTS) % A.tblocks;
         const int s = item / (RP_PARTS * A.tblocks);
-        pair_item<NT, ILP>(A, s, tb, part, bars, phase);
+        pair_item<NT, ILP, ORTHO>(A, s, tb, part, bars, phase);
     }
     RP_PAIR_SMEM_END
 }
@@ -698,6 +723,7 @@ void fast_take_setup(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<int>((size_t)L.nb * nf);                // idx
     a.template take<FacetPair>((size_t)L.nb * L.rstride / 2);    // records (facet pairs)
     a.template take<ChunkMeta>((size_t)L.nb * L.mstride);   // chunk meta
+    a.template take<double>((size_t)L.nb * 4);              // trace origins
     a.template take<float>((size_t)L.nb * nf);              // surface x
     a.template take<C32>((size_t)L.nb * nf);                // surface v
     a.template take<TraceMeta>(L.nb);
@@ -764,22 +790,30 @@ const size_t kFastBudget = (size_t)32 << 30;
 // Pair-kernel instantiation: sinc degree x (ILP facets per step, resident
 // blocks per SM).  cfg 0: 2 x 3, 1: 2 x 2, 2: 1 x 4, 3: 1 x 3.
 template <int NT>
-void (*pick_cfg(int cfg))(const PairArgs) {
+void (*pick_cfg(int cfg, bool ortho))(const PairArgs) {
+    if (ortho) {
+        switch (cfg) {
+            case 1: return k_pairs32<NT, 2, 2, true>;
+            case 2: return k_pairs32<NT, 1, 4, true>;
+            case 3: return k_pairs32<NT, 1, 3, true>;
+            default: return k_pairs32<NT, 2, 3, true>;
+        }
+    }
     switch (cfg) {
-        case 1: return k_pairs32<NT, 2, 2>;
-        case 2: return k_pairs32<NT, 1, 4>;
-        case 3: return k_pairs32<NT, 1, 3>;
-        default: return k_pairs32<NT, 2, 3>;
+        case 1: return k_pairs32<NT, 2, 2, false>;
+        case 2: return k_pairs32<NT, 1, 4, false>;
+        case 3: return k_pairs32<NT, 1, 3, false>;
+        default: return k_pairs32<NT, 2, 3, false>;
     }
 }
 
-void (*pick_pair_kernel(int deg, int cfg))(const PairArgs) {
+void (*pick_pair_kernel(int deg, int cfg, bool ortho))(const PairArgs) {
     switch (deg) {
-        case 3: return pick_cfg<3>(cfg);
-        case 4: return pick_cfg<4>(cfg);
-        case 5: return pick_cfg<5>(cfg);
-        case 6: return pick_cfg<6>(cfg);
-        default: return pick_cfg<0>(cfg);
+        case 3: return pick_cfg<3>(cfg, ortho);
+        case 4: return pick_cfg<4>(cfg, ortho);
+        case 5: return pick_cfg<5>(cfg, ortho);
+        case 6: return pick_cfg<6>(cfg, ortho);
+        default: return pick_cfg<0>(cfg, ortho);
     }
 }
 
@@ -910,7 +944,7 @@ struct Seg {
     FastLayout Lw, L;
     // setup stage
     uint8_t* fflags; int* tcnt; int* nill; int* ntl; unsigned long long* vmax; unsigned long long* dmin;
-    int* idx; FacetPair* rec; ChunkMeta* meta; float* sxv; C32* sv; TraceMeta* tm; uint8_t* tflags;
+    double* org; int* idx; FacetPair* rec; ChunkMeta* meta; float* sxv; C32* sv; TraceMeta* tm; uint8_t* tflags;
     int* tlist; int* bt0; int* misc; long long* acc; C32* refl; C32* sscr;
     // pair stage
     int Wt = 1;
@@ -964,6 +998,7 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
     g.idx = a.take<int>((size_t)nb * nfa);
     g.rec = a.take<FacetPair>((size_t)nb * Lw.rstride / 2);
     g.meta = a.take<ChunkMeta>((size_t)nb * Lw.mstride);
+    g.org = a.take<double>((size_t)nb * 4);
     g.sxv = a.take<float>((size_t)nb * nfa);
     g.sv = a.take<C32>((size_t)nb * nfa);
     g.tm = a.take<TraceMeta>(nb);
@@ -985,7 +1020,8 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
         RP_LAUNCHED();
         compact_flags(g.fflags, nf, nb, g.tcnt, g.nill, g.idx, nfa, true, st);
         k_facets32<<<dim3((unsigned)Lw.mstride, nb), RP_CHUNK, 0, st>>>(
-            sc->d_sorted, nfa, g.idx, g.nill, trb, dp, g.rec, g.meta, Lw.rstride, Lw.mstride, g.sxv, g.sv, g.vmax);
+            sc->d_sorted, nfa, g.idx, g.nill, trb, dp, g.rec, g.meta, Lw.rstride, Lw.mstride, g.sxv, g.sv, g.vmax,
+            g.org);
         RP_LAUNCHED();
         k_surf_fix32<<<dim3((unsigned)((nf + 256 * RP_SFIX_PER - 1) / (256 * RP_SFIX_PER)), nb), 256, 0, st>>>(
             nfa, g.nill, g.sxv, g.sv, g.vmax, nr, g.acc);
@@ -1015,7 +1051,7 @@ PairArgs seg_pair_args(const Seg& g) {
     const DevParams& dp = sc->dp;
     const int nr = sc->nr;
     PairArgs P;
-    P.rec = g.rec; P.meta = g.meta; P.rstride = g.Lw.rstride; P.mstride = g.Lw.mstride;
+    P.rec = g.rec; P.meta = g.meta; P.org = g.org; P.rstride = g.Lw.rstride; P.mstride = g.Lw.mstride;
     P.nill = g.nill; P.ntl = g.ntl; P.tlist = g.tlist; P.tstride = g.L.tstride;
     P.TG = sc->d_targets; P.nt = sc->nt; P.PR = sc->d_prisms; P.np = sc->np;
     P.bt0 = g.bt0; P.T = g.T; P.Wt = g.Wt; P.nb = g.nb;
@@ -1033,7 +1069,9 @@ PairArgs seg_pair_args(const Seg& g) {
     for (int k = 0; k < 8; ++k) P.sc[k] = (float)(g.coef[k] * std::pow(pik_d * pik_d, k));
     P.ealpha = dp.lossless ? 0.f : (float)(-2.0 * dp.alpha2 * 1.4426950408889634);
     P.eks = dp.lossless ? 0.f : (float)(-2.0 * dp.ks * dp.ks * 1.4426950408889634);
-    P.nidx = dp.nidx; P.inv_dr = 1.0 / dp.dr; P.inv_lam = dp.turn;
+    const double ktd = dp.nidx * dp.turn, kbd = dp.nidx / dp.dr;
+    P.kth = (float)ktd; P.ktl = (float)(ktd - (double)P.kth);
+    P.kbh = (float)kbd; P.kbl = (float)(kbd - (double)P.kbh);
     P.lossless = dp.lossless;
     return P;
 }
@@ -1061,7 +1099,7 @@ int launch_pairs(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsig
         const Seg& g = *ps[0];
         PairArgs P = seg_pair_args(g);
         P.work = d_work;
-        void (*pk)(const PairArgs) = pick_pair_kernel(g.deg, cfg);
+        void (*pk)(const PairArgs) = pick_pair_kernel(g.deg, cfg, g.sc->ortho != 0);
         RP_CUDA(cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem));
         int occ = 0;
         RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, RP_PAIR_THREADS, pair_smem));
@@ -1195,7 +1233,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     std::vector<PairJob> hp;
     std::vector<unsigned int> hps(1, 0u);
     for (Seg* g : ps) {
-        hp.push_back(PairJob{seg_pair_args(*g), g->deg});
+        hp.push_back(PairJob{seg_pair_args(*g), g->deg, g->sc->ortho});
         hps.push_back(hps.back() + (unsigned)(g->nb * hp.back().a.tblocks * RP_PARTS));
     }
     std::vector<ConvArgs> hc[3];

@@ -36,6 +36,7 @@ struct DevParams {
     double turn;   // phase turns per metre of range: pi_F / (pi lam), so that
                    // exp(-j (2 pi_F / lam) r) = exp(-j 2 pi r turn) (radar_kernels.cu:682)
     int nr, lossless, disable_surface, rerad_funct;
+    int ortho;           // facet frames orthonormal: records carry a.u, a.v instead of n
     int specular;        // specular mode (geometry_kernels.cu:434-446, 527-537, 563-570)
     int cmode;           // 0 linear convolution, 1 circular, 2 none (sim.cu:733-986)
     double c_over_c2;    // c / c_2 of refrRadarSignal's range (radar_kernels.cu:245)
@@ -122,6 +123,7 @@ struct rp_scene {
     float* d_C2S = nullptr;              // DIF_2nr(target chirp)
     float* d_HS = nullptr;               // DIF_M(crop kernel h) / M
     // ---- tuning
+    int ortho = 0;                       // every facet frame (n, u, v) orthonormal to 1e-5
     int pair_variant = 0;                // 0 auto (polynomial sinc where accurate), 1 special-function sinc
     int pair_cfg = 1;                    // pair-kernel (ILP, blocks/SM) configuration (1: 2 x 2)
     // ---- the scene's own workspace (rp_simulate / rp_simulate_device)

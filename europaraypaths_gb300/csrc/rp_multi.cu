@@ -11,7 +11,7 @@ namespace rpk {
 // Multi-job pair kernel: one persistent launch over the items of many
 // batches (scenes of different sizes, bin counts and sinc degrees).  Job j
 // owns items [start[j], start[j + 1]); a block copies the job's constants
-// into registers and dispatches on its sinc degree.
+// into registers and dispatches on its sinc degree and facet-frame kind.
 template <int ILP, int MINB>
 __global__ void __launch_bounds__(RP_PAIR_THREADS, MINB)
 k_pairs32m(const PairJob* __restrict__ jobs, const unsigned int* __restrict__ start, int njobs,
@@ -37,16 +37,27 @@ k_pairs32m(const PairJob* __restrict__ jobs, const unsigned int* __restrict__ st
         if (item >= total) break;
         const PairArgs A = jobs[j].a;
         const int deg = jobs[j].deg;
+        const int ortho = jobs[j].ortho;
         const unsigned int li = item - start[j];
         const int part = li % RP_PARTS;
         const int tb = (li / RP_PARTS) % A.tblocks;
         const int s = li / (RP_PARTS * A.tblocks);
-        switch (deg) {
-            case 3: pair_item<3, ILP>(A, s, tb, part, bars, phase); break;
-            case 4: pair_item<4, ILP>(A, s, tb, part, bars, phase); break;
-            case 5: pair_item<5, ILP>(A, s, tb, part, bars, phase); break;
-            case 6: pair_item<6, ILP>(A, s, tb, part, bars, phase); break;
-            default: pair_item<0, ILP>(A, s, tb, part, bars, phase); break;
+        if (ortho) {
+            switch (deg) {
+                case 3: pair_item<3, ILP, true>(A, s, tb, part, bars, phase); break;
+                case 4: pair_item<4, ILP, true>(A, s, tb, part, bars, phase); break;
+                case 5: pair_item<5, ILP, true>(A, s, tb, part, bars, phase); break;
+                case 6: pair_item<6, ILP, true>(A, s, tb, part, bars, phase); break;
+                default: pair_item<0, ILP, true>(A, s, tb, part, bars, phase); break;
+            }
+        } else {
+            switch (deg) {
+                case 3: pair_item<3, ILP, false>(A, s, tb, part, bars, phase); break;
+                case 4: pair_item<4, ILP, false>(A, s, tb, part, bars, phase); break;
+                case 5: pair_item<5, ILP, false>(A, s, tb, part, bars, phase); break;
+                case 6: pair_item<6, ILP, false>(A, s, tb, part, bars, phase); break;
+                default: pair_item<0, ILP, false>(A, s, tb, part, bars, phase); break;
+            }
         }
     }
     RP_PAIR_SMEM_END

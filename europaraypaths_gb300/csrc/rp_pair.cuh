@@ -32,12 +32,17 @@ using C32 = Cx<float>;
 // field of both facets in adjacent registers, the operand of one packed
 // two-lane FP32 instruction.  A chunk with an odd count ends with a pair
 // whose second facet repeats the first with K = 0 (it adds exact zeros).
+// In a scene whose facet frames (n, u, v) are all orthonormal the normal is
+// not needed (sin^2 of the incidence angle comes from the tangent
+// components) and fields 4 and 5 hold a.u and a.v instead (a = facet -
+// chunk centre), field 6 is unused.
 enum FacetField {
     F_DX, F_DY, F_DZ, F_Q,      // facet - chunk centre, |facet - chunk centre|^2
     F_NX, F_NY, F_NZ, F_XI,     // normal, xI = (Itd - rst) / dr
     F_UX, F_UY, F_UZ, F_PH,     // u tangent, -2 pi frac(Itd / lam) (radians)
     F_VX, F_VY, F_VZ, F_K,      // v tangent, K = hoisted amplitude factor
-    RP_NFIELD
+    RP_NFIELD,
+    F_AU = F_NX, F_AV = F_NY    // orthonormal-frame records
 };
 struct __align__(16) FacetPair {
     float4 v[RP_NFIELD / 2];
@@ -59,11 +64,18 @@ __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return __ffma2_rn(a, b, c
 __device__ __forceinline__ f2 mul2(f2 a, f2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ f2 add2(f2 a, f2 b) { return __fadd2_rn(a, b); }
 
+// Per chunk: its centre is the trace origin plus cf, exactly (cf is rounded
+// to FP32 first and the centre defined from it), so the pair kernel forms
+// the anchor distances in double-float FP32 arithmetic without error from cf.
 struct __align__(16) ChunkMeta {
-    double cx, cy, cz;     // chunk centre
+    float cfx, cfy, cfz;   // chunk centre - trace origin (exact)
+    float cch, ccl;        // |cf|^2 as a double-float (high, low)
+    float lo_off, hi_off;  // xmin - kb R, xmax + kb R: bin bounds relative to n T0 / dr
+    int n;                 // facets in the chunk
     float R;               // max |facet - centre|
     float xmin, xmax;      // range of (Itd - rst)/dr
-    int n;                 // facets in the chunk
+    int phase_ok;          // kt R < 40: the pairs' phase stays within +-42 turns
+    double cx, cy, cz;     // chunk centre (FP64: origin + cf)
     double bbmin[3], bbmax[3];
 };
 
@@ -108,6 +120,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
 struct PairArgs {
     const FacetPair* rec;   // [nb][rstride / 2] facet pairs
     const ChunkMeta* meta;
+    const double* org;      // [nb][4] trace origins (FP64)
     int64_t rstride, mstride;
     const int* nill;
     const int* ntl;
@@ -136,7 +149,8 @@ struct PairArgs {
     float sc[8];        // sinc polynomial in t' = a^2 / pik^2 (sinc_poly, scaled)
     float ealpha;       // -2 alpha2 log2(e)
     float eks;          // -2 ks^2 log2(e)
-    double nidx, inv_dr, inv_lam;   // inv_lam: turns per metre, pi_F / (pi lam)
+    float kth, ktl;     // n / lam (turns per metre) as a double-float
+    float kbh, kbl;     // n / dr (bins per metre) as a double-float
     int lossless;
 };
 
@@ -145,6 +159,7 @@ struct PairArgs {
 struct PairJob {
     PairArgs a;
     int deg;
+    int ortho;      // the batch's scene has orthonormal facet frames
 };
 
 // Per-(chunk, target) anchors of the split-precision evaluation.
@@ -154,7 +169,8 @@ struct Anchor {
     float ph0;            // -2 pi frac(n T0 / lam): phase of the anchor (radians)
     float xbase;          // n T0 / dr - blo (bins, relative to the window start)
     float tnx, tny, tnz;  // target normal
-    float eaT0;           // ealpha T0: the attenuation exponent at the anchor
+    float nDtn;           // -(target - chunk centre).(target normal)
+    float eaT0;           // ealpha T0 (+ eks with orthonormal frames): attenuation exponent at the anchor
 };
 
 // Hardware approximations (PTX rsqrt/rcp/ex2 .approx.ftz): single
@@ -217,33 +233,51 @@ __device__ __forceinline__ void sinc_sfu(float u, float& num, float& den) {
 // RED: reduce the phase to [-pi, pi] before the special-function sine and
 // cosine; the fast path skips it when the chunk keeps |phase| below 84 pi
 // (sin/cos.approx hold their accuracy over +-100 pi radians).
-template <int NT, bool RED = true>
+template <int NT, bool ORTHO, bool RED = true>
 __device__ __forceinline__ void pair_eval2(const FacetPair& r, const Anchor& an, const PairArgs& A, f2& xr,
                                            f2& vre, f2& vim) {
     const f2 ONE = bc(1.f), M1 = bc(-1.f);
     const f2 dx = fld<F_DX>(r), dy = fld<F_DY>(r), dz = fld<F_DZ>(r);
-    const f2 Dx = bc(an.Dx), Dy = bc(an.Dy), Dz = bc(an.Dz);
-    const f2 dd = fma2(Dx, dx, fma2(Dy, dy, mul2(Dz, dz)));
-    const f2 qd = fma2(bc(-2.f), dd, fld<F_Q>(r));              // Ttd^2 - T0^2
+    const f2 nDx = bc(-an.Dx), nDy = bc(-an.Dy), nDz = bc(-an.Dz);
+    const f2 ndd = fma2(nDx, dx, fma2(nDy, dy, mul2(nDz, dz)));  // -D.a
+    const f2 qd = fma2(bc(2.f), ndd, fld<F_Q>(r));               // Ttd^2 - T0^2
     const f2 d2 = add2(bc(an.T0sq), qd);
     const f2 rinv = make_float2(rsqrt_a(d2.x), rsqrt_a(d2.y));
     const f2 sT = fma2(d2, rinv, bc(an.T0));                     // Ttd + T0
     const f2 dT = mul2(qd, make_float2(rcp_a(sT.x), rcp_a(sT.y)));   // Ttd - T0 without cancellation
-    // e = facet - target; only squares of its dot products enter
-    const f2 ex = fma2(Dx, M1, dx), ey = fma2(Dy, M1, dy), ez = fma2(Dz, M1, dz);
-    const f2 pb = fma2(ex, fld<F_NX>(r), fma2(ey, fld<F_NY>(r), mul2(ez, fld<F_NZ>(r))));
-    const f2 pt = fma2(ex, bc(an.tnx), fma2(ey, bc(an.tny), mul2(ez, bc(an.tnz))));
-    const f2 pc = fma2(ex, fld<F_UX>(r), fma2(ey, fld<F_UY>(r), mul2(ez, fld<F_UZ>(r))));
-    const f2 pd = fma2(ex, fld<F_VX>(r), fma2(ey, fld<F_VY>(r), mul2(ez, fld<F_VZ>(r))));
-    const f2 inv_d2 = mul2(rinv, rinv);
-    const f2 cT2 = mul2(mul2(pb, pb), inv_d2);
-    const f2 aT = fma2(cT2, M1, ONE);
-    const f2 aD = fma2(mul2(mul2(pt, pt), inv_d2), M1, ONE);
-    const f2 X = fma2(pd, pd, bc(1e-30f));
-    const f2 h2 = fma2(pc, pc, X);
-    const f2 xs = mul2(X, make_float2(rcp_a(h2.x), rcp_a(h2.y)));
-    const f2 t1 = mul2(aT, xs), t3 = mul2(aD, xs);
-    const f2 t2 = fma2(t1, M1, aT), t4 = fma2(t3, M1, aD);
+    // t1..t4: the four squared sinc arguments over pik^2; aT = sin^2(Tth)
+    f2 aT, t1, t2, t3, t4;
+    if (ORTHO) {
+        // e = a - D: e.u = a.u - D.u etc. (a.u, a.v from the record), and
+        // sin^2(Tth) cos^2(Tph) = (e.v)^2 / d2, sin^2(Tth) sin^2(Tph) =
+        // (e.u)^2 / d2 because n, u, v are orthonormal
+        const f2 pc = fma2(nDx, fld<F_UX>(r), fma2(nDy, fld<F_UY>(r), fma2(nDz, fld<F_UZ>(r), fld<F_AU>(r))));
+        const f2 pd = fma2(nDx, fld<F_VX>(r), fma2(nDy, fld<F_VY>(r), fma2(nDz, fld<F_VZ>(r), fld<F_AV>(r))));
+        const f2 pt = fma2(dx, bc(an.tnx), fma2(dy, bc(an.tny), fma2(dz, bc(an.tnz), bc(an.nDtn))));
+        const f2 pcr = mul2(pc, rinv), pdr = mul2(pd, rinv), ptr = mul2(pt, rinv);
+        t1 = fma2(pdr, pdr, bc(1e-30f));
+        t2 = mul2(pcr, pcr);
+        aT = add2(t1, t2);
+        const f2 xs = mul2(t1, make_float2(rcp_a(aT.x), rcp_a(aT.y)));
+        const f2 aD = fma2(mul2(ptr, ptr), M1, ONE);
+        t3 = mul2(aD, xs);
+        t4 = fma2(t3, M1, aD);
+    } else {
+        // e = facet - target; only squares of its dot products enter
+        const f2 ex = fma2(nDx, ONE, dx), ey = fma2(nDy, ONE, dy), ez = fma2(nDz, ONE, dz);
+        const f2 pb = fma2(ex, fld<F_NX>(r), fma2(ey, fld<F_NY>(r), mul2(ez, fld<F_NZ>(r))));
+        const f2 pt = fma2(ex, bc(an.tnx), fma2(ey, bc(an.tny), mul2(ez, bc(an.tnz))));
+        const f2 pc = fma2(ex, fld<F_UX>(r), fma2(ey, fld<F_UY>(r), mul2(ez, fld<F_UZ>(r))));
+        const f2 pd = fma2(ex, fld<F_VX>(r), fma2(ey, fld<F_VY>(r), mul2(ez, fld<F_VZ>(r))));
+        const f2 inv_d2 = mul2(rinv, rinv);
+        aT = fma2(mul2(mul2(pb, pb), inv_d2), M1, ONE);
+        const f2 aD = fma2(mul2(mul2(pt, pt), inv_d2), M1, ONE);
+        const f2 X = fma2(pd, pd, bc(1e-30f));
+        const f2 h2 = fma2(pc, pc, X);
+        const f2 xs = mul2(X, make_float2(rcp_a(h2.x), rcp_a(h2.y)));
+        t1 = mul2(aT, xs); t3 = mul2(aD, xs);
+        t2 = fma2(t1, M1, aT); t4 = fma2(t3, M1, aD);
+    }
     f2 S;
     if (NT > 0) {
         constexpr int D = NT > 0 ? NT : 1;
@@ -259,8 +293,9 @@ __device__ __forceinline__ void pair_eval2(const FacetPair& r, const Anchor& an,
         S = make_float2(fabsf(__fdividef(n0, e0)), fabsf(__fdividef(n1, e1)));
     }
     // attenuation and roughness (zero constants when lossless); ealpha Ttd
-    // = ealpha T0 + ealpha (Ttd - T0)
-    const f2 e2 = fma2(bc(A.eks), cT2, fma2(bc(A.ealpha), dT, bc(an.eaT0)));
+    // = ealpha T0 + ealpha (Ttd - T0), eks cos^2(Tth) = eks - eks sin^2(Tth)
+    // (the eks term is part of the anchor's eaT0)
+    const f2 e2 = fma2(bc(-A.eks), aT, fma2(bc(A.ealpha), dT, bc(an.eaT0)));
     const f2 amp = mul2(mul2(fld<F_K>(r), S), mul2(rinv, make_float2(ex2_a(e2.x), ex2_a(e2.y))));
     f2 ph = fma2(bc(A.kr), dT, add2(fld<F_PH>(r), bc(an.ph0)));
     if (RED) {
@@ -418,19 +453,85 @@ __device__ __forceinline__ void bin_add_fast2(f2 xr, f2 vre, f2 vim, float2* win
     }
 }
 
+// ------------------------------------------------ double-float anchors --
+// Error-free transformations (Knuth TwoSum, FMA TwoProduct); the _rn
+// intrinsics keep the compiler from contracting or reordering them.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fadd_rn(s, -a);
+    e = __fadd_rn(__fadd_rn(a, -__fadd_rn(s, -bb)), __fadd_rn(b, -bb));
+}
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+    p = __fmul_rn(a, b);
+    e = __fmaf_rn(a, b, -p);
+}
+
+// T0 = |t' - cf| for t' = th + tl (double-float) and an exact FP32 cf, from
+// T0^2 = |t'|^2 - 2 t'.cf + |cf|^2 carried as double-floats and one Newton
+// correction of the FP32 square root: Th + Tl to ~1e-13 relative; Qh = T0^2
+// rounded to FP32.
+__device__ __forceinline__ void anchor_distance(float4 th, float4 tl, float cfx, float cfy, float cfz,
+                                                float cch, float ccl, float& Th, float& Tl, float& Qh) {
+    float px, ex, py, ey, pz, ez;
+    two_prod(th.x, cfx, px, ex);
+    two_prod(th.y, cfy, py, ey);
+    two_prod(th.z, cfz, pz, ez);
+    float s1, r1, s2, r2;
+    two_sum(px, py, s1, r1);
+    two_sum(s1, pz, s2, r2);
+    const float dl = __fadd_rn(__fadd_rn(__fadd_rn(ex, ey), __fadd_rn(ez, r1)),
+                               __fadd_rn(r2, __fmaf_rn(tl.x, cfx, __fmaf_rn(tl.y, cfy, __fmul_rn(tl.z, cfz)))));
+    // Q = |t'|^2 - 2 (s2 + dl) + |cf|^2
+    float a1, r3, a2, r4;
+    two_sum(th.w, __fmul_rn(-2.f, s2), a1, r3);
+    two_sum(a1, cch, a2, r4);
+    const float ql = __fadd_rn(__fadd_rn(__fmaf_rn(-2.f, dl, tl.w), ccl), __fadd_rn(r3, r4));
+    Qh = __fadd_rn(a2, ql);
+    const float Ql = __fadd_rn(ql, -__fadd_rn(Qh, -a2));
+    // sqrt: s = Qh rsqrt(Qh), then T0 = s + (Q - s^2) / (2 s)
+    const float y = rsqrt_a(Qh);
+    const float sq = __fmul_rn(Qh, y);
+    float ss, sse;
+    two_prod(sq, sq, ss, sse);
+    const float res = __fadd_rn(__fadd_rn(__fadd_rn(Qh, -ss), -sse), Ql);
+    const float corr = __fmul_rn(res, __fmul_rn(0.5f, y));
+    Th = __fadd_rn(sq, corr);
+    Tl = __fadd_rn(corr, -__fadd_rn(Th, -sq));
+}
+
+// frac((Th + Tl) (kh + kl)) in about [-1/2, 1/2]: the high product exactly
+// (its integer part removed exactly), plus the low terms.
+__device__ __forceinline__ float frac_dd(float Th, float Tl, float kh, float kl) {
+    float p, e;
+    two_prod(Th, kh, p, e);
+    const float lo = __fadd_rn(e, __fmaf_rn(Th, kl, __fmul_rn(Tl, kh)));
+    return __fadd_rn(__fadd_rn(p, -rintf(p)), lo);
+}
+
+// (Th + Tl) (kh + kl) = xi + xf with xi = floor of the high product.
+__device__ __forceinline__ int floor_dd(float Th, float Tl, float kh, float kl, float& xf) {
+    float p, e;
+    two_prod(Th, kh, p, e);
+    const float lo = __fadd_rn(e, __fmaf_rn(Th, kl, __fmul_rn(Tl, kh)));
+    const float fl = floorf(p);
+    xf = __fadd_rn(__fadd_rn(p, -fl), lo);
+    return (int)fl;
+}
+
 // Dynamic shared memory of the pair kernels: two record buffers, the
-// per-thread bin windows, the threads' FP64 target positions.
+// per-thread bin windows, the threads' target positions relative to the
+// trace origin as double-floats.
 extern __shared__ __align__(128) unsigned char pair_smem[];
 #define RP_PAIR_WIN_OFF (2 * RP_CHUNK_PAIRS * sizeof(FacetPair))
 #define RP_PAIR_TPOS_OFF (RP_PAIR_WIN_OFF + (size_t)RP_WIN * RP_PAIR_THREADS * sizeof(float2))
-#define RP_PAIR_SMEM_BYTES (RP_PAIR_TPOS_OFF + 3 * RP_PAIR_THREADS * sizeof(double))
+#define RP_PAIR_SMEM_BYTES (RP_PAIR_TPOS_OFF + 2 * RP_PAIR_THREADS * sizeof(float4))
 
-template <int NT, int ILP, class PA>
+template <int NT, int ILP, bool ORTHO, class PA>
 __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, uint64_t* bars, uint32_t* phase) {
     // every hot shared array is derived here from the shared symbol itself
     FacetPair* srec = reinterpret_cast<FacetPair*>(pair_smem);                     // [2][RP_CHUNK_PAIRS]
     float2* win = reinterpret_cast<float2*>(pair_smem + RP_PAIR_WIN_OFF);          // [RP_WIN][threads]
-    double* s_tpos = reinterpret_cast<double*>(pair_smem + RP_PAIR_TPOS_OFF);      // [3][threads]
+    float4* s_tq = reinterpret_cast<float4*>(pair_smem + RP_PAIR_TPOS_OFF);        // [2][threads]
     const int tid = threadIdx.x;
     const int nq = A.ntl[s];
     const int n = A.nill[s];
@@ -446,9 +547,15 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
     C32* Trow = nullptr;
     if (active) {
         const int64_t ti = A.tlist[(size_t)s * A.tstride + q];
-        s_tpos[tid] = A.TG[ti];
-        s_tpos[RP_PAIR_THREADS + tid] = A.TG[A.nt + ti];
-        s_tpos[2 * RP_PAIR_THREADS + tid] = A.TG[2 * A.nt + ti];
+        // t' = target - trace origin and |t'|^2 (FP64, once per item), kept
+        // as double-floats: high parts in s_tq[0], low parts in s_tq[1]
+        const double px = A.TG[ti] - A.org[4 * s], py = A.TG[A.nt + ti] - A.org[4 * s + 1],
+                     pz = A.TG[2 * A.nt + ti] - A.org[4 * s + 2];
+        const double p2 = px * px + py * py + pz * pz;
+        const float hx = (float)px, hy = (float)py, hz = (float)pz, h2 = (float)p2;
+        s_tq[tid] = make_float4(hx, hy, hz, h2);
+        s_tq[RP_PAIR_THREADS + tid] = make_float4((float)(px - hx), (float)(py - hy), (float)(pz - hz),
+                                                  (float)(p2 - h2));
         tnx = (float)A.TG[3 * A.nt + ti]; tny = (float)A.TG[4 * A.nt + ti];
         tnz = (float)A.TG[5 * A.nt + ti];
         b0 = A.bt0[(size_t)s * A.tstride + q];
@@ -483,27 +590,33 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         int blo = 0;
         bool fits = true;
         if (active) {
-            // FP64 anchors of this (chunk, target)
-            const double mcx = mp->cx, mcy = mp->cy, mcz = mp->cz;
-            const double Dx = s_tpos[tid] - mcx, Dy = s_tpos[RP_PAIR_THREADS + tid] - mcy,
-                         Dz = s_tpos[2 * RP_PAIR_THREADS + tid] - mcz;
-            const double T0 = sqrt(Dx * Dx + Dy * Dy + Dz * Dz);
-            const double xt = A.nidx * T0 * A.inv_dr;
-            const double tt = A.nidx * T0 * A.inv_lam;      // turns
-            const double lo = (double)mp->xmin + A.nidx * (T0 - (double)mp->R) * A.inv_dr;
-            const double hi = (double)mp->xmax + A.nidx * (T0 + (double)mp->R) * A.inv_dr;
-            blo = (int)floor(lo) - 1;
-            // every pair's bin x lies in [lo, hi] (triangle inequality on the
-            // chunk's bounding radius); with half a bin of margin for FP32
-            // rounding, both split bins stay inside the window and the trace
-            fits = blo >= 0 && blo + RP_WIN <= A.nr1 && hi + 0.5 < (double)(blo + RP_WIN - 1) &&
-                   (double)A.kt * (double)mp->R < 40.0;     // |kt dT| <= kt R: the phase bound
-            an.Dx = (float)Dx; an.Dy = (float)Dy; an.Dz = (float)Dz;
-            an.T0 = (float)T0; an.T0sq = (float)(T0 * T0);
-            an.ph0 = (float)(-2.0 * 3.14159265358979323846 * (tt - floor(tt)));
-            an.xbase = (float)(xt - (double)blo);
+            // anchors of this (chunk, target) in double-float FP32
+            const float4 th = s_tq[tid], tl = s_tq[RP_PAIR_THREADS + tid];
+            const float cfx = mp->cfx, cfy = mp->cfy, cfz = mp->cfz;
+            float Th, Tl, Qh;
+            anchor_distance(th, tl, cfx, cfy, cfz, mp->cch, mp->ccl, Th, Tl, Qh);
+            // n T0 / lam (turns) -> phase; n T0 / dr (bins) -> integer and fraction
+            const float fr = frac_dd(Th, Tl, A.kth, A.ktl);
+            float xf;
+            const int xi = floor_dd(Th, Tl, A.kbh, A.kbl, xf);
+            const float lo = xf + mp->lo_off, hi = xf + mp->hi_off;
+            const int blo_rel = floor_i(lo) - 1;
+            blo = xi + blo_rel;
+            // every pair's bin x lies in [lo, hi] (relative to xi; triangle
+            // inequality on the chunk's bounding radius); with half a bin of
+            // margin for FP32 rounding both split bins stay inside the window
+            // and the trace
+            fits = blo >= 0 && blo + RP_WIN <= A.nr1 && hi + 0.5f < (float)(blo_rel + RP_WIN - 1) &&
+                   mp->phase_ok;
+            an.Dx = __fadd_rn(__fadd_rn(th.x, -cfx), tl.x);
+            an.Dy = __fadd_rn(__fadd_rn(th.y, -cfy), tl.y);
+            an.Dz = __fadd_rn(__fadd_rn(th.z, -cfz), tl.z);
+            an.T0 = Th; an.T0sq = Qh;
+            an.ph0 = -6.28318530717958647f * fr;
+            an.xbase = xf - (float)blo_rel;
             an.tnx = tnx; an.tny = tny; an.tnz = tnz;
-            an.eaT0 = (float)((double)A.ealpha * T0);
+            an.nDtn = -fmaf(an.Dx, tnx, fmaf(an.Dy, tny, an.Dz * tnz));
+            an.eaT0 = fmaf(A.ealpha, Th, A.eks);
         }
         const bool all_fit = __all_sync(0xffffffffu, fits);
         if (active) {
@@ -518,22 +631,22 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
                     const FacetPair r0 = R[jp];
                     const FacetPair r1 = R[jp + 1];
                     f2 x0, re0, im0, x1, re1, im1;
-                    pair_eval2<NT, false>(r0, an, A, x0, re0, im0);
-                    pair_eval2<NT, false>(r1, an, A, x1, re1, im1);
+                    pair_eval2<NT, ORTHO, false>(r0, an, A, x0, re0, im0);
+                    pair_eval2<NT, ORTHO, false>(r1, an, A, x1, re1, im1);
                     bin_add_fast2(x0, re0, im0, win, tid);
                     bin_add_fast2(x1, re1, im1, win, tid);
                 }
                 for (; jp < npairs; ++jp) {
                     const FacetPair r0 = R[jp];
                     f2 x0, re0, im0;
-                    pair_eval2<NT, false>(r0, an, A, x0, re0, im0);
+                    pair_eval2<NT, ORTHO, false>(r0, an, A, x0, re0, im0);
                     bin_add_fast2(x0, re0, im0, win, tid);
                 }
             } else {
                 for (; jp < npairs; ++jp) {
                     const FacetPair r0 = R[jp];
                     f2 x0, re0, im0;
-                    pair_eval2<NT>(r0, an, A, x0, re0, im0);
+                    pair_eval2<NT, ORTHO>(r0, an, A, x0, re0, im0);
                     const bool two = 2 * jp + 1 < cnt;      // the second facet is not padding
                     if (prisms) {
                         const f2 dx = fld<F_DX>(r0), dy = fld<F_DY>(r0), dz = fld<F_DZ>(r0), q = fld<F_Q>(r0);

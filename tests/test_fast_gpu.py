@@ -115,3 +115,39 @@ def test_fast_vhf_band(built_lib, oracle, nr):
     assert got.shape[1] == nr
     assert np.array_equal(cnt, rcnt)
     check(got, ref)
+
+
+def _slope_frames(facets):
+    # tangents along the grid axes normalised independently, u ~ (1, 0,
+    # dz/dx) and v ~ (0, 1, dz/dy): not orthogonal on sloped facets
+    f = facets.copy()
+    dzdx, dzdy = -f[3] / f[5], -f[4] / f[5]
+    u = np.stack([np.ones_like(dzdx), np.zeros_like(dzdx), dzdx])
+    v = np.stack([np.zeros_like(dzdy), np.ones_like(dzdy), dzdy])
+    f[6:9] = u / np.linalg.norm(u, axis=0)
+    f[9:12] = v / np.linalg.norm(v, axis=0)
+    return f
+
+
+def test_fast_non_orthonormal_frames(built_lib, oracle):
+    # a rough surface whose facet frames are not orthonormal takes the
+    # general directivity (the facet normal from the record)
+    sc = _vhf_scene(2048, n_side=80)
+    sc["facets"] = _slope_frames(sc["facets"])
+    uv = np.abs(np.einsum("ij,ij->j", sc["facets"][6:9], sc["facets"][9:12]))
+    assert uv.max() > 1e-3
+    got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle)
+    assert np.array_equal(cnt, rcnt)
+    check(got, ref)
+
+
+def test_fast_orthonormal_and_general_frames_agree(built_lib, oracle, monkeypatch):
+    # the same orthonormal scene through both directivity forms: the
+    # orthonormal-frame shortcut is an identity, so they differ by rounding
+    sc = _vhf_scene(2048, n_side=80)
+    got_o, ref, _, _ = fast_vs_oracle(sc, oracle)
+    monkeypatch.setenv("RP_PAIR_ORTHO", "0")
+    got_g, _, _, _ = fast_vs_oracle(sc, oracle)
+    check(got_o, ref)
+    check(got_g, ref)
+    assert rel_l2(got_o, got_g) <= 1e-4, rel_l2(got_o, got_g)
