@@ -456,21 +456,27 @@ struct ConvArgs {
     const Cplx<float>* Hs;  // DIF_M(crop kernel) / M
     int nr, n2, N, M, crop_K, crop_all;
     float sig_scale;
-    C32* part;          // [nb][nsplit][nr]
+    C32* part;          // [nb][nsplit][n2]: per split, the targets' sum of u
     int nsplit;
     unsigned int* work;
 };
 
+// Per target: u = Psour (*) Ptarg (convolveComplex's linear convolution,
+// N = 2nr - 1 values) from four transforms of 2nr; the item's targets' u
+// are summed.  The rest of the chain (cropSpectrum, the inverse N-point
+// DFT, takeEveryOtherComplex) is linear in u and the same for every target,
+// so it runs once per trace on the sum (k_trace_m32) instead of per target.
 // Persistent over the items of one or more batches (job j owns items
-// [start[j], start[j + 1])).  X (2nr) and W (M = 4nr) hold every element at
-// its swizzled position (swz, rp_fft.cuh: conflict-free in shared memory,
-// within one 256-byte row in global memory); twiddles come from the SFU.
-// MODE 0: X and W in shared memory (nr <= 4096), the targets summed in
-// registers.  MODE 1: X in shared memory, W in this block's slot of the
-// global scratch (nr = 8192, where W no longer fits).  MODE 2: both in the
-// slot (nr >= 16384).  Modes 1 and 2 sum the targets in the item's partial
-// trace in global memory (same thread, same element, same target order as
-// the registers of mode 0, so every mode gives the same sums).
+// [start[j], start[j + 1])).  X (2nr) and W (2nr, + nr staging in modes 1
+// and 2) hold every element at its swizzled position (swz, rp_fft.cuh:
+// conflict-free in shared memory, within one 256-byte row in global
+// memory); twiddles come from the SFU.  MODE 0: X and W in shared memory
+// (nr <= 4096), the targets summed in registers.  MODE 1: X in shared
+// memory, W in this block's slot of the global scratch (nr = 8192).  MODE 2:
+// both in the slot (nr >= 16384).  Modes 1 and 2 sum the targets in the
+// item's partial row in global memory (same thread, same element, same
+// target order as the registers of mode 0, so every mode gives the same
+// sums).
 template <int KPT, int MODE>
 __global__ void __launch_bounds__(RP_CONV_THREADS, 1)
 k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ start, int njobs,
@@ -503,13 +509,12 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
         if (item0 >= total) break;
         curJ = jb;
         const unsigned int item = item0 - start[jb];
-        const int nr = A.nr, n2 = A.n2, N = A.N, M = A.M;
+        const int nr = A.nr, n2 = A.n2, N = A.N;
         Cplx<float>* const X = (MODE == 2) ? gbase : sbase;
         Cplx<float>* const W = (MODE == 0) ? sbase + n2 : (MODE == 1 ? gbase : gbase + n2);
         // the job's arguments in registers (the loops below store to shared
         // memory, which would otherwise force re-reads of A)
         const Cplx<float>* __restrict__ C2s = A.C2s;
-        const Cplx<float>* __restrict__ Hs = A.Hs;
         const C32* __restrict__ T = A.T;
         const int Wt = A.Wt, nbA = A.nb, nsplit = A.nsplit;
         const int64_t tstride = A.tstride;
@@ -522,12 +527,12 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
         const int q0 = sp * RP_CONV_SPLIT;
         if (q0 >= nq) continue;
         const int q1 = min(q0 + RP_CONV_SPLIT, nq);
-        C32* const out = part + ((size_t)s * nsplit + sp) * nr;
-        float accr[KPT], acci[KPT];
+        C32* const out = part + ((size_t)s * nsplit + sp) * n2;
+        float accr[2 * KPT], acci[2 * KPT];
 #pragma unroll
-        for (int i = 0; i < KPT; ++i) { accr[i] = 0.f; acci[i] = 0.f; }
+        for (int i = 0; i < 2 * KPT; ++i) { accr[i] = 0.f; acci[i] = 0.f; }
         if (MODE != 0)
-            for (int j = tid; j < nr; j += RP_CONV_THREADS) out[j] = C32{0.f, 0.f};
+            for (int j = tid; j < N; j += RP_CONV_THREADS) out[j] = C32{0.f, 0.f};
         for (int q = q0; q < q1; ++q) {
             const int b0 = bt0[(size_t)s * tstride + q];
             #pragma unroll 8
@@ -587,33 +592,22 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
             }
             __syncthreads();
             block_dit_s<float>(W, n2);                                // u (natural, N values)
-            #pragma unroll 8
-            for (int k = N + tid; k < M; k += RP_CONV_THREADS) W[swz(k)] = Cplx<float>{0.f, 0.f};
-            __syncthreads();
-            // cropSpectrum + inverse DFT on the N grid = circular convolution
-            // with the crop kernel h: linear convolution at M >= 2N - 1, then
-            // circ[n] = lin[n] + lin[n + N]
-            block_dif_s<float>(W, M);
-            #pragma unroll 8
-            for (int k = tid; k < M; k += RP_CONV_THREADS) W[swz(k)] = c_mul(W[swz(k)], Hs[k]);
-            __syncthreads();
-            block_dit_s<float>(W, M);
             if (MODE == 0) {
 #pragma unroll
-                for (int i = 0; i < KPT; ++i) {
+                for (int i = 0; i < 2 * KPT; ++i) {
                     const int j = tid + i * RP_CONV_THREADS;
-                    if (j < nr) {     // takeEveryOtherComplex: circ[2j]
-                        const Cplx<float> a = W[swz(2 * j)], b = W[swz(2 * j + N)];
-                        accr[i] += a.x + b.x;
-                        acci[i] += a.y + b.y;
+                    if (j < N) {
+                        const Cplx<float> a = W[swz(j)];
+                        accr[i] += a.x;
+                        acci[i] += a.y;
                     }
                 }
             } else {
-                for (int j = tid; j < nr; j += RP_CONV_THREADS) {
-                    const Cplx<float> a = W[swz(2 * j)], b = W[swz(2 * j + N)];
+                for (int j = tid; j < N; j += RP_CONV_THREADS) {
+                    const Cplx<float> a = W[swz(j)];
                     C32 o = out[j];
-                    o.x += a.x + b.x;
-                    o.y += a.y + b.y;
+                    o.x += a.x;
+                    o.y += a.y;
                     out[j] = o;
                 }
             }
@@ -621,36 +615,59 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
         }
         if (MODE == 0) {
 #pragma unroll
-            for (int i = 0; i < KPT; ++i) {
+            for (int i = 0; i < 2 * KPT; ++i) {
                 const int j = tid + i * RP_CONV_THREADS;
-                if (j < nr) out[j] = C32{accr[i], acci[i]};
+                if (j < N) out[j] = C32{accr[i], acci[i]};
             }
         }
     }
 }
 
-// sig = refl + sum of the per-split partial traces (split order), FP64.
-__global__ void k_sum32s(const int* __restrict__ nill, const int* __restrict__ ntl,
-                         const C32* __restrict__ refl, const C32* __restrict__ part, int nsplit, int nr,
-                         void* __restrict__ out, int out64, int s0) {
-    const int s = blockIdx.y;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nr) return;
-    double vr = 0.0, vi = 0.0;
-    if (nill[s] > 0) {
-        C32 r = refl[(size_t)s * nr + i];
-        vr = r.x; vi = r.y;
-        const int ns = (ntl[s] + RP_CONV_SPLIT - 1) / RP_CONV_SPLIT;
-        const C32* z = part + (size_t)s * nsplit * nr + i;
-        for (int q = 0; q < ns; ++q) {
-            C32 u = z[(size_t)q * nr];
-            vr += u.x;
-            vi += u.y;
-        }
+// Per trace (one block): the targets' u summed over the splits (split
+// order, FP64), then cropSpectrum and the inverse N-point DFT as the circular
+// convolution with the crop kernel h (its M-point spectrum Hs, M = 4nr >=
+// 2N - 1: linear convolution, then circ[n] = lin[n] + lin[n + N]),
+// takeEveryOtherComplex (circ[2j]) and sig = refl + that (FP64).  W: M
+// complex values in shared memory, or (gW != null) in this trace's slot of
+// global scratch.
+__global__ void __launch_bounds__(1024, 1)
+k_trace_m32(const int* __restrict__ nill, const int* __restrict__ ntl, const C32* __restrict__ refl,
+            const C32* __restrict__ part, int nsplit, int nr, const Cplx<float>* __restrict__ Hs,
+            Cplx<float>* __restrict__ gW, void* __restrict__ out, int out64, int s0) {
+    extern __shared__ __align__(16) unsigned char tsm[];
+    const int s = blockIdx.x;
+    const int n2 = 2 * nr, N = n2 - 1, M = 2 * n2;
+    Cplx<float>* W = gW ? gW + (size_t)s * M : reinterpret_cast<Cplx<float>*>(tsm);
+    const bool any = nill[s] > 0;
+    const int ns = any ? (ntl[s] + RP_CONV_SPLIT - 1) / RP_CONV_SPLIT : 0;
+    const C32* z = part + (size_t)s * nsplit * n2;
+    for (int k = threadIdx.x; k < M; k += blockDim.x) {
+        double vr = 0.0, vi = 0.0;
+        if (k < N)
+            for (int q = 0; q < ns; ++q) {
+                const C32 u = z[(size_t)q * n2 + k];
+                vr += u.x;
+                vi += u.y;
+            }
+        W[swz(k)] = Cplx<float>{(float)vr, (float)vi};
     }
-    const size_t o = (size_t)(s0 + s) * nr + i;
-    if (out64) reinterpret_cast<C64*>(out)[o] = C64{vr, vi};
-    else reinterpret_cast<float2*>(out)[o] = make_float2((float)vr, (float)vi);
+    __syncthreads();
+    block_dif_s<float>(W, M);
+    for (int k = threadIdx.x; k < M; k += blockDim.x) W[swz(k)] = c_mul(W[swz(k)], Hs[k]);
+    __syncthreads();
+    block_dit_s<float>(W, M);
+    for (int j = threadIdx.x; j < nr; j += blockDim.x) {
+        double vr = 0.0, vi = 0.0;
+        if (any) {
+            const C32 r = refl[(size_t)s * nr + j];
+            const Cplx<float> a = W[swz(2 * j)], b = W[swz(2 * j + N)];
+            vr = (double)r.x + ((double)a.x + (double)b.x);
+            vi = (double)r.y + ((double)a.y + (double)b.y);
+        }
+        const size_t o = (size_t)(s0 + s) * nr + j;
+        if (out64) reinterpret_cast<C64*>(out)[o] = C64{vr, vi};
+        else reinterpret_cast<float2*>(out)[o] = make_float2((float)vr, (float)vi);
+    }
 }
 
 __global__ void k_surf_conv32(const long long* __restrict__ acc, const int* __restrict__ nill,
@@ -737,7 +754,7 @@ void fast_take_setup(Aa& a, const rp_scene* sc, const FastLayout& L) {
 }
 
 // Storage mode of the range compression (k_conv32s): 0 X and W in shared
-// memory (2nr + 4nr complex64 = 48 nr bytes, 192 KiB at nr = 4096), 1 X in
+// memory (2 x 2nr complex64 = 32 nr bytes, 128 KiB at nr = 4096), 1 X in
 // shared memory and W in global scratch (nr = 8192), 2 both in global
 // scratch (nr >= 16384), 3 the Bluestein kernel k_conv32 (nr not a power of
 // two).
@@ -748,11 +765,17 @@ int conv_mode(const rp_scene* sc) {
     return 2;
 }
 
-// Complex values in one block's slot of the global compression scratch.
+// Complex values in one block's slot of the global compression scratch: W
+// (2nr) plus nr for the Ptarg shift, and X (2nr) in mode 2.
 size_t conv_gslot(const rp_scene* sc) {
     const int m = conv_mode(sc);
-    return m == 1 ? (size_t)sc->mS : (m == 2 ? (size_t)(2 * sc->nr + sc->mS) : 0);
+    return m == 1 ? (size_t)3 * sc->nr : (m == 2 ? (size_t)5 * sc->nr : 0);
 }
+
+// The per-trace crop stage (k_trace_m32) keeps its M = 4nr values in shared
+// memory up to this size, else in a per-trace slot of global scratch.
+const size_t kTraceSmemMax = (size_t)200 << 10;
+bool trace_m_global(const rp_scene* sc) { return (size_t)4 * sc->nr * sizeof(C32) > kTraceSmemMax; }
 
 int64_t conv_splits(int64_t tstride) { return (tstride + RP_CONV_SPLIT - 1) / RP_CONV_SPLIT; }
 
@@ -760,7 +783,8 @@ template <class Aa>
 void fast_take_pairs(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<C32>((size_t)RP_PARTS * L.nb * L.tstride * L.Wt);   // T parts
     if (conv_mode(sc) <= 2) {
-        a.template take<C32>((size_t)L.nb * conv_splits(L.tstride) * sc->nr);   // partial traces
+        a.template take<C32>((size_t)L.nb * conv_splits(L.tstride) * 2 * sc->nr);   // per-split sums of u
+        if (trace_m_global(sc)) a.template take<C32>((size_t)L.nb * 4 * sc->nr);   // per-trace crop stage
         // global compression scratch: one slot per SM (a wave takes one region
         // for all its segments, sized here per segment as an upper bound)
         if (conv_mode(sc) >= 1) a.template take<C32>((size_t)sc->sm_count * conv_gslot(sc));
@@ -952,6 +976,7 @@ struct Seg {
     int cmode = 0;          // compression storage mode (conv_mode)
     bool pairs = false;
     C32* T = nullptr; C32* Z = nullptr; C32* cscr = nullptr; C32* part = nullptr;
+    C32* tscr = nullptr;    // per-trace crop-stage scratch (nr > 4096)
 };
 
 struct SceneConst {
@@ -1211,7 +1236,8 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     for (Seg& g : segs) {
         g.T = b.take<C32>((size_t)RP_PARTS * g.nb * g.L.tstride * g.Wt);
         if (g.cmode <= 2) {
-            g.part = b.take<C32>((size_t)g.nb * g.nsplit * g.sc->nr);
+            g.part = b.take<C32>((size_t)g.nb * g.nsplit * 2 * g.sc->nr);
+            g.tscr = trace_m_global(g.sc) ? b.take<C32>((size_t)g.nb * 4 * g.sc->nr) : nullptr;
         } else {
             g.Z = b.take<C32>((size_t)g.nb * g.L.tstride * g.sc->nr);
             g.cscr = b.take<C32>((size_t)g.L.slots * g.L.slot);
@@ -1247,7 +1273,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
             hcs[m].push_back(hcs[m].back() + (unsigned)(g->nb * g->nsplit));
             max_nr[m] = std::max(max_nr[m], g->sc->nr);
             // shared memory: X and W (mode 0), X (mode 1), nothing (mode 2)
-            const size_t sx = m == 0 ? (size_t)(2 * g->sc->nr + g->sc->mS) : (m == 1 ? (size_t)(2 * g->sc->nr) : 0);
+            const size_t sx = m == 0 ? (size_t)(4 * g->sc->nr) : (m == 1 ? (size_t)(2 * g->sc->nr) : 0);
             csm[m] = std::max(csm[m], sx * sizeof(Cplx<float>));
         }
     }
@@ -1302,9 +1328,13 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
                                             g.Lw.surf_slot);
         RP_LAUNCHED();
         if (g.cmode <= 2) {
-            if (!g.pairs) RP_CUDA(cudaMemsetAsync(g.part, 0, sizeof(C32) * g.nb * g.nsplit * nr, st));
-            k_sum32s<<<dim3((nr + 255) / 256, g.nb), 256, 0, st>>>(g.nill, g.ntl, g.refl, g.part, g.nsplit, nr,
-                                                                  g.d_out, g.out64, (int)g.s0);
+            if (!g.pairs) RP_CUDA(cudaMemsetAsync(g.part, 0, sizeof(C32) * g.nb * g.nsplit * 2 * nr, st));
+            const size_t tsm = g.tscr ? 0 : (size_t)4 * nr * sizeof(C32);
+            RP_CUDA(cudaFuncSetAttribute(k_trace_m32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+            k_trace_m32<<<g.nb, 1024, tsm, st>>>(g.nill, g.ntl, g.refl, g.part, g.nsplit, nr,
+                                                 (const Cplx<float>*)sc->d_HS,
+                                                 reinterpret_cast<Cplx<float>*>(g.tscr), g.d_out, g.out64,
+                                                 (int)g.s0);
         } else {
             if (!g.pairs) RP_CUDA(cudaMemsetAsync(g.Z, 0, sizeof(C32) * g.nb * g.L.tstride * nr, st));
             k_sum32<<<dim3((nr + 255) / 256, g.nb), 256, 0, st>>>(g.nill, g.ntl, g.L.tstride, g.refl, g.Z, nr,

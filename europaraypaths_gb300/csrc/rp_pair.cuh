@@ -78,6 +78,7 @@ struct __align__(16) ChunkMeta {
     double cx, cy, cz;     // chunk centre (FP64: origin + cf)
     double bbmin[3], bbmax[3];
 };
+static_assert(sizeof(ChunkMeta) % 16 == 0, "ChunkMeta is staged by bulk copies");
 
 // ------------------------------------------------------------ TMA bulk --
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -520,11 +521,12 @@ __device__ __forceinline__ int floor_dd(float Th, float Tl, float kh, float kl, 
 
 // Dynamic shared memory of the pair kernels: two record buffers, the
 // per-thread bin windows, the threads' target positions relative to the
-// trace origin as double-floats.
+// trace origin as double-floats, the two staged chunks' metadata.
 extern __shared__ __align__(128) unsigned char pair_smem[];
 #define RP_PAIR_WIN_OFF (2 * RP_CHUNK_PAIRS * sizeof(FacetPair))
 #define RP_PAIR_TPOS_OFF (RP_PAIR_WIN_OFF + (size_t)RP_WIN * RP_PAIR_THREADS * sizeof(float2))
-#define RP_PAIR_SMEM_BYTES (RP_PAIR_TPOS_OFF + 2 * RP_PAIR_THREADS * sizeof(float4))
+#define RP_PAIR_META_OFF (RP_PAIR_TPOS_OFF + 2 * RP_PAIR_THREADS * sizeof(float4))
+#define RP_PAIR_SMEM_BYTES (RP_PAIR_META_OFF + 2 * sizeof(ChunkMeta))
 
 template <int NT, int ILP, bool ORTHO, class PA>
 __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, uint64_t* bars, uint32_t* phase) {
@@ -532,6 +534,7 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
     FacetPair* srec = reinterpret_cast<FacetPair*>(pair_smem);                     // [2][RP_CHUNK_PAIRS]
     float2* win = reinterpret_cast<float2*>(pair_smem + RP_PAIR_WIN_OFF);          // [RP_WIN][threads]
     float4* s_tq = reinterpret_cast<float4*>(pair_smem + RP_PAIR_TPOS_OFF);        // [2][threads]
+    ChunkMeta* smeta = reinterpret_cast<ChunkMeta*>(pair_smem + RP_PAIR_META_OFF);  // [2]
     const int tid = threadIdx.x;
     const int nq = A.ntl[s];
     const int n = A.nill[s];
@@ -562,12 +565,15 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         Trow = A.T + (((size_t)part * A.nb + s) * A.tstride + q) * A.Wt;
     }
     const FacetPair* rbase = A.rec + (size_t)s * (A.rstride / 2);
-    // prologue: stage chunk k0 (whole pairs: an odd count ends with a padded pair)
+    const ChunkMeta* mbase = A.meta + (size_t)s * A.mstride;
+    // prologue: stage chunk k0 and its metadata (whole pairs: an odd count
+    // ends with a padded pair)
     if (tid == 0) {
         int cnt = min(RP_CHUNK, n - k0 * RP_CHUNK);
         uint32_t bytes = (uint32_t)(((cnt + 1) >> 1) * sizeof(FacetPair));
-        mbar_expect_tx(&bars[0], bytes);
+        mbar_expect_tx(&bars[0], bytes + (uint32_t)sizeof(ChunkMeta));
         tma_bulk_g2s(srec, rbase + (size_t)k0 * RP_CHUNK_PAIRS, bytes, &bars[0]);
+        tma_bulk_g2s(smeta, mbase + k0, (uint32_t)sizeof(ChunkMeta), &bars[0]);
     }
     for (int k = k0; k < k1; ++k) {
         const int buf = (k - k0) & 1;
@@ -576,11 +582,12 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         if (tid == 0 && k + 1 < k1) {
             int cnt = min(RP_CHUNK, n - (k + 1) * RP_CHUNK);
             uint32_t bytes = (uint32_t)(((cnt + 1) >> 1) * sizeof(FacetPair));
-            mbar_expect_tx(&bars[buf ^ 1], bytes);
+            mbar_expect_tx(&bars[buf ^ 1], bytes + (uint32_t)sizeof(ChunkMeta));
             tma_bulk_g2s(srec + (buf ^ 1) * RP_CHUNK_PAIRS, rbase + (size_t)(k + 1) * RP_CHUNK_PAIRS, bytes,
                          &bars[buf ^ 1]);
+            tma_bulk_g2s(smeta + (buf ^ 1), mbase + k + 1, (uint32_t)sizeof(ChunkMeta), &bars[buf ^ 1]);
         }
-        const ChunkMeta* mp = A.meta + (size_t)s * A.mstride + k;
+        const ChunkMeta* mp = smeta + buf;
         if (!mbar_wait(&bars[buf], phase[buf])) {
             if (tid == 0) atomicOr(A.err + 1, 1u);
         }
@@ -621,7 +628,7 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         const bool all_fit = __all_sync(0xffffffffu, fits);
         if (active) {
             for (int w = 0; w < RP_WIN; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
-            const int cnt = mp->n;
+            const int cnt = min(RP_CHUNK, n - k * RP_CHUNK);    // = mp->n (bounds from the count, not the staged copy)
             const int npairs = (cnt + 1) >> 1;
             const bool prisms = (A.np > 0) && !A.lossless;
             int jp = 0;
