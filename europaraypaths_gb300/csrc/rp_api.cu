@@ -9,7 +9,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <numeric>
+#include <utility>
 #include <vector>
 
 #include "rp_internal.h"
@@ -47,6 +50,24 @@ void rp_set_error(const char* fmt, ...) {
 int rp_cuda_fail(cudaError_t e, const char* what) {
     rp_set_error("CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
     return RP_ERR_CUDA;
+}
+
+// Kernels whose dynamic shared memory depends on the scene are launched
+// from several host threads (server workers).  Their limit only ever grows,
+// per device and under a lock, so no launch meets a limit that another
+// thread lowered between this thread's raise and its launch.
+int rp_allow_dyn_smem(const void* fn, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> cur;
+    if (bytes <= (48u << 10)) return RP_OK;
+    int dev = 0;
+    RP_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    size_t& c = cur[{dev, fn}];
+    if (bytes <= c) return RP_OK;
+    RP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    c = bytes;
+    return RP_OK;
 }
 
 int Arena::reserve(size_t bytes) {

@@ -623,8 +623,27 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
     }
 }
 
-// Per trace (one block): the targets' u summed over the splits (split
-// order, FP64), then cropSpectrum and the inverse N-point DFT as the circular
+// The targets' u summed over the splits of each trace (split order, FP64),
+// written over split 0 (each thread owns its element).  Wide, so the FP64
+// sums spread over every SM.
+__global__ void k_usum32(const int* __restrict__ nill, const int* __restrict__ ntl, C32* __restrict__ part,
+                         int nsplit, int n2) {
+    const int s = blockIdx.y;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n2) return;
+    const int ns = nill[s] > 0 ? (ntl[s] + RP_CONV_SPLIT - 1) / RP_CONV_SPLIT : 0;
+    C32* z = part + (size_t)s * nsplit * n2 + k;
+    double vr = 0.0, vi = 0.0;
+    if (k < n2 - 1)
+        for (int q = 0; q < ns; ++q) {
+            const C32 u = z[(size_t)q * n2];
+            vr += u.x;
+            vi += u.y;
+        }
+    z[0] = C32{(float)vr, (float)vi};
+}
+
+// Per trace (one block): the summed u (split 0 after k_usum32), then cropSpectrum and the inverse N-point DFT as the circular
 // convolution with the crop kernel h (its M-point spectrum Hs, M = 4nr >=
 // 2N - 1: linear convolution, then circ[n] = lin[n] + lin[n + N]),
 // takeEveryOtherComplex (circ[2j]) and sig = refl + that (FP64).  W: M
@@ -639,17 +658,10 @@ k_trace_m32(const int* __restrict__ nill, const int* __restrict__ ntl, const C32
     const int n2 = 2 * nr, N = n2 - 1, M = 2 * n2;
     Cplx<float>* W = gW ? gW + (size_t)s * M : reinterpret_cast<Cplx<float>*>(tsm);
     const bool any = nill[s] > 0;
-    const int ns = any ? (ntl[s] + RP_CONV_SPLIT - 1) / RP_CONV_SPLIT : 0;
     const C32* z = part + (size_t)s * nsplit * n2;
     for (int k = threadIdx.x; k < M; k += blockDim.x) {
-        double vr = 0.0, vi = 0.0;
-        if (k < N)
-            for (int q = 0; q < ns; ++q) {
-                const C32 u = z[(size_t)q * n2 + k];
-                vr += u.x;
-                vi += u.y;
-            }
-        W[swz(k)] = Cplx<float>{(float)vr, (float)vi};
+        const C32 u = k < N ? z[k] : C32{0.f, 0.f};
+        W[swz(k)] = Cplx<float>{u.x, u.y};
     }
     __syncthreads();
     block_dif_s<float>(W, M);
@@ -897,7 +909,7 @@ void sinc_poly(double T, int D, double* mono) {
 template <int KPT, int MODE>
 int launch_conv_k(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, size_t csm, int sms, int slots,
                   unsigned int items, unsigned int* work, C32* gscr, size_t gslot, cudaStream_t st) {
-    RP_CUDA(cudaFuncSetAttribute(k_conv32s<KPT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+    if (int rc = rp_allow_dyn_smem((const void*)k_conv32s<KPT, MODE>, csm)) return rc;
     int occ = 0;
     RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv32s<KPT, MODE>, RP_CONV_THREADS, csm));
     int64_t gmax = (int64_t)std::max(occ, 1) * sms;
@@ -1125,7 +1137,7 @@ int launch_pairs(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsig
         PairArgs P = seg_pair_args(g);
         P.work = d_work;
         void (*pk)(const PairArgs) = pick_pair_kernel(g.deg, cfg, g.sc->ortho != 0);
-        RP_CUDA(cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem));
+        if (int rc = rp_allow_dyn_smem((const void*)pk, pair_smem)) return rc;
         int occ = 0;
         RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, RP_PAIR_THREADS, pair_smem));
         const int64_t items = (int64_t)g.nb * P.tblocks * RP_PARTS;
@@ -1330,7 +1342,9 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         if (g.cmode <= 2) {
             if (!g.pairs) RP_CUDA(cudaMemsetAsync(g.part, 0, sizeof(C32) * g.nb * g.nsplit * 2 * nr, st));
             const size_t tsm = g.tscr ? 0 : (size_t)4 * nr * sizeof(C32);
-            RP_CUDA(cudaFuncSetAttribute(k_trace_m32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+            if (int rc = rp_allow_dyn_smem((const void*)k_trace_m32, tsm)) return rc;
+            k_usum32<<<dim3((2 * nr + 255) / 256, g.nb), 256, 0, st>>>(g.nill, g.ntl, g.part, g.nsplit, 2 * nr);
+            RP_LAUNCHED();
             k_trace_m32<<<g.nb, 1024, tsm, st>>>(g.nill, g.ntl, g.refl, g.part, g.nsplit, nr,
                                                  (const Cplx<float>*)sc->d_HS,
                                                  reinterpret_cast<Cplx<float>*>(g.tscr), g.d_out, g.out64,

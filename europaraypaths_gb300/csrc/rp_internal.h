@@ -22,6 +22,8 @@
 
 void rp_set_error(const char* fmt, ...);
 int rp_cuda_fail(cudaError_t e, const char* what);
+// Raise fn's dynamic shared-memory limit to at least bytes (never lowers it).
+int rp_allow_dyn_smem(const void* fn, size_t bytes);
 
 #define RP_CUDA(call)                                                    \
     do {                                                                 \

@@ -76,7 +76,7 @@ int launch_pairs_multi(int cfg, const PairJob* d_jobs, const unsigned int* d_sta
                        unsigned int* d_work, int64_t items, int sms, cudaStream_t st) {
     const size_t smem = RP_PAIR_SMEM_BYTES;
     auto mk = pick_multi(cfg);
-    RP_CUDA(cudaFuncSetAttribute(mk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (int rc = rp_allow_dyn_smem((const void*)mk, smem)) return rc;
     int occ = 0;
     RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mk, RP_PAIR_THREADS, smem));
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(occ, 1) * sms, items));
