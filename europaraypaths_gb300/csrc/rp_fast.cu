@@ -823,22 +823,22 @@ FastLayout fast_layout(const rp_scene* sc, int nb, int64_t tstride, int Wt) {
 const size_t kFastBudget = (size_t)32 << 30;
 
 
-// Pair-kernel instantiation: sinc degree x (ILP facets per step, resident
-// blocks per SM).  cfg 0: 2 x 3, 1: 2 x 2, 2: 1 x 4, 3: 1 x 3.
+// Pair-kernel instantiation: sinc degree x frame kind x (ILP facet pairs per
+// step, resident blocks per SM).  cfg 0: 2 x 3, 1: 2 x 2, 2: 3 x 2, 3: 4 x 2.
 template <int NT>
 void (*pick_cfg(int cfg, bool ortho))(const PairArgs) {
     if (ortho) {
         switch (cfg) {
             case 1: return k_pairs32<NT, 2, 2, true>;
-            case 2: return k_pairs32<NT, 1, 4, true>;
-            case 3: return k_pairs32<NT, 1, 3, true>;
+            case 2: return k_pairs32<NT, 3, 2, true>;
+            case 3: return k_pairs32<NT, 4, 2, true>;
             default: return k_pairs32<NT, 2, 3, true>;
         }
     }
     switch (cfg) {
         case 1: return k_pairs32<NT, 2, 2, false>;
-        case 2: return k_pairs32<NT, 1, 4, false>;
-        case 3: return k_pairs32<NT, 1, 3, false>;
+        case 2: return k_pairs32<NT, 3, 2, false>;
+        case 3: return k_pairs32<NT, 4, 2, false>;
         default: return k_pairs32<NT, 2, 3, false>;
     }
 }

@@ -66,8 +66,8 @@ k_pairs32m(const PairJob* __restrict__ jobs, const unsigned int* __restrict__ st
 void (*pick_multi(int cfg))(const PairJob*, const unsigned int*, int, unsigned int*) {
     switch (cfg) {
         case 1: return k_pairs32m<2, 2>;
-        case 2: return k_pairs32m<1, 4>;
-        case 3: return k_pairs32m<1, 3>;
+        case 2: return k_pairs32m<3, 2>;
+        case 3: return k_pairs32m<4, 2>;
         default: return k_pairs32m<2, 3>;
     }
 }

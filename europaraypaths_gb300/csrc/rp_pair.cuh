@@ -633,15 +633,18 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
             const bool prisms = (A.np > 0) && !A.lossless;
             int jp = 0;
             if (all_fit && !prisms) {
-                if (ILP == 2)
-                for (; jp + 1 < npairs; jp += 2) {
-                    const FacetPair r0 = R[jp];
-                    const FacetPair r1 = R[jp + 1];
-                    f2 x0, re0, im0, x1, re1, im1;
-                    pair_eval2<NT, ORTHO, false>(r0, an, A, x0, re0, im0);
-                    pair_eval2<NT, ORTHO, false>(r1, an, A, x1, re1, im1);
-                    bin_add_fast2(x0, re0, im0, win, tid);
-                    bin_add_fast2(x1, re1, im1, win, tid);
+                // ILP pairs per step; binned in facet order, so every ILP
+                // gives the same sums
+                if (ILP > 1)
+                for (; jp + ILP <= npairs; jp += ILP) {
+                    f2 x[ILP], re[ILP], im[ILP];
+#pragma unroll
+                    for (int i = 0; i < ILP; ++i) {
+                        const FacetPair r0 = R[jp + i];
+                        pair_eval2<NT, ORTHO, false>(r0, an, A, x[i], re[i], im[i]);
+                    }
+#pragma unroll
+                    for (int i = 0; i < ILP; ++i) bin_add_fast2(x[i], re[i], im[i], win, tid);
                 }
                 for (; jp < npairs; ++jp) {
                     const FacetPair r0 = R[jp];
