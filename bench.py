@@ -422,11 +422,11 @@ def main():
         mufu_rate = opcount.MUFU_PER_EVAL * evals_rate
         roof = {"bound": "fp32", "kernel": "k_pairs32",
                 "achieved": fp32_rate / 1e12, "peak": fp32_peak / 1e12,
-                "unit": "T FP32-pipe instructions/s",
+                "unit": "T FP32 lane-operations/s",
                 "frac": fp32_rate / fp32_peak if fp32_peak else None,
-                # DRAM read+write of one launch from the committed ncu capture (2 traces: 247 + 30 MB),
-                # scaled by the traces per launch; the kernel is compute-bound (DRAM < 0.1 % of peak)
-                "traffic": 277.5e6 * tps / 2.0,
+                # DRAM read+write of one launch from the committed ncu capture (2 traces: 258.5 + 36.2
+                # MB), scaled by the traces per launch; the kernel is compute-bound (DRAM < 0.1 % of peak)
+                "traffic": 294.7e6 * tps / 2.0,
                 "traffic_unit": "bytes per launch (ncu, profiles/k_pairs32_large_scene.md, scaled)",
                 "peak_source": (f"nominal {opcount.FP32_FMA_PER_CLK_PER_SM} FP32 lanes/clk/SM x {n_sm} SMs x "
                                 f"{sm_mhz:.0f} MHz median SM clock under load; MEASURED_PEAKS.json holds HBM "
@@ -439,8 +439,7 @@ def main():
                           "peak": opcount.ISSUE_PER_CLK_PER_SM * n_sm * clk / 1e12,
                           "unit": "T thread-instructions/s",
                           "frac": (opcount.INSTR_PER_EVAL * evals_rate) / (opcount.ISSUE_PER_CLK_PER_SM * n_sm * clk),
-                          "instr_per_eval": opcount.INSTR_PER_EVAL,
-                          "note": "the binding limit: every instruction takes an issue slot"},
+                          "instr_per_eval": opcount.INSTR_PER_EVAL},
                 "pair_kernel_ms_per_launch": stage["pairs_ms"] / max(stage["pair_launches"], 1),
                 "pair_evals_per_s": evals_rate,
                 "pair_evals_per_launch": my_evals / max(stage["pair_launches"], 1),

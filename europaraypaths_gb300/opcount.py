@@ -10,28 +10,30 @@ The fused FP32 kernel (csrc/rp_fast.cu, k_pairs32) evaluates one
 the inbound one times -1/sqrt(P) in the non-specular mode; so one k_pairs32
 evaluation covers two metric pairs.
 
-Counts per k_pairs32 evaluation on the large scene (sinc polynomial of
-degree 3, the fast window path), measured from the kernel's executed
-instruction mix (ncu sass__inst_executed_per_opcode over one launch, divided
-by the evaluations of that launch); a higher sinc degree adds 4 FFMA per
-degree:
+Counts per k_pairs32 evaluation on the large scene (orthonormal facet
+frames, sinc polynomial of degree 3, the fast window path), counted from the
+kernel source for the packed two-lane FP32 instructions and measured for the
+rest (ncu: executed thread instructions and scalar FFMA/FMUL/FADD over one
+launch, divided by the evaluations of that launch); a higher sinc degree
+adds 4 FP32 lane operations per degree, general (non-orthonormal) frames
+about 10:
 
-* FP32-pipe instructions: 72 -- 34 FFMA, 26 FMUL, 10 FADD, 2 compare and
-  select.  The terms: distance and Ttd - T0 from the anchor, the four
-  direction dot products, 1 - cos^2 of both angles, the in-plane sinc split,
-  four degree-3 polynomials and their product, the attenuation exponent,
-  amplitude, phase and its scaling, phasor, bin coordinate, and the two-bin
-  window update.
-* MUFU (special-function) instructions: 7 -- rsqrt (1/Ttd), rcp (dT), rcp
-  (1/Ttd^2), rcp (1/h^2), ex2, sin and cos of the phase.
-* All instructions (the issue rate that bounds the kernel): 97.5 -- the
-  above plus 6 shared-memory accesses (record and window), the floor
-  conversion pair, address arithmetic and the loop.
+* FP32 lane operations: 60.4 -- 55 from packed two-lane instructions (one
+  lane per evaluation: anchor distance and Ttd - T0, three direction dot
+  products, the four squared sinc arguments, four degree-3 polynomials and
+  their product, the attenuation exponent, amplitude, phase, phasor, bin
+  coordinate and split weights) and 5.4 scalar (the two-bin window update
+  and the phase scaling of the special-function sine and cosine).
+* MUFU (special-function) instructions: 6 -- rsqrt (1/Ttd), rcp (dT), rcp
+  (the in-plane split), ex2, sin and cos of the phase.
+* All thread instructions: 54.9 -- a packed instruction issues once for two
+  evaluations; plus 4 shared-memory record loads and 4 window accesses per
+  evaluation, the floor conversion pair, address arithmetic and the loop.
 """
 
-FP32_OPS_PER_EVAL = 72
-MUFU_PER_EVAL = 7
-INSTR_PER_EVAL = 97.5
+FP32_OPS_PER_EVAL = 60.4
+MUFU_PER_EVAL = 6
+INSTR_PER_EVAL = 54.9
 EVALS_PER_TARGET_PAIR_METRIC = 0.5     # one evaluation covers two metric pairs
 
 # Nominal special-function throughput of a Blackwell SM (results per clock).
