@@ -649,7 +649,7 @@ __global__ void k_usum32(const int* __restrict__ nill, const int* __restrict__ n
 // takeEveryOtherComplex (circ[2j]) and sig = refl + that (FP64).  W: M
 // complex values in shared memory, or (gW != null) in this trace's slot of
 // global scratch.
-__global__ void __launch_bounds__(1024, 1)
+__global__ void __launch_bounds__(512, 1)
 k_trace_m32(const int* __restrict__ nill, const int* __restrict__ ntl, const C32* __restrict__ refl,
             const C32* __restrict__ part, int nsplit, int nr, const Cplx<float>* __restrict__ Hs,
             Cplx<float>* __restrict__ gW, void* __restrict__ out, int out64, int s0) {
@@ -1345,7 +1345,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
             if (int rc = rp_allow_dyn_smem((const void*)k_trace_m32, tsm)) return rc;
             k_usum32<<<dim3((2 * nr + 255) / 256, g.nb), 256, 0, st>>>(g.nill, g.ntl, g.part, g.nsplit, 2 * nr);
             RP_LAUNCHED();
-            k_trace_m32<<<g.nb, 1024, tsm, st>>>(g.nill, g.ntl, g.refl, g.part, g.nsplit, nr,
+            k_trace_m32<<<g.nb, 512, tsm, st>>>(g.nill, g.ntl, g.refl, g.part, g.nsplit, nr,
                                                  (const Cplx<float>*)sc->d_HS,
                                                  reinterpret_cast<Cplx<float>*>(g.tscr), g.d_out, g.out64,
                                                  (int)g.s0);

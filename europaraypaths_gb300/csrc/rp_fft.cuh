@@ -164,130 +164,14 @@ __device__ void block_dit(Cplx<T>* a, int n, const TW& tw, int log2M) {
     }
 }
 
-// Shared-memory variants for the hot range-compression kernel: twiddles come
-// from a shared table of M/4 entries (every index j * (M/L) used above is
-// below M/4 because j < L/4 in radix-4 stages and j = 0 in the radix-2
-// stage), and each thread first loads the inputs of U butterflies, then
-// computes and stores them, so the loads of a stage overlap.
-template <class T>
-struct SmemTw {
-    const Cplx<T>* t;
-    __device__ __forceinline__ Cplx<T> operator()(int k) const { return t[k]; }
-};
-
-template <class T, int U>
-__device__ __noinline__ void block_dif_u(Cplx<T>* a, int n, const Cplx<T>* tws, int log2M) {
-    const SmemTw<T> tw{tws};
-    const int m = fft_log2(n);
-    const int nb = n >> 2;
-    int L = n, lL = m;
-    for (; L >= 4; L >>= 2, lL -= 2) {
-        const int q4 = L >> 2, lq = lL - 2, msh = log2M - lL;
-        for (int t0 = threadIdx.x; t0 < nb; t0 += blockDim.x * U) {
-            Cplx<T> x[U][4];
-            int bb[U], jj[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int t = t0 + u * blockDim.x;
-                const int j = t & (q4 - 1);
-                jj[u] = j;
-                bb[u] = (t >> lq) * L + j;
-                if (t < nb) {
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) x[u][q] = a[bb[u] + q * q4];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int t = t0 + u * blockDim.x;
-                if (t >= nb) continue;
-                Cplx<T> t0c = c_add(x[u][0], x[u][2]), t1 = c_sub(x[u][0], x[u][2]);
-                Cplx<T> t2 = c_add(x[u][1], x[u][3]), t3 = c_sub(x[u][1], x[u][3]);
-                Cplx<T> y1 = Cplx<T>{t1.x + t3.y, t1.y - t3.x};
-                Cplx<T> y3 = Cplx<T>{t1.x - t3.y, t1.y + t3.x};
-                const int b = bb[u];
-                a[b] = c_add(t0c, t2);
-                Cplx<T> y2 = c_sub(t0c, t2);
-                if (jj[u] == 0) {
-                    a[b + q4] = y1; a[b + 2 * q4] = y2; a[b + 3 * q4] = y3;
-                } else {
-                    Cplx<T> w1 = tw(jj[u] << msh);
-                    Cplx<T> w2 = c_mul(w1, w1);
-                    Cplx<T> w3 = c_mul(w1, w2);
-                    a[b + q4] = c_mul(y1, w1);
-                    a[b + 2 * q4] = c_mul(y2, w2);
-                    a[b + 3 * q4] = c_mul(y3, w3);
-                }
-            }
-        }
-        __syncthreads();
-    }
-    if (L == 2) {
-        for (int t = threadIdx.x; t < n / 2; t += blockDim.x) dif2(a, 2, 0, t, tw, log2M - 1);
-        __syncthreads();
-    }
-}
-
-template <class T, int U>
-__device__ __noinline__ void block_dit_u(Cplx<T>* a, int n, const Cplx<T>* tws, int log2M) {
-    const SmemTw<T> tw{tws};
-    const int m = fft_log2(n);
-    const int nb = n >> 2;
-    int L, lL;
-    if (m & 1) {
-        for (int t = threadIdx.x; t < n / 2; t += blockDim.x) dit2(a, 2, 0, t, tw, log2M - 1);
-        __syncthreads();
-        L = 8; lL = 3;
-    } else {
-        L = 4; lL = 2;
-    }
-    for (; L <= n; L <<= 2, lL += 2) {
-        const int q4 = L >> 2, lq = lL - 2, msh = log2M - lL;
-        for (int t0 = threadIdx.x; t0 < nb; t0 += blockDim.x * U) {
-            Cplx<T> x[U][4];
-            int bb[U], jj[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int t = t0 + u * blockDim.x;
-                const int j = t & (q4 - 1);
-                jj[u] = j;
-                bb[u] = (t >> lq) * L + j;
-                if (t < nb) {
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) x[u][q] = a[bb[u] + q * q4];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int t = t0 + u * blockDim.x;
-                if (t >= nb) continue;
-                Cplx<T> x1 = x[u][1], x2 = x[u][2], x3 = x[u][3];
-                if (jj[u] != 0) {
-                    Cplx<T> w1 = tw(jj[u] << msh);
-                    Cplx<T> w2 = c_mul(w1, w1);
-                    Cplx<T> w3 = c_mul(w1, w2);
-                    x1 = c_mulc(x1, w1);
-                    x2 = c_mulc(x2, w2);
-                    x3 = c_mulc(x3, w3);
-                }
-                Cplx<T> t0c = c_add(x[u][0], x2), t1 = c_sub(x[u][0], x2), t2 = c_add(x1, x3), t3 = c_sub(x1, x3);
-                const int b = bb[u];
-                a[b] = c_add(t0c, t2);
-                a[b + 2 * q4] = c_sub(t0c, t2);
-                a[b + q4] = Cplx<T>{t1.x - t3.y, t1.y + t3.x};
-                a[b + 3 * q4] = Cplx<T>{t1.x + t3.y, t1.y - t3.x};
-            }
-        }
-        __syncthreads();
-    }
-}
-// Fused radix-4 stage pairs ("radix 16"): the 16 elements a[base + i*S],
-// i < 16, are closed under two consecutive radix-4 stages (DIF spans L, L/4
-// with S = L/16; DIT spans L, 4L with S = L/4), so one thread keeps them in
-// registers across both and a transform makes about half the passes over
-// shared memory (and half the barriers).  The stage schedule is the one
-// above, so outputs keep the same digit-reversed order.  Twiddles are
-// applied unconditionally (tw(0) = 1 exactly).
+// Fused radix-4 stage pairs ("radix 16", used by block_dif_s / block_dit_s
+// below): the 16 elements a[base + i*S], i < 16, are closed under two
+// consecutive radix-4 stages (DIF spans L, L/4 with S = L/16; DIT spans L,
+// 4L with S = L/4), so one thread keeps them in registers across both and a
+// transform makes about half the passes over shared memory (and half the
+// barriers).  The stage schedule is the one of block_dif / block_dit above,
+// so outputs keep the same digit-reversed order.  Twiddles are applied
+// unconditionally (tw(0) = 1 exactly).
 template <class T>
 __device__ __forceinline__ void r4_dif_reg(Cplx<T>& x0, Cplx<T>& x1, Cplx<T>& x2, Cplx<T>& x3, Cplx<T> w1) {
     const Cplx<T> t0 = c_add(x0, x2), t1 = c_sub(x0, x2), t2 = c_add(x1, x3), t3 = c_sub(x1, x3);
@@ -311,80 +195,6 @@ __device__ __forceinline__ void r4_dit_reg(Cplx<T>& x0, Cplx<T>& x1, Cplx<T>& x2
     x3 = Cplx<T>{t1.x + t3.y, t1.y - t3.x};
 }
 
-template <class T>
-__device__ __noinline__ void block_dif_f(Cplx<T>* a, int n, const Cplx<T>* tws, int log2M) {
-    const int m = fft_log2(n);
-    int L = n, lL = m;
-    for (; L >= 16; L >>= 4, lL -= 4) {
-        const int lS = lL - 4, S = 1 << lS;           // element stride L/16
-        const int msh1 = log2M - lL, msh2 = log2M - (lL - 2);
-        for (int g = threadIdx.x; g < (n >> 4); g += blockDim.x) {
-            const int b = g & (S - 1);
-            const int base = (g >> lS) * L + b;
-            Cplx<T> x[16];
-#pragma unroll
-            for (int i = 0; i < 16; ++i) x[i] = a[base + i * S];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) r4_dif_reg(x[i], x[i + 4], x[i + 8], x[i + 12], tws[(b + i * S) << msh1]);
-            const Cplx<T> w = tws[b << msh2];
-#pragma unroll
-            for (int c = 0; c < 4; ++c) r4_dif_reg(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3], w);
-#pragma unroll
-            for (int i = 0; i < 16; ++i) a[base + i * S] = x[i];
-        }
-        __syncthreads();
-    }
-    const SmemTw<T> tw{tws};
-    if (L >= 4) {   // one remaining radix-4 stage (L = 4 or 8)
-        for (int t = threadIdx.x; t < n / 4; t += blockDim.x) dif4(a, L, lL - 2, t, tw, log2M - lL);
-        __syncthreads();
-        L >>= 2;
-        lL -= 2;
-    }
-    if (L == 2) {
-        for (int t = threadIdx.x; t < n / 2; t += blockDim.x) dif2(a, 2, 0, t, tw, log2M - 1);
-        __syncthreads();
-    }
-}
-
-template <class T>
-__device__ __noinline__ void block_dit_f(Cplx<T>* a, int n, const Cplx<T>* tws, int log2M) {
-    const SmemTw<T> tw{tws};
-    const int m = fft_log2(n);
-    int L, lL;
-    if (m & 1) {
-        for (int t = threadIdx.x; t < n / 2; t += blockDim.x) dit2(a, 2, 0, t, tw, log2M - 1);
-        __syncthreads();
-        L = 8; lL = 3;
-    } else {
-        L = 4; lL = 2;
-    }
-    if ((m >> 1) & 1) {   // an odd number of radix-4 stages: the smallest runs alone
-        for (int t = threadIdx.x; t < n / 4; t += blockDim.x) dit4(a, L, lL - 2, t, tw, log2M - lL);
-        __syncthreads();
-        L <<= 2;
-        lL += 2;
-    }
-    for (; L <= n / 4; L <<= 4, lL += 4) {
-        const int lS = lL - 2, S = 1 << lS;           // element stride L/4
-        const int msh1 = log2M - lL, msh2 = log2M - (lL + 2);
-        for (int g = threadIdx.x; g < (n >> 4); g += blockDim.x) {
-            const int b = g & (S - 1);
-            const int base = (g >> lS) * (4 * L) + b;
-            Cplx<T> x[16];
-#pragma unroll
-            for (int i = 0; i < 16; ++i) x[i] = a[base + i * S];
-            const Cplx<T> w = tws[b << msh1];
-#pragma unroll
-            for (int c = 0; c < 4; ++c) r4_dit_reg(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3], w);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) r4_dit_reg(x[k], x[k + 4], x[k + 8], x[k + 12], tws[(b + k * S) << msh2]);
-#pragma unroll
-            for (int i = 0; i < 16; ++i) a[base + i * S] = x[i];
-        }
-        __syncthreads();
-    }
-}
 #endif
 
 #ifdef __CUDACC__
@@ -405,7 +215,7 @@ __device__ __forceinline__ Cplx<T> tw_sfu(int j, float step) {   // e^{-i j step
 }
 
 template <class T>
-__device__ __noinline__ void block_dif_s(Cplx<T>* a, int n) {
+__device__ __forceinline__ void block_dif_s(Cplx<T>* a, int n) {
     const int m = fft_log2(n);
     int L = n, lL = m;
     for (; L >= 16; L >>= 4, lL -= 4) {
@@ -451,7 +261,7 @@ __device__ __noinline__ void block_dif_s(Cplx<T>* a, int n) {
 }
 
 template <class T>
-__device__ __noinline__ void block_dit_s(Cplx<T>* a, int n) {
+__device__ __forceinline__ void block_dit_s(Cplx<T>* a, int n) {
     const int m = fft_log2(n);
     int L, lL;
     if (m & 1) {
