@@ -26,6 +26,7 @@
 #include <cmath>
 #include <map>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "rp_common.cuh"
@@ -1386,21 +1387,38 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
 }
 
 std::vector<int> host_target_bounds(const rp_scene* sc, const double* tr, int64_t ns) {
+    // An upper bound of each trace's in-aperture target count (k_target_flags
+    // keeps acos(cos) <= aperture): cos >= cos(aperture + 1e-9) - 1e-9, tested
+    // as (-r.v)^2 >= c0^2 |v|^2 without square roots or acos, so the bound is
+    // a superset of the device's decision.  It sizes the segment's buffers
+    // before any device work, so large calls split it over host threads.
     std::vector<int> ub(ns, 0);
     const int64_t nt = sc->nt;
     const double* tg = sc->h_targets.data();
-    const double ap = sc->dp.ap_rad + 1e-9;
-    for (int64_t s = 0; s < ns; ++s) {
+    const double c0 = std::cos(sc->dp.ap_rad + 1e-9) - 1e-9;
+    auto count = [&](int64_t s) {
         const double* r = tr + 9 * s;
         int c = 0;
         for (int64_t i = 0; i < nt; ++i) {
-            double vx = tg[i] - r[0], vy = tg[nt + i] - r[1], vz = tg[2 * nt + i] - r[2];
-            double m = std::sqrt(vx * vx + vy * vy + vz * vz);
-            double cs = -r[3] * vx / m - r[4] * vy / m - r[5] * vz / m;
-            cs = std::max(-1.0, std::min(1.0, cs));
-            if (!(std::acos(cs) > ap)) ++c;
+            const double vx = tg[i] - r[0], vy = tg[nt + i] - r[1], vz = tg[2 * nt + i] - r[2];
+            const double d = -(r[3] * vx + r[4] * vy + r[5] * vz);
+            const double m2 = vx * vx + vy * vy + vz * vz;
+            const bool in = c0 > 0.0 ? (d > 0.0 && d * d >= c0 * c0 * m2) : (d >= c0 * std::sqrt(m2));
+            c += in ? 1 : 0;
         }
         ub[s] = c;
+    };
+    const int64_t work = ns * nt;
+    const int nth = (int)std::min<int64_t>(std::min<int64_t>(ns, 16), std::max<int64_t>(1, work / 200000));
+    if (nth <= 1) {
+        for (int64_t s = 0; s < ns; ++s) count(s);
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nth; ++t)
+            th.emplace_back([&, t] {
+                for (int64_t s = t; s < ns; s += nth) count(s);
+            });
+        for (auto& x : th) x.join();
     }
     return ub;
 }
