@@ -454,6 +454,8 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
     d.ap_rad = p->aperture * (RP_PI / 180.0);
     d.ap_cos = std::cos(d.ap_rad);
     d.turn = RP_PI_F / (RP_PI * p->lam);
+    d.inv_dr = 1.0 / p->dr;
+    d.sqrt_eps12 = std::sqrt(p->eps_1 / p->eps_2);
     d.nr = p->nr; d.lossless = p->lossless; d.disable_surface = p->disable_surface;
     d.rerad_funct = p->rerad_funct;
     d.specular = p->specular ? 1 : 0;

@@ -77,26 +77,23 @@ __device__ __forceinline__ int block_excl_scan(int v, int* total) {
     return base + x - v;
 }
 
-// Pass 1 of facet culling: per-tile counts of illuminated facets and the
-// per-trace minimum source distance.  grid (tiles, traces).
+// Pass 1 of facet culling: the aperture flags and per-tile counts of
+// illuminated facets.  grid (tiles, traces).
 // pos: x,y,z SoA base (3 arrays of stride nf).
 static __global__ void k_cull_count(const double* __restrict__ pos, int64_t nf,
                                     const double* __restrict__ traces, double ap_rad,
-                                    uint8_t* __restrict__ flags, int* __restrict__ tile_cnt,
-                                    unsigned long long* __restrict__ dmin) {
+                                    uint8_t* __restrict__ flags, int* __restrict__ tile_cnt) {
     const int s = blockIdx.y;
     const TraceRow t = load_trace(traces, s);
     const float ap_cos = cosf((float)ap_rad);   // FP32: far inside the 1e-5 guard band
     const int64_t base = (int64_t)blockIdx.x * RP_TILE;
     int cnt = 0;
-    double dm = 1e300;
     for (int k = threadIdx.x; k < RP_TILE; k += blockDim.x) {
         int64_t i = base + k;
         uint8_t f = 0;
         if (i < nf) {
-            double d;
+            double d;       // unused here (the compiler drops its square root)
             f = illuminated_fast(pos[i], pos[nf + i], pos[2 * nf + i], t, ap_rad, ap_cos, &d) ? 1 : 0;
-            if (f) dm = fmin(dm, d);
         }
         if (i < nf) flags[(size_t)s * nf + i] = f;
         cnt += f;
@@ -104,7 +101,6 @@ static __global__ void k_cull_count(const double* __restrict__ pos, int64_t nf,
     int tot;
     block_excl_scan(cnt, &tot);
     if (threadIdx.x == 0) tile_cnt[(size_t)s * gridDim.x + blockIdx.x] = tot;
-    if (dm < 1e300) atomic_min_pos(dmin + s, dm);
 }
 
 // Pass 2: per trace, exclusive scan of the tile counts (one block per trace).

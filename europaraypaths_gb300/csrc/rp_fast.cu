@@ -103,7 +103,7 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
     if (k == 0 && threadIdx.x == 0) {
         org[4 * s] = ox; org[4 * s + 1] = oy; org[4 * s + 2] = oz; org[4 * s + 3] = 0.0;
     }
-    float xI = 0.f, rr = 0.f;
+    float xI = 0.f, rr = 0.f, amax = 0.f;
     float fv[RP_NFIELD];            // this facet's record fields (FacetField order)
 #pragma unroll
     for (int f = 0; f < RP_NFIELD; ++f) fv[f] = 0.f;
@@ -117,7 +117,7 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
         // reflection, as the reference's flag value gives).
         const double dxd = fx - t.sx, dyd = fy - t.sy, dzd = fz - t.sz;
         const double d = sqrt(dxd * dxd + dyd * dyd + dzd * dzd);
-        const float inv_d = (float)(1.0 / d);
+        const float inv_d = 1.f / (float)d;                 // angles are FP32
         const float Ix = (float)dxd * inv_d, Iy = (float)dyd * inv_d, Iz = (float)dzd * inv_d;
         const double nx = F[3 * nf + i], ny = F[4 * nf + i], nz = F[5 * nf + i];
         const double ux = F[6 * nf + i], uy = F[7 * nf + i], uz = F[8 * nf + i];
@@ -130,7 +130,7 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
         const float pv = Ix * (float)vx + Iy * (float)vy + Iz * (float)vz;
         const float hh = sqrtf(pu * pu + pv * pv);
         const float cph = hh > 0.f ? pv / hh : 1.f, sph = hh > 0.f ? pu / hh : 0.f;
-        const float sR = (float)sqrt(dp.eps1 / dp.eps2) * sI;
+        const float sR = (float)dp.sqrt_eps12 * sI;
         const bool tir = sR > 1.f;
         const float cR = tir ? cosf(1e4f) : sqrtf(fmaxf(0.f, 1.f - sR * sR));
         const float nu1 = (float)dp.nu1, nu2 = (float)dp.nu2;
@@ -160,14 +160,14 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
         const float ft = (float)(tt - floor(tt));
         float sn, cs;
         sincospif(-2.f * ft, &sn, &cs);
-        sx_o[(size_t)s * nf + j] = (float)((d - t.rst) / dp.dr);
+        xI = (float)((d - t.rst) * dp.inv_dr);
+        sx_o[(size_t)s * nf + j] = xI;
         sv_o[(size_t)s * nf + j] = C32{amp * cs, amp * sn};
-        atomic_max_pos(vmax + s, (double)amp);
+        amax = amp;
         // hoisted target-leg amplitude: sqrt(P Gr G frc n) lam^2 Dmax / ((4 pi)^2 Itd)
         const float Dmax = (4.f * (float)RP_PI_F * fsf * fsf) / (lamf * lamf);
         const float Kf = sqrtf((float)dp.P * grefr * G * (dp.lossless ? 1.f : frc) * (float)dp.nidx) * lamf *
                          lamf * Dmax / (f4 * df);
-        xI = (float)((d - t.rst) / dp.dr);
         const double ti = d * dp.turn;
         float ddx = (float)(fx - cx), ddy = (float)(fy - cy), ddz = (float)(fz - cz);
         rr = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
@@ -211,6 +211,9 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
             }
         }
     }
+    // the surface amplitude maximum of the trace: one atomic per chunk
+    const float bmax = block_reduce(amax, MaxOpF(), shf);
+    if (threadIdx.x == 0 && bmax > 0.f) atomic_max_pos(vmax + s, (double)bmax);
     float R = block_reduce(ok ? rr : 0.f, MaxOpF(), shf);
     float xmn = block_reduce(ok ? xI : 3e38f, MinOpF(), shf);
     float xmx = block_reduce(ok ? xI : -3e38f, MaxOpF(), shf);
@@ -749,7 +752,6 @@ void fast_take_setup(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<int>(L.nb);                             // nill
     a.template take<int>(L.nb);                             // ntl
     a.template take<unsigned long long>(L.nb);              // vmax
-    a.template take<unsigned long long>(L.nb);              // dmin
     a.template take<int>((size_t)L.nb * nf);                // idx
     a.template take<FacetPair>((size_t)L.nb * L.rstride / 2);    // records (facet pairs)
     a.template take<ChunkMeta>((size_t)L.nb * L.mstride);   // chunk meta
@@ -980,7 +982,7 @@ struct Seg {
     const double* coef = nullptr;
     FastLayout Lw, L;
     // setup stage
-    uint8_t* fflags; int* tcnt; int* nill; int* ntl; unsigned long long* vmax; unsigned long long* dmin;
+    uint8_t* fflags; int* tcnt; int* nill; int* ntl; unsigned long long* vmax;
     double* org; int* idx; FacetPair* rec; ChunkMeta* meta; float* sxv; C32* sv; TraceMeta* tm; uint8_t* tflags;
     int* tlist; int* bt0; int* misc; long long* acc; C32* refl; C32* sscr;
     // pair stage
@@ -1032,7 +1034,6 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
     g.nill = a.take<int>(nb);
     g.ntl = a.take<int>(nb);
     g.vmax = a.take<unsigned long long>(nb);
-    g.dmin = a.take<unsigned long long>(nb);
     g.idx = a.take<int>((size_t)nb * nfa);
     g.rec = a.take<FacetPair>((size_t)nb * Lw.rstride / 2);
     g.meta = a.take<ChunkMeta>((size_t)nb * Lw.mstride);
@@ -1049,12 +1050,11 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
     g.sscr = a.take<C32>((size_t)nb * Lw.surf_slot);
     const double* trb = g.trb;
     cudaMemsetAsync(g.vmax, 0, sizeof(unsigned long long) * nb, st);
-    cudaMemsetAsync(g.dmin, 0xff, sizeof(unsigned long long) * nb, st);
     cudaMemsetAsync(g.misc, 0, sizeof(int) * 8, st);
     cudaMemsetAsync(g.acc, 0, sizeof(long long) * nb * nr * 2, st);
     if (nf > 0) {
         k_cull_count<<<dim3((unsigned)((nf + RP_TILE - 1) / RP_TILE), nb), RP_TILE_THREADS, 0, st>>>(
-            sc->d_sorted, nf, trb, dp.ap_rad, g.fflags, g.tcnt, g.dmin);
+            sc->d_sorted, nf, trb, dp.ap_rad, g.fflags, g.tcnt);
         RP_LAUNCHED();
         compact_flags(g.fflags, nf, nb, g.tcnt, g.nill, g.idx, nfa, true, st);
         k_facets32<<<dim3((unsigned)Lw.mstride, nb), RP_CHUNK, 0, st>>>(

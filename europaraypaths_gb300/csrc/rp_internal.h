@@ -35,6 +35,7 @@ int rp_allow_dyn_smem(const void* fn, size_t bytes);
 struct DevParams {
     double lam, fs, P, nidx, eps1, eps2, nu1, nu2, alpha1, alpha2, ks, c1_over_c2;
     double dr, smpl, B, rng_res, ap_rad, ap_cos;
+    double inv_dr, sqrt_eps12;   // 1 / dr, sqrt(eps1 / eps2) (fast-form setup)
     double turn;   // phase turns per metre of range: pi_F / (pi lam), so that
                    // exp(-j (2 pi_F / lam) r) = exp(-j 2 pi r turn) (radar_kernels.cu:682)
     int nr, lossless, disable_surface, rerad_funct;

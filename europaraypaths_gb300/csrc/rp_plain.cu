@@ -390,7 +390,6 @@ void plain_take(A& a, const rp_scene* sc, const PlainLayout& L) {
     a.template take<int>(L.nb);                            // nill
     a.template take<int>(L.nb);                            // ntl
     a.template take<unsigned long long>(L.nb);             // vmax
-    a.template take<unsigned long long>(L.nb);             // dmin
     a.template take<int>((size_t)L.nb * nf);               // idx
     a.template take<double>((size_t)L.nb * nf);            // Itd
     a.template take<double>((size_t)L.nb * nf);            // Gi
@@ -497,7 +496,6 @@ int rp_plain_run(rp_scene* sc, rp_workspace* ws, const double* d_traces, int64_t
         int* d_nill = a.take<int>(nb);
         int* d_ntl = a.take<int>(nb);
         unsigned long long* vmax = a.take<unsigned long long>(nb);
-        unsigned long long* dmin = a.take<unsigned long long>(nb);
         int* idx = a.take<int>((size_t)nb * nfa);
         double* Itd = a.take<double>((size_t)nb * nfa);
         double* Gi = a.take<double>((size_t)nb * nfa);
@@ -521,14 +519,13 @@ int rp_plain_run(rp_scene* sc, rp_workspace* ws, const double* d_traces, int64_t
 
         g_timer.mark(0, st);
         RP_CUDA(cudaMemsetAsync(vmax, 0, sizeof(unsigned long long) * nb, st));
-        RP_CUDA(cudaMemsetAsync(dmin, 0xff, sizeof(unsigned long long) * nb, st));
         RP_CUDA(cudaMemsetAsync(acc, 0, sizeof(long long) * nb * nr * 2, st));
         RP_CUDA(cudaMemsetAsync(PT, 0, sizeof(C64) * nb * L.tstride * nr, st));
         RP_CUDA(cudaMemsetAsync(PS, 0, sizeof(C64) * nb * L.tstride * nr, st));
         // facets: cull + compaction (geometry_kernels.cu:75-204)
         if (nf > 0) {
             k_cull_count<<<dim3((unsigned)((nf + RP_TILE - 1) / RP_TILE), nb), RP_TILE_THREADS, 0, st>>>(
-                sc->d_facets, nf, trb, sc->dp.ap_rad, fflags, tcnt, dmin);
+                sc->d_facets, nf, trb, sc->dp.ap_rad, fflags, tcnt);
             RP_LAUNCHED();
             compact_flags(fflags, nf, nb, tcnt, d_nill, idx, nfa, true, st);
         } else {
