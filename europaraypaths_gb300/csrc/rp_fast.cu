@@ -180,9 +180,10 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
             fv[F_NX] = (float)nx; fv[F_NY] = (float)ny; fv[F_NZ] = (float)nz;
         }
         fv[F_XI] = xI;
-        fv[F_UX] = (float)ux; fv[F_UY] = (float)uy; fv[F_UZ] = (float)uz;
+        fv[F_UX] = 0.5f * (float)ux; fv[F_UY] = 0.5f * (float)uy; fv[F_UZ] = 0.5f * (float)uz;
         fv[F_PH] = (float)(-2.0 * RP_PI * (ti - floor(ti)));
-        fv[F_VX] = (float)vx; fv[F_VY] = (float)vy; fv[F_VZ] = (float)vz; fv[F_K] = (float)Kf;
+        fv[F_VX] = 0.5f * (float)vx; fv[F_VY] = 0.5f * (float)vy; fv[F_VZ] = 0.5f * (float)vz;
+        fv[F_K] = (float)Kf;
     }
     // interleave with the partner facet j ^ 1 (FacetPair): the even lane
     // writes fields 0-7 of the pair, the odd lane fields 8-15; a missing odd

@@ -39,8 +39,8 @@ using C32 = Cx<float>;
 enum FacetField {
     F_DX, F_DY, F_DZ, F_Q,      // facet - chunk centre, |facet - chunk centre|^2
     F_NX, F_NY, F_NZ, F_XI,     // normal, xI = (Itd - rst) / dr
-    F_UX, F_UY, F_UZ, F_PH,     // u tangent, -2 pi frac(Itd / lam) (radians)
-    F_VX, F_VY, F_VZ, F_K,      // v tangent, K = hoisted amplitude factor
+    F_UX, F_UY, F_UZ, F_PH,     // u tangent / 2, -2 pi frac(Itd / lam) (radians)
+    F_VX, F_VY, F_VZ, F_K,      // v tangent / 2, K = hoisted amplitude factor
     RP_NFIELD,
     F_AU = F_NX, F_AV = F_NY    // orthonormal-frame records
 };
@@ -63,6 +63,8 @@ __device__ __forceinline__ f2 bc(float a) { return make_float2(a, a); }
 __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ f2 mul2(f2 a, f2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ f2 add2(f2 a, f2 b) { return __fadd2_rn(a, b); }
+// Negation, folded by the compiler into the consuming packed instruction.
+__device__ __forceinline__ f2 neg2(f2 a) { return make_float2(-a.x, -a.y); }
 
 // Per chunk: its centre is the trace origin plus cf, exactly (cf is rounded
 // to FP32 first and the centre defined from it), so the pair kernel forms
@@ -239,9 +241,10 @@ __device__ __forceinline__ void pair_eval2(const FacetPair& r, const Anchor& an,
                                            f2& vre, f2& vim) {
     const f2 ONE = bc(1.f), M1 = bc(-1.f);
     const f2 dx = fld<F_DX>(r), dy = fld<F_DY>(r), dz = fld<F_DZ>(r);
-    const f2 nDx = bc(-an.Dx), nDy = bc(-an.Dy), nDz = bc(-an.Dz);
-    const f2 ndd = fma2(nDx, dx, fma2(nDy, dy, mul2(nDz, dz)));  // -D.a
-    const f2 qd = fma2(bc(2.f), ndd, fld<F_Q>(r));               // Ttd^2 - T0^2
+    // m = -2 D: Ttd^2 - T0^2 = |a|^2 - 2 D.a as one chain from |a|^2; the
+    // record's tangents are halved (exactly), so m.(u/2) = -D.u
+    const f2 mx = bc(-2.f * an.Dx), my = bc(-2.f * an.Dy), mz = bc(-2.f * an.Dz);
+    const f2 qd = fma2(mx, dx, fma2(my, dy, fma2(mz, dz, fld<F_Q>(r))));   // Ttd^2 - T0^2
     const f2 d2 = add2(bc(an.T0sq), qd);
     const f2 rinv = make_float2(rsqrt_a(d2.x), rsqrt_a(d2.y));
     const f2 sT = fma2(d2, rinv, bc(an.T0));                     // Ttd + T0
@@ -252,27 +255,29 @@ __device__ __forceinline__ void pair_eval2(const FacetPair& r, const Anchor& an,
         // e = a - D: e.u = a.u - D.u etc. (a.u, a.v from the record), and
         // sin^2(Tth) cos^2(Tph) = (e.v)^2 / d2, sin^2(Tth) sin^2(Tph) =
         // (e.u)^2 / d2 because n, u, v are orthonormal
-        const f2 pc = fma2(nDx, fld<F_UX>(r), fma2(nDy, fld<F_UY>(r), fma2(nDz, fld<F_UZ>(r), fld<F_AU>(r))));
-        const f2 pd = fma2(nDx, fld<F_VX>(r), fma2(nDy, fld<F_VY>(r), fma2(nDz, fld<F_VZ>(r), fld<F_AV>(r))));
+        const f2 pc = fma2(mx, fld<F_UX>(r), fma2(my, fld<F_UY>(r), fma2(mz, fld<F_UZ>(r), fld<F_AU>(r))));
+        const f2 pd = fma2(mx, fld<F_VX>(r), fma2(my, fld<F_VY>(r), fma2(mz, fld<F_VZ>(r), fld<F_AV>(r))));
         const f2 pt = fma2(dx, bc(an.tnx), fma2(dy, bc(an.tny), fma2(dz, bc(an.tnz), bc(an.nDtn))));
         const f2 pcr = mul2(pc, rinv), pdr = mul2(pd, rinv), ptr = mul2(pt, rinv);
         t1 = fma2(pdr, pdr, bc(1e-30f));
         t2 = mul2(pcr, pcr);
         aT = add2(t1, t2);
         const f2 xs = mul2(t1, make_float2(rcp_a(aT.x), rcp_a(aT.y)));
-        const f2 aD = fma2(mul2(ptr, ptr), M1, ONE);
+        const f2 aD = fma2(ptr, neg2(ptr), ONE);
         t3 = mul2(aD, xs);
         t4 = fma2(t3, M1, aD);
     } else {
-        // e = facet - target; only squares of its dot products enter
-        const f2 ex = fma2(nDx, ONE, dx), ey = fma2(nDy, ONE, dy), ez = fma2(nDz, ONE, dz);
+        // e = facet - target; only squares of its dot products enter (and
+        // the in-plane split is a ratio, so the halved tangents cancel)
+        const f2 hf = bc(0.5f);
+        const f2 ex = fma2(mx, hf, dx), ey = fma2(my, hf, dy), ez = fma2(mz, hf, dz);
         const f2 pb = fma2(ex, fld<F_NX>(r), fma2(ey, fld<F_NY>(r), mul2(ez, fld<F_NZ>(r))));
         const f2 pt = fma2(ex, bc(an.tnx), fma2(ey, bc(an.tny), mul2(ez, bc(an.tnz))));
         const f2 pc = fma2(ex, fld<F_UX>(r), fma2(ey, fld<F_UY>(r), mul2(ez, fld<F_UZ>(r))));
         const f2 pd = fma2(ex, fld<F_VX>(r), fma2(ey, fld<F_VY>(r), mul2(ez, fld<F_VZ>(r))));
-        const f2 inv_d2 = mul2(rinv, rinv);
-        aT = fma2(mul2(mul2(pb, pb), inv_d2), M1, ONE);
-        const f2 aD = fma2(mul2(mul2(pt, pt), inv_d2), M1, ONE);
+        const f2 pbr = mul2(pb, rinv), ptr = mul2(pt, rinv);
+        aT = fma2(pbr, neg2(pbr), ONE);
+        const f2 aD = fma2(ptr, neg2(ptr), ONE);
         const f2 X = fma2(pd, pd, bc(1e-30f));
         const f2 h2 = fma2(pc, pc, X);
         const f2 xs = mul2(X, make_float2(rcp_a(h2.x), rcp_a(h2.y)));
