@@ -229,6 +229,51 @@ def run_batch(args, objs, tracks, stream):
             "mix": bands}
 
 
+def run_io(n_facets=200_000, n_traces=200, nr=4096):
+    """Host file I/O of the binary stores against the reference's text formats
+    (seeded synthetic facets; no device work): parse a .fct text file vs map a
+    facet store, and write per-trace "%e %e" text files vs one radargram file."""
+    import shutil
+    import tempfile
+    from europaraypaths_gb300 import fileio, simple_surfaces as ss
+    rng = np.random.default_rng(7)
+    side = int(np.sqrt(n_facets))
+    dom = {"fs": 5.0, "nx": side, "ny": side, "ox": 0.0, "oy": 0.0}
+    facets = ss.surface_arrays(dom, "flat", heights=rng.normal(0.0, 2.0, (side, side)))
+    d = tempfile.mkdtemp()
+    try:
+        txt, store = os.path.join(d, "f.fct"), os.path.join(d, "f.rpf")
+        row = ":".join([",".join(["%.6f"] * 3)] * 4)
+        np.savetxt(txt, facets.T, fmt=row)
+        fileio.write_store(store, facets, fileio.STORE_FACETS)
+        t0 = time.perf_counter()
+        a = fileio.read_facets(txt)
+        t1 = time.perf_counter()
+        with fileio.MappedStore(store, fileio.STORE_FACETS) as m:
+            s = float(m.soa[:, ::4096].sum())        # touch the mapping
+        t2 = time.perf_counter()
+        b = fileio.load_facets(store)
+        t3 = time.perf_counter()
+        assert a.shape == b.shape and np.isfinite(s)
+        rdr = (rng.standard_normal((n_traces, nr)) + 1j * rng.standard_normal((n_traces, nr))).astype(np.complex64)
+        tdir = os.path.join(d, "t")
+        os.makedirs(tdir)
+        t4 = time.perf_counter()
+        for k in range(n_traces):
+            fileio.write_trace(os.path.join(tdir, f"s{k:06d}.txt"), rdr[k])
+        t5 = time.perf_counter()
+        fileio.write_radargram(os.path.join(d, "r.rdr"), rdr)
+        t6 = time.perf_counter()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    nf = facets.shape[1]
+    return {"facets": nf, "text_parse_s": t1 - t0, "store_map_s": t2 - t1, "store_load_copy_s": t3 - t2,
+            "parse_over_load": (t1 - t0) / max(t3 - t2, 1e-9), "traces": n_traces, "nr": nr,
+            "text_traces_write_s": t5 - t4, "radargram_write_s": t6 - t5,
+            "text_over_radargram": (t5 - t4) / max(t6 - t5, 1e-9),
+            "note": "host only; facets generated, written as .fct text and as a facet store"}
+
+
 def run_serving(args, objs, tracks, plain_value):
     """The serving loop: Poisson arrivals of flyby requests over the resident
     scenes (a scene drawn uniformly, 1-8 consecutive interior traces), served
@@ -319,6 +364,7 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--serve-seconds", type=float, default=15.0, help="serving-loop arrivals window (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson request rate, requests/s")
+    ap.add_argument("--no-io", dest="io", action="store_false", help="skip the host file-I/O measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -472,6 +518,11 @@ def main():
                             if simulator.autotune_query(False, d) >= 0}
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(sc, scene, track, args.cpu_targets, 1000)
+        if args.io and world == 1:
+            try:
+                line["io"] = run_io()
+            except Exception as e:
+                line["io"] = {"error": f"{type(e).__name__}: {e}"}
         if world == 1 and (args.batch_scenes > 0 or args.serve_seconds > 0):
             scene.close()
             specs, objs, tracks, t_build = batch_workload(args, local)

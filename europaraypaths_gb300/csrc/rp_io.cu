@@ -17,6 +17,8 @@
 #include <cstring>
 #include <dirent.h>
 #include <string>
+#include <fcntl.h>
+#include <sys/mman.h>
 #include <sys/stat.h>
 #include <unistd.h>
 #include <vector>
@@ -318,5 +320,170 @@ extern "C" int rp_clear_traces(const char* dir, int64_t* removed) {
     }
     closedir(dp);
     if (removed) *removed = k;
+    return RP_OK;
+}
+
+// ------------------------------------------------------------ binary store --
+// The binary replacements of the text formats: one 32-byte header (8-byte
+// magic, record count, column or bin count, element kind), then the data in
+// exactly the in-memory layout of the C ABI, so a store is memory-mapped and
+// handed to rp_scene_create without parsing or copying on the host:
+//   facets  "RPFCT01\0"  n, 12, 0   float64 SoA [12][n]
+//   targets "RPTGT01\0"  n,  7, 0   float64 SoA [7][n]
+//   radargram "RPRDR01\0" ns, nr, k  k = 0 complex64, 1 complex128, [ns][nr]
+// Header fields are little-endian int64, as on both supported hosts.
+namespace {
+
+const char kMagic[3][8] = {{'R', 'P', 'F', 'C', 'T', '0', '1', 0},
+                           {'R', 'P', 'T', 'G', 'T', '0', '1', 0},
+                           {'R', 'P', 'R', 'D', 'R', '0', '1', 0}};
+const int64_t kCols[2] = {12, 7};
+
+struct Header {
+    char magic[8];
+    int64_t n, m, kind;
+};
+static_assert(sizeof(Header) == 32, "binary store header is 32 bytes");
+
+struct Map {        // one read-only mapping of a store file
+    void* base;
+    size_t bytes;
+};
+
+int write_all(const char* path, const Header& h, const void* data, size_t bytes) {
+    FILE* f = fopen(path, "wb");
+    if (!f) { rp_set_error("Could not write %s: %s", path, strerror(errno)); return RP_ERR_IO; }
+    bool ok = fwrite(&h, sizeof(h), 1, f) == 1;
+    if (ok && bytes) ok = fwrite(data, 1, bytes, f) == bytes;
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) { rp_set_error("write error on %s", path); return RP_ERR_IO; }
+    return RP_OK;
+}
+
+int read_header(const char* path, int which, Header* h, size_t* file_bytes) {
+    int rc = check_file(path);
+    if (rc) return rc;
+    File fl(path);
+    if (!fl.f) { rp_set_error("Could not open %s: %s", path, strerror(errno)); return RP_ERR_IO; }
+    if (fread(h, sizeof(*h), 1, fl.f) != 1) { rp_set_error("%s: shorter than a store header", path); return RP_ERR_PARSE; }
+    if (memcmp(h->magic, kMagic[which], 8) != 0) { rp_set_error("%s: not a %s store", path,
+        which == 0 ? "facet" : (which == 1 ? "target" : "radargram")); return RP_ERR_PARSE; }
+    struct stat sb;
+    stat(path, &sb);
+    *file_bytes = (size_t)sb.st_size;
+    return RP_OK;
+}
+
+}  // namespace
+
+// Whether a file starts with a binary store header: 0 facets, 1 targets,
+// 2 radargram, -1 anything else (a text file).
+extern "C" int rp_store_kind(const char* path, int* kind) {
+    if (!path || !kind) { rp_set_error("rp_store_kind: null argument"); return RP_ERR_ARG; }
+    int rc = check_file(path);
+    if (rc) return rc;
+    File fl(path);
+    char m[8];
+    *kind = -1;
+    if (fl.f && fread(m, 1, 8, fl.f) == 8)
+        for (int k = 0; k < 3; ++k)
+            if (memcmp(m, kMagic[k], 8) == 0) *kind = k;
+    return RP_OK;
+}
+
+// Write a facet (kind 0, 12 columns) or target (kind 1, 7 columns) SoA store.
+extern "C" int rp_write_store(const char* path, int kind, const double* soa, int64_t n) {
+    if (!path || (kind != 0 && kind != 1) || n < 0 || (n > 0 && !soa)) {
+        rp_set_error("rp_write_store: bad argument");
+        return RP_ERR_ARG;
+    }
+    Header h;
+    memcpy(h.magic, kMagic[kind], 8);
+    h.n = n; h.m = kCols[kind]; h.kind = 0;
+    return write_all(path, h, soa, sizeof(double) * (size_t)kCols[kind] * (size_t)n);
+}
+
+// Memory-map a facet or target store read-only: *soa points at its [cols][n]
+// float64 data, valid until rp_unmap_store(*handle).
+extern "C" int rp_map_store(const char* path, int kind, const double** soa, int64_t* n, void** handle) {
+    if (!path || (kind != 0 && kind != 1) || !soa || !n || !handle) {
+        rp_set_error("rp_map_store: bad argument");
+        return RP_ERR_ARG;
+    }
+    Header h;
+    size_t fb = 0;
+    int rc = read_header(path, kind, &h, &fb);
+    if (rc) return rc;
+    if (h.n < 0 || h.m != kCols[kind] || h.kind != 0 ||
+        fb != sizeof(Header) + sizeof(double) * (size_t)h.m * (size_t)h.n) {
+        rp_set_error("%s: header (n %lld, columns %lld) does not match the file size %zu", path,
+                     (long long)h.n, (long long)h.m, fb);
+        return RP_ERR_PARSE;
+    }
+    int fd = open(path, O_RDONLY);
+    if (fd < 0) { rp_set_error("Could not open %s: %s", path, strerror(errno)); return RP_ERR_IO; }
+    void* base = mmap(nullptr, fb, PROT_READ, MAP_PRIVATE, fd, 0);
+    close(fd);
+    if (base == MAP_FAILED) { rp_set_error("mmap of %s failed: %s", path, strerror(errno)); return RP_ERR_IO; }
+    Map* m = new Map{base, fb};
+    *soa = reinterpret_cast<const double*>(static_cast<const char*>(base) + sizeof(Header));
+    *n = h.n;
+    *handle = m;
+    return RP_OK;
+}
+
+extern "C" int rp_unmap_store(void* handle) {
+    if (!handle) return RP_OK;
+    Map* m = static_cast<Map*>(handle);
+    munmap(m->base, m->bytes);
+    delete m;
+    return RP_OK;
+}
+
+// The whole radargram as one file: ns traces of nr complex64 (complex128 = 0)
+// or complex128 (complex128 = 1) values, trace-major.
+extern "C" int rp_write_radargram(const char* path, const void* data, int64_t ns, int64_t nr, int complex128) {
+    if (!path || ns < 0 || nr < 0 || (ns * nr > 0 && !data)) {
+        rp_set_error("rp_write_radargram: bad argument");
+        return RP_ERR_ARG;
+    }
+    Header h;
+    memcpy(h.magic, kMagic[2], 8);
+    h.n = ns; h.m = nr; h.kind = complex128 ? 1 : 0;
+    return write_all(path, h, data, (size_t)ns * (size_t)nr * (complex128 ? 16 : 8));
+}
+
+// Shape and element kind of a radargram file.
+extern "C" int rp_radargram_info(const char* path, int64_t* ns, int64_t* nr, int* complex128) {
+    if (!path || !ns || !nr || !complex128) { rp_set_error("rp_radargram_info: null argument"); return RP_ERR_ARG; }
+    Header h;
+    size_t fb = 0;
+    int rc = read_header(path, 2, &h, &fb);
+    if (rc) return rc;
+    const size_t es = h.kind == 1 ? 16 : 8;
+    if (h.n < 0 || h.m < 0 || (h.kind != 0 && h.kind != 1) || fb != sizeof(Header) + (size_t)h.n * (size_t)h.m * es) {
+        rp_set_error("%s: radargram header does not match the file size", path);
+        return RP_ERR_PARSE;
+    }
+    *ns = h.n; *nr = h.m; *complex128 = (int)h.kind;
+    return RP_OK;
+}
+
+// Read a radargram file into data (ns x nr of the file's element kind).
+extern "C" int rp_read_radargram(const char* path, void* data, int64_t ns, int64_t nr, int complex128) {
+    int64_t fns, fnr;
+    int fk;
+    int rc = rp_radargram_info(path, &fns, &fnr, &fk);
+    if (rc) return rc;
+    if (!data || fns != ns || fnr != nr || fk != (complex128 ? 1 : 0)) {
+        rp_set_error("rp_read_radargram: the buffer does not match %s", path);
+        return RP_ERR_ARG;
+    }
+    File fl(path);
+    const size_t bytes = (size_t)ns * (size_t)nr * (fk ? 16 : 8);
+    if (fseek(fl.f, (long)sizeof(Header), SEEK_SET) != 0 || (bytes && fread(data, 1, bytes, fl.f) != bytes)) {
+        rp_set_error("read error on %s", path);
+        return RP_ERR_IO;
+    }
     return RP_OK;
 }

@@ -8,7 +8,9 @@ and target files, and the optional source-path, gain-pattern, receive-window
 and attenuation-geometry files named in the JSON.  Writes ``outdir/s%06d.txt``
 ("%e %e" per range bin) for every trace that illuminates at least one facet,
 after removing old ``s*.txt`` files, and prints the run summary with
-traces/s.  Errors are reported with a non-zero exit status instead of an
+traces/s.  Facet and target inputs may also be binary stores (detected by
+their header); ``--radargram PATH`` writes every trace into one radargram
+file instead of the text files.  Errors are reported with a non-zero exit status instead of an
 abort.  ``debug_surface`` dumps are not produced.
 """
 import argparse
@@ -50,8 +52,8 @@ def load_inputs(params_path, facets_path, targets_path):
     rfile = j.get("rx_window_position_file", "NONE")
     if rfile != "NONE":
         rx = fileio.read_rx_window(rfile, ns)
-    targets = fileio.read_targets(targets_path)
-    facets = fileio.read_facets(facets_path)
+    targets = fileio.load_targets(targets_path)
+    facets = fileio.load_facets(facets_path)
     prisms = None
     afile = j.get("attenuation_geometry_file", "NONE")
     if afile != "NONE":
@@ -77,7 +79,7 @@ def pick_form(p, targets):
     return "fast" if default_mode and not ttype0 else "plain"
 
 
-def run(params_path, facets_path, targets_path, outdir, form="auto", batch=64, quiet=False):
+def run(params_path, facets_path, targets_path, outdir, form="auto", batch=64, quiet=False, radargram=None):
     t0 = time.perf_counter()
     fileio.check_directory(outdir)
     p, facets, targets, prisms, tr = load_inputs(params_path, facets_path, targets_path)
@@ -85,11 +87,18 @@ def run(params_path, facets_path, targets_path, outdir, form="auto", batch=64, q
         form = pick_form(p, np.asarray(targets).reshape(7, -1))
     from .simulator import Scene
     scene = Scene(p, facets, targets, prisms=prisms)
-    fileio.clear_traces(outdir)
     ns = tr.shape[0]
     written = 0
+    if radargram is not None:
+        rdr = np.zeros((ns, scene.nr), np.complex64)
+    else:
+        fileio.clear_traces(outdir)
     for s0 in range(0, ns, batch):
         out, counts = scene.simulate(tr[s0:s0 + batch], form=form, return_counts=True)
+        if radargram is not None:      # every trace, zero where nothing is illuminated
+            rdr[s0:s0 + out.shape[0]] = out
+            written += int(np.count_nonzero(counts[:, 0]))
+            continue
         for k in range(out.shape[0]):
             if counts[k, 0] == 0:
                 if not quiet:
@@ -98,6 +107,8 @@ def run(params_path, facets_path, targets_path, outdir, form="auto", batch=64, q
             fileio.write_trace(os.path.join(outdir, f"s{s0 + k:06d}.txt"), out[k])
             written += 1
     scene.close()
+    if radargram is not None:
+        fileio.write_radargram(radargram, rdr)
     dt = time.perf_counter() - t0
     if not quiet:
         print("=== Run summary ===")
@@ -116,9 +127,10 @@ def main(argv=None):
     ap.add_argument("outdir")
     ap.add_argument("--form", default="auto", choices=["auto", "fast", "plain"])
     ap.add_argument("--batch", type=int, default=64, help="traces per engine call")
+    ap.add_argument("--radargram", default=None, help="write one radargram file (all traces) instead of s*.txt")
     a = ap.parse_args(argv)
     try:
-        run(a.params, a.facets, a.targets, a.outdir, form=a.form, batch=a.batch)
+        run(a.params, a.facets, a.targets, a.outdir, form=a.form, batch=a.batch, radargram=a.radargram)
     except (_abi.RaypathError, KeyError, ValueError) as e:
         print(f"sim: {e}", file=sys.stderr)
         return 1

@@ -40,25 +40,27 @@ def prisms_from_conductivity(p, prisms_cond):
 
 
 class Scene:
-    """A resident scene: facets (12, N), targets (7, T), prisms (7, P) with alpha."""
+    """A resident scene: facets (12, N), targets (7, T), prisms (7, P) with alpha.
+
+    The library copies what it needs at creation; the scene keeps no
+    reference to the host arrays (which may be a store's memory mapping)."""
 
     def __init__(self, params, facets, targets=None, prisms=None, device=0):
         self.params = _as_params(params)
-        self.facets = np.ascontiguousarray(facets, dtype=np.float64).reshape(12, -1)
+        facets = np.ascontiguousarray(facets, dtype=np.float64).reshape(12, -1)
         if targets is None:
             targets = np.zeros((7, 0))
-        self.targets = np.ascontiguousarray(targets, dtype=np.float64).reshape(7, -1)
+        targets = np.ascontiguousarray(targets, dtype=np.float64).reshape(7, -1)
         if prisms is None:
             prisms = np.zeros((7, 0))
-        self.prisms = np.ascontiguousarray(prisms, dtype=np.float64).reshape(7, -1)
+        prisms = np.ascontiguousarray(prisms, dtype=np.float64).reshape(7, -1)
+        self.nf, self.nt, self.np = facets.shape[1], targets.shape[1], prisms.shape[1]
         self.nr = int(self.params.nr)
         self.device = int(device)
         self._h = ctypes.c_void_p()
         lib = _abi.lib()
-        rc = lib.rp_scene_create(ctypes.byref(self.params), self.facets.ctypes.data,
-                                 self.facets.shape[1], self.targets.ctypes.data,
-                                 self.targets.shape[1], self.prisms.ctypes.data,
-                                 self.prisms.shape[1], int(device), ctypes.byref(self._h))
+        rc = lib.rp_scene_create(ctypes.byref(self.params), facets.ctypes.data, self.nf, targets.ctypes.data,
+                                 self.nt, prisms.ctypes.data, self.np, int(device), ctypes.byref(self._h))
         _abi.check("rp_scene_create", rc)
 
     @property

@@ -310,6 +310,32 @@ int rp_read_prisms(const char* path, const rp_params* p, double* soa, int64_t ca
  * Replaces saveSignalToFile, src/CUDA/file_io.cu:284-296. */
 int rp_write_trace(const char* path, const float* re_im, int64_t nr);
 
+/* ---- binary stores (the text formats' replacements) -------------------
+ * No counterpart in the reference, which parses text with sscanf
+ * (loadFacetFile / loadTargetFile, src/CUDA/file_io.cu:337-426) and writes
+ * one text file per trace (saveSignalToFile, file_io.cu:284-296).  A store
+ * is a 32-byte header (8-byte magic, int64 record count, int64 column or
+ * bin count, int64 element kind) followed by the data in the C ABI's own
+ * layout: facets "RPFCT01" [12][n] float64 SoA, targets "RPTGT01" [7][n]
+ * float64 SoA, radargram "RPRDR01" [ns][nr] complex64 (kind 0) or
+ * complex128 (kind 1). */
+
+/* *kind = 0 facet store, 1 target store, 2 radargram, -1 other (text). */
+int rp_store_kind(const char* path, int* kind);
+
+/* Write a facet (kind 0) or target (kind 1) store of n records. */
+int rp_write_store(const char* path, int kind, const double* soa, int64_t n);
+
+/* Memory-map a facet or target store read-only; *soa stays valid (and may
+ * be passed to rp_scene_create) until rp_unmap_store(*handle). */
+int rp_map_store(const char* path, int kind, const double** soa, int64_t* n, void** handle);
+int rp_unmap_store(void* handle);
+
+/* The whole radargram in one file, trace-major. */
+int rp_write_radargram(const char* path, const void* data, int64_t ns, int64_t nr, int complex128);
+int rp_radargram_info(const char* path, int64_t* ns, int64_t* nr, int* complex128);
+int rp_read_radargram(const char* path, void* data, int64_t ns, int64_t nr, int complex128);
+
 /* The output directory must exist.  Replaces checkDirectoryExists,
  * src/CUDA/file_io.cu:266-281. */
 int rp_check_directory(const char* path);

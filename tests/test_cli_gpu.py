@@ -73,3 +73,27 @@ def test_cli_main_errors(built_lib, tmp_path):
     with contextlib.redirect_stderr(io.StringIO()):
         assert sim.main([str(tmp_path / "nope.json"), "f", "t", str(tmp_path)]) == 1
         assert sim.main(["p", "f", "t", str(tmp_path / "missing_dir")]) == 1
+
+
+def test_cli_binary_stores_and_radargram_file(built_lib, tmp_path):
+    # the same run from binary stores into one radargram file gives the
+    # traces the text path writes (to their 7 significant digits)
+    from europaraypaths_gb300 import fileio, sim
+    d = str(tmp_path)
+    _scene_files(d)
+    txt = os.path.join(d, "txt")
+    os.makedirs(txt)
+    args = [os.path.join(d, "params.json"), os.path.join(d, "facets.fct"), os.path.join(d, "targets.txt")]
+    with contextlib.redirect_stdout(io.StringIO()):
+        sim.run(*args, txt, form="fast")
+        rdr_txt = oh.compile_rdrgrm(txt, {"ns": 4})
+    assert fileio.main([args[1], os.path.join(d, "facets.rpf")]) == 0
+    assert fileio.main([args[2], os.path.join(d, "targets.rpt"), "--kind", "targets"]) == 0
+    rfile = os.path.join(d, "all.rdr")
+    with contextlib.redirect_stdout(io.StringIO()):
+        n = sim.run(args[0], os.path.join(d, "facets.rpf"), os.path.join(d, "targets.rpt"), d, form="fast",
+                    radargram=rfile)
+    assert n == 4
+    rdr = fileio.read_radargram(rfile)
+    assert rdr.shape == (4, rdr_txt.shape[0]) and rdr.dtype == np.complex64
+    assert rel_l2(rdr, rdr_txt.T) < 1e-6

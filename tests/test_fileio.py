@@ -101,3 +101,59 @@ def test_cli_input_loading(built_lib, tmp_path):
                                                      os.path.join(d, "t.txt"))
     assert facets.shape == (12, 400) and targets.shape == (7, 400) and prisms is None
     assert np.allclose(tr, tr_mod.linear_track(p))
+
+
+def test_binary_store_round_trip_and_kind(built_lib, tmp_path):
+    sc = tiny_scene()
+    fp, tp, xp = str(tmp_path / "f.rpf"), str(tmp_path / "t.rpt"), str(tmp_path / "x.txt")
+    fileio.write_store(fp, sc["facets"], fileio.STORE_FACETS)
+    fileio.write_store(tp, sc["targets"], fileio.STORE_TARGETS)
+    open(xp, "w").write("1,2,3\n")
+    assert [fileio.store_kind(p) for p in (fp, tp, xp)] == [0, 1, -1]
+    assert os.path.getsize(fp) == 32 + 8 * sc["facets"].size
+    with fileio.MappedStore(fp, fileio.STORE_FACETS) as m:
+        assert m.soa.shape == sc["facets"].shape and not m.soa.flags.writeable
+        assert np.array_equal(m.soa, sc["facets"])
+    assert np.array_equal(fileio.load_targets(tp), sc["targets"])
+    assert np.array_equal(fileio.load_targets(xp), fileio.read_targets(xp))
+
+
+def test_text_to_store_conversion_is_exact(built_lib, tmp_path):
+    txt = os.path.join(G, "surface_concave.fct")
+    dst = str(tmp_path / "c.rpf")
+    assert fileio.main([txt, dst]) == 0
+    assert np.array_equal(fileio.load_facets(dst), fileio.read_facets(txt))
+    tdst = str(tmp_path / "c.rpt")
+    assert fileio.main([os.path.join(G, "targets_flat.txt"), tdst, "--kind", "targets"]) == 0
+    assert np.array_equal(fileio.load_targets(tdst), fileio.read_targets(os.path.join(G, "targets_flat.txt")))
+
+
+def test_binary_store_errors(built_lib, tmp_path):
+    sc = tiny_scene()
+    fp = str(tmp_path / "f.rpf")
+    fileio.write_store(fp, sc["facets"], fileio.STORE_FACETS)
+    with pytest.raises(_abi.RaypathError) as e:          # a facet store is not a target store
+        fileio.MappedStore(fp, fileio.STORE_TARGETS)
+    assert e.value.rc == -3
+    data = open(fp, "rb").read()
+    open(fp, "wb").write(data[:-8])                       # truncated
+    with pytest.raises(_abi.RaypathError) as e:
+        fileio.MappedStore(fp, fileio.STORE_FACETS)
+    assert e.value.rc == -3 and "file size" in str(e.value)
+    with pytest.raises(_abi.RaypathError) as e:
+        fileio.MappedStore(str(tmp_path / "missing.rpf"), fileio.STORE_FACETS)
+    assert e.value.rc == -2
+
+
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+def test_radargram_file_round_trip(built_lib, tmp_path, dtype):
+    rng = np.random.default_rng(4)
+    rdr = (rng.standard_normal((5, 33)) + 1j * rng.standard_normal((5, 33))).astype(dtype)
+    p = str(tmp_path / "r.rdr")
+    fileio.write_radargram(p, rdr)
+    assert fileio.store_kind(p) == fileio.STORE_RADARGRAM
+    got = fileio.read_radargram(p)
+    assert got.dtype == dtype and np.array_equal(got, rdr)
+    empty = str(tmp_path / "e.rdr")
+    fileio.write_radargram(empty, np.zeros((0, 8), np.complex64))
+    assert fileio.read_radargram(empty).shape == (0, 8)
