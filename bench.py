@@ -274,6 +274,45 @@ def run_io(n_facets=200_000, n_traces=200, nr=4096):
             "note": "host only; facets generated, written as .fct text and as a facet store"}
 
 
+def run_focus(Nr=4096, Na=2000):
+    """Azimuth focusing (focus_rdrgrm) of a radargram the shape of the flyby's
+    (4096 bins x 2000 traces at 5 m, 50 km altitude, 3 deg aperture), seeded
+    synthetic values, end to end through the C ABI (host radargram in and
+    out).  One row also through the NumPy oracle: its rate on the host and the
+    parity of that row."""
+    import importlib
+    from europaraypaths_gb300 import focusing
+    rng = np.random.default_rng(9)
+    rdr = (rng.standard_normal((Nr, Na)) + 1j * rng.standard_normal((Nr, Na))).astype(np.complex64)
+    par = {"rx_window_m": 4096.5 * 299792480 / 4e6 / 4, "rx_window_offset_m": 49000.0, "rx_sample_rate": 4e6,
+           "aperture": 3.0, "spacing": 5.0, "altitude": 50000.0, "eps_1": 1.0, "eps_2": 3.15, "frequency": 9e6}
+    focusing.focus_rdrgrm(rdr[:64], dict(par))                    # warm-up (context, module load)
+    t0 = time.perf_counter()
+    out = focusing.focus_rdrgrm(rdr, dict(par))
+    t1 = time.perf_counter()
+    # algorithmic work: the terms of every pixel's convolution sum
+    macs = 0
+    for i in range(Nr):
+        rr = par["rx_window_m"] * (i / Nr) + par["rx_window_offset_m"]
+        h = int(rr * np.sin(np.radians(par["aperture"])) / par["spacing"])
+        j = np.arange(Na)
+        macs += int((np.minimum(Na, j + h) - np.maximum(0, j - h)).sum())
+    line = {"shape": [Nr, Na], "e2e_s": t1 - t0, "pixels_per_s": Nr * Na / (t1 - t0),
+            "complex_macs_per_s": macs / (t1 - t0), "complex_macs": macs,
+            "note": "host radargram in and out (65 MB each way), geometry and pixels on the device"}
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "oracle"))
+    nf = importlib.import_module("np_focus")
+    row = Nr // 2
+    t2 = time.perf_counter()
+    ref = nf.focus_rdrgrm(rdr.astype(np.complex128), dict(par), st=row, en=row + 1)
+    t3 = time.perf_counter()
+    line["cpu_oracle"] = {"pixels_per_s": 2 * Na / (t3 - t2), "cores": 1, "kind": "port",
+                          "sample": f"rows {row}-{row + 1} of the same radargram (NumPy oracle, one FFT per pixel)"}
+    a, b = out[row:row + 2].astype(np.complex128), ref[row:row + 2]
+    line["row_rel_l2_vs_oracle"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    return line
+
+
 def run_serving(args, objs, tracks, plain_value):
     """The serving loop: Poisson arrivals of flyby requests over the resident
     scenes (a scene drawn uniformly, 1-8 consecutive interior traces), served
@@ -365,6 +404,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=15.0, help="serving-loop arrivals window (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson request rate, requests/s")
     ap.add_argument("--no-io", dest="io", action="store_false", help="skip the host file-I/O measurement")
+    ap.add_argument("--no-focus", dest="focus", action="store_false", help="skip the azimuth-focusing measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -518,6 +558,11 @@ def main():
                             if simulator.autotune_query(False, d) >= 0}
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(sc, scene, track, args.cpu_targets, 1000)
+        if args.focus and world == 1:
+            try:
+                line["focus"] = run_focus()
+            except Exception as e:
+                line["focus"] = {"error": f"{type(e).__name__}: {e}"}
         if args.io and world == 1:
             try:
                 line["io"] = run_io()

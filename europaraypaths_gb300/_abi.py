@@ -114,6 +114,13 @@ _SIGS = {
     "rp_write_trace": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
     "rp_check_directory": ([ctypes.c_char_p], ctypes.c_int),
     "rp_clear_traces": ([ctypes.c_char_p, ctypes.c_void_p], ctypes.c_int),
+    "rp_focus_aperture": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+                           ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p],
+                          ctypes.c_int),
+    "rp_focus_geometry": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rp_focus_center": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p,
+                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
     "rp_store_kind": ([ctypes.c_char_p, ctypes.c_void_p], ctypes.c_int),
     "rp_write_store": ([ctypes.c_char_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64], ctypes.c_int),
     "rp_map_store": ([ctypes.c_char_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],

@@ -310,6 +310,43 @@ int rp_read_prisms(const char* path, const rp_params* p, double* soa, int64_t ca
  * Replaces saveSignalToFile, src/CUDA/file_io.cu:284-296. */
 int rp_write_trace(const char* path, const float* re_im, int64_t nr);
 
+/* ---- azimuth focusing (src/PYTHON/simple_focusing.py) ------------------
+ * The processing step after the simulation.  Radargrams are (Nr range bins,
+ * Na traces), row-major, complex64 (in128/out128 = 0) or complex128 (1), in
+ * host memory; the work runs on the current device, on stream (a
+ * cudaStream_t; NULL = the default stream). */
+typedef struct rp_focus_params {
+    double rx_window_m, rx_window_offset_m, rx_sample_rate;
+    double sin_aperture;    /* sin(aperture in radians), as the caller computes it */
+    double spacing;         /* trace spacing (m) */
+    double altitude;        /* source altitude (m) */
+    double eps_2;           /* subsurface permittivity */
+    double lam;             /* wavelength (m) */
+    double c1;              /* light speed of the slant-range-to-bin conversion (299792458) */
+    double bracket_hi;      /* upper bracket of the refraction angle (radians of 20 degrees) */
+} rp_focus_params;
+
+/* focus_rdrgrm (simple_focusing.py:310-404): every pixel of rows
+ * [row_lo, row_hi] focused over its range row's synthetic aperture; other
+ * rows are zero.  RP_ERR_ARG when a row's refraction angle has no root in
+ * [0, bracket_hi] (the reference's brentq raises there). */
+int rp_focus_aperture(const rp_focus_params* p, const void* rdr, int64_t nr_bins, int64_t na, int in128,
+                      int64_t row_lo, int64_t row_hi, void* out, int out128, void* stream);
+
+/* The per-row geometry of rp_focus_aperture for rows [row0, row0 + nrows):
+ * apt[2 r] = apt_smpl, apt[2 r + 1] = apt_hsmpl, and per aperture sample k
+ * the range bin rb[r * maxA + k] and matched-filter tap mf[2 (r * maxA + k)]
+ * (re, im) -- focus_rdrgrm's return_shifts / return_match_filter. */
+int rp_focus_geometry(const rp_focus_params* p, int64_t nr_bins, int64_t row0, int64_t nrows, int maxA, int* apt,
+                      int* rb, float* mf);
+
+/* full_focus_at_center (simple_focusing.py:115-185) given its per-trace
+ * integer range shifts and matched filter (mf: na complex64 as 2 floats):
+ * range-cell-migration correction by rolls and the azimuth matched filter
+ * at twice the trace count, cropped to na. */
+int rp_focus_center(const void* rdr, int64_t nr_bins, int64_t na, int in128, const int64_t* shifts, const float* mf,
+                    void* out, int out128, void* stream);
+
 /* ---- binary stores (the text formats' replacements) -------------------
  * No counterpart in the reference, which parses text with sscanf
  * (loadFacetFile / loadTargetFile, src/CUDA/file_io.cu:337-426) and writes
