@@ -46,6 +46,7 @@ class RpParams(ctypes.Structure):
         ("ks", _D), ("c_1", _D), ("c_2", _D), ("nu_1", _D), ("nu_2", _D),
         ("alpha1", _D), ("alpha2", _D), ("dr", _D),
         ("nr", _I), ("reserved", _I),
+        ("incoherent_seed", ctypes.c_int64),
     ]
 
     def as_dict(self):

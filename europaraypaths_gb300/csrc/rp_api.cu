@@ -422,13 +422,10 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
     // targets only.  Non-specular without linear convolution writes a 2nr
     // chirp into an nr (or unallocated) buffer (sim.cu:411-438, 851-856), and
     // ttype-1 targets without linear convolution use an unallocated chirp and
-    // temp buffer (sim.cu:864-872, 912): refused.  incoherent draws its
-    // phases from clock64() and is not reproducible: refused.
+    // temp buffer (sim.cu:864-872, 912): refused.  incoherent mode takes its
+    // surface phases from a seeded hash (rp_incoherent_turns) instead of
+    // clock64().
     const bool lin = p->convolution && p->convolution_linear;
-    if (p->incoherent) {
-        rp_set_error("rp_scene_create: incoherent mode is not implemented (clock64 phases)");
-        return RP_ERR_UNSUPPORTED;
-    }
     if (!p->specular && !lin) {
         rp_set_error("rp_scene_create: non-specular mode needs convolution=true, convolution_linear=true");
         return RP_ERR_UNSUPPORTED;
@@ -459,6 +456,8 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
     d.nr = p->nr; d.lossless = p->lossless; d.disable_surface = p->disable_surface;
     d.rerad_funct = p->rerad_funct;
     d.specular = p->specular ? 1 : 0;
+    d.incoherent = p->incoherent ? 1 : 0;
+    d.inc_seed = (unsigned long long)p->incoherent_seed;
     d.cmode = !p->convolution ? 2 : (p->convolution_linear ? 0 : 1);
     d.c_over_c2 = p->c / p->c_2;
     int rc;

@@ -69,7 +69,8 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
            const int* __restrict__ nill, const double* __restrict__ traces, DevParams dp,
            FacetPair* __restrict__ rec, ChunkMeta* __restrict__ meta, int64_t rstride,
            int64_t mstride, float* __restrict__ sx_o, C32* __restrict__ sv_o,
-           unsigned long long* __restrict__ vmax, double* __restrict__ org) {
+           unsigned long long* __restrict__ vmax, double* __restrict__ org,
+           const int64_t* __restrict__ order) {
     __shared__ double shd[32];
     __shared__ float shf[32];
     const int s = blockIdx.y;
@@ -159,7 +160,10 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
         const double tt = 2.0 * d * dp.turn;
         const float ft = (float)(tt - floor(tt));
         float sn, cs;
-        sincospif(-2.f * ft, &sn, &cs);
+        if (dp.incoherent)      // randomPhasor (radar_kernels.cu:741-742), seeded by the facet's input index
+            sincospif(2.f * (float)rp_incoherent_turns(dp.inc_seed, t.sx, t.sy, t.sz, order[i]), &sn, &cs);
+        else
+            sincospif(-2.f * ft, &sn, &cs);
         xI = (float)((d - t.rst) * dp.inv_dr);
         sx_o[(size_t)s * nf + j] = xI;
         sv_o[(size_t)s * nf + j] = C32{amp * cs, amp * sn};
@@ -1060,7 +1064,7 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
         compact_flags(g.fflags, nf, nb, g.tcnt, g.nill, g.idx, nfa, true, st);
         k_facets32<<<dim3((unsigned)Lw.mstride, nb), RP_CHUNK, 0, st>>>(
             sc->d_sorted, nfa, g.idx, g.nill, trb, dp, g.rec, g.meta, Lw.rstride, Lw.mstride, g.sxv, g.sv, g.vmax,
-            g.org);
+            g.org, sc->d_order);
         RP_LAUNCHED();
         k_surf_fix32<<<dim3((unsigned)((nf + 256 * RP_SFIX_PER - 1) / (256 * RP_SFIX_PER)), nb), 256, 0, st>>>(
             nfa, g.nill, g.sxv, g.sv, g.vmax, nr, g.acc);

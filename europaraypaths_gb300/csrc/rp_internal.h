@@ -36,6 +36,8 @@ struct DevParams {
     double lam, fs, P, nidx, eps1, eps2, nu1, nu2, alpha1, alpha2, ks, c1_over_c2;
     double dr, smpl, B, rng_res, ap_rad, ap_cos;
     double inv_dr, sqrt_eps12;   // 1 / dr, sqrt(eps1 / eps2) (fast-form setup)
+    unsigned long long inc_seed; // incoherent mode: the phase hash's seed
+    int incoherent;              // incoherent mode: surface phasors from rp_incoherent_turns
     double turn;   // phase turns per metre of range: pi_F / (pi lam), so that
                    // exp(-j (2 pi_F / lam) r) = exp(-j 2 pi r turn) (radar_kernels.cu:682)
     int nr, lossless, disable_surface, rerad_funct;

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "rp_internal.h"
 
@@ -209,6 +210,32 @@ __device__ Cx<R>* block_dft(Cx<R>* x, Cx<R>* wa, Cx<R>* wb, const PlanV<R>& pl, 
     if (pl.pow2) return block_fft<R>(x, wa, pl.log2M, sign, pl.tw);
     block_bluestein<R>(x, wa, wb, pl.n, pl.log2M, sign, pl.bw, pl.bW, pl.tw);
     return x;
+}
+
+// Incoherent mode's surface phase, in turns: a counter-based hash of (seed,
+// the source position's bits, the facet's index in the scene's input order)
+// made of the SplitMix64 mixing function (Steele, Lea, Flood 2014), its top
+// 24 bits as k / 2^24.  The reference draws the phase from clock64()
+// (randomPhasor, radar_kernels.cu:689-711), which no run reproduces.
+__host__ __device__ __forceinline__ uint64_t rp_mix64(uint64_t z) {
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+__host__ __device__ __forceinline__ uint64_t rp_dbits(double v) {
+#ifdef __CUDA_ARCH__
+    return (uint64_t)__double_as_longlong(v);
+#else
+    uint64_t u;
+    memcpy(&u, &v, sizeof(u));
+    return u;
+#endif
+}
+__host__ __device__ __forceinline__ double rp_incoherent_turns(uint64_t seed, double sx, double sy, double sz,
+                                                               int64_t facet) {
+    const uint64_t key = rp_mix64(rp_mix64(rp_mix64(rp_mix64(seed) ^ rp_dbits(sx)) ^ rp_dbits(sy)) ^ rp_dbits(sz));
+    return (double)(rp_mix64(key ^ (uint64_t)facet) >> 40) * (1.0 / 16777216.0);
 }
 
 __host__ __device__ __forceinline__ int ilog2(int n) {

@@ -50,6 +50,7 @@ size_t noalloc_slot_bytes(int nr, int M) {
 }
 
 struct NoallocArgs {
+    const int64_t* order;   // sorted facet position -> input index (incoherent phases)
     const double* F;      // sorted facet store, FP64 SoA [12][nf]
     int64_t nf;
     const double* traces;
@@ -87,10 +88,14 @@ __device__ __forceinline__ void surface_leg(const NoallocArgs& A, const TraceRow
     double Ps = d_friis(Pf, G, t.grefr, dp.lam, d);
     if (!dp.lossless) Ps *= fre;
     double amp = sqrt(Ps);
-    double tt = 2.0 * d * dp.turn;
-    double ft = tt - floor(tt);
     double sn, cs;
-    sincospi(-2.0 * ft, &sn, &cs);
+    if (dp.incoherent) {        // the seeded phases of incoherent mode (rp_incoherent_turns)
+        sincospi(2.0 * rp_incoherent_turns(dp.inc_seed, t.sx, t.sy, t.sz, A.order[i]), &sn, &cs);
+    } else {
+        double tt = 2.0 * d * dp.turn;
+        double ft = tt - floor(tt);
+        sincospi(-2.0 * ft, &sn, &cs);
+    }
     *x = (float)((d - t.rst) / dp.dr);
     *v = C32{(float)(amp * cs), (float)(amp * sn)};
     *amp_o = amp;
@@ -203,6 +208,7 @@ extern "C" int rp_surface_noalloc(const rp_scene* s, const double* d_traces, int
     }
     NoallocArgs A;
     A.F = s->d_sorted;
+    A.order = s->d_order;
     A.nf = s->nf;
     A.traces = d_traces;
     A.dp = s->dp;

@@ -81,9 +81,13 @@ __global__ void k_incident64(const double* __restrict__ F, int64_t nf, const int
     double Ps = d_friis(Pf, G, t.grefr, dp.lam, d);
     if (!dp.lossless) Ps *= fre;
     double amp = sqrt(Ps);
-    double phs = -(2.0 * RP_PI_F / dp.lam) * (2 * d);
     double sn, cs;
-    sincos(phs, &sn, &cs);
+    if (dp.incoherent) {        // randomPhasor (radar_kernels.cu:741-742), seeded
+        sincospi(2.0 * rp_incoherent_turns(dp.inc_seed, t.sx, t.sy, t.sz, i), &sn, &cs);
+    } else {
+        double phs = -(2.0 * RP_PI_F / dp.lam) * (2 * d);
+        sincos(phs, &sn, &cs);
+    }
     sx_o[o] = (d - t.rst) / dp.dr;
     sv_o[o] = C64{amp * cs, amp * sn};
     atomic_max_pos(vmax + s, amp);

@@ -186,6 +186,7 @@ def to_rp_params(j, derive=True):
     p.specular = int(bool(j["specular"]))
     p.lossless = int(bool(j["lossless"]))
     p.incoherent = int(bool(j.get("incoherent", False)))
+    p.incoherent_seed = int(j.get("incoherent_seed", 1))      # extension: seeded incoherent phases
     p.disable_surface = int(bool(j.get("disable_surface", False)))
     p.debug_surface = int(bool(j.get("debug_surface", False)))
     p.pol = 0

@@ -98,6 +98,13 @@ typedef struct rp_params {
     double dr;                   /* rx_window_m / nr                          */
     int32_t nr;                  /* range bins (float expression file_io.cu:212) */
     int32_t reserved;
+    /* ---- extension ---- */
+    int64_t incoherent_seed;     /* "incoherent_seed" (1): seeds incoherent mode's phases.
+                                  * The reference draws them from clock64()
+                                  * (randomPhasor, radar_kernels.cu:689-711); here the
+                                  * phase of facet i at source (sx, sy, sz) is a
+                                  * counter-based hash of (seed, sx, sy, sz, i) --
+                                  * reproducible, independent of batching. */
 } rp_params;
 
 /* Opaque resident scene (facet store, targets, prisms on the device). */

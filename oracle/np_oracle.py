@@ -185,6 +185,28 @@ def prism_distance(o, d, box, t):
     return out
 
 
+def _mix64(z):
+    """SplitMix64's mixing function on uint64 arrays (wrapping arithmetic)."""
+    with np.errstate(over="ignore"):
+        z = z + np.uint64(0x9e3779b97f4a7c15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xbf58476d1ce4e5b9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94d049bb133111eb)
+        return z ^ (z >> np.uint64(31))
+
+
+def incoherent_turns(seed, S, idx):
+    """Incoherent mode's seeded surface phases in turns (the reference draws
+    them from clock64(), radar_kernels.cu:689-711): SplitMix64 mixing over
+    (seed, the bits of the source position S, the facets' input indices),
+    the top 24 bits as k / 2^24."""
+    bits = np.asarray(S, dtype=np.float64).view(np.uint64)
+    key = _mix64(np.array([seed], dtype=np.uint64))
+    for b in bits:
+        key = _mix64(key ^ b)
+    r = _mix64(key ^ np.asarray(idx, dtype=np.uint64))
+    return (r >> np.uint64(40)).astype(np.float64) / 16777216.0
+
+
 def simulate(p, facets, targets, traces, prisms=None):
     """Run the reference trace loop (sim.cu:615-1008) in FP64.
 
@@ -256,7 +278,11 @@ def simulate(p, facets, targets, traces, prisms=None):
             Ps = Ps * fRe
         if not spec:
             psurf = np.zeros(nr, np.complex128)
-            bin_split_add(psurf, nr, (Itd - rst) / dr, phasor(2 * Itd, lam) * np.sqrt(Ps))
+            if p.get("incoherent", False):      # randomPhasor (radar_kernels.cu:741-742), seeded
+                ph = np.exp(2j * np.pi * incoherent_turns(p["incoherent_seed"], S, np.nonzero(ill)[0]))
+            else:
+                ph = phasor(2 * Itd, lam)
+            bin_split_add(psurf, nr, (Itd - rst) / dr, ph * np.sqrt(Ps))
             if p["disable_surface"]:
                 psurf[:] = 0.0
             refl = conv_linear(psurf, chirp1, nr)
@@ -391,6 +417,8 @@ def derive(j):
     p["dr"] = float(j["rx_window_m"]) / nr
     p["rerad_funct"] = int(j.get("rerad_funct", 1))
     p["lossless"] = bool(j.get("lossless", False))
+    p["incoherent"] = bool(j.get("incoherent", False))
+    p["incoherent_seed"] = int(j.get("incoherent_seed", 1))
     p["disable_surface"] = bool(j.get("disable_surface", False))
     p["specular"] = bool(j.get("specular", False))
     p["convolution"] = bool(j.get("convolution", True))

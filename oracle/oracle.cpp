@@ -76,6 +76,26 @@ inline double radar_eq(double P, double G, double fs, double lam, double d, doub
 }
 
 // radar_kernels.cu:681-686
+// Incoherent mode's seeded surface phase in turns (the reference draws it
+// from clock64(), radar_kernels.cu:689-711): the SplitMix64 mixing function
+// over (seed, the source position's bits, the facet's input index), top 24
+// bits.
+inline uint64_t mix64(uint64_t z) {
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+inline uint64_t dbits(double v) {
+    uint64_t u;
+    std::memcpy(&u, &v, sizeof(u));
+    return u;
+}
+inline double inc_turns(uint64_t seed, double sx, double sy, double sz, int64_t i) {
+    const uint64_t key = mix64(mix64(mix64(mix64(seed) ^ dbits(sx)) ^ dbits(sy)) ^ dbits(sz));
+    return (double)(mix64(key ^ (uint64_t)i) >> 40) / 16777216.0;
+}
+
 inline cd phasor(double r, double lam) {
     double ph = -(2.0 * PI_F / lam) * r;
     return cd(std::cos(ph), std::sin(ph));
@@ -349,7 +369,6 @@ int oracle_simulate(const rp_params* P, const double* facets, int64_t nf,
     // mode (sim.cu:733-986): conv mode 0 linear, 1 circular, 2 none
     const bool spec = p.specular != 0;
     const int cmode = !p.convolution ? 2 : (p.convolution_linear ? 0 : 1);
-    if (p.incoherent) return RP_ERR_UNSUPPORTED;
     if (!spec && cmode != 0) return RP_ERR_UNSUPPORTED;   // chirp written past its buffer (sim.cu:431-438, 851-856)
     if (spec && cmode != 0)
         for (int64_t t = 0; t < nt; ++t)
@@ -429,7 +448,11 @@ int oracle_simulate(const rp_params* P, const double* facets, int64_t nf,
                 double Pf = friis(p.power, grefr, Gi[j], lam, Itd[j]);
                 double Ps = friis(Pf, Gi[j], grefr, lam, Itd[j]);
                 if (!p.lossless) Ps *= fRe[j];
-                split_add(psurf.data(), nr, (Itd[j] - rst) / dr, phasor(2 * Itd[j], lam) * std::sqrt(Ps));
+                // incoherent mode: randomPhasor (radar_kernels.cu:741-742), seeded
+                const cd ph = p.incoherent ? std::polar(1.0, 2.0 * M_PI * inc_turns((uint64_t)p.incoherent_seed,
+                                                                                    sx, sy, sz, ill[j]))
+                                           : phasor(2 * Itd[j], lam);
+                split_add(psurf.data(), nr, (Itd[j] - rst) / dr, ph * std::sqrt(Ps));
             }
             if (p.disable_surface) std::fill(psurf.begin(), psurf.end(), cd(0, 0));
             conv_linear(psurf.data(), C1, nr, refl.data(), buf, wk);

@@ -96,8 +96,7 @@ def test_scene_create_rejects_bad_arguments(built_lib):
 
 @pytest.mark.parametrize("over,ttype", [({"convolution": False}, 1), ({"convolution_linear": False}, 1),
                                         ({"specular": True, "convolution": False}, 1),
-                                        ({"specular": True, "convolution_linear": False}, 1),
-                                        ({"incoherent": True}, 1)])
+                                        ({"specular": True, "convolution_linear": False}, 1)])
 def test_scene_create_refuses_undefined_modes(built_lib, over, ttype):
     # checked before any CUDA call: runs without a GPU
     import ctypes

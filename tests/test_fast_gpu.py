@@ -151,3 +151,11 @@ def test_fast_orthonormal_and_general_frames_agree(built_lib, oracle, monkeypatc
     check(got_o, ref)
     check(got_g, ref)
     assert rel_l2(got_o, got_g) <= 1e-4, rel_l2(got_o, got_g)
+
+
+def test_fast_incoherent_matches_oracle(built_lib, oracle):
+    # incoherent mode (seeded surface phases) in the fast form
+    sc = tiny_scene(incoherent=True, incoherent_seed=5)
+    got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle)
+    assert np.array_equal(cnt, rcnt)
+    check(got, ref)

@@ -131,3 +131,27 @@ def test_oracle_rejects_undefined_modes(oracle, over):
     p, _ = prep(sc, oracle)
     with pytest.raises(RuntimeError, match="-6"):
         oracle.simulate(p, sc["facets"], sc["targets"], tr_mod.linear_track(p))
+
+
+def test_oracle_incoherent_seeded(oracle):
+    # incoherent mode's surface phases come from a seeded hash of (seed,
+    # source position, facet index): the C++ and NumPy oracles agree, a run
+    # repeats exactly, another seed (or coherent mode) differs
+    got, ref, cnt, rcnt = both(tiny_scene(incoherent=True, incoherent_seed=7), oracle)
+    assert np.array_equal(cnt, rcnt) and rel_l2(got, ref) < 1e-12
+    assert np.array_equal(both(tiny_scene(incoherent=True, incoherent_seed=7), oracle)[0], got)
+    assert rel_l2(both(tiny_scene(incoherent=True, incoherent_seed=8), oracle)[0], got) > 1e-2
+    assert rel_l2(both(tiny_scene(), oracle)[0], got) > 1e-2
+    # a trace's result does not depend on the other traces of the call
+    sc = tiny_scene(incoherent=True, incoherent_seed=7)
+    p, _ = prep(sc, oracle)
+    tr = tr_mod.linear_track(p)
+    one, _ = oracle.simulate(p, sc["facets"], sc["targets"], tr[1:2])
+    assert np.array_equal(one[0], got[1])
+
+
+def test_incoherent_turns_distribution():
+    # the 24-bit phases are uniform on [0, 1): mean and variance of 1e5 draws
+    t = np_oracle.incoherent_turns(3, np.array([0.0, 1.0, 2.5e4]), np.arange(100000))
+    assert t.min() >= 0.0 and t.max() < 1.0
+    assert abs(t.mean() - 0.5) < 5e-3 and abs(t.var() - 1 / 12) < 2e-3

@@ -82,3 +82,11 @@ def test_fast_form_refuses_specular(built_lib):
     with simulator.Scene(sc["params"], sc["facets"], sc["targets"]) as scene:
         with pytest.raises(RuntimeError, match="RP_ERR_UNSUPPORTED|-6"):
             scene.simulate(form="fast")
+
+
+def test_plain_incoherent_matches_oracle(built_lib, oracle):
+    # incoherent mode: the seeded surface phases, FP64 like the oracle
+    sc = tiny_scene(incoherent=True, incoherent_seed=5)
+    got, ref, cnt, rcnt = run_both(sc, oracle)
+    assert np.array_equal(cnt, rcnt)
+    assert rel_l2(got, ref) < 1e-10

@@ -58,3 +58,24 @@ def test_surface_noalloc_matches_resident_fast_form(built_lib):
                                 ctypes.c_void_p(out.data_ptr()), None)
     assert rc == -7 and "at most 16 traces" in _abi.last_error()
     scene.close()
+
+
+def test_surface_noalloc_incoherent_matches_fast_form(built_lib):
+    # incoherent mode's seeded phases key on the facet's input index, which
+    # both entry points recover from the sorted store
+    import torch
+    from europaraypaths_gb300 import _abi, simulator, traces as tr_mod
+
+    sc = tiny_scene(nside=30, ns=3, incoherent=True, incoherent_seed=9)
+    scene = simulator.Scene(sc["params"], sc["facets"], targets=None)
+    tr = tr_mod.linear_track(scene.params)
+    d_tr = torch.from_numpy(np.ascontiguousarray(tr)).cuda()
+    ref = torch.zeros((tr.shape[0], scene.nr), dtype=torch.complex64, device="cuda")
+    scene.simulate_device(d_tr, ref, form="fast")
+    out = torch.zeros_like(ref)
+    _abi.check("rp_surface_noalloc", _abi.lib().rp_surface_noalloc(
+        ctypes.c_void_p(scene.handle), ctypes.c_void_p(d_tr.data_ptr()), tr.shape[0],
+        ctypes.c_void_p(out.data_ptr()), None))
+    torch.cuda.synchronize()
+    assert rel_l2(out.cpu().numpy(), ref.cpu().numpy()) <= TOL
+    scene.close()
