@@ -393,6 +393,34 @@ static int frames_orthonormal(const double* F, int64_t nf) {
     return 1;
 }
 
+// Bounding spheres (centre, radius) of every RP_CULL_TILE consecutive facets
+// of a [12][nf] FP64 store, for the culling kernel's tile test.  The radius
+// is inflated far beyond FP64 rounding so the test stays conservative.
+static std::vector<double> tile_spheres(const double* F, int64_t nf) {
+    const int64_t nt = (nf + RP_CULL_TILE - 1) / RP_CULL_TILE;
+    std::vector<double> out((size_t)4 * nt);
+    for (int64_t t = 0; t < nt; ++t) {
+        const int64_t i0 = t * RP_CULL_TILE, i1 = std::min(nf, i0 + RP_CULL_TILE);
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int64_t i = i0; i < i1; ++i)
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = std::min(lo[a], F[a * nf + i]);
+                hi[a] = std::max(hi[a], F[a * nf + i]);
+            }
+        const double c[3] = {0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2])};
+        double r2 = 0.0;
+        for (int64_t i = i0; i < i1; ++i) {
+            double q = 0.0;
+            for (int a = 0; a < 3; ++a) q += (F[a * nf + i] - c[a]) * (F[a * nf + i] - c[a]);
+            r2 = std::max(r2, q);
+        }
+        const double cn = std::fabs(c[0]) + std::fabs(c[1]) + std::fabs(c[2]);
+        out[4 * t] = c[0]; out[4 * t + 1] = c[1]; out[4 * t + 2] = c[2];
+        out[4 * t + 3] = std::sqrt(r2) * (1.0 + 1e-9) + 1e-9 * (1.0 + cn);
+    }
+    return out;
+}
+
 // Morton order of facet centres (spatial locality for the fast form).
 static uint64_t spread16(uint32_t v) {
     uint64_t x = v & 0xffff;
@@ -494,6 +522,9 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
             for (int64_t i = 0; i < nf; ++i) sorted[(size_t)c * nf + i] = facets[(size_t)c * nf + order[i]];
         if ((rc = upload(&s->d_order, order.data(), sizeof(int64_t) * nf, &s->store_bytes))) return fail(rc);
         if ((rc = upload(&s->d_sorted, sorted.data(), sizeof(double) * 12 * nf, &s->store_bytes))) return fail(rc);
+        const std::vector<double> ts = tile_spheres(sorted.data(), nf), tf = tile_spheres(facets, nf);
+        if ((rc = upload(&s->d_tiles_sorted, ts.data(), sizeof(double) * ts.size(), &s->store_bytes))) return fail(rc);
+        if ((rc = upload(&s->d_tiles_file, tf.data(), sizeof(double) * tf.size(), &s->store_bytes))) return fail(rc);
     }
     if ((rc = build_tables(s))) return fail(rc);
     s->ortho = nf > 0 ? frames_orthonormal(facets, nf) : 0;
@@ -511,7 +542,7 @@ extern "C" int rp_scene_destroy(rp_scene* s) {
     if (!s) return RP_OK;
     cudaSetDevice(s->device);
     if (s->own_stream) cudaStreamSynchronize(s->own_stream);
-    void* ptrs[] = {s->d_facets, s->d_targets, s->d_prisms, s->d_order, s->d_sorted,
+    void* ptrs[] = {s->d_facets, s->d_targets, s->d_prisms, s->d_order, s->d_sorted, s->d_tiles_sorted, s->d_tiles_file,
                     s->d_C1_64, s->d_C2_64, s->d_C1_32, s->d_C2_32, s->d_C2S,
                     s->d_HS, s->d_CR_64, s->d_CR_32};
     for (void* q : ptrs)

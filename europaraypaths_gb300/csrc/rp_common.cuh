@@ -5,7 +5,7 @@
 
 #include "rp_math.cuh"
 
-#define RP_TILE 1024        // elements per compaction tile
+#define RP_TILE RP_CULL_TILE   // elements per compaction tile (and per culling sphere)
 #define RP_TILE_THREADS 256
 
 // Trace row: sx,sy,sz, snx,sny,snz, rst, grefl_lin, grefr_lin.
@@ -77,21 +77,41 @@ __device__ __forceinline__ int block_excl_scan(int v, int* total) {
     return base + x - v;
 }
 
+// Whether every point of a tile's bounding sphere (c, r) lies outside the
+// aperture cone of a trace: the angle of the centre from the look direction
+// minus the sphere's angular radius exceeds the aperture by a margin far
+// above FP64 rounding, so no facet that the exact test keeps is skipped.
+__device__ __forceinline__ bool tile_outside(double4 sph, const TraceRow& t, double ap_rad) {
+    const double vx = sph.x - t.sx, vy = sph.y - t.sy, vz = sph.z - t.sz;
+    const double d = sqrt(vx * vx + vy * vy + vz * vz);
+    if (!(d > sph.w)) return false;
+    const double th = acos(clamp1(-(vx * t.snx + vy * t.sny + vz * t.snz) / d));
+    return th - asin(sph.w / d) > ap_rad + 1e-9;
+}
+
 // Pass 1 of facet culling: the aperture flags and per-tile counts of
-// illuminated facets.  grid (tiles, traces).
+// illuminated facets.  grid (tiles, traces).  With tile spheres (one per
+// RP_TILE facets of the store), a tile wholly outside the cone writes zero
+// flags without reading its positions.
 // pos: x,y,z SoA base (3 arrays of stride nf).
 static __global__ void k_cull_count(const double* __restrict__ pos, int64_t nf,
                                     const double* __restrict__ traces, double ap_rad,
-                                    uint8_t* __restrict__ flags, int* __restrict__ tile_cnt) {
+                                    uint8_t* __restrict__ flags, int* __restrict__ tile_cnt,
+                                    const double4* __restrict__ tiles) {
     const int s = blockIdx.y;
     const TraceRow t = load_trace(traces, s);
     const float ap_cos = cosf((float)ap_rad);   // FP32: far inside the 1e-5 guard band
     const int64_t base = (int64_t)blockIdx.x * RP_TILE;
+    // one thread decides for the block (FP64 transcendentals are slow on this GPU)
+    __shared__ int s_skip;
+    if (threadIdx.x == 0) s_skip = tiles != nullptr && tile_outside(tiles[blockIdx.x], t, ap_rad);
+    __syncthreads();
+    const bool skip = s_skip != 0;
     int cnt = 0;
     for (int k = threadIdx.x; k < RP_TILE; k += blockDim.x) {
         int64_t i = base + k;
         uint8_t f = 0;
-        if (i < nf) {
+        if (i < nf && !skip) {
             double d;       // unused here (the compiler drops its square root)
             f = illuminated_fast(pos[i], pos[nf + i], pos[2 * nf + i], t, ap_rad, ap_cos, &d) ? 1 : 0;
         }

@@ -1059,7 +1059,7 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
     cudaMemsetAsync(g.acc, 0, sizeof(long long) * nb * nr * 2, st);
     if (nf > 0) {
         k_cull_count<<<dim3((unsigned)((nf + RP_TILE - 1) / RP_TILE), nb), RP_TILE_THREADS, 0, st>>>(
-            sc->d_sorted, nf, trb, dp.ap_rad, g.fflags, g.tcnt);
+            sc->d_sorted, nf, trb, dp.ap_rad, g.fflags, g.tcnt, reinterpret_cast<const double4*>(sc->d_tiles_sorted));
         RP_LAUNCHED();
         compact_flags(g.fflags, nf, nb, g.tcnt, g.nill, g.idx, nfa, true, st);
         k_facets32<<<dim3((unsigned)Lw.mstride, nb), RP_CHUNK, 0, st>>>(

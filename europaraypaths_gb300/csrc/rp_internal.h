@@ -21,6 +21,8 @@
 #define RP_FIX_BITS 60
 
 void rp_set_error(const char* fmt, ...);
+#define RP_CULL_TILE 1024   // facets per compaction tile and per culling sphere
+
 int rp_cuda_fail(cudaError_t e, const char* what);
 // Raise fn's dynamic shared-memory limit to at least bytes (never lowers it).
 int rp_allow_dyn_smem(const void* fn, size_t bytes);
@@ -108,6 +110,8 @@ struct rp_scene {
     int any_ttype0 = 0;
     // ---- fast store: spatially sorted facets
     int64_t* d_order = nullptr;          // sorted position -> original index
+    double* d_tiles_sorted = nullptr;    // per RP_CULL_TILE sorted facets: bounding sphere (x, y, z, r)
+    double* d_tiles_file = nullptr;      // the same for the input-order store
     double* d_sorted = nullptr;          // FP64 SoA [12][nf] in sorted order
     // ---- per-scene spectral tables
     DftPlan plan2;                       // length 2 nr (linear chirp convolution)

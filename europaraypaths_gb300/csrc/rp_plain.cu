@@ -529,7 +529,8 @@ int rp_plain_run(rp_scene* sc, rp_workspace* ws, const double* d_traces, int64_t
         // facets: cull + compaction (geometry_kernels.cu:75-204)
         if (nf > 0) {
             k_cull_count<<<dim3((unsigned)((nf + RP_TILE - 1) / RP_TILE), nb), RP_TILE_THREADS, 0, st>>>(
-                sc->d_facets, nf, trb, sc->dp.ap_rad, fflags, tcnt);
+                sc->d_facets, nf, trb, sc->dp.ap_rad, fflags, tcnt,
+                reinterpret_cast<const double4*>(sc->d_tiles_file));
             RP_LAUNCHED();
             compact_flags(fflags, nf, nb, tcnt, d_nill, idx, nfa, true, st);
         } else {

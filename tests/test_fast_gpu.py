@@ -159,3 +159,13 @@ def test_fast_incoherent_matches_oracle(built_lib, oracle):
     got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle)
     assert np.array_equal(cnt, rcnt)
     check(got, ref)
+
+
+def test_fast_narrow_aperture_tile_culling(built_lib, oracle):
+    # a 1-degree aperture over a 40k-facet store: most 1024-facet culling
+    # tiles lie outside the cone and are skipped; the illuminated counts and
+    # the radargram still match the oracle exactly / within tolerance
+    sc = tiny_scene(nside=200, ntside=4, ns=3, aperture=1.0)
+    got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle)
+    assert np.array_equal(cnt, rcnt) and 0 < cnt[:, 0].max() < 40000 // 4
+    check(got, ref)

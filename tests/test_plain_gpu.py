@@ -90,3 +90,11 @@ def test_plain_incoherent_matches_oracle(built_lib, oracle):
     got, ref, cnt, rcnt = run_both(sc, oracle)
     assert np.array_equal(cnt, rcnt)
     assert rel_l2(got, ref) < 1e-10
+
+
+def test_plain_narrow_aperture_tile_culling(built_lib, oracle):
+    # the input-order store's culling tiles (rows of the facet grid)
+    sc = tiny_scene(nside=200, ntside=4, ns=3, aperture=1.0)
+    got, ref, cnt, rcnt = run_both(sc, oracle)
+    assert np.array_equal(cnt, rcnt) and 0 < cnt[:, 0].max() < 40000 // 4
+    assert rel_l2(got, ref) < 1e-10
