@@ -198,9 +198,12 @@ def run_batch(args, objs, tracks, stream):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     launches = 0
+    stage = {}
     for k in range(1, steps):
         _abi.check("rp_simulate_batch", lib.rp_simulate_batch(jobs(k), len(objs), ws.handle, sp))
         launches += simulator.last_launch_count()
+        for key, v in simulator.last_timing().items():
+            stage[key] = stage.get(key, 0.0) + v / (steps - 1)
     torch.cuda.synchronize()
     tb = time.perf_counter() - t0
     pairs = sum(opcount.pairs(np.concatenate(counts[k])) for k in range(1, steps))
@@ -222,7 +225,7 @@ def run_batch(args, objs, tracks, stream):
         bands[key] = bands.get(key, 0) + 1
     return {"value": pairs / tb, "unit": UNIT, "scenes": len(objs), "traces_per_scene_per_step": K,
             "steps": steps - 1, "ms_per_step": 1e3 * tb / (steps - 1), "pairs_per_step": pairs / (steps - 1),
-            "gpu_launches_per_step": launches / (steps - 1),
+            "gpu_launches_per_step": launches / (steps - 1), "stage_ms_per_step": stage,
             "one_scene_per_call": {"value": pairs / ts, "ms_per_step": 1e3 * ts / (steps - 1)},
             "batched_over_one_at_a_time": ts / tb,
             "tuned_multi_cfg": simulator.autotune_query(True),

@@ -596,6 +596,29 @@ extern "C" int rp_simulate_device(rp_scene* s, const double* d_traces, int64_t n
     return run_form(s, &s->ws, d_traces, ns, form, d_out, counts, st);
 }
 
+int rp_workspace::ensure_aux() {
+    if (aux_ready) return RP_OK;
+    for (int k = 0; k < kAux; ++k) {
+        RP_CUDA(cudaStreamCreateWithFlags(&aux[k], cudaStreamNonBlocking));
+        RP_CUDA(cudaEventCreateWithFlags(&ev_join[k], cudaEventDisableTiming));
+    }
+    RP_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    aux_ready = true;
+    return RP_OK;
+}
+
+void rp_workspace::fork(cudaStream_t st) {
+    cudaEventRecord(ev_fork, st);
+    for (int k = 0; k < kAux; ++k) cudaStreamWaitEvent(aux[k], ev_fork, 0);
+}
+
+void rp_workspace::join(cudaStream_t st) {
+    for (int k = 0; k < kAux; ++k) {
+        cudaEventRecord(ev_join[k], aux[k]);
+        cudaStreamWaitEvent(st, ev_join[k], 0);
+    }
+}
+
 extern "C" int rp_workspace_create(int device, rp_workspace** out) {
     if (!out) { rp_set_error("rp_workspace_create: null argument"); return RP_ERR_ARG; }
     *out = new rp_workspace();
@@ -609,6 +632,13 @@ extern "C" int rp_workspace_destroy(rp_workspace* ws) {
     cudaDeviceSynchronize();
     ws->arena.release();
     ws->arena2.release();
+    if (ws->aux_ready) {
+        for (int k = 0; k < rp_workspace::kAux; ++k) {
+            cudaStreamDestroy(ws->aux[k]);
+            cudaEventDestroy(ws->ev_join[k]);
+        }
+        cudaEventDestroy(ws->ev_fork);
+    }
     delete ws;
     return RP_OK;
 }

@@ -1215,7 +1215,16 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     Arena& a = ws->arena;
     a.reset();
     g_timer.mark(0, st);
-    for (Seg& g : segs) seg_setup(g, a, st);
+    // independent segments: their setup chains run concurrently on the
+    // workspace's auxiliary streams (buffers are disjoint arena slices)
+    const bool par = nseg > 1 && ws->ensure_aux() == RP_OK;
+    if (par) {
+        ws->fork(st);
+        for (int i = 0; i < nseg; ++i) seg_setup(segs[i], a, ws->aux[i % rp_workspace::kAux]);
+        ws->join(st);
+    } else {
+        for (Seg& g : segs) seg_setup(g, a, st);
+    }
     RP_CUDA(cudaGetLastError());
     std::vector<int> h_misc(8 * (size_t)nseg);
     for (int i = 0; i < nseg; ++i)
@@ -1337,31 +1346,36 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         RP_LAUNCHED();
     }
     g_timer.mark(3, st);
-    // ---- surface compression and the final sums
-    for (Seg& g : segs) {
+    // ---- surface compression and the final sums (per segment; concurrent
+    // on the auxiliary streams when the wave has several)
+    if (par) ws->fork(st);
+    for (int si = 0; si < nseg; ++si) {
+        Seg& g = segs[si];
+        const cudaStream_t ts = par ? ws->aux[si % rp_workspace::kAux] : st;
         const rp_scene* sc = g.sc;
         const int nr = sc->nr;
-        k_surf_conv32<<<g.nb, 256, 0, st>>>(g.acc, g.nill, g.vmax, sc->dp.disable_surface, nr,
+        k_surf_conv32<<<g.nb, 256, 0, ts>>>(g.acc, g.nill, g.vmax, sc->dp.disable_surface, nr,
                                             (const C32*)sc->d_C1_32, plan_view32(sc->plan2), g.refl, g.sscr,
                                             g.Lw.surf_slot);
         RP_LAUNCHED();
         if (g.cmode <= 2) {
-            if (!g.pairs) RP_CUDA(cudaMemsetAsync(g.part, 0, sizeof(C32) * g.nb * g.nsplit * 2 * nr, st));
+            if (!g.pairs) RP_CUDA(cudaMemsetAsync(g.part, 0, sizeof(C32) * g.nb * g.nsplit * 2 * nr, ts));
             const size_t tsm = g.tscr ? 0 : (size_t)4 * nr * sizeof(C32);
             if (int rc = rp_allow_dyn_smem((const void*)k_trace_m32, tsm)) return rc;
-            k_usum32<<<dim3((2 * nr + 255) / 256, g.nb), 256, 0, st>>>(g.nill, g.ntl, g.part, g.nsplit, 2 * nr);
+            k_usum32<<<dim3((2 * nr + 255) / 256, g.nb), 256, 0, ts>>>(g.nill, g.ntl, g.part, g.nsplit, 2 * nr);
             RP_LAUNCHED();
-            k_trace_m32<<<g.nb, 512, tsm, st>>>(g.nill, g.ntl, g.refl, g.part, g.nsplit, nr,
+            k_trace_m32<<<g.nb, 512, tsm, ts>>>(g.nill, g.ntl, g.refl, g.part, g.nsplit, nr,
                                                  (const Cplx<float>*)sc->d_HS,
                                                  reinterpret_cast<Cplx<float>*>(g.tscr), g.d_out, g.out64,
                                                  (int)g.s0);
         } else {
-            if (!g.pairs) RP_CUDA(cudaMemsetAsync(g.Z, 0, sizeof(C32) * g.nb * g.L.tstride * nr, st));
-            k_sum32<<<dim3((nr + 255) / 256, g.nb), 256, 0, st>>>(g.nill, g.ntl, g.L.tstride, g.refl, g.Z, nr,
+            if (!g.pairs) RP_CUDA(cudaMemsetAsync(g.Z, 0, sizeof(C32) * g.nb * g.L.tstride * nr, ts));
+            k_sum32<<<dim3((nr + 255) / 256, g.nb), 256, 0, ts>>>(g.nill, g.ntl, g.L.tstride, g.refl, g.Z, nr,
                                                                  g.d_out, g.out64, (int)g.s0);
         }
         RP_LAUNCHED();
     }
+    if (par) ws->join(st);
     g_timer.mark(4, st);
     RP_CUDA(cudaGetLastError());
     std::vector<std::vector<int>> cnt(nseg);

@@ -93,6 +93,17 @@ struct rp_workspace {
     int device = 0;
     Arena arena;     // setup buffers
     Arena arena2;    // pair-stage buffers, sized once the target-window width is known
+    // auxiliary streams: the segments of a multi-segment wave run their
+    // (small, independent) setup and tail kernels concurrently on these,
+    // forked from and joined back into the caller's stream by events
+    static const int kAux = 4;
+    cudaStream_t aux[kAux] = {};
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_join[kAux] = {};
+    bool aux_ready = false;
+    int ensure_aux();                                   // create them once (on the current device)
+    void fork(cudaStream_t st);                         // aux streams wait for st
+    void join(cudaStream_t st);                         // st waits for the aux streams
 };
 
 struct rp_scene {
