@@ -18,7 +18,7 @@ launch, divided by the evaluations of that launch); a higher sinc degree
 adds 4 FP32 lane operations per degree, general (non-orthonormal) frames
 about 10:
 
-* FP32 lane operations: 60.4 -- 55 from packed two-lane instructions (one
+* FP32 lane operations: 58.4 -- 53 from packed two-lane instructions (one
   lane per evaluation: anchor distance and Ttd - T0, three direction dot
   products, the four squared sinc arguments, four degree-3 polynomials and
   their product, the attenuation exponent, amplitude, phase, phasor, bin
@@ -26,14 +26,14 @@ about 10:
   and the phase scaling of the special-function sine and cosine).
 * MUFU (special-function) instructions: 6 -- rsqrt (1/Ttd), rcp (dT), rcp
   (the in-plane split), ex2, sin and cos of the phase.
-* All thread instructions: 54.9 -- a packed instruction issues once for two
+* All thread instructions: 53.4 -- a packed instruction issues once for two
   evaluations; plus 4 shared-memory record loads and 4 window accesses per
   evaluation, the floor conversion pair, address arithmetic and the loop.
 """
 
-FP32_OPS_PER_EVAL = 60.4
+FP32_OPS_PER_EVAL = 58.4
 MUFU_PER_EVAL = 6
-INSTR_PER_EVAL = 54.9
+INSTR_PER_EVAL = 53.4
 EVALS_PER_TARGET_PAIR_METRIC = 0.5     # one evaluation covers two metric pairs
 
 # Nominal special-function throughput of a Blackwell SM (results per clock).
