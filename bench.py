@@ -232,6 +232,49 @@ def run_batch(args, objs, tracks, stream):
             "mix": bands}
 
 
+def run_specular(args, sc, track, stream, default_value):
+    """Specular mode with linear convolution on the same large scene and
+    traces: the fast form's specular pair kernel (both refraction legs with
+    their facetReradiation factors, binned as two traces) and compression
+    with the outbound trace; pairs/s over interior traces, CUDA events on the
+    launching stream."""
+    import torch
+    from europaraypaths_gb300 import simulator, opcount
+    p = dict(sc["params"])
+    p["specular"] = True
+    scene = simulator.Scene(p, sc["facets"], sc["targets"], device=torch.cuda.current_device())
+    try:
+        n = args.spec_traces
+        steps = args.spec_steps
+        d_tr = [torch.from_numpy(np.ascontiguousarray(track[900 + k * n:900 + (k + 1) * n])).cuda()
+                for k in range(steps + 1)]
+        d_out = torch.empty((n, scene.nr), dtype=torch.complex64, device="cuda")
+        c = [np.zeros((n, 2), np.int64) for _ in range(steps + 1)]
+        scene.simulate_device(d_tr[0], d_out, form="fast", stream=stream, counts=c[0])   # warm-up, tuning
+        torch.cuda.synchronize()
+        stage = {"setup_ms": 0.0, "pairs_ms": 0.0, "compress_ms": 0.0, "tail_ms": 0.0}
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(1, steps + 1):
+            scene.simulate_device(d_tr[k], d_out, form="fast", stream=stream, counts=c[k])
+            t = simulator.last_timing()
+            for key in stage:
+                stage[key] += t[key] / steps
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        pairs = float(opcount.pairs(np.concatenate(c[1:]))) / steps
+        v = pairs / (ms / 1e3)
+        return {"value": v, "unit": UNIT, "traces_per_step": n, "steps": steps, "ms_per_step": ms,
+                "stage_ms_per_step": stage, "over_default_mode": v / default_value if default_value else None,
+                "pair_cfg": {f"degree_{d}": simulator.autotune_query(False, d, specular=True) for d in (0, 3, 4, 5, 6)
+                             if simulator.autotune_query(False, d, specular=True) >= 0},
+                "note": "same scene and traces as the headline with specular=true, convolution_linear=true"}
+    finally:
+        scene.close()
+
+
 def run_io(n_facets=200_000, n_traces=200, nr=4096):
     """Host file I/O of the binary stores against the reference's text formats
     (seeded synthetic facets; no device work): parse a .fct text file vs map a
@@ -408,6 +451,8 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson request rate, requests/s")
     ap.add_argument("--no-io", dest="io", action="store_false", help="skip the host file-I/O measurement")
     ap.add_argument("--no-focus", dest="focus", action="store_false", help="skip the azimuth-focusing measurement")
+    ap.add_argument("--spec-traces", type=int, default=4, help="traces per step of the specular-mode run (0 = skip)")
+    ap.add_argument("--spec-steps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -561,6 +606,11 @@ def main():
                             if simulator.autotune_query(False, d) >= 0}
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(sc, scene, track, args.cpu_targets, 1000)
+        if args.spec_traces > 0 and world == 1:
+            try:
+                line["specular"] = run_specular(args, sc, track, stream, value)
+            except Exception as e:
+                line["specular"] = {"error": f"{type(e).__name__}: {e}"}
         if args.focus and world == 1:
             try:
                 line["focus"] = run_focus()

@@ -344,8 +344,12 @@ static int build_tables(rp_scene* s) {
             for (size_t i = 0; i < v.size(); ++i) { b[2 * i] = (float)v[i].x; b[2 * i + 1] = (float)v[i].y; }
             return upload(d, b.data(), b.size() * sizeof(float), a);
         };
+        // the targets' chirp: genCenteredChirpPadded(2 rng_res), or the surface
+        // chirp (rng_res) in specular mode, which never regenerates it
+        // (sim.cu:851-856)
+        const double tres = s->dp.specular ? p.rng_res : 2 * p.rng_res;
         std::vector<Cplx<double>> c2(n2), h(M, Cplx<double>{0, 0});
-        for (int i = 0; i < n2; ++i) c2[i] = Cplx<double>{host_sinc((double)(i - nr / 2) * p.dr / (2 * p.rng_res)), 0.0};
+        for (int i = 0; i < n2; ++i) c2[i] = Cplx<double>{host_sinc((double)(i - nr / 2) * p.dr / tres), 0.0};
         host_dif(c2.data(), n2, f, lM);
         // cropSpectrum followed by the inverse N-point DFT is a circular
         // convolution with h[n] = (1/N) sum_{min(k,N-k) <= K} e^{2 pi i k n / N}
@@ -527,7 +531,8 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
         if ((rc = upload(&s->d_tiles_file, tf.data(), sizeof(double) * tf.size(), &s->store_bytes))) return fail(rc);
     }
     if ((rc = build_tables(s))) return fail(rc);
-    s->ortho = nf > 0 ? frames_orthonormal(facets, nf) : 0;
+    // specular mode evaluates cos Tth from the normal: general-frame records
+    s->ortho = (nf > 0 && !p->specular) ? frames_orthonormal(facets, nf) : 0;
     if (const char* v = getenv("RP_PAIR_ORTHO")) s->ortho = s->ortho && atoi(v) != 0;   // 0: general frames
     s->dp.ortho = s->ortho;
     if (const char* v = getenv("RP_PAIR_VARIANT")) s->pair_variant = atoi(v) == 1 ? 1 : 0;

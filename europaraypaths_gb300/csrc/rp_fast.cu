@@ -21,6 +21,14 @@
 //      leg times -1/sqrt(P) (radiateTarget = accumulateTarget with P = 1 and
 //      the phase of rngt - lam/2, radar_kernels.cu:834-892);
 //   5. surface range compression and a fixed-order sum over targets.
+//
+// Specular mode with linear convolution runs the same stages: the surface
+// leg is genReflPhasor's one-bin phasor of the specular energy
+// (radar_kernels.cu:314-346, geometry_kernels.cu:434-446), the pair kernel
+// is k_pairs32s (rp_spec.cu), which bins the outbound leg (with its own
+// facetReradiation factor) into a second trace T2, and compression uses T2
+// as Psour and the surface chirp for both target legs (specular mode never
+// regenerates it, sim.cu:851-856).
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -64,13 +72,26 @@ struct MinOpF { __device__ float operator()(float a, float b) const { return fmi
 struct MaxOpF { __device__ float operator()(float a, float b) const { return fmaxf(a, b); } };
 
 // ------------------------------------------------------ per-facet stage --
+// Specular mode's surface amplitude (genReflPhasor's fRe): facetReradiation
+// at twice the inclination times the radar equation, times rho^2 atm rough
+// (fre), geometry_kernels.cu:434-446; sin 2th = 2 sI cI.
+__device__ __forceinline__ float spec_surface_amp(const DevParams& dp, double grefl, double d, int n, float sI,
+                                                      float cI, float cph, float sph, float fre) {
+    const double fl = dp.fs / dp.lam, s2t = 2.0 * (double)sI * (double)cI;
+    const double v = (dp.fs * dp.fs / dp.lam) * d_sinc(fl * s2t * (double)cph) * d_sinc(-fl * s2t * (double)sph);
+    return (float)(v * v * d_radar_eq(dp.P, grefl, dp.fs, dp.lam, d, (double)n) * (double)fre);
+}
+
+// SPEC: specular mode (the scene's dp.specular), a separate instantiation so
+// the default mode's kernel carries none of its code.
+template <bool SPEC>
 __global__ void __launch_bounds__(RP_CHUNK)
 k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx,
            const int* __restrict__ nill, const double* __restrict__ traces, DevParams dp,
            FacetPair* __restrict__ rec, ChunkMeta* __restrict__ meta, int64_t rstride,
            int64_t mstride, float* __restrict__ sx_o, C32* __restrict__ sv_o,
            unsigned long long* __restrict__ vmax, double* __restrict__ org,
-           const int64_t* __restrict__ order) {
+           const int64_t* __restrict__ order, FacetSpec* __restrict__ spec) {
     __shared__ double shd[32];
     __shared__ float shf[32];
     const int s = blockIdx.y;
@@ -105,6 +126,7 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
         org[4 * s] = ox; org[4 * s + 1] = oy; org[4 * s + 2] = oz; org[4 * s + 3] = 0.0;
     }
     float xI = 0.f, rr = 0.f, amax = 0.f;
+    float spR = 0.f, spC = 1.f, spI = 1.f, spS = 0.f;    // sin/cos Rth, cos/sin Iph (specular records)
     float fv[RP_NFIELD];            // this facet's record fields (FacetField order)
 #pragma unroll
     for (int f = 0; f < RP_NFIELD; ++f) fv[f] = 0.f;
@@ -149,29 +171,40 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
         const float s2 = fabsf(a2) < 3.14159265e-6f ? 1.f : sinf(a2) / a2;
         const float D = (s1 * s2) * (s1 * s2);
         const float G = D * (4.f * (float)RP_PI_F * fsf * fsf) / (lamf * lamf);
-        // surface leg (surfacePT, radar_kernels.cu:714-764): two Friis hops
         const float f4 = (4.f * (float)RP_PI_FRIIS) * (4.f * (float)RP_PI_FRIIS);
         const float grefr = (float)t.grefr;
-        const float hop = lamf * lamf * G * grefr / (f4 * df * df);
-        float Ps = (float)dp.P * hop * hop;
-        if (!dp.lossless) Ps *= fre;
-        const float amp = sqrtf(Ps);
         // phase in turns: phasor(2 Itd) = exp(-j (2 pi_F/lam) 2 Itd) = exp(-j 2 pi tt)
         const double tt = 2.0 * d * dp.turn;
         const float ft = (float)(tt - floor(tt));
-        float sn, cs;
-        if (dp.incoherent)      // randomPhasor (radar_kernels.cu:741-742), seeded by the facet's input index
-            sincospif(2.f * (float)rp_incoherent_turns(dp.inc_seed, t.sx, t.sy, t.sz, order[i]), &sn, &cs);
-        else
-            sincospif(-2.f * ft, &sn, &cs);
+        float sn, cs, amp;
+        if constexpr (SPEC) {
+            // genReflPhasor: fRe exp(+j 4 pi_F Itd / lam)
+            amp = spec_surface_amp(dp, t.grefl, d, n, sI, cI, cph, sph, fre);
+            sincospif(2.f * ft, &sn, &cs);
+            spR = tir ? sinf(1e4f) : sR;
+            spC = cR;
+            spI = cph;
+            spS = sph;
+        } else {
+            // surface leg (surfacePT, radar_kernels.cu:714-764): two Friis hops
+            const float hop = lamf * lamf * G * grefr / (f4 * df * df);
+            float Ps = (float)dp.P * hop * hop;
+            if (!dp.lossless) Ps *= fre;
+            amp = sqrtf(Ps);
+            if (dp.incoherent)      // randomPhasor (radar_kernels.cu:741-742), seeded by the facet's input index
+                sincospif(2.f * (float)rp_incoherent_turns(dp.inc_seed, t.sx, t.sy, t.sz, order[i]), &sn, &cs);
+            else
+                sincospif(-2.f * ft, &sn, &cs);
+        }
         xI = (float)((d - t.rst) * dp.inv_dr);
         sx_o[(size_t)s * nf + j] = xI;
         sv_o[(size_t)s * nf + j] = C32{amp * cs, amp * sn};
-        amax = amp;
-        // hoisted target-leg amplitude: sqrt(P Gr G frc n) lam^2 Dmax / ((4 pi)^2 Itd)
+        amax = fabsf(amp);
+        // hoisted target-leg amplitude: sqrt(P Gr G frc n) lam^2 Dmax / ((4 pi)^2 Itd),
+        // times fs^2 / lam of the reradiation factors in specular mode
         const float Dmax = (4.f * (float)RP_PI_F * fsf * fsf) / (lamf * lamf);
         const float Kf = sqrtf((float)dp.P * grefr * G * (dp.lossless ? 1.f : frc) * (float)dp.nidx) * lamf *
-                         lamf * Dmax / (f4 * df);
+                         lamf * Dmax / (f4 * df) * ((SPEC && !dp.lossless) ? (float)(dp.fs * dp.fs / dp.lam) : 1.f);
         const double ti = d * dp.turn;
         float ddx = (float)(fx - cx), ddy = (float)(fy - cy), ddz = (float)(fz - cz);
         rr = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
@@ -215,6 +248,23 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
                 pr->v[h + i] = make_float4(e[f], o[f], e[f + 1], o[f + 1]);
             }
         }
+        if constexpr (SPEC) {     // the pair's FacetSpec (even lane r, odd lane p)
+            const float m[4] = {spR, spC, spI, spS};
+            float pm[4], e[4], o[4];
+#pragma unroll
+            for (int f = 0; f < 4; ++f) pm[f] = __shfl_xor_sync(0xffffffffu, m[f], 1);
+            const bool odd_ok = lane1 ? ok : pok;
+#pragma unroll
+            for (int f = 0; f < 4; ++f) {
+                e[f] = lane1 ? pm[f] : m[f];
+                o[f] = odd_ok ? (lane1 ? m[f] : pm[f]) : e[f];
+            }
+            if (pair_ok) {
+                FacetSpec* ps = spec + ((size_t)s * rstride + j) / 2;
+                if (lane1) ps->p = make_float4(e[2], o[2], e[3], o[3]);
+                else ps->r = make_float4(e[0], o[0], e[1], o[1]);
+            }
+        }
     }
     // the surface amplitude maximum of the trace: one atomic per chunk
     const float bmax = block_reduce(amax, MaxOpF(), shf);
@@ -253,7 +303,7 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
 __global__ void __launch_bounds__(256) k_surf_fix32(int64_t nf, const int* __restrict__ nill,
                                                     const float* __restrict__ sx, const C32* __restrict__ sv,
                                                     const unsigned long long* __restrict__ vmax, int nr,
-                                                    long long* __restrict__ acc) {
+                                                    long long* __restrict__ acc, int single) {
     __shared__ unsigned long long hist[2 * RP_SFIX_WIN];
     __shared__ int sh_min[32];
     const int s = blockIdx.y;
@@ -284,11 +334,12 @@ __global__ void __launch_bounds__(256) k_surf_fix32(int64_t nf, const int* __res
         double x = sx[(size_t)s * nf + j];
         if (!(x > -1.0) || x >= (double)nr) continue;
         long b = (long)x;
-        double w = x - (double)b;
+        // single (specular, genPhasorTrace): the whole phasor in the truncated bin
+        double w = single ? 0.0 : x - (double)b;
         C32 v = sv[(size_t)s * nf + j];
         const long long q[4] = {llrint((double)v.x * (1.0 - w) * scale), llrint((double)v.y * (1.0 - w) * scale),
                                 llrint((double)v.x * w * scale), llrint((double)v.y * w * scale)};
-        for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < 2 - single; ++h) {
             const long bb = b + h;
             if (h == 1 && bb >= nr) break;
             const long sl = bb - blo;
@@ -392,7 +443,7 @@ k_pairs32(const __grid_constant__ PairArgs A) {
         const int part = item % RP_PARTS;
         const int tb = (item / RP_PARTS) % A.tblocks;
         const int s = item / (RP_PARTS * A.tblocks);
-        pair_item<NT, ILP, ORTHO>(A, s, tb, part, bars, phase);
+        pair_item<NT, ILP, ORTHO, false>(A, s, tb, part, bars, phase);
     }
     RP_PAIR_SMEM_END
 }
@@ -400,11 +451,12 @@ k_pairs32(const __grid_constant__ PairArgs A) {
 // ---------------------------------------------------------- compression --
 // Per (trace, target): T = sum of the facet-range parts (fixed order) placed
 // at its window; Ptarg = linconv(T, chirp2); contribution =
-// convolveComplex(-T/sqrt(P), Ptarg) -> Z row (complex64, dense nr).
+// convolveComplex(-T/sqrt(P), Ptarg) -> Z row (complex64, dense nr).  In
+// specular mode (T2 != null) Psour is -T2/sqrt(P), the outbound leg's trace.
 __global__ void k_conv32(const int* __restrict__ ntl, int64_t tstride, int nb, const int* __restrict__ bt0,
-                         const C32* __restrict__ T, int Wt, C32* __restrict__ Z, const C32* __restrict__ C2,
-                         PlanV<float> p2, PlanV<float> pN, int crop_K, int crop_all, int nr, float sig_scale,
-                         C32* __restrict__ scratch, size_t slot) {
+                         const C32* __restrict__ T, const C32* __restrict__ T2, int Wt, C32* __restrict__ Z,
+                         const C32* __restrict__ C2, PlanV<float> p2, PlanV<float> pN, int crop_K, int crop_all,
+                         int nr, float sig_scale, C32* __restrict__ scratch, size_t slot) {
     C32* base = scratch + (size_t)blockIdx.x * slot;
     const int M = max(1 << p2.log2M, 1 << pN.log2M);
     C32* x = base;
@@ -414,6 +466,7 @@ __global__ void k_conv32(const int* __restrict__ ntl, int64_t tstride, int nb, c
     C32* B = A + M;
     C32* tr = B + M;        // dense nr
     C32* ptarg = tr + nr;   // nr
+    C32* tr2 = ptarg + nr;  // nr (specular)
     const int64_t items = (int64_t)nb * tstride;
     for (int64_t it = blockIdx.x; it < items; it += gridDim.x) {
         const int s = (int)(it / tstride);
@@ -431,10 +484,20 @@ __global__ void k_conv32(const int* __restrict__ ntl, int64_t tstride, int nb, c
                 }
             }
             tr[i] = v;
+            if (T2) {
+                C32 u2{0.f, 0.f};
+                if (o >= 0 && o < Wt)
+                    for (int p = 0; p < RP_PARTS; ++p) {
+                        const C32 u = T2[(((size_t)p * nb + s) * tstride + q) * Wt + o];
+                        u2.x += u.x;
+                        u2.y += u.y;
+                    }
+                tr2[i] = u2;
+            }
         }
         __syncthreads();
         conv_linear_block<float>(tr, C2, p2, nr, x, wa, wb, ptarg, 1.0f);
-        conv_complex_block<float>(tr, ptarg, pN, nr, crop_K, crop_all, A, B, wa, wb,
+        conv_complex_block<float>(T2 ? tr2 : tr, ptarg, pN, nr, crop_K, crop_all, A, B, wa, wb,
                                   Z + ((size_t)s * tstride + q) * nr, sig_scale);
     }
 }
@@ -446,6 +509,7 @@ __global__ void k_conv32(const int* __restrict__ ntl, int64_t tstride, int nb, c
 //   X = DIF(pad T)                         T = sum of the facet-range parts
 //   W = DIT(X * C2)[nr/2 ..] / 2nr         Ptarg (convolvePhasorChirpLinear)
 //   W = DIT(X * DIF(pad Ptarg)) * s / 2nr  u = Psour (*) Ptarg, Psour = s T
+//                                          (specular: X = DIF(pad T2) first)
 //                                          (length N = 2nr - 1: the N-point
 //                                          circular product has no wrap)
 //   W = DIT_M(DIF_M(pad u) * H)            u (*) h, h = IDFT_N(crop mask)
@@ -460,6 +524,7 @@ struct ConvArgs {
     int nb;
     const int* bt0;
     const C32* T;
+    const C32* T2;          // specular mode: the outbound leg's parts (Psour), else null
     int Wt;
     const Cplx<float>* C2s;
     const Cplx<float>* Hs;  // DIF_M(crop kernel) / M
@@ -486,7 +551,7 @@ struct ConvArgs {
 // item's partial row in global memory (same thread, same element, same
 // target order as the registers of mode 0, so every mode gives the same
 // sums).
-template <int KPT, int MODE>
+template <int KPT, int MODE, bool SPEC>
 __global__ void __launch_bounds__(RP_CONV_THREADS, 1)
 k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ start, int njobs,
           unsigned int* work, Cplx<float>* __restrict__ gscr, size_t gslot) {
@@ -525,6 +590,7 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
         // memory, which would otherwise force re-reads of A)
         const Cplx<float>* __restrict__ C2s = A.C2s;
         const C32* __restrict__ T = A.T;
+        const C32* __restrict__ T2 = A.T2;
         const int Wt = A.Wt, nbA = A.nb, nsplit = A.nsplit;
         const int64_t tstride = A.tstride;
         const float sig_scale = A.sig_scale;
@@ -591,6 +657,23 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
                 __syncthreads();
             }
             block_dif_s<float>(W, n2);
+            if constexpr (SPEC) {   // Psour = s T2, the outbound leg's own trace
+                #pragma unroll 8
+                for (int k = tid; k < n2; k += RP_CONV_THREADS) {
+                    Cplx<float> v{0.f, 0.f};
+                    const int o = k - b0;
+                    if (k < nr && o >= 0 && o < Wt) {
+                        for (int p = 0; p < RP_PARTS; ++p) {
+                            const C32 u = T2[(((size_t)p * nbA + s) * tstride + q) * Wt + o];
+                            v.x += u.x;
+                            v.y += u.y;
+                        }
+                    }
+                    X[swz(k)] = v;
+                }
+                __syncthreads();
+                block_dif_s<float>(X, n2);
+            }
             {
                 const float sc = sig_scale / (float)n2;
                 #pragma unroll 8
@@ -759,6 +842,7 @@ void fast_take_setup(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<unsigned long long>(L.nb);              // vmax
     a.template take<int>((size_t)L.nb * nf);                // idx
     a.template take<FacetPair>((size_t)L.nb * L.rstride / 2);    // records (facet pairs)
+    if (sc->dp.specular) a.template take<FacetSpec>((size_t)L.nb * L.rstride / 2);
     a.template take<ChunkMeta>((size_t)L.nb * L.mstride);   // chunk meta
     a.template take<double>((size_t)L.nb * 4);              // trace origins
     a.template take<float>((size_t)L.nb * nf);              // surface x
@@ -802,6 +886,7 @@ int64_t conv_splits(int64_t tstride) { return (tstride + RP_CONV_SPLIT - 1) / RP
 template <class Aa>
 void fast_take_pairs(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<C32>((size_t)RP_PARTS * L.nb * L.tstride * L.Wt);   // T parts
+    if (sc->dp.specular) a.template take<C32>((size_t)RP_PARTS * L.nb * L.tstride * L.Wt);   // T2 parts
     if (conv_mode(sc) <= 2) {
         a.template take<C32>((size_t)L.nb * conv_splits(L.tstride) * 2 * sc->nr);   // per-split sums of u
         if (trace_m_global(sc)) a.template take<C32>((size_t)L.nb * 4 * sc->nr);   // per-trace crop stage
@@ -822,7 +907,7 @@ FastLayout fast_layout(const rp_scene* sc, int nb, int64_t tstride, int Wt) {
     L.rstride = L.mstride * RP_CHUNK;
     L.Wt = std::max(Wt, 1);
     const int M = std::max(sc->plan2.M(), sc->planN.M());
-    L.slot = (size_t)5 * M + 2 * sc->nr;
+    L.slot = (size_t)5 * M + 3 * sc->nr;
     L.surf_slot = (size_t)3 * sc->plan2.M() + sc->nr;
     L.slots = std::max(1, 2 * sc->sm_count);
     return L;
@@ -914,35 +999,46 @@ void sinc_poly(double T, int D, double* mono) {
     }
 }
 
-template <int KPT, int MODE>
+template <int KPT, int MODE, bool SPEC>
 int launch_conv_k(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, size_t csm, int sms, int slots,
                   unsigned int items, unsigned int* work, C32* gscr, size_t gslot, cudaStream_t st) {
-    if (int rc = rp_allow_dyn_smem((const void*)k_conv32s<KPT, MODE>, csm)) return rc;
+    if (int rc = rp_allow_dyn_smem((const void*)k_conv32s<KPT, MODE, SPEC>, csm)) return rc;
     int occ = 0;
-    RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv32s<KPT, MODE>, RP_CONV_THREADS, csm));
+    RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv32s<KPT, MODE, SPEC>, RP_CONV_THREADS, csm));
     int64_t gmax = (int64_t)std::max(occ, 1) * sms;
     if (MODE != 0) gmax = std::min<int64_t>(gmax, slots);      // one scratch slot per block
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(gmax, items));
-    k_conv32s<KPT, MODE><<<grid, RP_CONV_THREADS, csm, st>>>(d_jobs, d_start, njobs, work,
-                                                              reinterpret_cast<Cplx<float>*>(gscr), gslot);
+    k_conv32s<KPT, MODE, SPEC><<<grid, RP_CONV_THREADS, csm, st>>>(d_jobs, d_start, njobs, work,
+                                                                    reinterpret_cast<Cplx<float>*>(gscr), gslot);
     RP_LAUNCHED();
     return RP_OK;
 }
 
 // One compression launch over a job table of one storage mode (modes 1 and
-// 2: at most `slots` blocks, one per slot of the global scratch).
+// 2: at most `slots` blocks, one per slot of the global scratch).  spec: the
+// table's segments are specular (a specular segment has a wave of its own).
+template <bool SPEC>
+int launch_conv32s_t(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, int mode, int max_nr,
+                     size_t csm, int sms, int slots, unsigned int items, unsigned int* work, C32* gscr,
+                     size_t gslot, cudaStream_t st) {
+#define RP_CONV_ARGS d_jobs, d_start, njobs, csm, sms, slots, items, work, gscr, gslot, st
+    if (mode == 1) return launch_conv_k<1, 1, SPEC>(RP_CONV_ARGS);
+    if (mode == 2) return launch_conv_k<1, 2, SPEC>(RP_CONV_ARGS);
+    const int kpt = (max_nr + RP_CONV_THREADS - 1) / RP_CONV_THREADS;
+    if (kpt <= 1) return launch_conv_k<1, 0, SPEC>(RP_CONV_ARGS);
+    if (kpt <= 2) return launch_conv_k<2, 0, SPEC>(RP_CONV_ARGS);
+    if (kpt <= 4) return launch_conv_k<4, 0, SPEC>(RP_CONV_ARGS);
+    return launch_conv_k<8, 0, SPEC>(RP_CONV_ARGS);
+#undef RP_CONV_ARGS
+}
+
 int launch_conv32s(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, int mode, int max_nr,
                    size_t csm, int sms, int slots, unsigned int items, unsigned int* work, C32* gscr,
-                   size_t gslot, cudaStream_t st) {
-#define RP_CONV_ARGS d_jobs, d_start, njobs, csm, sms, slots, items, work, gscr, gslot, st
-    if (mode == 1) return launch_conv_k<1, 1>(RP_CONV_ARGS);
-    if (mode == 2) return launch_conv_k<1, 2>(RP_CONV_ARGS);
-    const int kpt = (max_nr + RP_CONV_THREADS - 1) / RP_CONV_THREADS;
-    if (kpt <= 1) return launch_conv_k<1, 0>(RP_CONV_ARGS);
-    if (kpt <= 2) return launch_conv_k<2, 0>(RP_CONV_ARGS);
-    if (kpt <= 4) return launch_conv_k<4, 0>(RP_CONV_ARGS);
-    return launch_conv_k<8, 0>(RP_CONV_ARGS);
-#undef RP_CONV_ARGS
+                   size_t gslot, bool spec, cudaStream_t st) {
+    return spec ? launch_conv32s_t<true>(d_jobs, d_start, njobs, mode, max_nr, csm, sms, slots, items, work, gscr,
+                                         gslot, st)
+                : launch_conv32s_t<false>(d_jobs, d_start, njobs, mode, max_nr, csm, sms, slots, items, work, gscr,
+                                          gslot, st);
 }
 
 // ---------------------------------------------------------- autotuner ----
@@ -985,10 +1081,12 @@ struct Seg {
     int64_t* h_counts = nullptr;
     int deg = 0;
     const double* coef = nullptr;
+    const double* coefr = nullptr;
     FastLayout Lw, L;
     // setup stage
     uint8_t* fflags; int* tcnt; int* nill; int* ntl; unsigned long long* vmax;
     double* org; int* idx; FacetPair* rec; ChunkMeta* meta; float* sxv; C32* sv; TraceMeta* tm; uint8_t* tflags;
+    FacetSpec* spec = nullptr;     // specular mode
     int* tlist; int* bt0; int* misc; long long* acc; C32* refl; C32* sscr;
     // pair stage
     int Wt = 1;
@@ -996,12 +1094,14 @@ struct Seg {
     int cmode = 0;          // compression storage mode (conv_mode)
     bool pairs = false;
     C32* T = nullptr; C32* Z = nullptr; C32* cscr = nullptr; C32* part = nullptr;
+    C32* T2 = nullptr;      // specular mode: outbound-leg parts
     C32* tscr = nullptr;    // per-trace crop-stage scratch (nr > 4096)
 };
 
 struct SceneConst {
     int deg = 0;
     double coef[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double coefr[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // specular: facetReradiation's sinc on [0, pi fs / lam]
 };
 
 SceneConst scene_const(const rp_scene* sc) {
@@ -1009,6 +1109,10 @@ SceneConst scene_const(const rp_scene* sc) {
     const double pik_d = RP_PI * (RP_PI_F * sc->dp.fs / sc->dp.lam);
     k.deg = sinc_degree(pik_d, sc->pair_variant);
     if (k.deg > 0) sinc_poly(pik_d * pik_d, k.deg, k.coef);
+    // the reradiation argument is at most pi fs / lam < pik: the same degree
+    // fits it at least as well
+    const double pikr = RP_PI * sc->dp.fs / sc->dp.lam;
+    if (k.deg > 0) sinc_poly(pikr * pikr, k.deg, k.coefr);
     return k;
 }
 
@@ -1041,6 +1145,7 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
     g.vmax = a.take<unsigned long long>(nb);
     g.idx = a.take<int>((size_t)nb * nfa);
     g.rec = a.take<FacetPair>((size_t)nb * Lw.rstride / 2);
+    g.spec = dp.specular ? a.take<FacetSpec>((size_t)nb * Lw.rstride / 2) : nullptr;
     g.meta = a.take<ChunkMeta>((size_t)nb * Lw.mstride);
     g.org = a.take<double>((size_t)nb * 4);
     g.sxv = a.take<float>((size_t)nb * nfa);
@@ -1062,12 +1167,12 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
             sc->d_sorted, nf, trb, dp.ap_rad, g.fflags, g.tcnt, reinterpret_cast<const double4*>(sc->d_tiles_sorted));
         RP_LAUNCHED();
         compact_flags(g.fflags, nf, nb, g.tcnt, g.nill, g.idx, nfa, true, st);
-        k_facets32<<<dim3((unsigned)Lw.mstride, nb), RP_CHUNK, 0, st>>>(
+        (dp.specular ? k_facets32<true> : k_facets32<false>)<<<dim3((unsigned)Lw.mstride, nb), RP_CHUNK, 0, st>>>(
             sc->d_sorted, nfa, g.idx, g.nill, trb, dp, g.rec, g.meta, Lw.rstride, Lw.mstride, g.sxv, g.sv, g.vmax,
-            g.org, sc->d_order);
+            g.org, sc->d_order, g.spec);
         RP_LAUNCHED();
         k_surf_fix32<<<dim3((unsigned)((nf + 256 * RP_SFIX_PER - 1) / (256 * RP_SFIX_PER)), nb), 256, 0, st>>>(
-            nfa, g.nill, g.sxv, g.sv, g.vmax, nr, g.acc);
+            nfa, g.nill, g.sxv, g.sv, g.vmax, nr, g.acc, dp.specular);
         RP_LAUNCHED();
         k_tmeta32<<<nb, 256, 0, st>>>(g.meta, Lw.mstride, g.nill, g.tm);
         RP_LAUNCHED();
@@ -1116,6 +1221,15 @@ PairArgs seg_pair_args(const Seg& g) {
     P.kth = (float)ktd; P.ktl = (float)(ktd - (double)P.kth);
     P.kbh = (float)kbd; P.kbl = (float)(kbd - (double)P.kbh);
     P.lossless = dp.lossless;
+    // specular mode; lossless skips the reradiation factors with the rest of
+    // compRefrEnergyIn/Out (a polynomial of 1, or a zero argument)
+    P.spec = g.spec; P.T2 = g.T2;
+    const double pikr = RP_PI * dp.fs / dp.lam;
+    const bool rr = dp.specular && !dp.lossless;
+    for (int k = 0; k < 8; ++k) P.sr[k] = rr ? (float)(g.coefr[k] * std::pow(pikr * pikr, k)) : (k == 0 ? 1.f : 0.f);
+    P.pikr2 = rr ? (float)(pikr * pikr) : 0.f;
+    P.e21 = (float)(dp.eps2 / dp.eps1);
+    P.s2tir = (float)(std::sin(1e4) * std::sin(1e4));
     return P;
 }
 
@@ -1123,7 +1237,7 @@ ConvArgs seg_conv_args(const Seg& g) {
     const rp_scene* sc = g.sc;
     const int nr = sc->nr;
     ConvArgs C;
-    C.ntl = g.ntl; C.tstride = g.L.tstride; C.nb = g.nb; C.bt0 = g.bt0; C.T = g.T; C.Wt = g.Wt;
+    C.ntl = g.ntl; C.tstride = g.L.tstride; C.nb = g.nb; C.bt0 = g.bt0; C.T = g.T; C.T2 = g.T2; C.Wt = g.Wt;
     C.C2s = (const Cplx<float>*)sc->d_C2S; C.Hs = (const Cplx<float>*)sc->d_HS;
     C.nr = nr; C.n2 = 2 * nr; C.N = 2 * nr - 1; C.M = sc->mS;
     C.crop_K = sc->crop_K; C.crop_all = sc->crop_all;
@@ -1138,7 +1252,13 @@ ConvArgs seg_conv_args(const Seg& g) {
 int launch_pairs(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsigned int* d_start,
                  unsigned int* d_work, int cfg, int sms, cudaStream_t st) {
     const size_t pair_smem = RP_PAIR_SMEM_BYTES;
-    if (ps.size() == 1) {
+    if (ps.size() == 1 && ps[0]->sc->dp.specular) {     // specular waves hold one segment
+        const Seg& g = *ps[0];
+        PairArgs P = seg_pair_args(g);
+        P.work = d_work;
+        const int64_t items = (int64_t)g.nb * P.tblocks * RP_PARTS;
+        if (int rc = launch_pairs_spec(g.deg, cfg, P, items, sms, st)) return rc;
+    } else if (ps.size() == 1) {
         const Seg& g = *ps[0];
         PairArgs P = seg_pair_args(g);
         P.work = d_work;
@@ -1163,6 +1283,7 @@ int launch_pairs(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsig
 int zero_pairs(const std::vector<Seg*>& ps, unsigned int* d_work, cudaStream_t st) {
     for (const Seg* g : ps) {
         RP_CUDA(cudaMemsetAsync(g->T, 0, sizeof(C32) * RP_PARTS * g->nb * g->L.tstride * g->Wt, st));
+        if (g->T2) RP_CUDA(cudaMemsetAsync(g->T2, 0, sizeof(C32) * RP_PARTS * g->nb * g->L.tstride * g->Wt, st));
         RP_CUDA(cudaMemsetAsync(g->misc + 1, 0, sizeof(int) * 3, st));
     }
     RP_CUDA(cudaMemsetAsync(d_work, 0, sizeof(unsigned int), st));
@@ -1170,20 +1291,24 @@ int zero_pairs(const std::vector<Seg*>& ps, unsigned int* d_work, cudaStream_t s
 }
 
 // Choose the pair configuration of a wave: the tuned one, or probe all four
-// (each a full launch on this wave's items, outputs re-zeroed after).
+// (two for the specular kernel; each a full launch on this wave's items,
+// outputs re-zeroed after).  Tuned per kind: single kernel (0), multi-job
+// (1) or specular (2), and sinc degree.
 int choose_cfg(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsigned int* d_start,
                unsigned int* d_work, int sms, cudaStream_t st, int* cfg_out) {
-    const int multi = ps.size() > 1 ? 1 : 0;
-    const int deg = multi ? -1 : ps[0]->deg;
-    if (!autotune_on()) { *cfg_out = ps[0]->sc->pair_cfg; return RP_OK; }
+    const bool spec = ps.size() == 1 && ps[0]->sc->dp.specular;
+    const int multi = spec ? 2 : (ps.size() > 1 ? 1 : 0);
+    const int deg = multi == 1 ? -1 : ps[0]->deg;
+    const int ncfg = spec ? 2 : 4;
+    if (!autotune_on()) { *cfg_out = spec ? (ps[0]->sc->pair_cfg & 1) : ps[0]->sc->pair_cfg; return RP_OK; }
     int c = tuned_lookup(multi, deg);
     if (c >= 0) { *cfg_out = c; return RP_OK; }
     cudaEvent_t e0, e1;
     RP_CUDA(cudaEventCreate(&e0));
     RP_CUDA(cudaEventCreate(&e1));
     float best = 1e30f;
-    int bestc = ps[0]->sc->pair_cfg;
-    for (int k = 0; k < 4; ++k) {
+    int bestc = spec ? (ps[0]->sc->pair_cfg & 1) : ps[0]->sc->pair_cfg;
+    for (int k = 0; k < ncfg; ++k) {
         int rc = zero_pairs(ps, d_work, st);
         if (rc) return rc;
         RP_CUDA(cudaEventRecord(e0, st));
@@ -1262,6 +1387,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     b.reset();
     for (Seg& g : segs) {
         g.T = b.take<C32>((size_t)RP_PARTS * g.nb * g.L.tstride * g.Wt);
+        g.T2 = g.sc->dp.specular ? b.take<C32>((size_t)RP_PARTS * g.nb * g.L.tstride * g.Wt) : nullptr;
         if (g.cmode <= 2) {
             g.part = b.take<C32>((size_t)g.nb * g.nsplit * 2 * g.sc->nr);
             g.tscr = trace_m_global(g.sc) ? b.take<C32>((size_t)g.nb * 4 * g.sc->nr) : nullptr;
@@ -1281,8 +1407,10 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         d_cstart[m] = b.take<unsigned int>(cs[m].size() + 1);
     }
     RP_CUDA(cudaMemsetAsync(d_work, 0, sizeof(unsigned int) * 4, st));
-    for (Seg& g : segs)
+    for (Seg& g : segs) {
         RP_CUDA(cudaMemsetAsync(g.T, 0, sizeof(C32) * RP_PARTS * g.nb * g.L.tstride * g.Wt, st));
+        if (g.T2) RP_CUDA(cudaMemsetAsync(g.T2, 0, sizeof(C32) * RP_PARTS * g.nb * g.L.tstride * g.Wt, st));
+    }
     std::vector<PairJob> hp;
     std::vector<unsigned int> hps(1, 0u);
     for (Seg* g : ps) {
@@ -1333,14 +1461,16 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     for (int m = 0; m < 3; ++m) {
         if (cs[m].empty()) continue;
         int rc = launch_conv32s(d_cjobs[m], d_cstart[m], (int)cs[m].size(), m, max_nr[m], csm[m], sms, sms,
-                                hcs[m].back(), d_work + 1 + m, gscr, gslot[m], st);
+                                hcs[m].back(), d_work + 1 + m, gscr, gslot[m], cs[m][0]->sc->dp.specular != 0, st);
         if (rc) return rc;
     }
     for (Seg* g : ps) {
         if (g->cmode <= 2) continue;
         const rp_scene* sc = g->sc;
-        k_conv32<<<g->L.slots, 256, 0, st>>>(g->ntl, g->L.tstride, g->nb, g->bt0, g->T, g->Wt, g->Z,
-                                            (const C32*)sc->d_C2_32, plan_view32(sc->plan2), plan_view32(sc->planN),
+        // the targets' chirp: the surface chirp in specular mode (sim.cu:851-856)
+        k_conv32<<<g->L.slots, 256, 0, st>>>(g->ntl, g->L.tstride, g->nb, g->bt0, g->T, g->T2, g->Wt, g->Z,
+                                            (const C32*)(sc->dp.specular ? sc->d_C1_32 : sc->d_C2_32),
+                                            plan_view32(sc->plan2), plan_view32(sc->planN),
                                             sc->crop_K, sc->crop_all, sc->nr, (float)(-1.0 / std::sqrt(sc->dp.P)),
                                             g->cscr, g->L.slot);
         RP_LAUNCHED();
@@ -1354,7 +1484,8 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         const cudaStream_t ts = par ? ws->aux[si % rp_workspace::kAux] : st;
         const rp_scene* sc = g.sc;
         const int nr = sc->nr;
-        k_surf_conv32<<<g.nb, 256, 0, ts>>>(g.acc, g.nill, g.vmax, sc->dp.disable_surface, nr,
+        // disable_surface has no effect in specular mode (sim.cu:740-772)
+        k_surf_conv32<<<g.nb, 256, 0, ts>>>(g.acc, g.nill, g.vmax, sc->dp.specular ? 0 : sc->dp.disable_surface, nr,
                                             (const C32*)sc->d_C1_32, plan_view32(sc->plan2), g.refl, g.sscr,
                                             g.Lw.surf_slot);
         RP_LAUNCHED();
@@ -1466,9 +1597,9 @@ void next_segment(const rp_scene* sc, const std::vector<int>& ub, int64_t s0, in
 }
 
 int check_scene(const rp_scene* sc) {
-    if (sc->dp.specular || sc->dp.cmode != 0) {
-        rp_set_error("fast form: only the default mode (non-specular, linear convolution); the plain form "
-                     "runs the specular variants");
+    if (sc->dp.cmode != 0) {
+        rp_set_error("fast form: only linear convolution (the default mode and specular with linear "
+                     "convolution); the plain form runs the other specular variants");
         return RP_ERR_UNSUPPORTED;
     }
     if (sc->any_ttype0) {
@@ -1492,7 +1623,7 @@ size_t rp_fast_plan_bytes(const rp_scene* sc, const double* h_traces, int64_t ns
         int64_t tmax;
         size_t bytes;
         next_segment(sc, ub, s0, ns, &nb, &tmax, &bytes);
-        if (wave > 0 && wave + bytes > kFastBudget) {
+        if (wave > 0 && (sc->dp.specular || wave + bytes > kFastBudget)) {     // specular: one segment a wave
             peak = std::max(peak, wave);
             wave = 0;
         }
@@ -1531,7 +1662,10 @@ int rp_fast_batch(const rp_job* jobs, int njobs, rp_workspace* ws, cudaStream_t 
             int64_t tmax;
             size_t bytes;
             next_segment(sc, ub, s0, ns, &nb, &tmax, &bytes);
-            if (!wave.empty() && wave_bytes + bytes > kFastBudget) {
+            // a specular segment runs in a wave of its own (k_pairs32s is a
+            // single-batch kernel)
+            const bool alone = sc->dp.specular || (!wave.empty() && wave[0].sc->dp.specular);
+            if (!wave.empty() && (alone || wave_bytes + bytes > kFastBudget)) {
                 int rc = run_wave(wave, ws, st);
                 if (rc) return rc;
                 wave.clear();
@@ -1548,6 +1682,7 @@ int rp_fast_batch(const rp_job* jobs, int njobs, rp_workspace* ws, cudaStream_t 
             g.h_counts = jobs[j].counts;
             g.deg = kc[j].deg;
             g.coef = kc[j].coef;
+            g.coefr = kc[j].coefr;
             g.Lw = fast_layout(sc, nb, tmax, nr);
             wave.push_back(g);
             wave_bytes += bytes;
@@ -1583,7 +1718,7 @@ int rp_fast_run(rp_scene* sc, rp_workspace* ws, const double* d_traces, int64_t 
         std::vector<Seg> w(1);
         Seg& g = w[0];
         g.sc = sc; g.trb = d_traces + 9 * s0; g.s0 = s0; g.nb = nb; g.tmax = tmax;
-        g.d_out = d_out; g.out64 = 1; g.h_counts = h_counts; g.deg = kc.deg; g.coef = kc.coef;
+        g.d_out = d_out; g.out64 = 1; g.h_counts = h_counts; g.deg = kc.deg; g.coef = kc.coef; g.coefr = kc.coefr;
         g.Lw = fast_layout(sc, nb, tmax, sc->nr);
         rc = run_wave(w, ws, st);
         if (rc) return rc;
@@ -1600,7 +1735,8 @@ extern "C" int rp_autotune(int enable) {
 
 extern "C" int rp_autotune_query(int multi, int degree, int* cfg) {
     if (!cfg) { rp_set_error("rp_autotune_query: null cfg"); return RP_ERR_ARG; }
-    *cfg = tuned_lookup(multi ? 1 : 0, multi ? -1 : degree);
+    const int kind = multi == 2 ? 2 : (multi ? 1 : 0);
+    *cfg = tuned_lookup(kind, kind == 1 ? -1 : degree);
     return RP_OK;
 }
 

@@ -44,19 +44,19 @@ k_pairs32m(const PairJob* __restrict__ jobs, const unsigned int* __restrict__ st
         const int s = li / (RP_PARTS * A.tblocks);
         if (ortho) {
             switch (deg) {
-                case 3: pair_item<3, ILP, true>(A, s, tb, part, bars, phase); break;
-                case 4: pair_item<4, ILP, true>(A, s, tb, part, bars, phase); break;
-                case 5: pair_item<5, ILP, true>(A, s, tb, part, bars, phase); break;
-                case 6: pair_item<6, ILP, true>(A, s, tb, part, bars, phase); break;
-                default: pair_item<0, ILP, true>(A, s, tb, part, bars, phase); break;
+                case 3: pair_item<3, ILP, true, false>(A, s, tb, part, bars, phase); break;
+                case 4: pair_item<4, ILP, true, false>(A, s, tb, part, bars, phase); break;
+                case 5: pair_item<5, ILP, true, false>(A, s, tb, part, bars, phase); break;
+                case 6: pair_item<6, ILP, true, false>(A, s, tb, part, bars, phase); break;
+                default: pair_item<0, ILP, true, false>(A, s, tb, part, bars, phase); break;
             }
         } else {
             switch (deg) {
-                case 3: pair_item<3, ILP, false>(A, s, tb, part, bars, phase); break;
-                case 4: pair_item<4, ILP, false>(A, s, tb, part, bars, phase); break;
-                case 5: pair_item<5, ILP, false>(A, s, tb, part, bars, phase); break;
-                case 6: pair_item<6, ILP, false>(A, s, tb, part, bars, phase); break;
-                default: pair_item<0, ILP, false>(A, s, tb, part, bars, phase); break;
+                case 3: pair_item<3, ILP, false, false>(A, s, tb, part, bars, phase); break;
+                case 4: pair_item<4, ILP, false, false>(A, s, tb, part, bars, phase); break;
+                case 5: pair_item<5, ILP, false, false>(A, s, tb, part, bars, phase); break;
+                case 6: pair_item<6, ILP, false, false>(A, s, tb, part, bars, phase); break;
+                default: pair_item<0, ILP, false, false>(A, s, tb, part, bars, phase); break;
             }
         }
     }

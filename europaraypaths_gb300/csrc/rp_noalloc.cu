@@ -180,6 +180,11 @@ extern "C" int rp_surface_noalloc(const rp_scene* s, const double* d_traces, int
         rp_set_error("rp_surface_noalloc: bad argument");
         return RP_ERR_ARG;
     }
+    if (s->dp.specular) {
+        rp_set_error("rp_surface_noalloc: the default (non-specular) mode only; specular scenes use "
+                     "rp_simulate_device");
+        return RP_ERR_UNSUPPORTED;
+    }
     if (ns == 0) return RP_OK;
     const int nr = s->nr;
     if (ns > RP_NOALLOC_MAX_TRACES || nr > RP_NOALLOC_MAX_BINS) {

@@ -49,6 +49,15 @@ struct __align__(16) FacetPair {
 };
 #define RP_CHUNK_PAIRS (RP_CHUNK / 2)
 
+// Specular mode: the incident leg's refraction angle Rth and azimuth Iph of
+// both facets of a pair, as sines and cosines (facet 0 first in each pair of
+// components).  compRefrEnergyIn/Out take facetReradiation of Rth - Tth and
+// Iph - Tph (geometry_kernels.cu:527-537, 563-570).
+struct __align__(16) FacetSpec {
+    float4 r;   // {sin Rth, sin Rth, cos Rth, cos Rth}
+    float4 p;   // {cos Iph, cos Iph, sin Iph, sin Iph}
+};
+
 // Field f of both facets of a pair.
 template <int F>
 __device__ __forceinline__ float2 fld(const FacetPair& p) {
@@ -155,6 +164,14 @@ struct PairArgs {
     float kth, ktl;     // n / lam (turns per metre) as a double-float
     float kbh, kbl;     // n / dr (bins per metre) as a double-float
     int lossless;
+    // specular mode (k_pairs32s): the inbound and outbound legs differ by
+    // their facetReradiation factors and are binned into separate traces
+    const FacetSpec* spec;  // [nb][rstride / 2], like rec
+    C32* T2;                // outbound-leg parts, laid out like T
+    float sr[8];            // sinc polynomial in a^2 / pikr^2, pikr = pi fs / lam (scaled)
+    float pikr2;            // pikr^2 (special-function path)
+    float e21;              // eps2 / eps1: sin^2 of the outbound Snell angle over sin^2(Tth)
+    float s2tir;            // sin^2(1e4): the reference's total-internal-reflection angle
 };
 
 // A job of the multi-job pair kernel: a batch's arguments and its sinc
@@ -316,6 +333,100 @@ __device__ __forceinline__ void pair_eval2(const FacetPair& r, const Anchor& an,
     xr = fma2(bc(A.kb), dT, add2(fld<F_XI>(r), bc(an.xbase)));
 }
 
+// pair_eval2 for specular mode (general frames): also returns per lane the
+// facetReradiation amplitudes of the two refraction legs, g1 (inbound:
+// Rth - Tth, Iph - Tph) and g2 (outbound: the Snell angle of pi_F - Tth from
+// eps2 to eps1, Tph - Iph), each |sinc * sinc| with sinc(x) = sin(pi x)/(pi x)
+// of (fs/lam) sin(th) cos(ph) and (fs/lam) sin(th) sin(ph); the constant
+// fs^2/lam is part of the record's K.  From the dot products of e = facet -
+// target: cos Tth = e.n / |e|, sin Tth = sqrt(1 - cos^2), and (cos Tph, sin
+// Tph) = -(e.v, e.u) / |(e.v, e.u)|, so cos(Iph - Tph) and sin(Iph - Tph)
+// follow from the record's sines and cosines without angles.  A shift of e.v
+// by -1e-15 (below FP32 resolution for any other value) gives cos Tph = 1 at
+// e.u = e.v = 0, as atan2(0, 0) = 0 does.  Beyond total internal reflection
+// the reference's flag angle 1e4 gives sin^2(1e4).
+template <int NT, bool RED = true>
+__device__ __forceinline__ void pair_eval2s(const FacetPair& r, const FacetSpec& sp, const Anchor& an,
+                                            const PairArgs& A, f2& xr, f2& vre, f2& vim, f2& g1, f2& g2) {
+    const f2 ONE = bc(1.f), M1 = bc(-1.f);
+    const f2 dx = fld<F_DX>(r), dy = fld<F_DY>(r), dz = fld<F_DZ>(r);
+    const f2 mx = bc(-2.f * an.Dx), my = bc(-2.f * an.Dy), mz = bc(-2.f * an.Dz);
+    const f2 qd = fma2(mx, dx, fma2(my, dy, fma2(mz, dz, fld<F_Q>(r))));   // Ttd^2 - T0^2
+    const f2 d2 = add2(bc(an.T0sq), qd);
+    const f2 rinv = make_float2(rsqrt_a(d2.x), rsqrt_a(d2.y));
+    const f2 sT = fma2(d2, rinv, bc(an.T0));
+    const f2 dT = mul2(qd, make_float2(rcp_a(sT.x), rcp_a(sT.y)));
+    const f2 hf = bc(0.5f);
+    const f2 ex = fma2(mx, hf, dx), ey = fma2(my, hf, dy), ez = fma2(mz, hf, dz);
+    const f2 pb = fma2(ex, fld<F_NX>(r), fma2(ey, fld<F_NY>(r), mul2(ez, fld<F_NZ>(r))));
+    const f2 pt = fma2(ex, bc(an.tnx), fma2(ey, bc(an.tny), mul2(ez, bc(an.tnz))));
+    const f2 pc = fma2(ex, fld<F_UX>(r), fma2(ey, fld<F_UY>(r), mul2(ez, fld<F_UZ>(r))));
+    const f2 pd = add2(fma2(ex, fld<F_VX>(r), fma2(ey, fld<F_VY>(r), mul2(ez, fld<F_VZ>(r)))), bc(-1e-15f));
+    const f2 pbr = mul2(pb, rinv), ptr = mul2(pt, rinv);
+    const f2 aT = fma2(pbr, neg2(pbr), ONE);
+    const f2 aD = fma2(ptr, neg2(ptr), ONE);
+    const f2 X = mul2(pd, pd);
+    const f2 h2 = fma2(pc, pc, X);
+    const f2 rh = make_float2(rcp_a(h2.x), rcp_a(h2.y));
+    const f2 xs = mul2(X, rh);
+    const f2 t1 = mul2(aT, xs), t3 = mul2(aD, xs);
+    const f2 t2 = fma2(t1, M1, aT), t4 = fma2(t3, M1, aD);
+    // the reradiation legs: q1 = sin^2(Rth - Tth), q2 = sin^2 of the outbound
+    // Snell angle, cc / ss = cos^2 / sin^2 (Iph - Tph)
+    const f2 sR = make_float2(sp.r.x, sp.r.y), cR = make_float2(sp.r.z, sp.r.w);
+    const f2 cI = make_float2(sp.p.x, sp.p.y), sI = make_float2(sp.p.z, sp.p.w);
+    const f2 aTc = make_float2(fmaxf(aT.x, 1e-30f), fmaxf(aT.y, 1e-30f));
+    const f2 sTh = mul2(aTc, make_float2(rsqrt_a(aTc.x), rsqrt_a(aTc.y)));
+    const f2 st1 = fma2(sR, pbr, mul2(neg2(cR), sTh));
+    const f2 q1 = mul2(st1, st1);
+    const f2 q2r = mul2(bc(A.e21), aT);
+    const f2 q2 = make_float2(q2r.x > 1.f ? A.s2tir : q2r.x, q2r.y > 1.f ? A.s2tir : q2r.y);
+    const f2 cn = fma2(cI, pd, mul2(sI, pc));
+    const f2 sn = fma2(sI, pd, mul2(neg2(cI), pc));
+    const f2 cc = mul2(mul2(cn, cn), rh), ss = mul2(mul2(sn, sn), rh);
+    const f2 u1 = mul2(q1, cc), u2 = mul2(q1, ss), u3 = mul2(q2, cc), u4 = mul2(q2, ss);
+    f2 S;
+    if (NT > 0) {
+        constexpr int D = NT > 0 ? NT : 1;
+        S = mul2(mul2(sinc_poly2<D>(A.sc, t1), sinc_poly2<D>(A.sc, t2)),
+                 mul2(sinc_poly2<D>(A.sc, t3), sinc_poly2<D>(A.sc, t4)));
+        g1 = mul2(sinc_poly2<D>(A.sr, u1), sinc_poly2<D>(A.sr, u2));
+        g2 = mul2(sinc_poly2<D>(A.sr, u3), sinc_poly2<D>(A.sr, u4));
+        if (NT >= 5) {
+            S = make_float2(fabsf(S.x), fabsf(S.y));
+            g1 = make_float2(fabsf(g1.x), fabsf(g1.y));
+            g2 = make_float2(fabsf(g2.x), fabsf(g2.y));
+        }
+    } else {
+        const f2 P2 = bc(A.pik2);
+        const f2 w1 = mul2(t1, P2), w2 = mul2(t2, P2), w3 = mul2(t3, P2), w4 = mul2(t4, P2);
+        float n0 = 1.f, e0 = 1.f, n1 = 1.f, e1 = 1.f;
+        sinc_sfu(w1.x, n0, e0); sinc_sfu(w2.x, n0, e0); sinc_sfu(w3.x, n0, e0); sinc_sfu(w4.x, n0, e0);
+        sinc_sfu(w1.y, n1, e1); sinc_sfu(w2.y, n1, e1); sinc_sfu(w3.y, n1, e1); sinc_sfu(w4.y, n1, e1);
+        S = make_float2(fabsf(__fdividef(n0, e0)), fabsf(__fdividef(n1, e1)));
+        const f2 R2 = bc(A.pikr2);
+        const f2 v1 = mul2(u1, R2), v2 = mul2(u2, R2), v3 = mul2(u3, R2), v4 = mul2(u4, R2);
+        float a0 = 1.f, b0 = 1.f, a1 = 1.f, b1 = 1.f, c0 = 1.f, d0 = 1.f, c1 = 1.f, d1 = 1.f;
+        sinc_sfu(v1.x, a0, b0); sinc_sfu(v2.x, a0, b0); sinc_sfu(v1.y, a1, b1); sinc_sfu(v2.y, a1, b1);
+        sinc_sfu(v3.x, c0, d0); sinc_sfu(v4.x, c0, d0); sinc_sfu(v3.y, c1, d1); sinc_sfu(v4.y, c1, d1);
+        g1 = make_float2(fabsf(__fdividef(a0, b0)), fabsf(__fdividef(a1, b1)));
+        g2 = make_float2(fabsf(__fdividef(c0, d0)), fabsf(__fdividef(c1, d1)));
+    }
+    const f2 e2 = fma2(bc(-A.eks), aT, fma2(bc(A.ealpha), dT, bc(an.eaT0)));
+    const f2 amp = mul2(mul2(fld<F_K>(r), S), mul2(rinv, make_float2(ex2_a(e2.x), ex2_a(e2.y))));
+    f2 ph = fma2(bc(A.kr), dT, add2(fld<F_PH>(r), bc(an.ph0)));
+    if (RED) {
+        const f2 k = mul2(ph, bc(0.159154943091895336f));
+        ph = fma2(make_float2(rintf(k.x), rintf(k.y)), bc(-6.28318530717958647f), ph);
+    }
+    f2 sn2, cs2;
+    __sincosf(ph.x, &sn2.x, &cs2.x);
+    __sincosf(ph.y, &sn2.y, &cs2.y);
+    vre = mul2(amp, cs2);
+    vim = mul2(amp, sn2);
+    xr = fma2(bc(A.kb), dT, add2(fld<F_XI>(r), bc(an.xbase)));
+}
+
 // Attenuation-prism factor for one pair (compTargetRays, geometry_kernels.cu:
 // 317-342): exp2 of the change of the exponent from alpha2 * Ttd to
 // sum(alpha_p d_p) + alpha2 (Ttd - sum d_p).
@@ -459,6 +570,44 @@ __device__ __forceinline__ void bin_add_fast2(f2 xr, f2 vre, f2 vim, float2* win
     }
 }
 
+// bin_add_fast2 for specular mode: the same bins and split weights, the
+// inbound phasor times g1 into win and the outbound one times g2 into win2.
+__device__ __forceinline__ void bin_add_fast2s(f2 xr, f2 vre, f2 vim, f2 g1, f2 g2, float2* win, float2* win2,
+                                               int tid) {
+    const int f0 = floor_i(xr.x), f1 = floor_i(xr.y);
+    const f2 w = fma2(make_float2((float)f0, (float)f1), bc(-1.f), xr);
+    const f2 w0 = fma2(w, bc(-1.f), bc(1.f));
+    const f2 ar = mul2(vre, g1), ai = mul2(vim, g1), br = mul2(vre, g2), bi = mul2(vim, g2);
+    const unsigned s0 = min((unsigned)f0, (unsigned)(RP_WIN - 2));
+    const unsigned s1 = min((unsigned)f1, (unsigned)(RP_WIN - 2));
+    float2* const W[2] = {win, win2};
+    const float re0[2] = {ar.x, br.x}, im0[2] = {ai.x, bi.x}, re1[2] = {ar.y, br.y}, im1[2] = {ai.y, bi.y};
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float2* p0 = &W[h][s0 * RP_PAIR_THREADS + tid];
+        float2* p1 = p0 + RP_PAIR_THREADS;
+        float2 v0 = *p0, v1 = *p1;
+        v0.x = fmaf(re0[h], w0.x, v0.x);
+        v0.y = fmaf(im0[h], w0.x, v0.y);
+        v1.x = fmaf(re0[h], w.x, v1.x);
+        v1.y = fmaf(im0[h], w.x, v1.y);
+        *p0 = v0;
+        *p1 = v1;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float2* p0 = &W[h][s1 * RP_PAIR_THREADS + tid];
+        float2* p1 = p0 + RP_PAIR_THREADS;
+        float2 v0 = *p0, v1 = *p1;
+        v0.x = fmaf(re1[h], w0.y, v0.x);
+        v0.y = fmaf(im1[h], w0.y, v0.y);
+        v1.x = fmaf(re1[h], w.y, v1.x);
+        v1.y = fmaf(im1[h], w.y, v1.y);
+        *p0 = v0;
+        *p1 = v1;
+    }
+}
+
 // ------------------------------------------------ double-float anchors --
 // Error-free transformations (Knuth TwoSum, FMA TwoProduct); the _rn
 // intrinsics keep the compiler from contracting or reordering them.
@@ -532,14 +681,25 @@ extern __shared__ __align__(128) unsigned char pair_smem[];
 #define RP_PAIR_TPOS_OFF (RP_PAIR_WIN_OFF + (size_t)RP_WIN * RP_PAIR_THREADS * sizeof(float2))
 #define RP_PAIR_META_OFF (RP_PAIR_TPOS_OFF + 2 * RP_PAIR_THREADS * sizeof(float4))
 #define RP_PAIR_SMEM_BYTES (RP_PAIR_META_OFF + 2 * sizeof(ChunkMeta))
+// specular mode adds the outbound window and two staged FacetSpec chunks
+#define RP_PAIR_WIN2_OFF RP_PAIR_SMEM_BYTES
+#define RP_PAIR_SPEC_OFF (RP_PAIR_WIN2_OFF + (size_t)RP_WIN * RP_PAIR_THREADS * sizeof(float2))
+#define RP_PAIR_SPEC_SMEM_BYTES (RP_PAIR_SPEC_OFF + 2 * RP_CHUNK_PAIRS * sizeof(FacetSpec))
+static_assert(RP_PAIR_SPEC_OFF % 16 == 0, "FacetSpec chunks are staged by bulk copies");
 
-template <int NT, int ILP, bool ORTHO, class PA>
+template <int NT, int ILP, bool ORTHO, bool SPEC, class PA>
 __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, uint64_t* bars, uint32_t* phase) {
     // every hot shared array is derived here from the shared symbol itself
     FacetPair* srec = reinterpret_cast<FacetPair*>(pair_smem);                     // [2][RP_CHUNK_PAIRS]
     float2* win = reinterpret_cast<float2*>(pair_smem + RP_PAIR_WIN_OFF);          // [RP_WIN][threads]
     float4* s_tq = reinterpret_cast<float4*>(pair_smem + RP_PAIR_TPOS_OFF);        // [2][threads]
     ChunkMeta* smeta = reinterpret_cast<ChunkMeta*>(pair_smem + RP_PAIR_META_OFF);  // [2]
+    float2* win2 = nullptr;                                                         // [RP_WIN][threads]
+    FacetSpec* sspec = nullptr;                                                     // [2][RP_CHUNK_PAIRS]
+    if constexpr (SPEC) {
+        win2 = reinterpret_cast<float2*>(pair_smem + RP_PAIR_WIN2_OFF);
+        sspec = reinterpret_cast<FacetSpec*>(pair_smem + RP_PAIR_SPEC_OFF);
+    }
     const int tid = threadIdx.x;
     const int nq = A.ntl[s];
     const int n = A.nill[s];
@@ -553,6 +713,7 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
     float tnx = 0, tny = 0, tnz = 1;
     int b0 = 0;
     C32* Trow = nullptr;
+    C32* Trow2 = nullptr;
     if (active) {
         const int64_t ti = A.tlist[(size_t)s * A.tstride + q];
         // t' = target - trace origin and |t'|^2 (FP64, once per item), kept
@@ -568,6 +729,7 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         tnz = (float)A.TG[5 * A.nt + ti];
         b0 = A.bt0[(size_t)s * A.tstride + q];
         Trow = A.T + (((size_t)part * A.nb + s) * A.tstride + q) * A.Wt;
+        if constexpr (SPEC) Trow2 = A.T2 + (((size_t)part * A.nb + s) * A.tstride + q) * A.Wt;
     }
     const FacetPair* rbase = A.rec + (size_t)s * (A.rstride / 2);
     const ChunkMeta* mbase = A.meta + (size_t)s * A.mstride;
@@ -576,9 +738,12 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
     if (tid == 0) {
         int cnt = min(RP_CHUNK, n - k0 * RP_CHUNK);
         uint32_t bytes = (uint32_t)(((cnt + 1) >> 1) * sizeof(FacetPair));
-        mbar_expect_tx(&bars[0], bytes + (uint32_t)sizeof(ChunkMeta));
+        const uint32_t sbytes = SPEC ? (uint32_t)(((cnt + 1) >> 1) * sizeof(FacetSpec)) : 0u;
+        mbar_expect_tx(&bars[0], bytes + sbytes + (uint32_t)sizeof(ChunkMeta));
         tma_bulk_g2s(srec, rbase + (size_t)k0 * RP_CHUNK_PAIRS, bytes, &bars[0]);
         tma_bulk_g2s(smeta, mbase + k0, (uint32_t)sizeof(ChunkMeta), &bars[0]);
+        if constexpr (SPEC)
+            tma_bulk_g2s(sspec, A.spec + (size_t)s * (A.rstride / 2) + (size_t)k0 * RP_CHUNK_PAIRS, sbytes, &bars[0]);
     }
     for (int k = k0; k < k1; ++k) {
         const int buf = (k - k0) & 1;
@@ -587,10 +752,15 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         if (tid == 0 && k + 1 < k1) {
             int cnt = min(RP_CHUNK, n - (k + 1) * RP_CHUNK);
             uint32_t bytes = (uint32_t)(((cnt + 1) >> 1) * sizeof(FacetPair));
-            mbar_expect_tx(&bars[buf ^ 1], bytes + (uint32_t)sizeof(ChunkMeta));
+            const uint32_t sbytes = SPEC ? (uint32_t)(((cnt + 1) >> 1) * sizeof(FacetSpec)) : 0u;
+            mbar_expect_tx(&bars[buf ^ 1], bytes + sbytes + (uint32_t)sizeof(ChunkMeta));
             tma_bulk_g2s(srec + (buf ^ 1) * RP_CHUNK_PAIRS, rbase + (size_t)(k + 1) * RP_CHUNK_PAIRS, bytes,
                          &bars[buf ^ 1]);
             tma_bulk_g2s(smeta + (buf ^ 1), mbase + k + 1, (uint32_t)sizeof(ChunkMeta), &bars[buf ^ 1]);
+            if constexpr (SPEC)
+                tma_bulk_g2s(sspec + (buf ^ 1) * RP_CHUNK_PAIRS,
+                             A.spec + (size_t)s * (A.rstride / 2) + (size_t)(k + 1) * RP_CHUNK_PAIRS, sbytes,
+                             &bars[buf ^ 1]);
         }
         const ChunkMeta* mp = smeta + buf;
         if (!mbar_wait(&bars[buf], phase[buf])) {
@@ -598,6 +768,7 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         }
         phase[buf] ^= 1u;
         const FacetPair* R = srec + buf * RP_CHUNK_PAIRS;
+        const FacetSpec* RS = SPEC ? sspec + buf * RP_CHUNK_PAIRS : nullptr;
         Anchor an;
         int blo = 0;
         bool fits = true;
@@ -633,11 +804,51 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         const bool all_fit = __all_sync(0xffffffffu, fits);
         if (active) {
             for (int w = 0; w < RP_WIN; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
+            if constexpr (SPEC)
+                for (int w = 0; w < RP_WIN; ++w) win2[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
             const int cnt = min(RP_CHUNK, n - k * RP_CHUNK);    // = mp->n (bounds from the count, not the staged copy)
             const int npairs = (cnt + 1) >> 1;
             const bool prisms = (A.np > 0) && !A.lossless;
             int jp = 0;
-            if (all_fit && !prisms) {
+            if constexpr (SPEC) {
+                if (all_fit && !prisms) {
+                    for (; jp + ILP <= npairs; jp += ILP) {
+                        f2 x[ILP], re[ILP], im[ILP], ga[ILP], gb[ILP];
+#pragma unroll
+                        for (int i = 0; i < ILP; ++i)
+                            pair_eval2s<NT, false>(R[jp + i], RS[jp + i], an, A, x[i], re[i], im[i], ga[i], gb[i]);
+#pragma unroll
+                        for (int i = 0; i < ILP; ++i) bin_add_fast2s(x[i], re[i], im[i], ga[i], gb[i], win, win2, tid);
+                    }
+                    for (; jp < npairs; ++jp) {
+                        f2 x0, re0, im0, ga, gb;
+                        pair_eval2s<NT, false>(R[jp], RS[jp], an, A, x0, re0, im0, ga, gb);
+                        bin_add_fast2s(x0, re0, im0, ga, gb, win, win2, tid);
+                    }
+                } else
+                for (; jp < npairs; ++jp) {
+                    f2 x0, re0, im0, ga, gb;
+                    pair_eval2s<NT>(R[jp], RS[jp], an, A, x0, re0, im0, ga, gb);
+                    const bool two = 2 * jp + 1 < cnt;
+                    if (prisms) {
+                        const FacetPair& r0 = R[jp];
+                        const f2 dx = fld<F_DX>(r0), dy = fld<F_DY>(r0), dz = fld<F_DZ>(r0), q = fld<F_Q>(r0);
+                        const float f0 = prism_factor(make_float4(dx.x, dy.x, dz.x, q.x), mp->cx, mp->cy, mp->cz,
+                                                      an.Dx, an.Dy, an.Dz, an.T0sq, A.PR, A.np, A.ealpha);
+                        const float f1 = two ? prism_factor(make_float4(dx.y, dy.y, dz.y, q.y), mp->cx, mp->cy,
+                                                            mp->cz, an.Dx, an.Dy, an.Dz, an.T0sq, A.PR, A.np,
+                                                            A.ealpha)
+                                             : 0.f;
+                        re0.x *= f0; im0.x *= f0; re0.y *= f1; im0.y *= f1;
+                    }
+                    bin_add(x0.x, re0.x * ga.x, im0.x * ga.x, blo, b0, win, tid, Trow, A);
+                    bin_add(x0.x, re0.x * gb.x, im0.x * gb.x, blo, b0, win2, tid, Trow2, A);
+                    if (two) {
+                        bin_add(x0.y, re0.y * ga.y, im0.y * ga.y, blo, b0, win, tid, Trow, A);
+                        bin_add(x0.y, re0.y * gb.y, im0.y * gb.y, blo, b0, win2, tid, Trow2, A);
+                    }
+                }
+            } else if (all_fit && !prisms) {
                 // ILP pairs per step; binned in facet order, so every ILP
                 // gives the same sums
                 if (ILP > 1)
@@ -677,7 +888,7 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
                     if (two) bin_add(x0.y, re0.y, im0.y, blo, b0, win, tid, Trow, A);
                 }
             }
-            // flush the window into the owned trace
+            // flush the window into the owned trace (both legs' in specular mode)
             for (int w = 0; w < RP_WIN; ++w) {
                 const float2 v = win[w * RP_PAIR_THREADS + tid];
                 if (v.x != 0.f || v.y != 0.f) {
@@ -692,6 +903,21 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
                     }
                 }
             }
+            if constexpr (SPEC)
+                for (int w = 0; w < RP_WIN; ++w) {
+                    const float2 v = win2[w * RP_PAIR_THREADS + tid];
+                    if (v.x != 0.f || v.y != 0.f) {
+                        const int o = blo + w - b0;
+                        if (o >= 0 && o < A.Wt) {
+                            C32 t0 = Trow2[o];
+                            t0.x += v.x;
+                            t0.y += v.y;
+                            Trow2[o] = t0;
+                        } else {
+                            atomicOr(A.err, 1u);
+                        }
+                    }
+                }
         }
         __syncthreads();   // everyone done with buffer `buf` before it is refilled
     }
@@ -720,5 +946,9 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
 // cfg over items work items of njobs jobs.
 int launch_pairs_multi(int cfg, const PairJob* d_jobs, const unsigned int* d_start, int njobs,
                        unsigned int* d_work, int64_t items, int sms, cudaStream_t st);
+
+// Launch of the specular-mode pair kernel k_pairs32s (rp_spec.cu) of sinc
+// degree deg in configuration cfg (0 or 1) over items work items.
+int launch_pairs_spec(int deg, int cfg, const PairArgs& P, int64_t items, int sms, cudaStream_t st);
 
 }  // namespace rpk

@@ -225,8 +225,10 @@ def autotune(enable=True):
     _abi.lib().rp_autotune(1 if enable else 0)
 
 
-def autotune_query(multi, degree=0):
-    """The tuned pair-kernel configuration (0-3) or -1 when not tuned yet."""
+def autotune_query(multi, degree=0, specular=False):
+    """The tuned pair-kernel configuration (0-3; 0-1 for the specular-mode
+    kernel) or -1 when not tuned yet."""
     c = ctypes.c_int()
-    _abi.check("rp_autotune_query", _abi.lib().rp_autotune_query(int(bool(multi)), int(degree), ctypes.byref(c)))
+    kind = 2 if specular else int(bool(multi))
+    _abi.check("rp_autotune_query", _abi.lib().rp_autotune_query(kind, int(degree), ctypes.byref(c)))
     return c.value

@@ -212,7 +212,9 @@ int rp_simulate_batch(const rp_job* jobs, int njobs, rp_workspace* ws, void* str
  * sample of its work items and keeps the fastest for the process.  The
  * configurations give bitwise identical results. */
 int rp_autotune(int enable);
-/* The tuned configuration for (multi, degree), or -1 when not tuned yet. */
+/* The tuned configuration for (kind, degree), or -1 when not tuned yet.
+ * multi: 0 the single-batch kernel (configurations 0-3), 1 the multi-scene
+ * kernel (degree ignored), 2 the specular-mode kernel (configurations 0-1). */
 int rp_autotune_query(int multi, int degree, int* cfg);
 
 /*

@@ -76,14 +76,6 @@ def test_plain_specular_modes(built_lib, oracle, mode):
     assert rel_l2(got, ref) < 1e-10
 
 
-def test_fast_form_refuses_specular(built_lib):
-    from europaraypaths_gb300 import simulator
-    sc = tiny_scene(nside=12, ntside=2, ns=1, specular=True)
-    with simulator.Scene(sc["params"], sc["facets"], sc["targets"]) as scene:
-        with pytest.raises(RuntimeError, match="RP_ERR_UNSUPPORTED|-6"):
-            scene.simulate(form="fast")
-
-
 def test_plain_incoherent_matches_oracle(built_lib, oracle):
     # incoherent mode: the seeded surface phases, FP64 like the oracle
     sc = tiny_scene(incoherent=True, incoherent_seed=5)

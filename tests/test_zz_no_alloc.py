@@ -7,7 +7,8 @@ offers one entry point whose scratch is a fixed array inside the library.
 This test calls it through the C ABI twice in a row and checks both results
 against the resident fast form (rp_simulate_device) on a scene without
 targets, within the fast form's parity tolerance; it also checks that
-oversized requests are refused with RP_ERR_BUDGET.
+oversized requests are refused with RP_ERR_BUDGET and specular scenes (whose
+surface leg it does not compute) with RP_ERR_UNSUPPORTED.
 
 The file name sorts last so that a run stopping at the first failure has
 already run every other test.
@@ -78,4 +79,20 @@ def test_surface_noalloc_incoherent_matches_fast_form(built_lib):
         ctypes.c_void_p(out.data_ptr()), None))
     torch.cuda.synchronize()
     assert rel_l2(out.cpu().numpy(), ref.cpu().numpy()) <= TOL
+    scene.close()
+
+
+def test_surface_noalloc_refuses_specular(built_lib):
+    # its kernel is the default mode's surface leg: a specular scene is
+    # refused before any device work
+    import torch
+    from europaraypaths_gb300 import _abi, simulator
+
+    sc = tiny_scene(nside=12, ns=1, specular=True, rerad_funct=0)
+    scene = simulator.Scene(sc["params"], sc["facets"], targets=None)
+    d_tr = torch.zeros((1, 9), dtype=torch.float64, device="cuda")
+    out = torch.zeros((1, scene.nr), dtype=torch.complex64, device="cuda")
+    rc = _abi.lib().rp_surface_noalloc(ctypes.c_void_p(scene.handle), ctypes.c_void_p(d_tr.data_ptr()), 1,
+                                       ctypes.c_void_p(out.data_ptr()), None)
+    assert rc == -6 and "non-specular" in _abi.last_error()
     scene.close()
