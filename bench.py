@@ -232,17 +232,21 @@ def run_batch(args, objs, tracks, stream):
             "mix": bands}
 
 
-def run_specular(args, sc, track, stream, default_value):
-    """Specular mode with linear convolution on the same large scene and
-    traces: the fast form's specular pair kernel (both refraction legs with
-    their facetReradiation factors, binned as two traces) and compression
-    with the outbound trace; pairs/s over interior traces, CUDA events on the
-    launching stream."""
+def run_mode(args, sc, track, stream, default_value, specular=False, ttype0=False):
+    """Another mode on the same large scene and traces: specular mode with
+    linear convolution (the specular pair kernel: both refraction legs with
+    their facetReradiation factors, binned as two traces; compression with
+    the outbound trace), or every target ttype 0 (genRefrPhasor: one-bin
+    phasors, one chirp convolution per trace).  pairs/s over interior traces,
+    CUDA events on the launching stream."""
     import torch
     from europaraypaths_gb300 import simulator, opcount
     p = dict(sc["params"])
-    p["specular"] = True
-    scene = simulator.Scene(p, sc["facets"], sc["targets"], device=torch.cuda.current_device())
+    p["specular"] = bool(specular)
+    tg = np.array(sc["targets"], copy=True)
+    if ttype0:
+        tg[6, :] = 0.0
+    scene = simulator.Scene(p, sc["facets"], tg, device=torch.cuda.current_device())
     try:
         n = args.spec_traces
         steps = args.spec_steps
@@ -266,11 +270,14 @@ def run_specular(args, sc, track, stream, default_value):
         ms = e0.elapsed_time(e1) / steps
         pairs = float(opcount.pairs(np.concatenate(c[1:]))) / steps
         v = pairs / (ms / 1e3)
-        return {"value": v, "unit": UNIT, "traces_per_step": n, "steps": steps, "ms_per_step": ms,
-                "stage_ms_per_step": stage, "over_default_mode": v / default_value if default_value else None,
-                "pair_cfg": {f"degree_{d}": simulator.autotune_query(False, d, specular=True) for d in (0, 3, 4, 5, 6)
-                             if simulator.autotune_query(False, d, specular=True) >= 0},
-                "note": "same scene and traces as the headline with specular=true, convolution_linear=true"}
+        out = {"value": v, "unit": UNIT, "traces_per_step": n, "steps": steps, "ms_per_step": ms,
+               "stage_ms_per_step": stage, "over_default_mode": v / default_value if default_value else None,
+               "note": ("same scene and traces as the headline with "
+                        + ("every target ttype 0" if ttype0 else "specular=true, convolution_linear=true"))}
+        if specular:
+            out["pair_cfg"] = {f"degree_{d}": simulator.autotune_query(False, d, specular=True)
+                               for d in (0, 3, 4, 5, 6) if simulator.autotune_query(False, d, specular=True) >= 0}
+        return out
     finally:
         scene.close()
 
@@ -451,7 +458,8 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson request rate, requests/s")
     ap.add_argument("--no-io", dest="io", action="store_false", help="skip the host file-I/O measurement")
     ap.add_argument("--no-focus", dest="focus", action="store_false", help="skip the azimuth-focusing measurement")
-    ap.add_argument("--spec-traces", type=int, default=4, help="traces per step of the specular-mode run (0 = skip)")
+    ap.add_argument("--spec-traces", type=int, default=4,
+                    help="traces per step of the specular-mode and ttype-0 runs (0 = skip)")
     ap.add_argument("--spec-steps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -607,10 +615,11 @@ def main():
         if not args.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(sc, scene, track, args.cpu_targets, 1000)
         if args.spec_traces > 0 and world == 1:
-            try:
-                line["specular"] = run_specular(args, sc, track, stream, value)
-            except Exception as e:
-                line["specular"] = {"error": f"{type(e).__name__}: {e}"}
+            for key, kw in (("specular", {"specular": True}), ("ttype0", {"ttype0": True})):
+                try:
+                    line[key] = run_mode(args, sc, track, stream, value, **kw)
+                except Exception as e:
+                    line[key] = {"error": f"{type(e).__name__}: {e}"}
         if args.focus and world == 1:
             try:
                 line["focus"] = run_focus()

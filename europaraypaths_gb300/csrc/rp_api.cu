@@ -503,6 +503,20 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
     if (nt > 0) s->h_targets.assign(targets, targets + 7 * nt);
     for (int64_t t = 0; t < nt; ++t)
         if (targets[6 * nt + t] == 0.0) { s->any_ttype0 = 1; break; }
+    s->d_targets_fast = s->d_targets;
+    s->nt1 = nt;
+    if (s->any_ttype0) {
+        std::vector<int64_t> perm;
+        for (int pass = 0; pass < 2; ++pass)
+            for (int64_t t = 0; t < nt; ++t)
+                if ((targets[6 * nt + t] == 0.0) == (pass == 1)) perm.push_back(t);
+        std::vector<double> tf((size_t)7 * nt);
+        for (int c = 0; c < 7; ++c)
+            for (int64_t i = 0; i < nt; ++i) tf[(size_t)c * nt + i] = targets[(size_t)c * nt + perm[i]];
+        s->nt1 = 0;
+        while (s->nt1 < nt && tf[(size_t)6 * nt + s->nt1] != 0.0) ++s->nt1;
+        if ((rc = upload(&s->d_targets_fast, tf.data(), sizeof(double) * 7 * nt, &s->store_bytes))) return fail(rc);
+    }
     // spatially sorted copy for the fast form
     if (nf > 0) {
         double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
@@ -547,6 +561,7 @@ extern "C" int rp_scene_destroy(rp_scene* s) {
     if (!s) return RP_OK;
     cudaSetDevice(s->device);
     if (s->own_stream) cudaStreamSynchronize(s->own_stream);
+    if (s->d_targets_fast && s->d_targets_fast != s->d_targets) cudaFree(s->d_targets_fast);
     void* ptrs[] = {s->d_facets, s->d_targets, s->d_prisms, s->d_order, s->d_sorted, s->d_tiles_sorted, s->d_tiles_file,
                     s->d_C1_64, s->d_C2_64, s->d_C1_32, s->d_C2_32, s->d_C2S,
                     s->d_HS, s->d_CR_64, s->d_CR_32};

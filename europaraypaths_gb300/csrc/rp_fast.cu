@@ -82,16 +82,17 @@ __device__ __forceinline__ float spec_surface_amp(const DevParams& dp, double gr
     return (float)(v * v * d_radar_eq(dp.P, grefl, dp.fs, dp.lam, d, (double)n) * (double)fre);
 }
 
-// SPEC: specular mode (the scene's dp.specular), a separate instantiation so
-// the default mode's kernel carries none of its code.
-template <bool SPEC>
+// SPEC: specular mode (the scene's dp.specular); T0: the scene has ttype-0
+// targets (FacetT0 records).  Separate instantiations, so the default mode's
+// kernel carries none of their code.
+template <bool SPEC, bool T0>
 __global__ void __launch_bounds__(RP_CHUNK)
 k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx,
            const int* __restrict__ nill, const double* __restrict__ traces, DevParams dp,
            FacetPair* __restrict__ rec, ChunkMeta* __restrict__ meta, int64_t rstride,
            int64_t mstride, float* __restrict__ sx_o, C32* __restrict__ sv_o,
            unsigned long long* __restrict__ vmax, double* __restrict__ org,
-           const int64_t* __restrict__ order, FacetSpec* __restrict__ spec) {
+           const int64_t* __restrict__ order, FacetSpec* __restrict__ spec, FacetT0* __restrict__ t0rec) {
     __shared__ double shd[32];
     __shared__ float shf[32];
     const int s = blockIdx.y;
@@ -127,6 +128,7 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
     }
     float xI = 0.f, rr = 0.f, amax = 0.f;
     float spR = 0.f, spC = 1.f, spI = 1.f, spS = 0.f;    // sin/cos Rth, cos/sin Iph (specular records)
+    float t0a = 0.f, t0d = 0.f;                          // FacetT0: a0 and Itd
     float fv[RP_NFIELD];            // this facet's record fields (FacetField order)
 #pragma unroll
     for (int f = 0; f < RP_NFIELD; ++f) fv[f] = 0.f;
@@ -205,6 +207,19 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
         const float Dmax = (4.f * (float)RP_PI_F * fsf * fsf) / (lamf * lamf);
         const float Kf = sqrtf((float)dp.P * grefr * G * (dp.lossless ? 1.f : frc) * (float)dp.nidx) * lamf *
                          lamf * Dmax / (f4 * df) * ((SPEC && !dp.lossless) ? (float)(dp.fs * dp.fs / dp.lam) : 1.f);
+        if constexpr (T0) {
+            // genRefrPhasor's per-facet constants: frc^2 (fEI fEO) and radarEq's
+            // nill P Grefr^2 fs^4 / (4 pi)^2, times (fs^2/lam)^4 of the two
+            // reradiation factors in specular mode
+            const double f4d = (4.0 * RP_PI_FRIIS) * (4.0 * RP_PI_FRIIS), fs2 = dp.fs * dp.fs;
+            double a0 = (double)frc * (double)frc * (double)n * dp.P * t.grefr * t.grefr * fs2 * fs2 / f4d;
+            if (SPEC) {
+                const double r = fs2 / dp.lam;
+                a0 *= (r * r) * (r * r);
+            }
+            t0a = (float)a0;
+            t0d = (float)d;
+        }
         const double ti = d * dp.turn;
         float ddx = (float)(fx - cx), ddy = (float)(fy - cy), ddz = (float)(fz - cz);
         rr = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
@@ -264,6 +279,11 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
                 if (lane1) ps->p = make_float4(e[2], o[2], e[3], o[3]);
                 else ps->r = make_float4(e[0], o[0], e[1], o[1]);
             }
+        }
+        if constexpr (T0) {       // the pair's FacetT0 (even lane); a missing odd facet adds zero
+            const float pa = __shfl_xor_sync(0xffffffffu, t0a, 1), pdd = __shfl_xor_sync(0xffffffffu, t0d, 1);
+            if (pair_ok && !lane1)
+                t0rec[((size_t)s * rstride + j) / 2].v = make_float4(t0a, pok ? pa : 0.f, t0d, pok ? pdd : t0d);
         }
     }
     // the surface amplitude maximum of the trace: one atomic per chunk
@@ -414,7 +434,8 @@ __global__ void k_tsetup32(const double* __restrict__ TG, int64_t nt, const int*
         double f = fmax(fabs(lo), fabs(hi));
         dmax2 += f * f;
     }
-    const double kb = dp.nidx / dp.dr;
+    // bins per metre of Ttd: n (accumulateTarget) or c1/c2 (genRefrPhasor, ttype 0)
+    const double kb = (TG[6 * nt + ti] == 0.0 ? dp.c1_over_c2 : dp.nidx) / dp.dr;
     double lo = (double)m.xmin + kb * sqrt(dmin2);
     double hi = (double)m.xmax + kb * sqrt(dmax2);
     int b0 = (int)floor(lo) - 2;
@@ -424,6 +445,61 @@ __global__ void k_tsetup32(const double* __restrict__ TG, int64_t nt, const int*
     if (b1 < b0) b1 = b0;
     bt0[(size_t)s * tstride + q] = b0;
     atomicMax(maxw, b1 - b0);
+}
+
+// Per trace: the ttype-1 targets' count, the length of the leading run of
+// the ordered target list below nt1 (the fast form's store holds ttype-1
+// targets first).
+__global__ void k_ntl1(const int* __restrict__ tlist, const int* __restrict__ ntl, int64_t tstride, int64_t nt1,
+                       int nb, int* __restrict__ ntl1) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nb) return;
+    const int* l = tlist + (size_t)s * tstride;
+    int lo = 0, hi = ntl[s];            // first position with l[pos] >= nt1
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (l[mid] < nt1) lo = mid + 1; else hi = mid;
+    }
+    ntl1[s] = lo;
+}
+
+// ttype-0 targets: their phasor traces (rows [ntl1, ntl) of T, all facet-range
+// parts) summed per bin in target order (FP64), a dense trace per trace.
+__global__ void k_t0_sum32(const int* __restrict__ ntl1, const int* __restrict__ ntl, int64_t tstride,
+                           const int* __restrict__ bt0, const C32* __restrict__ T, int Wt, int nb, int nr,
+                           C32* __restrict__ sum0) {
+    const int s = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nr) return;
+    double vr = 0.0, vi = 0.0;
+    for (int q = ntl1[s]; q < ntl[s]; ++q) {
+        const int o = i - bt0[(size_t)s * tstride + q];
+        if (o < 0 || o >= Wt) continue;
+        for (int p = 0; p < RP_PARTS; ++p) {
+            const C32 u = T[(((size_t)p * nb + s) * tstride + q) * Wt + o];
+            vr += u.x;
+            vi += u.y;
+        }
+    }
+    sum0[(size_t)s * nr + i] = C32{(float)vr, (float)vi};
+}
+
+// The ttype-0 targets' contribution: the summed trace convolved with the
+// targets' chirp (genPhasorTrace + convolvePhasorChirpLinear per target,
+// sim.cu:940-966, is linear and the same chirp for all, so one convolution
+// of the sum per trace).
+__global__ void k_t0_conv32(const C32* __restrict__ sum0, int nr, const C32* __restrict__ C, PlanV<float> p2,
+                            C32* __restrict__ r0, C32* __restrict__ scratch, size_t slot) {
+    const int s = blockIdx.x;
+    C32* base = scratch + (size_t)s * slot;
+    const int M = 1 << p2.log2M;
+    C32* x = base;
+    C32* wa = x + M;
+    C32* wb = wa + M;
+    C32* in = wb + M;
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) in[i] = sum0[(size_t)s * nr + i];
+    __syncthreads();
+    conv_linear_block<float>(in, C, p2, nr, x, wa, wb, r0 + (size_t)s * nr, 1.0f);
 }
 
 // Single-batch pair kernel: the batch's constants live in the parameter
@@ -744,7 +820,8 @@ __global__ void k_usum32(const int* __restrict__ nill, const int* __restrict__ n
 __global__ void __launch_bounds__(512, 1)
 k_trace_m32(const int* __restrict__ nill, const int* __restrict__ ntl, const C32* __restrict__ refl,
             const C32* __restrict__ part, int nsplit, int nr, const Cplx<float>* __restrict__ Hs,
-            Cplx<float>* __restrict__ gW, void* __restrict__ out, int out64, int s0) {
+            Cplx<float>* __restrict__ gW, void* __restrict__ out, int out64, int s0,
+            const C32* __restrict__ r0) {
     extern __shared__ __align__(16) unsigned char tsm[];
     const int s = blockIdx.x;
     const int n2 = 2 * nr, N = n2 - 1, M = 2 * n2;
@@ -767,6 +844,10 @@ k_trace_m32(const int* __restrict__ nill, const int* __restrict__ ntl, const C32
             const Cplx<float> a = W[swz(2 * j)], b = W[swz(2 * j + N)];
             vr = (double)r.x + ((double)a.x + (double)b.x);
             vi = (double)r.y + ((double)a.y + (double)b.y);
+            if (r0) {       // ttype-0 targets
+                vr += (double)r0[(size_t)s * nr + j].x;
+                vi += (double)r0[(size_t)s * nr + j].y;
+            }
         }
         const size_t o = (size_t)(s0 + s) * nr + j;
         if (out64) reinterpret_cast<C64*>(out)[o] = C64{vr, vi};
@@ -798,7 +879,7 @@ __global__ void k_surf_conv32(const long long* __restrict__ acc, const int* __re
 // sig = refl + sum_q Z_q (target order), accumulated in FP64.
 __global__ void k_sum32(const int* __restrict__ nill, const int* __restrict__ ntl, int64_t tstride,
                         const C32* __restrict__ refl, const C32* __restrict__ Z, int nr,
-                        void* __restrict__ out, int out64, int s0) {
+                        void* __restrict__ out, int out64, int s0, const C32* __restrict__ r0) {
     const int s = blockIdx.y;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nr) return;
@@ -806,6 +887,10 @@ __global__ void k_sum32(const int* __restrict__ nill, const int* __restrict__ nt
     if (nill[s] > 0) {
         C32 r = refl[(size_t)s * nr + i];
         vr = r.x; vi = r.y;
+        if (r0) {           // ttype-0 targets
+            vr += r0[(size_t)s * nr + i].x;
+            vi += r0[(size_t)s * nr + i].y;
+        }
         const int n = ntl[s];
         const C32* z = Z + (size_t)s * tstride * nr + i;
         for (int q = 0; q < n; ++q) {
@@ -843,6 +928,10 @@ void fast_take_setup(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<int>((size_t)L.nb * nf);                // idx
     a.template take<FacetPair>((size_t)L.nb * L.rstride / 2);    // records (facet pairs)
     if (sc->dp.specular) a.template take<FacetSpec>((size_t)L.nb * L.rstride / 2);
+    if (sc->nt1 < sc->nt) {
+        a.template take<FacetT0>((size_t)L.nb * L.rstride / 2);
+        a.template take<int>(L.nb);                         // ntl1
+    }
     a.template take<ChunkMeta>((size_t)L.nb * L.mstride);   // chunk meta
     a.template take<double>((size_t)L.nb * 4);              // trace origins
     a.template take<float>((size_t)L.nb * nf);              // surface x
@@ -887,6 +976,7 @@ template <class Aa>
 void fast_take_pairs(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<C32>((size_t)RP_PARTS * L.nb * L.tstride * L.Wt);   // T parts
     if (sc->dp.specular) a.template take<C32>((size_t)RP_PARTS * L.nb * L.tstride * L.Wt);   // T2 parts
+    if (sc->nt1 < sc->nt) a.template take<C32>((size_t)L.nb * (2 * sc->nr + L.surf_slot));    // ttype-0 sum, r0, scratch
     if (conv_mode(sc) <= 2) {
         a.template take<C32>((size_t)L.nb * conv_splits(L.tstride) * 2 * sc->nr);   // per-split sums of u
         if (trace_m_global(sc)) a.template take<C32>((size_t)L.nb * 4 * sc->nr);   // per-trace crop stage
@@ -1087,6 +1177,8 @@ struct Seg {
     uint8_t* fflags; int* tcnt; int* nill; int* ntl; unsigned long long* vmax;
     double* org; int* idx; FacetPair* rec; ChunkMeta* meta; float* sxv; C32* sv; TraceMeta* tm; uint8_t* tflags;
     FacetSpec* spec = nullptr;     // specular mode
+    FacetT0* t0rec = nullptr;      // ttype-0 targets present
+    int* ntl1 = nullptr;           // ttype-1 targets per trace (= ntl without ttype-0 targets)
     int* tlist; int* bt0; int* misc; long long* acc; C32* refl; C32* sscr;
     // pair stage
     int Wt = 1;
@@ -1095,6 +1187,7 @@ struct Seg {
     bool pairs = false;
     C32* T = nullptr; C32* Z = nullptr; C32* cscr = nullptr; C32* part = nullptr;
     C32* T2 = nullptr;      // specular mode: outbound-leg parts
+    C32* sum0 = nullptr; C32* r0 = nullptr; C32* t0scr = nullptr;   // ttype-0 targets
     C32* tscr = nullptr;    // per-trace crop-stage scratch (nr > 4096)
 };
 
@@ -1146,12 +1239,15 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
     g.idx = a.take<int>((size_t)nb * nfa);
     g.rec = a.take<FacetPair>((size_t)nb * Lw.rstride / 2);
     g.spec = dp.specular ? a.take<FacetSpec>((size_t)nb * Lw.rstride / 2) : nullptr;
+    const bool t0 = sc->nt1 < nt;
+    g.t0rec = t0 ? a.take<FacetT0>((size_t)nb * Lw.rstride / 2) : nullptr;
     g.meta = a.take<ChunkMeta>((size_t)nb * Lw.mstride);
     g.org = a.take<double>((size_t)nb * 4);
     g.sxv = a.take<float>((size_t)nb * nfa);
     g.sv = a.take<C32>((size_t)nb * nfa);
     g.tm = a.take<TraceMeta>(nb);
     g.tflags = a.take<uint8_t>((size_t)nb * nta);
+    g.ntl1 = t0 ? a.take<int>(nb) : g.ntl;
     g.tlist = a.take<int>((size_t)nb * nta);
     g.bt0 = a.take<int>((size_t)nb * Lw.tstride);
     g.misc = a.take<int>(8);
@@ -1167,9 +1263,11 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
             sc->d_sorted, nf, trb, dp.ap_rad, g.fflags, g.tcnt, reinterpret_cast<const double4*>(sc->d_tiles_sorted));
         RP_LAUNCHED();
         compact_flags(g.fflags, nf, nb, g.tcnt, g.nill, g.idx, nfa, true, st);
-        (dp.specular ? k_facets32<true> : k_facets32<false>)<<<dim3((unsigned)Lw.mstride, nb), RP_CHUNK, 0, st>>>(
+        auto kf = dp.specular ? (t0 ? k_facets32<true, true> : k_facets32<true, false>)
+                              : (t0 ? k_facets32<false, true> : k_facets32<false, false>);
+        kf<<<dim3((unsigned)Lw.mstride, nb), RP_CHUNK, 0, st>>>(
             sc->d_sorted, nfa, g.idx, g.nill, trb, dp, g.rec, g.meta, Lw.rstride, Lw.mstride, g.sxv, g.sv, g.vmax,
-            g.org, sc->d_order, g.spec);
+            g.org, sc->d_order, g.spec, g.t0rec);
         RP_LAUNCHED();
         k_surf_fix32<<<dim3((unsigned)((nf + 256 * RP_SFIX_PER - 1) / (256 * RP_SFIX_PER)), nb), 256, 0, st>>>(
             nfa, g.nill, g.sxv, g.sv, g.vmax, nr, g.acc, dp.specular);
@@ -1180,17 +1278,22 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
         cudaMemsetAsync(g.nill, 0, sizeof(int) * nb, st);
     }
     if (nt > 0) {
-        k_target_flags<<<dim3((unsigned)((nt + 255) / 256), nb), 256, 0, st>>>(sc->d_targets, nt, trb, dp.ap_rad,
-                                                                            g.tflags);
+        k_target_flags<<<dim3((unsigned)((nt + 255) / 256), nb), 256, 0, st>>>(sc->d_targets_fast, nt, trb,
+                                                                            dp.ap_rad, g.tflags);
         RP_LAUNCHED();
         compact_flags(g.tflags, nt, nb, g.tcnt, g.ntl, g.tlist, Lw.tstride, false, st);
+        if (t0) {
+            k_ntl1<<<(nb + 63) / 64, 64, 0, st>>>(g.tlist, g.ntl, Lw.tstride, sc->nt1, nb, g.ntl1);
+            RP_LAUNCHED();
+        }
         if (nf > 0) {
             k_tsetup32<<<dim3((unsigned)((Lw.tstride + 255) / 256), nb), 256, 0, st>>>(
-                sc->d_targets, nt, g.tlist, g.ntl, Lw.tstride, g.tm, g.nill, dp, g.bt0, g.misc);
+                sc->d_targets_fast, nt, g.tlist, g.ntl, Lw.tstride, g.tm, g.nill, dp, g.bt0, g.misc);
             RP_LAUNCHED();
         }
     } else {
         cudaMemsetAsync(g.ntl, 0, sizeof(int) * nb, st);
+        if (g.ntl1 != g.ntl) cudaMemsetAsync(g.ntl1, 0, sizeof(int) * nb, st);
     }
 }
 
@@ -1200,8 +1303,8 @@ PairArgs seg_pair_args(const Seg& g) {
     const int nr = sc->nr;
     PairArgs P;
     P.rec = g.rec; P.meta = g.meta; P.org = g.org; P.rstride = g.Lw.rstride; P.mstride = g.Lw.mstride;
-    P.nill = g.nill; P.ntl = g.ntl; P.tlist = g.tlist; P.tstride = g.L.tstride;
-    P.TG = sc->d_targets; P.nt = sc->nt; P.PR = sc->d_prisms; P.np = sc->np;
+    P.nill = g.nill; P.ntl = g.ntl1; P.tlist = g.tlist; P.tstride = g.L.tstride;
+    P.TG = sc->d_targets_fast; P.nt = sc->nt; P.PR = sc->d_prisms; P.np = sc->np;
     P.bt0 = g.bt0; P.T = g.T; P.Wt = g.Wt; P.nb = g.nb;
     P.tblocks = (int)((g.L.tstride + RP_PAIR_THREADS - 1) / RP_PAIR_THREADS);
     P.work = reinterpret_cast<unsigned int*>(g.misc + 1);
@@ -1230,6 +1333,37 @@ PairArgs seg_pair_args(const Seg& g) {
     P.pikr2 = rr ? (float)(pikr * pikr) : 0.f;
     P.e21 = (float)(dp.eps2 / dp.eps1);
     P.s2tir = (float)(std::sin(1e4) * std::sin(1e4));
+    P.t0rec = nullptr; P.tq0 = nullptr;
+    return P;
+}
+
+// Arguments of the ttype-0 pair kernel: targets [ntl1, ntl) of each trace.
+// genRefrPhasor's path applies fEI and fEO (attenuation, roughness,
+// reradiation) whatever `lossless` says (sim.cu:940-966).
+PairArgs seg_pair_args_t0(const Seg& g) {
+    const DevParams& dp = g.sc->dp;
+    PairArgs P = seg_pair_args(g);
+    P.ntl = g.ntl; P.tq0 = g.ntl1; P.t0rec = g.t0rec;
+    P.lossless = 0;
+    P.ealpha = (float)(-2.0 * dp.alpha2 * 1.4426950408889634);
+    P.eks = (float)(-2.0 * dp.ks * dp.ks * 1.4426950408889634);
+    const double pikr = RP_PI * dp.fs / dp.lam;
+    for (int k = 0; k < 8; ++k) P.sr[k] = (float)(g.coefr[k] * std::pow(pikr * pikr, k));
+    P.pikr2 = (float)(pikr * pikr);
+    const double kb0 = dp.c1_over_c2 / dp.dr, kt0 = 2.0 * dp.turn * dp.c1_over_c2;
+    P.kb0 = (float)kb0;
+    P.kb0h = (float)kb0; P.kb0l = (float)(kb0 - (double)P.kb0h);
+    P.kt0h = (float)kt0; P.kt0l = (float)(kt0 - (double)P.kt0h);
+    P.kr0 = (float)(2.0 * RP_PI * kt0);
+    // rerad_funct (radar_kernels.cu:167-189) as a test on cos(TargetTh):
+    // 1 and 2 keep angles below 1 and 0.5 degree, 3 below 3 * 180 / pi_F
+    // radians (the reference's unit slip), 4 a Gaussian of width 1 degree
+    const int f = dp.rerad_funct;
+    P.rf = (f >= 1 && f <= 4) ? f : 0;
+    const double th0 = f == 1 ? RP_PI_F / 180 : (f == 2 ? 0.5 * RP_PI_F / 180 : 3 * 180 / RP_PI_F);
+    P.rcos = th0 >= RP_PI ? -2.f : (float)std::cos(th0);
+    const double sg = RP_PI_F / 180;
+    P.rgl = (float)(-0.5 * 1.4426950408889634 / (sg * sg));
     return P;
 }
 
@@ -1237,7 +1371,7 @@ ConvArgs seg_conv_args(const Seg& g) {
     const rp_scene* sc = g.sc;
     const int nr = sc->nr;
     ConvArgs C;
-    C.ntl = g.ntl; C.tstride = g.L.tstride; C.nb = g.nb; C.bt0 = g.bt0; C.T = g.T; C.T2 = g.T2; C.Wt = g.Wt;
+    C.ntl = g.ntl1; C.tstride = g.L.tstride; C.nb = g.nb; C.bt0 = g.bt0; C.T = g.T; C.T2 = g.T2; C.Wt = g.Wt;
     C.C2s = (const Cplx<float>*)sc->d_C2S; C.Hs = (const Cplx<float>*)sc->d_HS;
     C.nr = nr; C.n2 = 2 * nr; C.N = 2 * nr - 1; C.M = sc->mS;
     C.crop_K = sc->crop_K; C.crop_all = sc->crop_all;
@@ -1388,6 +1522,11 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     for (Seg& g : segs) {
         g.T = b.take<C32>((size_t)RP_PARTS * g.nb * g.L.tstride * g.Wt);
         g.T2 = g.sc->dp.specular ? b.take<C32>((size_t)RP_PARTS * g.nb * g.L.tstride * g.Wt) : nullptr;
+        if (g.t0rec) {
+            g.sum0 = b.take<C32>((size_t)g.nb * g.sc->nr);
+            g.r0 = b.take<C32>((size_t)g.nb * g.sc->nr);
+            g.t0scr = b.take<C32>((size_t)g.nb * g.Lw.surf_slot);
+        }
         if (g.cmode <= 2) {
             g.part = b.take<C32>((size_t)g.nb * g.nsplit * 2 * g.sc->nr);
             g.tscr = trace_m_global(g.sc) ? b.take<C32>((size_t)g.nb * 4 * g.sc->nr) : nullptr;
@@ -1397,7 +1536,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         }
     }
     C32* gscr = gscr_n ? b.take<C32>(gscr_n) : nullptr;
-    unsigned int* d_work = b.take<unsigned int>(4);
+    unsigned int* d_work = b.take<unsigned int>(4 + nseg);     // pairs, 3 compression modes, ttype-0 per segment
     PairJob* d_pjobs = b.take<PairJob>(std::max<size_t>(ps.size(), 1));
     unsigned int* d_pstart = b.take<unsigned int>(ps.size() + 1);
     ConvArgs* d_cjobs[3];
@@ -1406,7 +1545,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         d_cjobs[m] = b.take<ConvArgs>(std::max<size_t>(cs[m].size(), 1));
         d_cstart[m] = b.take<unsigned int>(cs[m].size() + 1);
     }
-    RP_CUDA(cudaMemsetAsync(d_work, 0, sizeof(unsigned int) * 4, st));
+    RP_CUDA(cudaMemsetAsync(d_work, 0, sizeof(unsigned int) * (4 + nseg), st));
     for (Seg& g : segs) {
         RP_CUDA(cudaMemsetAsync(g.T, 0, sizeof(C32) * RP_PARTS * g.nb * g.L.tstride * g.Wt, st));
         if (g.T2) RP_CUDA(cudaMemsetAsync(g.T2, 0, sizeof(C32) * RP_PARTS * g.nb * g.L.tstride * g.Wt, st));
@@ -1452,6 +1591,17 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         rc = launch_pairs(ps, d_pjobs, d_pstart, d_work, cfg, sms, st);
         if (rc) return rc;
         ++g_timer.pair_launches;
+        // ttype-0 targets: one launch per segment that has them
+        for (int i = 0; i < nseg; ++i) {
+            Seg& g = segs[i];
+            if (!g.pairs || !g.t0rec) continue;
+            PairArgs P0 = seg_pair_args_t0(g);
+            P0.work = d_work + 4 + i;
+            const int64_t items = (int64_t)g.nb * P0.tblocks * RP_PARTS;
+            rc = launch_pairs_t0(g.deg, g.sc->ortho != 0, g.sc->dp.specular != 0, P0, items, sms, st);
+            if (rc) return rc;
+            RP_LAUNCHED();
+        }
     } else {
         g_timer.mark(1, st);
     }
@@ -1468,7 +1618,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         if (g->cmode <= 2) continue;
         const rp_scene* sc = g->sc;
         // the targets' chirp: the surface chirp in specular mode (sim.cu:851-856)
-        k_conv32<<<g->L.slots, 256, 0, st>>>(g->ntl, g->L.tstride, g->nb, g->bt0, g->T, g->T2, g->Wt, g->Z,
+        k_conv32<<<g->L.slots, 256, 0, st>>>(g->ntl1, g->L.tstride, g->nb, g->bt0, g->T, g->T2, g->Wt, g->Z,
                                             (const C32*)(sc->dp.specular ? sc->d_C1_32 : sc->d_C2_32),
                                             plan_view32(sc->plan2), plan_view32(sc->planN),
                                             sc->crop_K, sc->crop_all, sc->nr, (float)(-1.0 / std::sqrt(sc->dp.P)),
@@ -1489,20 +1639,30 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
                                             (const C32*)sc->d_C1_32, plan_view32(sc->plan2), g.refl, g.sscr,
                                             g.Lw.surf_slot);
         RP_LAUNCHED();
+        const C32* r0 = nullptr;
+        if (g.pairs && g.t0rec) {      // ttype-0 targets: ordered sum, one chirp convolution per trace
+            k_t0_sum32<<<dim3((nr + 127) / 128, g.nb), 128, 0, ts>>>(g.ntl1, g.ntl, g.L.tstride, g.bt0, g.T, g.Wt,
+                                                                    g.nb, nr, g.sum0);
+            RP_LAUNCHED();
+            k_t0_conv32<<<g.nb, 256, 0, ts>>>(g.sum0, nr, (const C32*)(sc->dp.specular ? sc->d_C1_32 : sc->d_C2_32),
+                                             plan_view32(sc->plan2), g.r0, g.t0scr, g.Lw.surf_slot);
+            RP_LAUNCHED();
+            r0 = g.r0;
+        }
         if (g.cmode <= 2) {
             if (!g.pairs) RP_CUDA(cudaMemsetAsync(g.part, 0, sizeof(C32) * g.nb * g.nsplit * 2 * nr, ts));
             const size_t tsm = g.tscr ? 0 : (size_t)4 * nr * sizeof(C32);
             if (int rc = rp_allow_dyn_smem((const void*)k_trace_m32, tsm)) return rc;
-            k_usum32<<<dim3((2 * nr + 255) / 256, g.nb), 256, 0, ts>>>(g.nill, g.ntl, g.part, g.nsplit, 2 * nr);
+            k_usum32<<<dim3((2 * nr + 255) / 256, g.nb), 256, 0, ts>>>(g.nill, g.ntl1, g.part, g.nsplit, 2 * nr);
             RP_LAUNCHED();
-            k_trace_m32<<<g.nb, 512, tsm, ts>>>(g.nill, g.ntl, g.refl, g.part, g.nsplit, nr,
+            k_trace_m32<<<g.nb, 512, tsm, ts>>>(g.nill, g.ntl1, g.refl, g.part, g.nsplit, nr,
                                                  (const Cplx<float>*)sc->d_HS,
                                                  reinterpret_cast<Cplx<float>*>(g.tscr), g.d_out, g.out64,
-                                                 (int)g.s0);
+                                                 (int)g.s0, r0);
         } else {
             if (!g.pairs) RP_CUDA(cudaMemsetAsync(g.Z, 0, sizeof(C32) * g.nb * g.L.tstride * nr, ts));
-            k_sum32<<<dim3((nr + 255) / 256, g.nb), 256, 0, ts>>>(g.nill, g.ntl, g.L.tstride, g.refl, g.Z, nr,
-                                                                 g.d_out, g.out64, (int)g.s0);
+            k_sum32<<<dim3((nr + 255) / 256, g.nb), 256, 0, ts>>>(g.nill, g.ntl1, g.L.tstride, g.refl, g.Z, nr,
+                                                                 g.d_out, g.out64, (int)g.s0, r0);
         }
         RP_LAUNCHED();
     }
@@ -1600,10 +1760,6 @@ int check_scene(const rp_scene* sc) {
     if (sc->dp.cmode != 0) {
         rp_set_error("fast form: only linear convolution (the default mode and specular with linear "
                      "convolution); the plain form runs the other specular variants");
-        return RP_ERR_UNSUPPORTED;
-    }
-    if (sc->any_ttype0) {
-        rp_set_error("fast form: ttype-0 targets are handled by the plain form only");
         return RP_ERR_UNSUPPORTED;
     }
     if (sc->planN.pow2) { rp_set_error("internal: N = 2 nr - 1 is a power of two"); return RP_ERR_INTERNAL; }

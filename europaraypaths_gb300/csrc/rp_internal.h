@@ -119,6 +119,11 @@ struct rp_scene {
     double* d_prisms = nullptr;
     std::vector<double> h_targets;       // host copy of the targets (aperture bounds)
     int any_ttype0 = 0;
+    // the fast form's copy of the targets, ttype-1 targets first (stable), so
+    // each trace's ordered in-aperture list is both kinds' lists in turn;
+    // the same pointer as d_targets when every target is ttype 1
+    double* d_targets_fast = nullptr;
+    int64_t nt1 = 0;                     // ttype-1 targets (the first nt1 of d_targets_fast)
     // ---- fast store: spatially sorted facets
     int64_t* d_order = nullptr;          // sorted position -> original index
     double* d_tiles_sorted = nullptr;    // per RP_CULL_TILE sorted facets: bounding sphere (x, y, z, r)

@@ -58,6 +58,13 @@ struct __align__(16) FacetSpec {
     float4 p;   // {cos Iph, cos Iph, sin Iph, sin Iph}
 };
 
+// ttype-0 targets (genRefrPhasor): per facet of a pair the trace's constant
+// frc^2 nill P Grefr^2 fs^4 / (4 pi)^2 (times (fs^2/lam)^4 in specular mode)
+// and Itd in FP32.
+struct __align__(16) FacetT0 {
+    float4 v;   // {a0, a0, Itd, Itd}
+};
+
 // Field f of both facets of a pair.
 template <int F>
 __device__ __forceinline__ float2 fld(const FacetPair& p) {
@@ -172,6 +179,16 @@ struct PairArgs {
     float pikr2;            // pikr^2 (special-function path)
     float e21;              // eps2 / eps1: sin^2 of the outbound Snell angle over sin^2(Tth)
     float s2tir;            // sin^2(1e4): the reference's total-internal-reflection angle
+    // ttype-0 targets (pair_item_t0): targets [tq0[s], ntl[s]) of the list
+    const FacetT0* t0rec;   // [nb][rstride / 2]
+    const int* tq0;
+    float kb0;              // c1/c2 / dr: bins per metre of Ttd
+    float kb0h, kb0l;       // the same as a double-float
+    float kt0h, kt0l;       // 2 turn c1/c2: phase turns per metre of Ttd, double-float
+    float kr0;              // 2 pi kt0 (radians per metre)
+    int rf;                 // rerad_funct: 0 none, 1-3 angle threshold, 4 Gaussian
+    float rcos;             // threshold on cos(TargetTh) for rf 1-3
+    float rgl;              // rf 4: -0.5 log2(e) / (pi_F/180)^2
 };
 
 // A job of the multi-job pair kernel: a batch's arguments and its sinc
@@ -345,6 +362,43 @@ __device__ __forceinline__ void pair_eval2(const FacetPair& r, const Anchor& an,
 // by -1e-15 (below FP32 resolution for any other value) gives cos Tph = 1 at
 // e.u = e.v = 0, as atan2(0, 0) = 0 does.  Beyond total internal reflection
 // the reference's flag angle 1e4 gives sin^2(1e4).
+// The two reradiation amplitudes g1, g2 of pair_eval2s from cos Tth = pbr,
+// sin^2 Tth = aT, the in-plane components pc, pd (pd already shifted) and
+// rh = 1 / (pc^2 + pd^2).
+template <int NT>
+__device__ __forceinline__ void spec_rerad2(const FacetSpec& sp, const PairArgs& A, f2 pbr, f2 aT, f2 pc, f2 pd,
+                                            f2 rh, f2& g1, f2& g2) {
+    const f2 sR = make_float2(sp.r.x, sp.r.y), cR = make_float2(sp.r.z, sp.r.w);
+    const f2 cI = make_float2(sp.p.x, sp.p.y), sI = make_float2(sp.p.z, sp.p.w);
+    const f2 aTc = make_float2(fmaxf(aT.x, 1e-30f), fmaxf(aT.y, 1e-30f));
+    const f2 sTh = mul2(aTc, make_float2(rsqrt_a(aTc.x), rsqrt_a(aTc.y)));
+    const f2 st1 = fma2(sR, pbr, mul2(neg2(cR), sTh));
+    const f2 q1 = mul2(st1, st1);
+    const f2 q2r = mul2(bc(A.e21), aT);
+    const f2 q2 = make_float2(q2r.x > 1.f ? A.s2tir : q2r.x, q2r.y > 1.f ? A.s2tir : q2r.y);
+    const f2 cn = fma2(cI, pd, mul2(sI, pc));
+    const f2 sn = fma2(sI, pd, mul2(neg2(cI), pc));
+    const f2 cc = mul2(mul2(cn, cn), rh), ss = mul2(mul2(sn, sn), rh);
+    const f2 u1 = mul2(q1, cc), u2 = mul2(q1, ss), u3 = mul2(q2, cc), u4 = mul2(q2, ss);
+    if (NT > 0) {
+        constexpr int D = NT > 0 ? NT : 1;
+        g1 = mul2(sinc_poly2<D>(A.sr, u1), sinc_poly2<D>(A.sr, u2));
+        g2 = mul2(sinc_poly2<D>(A.sr, u3), sinc_poly2<D>(A.sr, u4));
+        if (NT >= 5) {
+            g1 = make_float2(fabsf(g1.x), fabsf(g1.y));
+            g2 = make_float2(fabsf(g2.x), fabsf(g2.y));
+        }
+    } else {
+        const f2 R2 = bc(A.pikr2);
+        const f2 v1 = mul2(u1, R2), v2 = mul2(u2, R2), v3 = mul2(u3, R2), v4 = mul2(u4, R2);
+        float a0 = 1.f, b0 = 1.f, a1 = 1.f, b1 = 1.f, c0 = 1.f, d0 = 1.f, c1 = 1.f, d1 = 1.f;
+        sinc_sfu(v1.x, a0, b0); sinc_sfu(v2.x, a0, b0); sinc_sfu(v1.y, a1, b1); sinc_sfu(v2.y, a1, b1);
+        sinc_sfu(v3.x, c0, d0); sinc_sfu(v4.x, c0, d0); sinc_sfu(v3.y, c1, d1); sinc_sfu(v4.y, c1, d1);
+        g1 = make_float2(fabsf(__fdividef(a0, b0)), fabsf(__fdividef(a1, b1)));
+        g2 = make_float2(fabsf(__fdividef(c0, d0)), fabsf(__fdividef(c1, d1)));
+    }
+}
+
 template <int NT, bool RED = true>
 __device__ __forceinline__ void pair_eval2s(const FacetPair& r, const FacetSpec& sp, const Anchor& an,
                                             const PairArgs& A, f2& xr, f2& vre, f2& vim, f2& g1, f2& g2) {
@@ -371,32 +425,14 @@ __device__ __forceinline__ void pair_eval2s(const FacetPair& r, const FacetSpec&
     const f2 xs = mul2(X, rh);
     const f2 t1 = mul2(aT, xs), t3 = mul2(aD, xs);
     const f2 t2 = fma2(t1, M1, aT), t4 = fma2(t3, M1, aD);
-    // the reradiation legs: q1 = sin^2(Rth - Tth), q2 = sin^2 of the outbound
-    // Snell angle, cc / ss = cos^2 / sin^2 (Iph - Tph)
-    const f2 sR = make_float2(sp.r.x, sp.r.y), cR = make_float2(sp.r.z, sp.r.w);
-    const f2 cI = make_float2(sp.p.x, sp.p.y), sI = make_float2(sp.p.z, sp.p.w);
-    const f2 aTc = make_float2(fmaxf(aT.x, 1e-30f), fmaxf(aT.y, 1e-30f));
-    const f2 sTh = mul2(aTc, make_float2(rsqrt_a(aTc.x), rsqrt_a(aTc.y)));
-    const f2 st1 = fma2(sR, pbr, mul2(neg2(cR), sTh));
-    const f2 q1 = mul2(st1, st1);
-    const f2 q2r = mul2(bc(A.e21), aT);
-    const f2 q2 = make_float2(q2r.x > 1.f ? A.s2tir : q2r.x, q2r.y > 1.f ? A.s2tir : q2r.y);
-    const f2 cn = fma2(cI, pd, mul2(sI, pc));
-    const f2 sn = fma2(sI, pd, mul2(neg2(cI), pc));
-    const f2 cc = mul2(mul2(cn, cn), rh), ss = mul2(mul2(sn, sn), rh);
-    const f2 u1 = mul2(q1, cc), u2 = mul2(q1, ss), u3 = mul2(q2, cc), u4 = mul2(q2, ss);
+    // the reradiation legs (spec_rerad2)
+    spec_rerad2<NT>(sp, A, pbr, aT, pc, pd, rh, g1, g2);
     f2 S;
     if (NT > 0) {
         constexpr int D = NT > 0 ? NT : 1;
         S = mul2(mul2(sinc_poly2<D>(A.sc, t1), sinc_poly2<D>(A.sc, t2)),
                  mul2(sinc_poly2<D>(A.sc, t3), sinc_poly2<D>(A.sc, t4)));
-        g1 = mul2(sinc_poly2<D>(A.sr, u1), sinc_poly2<D>(A.sr, u2));
-        g2 = mul2(sinc_poly2<D>(A.sr, u3), sinc_poly2<D>(A.sr, u4));
-        if (NT >= 5) {
-            S = make_float2(fabsf(S.x), fabsf(S.y));
-            g1 = make_float2(fabsf(g1.x), fabsf(g1.y));
-            g2 = make_float2(fabsf(g2.x), fabsf(g2.y));
-        }
+        if (NT >= 5) S = make_float2(fabsf(S.x), fabsf(S.y));
     } else {
         const f2 P2 = bc(A.pik2);
         const f2 w1 = mul2(t1, P2), w2 = mul2(t2, P2), w3 = mul2(t3, P2), w4 = mul2(t4, P2);
@@ -404,13 +440,6 @@ __device__ __forceinline__ void pair_eval2s(const FacetPair& r, const FacetSpec&
         sinc_sfu(w1.x, n0, e0); sinc_sfu(w2.x, n0, e0); sinc_sfu(w3.x, n0, e0); sinc_sfu(w4.x, n0, e0);
         sinc_sfu(w1.y, n1, e1); sinc_sfu(w2.y, n1, e1); sinc_sfu(w3.y, n1, e1); sinc_sfu(w4.y, n1, e1);
         S = make_float2(fabsf(__fdividef(n0, e0)), fabsf(__fdividef(n1, e1)));
-        const f2 R2 = bc(A.pikr2);
-        const f2 v1 = mul2(u1, R2), v2 = mul2(u2, R2), v3 = mul2(u3, R2), v4 = mul2(u4, R2);
-        float a0 = 1.f, b0 = 1.f, a1 = 1.f, b1 = 1.f, c0 = 1.f, d0 = 1.f, c1 = 1.f, d1 = 1.f;
-        sinc_sfu(v1.x, a0, b0); sinc_sfu(v2.x, a0, b0); sinc_sfu(v1.y, a1, b1); sinc_sfu(v2.y, a1, b1);
-        sinc_sfu(v3.x, c0, d0); sinc_sfu(v4.x, c0, d0); sinc_sfu(v3.y, c1, d1); sinc_sfu(v4.y, c1, d1);
-        g1 = make_float2(fabsf(__fdividef(a0, b0)), fabsf(__fdividef(a1, b1)));
-        g2 = make_float2(fabsf(__fdividef(c0, d0)), fabsf(__fdividef(c1, d1)));
     }
     const f2 e2 = fma2(bc(-A.eks), aT, fma2(bc(A.ealpha), dT, bc(an.eaT0)));
     const f2 amp = mul2(mul2(fld<F_K>(r), S), mul2(rinv, make_float2(ex2_a(e2.x), ex2_a(e2.y))));
@@ -605,6 +634,47 @@ __device__ __forceinline__ void bin_add_fast2s(f2 xr, f2 vre, f2 vim, f2 g1, f2 
         v1.y = fmaf(im1[h], w.y, v1.y);
         *p0 = v0;
         *p1 = v1;
+    }
+}
+
+// One ttype-0 phasor into the thread's window, or (outside it) its target
+// row: the whole phasor in the truncated bin (genRefrPhasor +
+// genPhasorTrace, radar_kernels.cu:351-398, 401-448); x in (-1, 0) gives bin
+// 0, bins outside the trace are dropped.
+__device__ __forceinline__ void bin_add1(float xr, float vre, float vim, int blo, int b0, float2* win, int tid,
+                                         C32* Trow, const PairArgs& A) {
+    const int sl = floor_i(xr);
+    int b = blo + sl;
+    if ((unsigned)sl < (unsigned)RP_WIN && (unsigned)b < (unsigned)A.nr) {
+        float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
+        float2 v0 = *p0;
+        v0.x += vre;
+        v0.y += vim;
+        *p0 = v0;
+        return;
+    }
+    if (b < 0) {
+        if (b != -1) return;
+        b = 0;
+    }
+    if (b >= A.nr) return;
+    const int sw = b - blo;
+    if ((unsigned)sw < (unsigned)RP_WIN) {
+        float2* p0 = &win[sw * RP_PAIR_THREADS + tid];
+        float2 v0 = *p0;
+        v0.x += vre;
+        v0.y += vim;
+        *p0 = v0;
+        return;
+    }
+    const int o = b - b0;
+    if (o >= 0 && o < A.Wt) {
+        C32 t0 = Trow[o];
+        t0.x += vre;
+        t0.y += vim;
+        Trow[o] = t0;
+    } else {
+        atomicOr(A.err, 1u);
     }
 }
 
@@ -923,6 +993,257 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
     }
 }
 
+// --------------------------------------------------- ttype-0 targets --
+// Two (facet, target) evaluations for a ttype-0 target: genRefrPhasor
+// (radar_kernels.cu:351-398) with compRefrEnergyIn/Out's factors
+// (geometry_kernels.cu:520-584).  Amplitude rerad(TargetTh) fEI fEO
+// radarEq(Itd + Ttd), phase +4 pi_F rngt / lam, bin (rngt - rst) / dr at
+// rngt = Itd + Ttd c1/c2.  fEI fEO = att^2 rough^2 frc^2 (times both
+// reradiation factors in specular mode), and att^2 rough^2 = exp2(4 e2) with
+// pair_eval2's exponent e2; frc^2 and the radar equation's constants are the
+// record's a0.  The facet's part of the phase, 4 pi_F Itd / lam, is -2 times
+// the record's -2 pi frac(Itd / lam_F) (mod 2 pi).
+template <int NT, bool ORTHO, bool SPEC>
+__device__ __forceinline__ void pair_eval2t0(const FacetPair& r, const FacetSpec* sp, const FacetT0& t0,
+                                             const Anchor& an, const PairArgs& A, f2& xr, f2& vre, f2& vim) {
+    const f2 ONE = bc(1.f);
+    const f2 dx = fld<F_DX>(r), dy = fld<F_DY>(r), dz = fld<F_DZ>(r);
+    const f2 mx = bc(-2.f * an.Dx), my = bc(-2.f * an.Dy), mz = bc(-2.f * an.Dz);
+    const f2 qd = fma2(mx, dx, fma2(my, dy, fma2(mz, dz, fld<F_Q>(r))));   // Ttd^2 - T0^2
+    const f2 d2 = add2(bc(an.T0sq), qd);
+    const f2 rinv = make_float2(rsqrt_a(d2.x), rsqrt_a(d2.y));
+    const f2 sT = fma2(d2, rinv, bc(an.T0));
+    const f2 dT = mul2(qd, make_float2(rcp_a(sT.x), rcp_a(sT.y)));
+    f2 aT, ptr, gg = ONE;
+    if (ORTHO) {
+        const f2 pc = fma2(mx, fld<F_UX>(r), fma2(my, fld<F_UY>(r), fma2(mz, fld<F_UZ>(r), fld<F_AU>(r))));
+        const f2 pd = fma2(mx, fld<F_VX>(r), fma2(my, fld<F_VY>(r), fma2(mz, fld<F_VZ>(r), fld<F_AV>(r))));
+        const f2 pt = fma2(dx, bc(an.tnx), fma2(dy, bc(an.tny), fma2(dz, bc(an.tnz), bc(an.nDtn))));
+        const f2 pcr = mul2(pc, rinv), pdr = mul2(pd, rinv);
+        ptr = mul2(pt, rinv);
+        aT = fma2(pdr, pdr, mul2(pcr, pcr));
+    } else {
+        const f2 hf = bc(0.5f);
+        const f2 ex = fma2(mx, hf, dx), ey = fma2(my, hf, dy), ez = fma2(mz, hf, dz);
+        const f2 pb = fma2(ex, fld<F_NX>(r), fma2(ey, fld<F_NY>(r), mul2(ez, fld<F_NZ>(r))));
+        const f2 pt = fma2(ex, bc(an.tnx), fma2(ey, bc(an.tny), mul2(ez, bc(an.tnz))));
+        const f2 pbr = mul2(pb, rinv);
+        ptr = mul2(pt, rinv);
+        aT = fma2(pbr, neg2(pbr), ONE);
+        if (SPEC) {
+            const f2 pc = fma2(ex, fld<F_UX>(r), fma2(ey, fld<F_UY>(r), mul2(ez, fld<F_UZ>(r))));
+            const f2 pd = add2(fma2(ex, fld<F_VX>(r), fma2(ey, fld<F_VY>(r), mul2(ez, fld<F_VZ>(r)))),
+                               bc(-1e-15f));
+            const f2 h2 = fma2(pc, pc, mul2(pd, pd));
+            const f2 rh = make_float2(rcp_a(h2.x), rcp_a(h2.y));
+            f2 g1, g2;
+            spec_rerad2<NT>(*sp, A, pbr, aT, pc, pd, rh, g1, g2);
+            const f2 g = mul2(g1, g2);
+            gg = mul2(g, g);
+        }
+    }
+    // rerad_funct of TargetTh (radar_kernels.cu:167-189): cos TargetTh = ptr
+    f2 rr = ONE;
+    if (A.rf >= 1 && A.rf <= 3) {
+        rr = make_float2(ptr.x > A.rcos ? 1.f : 0.f, ptr.y > A.rcos ? 1.f : 0.f);
+    } else if (A.rf == 4) {
+        const float th0 = acosf(fminf(1.f, fmaxf(-1.f, ptr.x))), th1 = acosf(fminf(1.f, fmaxf(-1.f, ptr.y)));
+        rr = make_float2(ex2_a(A.rgl * th0 * th0), ex2_a(A.rgl * th1 * th1));
+    }
+    const f2 e2 = fma2(bc(-A.eks), aT, fma2(bc(A.ealpha), dT, bc(an.eaT0)));
+    const f2 e4 = mul2(e2, bc(4.f));
+    // radarEq: a0 / (Itd + Ttd)^4
+    const f2 fS = add2(make_float2(t0.v.z, t0.v.w), add2(bc(an.T0), dT));
+    const f2 ri = make_float2(rcp_a(fS.x), rcp_a(fS.y));
+    const f2 r2 = mul2(ri, ri);
+    const f2 amp = mul2(mul2(mul2(make_float2(t0.v.x, t0.v.y), mul2(r2, r2)), mul2(rr, gg)),
+                        make_float2(ex2_a(e4.x), ex2_a(e4.y)));
+    f2 ph = fma2(bc(A.kr0), dT, fma2(fld<F_PH>(r), bc(-2.f), bc(an.ph0)));
+    const f2 k = mul2(ph, bc(0.159154943091895336f));
+    ph = fma2(make_float2(rintf(k.x), rintf(k.y)), bc(-6.28318530717958647f), ph);
+    f2 sn, cs;
+    __sincosf(ph.x, &sn.x, &cs.x);
+    __sincosf(ph.y, &sn.y, &cs.y);
+    vre = mul2(amp, cs);
+    vim = mul2(amp, sn);
+    xr = fma2(bc(A.kb0), dT, add2(fld<F_XI>(r), bc(an.xbase)));
+}
+
+// Shared memory of the ttype-0 pair kernel: pair_item's layout, then the
+// staged FacetT0 and (specular) FacetSpec chunks.
+#define RP_PAIR_T0_OFF RP_PAIR_SMEM_BYTES
+#define RP_PAIR_T0SPEC_OFF (RP_PAIR_T0_OFF + 2 * RP_CHUNK_PAIRS * sizeof(FacetT0))
+#define RP_PAIR_T0_SMEM_BYTES(spec) (RP_PAIR_T0SPEC_OFF + ((spec) ? 2 * RP_CHUNK_PAIRS * sizeof(FacetSpec) : 0))
+static_assert(RP_PAIR_T0SPEC_OFF % 16 == 0, "staged by bulk copies");
+
+// One work item of the ttype-0 pair kernel: the targets [tq0[s], ntl[s]) of
+// trace s, block tb of them, facet-range part `part`.  The chunk staging and
+// the double-float anchors are pair_item's; the anchors use c1/c2 in place
+// of n and a positive phase, and every phasor goes to one bin.
+template <int NT, int ILP, bool ORTHO, bool SPEC>
+__device__ __forceinline__ void pair_item_t0(const PairArgs& A, int s, int tb, int part, uint64_t* bars,
+                                             uint32_t* phase) {
+    FacetPair* srec = reinterpret_cast<FacetPair*>(pair_smem);
+    float2* win = reinterpret_cast<float2*>(pair_smem + RP_PAIR_WIN_OFF);
+    float4* s_tq = reinterpret_cast<float4*>(pair_smem + RP_PAIR_TPOS_OFF);
+    ChunkMeta* smeta = reinterpret_cast<ChunkMeta*>(pair_smem + RP_PAIR_META_OFF);
+    FacetT0* st0 = reinterpret_cast<FacetT0*>(pair_smem + RP_PAIR_T0_OFF);
+    FacetSpec* sspec = SPEC ? reinterpret_cast<FacetSpec*>(pair_smem + RP_PAIR_T0SPEC_OFF) : nullptr;
+    const int tid = threadIdx.x;
+    const int qs = A.tq0[s];
+    const int nq = A.ntl[s] - qs;
+    const int n = A.nill[s];
+    if (tb * RP_PAIR_THREADS >= nq || n == 0) return;
+    const int nchunks = (n + RP_CHUNK - 1) / RP_CHUNK;
+    const int k0 = (int)((int64_t)nchunks * part / RP_PARTS);
+    const int k1 = (int)((int64_t)nchunks * (part + 1) / RP_PARTS);
+    if (k0 >= k1) return;
+    const int ql = tb * RP_PAIR_THREADS + tid;
+    const bool active = ql < nq;
+    const int q = qs + ql;
+    float tnx = 0, tny = 0, tnz = 1;
+    int b0 = 0;
+    C32* Trow = nullptr;
+    if (active) {
+        const int64_t ti = A.tlist[(size_t)s * A.tstride + q];
+        const double px = A.TG[ti] - A.org[4 * s], py = A.TG[A.nt + ti] - A.org[4 * s + 1],
+                     pz = A.TG[2 * A.nt + ti] - A.org[4 * s + 2];
+        const double p2 = px * px + py * py + pz * pz;
+        const float hx = (float)px, hy = (float)py, hz = (float)pz, h2 = (float)p2;
+        s_tq[tid] = make_float4(hx, hy, hz, h2);
+        s_tq[RP_PAIR_THREADS + tid] = make_float4((float)(px - hx), (float)(py - hy), (float)(pz - hz),
+                                                  (float)(p2 - h2));
+        tnx = (float)A.TG[3 * A.nt + ti]; tny = (float)A.TG[4 * A.nt + ti];
+        tnz = (float)A.TG[5 * A.nt + ti];
+        b0 = A.bt0[(size_t)s * A.tstride + q];
+        Trow = A.T + (((size_t)part * A.nb + s) * A.tstride + q) * A.Wt;
+    }
+    const size_t pbase = (size_t)s * (A.rstride / 2);
+    const FacetPair* rbase = A.rec + pbase;
+    const ChunkMeta* mbase = A.meta + (size_t)s * A.mstride;
+    auto stage = [&](int k, int b) {
+        const int cnt = min(RP_CHUNK, n - k * RP_CHUNK);
+        const uint32_t np = (uint32_t)((cnt + 1) >> 1);
+        const uint32_t bytes = np * (uint32_t)sizeof(FacetPair), tb0 = np * (uint32_t)sizeof(FacetT0);
+        const uint32_t sb = SPEC ? np * (uint32_t)sizeof(FacetSpec) : 0u;
+        mbar_expect_tx(&bars[b], bytes + tb0 + sb + (uint32_t)sizeof(ChunkMeta));
+        tma_bulk_g2s(srec + b * RP_CHUNK_PAIRS, rbase + (size_t)k * RP_CHUNK_PAIRS, bytes, &bars[b]);
+        tma_bulk_g2s(smeta + b, mbase + k, (uint32_t)sizeof(ChunkMeta), &bars[b]);
+        tma_bulk_g2s(st0 + b * RP_CHUNK_PAIRS, A.t0rec + pbase + (size_t)k * RP_CHUNK_PAIRS, tb0, &bars[b]);
+        if (SPEC)
+            tma_bulk_g2s(sspec + b * RP_CHUNK_PAIRS, A.spec + pbase + (size_t)k * RP_CHUNK_PAIRS, sb, &bars[b]);
+    };
+    if (tid == 0) stage(k0, 0);
+    for (int k = k0; k < k1; ++k) {
+        const int buf = (k - k0) & 1;
+        if (tid == 0 && k + 1 < k1) stage(k + 1, buf ^ 1);
+        const ChunkMeta* mp = smeta + buf;
+        if (!mbar_wait(&bars[buf], phase[buf])) {
+            if (tid == 0) atomicOr(A.err + 1, 1u);
+        }
+        phase[buf] ^= 1u;
+        const FacetPair* R = srec + buf * RP_CHUNK_PAIRS;
+        const FacetT0* R0 = st0 + buf * RP_CHUNK_PAIRS;
+        const FacetSpec* RS = SPEC ? sspec + buf * RP_CHUNK_PAIRS : nullptr;
+        Anchor an;
+        int blo = 0;
+        bool fits = true;
+        if (active) {
+            const float4 th = s_tq[tid], tl = s_tq[RP_PAIR_THREADS + tid];
+            const float cfx = mp->cfx, cfy = mp->cfy, cfz = mp->cfz;
+            float Th, Tl, Qh;
+            anchor_distance(th, tl, cfx, cfy, cfz, mp->cch, mp->ccl, Th, Tl, Qh);
+            const float fr = frac_dd(Th, Tl, A.kt0h, A.kt0l);
+            float xf;
+            const int xi = floor_dd(Th, Tl, A.kb0h, A.kb0l, xf);
+            const float lo = xf + fmaf(-A.kb0, mp->R, mp->xmin), hi = xf + fmaf(A.kb0, mp->R, mp->xmax);
+            const int blo_rel = floor_i(lo) - 1;
+            blo = xi + blo_rel;
+            fits = blo >= 0 && blo + RP_WIN <= A.nr && hi + 0.5f < (float)(blo_rel + RP_WIN);
+            an.Dx = __fadd_rn(__fadd_rn(th.x, -cfx), tl.x);
+            an.Dy = __fadd_rn(__fadd_rn(th.y, -cfy), tl.y);
+            an.Dz = __fadd_rn(__fadd_rn(th.z, -cfz), tl.z);
+            an.T0 = Th; an.T0sq = Qh;
+            an.ph0 = 6.28318530717958647f * fr;
+            an.xbase = xf - (float)blo_rel;
+            an.tnx = tnx; an.tny = tny; an.tnz = tnz;
+            an.nDtn = -fmaf(an.Dx, tnx, fmaf(an.Dy, tny, an.Dz * tnz));
+            an.eaT0 = fmaf(A.ealpha, Th, A.eks);
+        }
+        const bool all_fit = __all_sync(0xffffffffu, fits);
+        if (active) {
+            for (int w = 0; w < RP_WIN; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
+            const int cnt = min(RP_CHUNK, n - k * RP_CHUNK);
+            const int npairs = (cnt + 1) >> 1;
+            const bool prisms = A.np > 0;
+            int jp = 0;
+            if (all_fit && !prisms) {
+                // every pair's bin is inside the window and the trace
+                for (; jp < npairs; jp += ILP) {
+                    f2 x[ILP], re[ILP], im[ILP];
+#pragma unroll
+                    for (int i = 0; i < ILP; ++i) {
+                        const int j = min(jp + i, npairs - 1);
+                        pair_eval2t0<NT, ORTHO, SPEC>(R[j], SPEC ? RS + j : nullptr, R0[j], an, A, x[i], re[i], im[i]);
+                    }
+#pragma unroll
+                    for (int i = 0; i < ILP; ++i) {
+                        if (jp + i >= npairs) break;
+                        const unsigned s0 = min((unsigned)floor_i(x[i].x), (unsigned)(RP_WIN - 1));
+                        const unsigned s1 = min((unsigned)floor_i(x[i].y), (unsigned)(RP_WIN - 1));
+                        float2* p0 = &win[s0 * RP_PAIR_THREADS + tid];
+                        float2 v0 = *p0;
+                        v0.x += re[i].x;
+                        v0.y += im[i].x;
+                        *p0 = v0;
+                        float2* p1 = &win[s1 * RP_PAIR_THREADS + tid];
+                        float2 v1 = *p1;
+                        v1.x += re[i].y;
+                        v1.y += im[i].y;
+                        *p1 = v1;
+                    }
+                }
+            } else {
+                for (; jp < npairs; ++jp) {
+                    f2 x0, re0, im0;
+                    pair_eval2t0<NT, ORTHO, SPEC>(R[jp], SPEC ? RS + jp : nullptr, R0[jp], an, A, x0, re0, im0);
+                    const bool two = 2 * jp + 1 < cnt;
+                    if (prisms) {
+                        // the prisms' change of att, squared (att^2 here, sqrt(att) in prism_factor);
+                        // ttype-0 targets take fEI and fEO whatever lossless says (sim.cu:940-966)
+                        const FacetPair& r0 = R[jp];
+                        const f2 dx = fld<F_DX>(r0), dy = fld<F_DY>(r0), dz = fld<F_DZ>(r0), qq = fld<F_Q>(r0);
+                        float f0 = prism_factor(make_float4(dx.x, dy.x, dz.x, qq.x), mp->cx, mp->cy, mp->cz,
+                                                an.Dx, an.Dy, an.Dz, an.T0sq, A.PR, A.np, A.ealpha);
+                        float f1 = two ? prism_factor(make_float4(dx.y, dy.y, dz.y, qq.y), mp->cx, mp->cy, mp->cz,
+                                                      an.Dx, an.Dy, an.Dz, an.T0sq, A.PR, A.np, A.ealpha)
+                                       : 0.f;
+                        f0 *= f0; f0 *= f0; f1 *= f1; f1 *= f1;
+                        re0.x *= f0; im0.x *= f0; re0.y *= f1; im0.y *= f1;
+                    }
+                    bin_add1(x0.x, re0.x, im0.x, blo, b0, win, tid, Trow, A);
+                    if (two) bin_add1(x0.y, re0.y, im0.y, blo, b0, win, tid, Trow, A);
+                }
+            }
+            for (int w = 0; w < RP_WIN; ++w) {
+                const float2 v = win[w * RP_PAIR_THREADS + tid];
+                if (v.x != 0.f || v.y != 0.f) {
+                    const int o = blo + w - b0;
+                    if (o >= 0 && o < A.Wt) {
+                        C32 t0 = Trow[o];
+                        t0.x += v.x;
+                        t0.y += v.y;
+                        Trow[o] = t0;
+                    } else {
+                        atomicOr(A.err, 1u);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 #define RP_PAIR_SMEM_DECL                                                                       \
     __shared__ uint64_t bars[2];                                                                \
     __shared__ unsigned int s_item;                                                             \
@@ -950,5 +1271,9 @@ int launch_pairs_multi(int cfg, const PairJob* d_jobs, const unsigned int* d_sta
 // Launch of the specular-mode pair kernel k_pairs32s (rp_spec.cu) of sinc
 // degree deg in configuration cfg (0 or 1) over items work items.
 int launch_pairs_spec(int deg, int cfg, const PairArgs& P, int64_t items, int sms, cudaStream_t st);
+
+// Launch of the ttype-0 pair kernel k_pairs32t0 (rp_spec.cu) over items work
+// items (deg matters in specular mode only).
+int launch_pairs_t0(int deg, bool ortho, bool spec, const PairArgs& P, int64_t items, int sms, cudaStream_t st);
 
 }  // namespace rpk

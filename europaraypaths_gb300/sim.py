@@ -72,11 +72,9 @@ def load_inputs(params_path, facets_path, targets_path):
 
 def pick_form(p, targets):
     """``auto``: the fast form for linear convolution (the default mode and
-    specular with linear convolution) without ttype-0 targets, else the plain
+    specular with linear convolution, targets of either type), else the plain
     FP64 form, which runs every mode the reference defines."""
-    linear = bool(p.convolution and p.convolution_linear)
-    ttype0 = targets.shape[1] > 0 and bool(np.any(targets[6] == 0.0))
-    return "fast" if linear and not ttype0 else "plain"
+    return "fast" if (p.convolution and p.convolution_linear) else "plain"
 
 
 def run(params_path, facets_path, targets_path, outdir, form="auto", batch=64, quiet=False, radargram=None):

@@ -33,12 +33,12 @@ def _spec(sc, **over):
     return sc
 
 
-def _run(sc, oracle, traces=None, prisms=None, targets=None):
+def _run(sc, oracle, traces=None, prisms=None, targets=None, complex128=False):
     from europaraypaths_gb300 import simulator, traces as tr_mod
     tg = sc["targets"] if targets is None else targets
     scene = simulator.Scene(sc["params"], sc["facets"], tg, prisms=prisms)
     tr = tr_mod.linear_track(scene.params) if traces is None else traces
-    got, cnt = scene.simulate(tr, form="fast", return_counts=True)
+    got, cnt = scene.simulate(tr, form="fast", complex128=complex128, return_counts=True)
     ref, rcnt = oracle.simulate(scene.params, sc["facets"], tg, tr, prisms_soa=prisms)
     scene.close()
     return got, ref, cnt, rcnt
@@ -52,13 +52,17 @@ def check(got, ref):
 
 
 def check_targets(sc, oracle, traces=None, prisms=None):
-    """The whole radargram and the target legs alone against the oracle."""
+    """The whole radargram and the target legs alone against the oracle.  The
+    target part is the difference of two complex128 radargrams (the fast
+    form's final sum is FP64 and its surface part is the same bits in both
+    runs), so targets far weaker than the surface keep their precision."""
     got, ref, cnt, rcnt = _run(sc, oracle, traces=traces, prisms=prisms)
     assert np.array_equal(cnt, rcnt)
     check(got, ref)
     empty = np.zeros((7, 0))
-    got0, ref0, _, _ = _run(sc, oracle, traces=traces, prisms=prisms, targets=empty)
-    dg, dr = got - got0, ref - ref0
+    g1, _, _, _ = _run(sc, oracle, traces=traces, prisms=prisms, complex128=True)
+    got0, ref0, _, _ = _run(sc, oracle, traces=traces, prisms=prisms, targets=empty, complex128=True)
+    dg, dr = g1 - got0, ref - ref0
     assert np.abs(dr).max() > 0
     assert rel_l2(dg, dr) <= REL_L2, rel_l2(dg, dr)
     return got, ref
@@ -157,14 +161,14 @@ def test_fast_specular_batched_with_default_mode(built_lib):
 
 
 def test_fast_refuses_other_specular_modes(built_lib):
-    # circular convolution (ttype-0 targets) and ttype-0 targets with linear
-    # convolution stay in the plain form
+    # circular convolution and no convolution (ttype-0 targets) stay in the
+    # plain form
     from europaraypaths_gb300 import simulator
     circ = _spec(tiny_scene(nside=12, ntside=2, ns=1), convolution_linear=False)
     circ["targets"][6, :] = 0.0
-    lin0 = _spec(tiny_scene(nside=12, ntside=2, ns=1))
-    lin0["targets"][6, ::2] = 0.0
-    for sc in (circ, lin0):
+    none = _spec(tiny_scene(nside=12, ntside=2, ns=1), convolution=False)
+    none["targets"][6, :] = 0.0
+    for sc in (circ, none):
         with simulator.Scene(sc["params"], sc["facets"], sc["targets"]) as scene:
             with pytest.raises(RuntimeError, match="RP_ERR_UNSUPPORTED|-6"):
                 scene.simulate(form="fast")
