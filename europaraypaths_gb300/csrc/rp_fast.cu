@@ -464,22 +464,56 @@ __global__ void k_ntl1(const int* __restrict__ tlist, const int* __restrict__ nt
 }
 
 // ttype-0 targets: their phasor traces (rows [ntl1, ntl) of T, all facet-range
-// parts) summed per bin in target order (FP64), a dense trace per trace.
-__global__ void k_t0_sum32(const int* __restrict__ ntl1, const int* __restrict__ ntl, int64_t tstride,
-                           const int* __restrict__ bt0, const C32* __restrict__ T, int Wt, int nb, int nr,
-                           C32* __restrict__ sum0) {
+// parts) summed per bin in target order (FP64) into a dense trace per trace,
+// in two passes.  Pass 1: the trace's targets in RP_T0_GROUPS consecutive
+// groups (a fixed split of the trace's own list, so the sums never depend on
+// the batch); a block adds its group's rows, one target after the other,
+// into a dense FP64 partial (shared memory when it fits, else its slot of
+// gpart).  Pass 2: the groups' partials summed in group order.
+#define RP_T0_GROUPS 32
+#define RP_T0_SMEM_MAX ((size_t)160 << 10)
+__global__ void __launch_bounds__(256) k_t0_part32(const int* __restrict__ ntl1, const int* __restrict__ ntl,
+                                                   int64_t tstride, const int* __restrict__ bt0,
+                                                   const C32* __restrict__ T, int Wt, int nb, int nr,
+                                                   double2* __restrict__ gpart, int use_smem) {
+    extern __shared__ __align__(16) unsigned char t0sm[];
+    const int g = blockIdx.x, s = blockIdx.y;
+    double2* acc = use_smem ? reinterpret_cast<double2*>(t0sm) : gpart + ((size_t)s * RP_T0_GROUPS + g) * nr;
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) acc[i] = make_double2(0.0, 0.0);
+    __syncthreads();
+    const int a = ntl1[s], n0 = ntl[s] - a;
+    const int q0 = a + (int)((int64_t)n0 * g / RP_T0_GROUPS), q1 = a + (int)((int64_t)n0 * (g + 1) / RP_T0_GROUPS);
+    for (int q = q0; q < q1; ++q) {
+        const int b0 = bt0[(size_t)s * tstride + q];
+        for (int o = threadIdx.x; o < Wt; o += blockDim.x) {
+            const int i = b0 + o;
+            if (i >= nr) break;
+            double vr = 0.0, vi = 0.0;
+            for (int p = 0; p < RP_PARTS; ++p) {
+                const C32 u = T[(((size_t)p * nb + s) * tstride + q) * Wt + o];
+                vr += u.x;
+                vi += u.y;
+            }
+            double2 c = acc[i];
+            c.x += vr;
+            c.y += vi;
+            acc[i] = c;
+        }
+        __syncthreads();    // the next target's row may cover the same bins
+    }
+    if (use_smem)
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) gpart[((size_t)s * RP_T0_GROUPS + g) * nr + i] = acc[i];
+}
+
+__global__ void k_t0_sum32(const double2* __restrict__ gpart, int nr, C32* __restrict__ sum0) {
     const int s = blockIdx.y;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nr) return;
     double vr = 0.0, vi = 0.0;
-    for (int q = ntl1[s]; q < ntl[s]; ++q) {
-        const int o = i - bt0[(size_t)s * tstride + q];
-        if (o < 0 || o >= Wt) continue;
-        for (int p = 0; p < RP_PARTS; ++p) {
-            const C32 u = T[(((size_t)p * nb + s) * tstride + q) * Wt + o];
-            vr += u.x;
-            vi += u.y;
-        }
+    for (int g = 0; g < RP_T0_GROUPS; ++g) {
+        const double2 c = gpart[((size_t)s * RP_T0_GROUPS + g) * nr + i];
+        vr += c.x;
+        vi += c.y;
     }
     sum0[(size_t)s * nr + i] = C32{(float)vr, (float)vi};
 }
@@ -976,7 +1010,10 @@ template <class Aa>
 void fast_take_pairs(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<C32>((size_t)RP_PARTS * L.nb * L.tstride * L.Wt);   // T parts
     if (sc->dp.specular) a.template take<C32>((size_t)RP_PARTS * L.nb * L.tstride * L.Wt);   // T2 parts
-    if (sc->nt1 < sc->nt) a.template take<C32>((size_t)L.nb * (2 * sc->nr + L.surf_slot));    // ttype-0 sum, r0, scratch
+    if (sc->nt1 < sc->nt) {       // ttype-0 sum, r0, scratch, group partials
+        a.template take<C32>((size_t)L.nb * (2 * sc->nr + L.surf_slot));
+        a.template take<double2>((size_t)L.nb * RP_T0_GROUPS * sc->nr);
+    }
     if (conv_mode(sc) <= 2) {
         a.template take<C32>((size_t)L.nb * conv_splits(L.tstride) * 2 * sc->nr);   // per-split sums of u
         if (trace_m_global(sc)) a.template take<C32>((size_t)L.nb * 4 * sc->nr);   // per-trace crop stage
@@ -1188,6 +1225,7 @@ struct Seg {
     C32* T = nullptr; C32* Z = nullptr; C32* cscr = nullptr; C32* part = nullptr;
     C32* T2 = nullptr;      // specular mode: outbound-leg parts
     C32* sum0 = nullptr; C32* r0 = nullptr; C32* t0scr = nullptr;   // ttype-0 targets
+    double2* t0part = nullptr;
     C32* tscr = nullptr;    // per-trace crop-stage scratch (nr > 4096)
 };
 
@@ -1526,6 +1564,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
             g.sum0 = b.take<C32>((size_t)g.nb * g.sc->nr);
             g.r0 = b.take<C32>((size_t)g.nb * g.sc->nr);
             g.t0scr = b.take<C32>((size_t)g.nb * g.Lw.surf_slot);
+            g.t0part = b.take<double2>((size_t)g.nb * RP_T0_GROUPS * g.sc->nr);
         }
         if (g.cmode <= 2) {
             g.part = b.take<C32>((size_t)g.nb * g.nsplit * 2 * g.sc->nr);
@@ -1641,8 +1680,15 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         RP_LAUNCHED();
         const C32* r0 = nullptr;
         if (g.pairs && g.t0rec) {      // ttype-0 targets: ordered sum, one chirp convolution per trace
-            k_t0_sum32<<<dim3((nr + 127) / 128, g.nb), 128, 0, ts>>>(g.ntl1, g.ntl, g.L.tstride, g.bt0, g.T, g.Wt,
-                                                                    g.nb, nr, g.sum0);
+            const size_t psm = (size_t)nr * sizeof(double2);
+            const int use_smem = psm <= RP_T0_SMEM_MAX;
+            if (use_smem) {
+                if (int rc = rp_allow_dyn_smem((const void*)k_t0_part32, psm)) return rc;
+            }
+            k_t0_part32<<<dim3(RP_T0_GROUPS, g.nb), 256, use_smem ? psm : 0, ts>>>(
+                g.ntl1, g.ntl, g.L.tstride, g.bt0, g.T, g.Wt, g.nb, nr, g.t0part, use_smem);
+            RP_LAUNCHED();
+            k_t0_sum32<<<dim3((nr + 255) / 256, g.nb), 256, 0, ts>>>(g.t0part, nr, g.sum0);
             RP_LAUNCHED();
             k_t0_conv32<<<g.nb, 256, 0, ts>>>(g.sum0, nr, (const C32*)(sc->dp.specular ? sc->d_C1_32 : sc->d_C2_32),
                                              plan_view32(sc->plan2), g.r0, g.t0scr, g.Lw.surf_slot);
