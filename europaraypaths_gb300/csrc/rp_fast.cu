@@ -521,9 +521,11 @@ __global__ void k_t0_sum32(const double2* __restrict__ gpart, int nr, C32* __res
 // The ttype-0 targets' contribution: the summed trace convolved with the
 // targets' chirp (genPhasorTrace + convolvePhasorChirpLinear per target,
 // sim.cu:940-966, is linear and the same chirp for all, so one convolution
-// of the sum per trace).
+// of the sum per trace).  circ: specular mode with circular convolution,
+// the nr-point convolution with genChirp's wrapped chirp CR (sim.cu:959).
 __global__ void k_t0_conv32(const C32* __restrict__ sum0, int nr, const C32* __restrict__ C, PlanV<float> p2,
-                            C32* __restrict__ r0, C32* __restrict__ scratch, size_t slot) {
+                            C32* __restrict__ r0, C32* __restrict__ scratch, size_t slot, int circ,
+                            const C32* __restrict__ CR, PlanV<float> pR) {
     const int s = blockIdx.x;
     C32* base = scratch + (size_t)s * slot;
     const int M = 1 << p2.log2M;
@@ -533,7 +535,8 @@ __global__ void k_t0_conv32(const C32* __restrict__ sum0, int nr, const C32* __r
     C32* in = wb + M;
     for (int i = threadIdx.x; i < nr; i += blockDim.x) in[i] = sum0[(size_t)s * nr + i];
     __syncthreads();
-    conv_linear_block<float>(in, C, p2, nr, x, wa, wb, r0 + (size_t)s * nr, 1.0f);
+    if (circ) conv_circular_block<float>(in, CR, pR, nr, x, wa, wb, r0 + (size_t)s * nr);
+    else conv_linear_block<float>(in, C, p2, nr, x, wa, wb, r0 + (size_t)s * nr, 1.0f);
 }
 
 // Single-batch pair kernel: the batch's constants live in the parameter
@@ -1673,11 +1676,18 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         const cudaStream_t ts = par ? ws->aux[si % rp_workspace::kAux] : st;
         const rp_scene* sc = g.sc;
         const int nr = sc->nr;
-        // disable_surface has no effect in specular mode (sim.cu:740-772)
-        k_surf_conv32<<<g.nb, 256, 0, ts>>>(g.acc, g.nill, g.vmax, sc->dp.specular ? 0 : sc->dp.disable_surface, nr,
-                                            (const C32*)sc->d_C1_32, plan_view32(sc->plan2), g.refl, g.sscr,
-                                            g.Lw.surf_slot);
-        RP_LAUNCHED();
+        const bool circ = sc->dp.cmode == 1;
+        if (circ) {
+            // specular with circular convolution: the reference's surface
+            // convolution is commented out, so the surface is zero (sim.cu:765-767)
+            RP_CUDA(cudaMemsetAsync(g.refl, 0, sizeof(C32) * g.nb * nr, ts));
+        } else {
+            // disable_surface has no effect in specular mode (sim.cu:740-772)
+            k_surf_conv32<<<g.nb, 256, 0, ts>>>(g.acc, g.nill, g.vmax, sc->dp.specular ? 0 : sc->dp.disable_surface,
+                                                nr, (const C32*)sc->d_C1_32, plan_view32(sc->plan2), g.refl, g.sscr,
+                                                g.Lw.surf_slot);
+            RP_LAUNCHED();
+        }
         const C32* r0 = nullptr;
         if (g.pairs && g.t0rec) {      // ttype-0 targets: ordered sum, one chirp convolution per trace
             const size_t psm = (size_t)nr * sizeof(double2);
@@ -1691,7 +1701,9 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
             k_t0_sum32<<<dim3((nr + 255) / 256, g.nb), 256, 0, ts>>>(g.t0part, nr, g.sum0);
             RP_LAUNCHED();
             k_t0_conv32<<<g.nb, 256, 0, ts>>>(g.sum0, nr, (const C32*)(sc->dp.specular ? sc->d_C1_32 : sc->d_C2_32),
-                                             plan_view32(sc->plan2), g.r0, g.t0scr, g.Lw.surf_slot);
+                                             plan_view32(sc->plan2), g.r0, g.t0scr, g.Lw.surf_slot, circ ? 1 : 0,
+                                             (const C32*)sc->d_CR_32, circ ? plan_view32(sc->planR)
+                                                                           : plan_view32(sc->plan2));
             RP_LAUNCHED();
             r0 = g.r0;
         }
@@ -1803,9 +1815,11 @@ void next_segment(const rp_scene* sc, const std::vector<int>& ub, int64_t s0, in
 }
 
 int check_scene(const rp_scene* sc) {
-    if (sc->dp.cmode != 0) {
-        rp_set_error("fast form: only linear convolution (the default mode and specular with linear "
-                     "convolution); the plain form runs the other specular variants");
+    // cmode 1 (circular convolution) exists in specular mode with ttype-0
+    // targets only (rp_scene_create refuses the rest)
+    if (sc->dp.cmode == 2) {
+        rp_set_error("fast form: specular mode without convolution (direct sums over every bin) runs in "
+                     "the plain form");
         return RP_ERR_UNSUPPORTED;
     }
     if (sc->planN.pow2) { rp_set_error("internal: N = 2 nr - 1 is a power of two"); return RP_ERR_INTERNAL; }

@@ -160,18 +160,30 @@ def test_fast_specular_batched_with_default_mode(built_lib):
             sc.close()
 
 
-def test_fast_refuses_other_specular_modes(built_lib):
-    # circular convolution and no convolution (ttype-0 targets) stay in the
-    # plain form
+def test_fast_refuses_specular_without_convolution(built_lib):
+    # no convolution (reflRadarSignal / refrRadarSignal direct sums) stays in
+    # the plain form
     from europaraypaths_gb300 import simulator
-    circ = _spec(tiny_scene(nside=12, ntside=2, ns=1), convolution_linear=False)
-    circ["targets"][6, :] = 0.0
     none = _spec(tiny_scene(nside=12, ntside=2, ns=1), convolution=False)
     none["targets"][6, :] = 0.0
-    for sc in (circ, none):
-        with simulator.Scene(sc["params"], sc["facets"], sc["targets"]) as scene:
-            with pytest.raises(RuntimeError, match="RP_ERR_UNSUPPORTED|-6"):
-                scene.simulate(form="fast")
+    with simulator.Scene(none["params"], none["facets"], none["targets"]) as scene:
+        with pytest.raises(RuntimeError, match="RP_ERR_UNSUPPORTED|-6"):
+            scene.simulate(form="fast")
+
+
+@pytest.mark.parametrize("nr", [None, 250])
+def test_fast_specular_circular_convolution(built_lib, oracle, nr):
+    # circular convolution (ttype-0 targets only): the surface is zero (the
+    # reference's convolution call is commented out) and the targets' summed
+    # phasor trace is convolved with genChirp's wrapped chirp; nr = 250: the
+    # nr-point Bluestein transform
+    from europaraypaths_gb300 import scenes
+    over = {} if nr is None else {"rx_window_m": scenes.rx_window_for_bins(nr, 4e6), "rx_window_offset_m": 24000.0}
+    sc = _spec(tiny_scene(**over), convolution_linear=False)
+    sc["targets"][6, :] = 0.0
+    got, ref, cnt, rcnt = _run(sc, oracle, complex128=True)
+    assert np.array_equal(cnt, rcnt)
+    check(got, ref)
 
 
 def test_fast_specular_autotuner_records_choice(built_lib):

@@ -124,6 +124,8 @@ def test_sim_auto_picks_fast_form_for_ttype0(built_lib):
     sc = _t0(tiny_scene(nside=12, ntside=2, ns=1))
     p = param_gen.to_rp_params(sc["params"])
     assert sim.pick_form(p, sc["targets"]) == "fast"
-    sc["params"]["convolution_linear"] = False
     sc["params"]["specular"] = True
+    sc["params"]["convolution_linear"] = False       # circular convolution: fast form
+    assert sim.pick_form(param_gen.to_rp_params(sc["params"]), sc["targets"]) == "fast"
+    sc["params"]["convolution"] = False              # direct sums: plain form
     assert sim.pick_form(param_gen.to_rp_params(sc["params"]), sc["targets"]) == "plain"
