@@ -1013,6 +1013,8 @@ template <class Aa>
 void fast_take_pairs(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<C32>((size_t)RP_PARTS * L.nb * L.tstride * L.Wt);   // T parts
     if (sc->dp.specular) a.template take<C32>((size_t)RP_PARTS * L.nb * L.tstride * L.Wt);   // T2 parts
+    if (sc->dp.cmode == 2)        // direct sums: the facet groups' partial traces
+        a.template take<double2>((size_t)L.nb * RP_DS_GROUPS * sc->nr);
     if (sc->nt1 < sc->nt) {       // ttype-0 sum, r0, scratch, group partials
         a.template take<C32>((size_t)L.nb * (2 * sc->nr + L.surf_slot));
         a.template take<double2>((size_t)L.nb * RP_T0_GROUPS * sc->nr);
@@ -1229,6 +1231,7 @@ struct Seg {
     C32* T2 = nullptr;      // specular mode: outbound-leg parts
     C32* sum0 = nullptr; C32* r0 = nullptr; C32* t0scr = nullptr;   // ttype-0 targets
     double2* t0part = nullptr;
+    double2* dpart = nullptr;       // specular mode without convolution: direct-sum partials
     C32* tscr = nullptr;    // per-trace crop-stage scratch (nr > 4096)
 };
 
@@ -1541,7 +1544,9 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         g.L = fast_layout(g.sc, g.nb, g.tmax, g.Wt);
         g.cmode = conv_mode(g.sc);
         g.nsplit = (int)conv_splits(g.L.tstride);
-        g.pairs = g.sc->nt > 0 && g.sc->nf > 0 && g.tmax > 0;
+        // specular mode without convolution has no pair or compression
+        // stage: its direct sums (launch_direct) take the facets and pairs
+        g.pairs = g.sc->nt > 0 && g.sc->nf > 0 && g.tmax > 0 && g.sc->dp.cmode != 2;
         if (g.pairs) ps.push_back(&g);
         if (g.pairs && g.cmode <= 2) {
             cs[g.cmode].push_back(&g);
@@ -1563,6 +1568,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     for (Seg& g : segs) {
         g.T = b.take<C32>((size_t)RP_PARTS * g.nb * g.L.tstride * g.Wt);
         g.T2 = g.sc->dp.specular ? b.take<C32>((size_t)RP_PARTS * g.nb * g.L.tstride * g.Wt) : nullptr;
+        g.dpart = g.sc->dp.cmode == 2 ? b.take<double2>((size_t)g.nb * RP_DS_GROUPS * g.sc->nr) : nullptr;
         if (g.t0rec) {
             g.sum0 = b.take<C32>((size_t)g.nb * g.sc->nr);
             g.r0 = b.take<C32>((size_t)g.nb * g.sc->nr);
@@ -1676,6 +1682,25 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         const cudaStream_t ts = par ? ws->aux[si % rp_workspace::kAux] : st;
         const rp_scene* sc = g.sc;
         const int nr = sc->nr;
+        if (g.dpart) {          // specular mode without convolution
+            DirectArgs D;
+            const DevParams& dp = sc->dp;
+            D.F = sc->d_sorted; D.nf = std::max<int64_t>(sc->nf, 1); D.idx = g.idx; D.nill = g.nill; D.traces = g.trb;
+            D.TG = sc->d_targets_fast; D.nt = sc->nt; D.tlist = g.tlist; D.ntl = g.ntl; D.tstride = g.Lw.tstride;
+            D.sv = g.sv; D.spec = g.spec; D.t0rec = g.t0rec; D.rstride = g.Lw.rstride;
+            D.PR = sc->d_prisms; D.np = sc->np; D.nr = nr;
+            D.beta = dp.dr / dp.rng_res; D.inv_dr = dp.inv_dr; D.turn2 = 2.0 * dp.turn; D.c_c2 = dp.c_over_c2;
+            D.alpha2 = dp.alpha2; D.ks2 = (float)(dp.ks * dp.ks);
+            D.e21 = (float)(dp.eps2 / dp.eps1); D.s2tir = (float)(std::sin(1e4) * std::sin(1e4));
+            const double pikr = RP_PI * dp.fs / dp.lam;
+            D.pikr2 = (float)(pikr * pikr);
+            const PairArgs R = seg_pair_args_t0(g);        // the rerad_funct test
+            D.rf = R.rf; D.rcos = R.rcos; D.rgl = R.rgl;
+            D.part = g.dpart;
+            if (int rc = launch_direct(D, g.nb, g.d_out, g.out64, (int)g.s0, ts)) return rc;
+            RP_LAUNCHED();
+            continue;
+        }
         const bool circ = sc->dp.cmode == 1;
         if (circ) {
             // specular with circular convolution: the reference's surface
@@ -1815,13 +1840,9 @@ void next_segment(const rp_scene* sc, const std::vector<int>& ub, int64_t s0, in
 }
 
 int check_scene(const rp_scene* sc) {
-    // cmode 1 (circular convolution) exists in specular mode with ttype-0
-    // targets only (rp_scene_create refuses the rest)
-    if (sc->dp.cmode == 2) {
-        rp_set_error("fast form: specular mode without convolution (direct sums over every bin) runs in "
-                     "the plain form");
-        return RP_ERR_UNSUPPORTED;
-    }
+    // every mode rp_scene_create accepts runs here: the default mode,
+    // specular with linear convolution, and specular with circular or no
+    // convolution (ttype-0 targets only)
     if (sc->planN.pow2) { rp_set_error("internal: N = 2 nr - 1 is a power of two"); return RP_ERR_INTERNAL; }
     return RP_OK;
 }

@@ -1276,4 +1276,39 @@ int launch_pairs_spec(int deg, int cfg, const PairArgs& P, int64_t items, int sm
 // items (deg matters in specular mode only).
 int launch_pairs_t0(int deg, bool ortho, bool spec, const PairArgs& P, int64_t items, int sms, cudaStream_t st);
 
+// Specular mode without convolution (rp_direct.cu): the direct sums of
+// reflRadarSignal and refrRadarSignal per (trace, bin).
+#define RP_DS_THREADS 256     // bins per tile = facets per staged chunk
+#define RP_DS_GROUPS 16       // fixed facet-chunk groups per trace (ordered partial sums)
+struct DirectArgs {
+    const double* F;        // sorted facet store, SoA [12][nf]
+    int64_t nf;             // its stride, also the stride of idx and sv
+    const int* idx;         // [nb][nf] illuminated facets (store order)
+    const int* nill;
+    const double* traces;   // [nb][9]
+    const double* TG;       // fast target store [7][nt]
+    int64_t nt;
+    const int* tlist;       // [nb][tstride] in-aperture targets (all ttype 0 in this mode)
+    const int* ntl;
+    int64_t tstride;
+    const C32* sv;          // [nb][nf] surface phasors fRe exp(+j 4 pi_F Itd / lam)
+    const FacetSpec* spec;  // [nb][rstride / 2]
+    const FacetT0* t0rec;   // [nb][rstride / 2]
+    int64_t rstride;
+    const double* PR;       // prisms
+    int64_t np;
+    int nr;
+    double beta;            // dr / rng_res: sinc((r - R)/res) = sinc(beta (i - x))
+    double inv_dr;
+    double turn2;           // 2 turn: phase 4 pi_F R / lam = 2 pi (turn2 R)
+    double c_c2;            // c / c2 of refrRadarSignal's range
+    double alpha2;
+    float ks2;              // ks^2
+    float e21, s2tir, pikr2;
+    int rf;
+    float rcos, rgl;
+    double2* part;          // [nb][RP_DS_GROUPS][nr]
+};
+int launch_direct(const DirectArgs& A, int nb, void* d_out, int out64, int s0, cudaStream_t st);
+
 }  // namespace rpk

@@ -71,10 +71,10 @@ def load_inputs(params_path, facets_path, targets_path):
 
 
 def pick_form(p, targets):
-    """``auto``: the fast form whenever the mode convolves (the default mode,
-    specular with linear or circular convolution, targets of either type),
-    else the plain FP64 form, which runs every mode the reference defines."""
-    return "fast" if p.convolution else "plain"
+    """``auto``: the fast form, which runs every mode the reference defines
+    (the default mode; specular with linear, circular or no convolution;
+    targets of either type).  ``plain`` selects the FP64 form explicitly."""
+    return "fast"
 
 
 def run(params_path, facets_path, targets_path, outdir, form="auto", batch=64, quiet=False, radargram=None):

@@ -160,15 +160,29 @@ def test_fast_specular_batched_with_default_mode(built_lib):
             sc.close()
 
 
-def test_fast_refuses_specular_without_convolution(built_lib):
-    # no convolution (reflRadarSignal / refrRadarSignal direct sums) stays in
-    # the plain form
-    from europaraypaths_gb300 import simulator
-    none = _spec(tiny_scene(nside=12, ntside=2, ns=1), convolution=False)
-    none["targets"][6, :] = 0.0
-    with simulator.Scene(none["params"], none["facets"], none["targets"]) as scene:
-        with pytest.raises(RuntimeError, match="RP_ERR_UNSUPPORTED|-6"):
-            scene.simulate(form="fast")
+@pytest.mark.parametrize("case", ["targets", "surface_only", "prisms_rerad4", "non_pow2"])
+def test_fast_specular_without_convolution(built_lib, oracle, case):
+    # no convolution: reflRadarSignal and refrRadarSignal, direct sums of
+    # sinc((r - R)/res) phasors over every (source, bin), ttype-0 targets
+    from europaraypaths_gb300 import scenes
+    over = {"convolution": False}
+    if case == "non_pow2":
+        over.update(rx_window_m=scenes.rx_window_for_bins(250, 4e6), rx_window_offset_m=24000.0)
+    sc = _spec(tiny_scene(), **over)
+    sc["targets"][6, :] = 0.0
+    prisms = None
+    if case == "prisms_rerad4":
+        sc["params"]["rerad_funct"] = 4
+        prisms = np.array([[2e-3], [-500.0], [-500.0], [-1200.0], [300.0], [400.0], [-100.0]])
+    tg = np.zeros((7, 0)) if case == "surface_only" else None
+    got, ref, cnt, rcnt = _run(sc, oracle, prisms=prisms, targets=tg, complex128=True)
+    assert np.array_equal(cnt, rcnt)
+    check(got, ref)
+    if tg is None:      # the targets' part alone (complex128 difference)
+        got0, ref0, _, _ = _run(sc, oracle, prisms=prisms, targets=np.zeros((7, 0)), complex128=True)
+        dg, dr = got - got0, ref - ref0
+        assert np.abs(dr).max() > 0
+        assert rel_l2(dg, dr) <= REL_L2, rel_l2(dg, dr)
 
 
 @pytest.mark.parametrize("nr", [None, 250])

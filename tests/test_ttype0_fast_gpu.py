@@ -125,7 +125,7 @@ def test_sim_auto_picks_fast_form_for_ttype0(built_lib):
     p = param_gen.to_rp_params(sc["params"])
     assert sim.pick_form(p, sc["targets"]) == "fast"
     sc["params"]["specular"] = True
-    sc["params"]["convolution_linear"] = False       # circular convolution: fast form
+    sc["params"]["convolution_linear"] = False       # circular convolution
     assert sim.pick_form(param_gen.to_rp_params(sc["params"]), sc["targets"]) == "fast"
-    sc["params"]["convolution"] = False              # direct sums: plain form
-    assert sim.pick_form(param_gen.to_rp_params(sc["params"]), sc["targets"]) == "plain"
+    sc["params"]["convolution"] = False              # direct sums
+    assert sim.pick_form(param_gen.to_rp_params(sc["params"]), sc["targets"]) == "fast"
