@@ -282,6 +282,55 @@ def run_mode(args, sc, track, stream, default_value, specular=False, ttype0=Fals
         scene.close()
 
 
+def run_direct(args, sc, track, stream):
+    """Specular mode without convolution (reflRadarSignal / refrRadarSignal
+    direct sums over sources x bins) on the large scene's facets: the fast
+    form over every 64th target (all ttype 0), in source-bin terms/s, and one
+    surface-only trace in both forms (the plain form's FP64 direct sum)."""
+    import torch
+    from europaraypaths_gb300 import simulator
+    p = dict(sc["params"])
+    p.update(specular=True, convolution=False)
+    tg = np.array(sc["targets"], copy=True)[:, ::64]
+    tg[6, :] = 0.0
+    dev = torch.cuda.current_device()
+    out = {"note": "large-scene facets, every 64th target as ttype 0, specular=true, convolution=false"}
+
+    def timed(scene, tr, form):
+        d = torch.from_numpy(np.ascontiguousarray(tr)).cuda()
+        o = torch.empty((tr.shape[0], scene.nr), dtype=torch.complex64, device="cuda")
+        c = np.zeros((tr.shape[0], 2), np.int64)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        scene.simulate_device(d, o, form=form, stream=stream, counts=c)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), c
+
+    scene = simulator.Scene(p, sc["facets"], tg, device=dev)
+    try:
+        n = 2
+        timed(scene, track[900:900 + n], "fast")          # warm-up
+        ms, c = timed(scene, track[1000:1000 + n], "fast")
+        terms = float(np.sum(c[:, 0].astype(np.float64) * (1 + c[:, 1]))) * scene.nr
+        out.update({"value": terms / (ms / 1e3), "unit": "source-bin terms/s", "traces": n, "ms": ms,
+                    "mean_counts_per_trace": [float(c[:, 0].mean()), float(c[:, 1].mean())]})
+    finally:
+        scene.close()
+    scene = simulator.Scene(p, sc["facets"], np.zeros((7, 0)), device=dev)
+    try:
+        tr = track[1000:1001]
+        timed(scene, tr, "fast")
+        fms, _ = timed(scene, tr, "fast")
+        pms, _ = timed(scene, tr, "plain")
+        out["surface_only_1_trace"] = {"fast_ms": fms, "plain_ms": pms, "fast_over_plain": pms / fms}
+    finally:
+        scene.close()
+    return out
+
+
 def run_io(n_facets=200_000, n_traces=200, nr=4096):
     """Host file I/O of the binary stores against the reference's text formats
     (seeded synthetic facets; no device work): parse a .fct text file vs map a
@@ -620,6 +669,10 @@ def main():
                     line[key] = run_mode(args, sc, track, stream, value, **kw)
                 except Exception as e:
                     line[key] = {"error": f"{type(e).__name__}: {e}"}
+            try:
+                line["direct"] = run_direct(args, sc, track, stream)
+            except Exception as e:
+                line["direct"] = {"error": f"{type(e).__name__}: {e}"}
         if args.focus and world == 1:
             try:
                 line["focus"] = run_focus()

@@ -11,10 +11,12 @@
 // (pi beta (i - x_j)): each source carries two complex weights c_j, s_j
 // (w_j cos / sin(pi beta x_j) / (pi beta)) and a bin i adds c_j / (i - x_j)
 // and s_j / (i - x_j) -- one reciprocal and four FMAs per (source, bin) --
-// and multiplies the sums by sin(pi beta i), cos(pi beta i) once.  Sources
-// within one bin of i (where the two products would cancel) take the sinc
-// directly.  The per-source geometry (ranges, phases) is FP64, amplitudes
-// FP32.
+// and multiplies the sums by sin(pi beta i), cos(pi beta i) once.  A source
+// at |i - x_j| = d contributes terms of size |w| / (pi beta d) to the FP32
+// sums, whose rounding then costs about 2 eps / (pi beta d) of |w| in the
+// recombined bin: sources closer than RP_DS_NEAR (1/128 bin: at most ~2e-5
+// of |w| beyond it) take the sinc directly instead.  The per-source
+// geometry (ranges, phases) is FP64, amplitudes FP32.
 #include <algorithm>
 
 #include "rp_common.cuh"
@@ -24,6 +26,8 @@
 namespace rpk {
 
 namespace {
+
+#define RP_DS_NEAR (1.f / 128.f)
 
 // sin(pi beta x), cos(pi beta x) for a large x: exact reduction in FP64.
 __device__ __forceinline__ void sincospi_bx(double bx, float& sp, float& cp) {
@@ -43,43 +47,64 @@ __device__ __forceinline__ void ds_entry(double x, float wr, float wi, double ba
     eb = make_float4(wi * sp * ip, wr, wi, 0.f);
 }
 
-// The bin's sums over the block's staged entries (FP32 within the batch).
-__device__ __forceinline__ void ds_accumulate(const float4* sa, const float4* sb, float fi, float pib, double* acc) {
-    float cr = 0.f, ci = 0.f, sr = 0.f, si = 0.f, nre = 0.f, nim = 0.f;
-#pragma unroll 4
+// The thread's RP_DS_BPT bins (fi[b]: positions relative to the tile
+// centre) take every staged entry; sums in FP32 over the block's facet
+// group (its FP64 total is formed across groups).
+__device__ __forceinline__ void ds_accumulate(const float4* sa, const float4* sb, const float* fi, float pib,
+                                              float (*acc)[6]) {
+#pragma unroll 2
     for (int k = 0; k < RP_DS_THREADS; ++k) {
         const float4 a = sa[k], b = sb[k];
-        const float d = fi - a.x;
-        if (fabsf(d) < 1.f) {
-            const float z = pib * d;
-            const float sc = fabsf(z) < 3.14159265e-6f ? 1.f : __sinf(z) / z;
-            nre = fmaf(b.y, sc, nre);
-            nim = fmaf(b.z, sc, nim);
-        } else {
-            const float r = rcp_a(d);
-            cr = fmaf(a.y, r, cr);
-            ci = fmaf(a.z, r, ci);
-            sr = fmaf(a.w, r, sr);
-            si = fmaf(b.x, r, si);
+        bool any_near = false;
+        // far field, branch-free (the near bins get r = 0 here)
+#pragma unroll
+        for (int q = 0; q < RP_DS_BPT; ++q) {
+            const float d = fi[q] - a.x;
+            const bool near = fabsf(d) < RP_DS_NEAR;
+            any_near |= near;
+            const float r = near ? 0.f : rcp_a(d);
+            acc[q][0] = fmaf(a.y, r, acc[q][0]);
+            acc[q][1] = fmaf(a.z, r, acc[q][1]);
+            acc[q][2] = fmaf(a.w, r, acc[q][2]);
+            acc[q][3] = fmaf(b.x, r, acc[q][3]);
+        }
+        // the source's near bin (if any): the sinc itself
+        if (__any_sync(0xffffffffu, any_near)) {
+#pragma unroll
+            for (int q = 0; q < RP_DS_BPT; ++q) {
+                const float d = fi[q] - a.x;
+                if (fabsf(d) < RP_DS_NEAR) {
+                    const float z = pib * d;
+                    const float sc = fabsf(z) < 3.14159265e-6f ? 1.f : __sinf(z) / z;
+                    acc[q][4] = fmaf(b.y, sc, acc[q][4]);
+                    acc[q][5] = fmaf(b.z, sc, acc[q][5]);
+                }
+            }
         }
     }
-    acc[0] += cr; acc[1] += ci; acc[2] += sr; acc[3] += si; acc[4] += nre; acc[5] += nim;
 }
 
-// Block (tile of RP_DS_THREADS bins, facet group g, trace s).  Each thread
-// stages one facet of the chunk and evaluates that facet's sources: its
-// surface phasor, then its pair with every in-aperture target in list order.
-__global__ void __launch_bounds__(RP_DS_THREADS) k_direct32(const __grid_constant__ DirectArgs A) {
+// Block (tile of RP_DS_TILE bins, facet group g, trace s); thread tid owns
+// bins tile base + tid + k RP_DS_THREADS.  Each thread stages one facet of
+// the chunk and evaluates that facet's sources: its surface phasor, then its
+// pair with every in-aperture target in list order.
+__global__ void __launch_bounds__(RP_DS_THREADS, 1) k_direct32(const __grid_constant__ DirectArgs A) {
     __shared__ float4 sa[RP_DS_THREADS], sb[RP_DS_THREADS];
     const int tile = blockIdx.x, g = blockIdx.y, s = blockIdx.z, tid = threadIdx.x;
     const int n = A.nill[s];
-    const int i = tile * RP_DS_THREADS + tid;
-    const double base = (double)(tile * RP_DS_THREADS);
-    const float fi = (float)tid;
+    // entries carry x relative to the tile centre (small, exact in FP32)
+    const double base = (double)(tile * RP_DS_TILE + RP_DS_TILE / 2);
+    float fi[RP_DS_BPT];
+#pragma unroll
+    for (int q = 0; q < RP_DS_BPT; ++q) fi[q] = (float)(tid + q * RP_DS_THREADS - RP_DS_TILE / 2);
     const float pib = (float)(RP_PI * A.beta);
     const TraceRow t = load_trace(A.traces, s);
     const int nq = A.ntl[s];
-    double acc[6] = {0, 0, 0, 0, 0, 0};
+    float acc[RP_DS_BPT][6];
+#pragma unroll
+    for (int q = 0; q < RP_DS_BPT; ++q)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) acc[q][k] = 0.f;
     const int nch = (n + RP_DS_THREADS - 1) / RP_DS_THREADS;
     const int c0 = (int)((int64_t)nch * g / RP_DS_GROUPS), c1 = (int)((int64_t)nch * (g + 1) / RP_DS_GROUPS);
     for (int c = c0; c < c1; ++c) {
@@ -125,8 +150,12 @@ __global__ void __launch_bounds__(RP_DS_THREADS) k_direct32(const __grid_constan
             if (ok) {
                 const int64_t ti = A.tlist[(size_t)s * A.tstride + q];
                 const double ex = fx - A.TG[ti], ey = fy - A.TG[A.nt + ti], ez = fz - A.TG[2 * A.nt + ti];
-                const double Ttd = sqrt(ex * ex + ey * ey + ez * ez);
-                const float rinv = (float)(1.0 / Ttd);
+                // Ttd from an FP32 reciprocal square root and one FP64 Newton step
+                const double T2 = ex * ex + ey * ey + ez * ez;
+                const float r0 = rsqrt_a((float)T2);
+                const double rr0 = (double)r0;
+                const double Ttd = T2 * rr0 * (1.5 - 0.5 * T2 * rr0 * rr0);
+                const float rinv = r0;
                 const float exf = (float)ex, eyf = (float)ey, ezf = (float)ez;
                 const float pbr = (exf * nx + eyf * ny + ezf * nz) * rinv;     // cos Tth
                 const float aT = fmaxf(0.f, 1.f - pbr * pbr);
@@ -179,12 +208,16 @@ __global__ void __launch_bounds__(RP_DS_THREADS) k_direct32(const __grid_constan
             ds_accumulate(sa, sb, fi, pib, acc);
         }
     }
-    if (i < A.nr) {
-        double sp, cp;
-        sincospi(A.beta * (double)i, &sp, &cp);
-        const double re = sp * acc[0] - cp * acc[2] + acc[4];
-        const double im = sp * acc[1] - cp * acc[3] + acc[5];
-        A.part[((size_t)s * RP_DS_GROUPS + g) * A.nr + i] = make_double2(re, im);
+#pragma unroll
+    for (int q = 0; q < RP_DS_BPT; ++q) {
+        const int i = tile * RP_DS_TILE + tid + q * RP_DS_THREADS;
+        if (i < A.nr) {
+            double sp, cp;
+            sincospi(A.beta * (double)i, &sp, &cp);
+            const double re = sp * acc[q][0] - cp * acc[q][2] + acc[q][4];
+            const double im = sp * acc[q][1] - cp * acc[q][3] + acc[q][5];
+            A.part[((size_t)s * RP_DS_GROUPS + g) * A.nr + i] = make_double2(re, im);
+        }
     }
 }
 
@@ -207,7 +240,7 @@ __global__ void k_direct_fin(const double2* __restrict__ part, int nr, void* __r
 }  // namespace
 
 int launch_direct(const DirectArgs& A, int nb, void* d_out, int out64, int s0, cudaStream_t st) {
-    const dim3 grid((unsigned)((A.nr + RP_DS_THREADS - 1) / RP_DS_THREADS), RP_DS_GROUPS, (unsigned)nb);
+    const dim3 grid((unsigned)((A.nr + RP_DS_TILE - 1) / RP_DS_TILE), RP_DS_GROUPS, (unsigned)nb);
     k_direct32<<<grid, RP_DS_THREADS, 0, st>>>(A);
     RP_CUDA(cudaGetLastError());
     k_direct_fin<<<dim3((unsigned)((A.nr + 255) / 256), (unsigned)nb), 256, 0, st>>>(A.part, A.nr, d_out, out64, s0);

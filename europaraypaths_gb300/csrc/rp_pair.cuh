@@ -1278,8 +1278,10 @@ int launch_pairs_t0(int deg, bool ortho, bool spec, const PairArgs& P, int64_t i
 
 // Specular mode without convolution (rp_direct.cu): the direct sums of
 // reflRadarSignal and refrRadarSignal per (trace, bin).
-#define RP_DS_THREADS 256     // bins per tile = facets per staged chunk
-#define RP_DS_GROUPS 16       // fixed facet-chunk groups per trace (ordered partial sums)
+#define RP_DS_THREADS 256     // facets per staged chunk
+#define RP_DS_BPT 8           // bins per thread (strided by RP_DS_THREADS)
+#define RP_DS_TILE (RP_DS_THREADS * RP_DS_BPT)
+#define RP_DS_GROUPS 128      // fixed facet-chunk groups per trace (ordered partial sums)
 struct DirectArgs {
     const double* F;        // sorted facet store, SoA [12][nf]
     int64_t nf;             // its stride, also the stride of idx and sv
