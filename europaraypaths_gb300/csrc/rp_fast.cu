@@ -1424,12 +1424,41 @@ ConvArgs seg_conv_args(const Seg& g) {
     return C;
 }
 
-// Pair launch of a wave: the single-batch kernel (constants in the parameter
-// bank) for one segment, the multi-job kernel otherwise.  cap bounds the
-// items taken (autotuner probes); UINT_MAX runs everything.
-int launch_pairs(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsigned int* d_start,
-                 unsigned int* d_work, int cfg, int sms, cudaStream_t st) {
+// The single-batch pair kernel of one segment in configuration cfg.
+int launch_pairs_one(const Seg& g, unsigned int* work, int cfg, int sms, cudaStream_t st) {
     const size_t pair_smem = RP_PAIR_SMEM_BYTES;
+    PairArgs P = seg_pair_args(g);
+    P.work = work;
+    void (*pk)(const PairArgs) = pick_pair_kernel(g.deg, cfg, g.sc->ortho != 0);
+    if (int rc = rp_allow_dyn_smem((const void*)pk, pair_smem)) return rc;
+    int occ = 0;
+    RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, RP_PAIR_THREADS, pair_smem));
+    const int64_t items = (int64_t)g.nb * P.tblocks * RP_PARTS;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(occ, 1) * sms, items));
+    pk<<<grid, RP_PAIR_THREADS, pair_smem, st>>>(P);
+    return RP_OK;
+}
+
+// Pair launch of a wave: the single-batch kernel (constants in the parameter
+// bank) for one segment; for several, the multi-job kernel (cfg 0-3) or one
+// single-batch kernel per segment (cfg 4-7: configuration cfg - 4), on the
+// workspace's auxiliary streams when par.  The multi-job kernel holds its
+// job's constants in registers and local memory; the per-segment kernels
+// read theirs from the parameter bank, at the price of one launch each.
+// seg_work: one work counter per segment of ps.
+int launch_pairs(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsigned int* d_start,
+                 unsigned int* d_work, unsigned int* seg_work, int cfg, int sms, cudaStream_t st,
+                 rp_workspace* ws, bool par) {
+    if (ps.size() > 1 && cfg >= 4) {
+        if (par) ws->fork(st);
+        for (size_t i = 0; i < ps.size(); ++i) {
+            const cudaStream_t ss = par ? ws->aux[i % rp_workspace::kAux] : st;
+            if (int rc = launch_pairs_one(*ps[i], seg_work + i, cfg - 4, sms, ss)) return rc;
+            RP_LAUNCHED();
+        }
+        if (par) ws->join(st);
+        return RP_OK;
+    }
     if (ps.size() == 1 && ps[0]->sc->dp.specular) {     // specular waves hold one segment
         const Seg& g = *ps[0];
         PairArgs P = seg_pair_args(g);
@@ -1437,16 +1466,7 @@ int launch_pairs(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsig
         const int64_t items = (int64_t)g.nb * P.tblocks * RP_PARTS;
         if (int rc = launch_pairs_spec(g.deg, cfg, P, items, sms, st)) return rc;
     } else if (ps.size() == 1) {
-        const Seg& g = *ps[0];
-        PairArgs P = seg_pair_args(g);
-        P.work = d_work;
-        void (*pk)(const PairArgs) = pick_pair_kernel(g.deg, cfg, g.sc->ortho != 0);
-        if (int rc = rp_allow_dyn_smem((const void*)pk, pair_smem)) return rc;
-        int occ = 0;
-        RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, RP_PAIR_THREADS, pair_smem));
-        const int64_t items = (int64_t)g.nb * P.tblocks * RP_PARTS;
-        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(occ, 1) * sms, items));
-        pk<<<grid, RP_PAIR_THREADS, pair_smem, st>>>(P);
+        if (int rc = launch_pairs_one(*ps[0], d_work, cfg, sms, st)) return rc;
     } else {
         int64_t items = 0;
         for (const Seg* g : ps) items += (int64_t)g->nb * ((g->L.tstride + RP_PAIR_THREADS - 1) / RP_PAIR_THREADS) * RP_PARTS;
@@ -1457,40 +1477,48 @@ int launch_pairs(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsig
     return RP_OK;
 }
 
-// Zero the pair-stage outputs of a wave (T windows, work counter, flags).
-int zero_pairs(const std::vector<Seg*>& ps, unsigned int* d_work, cudaStream_t st) {
+// Zero the pair-stage outputs of a wave (T windows, work counters, flags).
+int zero_pairs(const std::vector<Seg*>& ps, unsigned int* d_work, unsigned int* seg_work, cudaStream_t st) {
     for (const Seg* g : ps) {
         RP_CUDA(cudaMemsetAsync(g->T, 0, sizeof(C32) * RP_PARTS * g->nb * g->L.tstride * g->Wt, st));
         if (g->T2) RP_CUDA(cudaMemsetAsync(g->T2, 0, sizeof(C32) * RP_PARTS * g->nb * g->L.tstride * g->Wt, st));
         RP_CUDA(cudaMemsetAsync(g->misc + 1, 0, sizeof(int) * 3, st));
     }
     RP_CUDA(cudaMemsetAsync(d_work, 0, sizeof(unsigned int), st));
+    RP_CUDA(cudaMemsetAsync(seg_work, 0, sizeof(unsigned int) * ps.size(), st));
     return RP_OK;
 }
 
-// Choose the pair configuration of a wave: the tuned one, or probe all four
-// (two for the specular kernel; each a full launch on this wave's items,
-// outputs re-zeroed after).  Tuned per kind: single kernel (0), multi-job
-// (1) or specular (2), and sinc degree.
+// Choose the pair configuration of a wave: the tuned one, or probe every
+// candidate (four for one segment, two for the specular kernel, eight for a
+// multi-segment wave: the multi-job kernel and per-segment launches in each
+// configuration); each probe is a full launch on this wave's items, outputs
+// re-zeroed after.  Tuned per kind: single kernel (0), multi-segment (1) or
+// specular (2), and sinc degree.
 int choose_cfg(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsigned int* d_start,
-               unsigned int* d_work, int sms, cudaStream_t st, int* cfg_out) {
+               unsigned int* d_work, unsigned int* seg_work, int sms, cudaStream_t st, rp_workspace* ws,
+               bool par, int* cfg_out) {
     const bool spec = ps.size() == 1 && ps[0]->sc->dp.specular;
     const int multi = spec ? 2 : (ps.size() > 1 ? 1 : 0);
     const int deg = multi == 1 ? -1 : ps[0]->deg;
-    const int ncfg = spec ? 2 : 4;
-    if (!autotune_on()) { *cfg_out = spec ? (ps[0]->sc->pair_cfg & 1) : ps[0]->sc->pair_cfg; return RP_OK; }
+    const int ncfg = spec ? 2 : (multi == 1 ? 8 : 4);
+    if (!autotune_on()) {
+        const int c = ps[0]->sc->pair_cfg;
+        *cfg_out = spec ? (c & 1) : (multi == 1 ? c : (c & 3));
+        return RP_OK;
+    }
     int c = tuned_lookup(multi, deg);
     if (c >= 0) { *cfg_out = c; return RP_OK; }
     cudaEvent_t e0, e1;
     RP_CUDA(cudaEventCreate(&e0));
     RP_CUDA(cudaEventCreate(&e1));
     float best = 1e30f;
-    int bestc = spec ? (ps[0]->sc->pair_cfg & 1) : ps[0]->sc->pair_cfg;
+    int bestc = spec ? (ps[0]->sc->pair_cfg & 1) : (ps[0]->sc->pair_cfg & 3);
     for (int k = 0; k < ncfg; ++k) {
-        int rc = zero_pairs(ps, d_work, st);
+        int rc = zero_pairs(ps, d_work, seg_work, st);
         if (rc) return rc;
         RP_CUDA(cudaEventRecord(e0, st));
-        rc = launch_pairs(ps, d_jobs, d_start, d_work, k, sms, st);
+        rc = launch_pairs(ps, d_jobs, d_start, d_work, seg_work, k, sms, st, ws, par);
         if (rc) return rc;
         RP_CUDA(cudaEventRecord(e1, st));
         RP_CUDA(cudaEventSynchronize(e1));
@@ -1502,7 +1530,7 @@ int choose_cfg(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsigne
     cudaEventDestroy(e1);
     tuned_store(multi, deg, bestc);
     *cfg_out = bestc;
-    return zero_pairs(ps, d_work, st);
+    return zero_pairs(ps, d_work, seg_work, st);
 }
 
 int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
@@ -1584,7 +1612,9 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         }
     }
     C32* gscr = gscr_n ? b.take<C32>(gscr_n) : nullptr;
-    unsigned int* d_work = b.take<unsigned int>(4 + nseg);     // pairs, 3 compression modes, ttype-0 per segment
+    // work counters: pairs, 3 compression modes, ttype-0 per segment, pairs per segment
+    unsigned int* d_work = b.take<unsigned int>(4 + 2 * nseg);
+    unsigned int* seg_work = d_work + 4 + nseg;
     PairJob* d_pjobs = b.take<PairJob>(std::max<size_t>(ps.size(), 1));
     unsigned int* d_pstart = b.take<unsigned int>(ps.size() + 1);
     ConvArgs* d_cjobs[3];
@@ -1593,7 +1623,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         d_cjobs[m] = b.take<ConvArgs>(std::max<size_t>(cs[m].size(), 1));
         d_cstart[m] = b.take<unsigned int>(cs[m].size() + 1);
     }
-    RP_CUDA(cudaMemsetAsync(d_work, 0, sizeof(unsigned int) * (4 + nseg), st));
+    RP_CUDA(cudaMemsetAsync(d_work, 0, sizeof(unsigned int) * (4 + 2 * nseg), st));
     for (Seg& g : segs) {
         RP_CUDA(cudaMemsetAsync(g.T, 0, sizeof(C32) * RP_PARTS * g.nb * g.L.tstride * g.Wt, st));
         if (g.T2) RP_CUDA(cudaMemsetAsync(g.T2, 0, sizeof(C32) * RP_PARTS * g.nb * g.L.tstride * g.Wt, st));
@@ -1633,10 +1663,10 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     // ---- pair stage: one launch for the wave
     if (!ps.empty()) {
         int cfg = 0;
-        int rc = choose_cfg(ps, d_pjobs, d_pstart, d_work, sms, st, &cfg);
+        int rc = choose_cfg(ps, d_pjobs, d_pstart, d_work, seg_work, sms, st, ws, par, &cfg);
         if (rc) return rc;
         g_timer.mark(1, st);
-        rc = launch_pairs(ps, d_pjobs, d_pstart, d_work, cfg, sms, st);
+        rc = launch_pairs(ps, d_pjobs, d_pstart, d_work, seg_work, cfg, sms, st, ws, par);
         if (rc) return rc;
         ++g_timer.pair_launches;
         // ttype-0 targets: one launch per segment that has them

@@ -213,8 +213,10 @@ int rp_simulate_batch(const rp_job* jobs, int njobs, rp_workspace* ws, void* str
  * configurations give bitwise identical results. */
 int rp_autotune(int enable);
 /* The tuned configuration for (kind, degree), or -1 when not tuned yet.
- * multi: 0 the single-batch kernel (configurations 0-3), 1 the multi-scene
- * kernel (degree ignored), 2 the specular-mode kernel (configurations 0-1). */
+ * multi: 0 the single-batch kernel (configurations 0-3), 1 multi-segment
+ * waves (degree ignored; 0-3 the multi-scene kernel, 4-7 one single-batch
+ * kernel per segment in configuration cfg - 4), 2 the specular-mode kernel
+ * (configurations 0-1). */
 int rp_autotune_query(int multi, int degree, int* cfg);
 
 /*

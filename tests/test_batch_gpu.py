@@ -54,6 +54,32 @@ def test_batch_equals_single_and_oracle(built_lib, oracle):
             sc.close()
 
 
+def test_batch_per_segment_launches_bitwise(built_lib):
+    # multi-segment waves in configurations 4-7 (one single-batch kernel per
+    # segment, on the workspace's auxiliary streams): bitwise the same
+    # radargrams as the multi-job kernel
+    from europaraypaths_gb300 import simulator, traces as tr_mod
+    scs = _scenes()
+    res = {}
+    simulator.autotune(False)
+    try:
+        for cfg in (1, 5, 7):
+            os.environ["RP_PAIR_CFG"] = str(cfg)
+            scenes = [simulator.Scene(s["params"], s["facets"], s["targets"]) for s in scs]
+            try:
+                trs = [tr_mod.linear_track(sc.params) for sc in scenes]
+                res[cfg] = simulator.simulate_batch(list(zip(scenes, trs)))
+            finally:
+                for sc in scenes:
+                    sc.close()
+    finally:
+        os.environ.pop("RP_PAIR_CFG", None)
+        simulator.autotune(True)
+    for cfg in (5, 7):
+        for a, b in zip(res[1], res[cfg]):
+            assert np.array_equal(_bits(a), _bits(b))
+
+
 def test_many_segments_multi_kernel(built_lib):
     # 70 traces = two segments of one scene in one wave: the multi-job kernel
     from europaraypaths_gb300 import simulator, traces as tr_mod
