@@ -63,12 +63,16 @@ k_pairs32m(const PairJob* __restrict__ jobs, const unsigned int* __restrict__ st
     RP_PAIR_SMEM_END
 }
 
+// Configurations (facet pairs per step x resident blocks per SM).  The job's
+// scene constants take registers here (the single-batch kernel reads them
+// from the parameter bank), so at 2 blocks per SM the body spills ~900
+// bytes a thread; at 1 block per SM it fits in 255 registers.
 void (*pick_multi(int cfg))(const PairJob*, const unsigned int*, int, unsigned int*) {
     switch (cfg) {
-        case 1: return k_pairs32m<2, 2>;
+        case 1: return k_pairs32m<3, 1>;
         case 2: return k_pairs32m<3, 2>;
         case 3: return k_pairs32m<4, 2>;
-        default: return k_pairs32m<2, 3>;
+        default: return k_pairs32m<4, 1>;
     }
 }
 
