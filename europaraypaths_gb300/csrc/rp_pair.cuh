@@ -678,6 +678,37 @@ __device__ __forceinline__ void bin_add1(float xr, float vre, float vim, int blo
     }
 }
 
+// Flush a thread's bin window into its target's row: each non-zero bin adds
+// to the row element it covers (outside the row: the window-overflow flag).
+// Every row load is issued before the first add, so the up to RP_WIN
+// read-modify-writes overlap instead of waiting on one another.
+__device__ __forceinline__ void flush_window(const float2* win, int tid, int blo, int b0, C32* Trow, int Wt,
+                                             unsigned int* err) {
+    float2 v[RP_WIN];
+    C32 t[RP_WIN];
+#pragma unroll
+    for (int w = 0; w < RP_WIN; ++w) v[w] = win[w * RP_PAIR_THREADS + tid];
+#pragma unroll
+    for (int w = 0; w < RP_WIN; ++w) {
+        const int o = blo + w - b0;
+        const bool nz = v[w].x != 0.f || v[w].y != 0.f;
+        t[w] = (nz && o >= 0 && o < Wt) ? Trow[o] : C32{0.f, 0.f};
+    }
+#pragma unroll
+    for (int w = 0; w < RP_WIN; ++w) {
+        if (v[w].x != 0.f || v[w].y != 0.f) {
+            const int o = blo + w - b0;
+            if (o >= 0 && o < Wt) {
+                t[w].x += v[w].x;
+                t[w].y += v[w].y;
+                Trow[o] = t[w];
+            } else {
+                atomicOr(err, 1u);
+            }
+        }
+    }
+}
+
 // ------------------------------------------------ double-float anchors --
 // Error-free transformations (Knuth TwoSum, FMA TwoProduct); the _rn
 // intrinsics keep the compiler from contracting or reordering them.
@@ -959,35 +990,8 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
                 }
             }
             // flush the window into the owned trace (both legs' in specular mode)
-            for (int w = 0; w < RP_WIN; ++w) {
-                const float2 v = win[w * RP_PAIR_THREADS + tid];
-                if (v.x != 0.f || v.y != 0.f) {
-                    const int o = blo + w - b0;
-                    if (o >= 0 && o < A.Wt) {
-                        C32 t0 = Trow[o];
-                        t0.x += v.x;
-                        t0.y += v.y;
-                        Trow[o] = t0;
-                    } else {
-                        atomicOr(A.err, 1u);
-                    }
-                }
-            }
-            if constexpr (SPEC)
-                for (int w = 0; w < RP_WIN; ++w) {
-                    const float2 v = win2[w * RP_PAIR_THREADS + tid];
-                    if (v.x != 0.f || v.y != 0.f) {
-                        const int o = blo + w - b0;
-                        if (o >= 0 && o < A.Wt) {
-                            C32 t0 = Trow2[o];
-                            t0.x += v.x;
-                            t0.y += v.y;
-                            Trow2[o] = t0;
-                        } else {
-                            atomicOr(A.err, 1u);
-                        }
-                    }
-                }
+            flush_window(win, tid, blo, b0, Trow, A.Wt, A.err);
+            if constexpr (SPEC) flush_window(win2, tid, blo, b0, Trow2, A.Wt, A.err);
         }
         __syncthreads();   // everyone done with buffer `buf` before it is refilled
     }
@@ -1225,20 +1229,7 @@ __device__ __forceinline__ void pair_item_t0(const PairArgs& A, int s, int tb, i
                     if (two) bin_add1(x0.y, re0.y, im0.y, blo, b0, win, tid, Trow, A);
                 }
             }
-            for (int w = 0; w < RP_WIN; ++w) {
-                const float2 v = win[w * RP_PAIR_THREADS + tid];
-                if (v.x != 0.f || v.y != 0.f) {
-                    const int o = blo + w - b0;
-                    if (o >= 0 && o < A.Wt) {
-                        C32 t0 = Trow[o];
-                        t0.x += v.x;
-                        t0.y += v.y;
-                        Trow[o] = t0;
-                    } else {
-                        atomicOr(A.err, 1u);
-                    }
-                }
-            }
+            flush_window(win, tid, blo, b0, Trow, A.Wt, A.err);
         }
         __syncthreads();
     }
