@@ -556,7 +556,7 @@ k_pairs32(const __grid_constant__ PairArgs A) {
         const int part = item % RP_PARTS;
         const int tb = (item / RP_PARTS) % A.tblocks;
         const int s = item / (RP_PARTS * A.tblocks);
-        pair_item<NT, ILP, ORTHO, false>(A, s, tb, part, bars, phase);
+        pair_item<NT, ILP, ORTHO, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase);
     }
     RP_PAIR_SMEM_END
 }
@@ -1426,7 +1426,7 @@ ConvArgs seg_conv_args(const Seg& g) {
 
 // The single-batch pair kernel of one segment in configuration cfg.
 int launch_pairs_one(const Seg& g, unsigned int* work, int cfg, int sms, cudaStream_t st) {
-    const size_t pair_smem = RP_PAIR_SMEM_BYTES;
+    const size_t pair_smem = pair_smem_bytes(RP_WIN_WIDE);
     PairArgs P = seg_pair_args(g);
     P.work = work;
     void (*pk)(const PairArgs) = pick_pair_kernel(g.deg, cfg, g.sc->ortho != 0);

@@ -44,19 +44,19 @@ k_pairs32m(const PairJob* __restrict__ jobs, const unsigned int* __restrict__ st
         const int s = li / (RP_PARTS * A.tblocks);
         if (ortho) {
             switch (deg) {
-                case 3: pair_item<3, ILP, true, false>(A, s, tb, part, bars, phase); break;
-                case 4: pair_item<4, ILP, true, false>(A, s, tb, part, bars, phase); break;
-                case 5: pair_item<5, ILP, true, false>(A, s, tb, part, bars, phase); break;
-                case 6: pair_item<6, ILP, true, false>(A, s, tb, part, bars, phase); break;
-                default: pair_item<0, ILP, true, false>(A, s, tb, part, bars, phase); break;
+                case 3: pair_item<3, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                case 4: pair_item<4, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                case 5: pair_item<5, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                case 6: pair_item<6, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                default: pair_item<0, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
             }
         } else {
             switch (deg) {
-                case 3: pair_item<3, ILP, false, false>(A, s, tb, part, bars, phase); break;
-                case 4: pair_item<4, ILP, false, false>(A, s, tb, part, bars, phase); break;
-                case 5: pair_item<5, ILP, false, false>(A, s, tb, part, bars, phase); break;
-                case 6: pair_item<6, ILP, false, false>(A, s, tb, part, bars, phase); break;
-                default: pair_item<0, ILP, false, false>(A, s, tb, part, bars, phase); break;
+                case 3: pair_item<3, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                case 4: pair_item<4, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                case 5: pair_item<5, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                case 6: pair_item<6, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                default: pair_item<0, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
             }
         }
     }
@@ -78,7 +78,7 @@ void (*pick_multi(int cfg))(const PairJob*, const unsigned int*, int, unsigned i
 
 int launch_pairs_multi(int cfg, const PairJob* d_jobs, const unsigned int* d_start, int njobs,
                        unsigned int* d_work, int64_t items, int sms, cudaStream_t st) {
-    const size_t smem = RP_PAIR_SMEM_BYTES;
+    const size_t smem = pair_smem_bytes(RP_WIN_WIDE);
     auto mk = pick_multi(cfg);
     if (int rc = rp_allow_dyn_smem((const void*)mk, smem)) return rc;
     int occ = 0;

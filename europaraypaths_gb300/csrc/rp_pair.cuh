@@ -18,7 +18,9 @@
 
 #define RP_CHUNK 256          // facets per chunk (one record tile)
 #define RP_PAIR_THREADS 256   // targets per pair-kernel block
-#define RP_WIN 16             // bins in a thread's per-chunk window
+#define RP_WIN 16             // bins in a thread's per-chunk window (specular kernel: two windows)
+#define RP_WIN_WIDE 24        // the default-mode and ttype-0 kernels' window: a 256-facet chunk of
+                              // 2.5 m facets at 12.5 m bins spans up to ~14 bins for one target
 #define RP_PARTS 4            // facet-range splits per (trace, target block)
 #define RP_SPIN_LIMIT (1 << 22)
 
@@ -487,6 +489,7 @@ static __device__ __noinline__ float prism_factor(float4 ra, double cx, double c
 // (an exact half rounds either way; the split is continuous there, so both
 // give the same contributions); x in (-1, 0) is truncated to bin 0 as the
 // reference does.
+template <int W>
 static __device__ __noinline__ void bin_add_edge(int b, float w, float vre, float vim, int blo, int b0,
                                           float2* win, int tid, C32* Trow, int nr, int Wt,
                                           unsigned int* err) {
@@ -499,7 +502,7 @@ static __device__ __noinline__ void bin_add_edge(int b, float w, float vre, floa
     const float w0 = 1.f - w;
     const bool two = (b + 1) < nr;
     const int sl = b - blo;
-    if ((unsigned)sl < (unsigned)(RP_WIN - 1)) {
+    if ((unsigned)sl < (unsigned)(W - 1)) {
         float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
         float2 v0 = *p0;
         v0.x = fmaf(vre, w0, v0.x);
@@ -544,12 +547,13 @@ __device__ __forceinline__ int floor_i(float x) {
     return r;
 }
 
+template <int W>
 __device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo, int b0,
                                         float2* win, int tid, C32* Trow, const PairArgs& A) {
     const int sl = floor_i(xr);
     const float w = xr - (float)sl;
     const int b = blo + sl;
-    if ((unsigned)sl < (unsigned)(RP_WIN - 1) && (unsigned)b < (unsigned)A.nr1) {
+    if ((unsigned)sl < (unsigned)(W - 1) && (unsigned)b < (unsigned)A.nr1) {
         float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
         float2* p1 = p0 + RP_PAIR_THREADS;
         float2 v0 = *p0, v1 = *p1;
@@ -561,7 +565,7 @@ __device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo,
         *p0 = v0;
         *p1 = v1;
     } else {
-        bin_add_edge(b, w, vre, vim, blo, b0, win, tid, Trow, A.nr, A.Wt, A.err);
+        bin_add_edge<W>(b, w, vre, vim, blo, b0, win, tid, Trow, A.nr, A.Wt, A.err);
     }
 }
 
@@ -569,12 +573,13 @@ __device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo,
 // fall inside the window and the trace (pair_item checks that per chunk and
 // warp): no range tests, no edge path, lane 0 before lane 1.  The clamp only
 // keeps a (never expected) stray bin inside the window.
+template <int W>
 __device__ __forceinline__ void bin_add_fast2(f2 xr, f2 vre, f2 vim, float2* win, int tid) {
     const int f0 = floor_i(xr.x), f1 = floor_i(xr.y);
     const f2 w = fma2(make_float2((float)f0, (float)f1), bc(-1.f), xr);
     const f2 w0 = fma2(w, bc(-1.f), bc(1.f));
     {
-        const unsigned sl = min((unsigned)f0, (unsigned)(RP_WIN - 2));
+        const unsigned sl = min((unsigned)f0, (unsigned)(W - 2));
         float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
         float2* p1 = p0 + RP_PAIR_THREADS;
         float2 v0 = *p0, v1 = *p1;
@@ -586,7 +591,7 @@ __device__ __forceinline__ void bin_add_fast2(f2 xr, f2 vre, f2 vim, float2* win
         *p1 = v1;
     }
     {
-        const unsigned sl = min((unsigned)f1, (unsigned)(RP_WIN - 2));
+        const unsigned sl = min((unsigned)f1, (unsigned)(W - 2));
         float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
         float2* p1 = p0 + RP_PAIR_THREADS;
         float2 v0 = *p0, v1 = *p1;
@@ -641,11 +646,12 @@ __device__ __forceinline__ void bin_add_fast2s(f2 xr, f2 vre, f2 vim, f2 g1, f2 
 // row: the whole phasor in the truncated bin (genRefrPhasor +
 // genPhasorTrace, radar_kernels.cu:351-398, 401-448); x in (-1, 0) gives bin
 // 0, bins outside the trace are dropped.
+template <int W>
 __device__ __forceinline__ void bin_add1(float xr, float vre, float vim, int blo, int b0, float2* win, int tid,
                                          C32* Trow, const PairArgs& A) {
     const int sl = floor_i(xr);
     int b = blo + sl;
-    if ((unsigned)sl < (unsigned)RP_WIN && (unsigned)b < (unsigned)A.nr) {
+    if ((unsigned)sl < (unsigned)W && (unsigned)b < (unsigned)A.nr) {
         float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
         float2 v0 = *p0;
         v0.x += vre;
@@ -659,7 +665,7 @@ __device__ __forceinline__ void bin_add1(float xr, float vre, float vim, int blo
     }
     if (b >= A.nr) return;
     const int sw = b - blo;
-    if ((unsigned)sw < (unsigned)RP_WIN) {
+    if ((unsigned)sw < (unsigned)W) {
         float2* p0 = &win[sw * RP_PAIR_THREADS + tid];
         float2 v0 = *p0;
         v0.x += vre;
@@ -680,30 +686,35 @@ __device__ __forceinline__ void bin_add1(float xr, float vre, float vim, int blo
 
 // Flush a thread's bin window into its target's row: each non-zero bin adds
 // to the row element it covers (outside the row: the window-overflow flag).
-// Every row load is issued before the first add, so the up to RP_WIN
-// read-modify-writes overlap instead of waiting on one another.
+// In groups of 8 bins, every row load of a group is issued before its first
+// add, so the read-modify-writes overlap instead of waiting on one another.
+template <int W>
 __device__ __forceinline__ void flush_window(const float2* win, int tid, int blo, int b0, C32* Trow, int Wt,
                                              unsigned int* err) {
-    float2 v[RP_WIN];
-    C32 t[RP_WIN];
+    static_assert(W % 8 == 0, "windows flush in groups of 8 bins");
 #pragma unroll
-    for (int w = 0; w < RP_WIN; ++w) v[w] = win[w * RP_PAIR_THREADS + tid];
+    for (int g = 0; g < W; g += 8) {
+        float2 v[8];
+        C32 t[8];
 #pragma unroll
-    for (int w = 0; w < RP_WIN; ++w) {
-        const int o = blo + w - b0;
-        const bool nz = v[w].x != 0.f || v[w].y != 0.f;
-        t[w] = (nz && o >= 0 && o < Wt) ? Trow[o] : C32{0.f, 0.f};
-    }
+        for (int w = 0; w < 8; ++w) v[w] = win[(g + w) * RP_PAIR_THREADS + tid];
 #pragma unroll
-    for (int w = 0; w < RP_WIN; ++w) {
-        if (v[w].x != 0.f || v[w].y != 0.f) {
-            const int o = blo + w - b0;
-            if (o >= 0 && o < Wt) {
-                t[w].x += v[w].x;
-                t[w].y += v[w].y;
-                Trow[o] = t[w];
-            } else {
-                atomicOr(err, 1u);
+        for (int w = 0; w < 8; ++w) {
+            const int o = blo + g + w - b0;
+            const bool nz = v[w].x != 0.f || v[w].y != 0.f;
+            t[w] = (nz && o >= 0 && o < Wt) ? Trow[o] : C32{0.f, 0.f};
+        }
+#pragma unroll
+        for (int w = 0; w < 8; ++w) {
+            if (v[w].x != 0.f || v[w].y != 0.f) {
+                const int o = blo + g + w - b0;
+                if (o >= 0 && o < Wt) {
+                    t[w].x += v[w].x;
+                    t[w].y += v[w].y;
+                    Trow[o] = t[w];
+                } else {
+                    atomicOr(err, 1u);
+                }
             }
         }
     }
@@ -778,24 +789,28 @@ __device__ __forceinline__ int floor_dd(float Th, float Tl, float kh, float kl, 
 // per-thread bin windows, the threads' target positions relative to the
 // trace origin as double-floats, the two staged chunks' metadata.
 extern __shared__ __align__(128) unsigned char pair_smem[];
-#define RP_PAIR_WIN_OFF (2 * RP_CHUNK_PAIRS * sizeof(FacetPair))
-#define RP_PAIR_TPOS_OFF (RP_PAIR_WIN_OFF + (size_t)RP_WIN * RP_PAIR_THREADS * sizeof(float2))
-#define RP_PAIR_META_OFF (RP_PAIR_TPOS_OFF + 2 * RP_PAIR_THREADS * sizeof(float4))
-#define RP_PAIR_SMEM_BYTES (RP_PAIR_META_OFF + 2 * sizeof(ChunkMeta))
-// specular mode adds the outbound window and two staged FacetSpec chunks
-#define RP_PAIR_WIN2_OFF RP_PAIR_SMEM_BYTES
+// Offsets for a window of W bins.
+__host__ __device__ constexpr size_t pair_win_off() { return 2 * RP_CHUNK_PAIRS * sizeof(FacetPair); }
+__host__ __device__ constexpr size_t pair_tpos_off(int W) { return pair_win_off() + (size_t)W * RP_PAIR_THREADS * sizeof(float2); }
+__host__ __device__ constexpr size_t pair_meta_off(int W) { return pair_tpos_off(W) + 2 * RP_PAIR_THREADS * sizeof(float4); }
+__host__ __device__ constexpr size_t pair_smem_bytes(int W) { return pair_meta_off(W) + 2 * sizeof(ChunkMeta); }
+// specular mode (window RP_WIN) adds the outbound window and two staged
+// FacetSpec chunks
+#define RP_PAIR_WIN2_OFF pair_smem_bytes(RP_WIN)
 #define RP_PAIR_SPEC_OFF (RP_PAIR_WIN2_OFF + (size_t)RP_WIN * RP_PAIR_THREADS * sizeof(float2))
 #define RP_PAIR_SPEC_SMEM_BYTES (RP_PAIR_SPEC_OFF + 2 * RP_CHUNK_PAIRS * sizeof(FacetSpec))
 static_assert(RP_PAIR_SPEC_OFF % 16 == 0, "FacetSpec chunks are staged by bulk copies");
+static_assert(pair_smem_bytes(RP_WIN_WIDE) % 16 == 0, "FacetT0 chunks are staged by bulk copies");
 
-template <int NT, int ILP, bool ORTHO, bool SPEC, class PA>
+template <int NT, int ILP, bool ORTHO, bool SPEC, int W, class PA>
 __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, uint64_t* bars, uint32_t* phase) {
+    static_assert(!SPEC || W == RP_WIN, "the specular layout holds two RP_WIN windows");
     // every hot shared array is derived here from the shared symbol itself
     FacetPair* srec = reinterpret_cast<FacetPair*>(pair_smem);                     // [2][RP_CHUNK_PAIRS]
-    float2* win = reinterpret_cast<float2*>(pair_smem + RP_PAIR_WIN_OFF);          // [RP_WIN][threads]
-    float4* s_tq = reinterpret_cast<float4*>(pair_smem + RP_PAIR_TPOS_OFF);        // [2][threads]
-    ChunkMeta* smeta = reinterpret_cast<ChunkMeta*>(pair_smem + RP_PAIR_META_OFF);  // [2]
-    float2* win2 = nullptr;                                                         // [RP_WIN][threads]
+    float2* win = reinterpret_cast<float2*>(pair_smem + pair_win_off());           // [W][threads]
+    float4* s_tq = reinterpret_cast<float4*>(pair_smem + pair_tpos_off(W));        // [2][threads]
+    ChunkMeta* smeta = reinterpret_cast<ChunkMeta*>(pair_smem + pair_meta_off(W));  // [2]
+    float2* win2 = nullptr;                                                         // [W][threads]
     FacetSpec* sspec = nullptr;                                                     // [2][RP_CHUNK_PAIRS]
     if constexpr (SPEC) {
         win2 = reinterpret_cast<float2*>(pair_smem + RP_PAIR_WIN2_OFF);
@@ -890,7 +905,7 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
             // inequality on the chunk's bounding radius); with half a bin of
             // margin for FP32 rounding both split bins stay inside the window
             // and the trace
-            fits = blo >= 0 && blo + RP_WIN <= A.nr1 && hi + 0.5f < (float)(blo_rel + RP_WIN - 1) &&
+            fits = blo >= 0 && blo + W <= A.nr1 && hi + 0.5f < (float)(blo_rel + W - 1) &&
                    mp->phase_ok;
             an.Dx = __fadd_rn(__fadd_rn(th.x, -cfx), tl.x);
             an.Dy = __fadd_rn(__fadd_rn(th.y, -cfy), tl.y);
@@ -904,9 +919,9 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         }
         const bool all_fit = __all_sync(0xffffffffu, fits);
         if (active) {
-            for (int w = 0; w < RP_WIN; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
+            for (int w = 0; w < W; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
             if constexpr (SPEC)
-                for (int w = 0; w < RP_WIN; ++w) win2[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
+                for (int w = 0; w < W; ++w) win2[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
             const int cnt = min(RP_CHUNK, n - k * RP_CHUNK);    // = mp->n (bounds from the count, not the staged copy)
             const int npairs = (cnt + 1) >> 1;
             const bool prisms = (A.np > 0) && !A.lossless;
@@ -942,11 +957,11 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
                                              : 0.f;
                         re0.x *= f0; im0.x *= f0; re0.y *= f1; im0.y *= f1;
                     }
-                    bin_add(x0.x, re0.x * ga.x, im0.x * ga.x, blo, b0, win, tid, Trow, A);
-                    bin_add(x0.x, re0.x * gb.x, im0.x * gb.x, blo, b0, win2, tid, Trow2, A);
+                    bin_add<W>(x0.x, re0.x * ga.x, im0.x * ga.x, blo, b0, win, tid, Trow, A);
+                    bin_add<W>(x0.x, re0.x * gb.x, im0.x * gb.x, blo, b0, win2, tid, Trow2, A);
                     if (two) {
-                        bin_add(x0.y, re0.y * ga.y, im0.y * ga.y, blo, b0, win, tid, Trow, A);
-                        bin_add(x0.y, re0.y * gb.y, im0.y * gb.y, blo, b0, win2, tid, Trow2, A);
+                        bin_add<W>(x0.y, re0.y * ga.y, im0.y * ga.y, blo, b0, win, tid, Trow, A);
+                        bin_add<W>(x0.y, re0.y * gb.y, im0.y * gb.y, blo, b0, win2, tid, Trow2, A);
                     }
                 }
             } else if (all_fit && !prisms) {
@@ -961,13 +976,13 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
                         pair_eval2<NT, ORTHO, false>(r0, an, A, x[i], re[i], im[i]);
                     }
 #pragma unroll
-                    for (int i = 0; i < ILP; ++i) bin_add_fast2(x[i], re[i], im[i], win, tid);
+                    for (int i = 0; i < ILP; ++i) bin_add_fast2<W>(x[i], re[i], im[i], win, tid);
                 }
                 for (; jp < npairs; ++jp) {
                     const FacetPair r0 = R[jp];
                     f2 x0, re0, im0;
                     pair_eval2<NT, ORTHO, false>(r0, an, A, x0, re0, im0);
-                    bin_add_fast2(x0, re0, im0, win, tid);
+                    bin_add_fast2<W>(x0, re0, im0, win, tid);
                 }
             } else {
                 for (; jp < npairs; ++jp) {
@@ -985,13 +1000,13 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
                                              : 0.f;
                         re0.x *= f0; im0.x *= f0; re0.y *= f1; im0.y *= f1;
                     }
-                    bin_add(x0.x, re0.x, im0.x, blo, b0, win, tid, Trow, A);
-                    if (two) bin_add(x0.y, re0.y, im0.y, blo, b0, win, tid, Trow, A);
+                    bin_add<W>(x0.x, re0.x, im0.x, blo, b0, win, tid, Trow, A);
+                    if (two) bin_add<W>(x0.y, re0.y, im0.y, blo, b0, win, tid, Trow, A);
                 }
             }
             // flush the window into the owned trace (both legs' in specular mode)
-            flush_window(win, tid, blo, b0, Trow, A.Wt, A.err);
-            if constexpr (SPEC) flush_window(win2, tid, blo, b0, Trow2, A.Wt, A.err);
+            flush_window<W>(win, tid, blo, b0, Trow, A.Wt, A.err);
+            if constexpr (SPEC) flush_window<W>(win2, tid, blo, b0, Trow2, A.Wt, A.err);
         }
         __syncthreads();   // everyone done with buffer `buf` before it is refilled
     }
@@ -1075,24 +1090,26 @@ __device__ __forceinline__ void pair_eval2t0(const FacetPair& r, const FacetSpec
 
 // Shared memory of the ttype-0 pair kernel: pair_item's layout, then the
 // staged FacetT0 and (specular) FacetSpec chunks.
-#define RP_PAIR_T0_OFF RP_PAIR_SMEM_BYTES
-#define RP_PAIR_T0SPEC_OFF (RP_PAIR_T0_OFF + 2 * RP_CHUNK_PAIRS * sizeof(FacetT0))
-#define RP_PAIR_T0_SMEM_BYTES(spec) (RP_PAIR_T0SPEC_OFF + ((spec) ? 2 * RP_CHUNK_PAIRS * sizeof(FacetSpec) : 0))
-static_assert(RP_PAIR_T0SPEC_OFF % 16 == 0, "staged by bulk copies");
+__host__ __device__ constexpr size_t pair_t0_off(int W) { return pair_smem_bytes(W); }
+__host__ __device__ constexpr size_t pair_t0spec_off(int W) { return pair_t0_off(W) + 2 * RP_CHUNK_PAIRS * sizeof(FacetT0); }
+__host__ __device__ constexpr size_t pair_t0_smem_bytes(int W, bool spec) {
+    return pair_t0spec_off(W) + (spec ? 2 * RP_CHUNK_PAIRS * sizeof(FacetSpec) : 0);
+}
+static_assert(pair_t0spec_off(RP_WIN_WIDE) % 16 == 0, "staged by bulk copies");
 
 // One work item of the ttype-0 pair kernel: the targets [tq0[s], ntl[s]) of
 // trace s, block tb of them, facet-range part `part`.  The chunk staging and
 // the double-float anchors are pair_item's; the anchors use c1/c2 in place
 // of n and a positive phase, and every phasor goes to one bin.
-template <int NT, int ILP, bool ORTHO, bool SPEC>
+template <int NT, int ILP, bool ORTHO, bool SPEC, int W>
 __device__ __forceinline__ void pair_item_t0(const PairArgs& A, int s, int tb, int part, uint64_t* bars,
                                              uint32_t* phase) {
     FacetPair* srec = reinterpret_cast<FacetPair*>(pair_smem);
-    float2* win = reinterpret_cast<float2*>(pair_smem + RP_PAIR_WIN_OFF);
-    float4* s_tq = reinterpret_cast<float4*>(pair_smem + RP_PAIR_TPOS_OFF);
-    ChunkMeta* smeta = reinterpret_cast<ChunkMeta*>(pair_smem + RP_PAIR_META_OFF);
-    FacetT0* st0 = reinterpret_cast<FacetT0*>(pair_smem + RP_PAIR_T0_OFF);
-    FacetSpec* sspec = SPEC ? reinterpret_cast<FacetSpec*>(pair_smem + RP_PAIR_T0SPEC_OFF) : nullptr;
+    float2* win = reinterpret_cast<float2*>(pair_smem + pair_win_off());
+    float4* s_tq = reinterpret_cast<float4*>(pair_smem + pair_tpos_off(W));
+    ChunkMeta* smeta = reinterpret_cast<ChunkMeta*>(pair_smem + pair_meta_off(W));
+    FacetT0* st0 = reinterpret_cast<FacetT0*>(pair_smem + pair_t0_off(W));
+    FacetSpec* sspec = SPEC ? reinterpret_cast<FacetSpec*>(pair_smem + pair_t0spec_off(W)) : nullptr;
     const int tid = threadIdx.x;
     const int qs = A.tq0[s];
     const int nq = A.ntl[s] - qs;
@@ -1163,7 +1180,7 @@ __device__ __forceinline__ void pair_item_t0(const PairArgs& A, int s, int tb, i
             const float lo = xf + fmaf(-A.kb0, mp->R, mp->xmin), hi = xf + fmaf(A.kb0, mp->R, mp->xmax);
             const int blo_rel = floor_i(lo) - 1;
             blo = xi + blo_rel;
-            fits = blo >= 0 && blo + RP_WIN <= A.nr && hi + 0.5f < (float)(blo_rel + RP_WIN);
+            fits = blo >= 0 && blo + W <= A.nr && hi + 0.5f < (float)(blo_rel + W);
             an.Dx = __fadd_rn(__fadd_rn(th.x, -cfx), tl.x);
             an.Dy = __fadd_rn(__fadd_rn(th.y, -cfy), tl.y);
             an.Dz = __fadd_rn(__fadd_rn(th.z, -cfz), tl.z);
@@ -1176,7 +1193,7 @@ __device__ __forceinline__ void pair_item_t0(const PairArgs& A, int s, int tb, i
         }
         const bool all_fit = __all_sync(0xffffffffu, fits);
         if (active) {
-            for (int w = 0; w < RP_WIN; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
+            for (int w = 0; w < W; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
             const int cnt = min(RP_CHUNK, n - k * RP_CHUNK);
             const int npairs = (cnt + 1) >> 1;
             const bool prisms = A.np > 0;
@@ -1193,8 +1210,8 @@ __device__ __forceinline__ void pair_item_t0(const PairArgs& A, int s, int tb, i
 #pragma unroll
                     for (int i = 0; i < ILP; ++i) {
                         if (jp + i >= npairs) break;
-                        const unsigned s0 = min((unsigned)floor_i(x[i].x), (unsigned)(RP_WIN - 1));
-                        const unsigned s1 = min((unsigned)floor_i(x[i].y), (unsigned)(RP_WIN - 1));
+                        const unsigned s0 = min((unsigned)floor_i(x[i].x), (unsigned)(W - 1));
+                        const unsigned s1 = min((unsigned)floor_i(x[i].y), (unsigned)(W - 1));
                         float2* p0 = &win[s0 * RP_PAIR_THREADS + tid];
                         float2 v0 = *p0;
                         v0.x += re[i].x;
@@ -1225,11 +1242,11 @@ __device__ __forceinline__ void pair_item_t0(const PairArgs& A, int s, int tb, i
                         f0 *= f0; f0 *= f0; f1 *= f1; f1 *= f1;
                         re0.x *= f0; im0.x *= f0; re0.y *= f1; im0.y *= f1;
                     }
-                    bin_add1(x0.x, re0.x, im0.x, blo, b0, win, tid, Trow, A);
-                    if (two) bin_add1(x0.y, re0.y, im0.y, blo, b0, win, tid, Trow, A);
+                    bin_add1<W>(x0.x, re0.x, im0.x, blo, b0, win, tid, Trow, A);
+                    if (two) bin_add1<W>(x0.y, re0.y, im0.y, blo, b0, win, tid, Trow, A);
                 }
             }
-            flush_window(win, tid, blo, b0, Trow, A.Wt, A.err);
+            flush_window<W>(win, tid, blo, b0, Trow, A.Wt, A.err);
         }
         __syncthreads();
     }

@@ -30,7 +30,7 @@ k_pairs32s(const __grid_constant__ PairArgs A) {
         const int part = item % RP_PARTS;
         const int tb = (item / RP_PARTS) % A.tblocks;
         const int s = item / (RP_PARTS * A.tblocks);
-        pair_item<NT, ILP, false, true>(A, s, tb, part, bars, phase);
+        pair_item<NT, ILP, false, true, RP_WIN>(A, s, tb, part, bars, phase);
     }
     RP_PAIR_SMEM_END
 }
@@ -76,7 +76,7 @@ k_pairs32t0(const __grid_constant__ PairArgs A) {
         const int part = item % RP_PARTS;
         const int tb = (item / RP_PARTS) % A.tblocks;
         const int s = item / (RP_PARTS * A.tblocks);
-        pair_item_t0<NT, 2, ORTHO, SPEC>(A, s, tb, part, bars, phase);
+        pair_item_t0<NT, 2, ORTHO, SPEC, RP_WIN_WIDE>(A, s, tb, part, bars, phase);
     }
     RP_PAIR_SMEM_END
 }
@@ -94,7 +94,7 @@ int launch_pairs_t0(int deg, bool ortho, bool spec, const PairArgs& P, int64_t i
             default: pk = k_pairs32t0<0, false, true>; break;
         }
     }
-    const size_t smem = RP_PAIR_T0_SMEM_BYTES(spec);
+    const size_t smem = pair_t0_smem_bytes(RP_WIN_WIDE, spec);
     if (int rc = rp_allow_dyn_smem((const void*)pk, smem)) return rc;
     int occ = 0;
     RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, RP_PAIR_THREADS, smem));
