@@ -615,9 +615,9 @@ def main():
                 "achieved": fp32_rate / 1e12, "peak": fp32_peak / 1e12,
                 "unit": "T FP32 lane-operations/s",
                 "frac": fp32_rate / fp32_peak if fp32_peak else None,
-                # DRAM read+write of one launch from the committed ncu capture (2 traces: 247.0 + 32.8
+                # DRAM read+write of one launch from the committed ncu capture (2 traces: 276.2 + 36.2
                 # MB), scaled by the traces per launch; the kernel is compute-bound (DRAM < 0.1 % of peak)
-                "traffic": 279.8e6 * tps / 2.0,
+                "traffic": 312.4e6 * tps / 2.0,
                 "traffic_unit": "bytes per launch (ncu, profiles/k_pairs32_large_scene.md, scaled)",
                 "peak_source": (f"nominal {opcount.FP32_FMA_PER_CLK_PER_SM} FP32 lanes/clk/SM x {n_sm} SMs x "
                                 f"{sm_mhz:.0f} MHz median SM clock under load; MEASURED_PEAKS.json holds HBM "

@@ -26,14 +26,14 @@ about 10:
   and the phase scaling of the special-function sine and cosine).
 * MUFU (special-function) instructions: 6 -- rsqrt (1/Ttd), rcp (dT), rcp
   (the in-plane split), ex2, sin and cos of the phase.
-* All thread instructions: 53.4 -- a packed instruction issues once for two
+* All thread instructions: 54.0 -- a packed instruction issues once for two
   evaluations; plus 4 shared-memory record loads and 4 window accesses per
   evaluation, the floor conversion pair, address arithmetic and the loop.
 """
 
 FP32_OPS_PER_EVAL = 58.4
 MUFU_PER_EVAL = 6
-INSTR_PER_EVAL = 53.4
+INSTR_PER_EVAL = 54.0
 EVALS_PER_TARGET_PAIR_METRIC = 0.5     # one evaluation covers two metric pairs
 
 # Nominal special-function throughput of a Blackwell SM (results per clock).
