@@ -658,9 +658,10 @@ struct ConvArgs {
 // and 2) hold every element at its swizzled position (swz, rp_fft.cuh:
 // conflict-free in shared memory, within one 256-byte row in global
 // memory); twiddles come from the SFU.  MODE 0: X and W in shared memory
-// (nr <= 4096), the targets summed in registers.  MODE 1: X in shared
-// memory, W in this block's slot of the global scratch (nr = 8192).  MODE 2:
-// both in the slot (nr >= 16384).  Modes 1 and 2 sum the targets in the
+// (nr <= 4096), the targets summed in registers.  MODE 1 (nr = 8192): every
+// transform in one 2nr buffer of shared memory; X waits in this block's slot
+// of the global scratch between its two uses.  MODE 2: X and W in the slot
+// (nr >= 16384).  Modes 1 and 2 sum the targets in the
 // item's partial row in global memory (same thread, same element, same
 // target order as the registers of mode 0, so every mode gives the same
 // sums).
@@ -723,6 +724,91 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
             for (int j = tid; j < N; j += RP_CONV_THREADS) out[j] = C32{0.f, 0.f};
         for (int q = q0; q < q1; ++q) {
             const int b0 = bt0[(size_t)s * tstride + q];
+            if constexpr (MODE == 1) {
+                // every transform in shared memory (S, 2nr values); X =
+                // DIF(pad T) waits in the block's global slot (Xg) between
+                // its two uses, Ptarg moves through Mv (nr values)
+                Cplx<float>* const S = sbase;
+                Cplx<float>* const Xg = gbase;
+                Cplx<float>* const Mv = gbase + n2;
+                #pragma unroll 8
+                for (int k = tid; k < n2; k += RP_CONV_THREADS) {
+                    Cplx<float> v{0.f, 0.f};
+                    const int o = k - b0;
+                    if (k < nr && o >= 0 && o < Wt) {
+                        for (int p = 0; p < RP_PARTS; ++p) {
+                            const C32 u = T[(((size_t)p * nbA + s) * tstride + q) * Wt + o];
+                            v.x += u.x;
+                            v.y += u.y;
+                        }
+                    }
+                    S[swz(k)] = v;
+                }
+                __syncthreads();
+                block_dif_s<float>(S, n2);
+                #pragma unroll 8
+                for (int k = tid; k < n2; k += RP_CONV_THREADS) {
+                    const Cplx<float> v = S[swz(k)];
+                    Xg[swz(k)] = v;
+                    S[swz(k)] = c_mul(v, C2s[k]);
+                }
+                __syncthreads();
+                block_dit_s<float>(S, n2);
+                {   // Ptarg = S[nr/2 + k] / n2 moved to the front, zero padded
+                    const float inv = 1.f / (float)n2;
+                    for (int k = tid; k < nr; k += RP_CONV_THREADS) Mv[k] = S[swz(nr / 2 + k)];
+                    __syncthreads();
+                    for (int k = tid; k < nr; k += RP_CONV_THREADS) {
+                        const Cplx<float> v = Mv[k];
+                        S[swz(k)] = Cplx<float>{v.x * inv, v.y * inv};
+                    }
+                    #pragma unroll 8
+                    for (int k = nr + tid; k < n2; k += RP_CONV_THREADS) S[swz(k)] = Cplx<float>{0.f, 0.f};
+                    __syncthreads();
+                }
+                block_dif_s<float>(S, n2);
+                if constexpr (SPEC) {
+                    // Psour = s T2: DIF(Ptarg) moves to the slot, S takes DIF(pad T2)
+                    #pragma unroll 8
+                    for (int k = tid; k < n2; k += RP_CONV_THREADS) Xg[swz(k)] = S[swz(k)];
+                    __syncthreads();
+                    #pragma unroll 8
+                    for (int k = tid; k < n2; k += RP_CONV_THREADS) {
+                        Cplx<float> v{0.f, 0.f};
+                        const int o = k - b0;
+                        if (k < nr && o >= 0 && o < Wt) {
+                            for (int p = 0; p < RP_PARTS; ++p) {
+                                const C32 u = T2[(((size_t)p * nbA + s) * tstride + q) * Wt + o];
+                                v.x += u.x;
+                                v.y += u.y;
+                            }
+                        }
+                        S[swz(k)] = v;
+                    }
+                    __syncthreads();
+                    block_dif_s<float>(S, n2);
+                }
+                {
+                    const float sc = sig_scale / (float)n2;
+                    #pragma unroll 8
+                    for (int k = tid; k < n2; k += RP_CONV_THREADS) {
+                        // the spectra's product in the same operand order as the other modes
+                        const Cplx<float> v = SPEC ? c_mul(S[swz(k)], Xg[swz(k)]) : c_mul(Xg[swz(k)], S[swz(k)]);
+                        S[swz(k)] = Cplx<float>{v.x * sc, v.y * sc};
+                    }
+                }
+                __syncthreads();
+                block_dit_s<float>(S, n2);                            // u (natural, N values)
+                for (int j = tid; j < N; j += RP_CONV_THREADS) {
+                    const Cplx<float> a = S[swz(j)];
+                    C32 o = out[j];
+                    o.x += a.x;
+                    o.y += a.y;
+                    out[j] = o;
+                }
+                __syncthreads();
+                continue;
+            }
             #pragma unroll 8
             for (int k = tid; k < n2; k += RP_CONV_THREADS) {
                 Cplx<float> v{0.f, 0.f};
@@ -984,10 +1070,10 @@ void fast_take_setup(Aa& a, const rp_scene* sc, const FastLayout& L) {
 }
 
 // Storage mode of the range compression (k_conv32s): 0 X and W in shared
-// memory (2 x 2nr complex64 = 32 nr bytes, 128 KiB at nr = 4096), 1 X in
-// shared memory and W in global scratch (nr = 8192), 2 both in global
-// scratch (nr >= 16384), 3 the Bluestein kernel k_conv32 (nr not a power of
-// two).
+// memory (2 x 2nr complex64 = 32 nr bytes, 128 KiB at nr = 4096), 1 the
+// transforms in shared memory and X parked in global scratch (nr = 8192),
+// 2 both in global scratch (nr >= 16384), 3 the Bluestein kernel k_conv32
+// (nr not a power of two).
 int conv_mode(const rp_scene* sc) {
     if (!sc->smem_conv) return 3;
     if (sc->nr <= 4096) return 0;
@@ -995,8 +1081,9 @@ int conv_mode(const rp_scene* sc) {
     return 2;
 }
 
-// Complex values in one block's slot of the global compression scratch: W
-// (2nr) plus nr for the Ptarg shift, and X (2nr) in mode 2.
+// Complex values in one block's slot of the global compression scratch: 2nr
+// (W in mode 2, X in mode 1) plus nr for the Ptarg shift, and X (2nr) in
+// mode 2.
 size_t conv_gslot(const rp_scene* sc) {
     const int m = conv_mode(sc);
     return m == 1 ? (size_t)3 * sc->nr : (m == 2 ? (size_t)5 * sc->nr : 0);
