@@ -111,3 +111,28 @@ def test_scene_create_refuses_undefined_modes(built_lib, over, ttype):
     rc = built_lib.rp_scene_create(ctypes.byref(p), f.ctypes.data, f.shape[1], t.ctypes.data, t.shape[1],
                                    None, 0, 0, ctypes.byref(h))
     assert rc == -6, _abi.last_error()
+
+
+def test_autotune_query_kinds_without_a_gpu(built_lib):
+    # the tuned-configuration table is host state: every kind (single-batch,
+    # multi-segment, specular) answers -1 before any launch, and an unknown
+    # degree too
+    from europaraypaths_gb300 import simulator
+    assert simulator.autotune_query(False, 99) == -1
+    assert simulator.autotune_query(True) in range(-1, 8)
+    assert simulator.autotune_query(False, 99, specular=True) == -1
+
+
+def test_sim_auto_form_is_fast_for_every_mode():
+    # every mode the reference defines runs in the fast form
+    import numpy as np
+    from europaraypaths_gb300 import param_gen, scenes, sim
+    base = scenes.small_plain(n_facets_side=10, n_targets_side=2, ns=2)
+    for over in ({}, {"specular": True}, {"specular": True, "convolution_linear": False},
+                 {"specular": True, "convolution": False}):
+        p = dict(base["params"])
+        p.update(over)
+        tg = np.array(base["targets"], copy=True)
+        if over.get("convolution") is False or over.get("convolution_linear") is False:
+            tg[6, :] = 0.0
+        assert sim.pick_form(param_gen.to_rp_params(p), tg) == "fast"
