@@ -550,8 +550,8 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
     if (const char* v = getenv("RP_PAIR_ORTHO")) s->ortho = s->ortho && atoi(v) != 0;   // 0: general frames
     s->dp.ortho = s->ortho;
     if (const char* v = getenv("RP_PAIR_VARIANT")) s->pair_variant = atoi(v) == 1 ? 1 : 0;
-    // 0-3 for one segment (taken & 3), 4-7 also for multi-segment waves
-    if (const char* v = getenv("RP_PAIR_CFG")) s->pair_cfg = std::max(0, std::min(7, atoi(v)));
+    // 0-3 for one segment (taken & 3), 4-9 also for multi-segment waves
+    if (const char* v = getenv("RP_PAIR_CFG")) s->pair_cfg = std::max(0, std::min(9, atoi(v)));
     cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return fail(rp_cuda_fail(e, "cudaStreamCreate"));
     *out = s;

@@ -1527,15 +1527,21 @@ int launch_pairs_one(const Seg& g, unsigned int* work, int cfg, int sms, cudaStr
 }
 
 // Pair launch of a wave: the single-batch kernel (constants in the parameter
-// bank) for one segment; for several, the multi-job kernel (cfg 0-3) or one
-// single-batch kernel per segment (cfg 4-7: configuration cfg - 4), on the
-// workspace's auxiliary streams when par.  The multi-job kernel holds its
-// job's constants in registers and local memory; the per-segment kernels
-// read theirs from the parameter bank, at the price of one launch each.
-// seg_work: one work counter per segment of ps.
-int launch_pairs(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsigned int* d_start,
-                 unsigned int* d_work, unsigned int* seg_work, int cfg, int sms, cudaStream_t st,
-                 rp_workspace* ws, bool par) {
+// bank) for one segment; for several, the multi-job kernel (cfg 0-3), one
+// single-batch kernel per segment (cfg 4-7: configuration cfg - 4, on the
+// workspace's auxiliary streams when par), or one per-kind multi-job kernel
+// per (sinc degree, frame kind) group with the jobs in the parameter space
+// (cfg 8-9).  The multi-job kernel's 10-way dispatch makes it spill; the
+// other two read their constants from the parameter bank.  seg_work: one
+// work counter per segment of ps; h_jobs: the job table on the host.
+int launch_pairs(const std::vector<Seg*>& ps, const PairJob* d_jobs, const PairJob* h_jobs,
+                 const unsigned int* d_start, unsigned int* d_work, unsigned int* seg_work, int cfg, int sms,
+                 cudaStream_t st, rp_workspace* ws, bool par) {
+    if (ps.size() > 1 && cfg >= 8) {
+        if (int rc = launch_pairs_multik(cfg - 8, h_jobs, (int)ps.size(), seg_work, sms, st)) return rc;
+        RP_LAUNCHED();
+        return RP_OK;
+    }
     if (ps.size() > 1 && cfg >= 4) {
         if (par) ws->fork(st);
         for (size_t i = 0; i < ps.size(); ++i) {
@@ -1582,13 +1588,13 @@ int zero_pairs(const std::vector<Seg*>& ps, unsigned int* d_work, unsigned int* 
 // configuration); each probe is a full launch on this wave's items, outputs
 // re-zeroed after.  Tuned per kind: single kernel (0), multi-segment (1) or
 // specular (2), and sinc degree.
-int choose_cfg(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsigned int* d_start,
-               unsigned int* d_work, unsigned int* seg_work, int sms, cudaStream_t st, rp_workspace* ws,
-               bool par, int* cfg_out) {
+int choose_cfg(const std::vector<Seg*>& ps, const PairJob* d_jobs, const PairJob* h_jobs,
+               const unsigned int* d_start, unsigned int* d_work, unsigned int* seg_work, int sms, cudaStream_t st,
+               rp_workspace* ws, bool par, int* cfg_out) {
     const bool spec = ps.size() == 1 && ps[0]->sc->dp.specular;
     const int multi = spec ? 2 : (ps.size() > 1 ? 1 : 0);
     const int deg = multi == 1 ? -1 : ps[0]->deg;
-    const int ncfg = spec ? 2 : (multi == 1 ? 8 : 4);
+    const int ncfg = spec ? 2 : (multi == 1 ? 10 : 4);
     if (!autotune_on()) {
         const int c = ps[0]->sc->pair_cfg;
         *cfg_out = spec ? (c & 1) : (multi == 1 ? c : (c & 3));
@@ -1605,7 +1611,7 @@ int choose_cfg(const std::vector<Seg*>& ps, const PairJob* d_jobs, const unsigne
         int rc = zero_pairs(ps, d_work, seg_work, st);
         if (rc) return rc;
         RP_CUDA(cudaEventRecord(e0, st));
-        rc = launch_pairs(ps, d_jobs, d_start, d_work, seg_work, k, sms, st, ws, par);
+        rc = launch_pairs(ps, d_jobs, h_jobs, d_start, d_work, seg_work, k, sms, st, ws, par);
         if (rc) return rc;
         RP_CUDA(cudaEventRecord(e1, st));
         RP_CUDA(cudaEventSynchronize(e1));
@@ -1750,10 +1756,10 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     // ---- pair stage: one launch for the wave
     if (!ps.empty()) {
         int cfg = 0;
-        int rc = choose_cfg(ps, d_pjobs, d_pstart, d_work, seg_work, sms, st, ws, par, &cfg);
+        int rc = choose_cfg(ps, d_pjobs, hp.data(), d_pstart, d_work, seg_work, sms, st, ws, par, &cfg);
         if (rc) return rc;
         g_timer.mark(1, st);
-        rc = launch_pairs(ps, d_pjobs, d_pstart, d_work, seg_work, cfg, sms, st, ws, par);
+        rc = launch_pairs(ps, d_pjobs, hp.data(), d_pstart, d_work, seg_work, cfg, sms, st, ws, par);
         if (rc) return rc;
         ++g_timer.pair_launches;
         // ttype-0 targets: one launch per segment that has them

@@ -2,6 +2,7 @@
 // work items of many batches (scenes of different sizes, bands, bin counts
 // and sinc degrees).  Its own translation unit (see rp_pair.cuh).
 #include <algorithm>
+#include <vector>
 
 #include "rp_internal.h"
 #include "rp_pair.cuh"
@@ -61,6 +62,87 @@ k_pairs32m(const PairJob* __restrict__ jobs, const unsigned int* __restrict__ st
         }
     }
     RP_PAIR_SMEM_END
+}
+
+// Multi-job pair kernel for one (sinc degree, frame kind), with the group's
+// jobs in the parameter space: grid row blockIdx.y is job j, so the job
+// index is uniform and the scene constants come from the parameter bank.
+// One variant per kernel: the 10-way dispatch of k_pairs32m is what makes
+// its body spill (~900 bytes a thread; ~50 here).  Every job gets a
+// full-width row of blocks; the rows of finished jobs exit at once.
+template <int NT, bool ORTHO, int ILP>
+__global__ void __launch_bounds__(RP_PAIR_THREADS, 2)
+k_pairs32mk(const __grid_constant__ PairJobTable T, unsigned int* work) {
+    RP_PAIR_SMEM_DECL
+    const int j = blockIdx.y;
+    const PairArgs& A = T.job[j].a;
+    const unsigned int items = (unsigned)A.nb * A.tblocks * RP_PARTS;
+    unsigned int* const wk = work + T.wi[j];
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(wk, 1u);
+        __syncthreads();
+        const unsigned int item = s_item;
+        __syncthreads();
+        if (item >= items) break;
+        const int part = item % RP_PARTS;
+        const int tb = (item / RP_PARTS) % A.tblocks;
+        const int s = item / (RP_PARTS * A.tblocks);
+        pair_item<NT, ILP, ORTHO, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase);
+    }
+    RP_PAIR_SMEM_END
+}
+
+template <int ILP>
+void (*pick_mk(int deg, bool ortho))(const PairJobTable, unsigned int*) {
+    if (ortho) {
+        switch (deg) {
+            case 3: return k_pairs32mk<3, true, ILP>;
+            case 4: return k_pairs32mk<4, true, ILP>;
+            case 5: return k_pairs32mk<5, true, ILP>;
+            case 6: return k_pairs32mk<6, true, ILP>;
+            default: return k_pairs32mk<0, true, ILP>;
+        }
+    }
+    switch (deg) {
+        case 3: return k_pairs32mk<3, false, ILP>;
+        case 4: return k_pairs32mk<4, false, ILP>;
+        case 5: return k_pairs32mk<5, false, ILP>;
+        case 6: return k_pairs32mk<6, false, ILP>;
+        default: return k_pairs32mk<0, false, ILP>;
+    }
+}
+
+int launch_pairs_multik(int cfg, const PairJob* h_jobs, int njobs, unsigned int* work, int sms, cudaStream_t st) {
+    const size_t smem = pair_smem_bytes(RP_WIN_WIDE);
+    std::vector<char> done(njobs, 0);
+    for (int a = 0; a < njobs; ++a) {
+        if (done[a]) continue;
+        const int deg = h_jobs[a].deg;
+        const bool ortho = h_jobs[a].ortho != 0;
+        auto mk = (cfg & 1) ? pick_mk<4>(deg, ortho) : pick_mk<3>(deg, ortho);
+        if (int rc = rp_allow_dyn_smem((const void*)mk, smem)) return rc;
+        int occ = 0;
+        RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mk, RP_PAIR_THREADS, smem));
+        // the jobs of this kind, RP_MAXJ per launch
+        PairJobTable T;
+        int n = 0;
+        for (int b = a; b <= njobs; ++b) {
+            const bool take = b < njobs && !done[b] && h_jobs[b].deg == deg && (h_jobs[b].ortho != 0) == ortho;
+            if (take) {
+                T.job[n] = h_jobs[b];
+                T.wi[n] = b;
+                done[b] = 1;
+                ++n;
+            }
+            if (n > 0 && (n == RP_MAXJ || b == njobs)) {
+                T.njobs = n;
+                mk<<<dim3((unsigned)(std::max(occ, 1) * sms), (unsigned)n), RP_PAIR_THREADS, smem, st>>>(T, work);
+                RP_CUDA(cudaGetLastError());
+                n = 0;
+            }
+        }
+    }
+    return RP_OK;
 }
 
 // Configurations (facet pairs per step x resident blocks per SM).  The job's

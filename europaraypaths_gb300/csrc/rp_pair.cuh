@@ -201,6 +201,16 @@ struct PairJob {
     int ortho;      // the batch's scene has orthonormal facet frames
 };
 
+// Jobs of one k_pairs32mk launch, passed in the parameter space (< 32 KB);
+// wi[j]: job j's work-counter index.
+#define RP_MAXJ 80
+struct PairJobTable {
+    PairJob job[RP_MAXJ];
+    int wi[RP_MAXJ];
+    int njobs;
+};
+static_assert(sizeof(PairJobTable) <= 32000, "kernel parameters are limited to 32 KB");
+
 // Per-(chunk, target) anchors of the split-precision evaluation.
 struct Anchor {
     float Dx, Dy, Dz;     // target - chunk centre (FP32 of an FP64 difference)
@@ -1275,6 +1285,11 @@ __device__ __forceinline__ void pair_item_t0(const PairArgs& A, int s, int tb, i
 // cfg over items work items of njobs jobs.
 int launch_pairs_multi(int cfg, const PairJob* d_jobs, const unsigned int* d_start, int njobs,
                        unsigned int* d_work, int64_t items, int sms, cudaStream_t st);
+
+// Launches of the per-kind multi-job kernels k_pairs32mk (rp_multi.cu), one
+// per (sinc degree, frame kind) group of h_jobs (host copies); work[j] is
+// job j's counter; cfg 0: 3 facet pairs per step, 1: 4.
+int launch_pairs_multik(int cfg, const PairJob* h_jobs, int njobs, unsigned int* work, int sms, cudaStream_t st);
 
 // Launch of the specular-mode pair kernel k_pairs32s (rp_spec.cu) of sinc
 // degree deg in configuration cfg (0 or 1) over items work items.

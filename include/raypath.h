@@ -215,7 +215,8 @@ int rp_autotune(int enable);
 /* The tuned configuration for (kind, degree), or -1 when not tuned yet.
  * multi: 0 the single-batch kernel (configurations 0-3), 1 multi-segment
  * waves (degree ignored; 0-3 the multi-scene kernel, 4-7 one single-batch
- * kernel per segment in configuration cfg - 4), 2 the specular-mode kernel
+ * kernel per segment in configuration cfg - 4, 8-9 one multi-scene kernel
+ * per sinc-degree and frame-kind group), 2 the specular-mode kernel
  * (configurations 0-1). */
 int rp_autotune_query(int multi, int degree, int* cfg);
 

@@ -119,7 +119,7 @@ def test_autotune_query_kinds_without_a_gpu(built_lib):
     # degree too
     from europaraypaths_gb300 import simulator
     assert simulator.autotune_query(False, 99) == -1
-    assert simulator.autotune_query(True) in range(-1, 8)
+    assert simulator.autotune_query(True) in range(-1, 10)
     assert simulator.autotune_query(False, 99, specular=True) == -1
 
 

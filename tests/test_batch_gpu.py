@@ -56,14 +56,15 @@ def test_batch_equals_single_and_oracle(built_lib, oracle):
 
 def test_batch_per_segment_launches_bitwise(built_lib):
     # multi-segment waves in configurations 4-7 (one single-batch kernel per
-    # segment, on the workspace's auxiliary streams): bitwise the same
+    # segment, on the workspace's auxiliary streams) and 8-9 (one multi-job
+    # kernel per sinc-degree and frame-kind group): bitwise the same
     # radargrams as the multi-job kernel
     from europaraypaths_gb300 import simulator, traces as tr_mod
     scs = _scenes()
     res = {}
     simulator.autotune(False)
     try:
-        for cfg in (1, 5, 7):
+        for cfg in (1, 5, 7, 8, 9):
             os.environ["RP_PAIR_CFG"] = str(cfg)
             scenes = [simulator.Scene(s["params"], s["facets"], s["targets"]) for s in scs]
             try:
@@ -75,7 +76,7 @@ def test_batch_per_segment_launches_bitwise(built_lib):
     finally:
         os.environ.pop("RP_PAIR_CFG", None)
         simulator.autotune(True)
-    for cfg in (5, 7):
+    for cfg in (5, 7, 8, 9):
         for a, b in zip(res[1], res[cfg]):
             assert np.array_equal(_bits(a), _bits(b))
 
