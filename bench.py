@@ -151,6 +151,24 @@ def cpu_baseline(sc, scene, track, max_targets, trace_index):
                       f"targets: {p} pairs in {dt:.2f} s (FP64 C++ oracle, OpenMP over targets)"}
 
 
+def accuracy_vs_plain(scene, d_tr, plain_out, plain_counts, stream):
+    """The fast form on the traces the plain FP64 form just ran (traces of the
+    timed workload, every target), compared at the accuracy bar: relative
+    L2, max phase error above -40 dB of each trace's peak, peak-bin match,
+    and equal illuminated-facet / in-aperture-target counts."""
+    import torch
+    from europaraypaths_gb300 import accuracy
+    fout = torch.empty((d_tr.shape[0], scene.nr), dtype=torch.complex64, device="cuda")
+    fc = np.zeros_like(plain_counts)
+    scene.simulate_device(d_tr, fout, form="fast", stream=stream, counts=fc)
+    torch.cuda.synchronize()
+    res = accuracy.compare(fout.cpu().numpy(), plain_out.cpu().numpy())
+    res.update({"reference": "plain FP64 form (complex128) on the same traces, all targets",
+                "trace_index": 1000, "counts_match": bool(np.array_equal(fc, plain_counts)),
+                "counts": plain_counts.tolist(), "within_bar": accuracy.within_bar(res)})
+    return res
+
+
 def batch_workload(args, device):
     """The uneven-scenes workload: resident scenes and, per step, a few
     interior traces of every scene (the traces of one step are consecutive)."""
@@ -631,6 +649,19 @@ def main():
                           "unit": "T thread-instructions/s",
                           "frac": (opcount.INSTR_PER_EVAL * evals_rate) / (opcount.ISSUE_PER_CLK_PER_SM * n_sm * clk),
                           "instr_per_eval": opcount.INSTR_PER_EVAL},
+                "peak_kind": "nominal (no FP32 entry in MEASURED_PEAKS.json)",
+                # the reference chain's op count per target leg (two legs per evaluation):
+                # the rate the pair kernel delivers in the reference's own arithmetic
+                "algorithmic": {
+                    "achieved": 2 * opcount.REF_FMA_PER_TARGET_LEG * evals_rate / 1e12,
+                    "peak": fp32_peak / 1e12, "unit": "T FP32 FMA-class ops/s (reference chain)",
+                    "frac": (2 * opcount.REF_FMA_PER_TARGET_LEG * evals_rate) / fp32_peak if fp32_peak else None,
+                    "ops_per_target_leg": opcount.REF_FMA_PER_TARGET_LEG,
+                    "sfu_achieved": 2 * opcount.REF_SFU_PER_TARGET_LEG * evals_rate / 1e12,
+                    "sfu_peak": mufu_peak / 1e12,
+                    "sfu_frac": (2 * opcount.REF_SFU_PER_TARGET_LEG * evals_rate) / mufu_peak if mufu_peak else None,
+                    "note": "above 1: hoisted incident terms and the outbound leg's reuse of the inbound "
+                            "evaluation; frac above is the instruction-level fraction"},
                 "pair_kernel_ms_per_launch": stage["pairs_ms"] / max(stage["pair_launches"], 1),
                 "pair_evals_per_s": evals_rate,
                 "pair_evals_per_launch": my_evals / max(stage["pair_launches"], 1),
@@ -647,18 +678,19 @@ def main():
                 "e2e": e2e, "roofline": roof, "clocks": clocks, "gpu_launches": launches}
         if args.plain_traces > 0 and world == 1:
             ptr = torch.from_numpy(np.ascontiguousarray(track[1000:1000 + args.plain_traces])).cuda()
-            pout = torch.empty((args.plain_traces, nr), dtype=torch.complex64, device="cuda")
+            pout = torch.empty((args.plain_traces, nr), dtype=torch.complex128, device="cuda")
             pc = np.zeros((args.plain_traces, 2), np.int64)
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            scene.simulate_device(ptr, pout, form="plain", stream=stream, counts=pc)
+            scene.simulate_device(ptr, pout, form="plain", stream=stream, counts=pc, complex128=True)
             e1.record(stream)
             torch.cuda.synchronize()
             pv = opcount.pairs(pc) / (e0.elapsed_time(e1) / 1e3)
             line["plain_form"] = {"value": pv, "unit": UNIT, "traces": args.plain_traces,
                                   "fast_over_plain": value / pv if pv else None}
+            line["accuracy"] = accuracy_vs_plain(scene, ptr, pout, pc, stream)
         roof["pair_cfg"] = {f"degree_{d}": simulator.autotune_query(False, d) for d in (0, 3, 4, 5, 6)
                             if simulator.autotune_query(False, d) >= 0}
         if not args.no_cpu_baseline and world == 1:

@@ -10,16 +10,24 @@
 // rp_surface_noalloc, which calls no cudaMalloc, cudaFree or other
 // allocating routine.
 //
-// One kernel block per trace does the whole surface leg of the fast form:
-// the aperture test, the per-facet incident leg in FP64 (compIncidentRays,
-// snellsLaw, compReflectedEnergy and surfacePT; geometry_kernels.cu:103-140,
-// 426-517, radar_kernels.cu:714-764), fixed-point binning, and the linear
-// chirp convolution (convolvePhasorChirpLinear, radar_kernels.cu:554-649).
-// The arithmetic is the same as the resident fast form's, so the columns
-// match rp_simulate_device's for a scene without targets.
+// One kernel block per trace does the whole surface leg: the aperture test,
+// the per-facet incident leg (compIncidentRays, snellsLaw,
+// compReflectedEnergy and surfacePT; geometry_kernels.cu:103-140, 426-517,
+// radar_kernels.cu:714-764), fixed-point binning, and the linear chirp
+// convolution (convolvePhasorChirpLinear, radar_kernels.cu:554-649).
+// Precision: the incident leg runs in FP64 here, angles included, where the
+// resident fast form's facet kernel takes its angles in FP32; the phasors
+// are rounded to FP32 for binning and the convolution is the fast form's
+// FP32 transform.  The columns therefore agree with rp_simulate_device's
+// fast form to about 1e-7 relative L2 (the test holds 1e-6) and with the
+// FP64 oracle to the same order (the test holds 1e-5), not bit for bit.
+//
+// Cost: the block walks the scene's 1024-facet culling tiles; a tile whose
+// bounding sphere lies wholly outside the trace's aperture cone is skipped
+// without reading its facets, so each trace evaluates the facets of the
+// tiles that touch its footprint, twice (once for the count and the
+// fixed-point scale, once to bin).
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "rp_common.cuh"
 #include "rp_conv.cuh"
@@ -53,6 +61,7 @@ struct NoallocArgs {
     const int64_t* order;   // sorted facet position -> input index (incoherent phases)
     const double* F;      // sorted facet store, FP64 SoA [12][nf]
     int64_t nf;
+    const double4* tiles;   // bounding sphere per RP_CULL_TILE sorted facets (may be null)
     const double* traces;
     DevParams dp;
     const C32* C1;
@@ -101,9 +110,20 @@ __device__ __forceinline__ void surface_leg(const NoallocArgs& A, const TraceRow
     *amp_o = amp;
 }
 
+// Whether tile tb of the sorted store may hold illuminated facets (one
+// thread tests the tile's sphere; the answer is block-uniform).
+__device__ __forceinline__ bool tile_live(const NoallocArgs& A, const TraceRow& t, int64_t tb, int* s_live) {
+    if (threadIdx.x == 0) s_live[0] = (A.tiles == nullptr) || !tile_outside(A.tiles[tb], t, A.dp.ap_rad);
+    __syncthreads();
+    const bool live = s_live[0] != 0;
+    __syncthreads();   // everyone has read the flag before thread 0 rewrites it
+    return live;
+}
+
 __global__ void __launch_bounds__(256) k_surface_noalloc(NoallocArgs A) {
     __shared__ double sh_max[32];
     __shared__ int sh_cnt[32];
+    __shared__ int s_live[1];
     const int s = blockIdx.x;
     const int nr = A.dp.nr;
     const TraceRow t = load_trace(A.traces, s);
@@ -118,12 +138,17 @@ __global__ void __launch_bounds__(256) k_surface_noalloc(NoallocArgs A) {
     C32* wb = wa + M;
     for (int i = threadIdx.x; i < 2 * nr; i += blockDim.x) acc[i] = 0;   // bins start at zero
     // pass 1: illuminated count and the largest amplitude (the fixed-point scale)
+    const int64_t ntiles = (A.nf + RP_CULL_TILE - 1) / RP_CULL_TILE;
     int cnt = 0;
     double vm = 0.0;
-    for (int64_t i = threadIdx.x; i < A.nf; i += blockDim.x) {
-        bool ok; float xx; C32 v; double amp;
-        surface_leg(A, t, i, &ok, &xx, &v, &amp);
-        if (ok) { ++cnt; vm = fmax(vm, amp); }
+    for (int64_t tb = 0; tb < ntiles; ++tb) {
+        if (!tile_live(A, t, tb, s_live)) continue;
+        const int64_t end = min(A.nf, (tb + 1) * (int64_t)RP_CULL_TILE);
+        for (int64_t i = tb * RP_CULL_TILE + threadIdx.x; i < end; i += blockDim.x) {
+            bool ok; float xx; C32 v; double amp;
+            surface_leg(A, t, i, &ok, &xx, &v, &amp);
+            if (ok) { ++cnt; vm = fmax(vm, amp); }
+        }
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int o = 16; o > 0; o >>= 1) {
@@ -143,19 +168,23 @@ __global__ void __launch_bounds__(256) k_surface_noalloc(NoallocArgs A) {
     // pass 2: fixed-point binning (order-independent integer sums)
     if (vm > 0) {
         const double scale = ldexp(1.0, RP_FIX_BITS) / (2.0 * (double)n * vm);
-        for (int64_t i = threadIdx.x; i < A.nf; i += blockDim.x) {
-            bool ok; float xf; C32 v; double amp;
-            surface_leg(A, t, i, &ok, &xf, &v, &amp);
-            if (!ok) continue;
-            double xx = xf;
-            if (!(xx > -1.0) || xx >= (double)nr) continue;
-            long b = (long)xx;
-            double w = xx - (double)b;
-            fix_add(acc + 2 * b, (double)v.x * (1.0 - w), scale);
-            fix_add(acc + 2 * b + 1, (double)v.y * (1.0 - w), scale);
-            if (b + 1 < nr) {
-                fix_add(acc + 2 * (b + 1), (double)v.x * w, scale);
-                fix_add(acc + 2 * (b + 1) + 1, (double)v.y * w, scale);
+        for (int64_t tb = 0; tb < ntiles; ++tb) {
+            if (!tile_live(A, t, tb, s_live)) continue;
+            const int64_t end = min(A.nf, (tb + 1) * (int64_t)RP_CULL_TILE);
+            for (int64_t i = tb * RP_CULL_TILE + threadIdx.x; i < end; i += blockDim.x) {
+                bool ok; float xf; C32 v; double amp;
+                surface_leg(A, t, i, &ok, &xf, &v, &amp);
+                if (!ok) continue;
+                double xx = xf;
+                if (!(xx > -1.0) || xx >= (double)nr) continue;
+                long b = (long)xx;
+                double w = xx - (double)b;
+                fix_add(acc + 2 * b, (double)v.x * (1.0 - w), scale);
+                fix_add(acc + 2 * b + 1, (double)v.y * (1.0 - w), scale);
+                if (b + 1 < nr) {
+                    fix_add(acc + 2 * (b + 1), (double)v.x * w, scale);
+                    fix_add(acc + 2 * (b + 1) + 1, (double)v.y * w, scale);
+                }
             }
         }
     }
@@ -167,10 +196,6 @@ __global__ void __launch_bounds__(256) k_surface_noalloc(NoallocArgs A) {
     __syncthreads();
     conv_linear_block<float>(in, A.C1, A.p2, nr, x, wa, wb, reinterpret_cast<C32*>(orow), 1.0f);
 }
-
-// Device address of the scratch array, looked up once per device.
-std::mutex g_mu;
-void* g_addr[64] = {};
 
 }  // namespace
 
@@ -201,20 +226,20 @@ extern "C" int rp_surface_noalloc(const rp_scene* s, const double* d_traces, int
     }
     if (s->device < 0 || s->device >= 64) { rp_set_error("rp_surface_noalloc: device ordinal"); return RP_ERR_ARG; }
     RP_CUDA(cudaSetDevice(s->device));
+    // The array's device address in the current context, looked up on every
+    // call (no allocation; the first call in a context also loads the
+    // library's module): a cached address would go stale if the context were
+    // reset and re-created.
     void* ptr = nullptr;
     {
-        std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_addr[s->device]) {
-            cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-            if (e != cudaSuccess) return rp_cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-            g_addr[s->device] = ptr;
-        }
-        ptr = g_addr[s->device];
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) return rp_cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
     }
     NoallocArgs A;
     A.F = s->d_sorted;
     A.order = s->d_order;
     A.nf = s->nf;
+    A.tiles = reinterpret_cast<const double4*>(s->d_tiles_sorted);
     A.traces = d_traces;
     A.dp = s->dp;
     A.C1 = reinterpret_cast<const C32*>(s->d_C1_32);

@@ -31,6 +31,20 @@ about 10:
   evaluation, the floor conversion pair, address arithmetic and the loop.
 """
 
+# The reference chain's own cost per leg (its kernels as written: every leg
+# recomputes the incident geometry, three facet_G directivities with their
+# sinc sines, Snell, Fresnel and the exponentials; geometry_kernels.cu:
+# 103-140, 207-350, 410-412, 426-584, radar_kernels.cu:658-892): about 150
+# FP32 FMA-class operations and 25 special-function operations per target
+# leg, 120 and 20 per surface leg.  This is the algorithmic basis of the
+# roofline: the fast form's hoisting (incident terms once per facet and
+# trace) and the outbound leg's reuse of the inbound evaluation show up as
+# a rate above the FP32 line on this basis.
+REF_FMA_PER_TARGET_LEG = 150
+REF_SFU_PER_TARGET_LEG = 25
+REF_FMA_PER_SURFACE_LEG = 120
+REF_SFU_PER_SURFACE_LEG = 20
+
 FP32_OPS_PER_EVAL = 58.4
 MUFU_PER_EVAL = 6
 INSTR_PER_EVAL = 54.0

@@ -144,6 +144,33 @@ def surface_arrays(params, stype, heights=None):
     return _soa(fxxs, fyys, fzzs, n_hat, u_hat, v_hat, mask)
 
 
+def surface_arrays_blocked(params, heights, rows_per_block=256):
+    """``surface_arrays(params, "flat", heights)`` for large grids, by blocks
+    of rows: the same values bit for bit (``gen_normals`` runs on each block
+    with two halo rows on either side, so the grid's edge rows keep its edge
+    rule), without the whole-grid (ny, nx, 3) temporaries."""
+    z = np.asarray(heights, dtype=np.float64)
+    ny, nx = z.shape
+    if ny < 3:
+        return surface_arrays(params, "flat", heights=z)
+    out = np.empty((12, ny * nx))
+    xs = np.arange(nx) * params["fs"] + params["ox"]
+    ys = np.arange(ny) * params["fs"] + params["oy"]
+    for r0 in range(0, ny, rows_per_block):
+        r1 = min(ny, r0 + rows_per_block)
+        h0, h1 = max(0, r0 - 2), min(ny, r1 + 2)
+        n_hat, u_hat, v_hat = gen_normals(params, z[h0:h1])
+        a, b = r0 - h0, r0 - h0 + (r1 - r0)
+        sl = slice(r0 * nx, r1 * nx)
+        out[0, sl] = np.tile(xs, r1 - r0)
+        out[1, sl] = np.repeat(ys[r0:r1], nx)
+        out[2, sl] = z[r0:r1].ravel()
+        for k, arr in enumerate((n_hat, u_hat, v_hat)):
+            for i in range(3):
+                out[3 + 3 * k + i, sl] = arr[a:b, :, i].ravel()
+    return out
+
+
 def make_surface(params, stype, filename, obj=None):
     """Write a facet file for a named surface (simple_surfaces.py:147-201)."""
     soa = surface_arrays(params, stype)

@@ -22,6 +22,27 @@ FORMS = {"plain": _abi.RP_FORM_PLAIN_F64, "fast": _abi.RP_FORM_FAST_F32}
 OUT_COMPLEX128 = 0x100
 
 
+# cudaStreamLegacy: the legacy default stream as an explicit handle.  A NULL
+# stream handle means "the library's own stream" in the C ABI, so torch's
+# default stream (handle 0) is passed as this value instead.
+CUDA_STREAM_LEGACY = 0x1
+
+
+def stream_handle(stream=None, device=None):
+    """The cudaStream_t to hand to the C ABI for a torch stream.
+
+    ``None`` selects torch's current stream on ``device``, so the call is
+    ordered after the torch work that produced its inputs (and before the
+    work that reads its outputs).  Torch's default stream has handle 0,
+    which the C ABI would read as "the library's own stream"; it is passed
+    as cudaStreamLegacy instead."""
+    import torch
+    if stream is None:
+        stream = torch.cuda.current_stream(device)
+    h = int(stream.cuda_stream)
+    return ctypes.c_void_p(h if h != 0 else CUDA_STREAM_LEGACY)
+
+
 def _as_params(params):
     if isinstance(params, _abi.RpParams):
         return params
@@ -114,20 +135,23 @@ class Scene:
     def simulate_device(self, d_traces, d_out, form="fast", stream=None, complex128=False,
                         counts=None):
         """Resident-input path: d_traces (ns, 9) float64 and d_out (ns, nr)
-        complex64 torch CUDA tensors; runs on ``stream`` (a torch stream).
+        complex64 torch CUDA tensors; runs on ``stream`` (a torch stream;
+        default: torch's current stream on the scene's device, so the call is
+        ordered after the torch work that filled its inputs).
         ``counts``: optional int64 numpy array (ns, 2) filled with N_ill, N_t."""
         ns = int(d_traces.shape[0])
         f = FORMS[form] | (OUT_COMPLEX128 if complex128 else 0)
-        sp = None if stream is None else ctypes.c_void_p(stream.cuda_stream)
+        sp = stream_handle(stream, self.device)
         cp = None if counts is None else counts.ctypes.data
         rc = _abi.lib().rp_simulate_device(self._h, ctypes.c_void_p(d_traces.data_ptr()), ns, f,
                                            ctypes.c_void_p(d_out.data_ptr()), cp, sp)
         _abi.check("rp_simulate_device", rc)
 
     def simulate_host_ptrs(self, traces_ptr, ns, out_ptr, form="fast", stream=None, counts=None):
-        """rp_simulate on raw host pointers (e.g. pinned torch tensors)."""
+        """rp_simulate on raw host pointers (e.g. pinned torch tensors); runs
+        on ``stream`` (default: torch's current stream on the scene's device)."""
         f = FORMS[form]
-        sp = None if stream is None else ctypes.c_void_p(stream.cuda_stream)
+        sp = stream_handle(stream, self.device)
         cp = None if counts is None else counts.ctypes.data
         rc = _abi.lib().rp_simulate(self._h, ctypes.c_void_p(traces_ptr), int(ns), f,
                                     ctypes.c_void_p(out_ptr), 0, cp, sp)
@@ -212,9 +236,7 @@ def simulate_batch(jobs, workspace=None, stream=None, return_counts=False):
         d_out.append(o)
         counts.append(c)
         arr[i] = _abi.RpJob(sc.handle, t.data_ptr(), tr.shape[0], o.data_ptr(), c.ctypes.data)
-    st = torch.cuda.current_stream(dev) if stream is None else stream
-    torch.cuda.synchronize(dev)
-    rc = _abi.lib().rp_simulate_batch(arr, len(jobs), ws.handle, ctypes.c_void_p(st.cuda_stream))
+    rc = _abi.lib().rp_simulate_batch(arr, len(jobs), ws.handle, stream_handle(stream, dev))
     _abi.check("rp_simulate_batch", rc)
     outs = [o.cpu().numpy() for o in d_out]
     return (outs, counts) if return_counts else outs

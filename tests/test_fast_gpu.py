@@ -7,7 +7,7 @@ peak, and an exact match of every trace's peak range bin.
 import numpy as np
 import pytest
 
-from helpers import peak_bins, phase_err_max, rel_l2, tiny_scene
+from helpers import peak_bins, phase_err_max, rel_l2, tiny_scene, vhf_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -89,28 +89,12 @@ def test_fast_polynomial_sinc_regimes(built_lib, oracle, nside):
     check(got, ref)
 
 
-def _vhf_scene(nr, n_side=120, fs=2.5, nt_side=4, ns=2, seed=5):
-    # 60 MHz / 10 MHz chirp sampled at 24 MHz, 2.5 m facets (the VHF band of
-    # the batched and flyby workloads), a rough layer 1 km deep
-    from europaraypaths_gb300 import scenes, simple_surfaces as ss
-    p = scenes.base_params(60e6, 10e6, 24e6, nr, 3.0, 3.15, 1e-6, 1.0, fs, 25e3, ns, 20.0, 7.3)
-    side = n_side * fs
-    dom = {"fs": fs, "nx": n_side, "ny": n_side, "ox": -side / 2, "oy": -side / 2}
-    h = scenes.gaussian_field(n_side, n_side, fs, 1.0, 20.0, seed)
-    facets = ss.surface_arrays(dom, "flat", heights=h)
-    tfs = side / nt_side
-    tdom = {"fs": tfs, "nx": nt_side, "ny": nt_side, "ox": -side / 2, "oy": -side / 2}
-    th = scenes.gaussian_field(nt_side, nt_side, tfs, 2.0, 50.0, seed + 1)
-    targets = ss.target_arrays(tdom, "flat", zoffset=-1000.0, heights=th)
-    return {"params": p, "facets": facets, "targets": targets}
-
-
 @pytest.mark.parametrize("nr", [4096, 8192, 16384, 6000])
 def test_fast_vhf_band(built_lib, oracle, nr):
     # compression storage modes: 4096 bins all in shared memory, 8192 the
     # product spectrum in global scratch, 16384 both buffers in global
     # scratch, 6000 (not a power of two) the Bluestein kernel
-    sc = _vhf_scene(nr)
+    sc = vhf_scene(nr)
     got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle)
     assert got.shape[1] == nr
     assert np.array_equal(cnt, rcnt)
@@ -132,7 +116,7 @@ def _slope_frames(facets):
 def test_fast_non_orthonormal_frames(built_lib, oracle):
     # a rough surface whose facet frames are not orthonormal takes the
     # general directivity (the facet normal from the record)
-    sc = _vhf_scene(2048, n_side=80)
+    sc = vhf_scene(2048, n_side=80)
     sc["facets"] = _slope_frames(sc["facets"])
     uv = np.abs(np.einsum("ij,ij->j", sc["facets"][6:9], sc["facets"][9:12]))
     assert uv.max() > 1e-3
@@ -144,7 +128,7 @@ def test_fast_non_orthonormal_frames(built_lib, oracle):
 def test_fast_orthonormal_and_general_frames_agree(built_lib, oracle, monkeypatch):
     # the same orthonormal scene through both directivity forms: the
     # orthonormal-frame shortcut is an identity, so they differ by rounding
-    sc = _vhf_scene(2048, n_side=80)
+    sc = vhf_scene(2048, n_side=80)
     got_o, ref, _, _ = fast_vs_oracle(sc, oracle)
     monkeypatch.setenv("RP_PAIR_ORTHO", "0")
     got_g, _, _, _ = fast_vs_oracle(sc, oracle)

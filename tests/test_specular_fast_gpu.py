@@ -101,8 +101,8 @@ def test_fast_specular_non_pow2_bins(built_lib, oracle):
 def test_fast_specular_vhf_band(built_lib, oracle, nr):
     # 60 MHz, 2.5 m facets: degree-6 gain polynomial, reradiation arguments up
     # to pi/2; 8192 bins: the product spectrum in global scratch
-    from test_fast_gpu import _vhf_scene
-    sc = _vhf_scene(nr)
+    from helpers import vhf_scene
+    sc = vhf_scene(nr)
     sc["params"].update({"specular": True, "rerad_funct": 0})
     got, ref = check_targets(sc, oracle)
     assert got.shape[1] == nr

@@ -83,8 +83,8 @@ def test_fast_ttype0_non_pow2_bins(built_lib, oracle):
 
 
 def test_fast_ttype0_vhf_band(built_lib, oracle):
-    from test_fast_gpu import _vhf_scene
-    sc = _vhf_scene(8192)
+    from helpers import vhf_scene
+    sc = vhf_scene(8192)
     sc["targets"][6, ::2] = 0.0
     got, ref = check_targets(sc, oracle)
     assert got.shape[1] == 8192
