@@ -349,6 +349,78 @@ def run_direct(args, sc, track, stream):
     return out
 
 
+def run_flyby(args, stream):
+    """The flyby-scale scene: 64M facets (8000x8000 at 2.5 m), two rough
+    layers (320k targets), 10,000 traces at 25 km, 60 MHz / 10 MHz sampled
+    at 24 MHz into 16384 bins.  pairs/s of the fast form over interior
+    traces (inputs resident, CUDA events on the launching stream), the stage
+    times, and one interior trace against the plain FP64 form (all targets)."""
+    import torch
+    from europaraypaths_gb300 import accuracy, opcount, scenes, simulator
+    dev = torch.cuda.current_device()
+    t0 = time.perf_counter()
+    sc = scenes.flyby(n_facets_side=args.flyby_facets_side)
+    t1 = time.perf_counter()
+    scene = simulator.Scene(sc["params"], sc["facets"], sc["targets"], device=dev)
+    t2 = time.perf_counter()
+    sc["facets"] = None                      # the scene holds its own device stores
+    try:
+        track = scene.default_traces()
+        n, steps = args.flyby_traces, args.flyby_steps
+        lo = track.shape[0] // 4
+        span = max(track.shape[0] // 2 - n, 1)
+        d_tr = [torch.from_numpy(np.ascontiguousarray(track[lo + (97 * k) % span:lo + (97 * k) % span + n])).cuda()
+                for k in range(steps + 1)]
+        d_out = torch.empty((n, scene.nr), dtype=torch.complex64, device="cuda")
+        c = [np.zeros((n, 2), np.int64) for _ in range(steps + 1)]
+        scene.simulate_device(d_tr[0], d_out, form="fast", stream=stream, counts=c[0])   # warm-up, tuning
+        torch.cuda.synchronize()
+        stage = {"setup_ms": 0.0, "pairs_ms": 0.0, "compress_ms": 0.0, "tail_ms": 0.0}
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(1, steps + 1):
+            scene.simulate_device(d_tr[k], d_out, form="fast", stream=stream, counts=c[k])
+            t = simulator.last_timing()
+            for key in stage:
+                stage[key] += t[key] / steps
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        cc = np.concatenate(c[1:])
+        pairs = float(opcount.pairs(cc)) / steps
+        out = {"value": pairs / (ms / 1e3), "unit": UNIT, "traces_per_step": n, "steps": steps, "ms_per_step": ms,
+               "stage_ms_per_step": stage, "mean_counts_per_trace": [float(cc[:, 0].mean()), float(cc[:, 1].mean())],
+               "pair_evals_per_s": float(opcount.target_evals(cc)) / steps / (stage["pairs_ms"] / 1e3)
+               if stage["pairs_ms"] > 0 else None,
+               "scene_generate_s": t1 - t0, "scene_create_s": t2 - t1,
+               "workload": (f"flyby: {args.flyby_facets_side}x{args.flyby_facets_side} facets at 2.5 m "
+                            f"({args.flyby_facets_side ** 2 / 1e6:g}M), fractal H=0.75 RMS 8 m; rough layers 1 km and "
+                            f"3 km deep as targets at 50 m ({sc['targets'].shape[1]}); {track.shape[0]} traces at "
+                            "25 km, 2 m spacing; 60 MHz/10 MHz, 24 MHz sampling, 16384 bins; aperture 3 deg; "
+                            "seeded synthetic")}
+        if args.flyby_plain:
+            k = track.shape[0] // 2
+            ptr = torch.from_numpy(np.ascontiguousarray(track[k:k + 1])).cuda()
+            pout = torch.empty((1, scene.nr), dtype=torch.complex128, device="cuda")
+            pc = np.zeros((1, 2), np.int64)
+            torch.cuda.synchronize()
+            p0 = torch.cuda.Event(enable_timing=True)
+            p1 = torch.cuda.Event(enable_timing=True)
+            p0.record(stream)
+            scene.simulate_device(ptr, pout, form="plain", stream=stream, counts=pc, complex128=True)
+            p1.record(stream)
+            torch.cuda.synchronize()
+            pv = opcount.pairs(pc) / (p0.elapsed_time(p1) / 1e3)
+            out["plain_form"] = {"value": pv, "unit": UNIT, "traces": 1, "fast_over_plain": out["value"] / pv}
+            acc = accuracy_vs_plain(scene, ptr, pout, pc, stream)
+            acc["trace_index"] = k
+            out["accuracy"] = acc
+        return out
+    finally:
+        scene.close()
+
+
 def run_io(n_facets=200_000, n_traces=200, nr=4096):
     """Host file I/O of the binary stores against the reference's text formats
     (seeded synthetic facets; no device work): parse a .fct text file vs map a
@@ -467,6 +539,60 @@ def run_serving(args, objs, tracks, plain_value):
     return st
 
 
+def run_serving_flybys(args, objs, tracks, plain_value):
+    """The serving loop at the flyby-request load: Poisson arrivals at
+    ``serve_rate`` requests/s for ``flyby_serve_seconds``; each request is a
+    flyby over one of the resident uneven scenes (drawn uniformly; up to 4M
+    facets) of U{50..2000} consecutive traces (capped at the scene's track).
+    The server cuts requests into 16-trace steps, keeps at most 16 requests
+    active, takes the next step of up to 16 of them per worker call (4
+    workers, overlapping on the device) and sheds requests still queued
+    after ``flyby_serve_max_wait`` seconds.  Latency is submit to result."""
+    from europaraypaths_gb300 import serving
+    rng = np.random.default_rng(44)
+    srv = serving.Server(workers=4, device=objs[0].device, max_batch=16, step_traces=16, max_active=16,
+                         max_wait=args.flyby_serve_max_wait)
+    sids = [srv.adopt_scene(o) for o in objs]
+    n_req = int(args.serve_rate * args.flyby_serve_seconds)
+    gaps = rng.exponential(1.0 / args.serve_rate, n_req)
+    reqs, offered_traces = [], 0
+    t_start = time.perf_counter()
+    t_next = t_start
+    for g in gaps:
+        t_next += g
+        dt = t_next - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        i = int(rng.integers(0, len(objs)))
+        ns = tracks[i].shape[0]
+        n = min(int(rng.integers(50, 2001)), ns)
+        lo = int(rng.integers(0, ns - n + 1))
+        reqs.append((n, srv.submit(sids[i], tracks[i][lo:lo + n])))
+        offered_traces += n
+    t_arrivals = time.perf_counter() - t_start
+    served_traces, shed = 0, 0
+    for n, r in reqs:
+        try:
+            r.result(timeout=900)
+            served_traces += n
+        except serving.ShedError:
+            shed += 1
+    t_done = time.perf_counter() - t_start
+    st = srv.stats()
+    srv.close(keep_scenes=True)
+    st.update({"requests": n_req, "rate_req_s": args.serve_rate, "arrival_window_s": t_arrivals,
+               "drained_after_s": t_done, "workers": 4, "step_traces": 16, "max_active": 16,
+               "max_wait_s": args.flyby_serve_max_wait,
+               "offered_traces": offered_traces, "served_traces": served_traces,
+               "request": "flyby over a uniform uneven scene (<= 4M facets), U{50..2000} consecutive traces",
+               "served_pairs_per_s_over_plain_form": (st["pairs_per_s"] / plain_value)
+               if (plain_value and st.get("pairs_per_s")) else None,
+               "note": ("offered load far above one GPU's capacity (requests average ~1000 traces): the "
+                        "queue-wait bound sheds what cannot start in time; latency = wait + service time "
+                        "shared by up to 16 active requests, the tail being the largest requests")})
+    return st
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -523,11 +649,23 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--serve-seconds", type=float, default=15.0, help="serving-loop arrivals window (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson request rate, requests/s")
+    ap.add_argument("--flyby-serve-seconds", type=float, default=15.0,
+                    help="arrivals window of the serving loop at flyby-request sizes (0 = skip)")
+    ap.add_argument("--flyby-serve-max-wait", type=float, default=5.0,
+                    help="queue-wait bound (s) of that serving run; older queued requests are shed")
     ap.add_argument("--no-io", dest="io", action="store_false", help="skip the host file-I/O measurement")
     ap.add_argument("--no-focus", dest="focus", action="store_false", help="skip the azimuth-focusing measurement")
     ap.add_argument("--spec-traces", type=int, default=4,
                     help="traces per step of the specular-mode and ttype-0 runs (0 = skip)")
     ap.add_argument("--spec-steps", type=int, default=3)
+    ap.add_argument("--flyby-traces", type=int, default=32,
+                    help="traces per step of the flyby-scale scene (0 = skip the flyby entry)")
+    ap.add_argument("--flyby-steps", type=int, default=2)
+    ap.add_argument("--flyby-facets-side", type=int, default=8000,
+                    help="facets per side of the flyby scene at 2.5 m (8000: the 64M-facet scene; "
+                         "2000: a 5 km square with the same band, altitude and aperture)")
+    ap.add_argument("--no-flyby-plain", dest="flyby_plain", action="store_false",
+                    help="skip the flyby trace in the plain FP64 form (accuracy check)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -705,6 +843,11 @@ def main():
                 line["direct"] = run_direct(args, sc, track, stream)
             except Exception as e:
                 line["direct"] = {"error": f"{type(e).__name__}: {e}"}
+        if args.flyby_traces > 0 and world == 1:
+            try:
+                line["flyby"] = run_flyby(args, stream)
+            except Exception as e:
+                line["flyby"] = {"error": f"{type(e).__name__}: {e}"}
         if args.focus and world == 1:
             try:
                 line["focus"] = run_focus()
@@ -715,7 +858,7 @@ def main():
                 line["io"] = run_io()
             except Exception as e:
                 line["io"] = {"error": f"{type(e).__name__}: {e}"}
-        if world == 1 and (args.batch_scenes > 0 or args.serve_seconds > 0):
+        if world == 1 and (args.batch_scenes > 0 or args.serve_seconds > 0 or args.flyby_serve_seconds > 0):
             scene.close()
             specs, objs, tracks, t_build = batch_workload(args, local)
             if args.batch_scenes > 0:
@@ -724,12 +867,17 @@ def main():
                     line["batch"]["setup_s"] = t_build
                 except Exception as e:       # reported in the line; the headline stands
                     line["batch"] = {"error": f"{type(e).__name__}: {e}"}
+            plain = line.get("plain_form", {}).get("value")
             if args.serve_seconds > 0:
-                plain = line.get("plain_form", {}).get("value")
                 try:
                     line["serving"] = run_serving(args, objs, tracks, plain)
                 except Exception as e:
                     line["serving"] = {"error": f"{type(e).__name__}: {e}"}
+            if args.flyby_serve_seconds > 0:
+                try:
+                    line["serving_flybys"] = run_serving_flybys(args, objs, tracks, plain)
+                except Exception as e:
+                    line["serving_flybys"] = {"error": f"{type(e).__name__}: {e}"}
             for o in objs:
                 o.close()
         print(json.dumps(line), flush=True)

@@ -98,6 +98,7 @@ _SIGS = {
     "rp_server_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p,
                           ctypes.c_void_p], ctypes.c_int),
     "rp_server_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "rp_server_configure": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "rp_submit": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rp_poll": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int], ctypes.c_int),

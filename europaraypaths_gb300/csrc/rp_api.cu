@@ -325,8 +325,9 @@ static int build_tables(rp_scene* s) {
         if (!(std::fabs((double)m * p.rx_sample_rate / N) > p.bandwidth)) K = m;
     s->crop_K = K;
     s->crop_all = (K >= N / 2);
-    // shared-memory path tables: nr a power of two, M = 4 nr
-    if (is_pow2(nr) && nr >= 4) {
+    // shared-memory path tables: nr a power of two (>= 16: the compression
+    // kernel's outer passes hold 16 elements a thread), M = 4 nr
+    if (is_pow2(nr) && nr >= 16) {
         const int n2 = 2 * nr, M = 4 * nr;
         int lM = 0;
         while ((1 << lM) < M) ++lM;
@@ -542,6 +543,7 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
         if ((rc = upload(&s->d_sorted, sorted.data(), sizeof(double) * 12 * nf, &s->store_bytes))) return fail(rc);
         const std::vector<double> ts = tile_spheres(sorted.data(), nf), tf = tile_spheres(facets, nf);
         if ((rc = upload(&s->d_tiles_sorted, ts.data(), sizeof(double) * ts.size(), &s->store_bytes))) return fail(rc);
+        s->h_tiles_sorted = ts;
         if ((rc = upload(&s->d_tiles_file, tf.data(), sizeof(double) * tf.size(), &s->store_bytes))) return fail(rc);
     }
     if ((rc = build_tables(s))) return fail(rc);
@@ -552,6 +554,12 @@ extern "C" int rp_scene_create(const rp_params* p, const double* facets, int64_t
     if (const char* v = getenv("RP_PAIR_VARIANT")) s->pair_variant = atoi(v) == 1 ? 1 : 0;
     // 0-3 for one segment (taken & 3), 4-9 also for multi-segment waves
     if (const char* v = getenv("RP_PAIR_CFG")) s->pair_cfg = std::max(0, std::min(9, atoi(v)));
+    // test mode of the timeout path: the pair kernels issue no bulk copy and
+    // give up after a short bounded wait, so the call returns RP_ERR_TIMEOUT
+    // with nothing in flight
+    if (const char* v = getenv("RP_TEST_STALL_COPIES")) {
+        if (atoi(v) != 0) { s->stall_copies = 1; s->spin_limit = RP_SPIN_LIMIT_TEST; }
+    }
     cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return fail(rp_cuda_fail(e, "cudaStreamCreate"));
     *out = s;

@@ -124,8 +124,10 @@ static __global__ void k_cull_count(const double* __restrict__ pos, int64_t nf,
 }
 
 // Pass 2: per trace, exclusive scan of the tile counts (one block per trace).
+// A count above the list's capacity is cut to it and, with over != null,
+// raises the flag (the host then reports an internal error).
 static __global__ void k_scan_tiles(int* __restrict__ tile_cnt, int ntiles, int* __restrict__ total,
-                                    int64_t cap) {
+                                    int64_t cap, int* __restrict__ over) {
     const int s = blockIdx.x;
     int* c = tile_cnt + (size_t)s * ntiles;
     int carry = 0;
@@ -137,7 +139,10 @@ static __global__ void k_scan_tiles(int* __restrict__ tile_cnt, int ntiles, int*
         if (i < ntiles) c[i] = carry + ex;
         carry += tot;
     }
-    if (threadIdx.x == 0) total[s] = (int)min((int64_t)carry, cap);
+    if (threadIdx.x == 0) {
+        total[s] = (int)min((int64_t)carry, cap);
+        if (over && (int64_t)carry > cap) atomicOr(over, 1);
+    }
 }
 
 // Pass 3: scatter the original indices of flagged elements in order.
@@ -205,7 +210,7 @@ static __global__ void k_count_flags(const uint8_t* __restrict__ flags, int64_t 
 // per-tile counts are already in tile_cnt (the facet cull fuses them).
 static inline void compact_flags(const uint8_t* flags, int64_t n, int ns, int* tile_cnt,
                                  int* d_total, int* idx, int64_t stride, bool counted,
-                                 cudaStream_t st) {
+                                 cudaStream_t st, int* over = nullptr) {
     const int nt = (int)((n + RP_TILE - 1) / RP_TILE);
     if (nt == 0 || ns == 0) {
         if (ns) cudaMemsetAsync(d_total, 0, sizeof(int) * ns, st);
@@ -215,7 +220,7 @@ static inline void compact_flags(const uint8_t* flags, int64_t n, int ns, int* t
         k_count_flags<<<dim3(nt, ns), RP_TILE_THREADS, 0, st>>>(flags, n, tile_cnt);
         RP_LAUNCHED();
     }
-    k_scan_tiles<<<ns, 1024, 0, st>>>(tile_cnt, nt, d_total, stride);
+    k_scan_tiles<<<ns, 1024, 0, st>>>(tile_cnt, nt, d_total, stride, over);
     RP_LAUNCHED();
     k_scatter<<<dim3(nt, ns), RP_TILE_THREADS, 0, st>>>(flags, n, tile_cnt, nt, idx, stride);
     RP_LAUNCHED();

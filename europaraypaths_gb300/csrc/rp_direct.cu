@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(RP_DS_THREADS, 1) k_direct32(const __grid_cons
         float sR = 0, cR = 1, cI = 1, sI = 0, a0 = 0;
         float4 ea = make_float4(1e30f, 0.f, 0.f, 0.f), eb = make_float4(0.f, 0.f, 0.f, 0.f);
         if (ok) {
-            const int64_t f = A.idx[(size_t)s * A.nf + j];
+            const int64_t f = A.idx[(size_t)s * A.fstride + j];
             const double* F = A.F;
             const int64_t m = A.nf;
             fx = F[f]; fy = F[m + f]; fz = F[2 * m + f];
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(RP_DS_THREADS, 1) k_direct32(const __grid_cons
                 a0 = ln ? tv.y : tv.x;
             }
             // reflRadarSignal's source: fRe exp(+j 4 pi_F Itd / lam) at Itd
-            const C32 w = A.sv[(size_t)s * A.nf + j];
+            const C32 w = A.sv[(size_t)s * A.fstride + j];
             ds_entry((itd - t.rst) * A.inv_dr, w.x, w.y, base, A, ea, eb);
         }
         __syncthreads();            // the previous batch's entries are consumed

@@ -87,7 +87,7 @@ __device__ __forceinline__ float spec_surface_amp(const DevParams& dp, double gr
 // kernel carries none of their code.
 template <bool SPEC, bool T0>
 __global__ void __launch_bounds__(RP_CHUNK)
-k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx,
+k_facets32(const double* __restrict__ F, int64_t nf, int64_t fstride, const int* __restrict__ idx,
            const int* __restrict__ nill, const double* __restrict__ traces, DevParams dp,
            FacetPair* __restrict__ rec, ChunkMeta* __restrict__ meta, int64_t rstride,
            int64_t mstride, float* __restrict__ sx_o, C32* __restrict__ sv_o,
@@ -105,7 +105,7 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
     double fx = 0, fy = 0, fz = 0;
     int64_t i = 0;
     if (ok) {
-        i = idx[(size_t)s * nf + j];
+        i = idx[(size_t)s * fstride + j];
         fx = F[i]; fy = F[nf + i]; fz = F[2 * nf + i];
     }
     // chunk bounding box and centre (FP64)
@@ -118,7 +118,7 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
     // the trace origin is its first illuminated facet; the chunk centre is
     // the origin plus the FP32 rounding of (bounding-box centre - origin), so
     // its offset cf from the origin is exact in FP32
-    const int64_t i0 = idx[(size_t)s * nf];
+    const int64_t i0 = idx[(size_t)s * fstride];
     const double ox = F[i0], oy = F[nf + i0], oz = F[2 * nf + i0];
     const float cfx = (float)(0.5 * (mnx + mxx) - ox), cfy = (float)(0.5 * (mny + mxy) - oy),
                 cfz = (float)(0.5 * (mnz + mxz) - oz);
@@ -199,8 +199,8 @@ k_facets32(const double* __restrict__ F, int64_t nf, const int* __restrict__ idx
                 sincospif(-2.f * ft, &sn, &cs);
         }
         xI = (float)((d - t.rst) * dp.inv_dr);
-        sx_o[(size_t)s * nf + j] = xI;
-        sv_o[(size_t)s * nf + j] = C32{amp * cs, amp * sn};
+        sx_o[(size_t)s * fstride + j] = xI;
+        sv_o[(size_t)s * fstride + j] = C32{amp * cs, amp * sn};
         amax = fabsf(amp);
         // hoisted target-leg amplitude: sqrt(P Gr G frc n) lam^2 Dmax / ((4 pi)^2 Itd),
         // times fs^2 / lam of the reradiation factors in specular mode
@@ -490,9 +490,10 @@ __global__ void __launch_bounds__(256) k_t0_part32(const int* __restrict__ ntl1,
             if (i >= nr) break;
             double vr = 0.0, vi = 0.0;
             for (int p = 0; p < RP_PARTS; ++p) {
-                const C32 u = T[(((size_t)p * nb + s) * tstride + q) * Wt + o];
-                vr += u.x;
-                vi += u.y;
+                const size_t ui = (((size_t)p * nb + s) * tstride + q) * Wt + o;
+                const float4 u = reinterpret_cast<const float4*>(T)[ui];
+                vr += (double)u.x + (double)u.z;
+                vi += (double)u.y + (double)u.w;
             }
             double2 c = acc[i];
             c.x += vr;
@@ -556,7 +557,7 @@ k_pairs32(const __grid_constant__ PairArgs A) {
         const int part = item % RP_PARTS;
         const int tb = (item / RP_PARTS) % A.tblocks;
         const int s = item / (RP_PARTS * A.tblocks);
-        pair_item<NT, ILP, ORTHO, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase);
+        if (!pair_item<NT, ILP, ORTHO, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase)) break;
     }
     RP_PAIR_SMEM_END
 }
@@ -591,9 +592,10 @@ __global__ void k_conv32(const int* __restrict__ ntl, int64_t tstride, int nb, c
             const int o = i - b0;
             if (o >= 0 && o < Wt) {
                 for (int p = 0; p < RP_PARTS; ++p) {
-                    const C32 u = T[(((size_t)p * nb + s) * tstride + q) * Wt + o];
-                    v.x += u.x;
-                    v.y += u.y;
+                    const size_t ui = (((size_t)p * nb + s) * tstride + q) * Wt + o;
+                    const float4 u = reinterpret_cast<const float4*>(T)[ui];
+                    v.x += u.x + u.z;
+                    v.y += u.y + u.w;
                 }
             }
             tr[i] = v;
@@ -601,9 +603,10 @@ __global__ void k_conv32(const int* __restrict__ ntl, int64_t tstride, int nb, c
                 C32 u2{0.f, 0.f};
                 if (o >= 0 && o < Wt)
                     for (int p = 0; p < RP_PARTS; ++p) {
-                        const C32 u = T2[(((size_t)p * nb + s) * tstride + q) * Wt + o];
-                        u2.x += u.x;
-                        u2.y += u.y;
+                        const size_t ui = (((size_t)p * nb + s) * tstride + q) * Wt + o;
+                        const float4 u = reinterpret_cast<const float4*>(T2)[ui];
+                        u2.x += u.x + u.z;
+                        u2.y += u.y + u.w;
                     }
                 tr2[i] = u2;
             }
@@ -615,28 +618,17 @@ __global__ void k_conv32(const int* __restrict__ ntl, int64_t tstride, int nb, c
     }
 }
 
-// Shared-memory range compression (nr a power of two, 6 nr complex values of
-// shared memory).  One work item = RP_CONV_SPLIT consecutive targets of one
-// trace; their contributions are summed in target order in registers and
-// written as one partial trace.  Per target (X: 2nr, W: M = 4nr):
-//   X = DIF(pad T)                         T = sum of the facet-range parts
-//   W = DIT(X * C2)[nr/2 ..] / 2nr         Ptarg (convolvePhasorChirpLinear)
-//   W = DIT(X * DIF(pad Ptarg)) * s / 2nr  u = Psour (*) Ptarg, Psour = s T
-//                                          (specular: X = DIF(pad T2) first)
-//                                          (length N = 2nr - 1: the N-point
-//                                          circular product has no wrap)
-//   W = DIT_M(DIF_M(pad u) * H)            u (*) h, h = IDFT_N(crop mask)
-//   out[j] += W[2j] + W[2j + N]            circular on N, takeEveryOtherComplex
-// cropSpectrum + IDFT_N is the fixed circular convolution with h, so the two
-// N-point Bluestein transforms of convolveComplex reduce to one linear
-// convolution at M >= 2N - 1 (radar_kernels.cu:554-649,
+// Arguments of one segment's range compression (a job of k_conv32s): the
+// targets' rows T (and T2), their windows, the target chirp's spectrum C2s
+// and the crop kernel's Hs (both in the in-place transforms' digit-reversed
+// order), and the per-split sums of u it writes (radar_kernels.cu:554-649,
 // elementary_kernels.cu:258-353).
 struct ConvArgs {
     const int* ntl;
     int64_t tstride;
     int nb;
     const int* bt0;
-    const C32* T;
+    const C32* T;           // rows [RP_PARTS][nb][tstride][Wt], each element {high, low}
     const C32* T2;          // specular mode: the outbound leg's parts (Psour), else null
     int Wt;
     const Cplx<float>* C2s;
@@ -648,24 +640,74 @@ struct ConvArgs {
     unsigned int* work;
 };
 
-// Per target: u = Psour (*) Ptarg (convolveComplex's linear convolution,
-// N = 2nr - 1 values) from four transforms of 2nr; the item's targets' u
-// are summed.  The rest of the chain (cropSpectrum, the inverse N-point
-// DFT, takeEveryOtherComplex) is linear in u and the same for every target,
-// so it runs once per trace on the sum (k_trace_m32) instead of per target.
+// The target's trace (the facet-range parts summed in fixed order, each
+// part's row element high + low) at position k of the zero-padded 2nr input:
+// zero outside the target's window [b0, b0 + Wt) and beyond nr.
+__device__ __forceinline__ Cplx<float> trace_at(const C32* __restrict__ T, size_t pstride, size_t qbase, int k,
+                                                int b0, int Wt, int nr) {
+    Cplx<float> v{0.f, 0.f};
+    const int o = k - b0;
+    if (k < nr && o >= 0 && o < Wt) {
+        const float4* T4 = reinterpret_cast<const float4*>(T);
+        for (int p = 0; p < RP_PARTS; ++p) {
+            const float4 u = T4[(size_t)p * pstride + qbase + o];
+            v.x += u.x + u.z;
+            v.y += u.y + u.w;
+        }
+    }
+    return v;
+}
+
+// DIF of the zero-padded target trace into a (n values): the first fused
+// pass reads its 16 inputs straight from the target's rows (only the window
+// is non-zero), the rest run in place.  Ends with a barrier.
+__device__ __forceinline__ void dif_trace(Cplx<float>* a, const C32* __restrict__ T, size_t pstride, size_t qbase,
+                                          int b0, int Wt, int nr, int n) {
+    const int S = n >> 4;
+    for (int g = threadIdx.x; g < S; g += RP_CONV_THREADS) {
+        Cplx<float> x[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) x[i] = trace_at(T, pstride, qbase, g + i * S, b0, Wt, nr);
+        dif16_regs(x, g, n);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) a[swz(g + i * S)] = x[i];
+    }
+    __syncthreads();
+    block_dif_s_from(a, n, n >> 4);
+}
+
+// Shared-memory range compression (nr a power of two >= 32).  One work item =
+// RP_CONV_SPLIT consecutive targets of one trace; their contributions are
+// summed in target order and written as one partial trace.  Per target (n =
+// 2nr values in X and W):
+//   X = DIF(pad T)                         T = sum of the facet-range parts
+//   W = DIT(X * C2)[nr/2 ..] / 2nr         Ptarg (convolvePhasorChirpLinear)
+//   W = DIT(X * DIF(pad Ptarg)) * s / 2nr  u = Psour (*) Ptarg, Psour = s T
+//                                          (specular: X = DIF(pad T2) first)
+//                                          (length N = 2nr - 1: the N-point
+//                                          circular product has no wrap)
+// The rest of the chain (cropSpectrum, the inverse N-point DFT,
+// takeEveryOtherComplex) is linear in u and the same for every target, so it
+// runs once per trace on the sum (k_trace_m32).  The transforms are the
+// in-place stages of rp_fft.cuh with the elements at swizzled positions, and
+// three pass boundaries are crossed in registers instead of shared memory:
+//  * the first DIF pass of X reads the target's rows directly;
+//  * Ptarg is a shift by nr/2 = 4 S of the first transform's natural-order
+//    output, S = n / 16, and the first DIF pass of the second transform reads
+//    elements g + i S (i < 8 non-zero) -- exactly the registers x[i + 4] that
+//    the last DIT pass of the first transform leaves in the same thread -- so
+//    the two passes and the shift run back to back in registers;
+//  * the last DIT pass of the product transform adds its outputs u[g + i S]
+//    straight into the item's sums.
 // Persistent over the items of one or more batches (job j owns items
-// [start[j], start[j + 1])).  X (2nr) and W (2nr, + nr staging in modes 1
-// and 2) hold every element at its swizzled position (swz, rp_fft.cuh:
-// conflict-free in shared memory, within one 256-byte row in global
-// memory); twiddles come from the SFU.  MODE 0: X and W in shared memory
-// (nr <= 4096), the targets summed in registers.  MODE 1 (nr = 8192): every
-// transform in one 2nr buffer of shared memory; X waits in this block's slot
-// of the global scratch between its two uses.  MODE 2: X and W in the slot
-// (nr >= 16384).  Modes 1 and 2 sum the targets in the
-// item's partial row in global memory (same thread, same element, same
-// target order as the registers of mode 0, so every mode gives the same
-// sums).
-template <int KPT, int MODE, bool SPEC>
+// [start[j], start[j + 1])); twiddles come from the SFU.  MODE 0: X and W in
+// shared memory (nr <= 4096), the sums in registers (thread g owns elements
+// g + i S).  MODE 1 (nr = 8192): every transform in one n-value buffer of
+// shared memory; X waits in this block's slot of the global scratch between
+// its two uses.  MODE 2: X and W in the slot (nr >= 16384).  Modes 1 and 2
+// sum the targets in the item's partial row in global memory (same element,
+// same target order as mode 0, so every mode gives the same sums).
+template <int MODE, bool SPEC>
 __global__ void __launch_bounds__(RP_CONV_THREADS, 1)
 k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ start, int njobs,
           unsigned int* work, Cplx<float>* __restrict__ gscr, size_t gslot) {
@@ -698,15 +740,18 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
         curJ = jb;
         const unsigned int item = item0 - start[jb];
         const int nr = A.nr, n2 = A.n2, N = A.N;
-        Cplx<float>* const X = (MODE == 2) ? gbase : sbase;
-        Cplx<float>* const W = (MODE == 0) ? sbase + n2 : (MODE == 1 ? gbase : gbase + n2);
+        const int S = n2 >> 4;                  // groups of the outer fused passes
+        // X: DIF(pad T) (and DIF(pad T2) in specular mode); W: the working transform
+        Cplx<float>* const X = (MODE == 2) ? gbase : (MODE == 1 ? gbase : sbase);
+        Cplx<float>* const W = (MODE == 0) ? sbase + n2 : (MODE == 1 ? sbase : gbase + n2);
         // the job's arguments in registers (the loops below store to shared
         // memory, which would otherwise force re-reads of A)
         const Cplx<float>* __restrict__ C2s = A.C2s;
         const C32* __restrict__ T = A.T;
         const C32* __restrict__ T2 = A.T2;
-        const int Wt = A.Wt, nbA = A.nb, nsplit = A.nsplit;
+        const int Wt = A.Wt, nsplit = A.nsplit;
         const int64_t tstride = A.tstride;
+        const size_t pstride = (size_t)A.nb * tstride * Wt;
         const float sig_scale = A.sig_scale;
         const int* __restrict__ bt0 = A.bt0;
         C32* __restrict__ part = A.part;
@@ -717,197 +762,100 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
         if (q0 >= nq) continue;
         const int q1 = min(q0 + RP_CONV_SPLIT, nq);
         C32* const out = part + ((size_t)s * nsplit + sp) * n2;
-        float accr[2 * KPT], acci[2 * KPT];
+        float accr[16], acci[16];               // MODE 0: u at g + i S, g = tid
 #pragma unroll
-        for (int i = 0; i < 2 * KPT; ++i) { accr[i] = 0.f; acci[i] = 0.f; }
+        for (int i = 0; i < 16; ++i) { accr[i] = 0.f; acci[i] = 0.f; }
         if (MODE != 0)
             for (int j = tid; j < N; j += RP_CONV_THREADS) out[j] = C32{0.f, 0.f};
+        const float inv = 1.f / (float)n2;
+        const float sc = sig_scale / (float)n2;
         for (int q = q0; q < q1; ++q) {
             const int b0 = bt0[(size_t)s * tstride + q];
+            const size_t qbase = ((size_t)s * tstride + q) * Wt;
+            // ---- X = DIF(pad T); W = X * C2 (mode 1: X parks in the slot)
             if constexpr (MODE == 1) {
-                // every transform in shared memory (S, 2nr values); X =
-                // DIF(pad T) waits in the block's global slot (Xg) between
-                // its two uses, Ptarg moves through Mv (nr values)
-                Cplx<float>* const S = sbase;
-                Cplx<float>* const Xg = gbase;
-                Cplx<float>* const Mv = gbase + n2;
+                dif_trace(W, T, pstride, qbase, b0, Wt, nr, n2);
                 #pragma unroll 8
                 for (int k = tid; k < n2; k += RP_CONV_THREADS) {
-                    Cplx<float> v{0.f, 0.f};
-                    const int o = k - b0;
-                    if (k < nr && o >= 0 && o < Wt) {
-                        for (int p = 0; p < RP_PARTS; ++p) {
-                            const C32 u = T[(((size_t)p * nbA + s) * tstride + q) * Wt + o];
-                            v.x += u.x;
-                            v.y += u.y;
-                        }
-                    }
-                    S[swz(k)] = v;
+                    const Cplx<float> v = W[swz(k)];
+                    X[swz(k)] = v;
+                    W[swz(k)] = c_mul(v, C2s[k]);
                 }
-                __syncthreads();
-                block_dif_s<float>(S, n2);
+            } else {
+                dif_trace(X, T, pstride, qbase, b0, Wt, nr, n2);
                 #pragma unroll 8
-                for (int k = tid; k < n2; k += RP_CONV_THREADS) {
-                    const Cplx<float> v = S[swz(k)];
-                    Xg[swz(k)] = v;
-                    S[swz(k)] = c_mul(v, C2s[k]);
-                }
-                __syncthreads();
-                block_dit_s<float>(S, n2);
-                {   // Ptarg = S[nr/2 + k] / n2 moved to the front, zero padded
-                    const float inv = 1.f / (float)n2;
-                    for (int k = tid; k < nr; k += RP_CONV_THREADS) Mv[k] = S[swz(nr / 2 + k)];
-                    __syncthreads();
-                    for (int k = tid; k < nr; k += RP_CONV_THREADS) {
-                        const Cplx<float> v = Mv[k];
-                        S[swz(k)] = Cplx<float>{v.x * inv, v.y * inv};
-                    }
+                for (int k = tid; k < n2; k += RP_CONV_THREADS) W[swz(k)] = c_mul(X[swz(k)], C2s[k]);
+            }
+            __syncthreads();
+            // ---- Ptarg: every DIT stage but the last fused pass, then that
+            // pass, the shift by nr/2 with the 1/2nr scale and zero padding,
+            // and the first DIF pass of DIF(pad Ptarg), in registers
+            block_dit_s_upto(W, n2, n2 >> 4);
+            for (int g = tid; g < S; g += RP_CONV_THREADS) {
+                Cplx<float> x[16];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) x[i] = W[swz(g + i * S)];
+                dit16_regs(x, g, n2 >> 2);
+#pragma unroll
+                for (int i = 0; i < 8; ++i) x[i] = Cplx<float>{x[i + 4].x * inv, x[i + 4].y * inv};
+#pragma unroll
+                for (int i = 8; i < 16; ++i) x[i] = Cplx<float>{0.f, 0.f};
+                dif16_regs(x, g, n2);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) W[swz(g + i * S)] = x[i];
+            }
+            __syncthreads();
+            block_dif_s_from(W, n2, n2 >> 4);
+            // ---- the spectra's product, scaled
+            if constexpr (SPEC) {
+                // Psour = s T2, the outbound leg's own trace: mode 1 parks
+                // DIF(Ptarg) in the slot and transforms T2 in shared memory
+                if constexpr (MODE == 1) {
                     #pragma unroll 8
-                    for (int k = nr + tid; k < n2; k += RP_CONV_THREADS) S[swz(k)] = Cplx<float>{0.f, 0.f};
+                    for (int k = tid; k < n2; k += RP_CONV_THREADS) X[swz(k)] = W[swz(k)];
                     __syncthreads();
+                    dif_trace(W, T2, pstride, qbase, b0, Wt, nr, n2);
+                } else {
+                    dif_trace(X, T2, pstride, qbase, b0, Wt, nr, n2);
                 }
-                block_dif_s<float>(S, n2);
-                if constexpr (SPEC) {
-                    // Psour = s T2: DIF(Ptarg) moves to the slot, S takes DIF(pad T2)
-                    #pragma unroll 8
-                    for (int k = tid; k < n2; k += RP_CONV_THREADS) Xg[swz(k)] = S[swz(k)];
-                    __syncthreads();
-                    #pragma unroll 8
-                    for (int k = tid; k < n2; k += RP_CONV_THREADS) {
-                        Cplx<float> v{0.f, 0.f};
-                        const int o = k - b0;
-                        if (k < nr && o >= 0 && o < Wt) {
-                            for (int p = 0; p < RP_PARTS; ++p) {
-                                const C32 u = T2[(((size_t)p * nbA + s) * tstride + q) * Wt + o];
-                                v.x += u.x;
-                                v.y += u.y;
-                            }
-                        }
-                        S[swz(k)] = v;
-                    }
-                    __syncthreads();
-                    block_dif_s<float>(S, n2);
-                }
-                {
-                    const float sc = sig_scale / (float)n2;
-                    #pragma unroll 8
-                    for (int k = tid; k < n2; k += RP_CONV_THREADS) {
-                        // the spectra's product in the same operand order as the other modes
-                        const Cplx<float> v = SPEC ? c_mul(S[swz(k)], Xg[swz(k)]) : c_mul(Xg[swz(k)], S[swz(k)]);
-                        S[swz(k)] = Cplx<float>{v.x * sc, v.y * sc};
-                    }
-                }
-                __syncthreads();
-                block_dit_s<float>(S, n2);                            // u (natural, N values)
-                for (int j = tid; j < N; j += RP_CONV_THREADS) {
-                    const Cplx<float> a = S[swz(j)];
-                    C32 o = out[j];
-                    o.x += a.x;
-                    o.y += a.y;
-                    out[j] = o;
-                }
-                __syncthreads();
-                continue;
             }
             #pragma unroll 8
             for (int k = tid; k < n2; k += RP_CONV_THREADS) {
-                Cplx<float> v{0.f, 0.f};
-                const int o = k - b0;
-                if (k < nr && o >= 0 && o < Wt) {
-                    for (int p = 0; p < RP_PARTS; ++p) {
-                        const C32 u = T[(((size_t)p * nbA + s) * tstride + q) * Wt + o];
-                        v.x += u.x;
-                        v.y += u.y;
-                    }
-                }
-                X[swz(k)] = v;
+                // the operand order of the product is the same in every mode
+                const Cplx<float> v = (SPEC && MODE == 1) ? c_mul(W[swz(k)], X[swz(k)]) : c_mul(X[swz(k)], W[swz(k)]);
+                W[swz(k)] = Cplx<float>{v.x * sc, v.y * sc};
             }
             __syncthreads();
-            block_dif_s<float>(X, n2);
-            #pragma unroll 8
-            for (int k = tid; k < n2; k += RP_CONV_THREADS) W[swz(k)] = c_mul(X[swz(k)], C2s[k]);
-            __syncthreads();
-            block_dit_s<float>(W, n2);
-            {   // Ptarg = W[nr/2 + k] / n2 moved to the front, zero padded
-                const float inv = 1.f / (float)n2;
-                if (MODE == 0) {    // through registers
-                    Cplx<float> keep[KPT];
+            // ---- u = DIT(...): the last fused pass adds into the sums
+            block_dit_s_upto(W, n2, n2 >> 4);
+            for (int g = tid; g < S; g += RP_CONV_THREADS) {
+                Cplx<float> x[16];
 #pragma unroll
-                    for (int c = 0; c < KPT; ++c) {
-                        const int k = tid + c * RP_CONV_THREADS;
-                        if (k < nr) keep[c] = W[swz(nr / 2 + k)];
-                    }
-                    __syncthreads();
+                for (int i = 0; i < 16; ++i) x[i] = W[swz(g + i * S)];
+                dit16_regs(x, g, n2 >> 2);
+                if (MODE == 0) {
 #pragma unroll
-                    for (int c = 0; c < KPT; ++c) {
-                        const int k = tid + c * RP_CONV_THREADS;
-                        if (k < nr) W[swz(k)] = Cplx<float>{keep[c].x * inv, keep[c].y * inv};
-                    }
-                } else {            // through W's unused upper part [n2, n2 + nr)
-                    for (int k = tid; k < nr; k += RP_CONV_THREADS) W[swz(n2 + k)] = W[swz(nr / 2 + k)];
-                    __syncthreads();
-                    for (int k = tid; k < nr; k += RP_CONV_THREADS) {
-                        const Cplx<float> v = W[swz(n2 + k)];
-                        W[swz(k)] = Cplx<float>{v.x * inv, v.y * inv};
-                    }
-                }
-                #pragma unroll 8
-                for (int k = nr + tid; k < n2; k += RP_CONV_THREADS) W[swz(k)] = Cplx<float>{0.f, 0.f};
-                __syncthreads();
-            }
-            block_dif_s<float>(W, n2);
-            if constexpr (SPEC) {   // Psour = s T2, the outbound leg's own trace
-                #pragma unroll 8
-                for (int k = tid; k < n2; k += RP_CONV_THREADS) {
-                    Cplx<float> v{0.f, 0.f};
-                    const int o = k - b0;
-                    if (k < nr && o >= 0 && o < Wt) {
-                        for (int p = 0; p < RP_PARTS; ++p) {
-                            const C32 u = T2[(((size_t)p * nbA + s) * tstride + q) * Wt + o];
-                            v.x += u.x;
-                            v.y += u.y;
+                    for (int i = 0; i < 16; ++i)
+                        if (g + i * S < N) { accr[i] += x[i].x; acci[i] += x[i].y; }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const int j = g + i * S;
+                        if (j < N) {
+                            C32 o = out[j];
+                            o.x += x[i].x;
+                            o.y += x[i].y;
+                            out[j] = o;
                         }
                     }
-                    X[swz(k)] = v;
-                }
-                __syncthreads();
-                block_dif_s<float>(X, n2);
-            }
-            {
-                const float sc = sig_scale / (float)n2;
-                #pragma unroll 8
-                for (int k = tid; k < n2; k += RP_CONV_THREADS) {
-                    Cplx<float> v = c_mul(X[swz(k)], W[swz(k)]);
-                    W[swz(k)] = Cplx<float>{v.x * sc, v.y * sc};
-                }
-            }
-            __syncthreads();
-            block_dit_s<float>(W, n2);                                // u (natural, N values)
-            if (MODE == 0) {
-#pragma unroll
-                for (int i = 0; i < 2 * KPT; ++i) {
-                    const int j = tid + i * RP_CONV_THREADS;
-                    if (j < N) {
-                        const Cplx<float> a = W[swz(j)];
-                        accr[i] += a.x;
-                        acci[i] += a.y;
-                    }
-                }
-            } else {
-                for (int j = tid; j < N; j += RP_CONV_THREADS) {
-                    const Cplx<float> a = W[swz(j)];
-                    C32 o = out[j];
-                    o.x += a.x;
-                    o.y += a.y;
-                    out[j] = o;
                 }
             }
             __syncthreads();
         }
-        if (MODE == 0) {
+        if (MODE == 0 && tid < S) {
 #pragma unroll
-            for (int i = 0; i < 2 * KPT; ++i) {
-                const int j = tid + i * RP_CONV_THREADS;
+            for (int i = 0; i < 16; ++i) {
+                const int j = tid + i * S;
                 if (j < N) out[j] = C32{accr[i], acci[i]};
             }
         }
@@ -1031,7 +979,8 @@ __global__ void k_sum32(const int* __restrict__ nill, const int* __restrict__ nt
 struct FastLayout {
     int nb;
     int64_t tstride;
-    int64_t rstride;     // records per trace (nf rounded to chunks)
+    int64_t fstride;     // illuminated facets a trace can hold (host bound, <= nf)
+    int64_t rstride;     // records per trace (fstride rounded to chunks)
     int64_t mstride;     // chunks per trace
     int Wt;
     int slots;
@@ -1048,7 +997,7 @@ void fast_take_setup(Aa& a, const rp_scene* sc, const FastLayout& L) {
     a.template take<int>(L.nb);                             // nill
     a.template take<int>(L.nb);                             // ntl
     a.template take<unsigned long long>(L.nb);              // vmax
-    a.template take<int>((size_t)L.nb * nf);                // idx
+    a.template take<int>((size_t)L.nb * L.fstride);         // idx
     a.template take<FacetPair>((size_t)L.nb * L.rstride / 2);    // records (facet pairs)
     if (sc->dp.specular) a.template take<FacetSpec>((size_t)L.nb * L.rstride / 2);
     if (sc->nt1 < sc->nt) {
@@ -1057,8 +1006,8 @@ void fast_take_setup(Aa& a, const rp_scene* sc, const FastLayout& L) {
     }
     a.template take<ChunkMeta>((size_t)L.nb * L.mstride);   // chunk meta
     a.template take<double>((size_t)L.nb * 4);              // trace origins
-    a.template take<float>((size_t)L.nb * nf);              // surface x
-    a.template take<C32>((size_t)L.nb * nf);                // surface v
+    a.template take<float>((size_t)L.nb * L.fstride);       // surface x
+    a.template take<C32>((size_t)L.nb * L.fstride);         // surface v
     a.template take<TraceMeta>(L.nb);
     a.template take<uint8_t>((size_t)L.nb * nt);            // target flags
     a.template take<int>((size_t)L.nb * nt);                // tlist
@@ -1081,12 +1030,11 @@ int conv_mode(const rp_scene* sc) {
     return 2;
 }
 
-// Complex values in one block's slot of the global compression scratch: 2nr
-// (W in mode 2, X in mode 1) plus nr for the Ptarg shift, and X (2nr) in
-// mode 2.
+// Complex values in one block's slot of the global compression scratch: X
+// (2nr) in mode 1, X and W (2nr each) in mode 2.
 size_t conv_gslot(const rp_scene* sc) {
     const int m = conv_mode(sc);
-    return m == 1 ? (size_t)3 * sc->nr : (m == 2 ? (size_t)5 * sc->nr : 0);
+    return m == 1 ? (size_t)2 * sc->nr : (m == 2 ? (size_t)4 * sc->nr : 0);
 }
 
 // The per-trace crop stage (k_trace_m32) keeps its M = 4nr values in shared
@@ -1098,8 +1046,8 @@ int64_t conv_splits(int64_t tstride) { return (tstride + RP_CONV_SPLIT - 1) / RP
 
 template <class Aa>
 void fast_take_pairs(Aa& a, const rp_scene* sc, const FastLayout& L) {
-    a.template take<C32>((size_t)RP_PARTS * L.nb * L.tstride * L.Wt);   // T parts
-    if (sc->dp.specular) a.template take<C32>((size_t)RP_PARTS * L.nb * L.tstride * L.Wt);   // T2 parts
+    a.template take<C32>((size_t)2 * RP_PARTS * L.nb * L.tstride * L.Wt);   // T parts (high, low)
+    if (sc->dp.specular) a.template take<C32>((size_t)2 * RP_PARTS * L.nb * L.tstride * L.Wt);   // T2 parts
     if (sc->dp.cmode == 2)        // direct sums: the facet groups' partial traces
         a.template take<double2>((size_t)L.nb * RP_DS_GROUPS * sc->nr);
     if (sc->nt1 < sc->nt) {       // ttype-0 sum, r0, scratch, group partials
@@ -1118,11 +1066,12 @@ void fast_take_pairs(Aa& a, const rp_scene* sc, const FastLayout& L) {
     }
 }
 
-FastLayout fast_layout(const rp_scene* sc, int nb, int64_t tstride, int Wt) {
+FastLayout fast_layout(const rp_scene* sc, int nb, int64_t tstride, int Wt, int64_t fstride) {
     FastLayout L;
     L.nb = nb;
     L.tstride = std::max<int64_t>(tstride, 1);
-    L.mstride = std::max<int64_t>((sc->nf + RP_CHUNK - 1) / RP_CHUNK, 1);
+    L.fstride = std::max<int64_t>(std::min<int64_t>(fstride, sc->nf), 1);
+    L.mstride = std::max<int64_t>((L.fstride + RP_CHUNK - 1) / RP_CHUNK, 1);
     L.rstride = L.mstride * RP_CHUNK;
     L.Wt = std::max(Wt, 1);
     const int M = std::max(sc->plan2.M(), sc->planN.M());
@@ -1218,17 +1167,17 @@ void sinc_poly(double T, int D, double* mono) {
     }
 }
 
-template <int KPT, int MODE, bool SPEC>
+template <int MODE, bool SPEC>
 int launch_conv_k(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, size_t csm, int sms, int slots,
                   unsigned int items, unsigned int* work, C32* gscr, size_t gslot, cudaStream_t st) {
-    if (int rc = rp_allow_dyn_smem((const void*)k_conv32s<KPT, MODE, SPEC>, csm)) return rc;
+    if (int rc = rp_allow_dyn_smem((const void*)k_conv32s<MODE, SPEC>, csm)) return rc;
     int occ = 0;
-    RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv32s<KPT, MODE, SPEC>, RP_CONV_THREADS, csm));
+    RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv32s<MODE, SPEC>, RP_CONV_THREADS, csm));
     int64_t gmax = (int64_t)std::max(occ, 1) * sms;
     if (MODE != 0) gmax = std::min<int64_t>(gmax, slots);      // one scratch slot per block
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(gmax, items));
-    k_conv32s<KPT, MODE, SPEC><<<grid, RP_CONV_THREADS, csm, st>>>(d_jobs, d_start, njobs, work,
-                                                                    reinterpret_cast<Cplx<float>*>(gscr), gslot);
+    k_conv32s<MODE, SPEC><<<grid, RP_CONV_THREADS, csm, st>>>(d_jobs, d_start, njobs, work,
+                                                              reinterpret_cast<Cplx<float>*>(gscr), gslot);
     RP_LAUNCHED();
     return RP_OK;
 }
@@ -1240,14 +1189,11 @@ template <bool SPEC>
 int launch_conv32s_t(const ConvArgs* d_jobs, const unsigned int* d_start, int njobs, int mode, int max_nr,
                      size_t csm, int sms, int slots, unsigned int items, unsigned int* work, C32* gscr,
                      size_t gslot, cudaStream_t st) {
+    (void)max_nr;
 #define RP_CONV_ARGS d_jobs, d_start, njobs, csm, sms, slots, items, work, gscr, gslot, st
-    if (mode == 1) return launch_conv_k<1, 1, SPEC>(RP_CONV_ARGS);
-    if (mode == 2) return launch_conv_k<1, 2, SPEC>(RP_CONV_ARGS);
-    const int kpt = (max_nr + RP_CONV_THREADS - 1) / RP_CONV_THREADS;
-    if (kpt <= 1) return launch_conv_k<1, 0, SPEC>(RP_CONV_ARGS);
-    if (kpt <= 2) return launch_conv_k<2, 0, SPEC>(RP_CONV_ARGS);
-    if (kpt <= 4) return launch_conv_k<4, 0, SPEC>(RP_CONV_ARGS);
-    return launch_conv_k<8, 0, SPEC>(RP_CONV_ARGS);
+    if (mode == 1) return launch_conv_k<1, SPEC>(RP_CONV_ARGS);
+    if (mode == 2) return launch_conv_k<2, SPEC>(RP_CONV_ARGS);
+    return launch_conv_k<0, SPEC>(RP_CONV_ARGS);
 #undef RP_CONV_ARGS
 }
 
@@ -1295,6 +1241,7 @@ struct Seg {
     int64_t s0 = 0;                // first row in the job's output
     int nb = 0;
     int64_t tmax = 0;
+    int64_t fmax = 0;              // illuminated-facet capacity per trace (host bound)
     void* d_out = nullptr;
     int out64 = 0;
     int64_t* h_counts = nullptr;
@@ -1315,6 +1262,8 @@ struct Seg {
     int cmode = 0;          // compression storage mode (conv_mode)
     bool pairs = false;
     C32* T = nullptr; C32* Z = nullptr; C32* cscr = nullptr; C32* part = nullptr;
+    // row elements of T (and T2); each is {high, low}, two C32
+    int64_t row_elems() const { return (int64_t)RP_PARTS * nb * L.tstride * Wt; }
     C32* T2 = nullptr;      // specular mode: outbound-leg parts
     C32* sum0 = nullptr; C32* r0 = nullptr; C32* t0scr = nullptr;   // ttype-0 targets
     double2* t0part = nullptr;
@@ -1367,15 +1316,15 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
     g.nill = a.take<int>(nb);
     g.ntl = a.take<int>(nb);
     g.vmax = a.take<unsigned long long>(nb);
-    g.idx = a.take<int>((size_t)nb * nfa);
+    g.idx = a.take<int>((size_t)nb * Lw.fstride);
     g.rec = a.take<FacetPair>((size_t)nb * Lw.rstride / 2);
     g.spec = dp.specular ? a.take<FacetSpec>((size_t)nb * Lw.rstride / 2) : nullptr;
     const bool t0 = sc->nt1 < nt;
     g.t0rec = t0 ? a.take<FacetT0>((size_t)nb * Lw.rstride / 2) : nullptr;
     g.meta = a.take<ChunkMeta>((size_t)nb * Lw.mstride);
     g.org = a.take<double>((size_t)nb * 4);
-    g.sxv = a.take<float>((size_t)nb * nfa);
-    g.sv = a.take<C32>((size_t)nb * nfa);
+    g.sxv = a.take<float>((size_t)nb * Lw.fstride);
+    g.sv = a.take<C32>((size_t)nb * Lw.fstride);
     g.tm = a.take<TraceMeta>(nb);
     g.tflags = a.take<uint8_t>((size_t)nb * nta);
     g.ntl1 = t0 ? a.take<int>(nb) : g.ntl;
@@ -1393,15 +1342,16 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
         k_cull_count<<<dim3((unsigned)((nf + RP_TILE - 1) / RP_TILE), nb), RP_TILE_THREADS, 0, st>>>(
             sc->d_sorted, nf, trb, dp.ap_rad, g.fflags, g.tcnt, reinterpret_cast<const double4*>(sc->d_tiles_sorted));
         RP_LAUNCHED();
-        compact_flags(g.fflags, nf, nb, g.tcnt, g.nill, g.idx, nfa, true, st);
+        compact_flags(g.fflags, nf, nb, g.tcnt, g.nill, g.idx, Lw.fstride, true, st, g.misc + 6);
         auto kf = dp.specular ? (t0 ? k_facets32<true, true> : k_facets32<true, false>)
                               : (t0 ? k_facets32<false, true> : k_facets32<false, false>);
         kf<<<dim3((unsigned)Lw.mstride, nb), RP_CHUNK, 0, st>>>(
-            sc->d_sorted, nfa, g.idx, g.nill, trb, dp, g.rec, g.meta, Lw.rstride, Lw.mstride, g.sxv, g.sv, g.vmax,
+            sc->d_sorted, nfa, Lw.fstride, g.idx, g.nill, trb, dp, g.rec, g.meta, Lw.rstride, Lw.mstride, g.sxv, g.sv,
+            g.vmax,
             g.org, sc->d_order, g.spec, g.t0rec);
         RP_LAUNCHED();
-        k_surf_fix32<<<dim3((unsigned)((nf + 256 * RP_SFIX_PER - 1) / (256 * RP_SFIX_PER)), nb), 256, 0, st>>>(
-            nfa, g.nill, g.sxv, g.sv, g.vmax, nr, g.acc, dp.specular);
+        k_surf_fix32<<<dim3((unsigned)((Lw.fstride + 256 * RP_SFIX_PER - 1) / (256 * RP_SFIX_PER)), nb), 256, 0,
+                       st>>>(Lw.fstride, g.nill, g.sxv, g.sv, g.vmax, nr, g.acc, dp.specular);
         RP_LAUNCHED();
         k_tmeta32<<<nb, 256, 0, st>>>(g.meta, Lw.mstride, g.nill, g.tm);
         RP_LAUNCHED();
@@ -1412,7 +1362,7 @@ void seg_setup(Seg& g, Arena& a, cudaStream_t st) {
         k_target_flags<<<dim3((unsigned)((nt + 255) / 256), nb), 256, 0, st>>>(sc->d_targets_fast, nt, trb,
                                                                             dp.ap_rad, g.tflags);
         RP_LAUNCHED();
-        compact_flags(g.tflags, nt, nb, g.tcnt, g.ntl, g.tlist, Lw.tstride, false, st);
+        compact_flags(g.tflags, nt, nb, g.tcnt, g.ntl, g.tlist, Lw.tstride, false, st, g.misc + 6);
         if (t0) {
             k_ntl1<<<(nb + 63) / 64, 64, 0, st>>>(g.tlist, g.ntl, Lw.tstride, sc->nt1, nb, g.ntl1);
             RP_LAUNCHED();
@@ -1440,6 +1390,8 @@ PairArgs seg_pair_args(const Seg& g) {
     P.tblocks = (int)((g.L.tstride + RP_PAIR_THREADS - 1) / RP_PAIR_THREADS);
     P.work = reinterpret_cast<unsigned int*>(g.misc + 1);
     P.err = reinterpret_cast<unsigned int*>(g.misc + 2);
+    P.spin_limit = sc->spin_limit;
+    P.stall_copies = sc->stall_copies;
     P.nr_f = (float)nr; P.nr = nr; P.nr1 = nr - 1;
     P.kb = (float)(dp.nidx / dp.dr);
     P.kt = (float)(dp.nidx * dp.turn);
@@ -1573,8 +1525,8 @@ int launch_pairs(const std::vector<Seg*>& ps, const PairJob* d_jobs, const PairJ
 // Zero the pair-stage outputs of a wave (T windows, work counters, flags).
 int zero_pairs(const std::vector<Seg*>& ps, unsigned int* d_work, unsigned int* seg_work, cudaStream_t st) {
     for (const Seg* g : ps) {
-        RP_CUDA(cudaMemsetAsync(g->T, 0, sizeof(C32) * RP_PARTS * g->nb * g->L.tstride * g->Wt, st));
-        if (g->T2) RP_CUDA(cudaMemsetAsync(g->T2, 0, sizeof(C32) * RP_PARTS * g->nb * g->L.tstride * g->Wt, st));
+        RP_CUDA(cudaMemsetAsync(g->T, 0, sizeof(C32) * 2 * g->row_elems(), st));
+        if (g->T2) RP_CUDA(cudaMemsetAsync(g->T2, 0, sizeof(C32) * 2 * g->row_elems(), st));
         RP_CUDA(cudaMemsetAsync(g->misc + 1, 0, sizeof(int) * 3, st));
     }
     RP_CUDA(cudaMemsetAsync(d_work, 0, sizeof(unsigned int), st));
@@ -1595,7 +1547,8 @@ int choose_cfg(const std::vector<Seg*>& ps, const PairJob* d_jobs, const PairJob
     const int multi = spec ? 2 : (ps.size() > 1 ? 1 : 0);
     const int deg = multi == 1 ? -1 : ps[0]->deg;
     const int ncfg = spec ? 2 : (multi == 1 ? 10 : 4);
-    if (!autotune_on()) {
+    // a scene in the stalled-copy test mode never tunes: its launches time out
+    if (!autotune_on() || ps[0]->sc->stall_copies) {
         const int c = ps[0]->sc->pair_cfg;
         *cfg_out = spec ? (c & 1) : (multi == 1 ? c : (c & 3));
         return RP_OK;
@@ -1656,13 +1609,18 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     g_timer.mark(1, st);
     RP_CUDA(cudaStreamSynchronize(st));
     g_timer.collect(0, 1);
+    for (int i = 0; i < nseg; ++i)
+        if (h_misc[8 * i + 6]) {
+            rp_set_error("fast form: an illuminated-facet or target list exceeded its capacity");
+            return RP_ERR_INTERNAL;
+        }
     // ---- pair-stage buffers and job tables
     std::vector<Seg*> ps, cs[3];
     size_t gslot[3] = {0, 0, 0};
     for (int i = 0; i < nseg; ++i) {
         Seg& g = segs[i];
         g.Wt = std::max(1, std::min(g.sc->nr, (h_misc[8 * i] + 3) & ~3));
-        g.L = fast_layout(g.sc, g.nb, g.tmax, g.Wt);
+        g.L = fast_layout(g.sc, g.nb, g.tmax, g.Wt, g.fmax);
         g.cmode = conv_mode(g.sc);
         g.nsplit = (int)conv_splits(g.L.tstride);
         // specular mode without convolution has no pair or compression
@@ -1687,8 +1645,8 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     Arena& b = ws->arena2;
     b.reset();
     for (Seg& g : segs) {
-        g.T = b.take<C32>((size_t)RP_PARTS * g.nb * g.L.tstride * g.Wt);
-        g.T2 = g.sc->dp.specular ? b.take<C32>((size_t)RP_PARTS * g.nb * g.L.tstride * g.Wt) : nullptr;
+        g.T = b.take<C32>((size_t)2 * RP_PARTS * g.nb * g.L.tstride * g.Wt);
+        g.T2 = g.sc->dp.specular ? b.take<C32>((size_t)2 * RP_PARTS * g.nb * g.L.tstride * g.Wt) : nullptr;
         g.dpart = g.sc->dp.cmode == 2 ? b.take<double2>((size_t)g.nb * RP_DS_GROUPS * g.sc->nr) : nullptr;
         if (g.t0rec) {
             g.sum0 = b.take<C32>((size_t)g.nb * g.sc->nr);
@@ -1718,8 +1676,8 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     }
     RP_CUDA(cudaMemsetAsync(d_work, 0, sizeof(unsigned int) * (4 + 2 * nseg), st));
     for (Seg& g : segs) {
-        RP_CUDA(cudaMemsetAsync(g.T, 0, sizeof(C32) * RP_PARTS * g.nb * g.L.tstride * g.Wt, st));
-        if (g.T2) RP_CUDA(cudaMemsetAsync(g.T2, 0, sizeof(C32) * RP_PARTS * g.nb * g.L.tstride * g.Wt, st));
+        RP_CUDA(cudaMemsetAsync(g.T, 0, sizeof(C32) * 2 * g.row_elems(), st));
+        if (g.T2) RP_CUDA(cudaMemsetAsync(g.T2, 0, sizeof(C32) * 2 * g.row_elems(), st));
     }
     std::vector<PairJob> hp;
     std::vector<unsigned int> hps(1, 0u);
@@ -1808,7 +1766,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         if (g.dpart) {          // specular mode without convolution
             DirectArgs D;
             const DevParams& dp = sc->dp;
-            D.F = sc->d_sorted; D.nf = std::max<int64_t>(sc->nf, 1); D.idx = g.idx; D.nill = g.nill; D.traces = g.trb;
+            D.F = sc->d_sorted; D.nf = std::max<int64_t>(sc->nf, 1); D.fstride = g.Lw.fstride; D.idx = g.idx; D.nill = g.nill; D.traces = g.trb;
             D.TG = sc->d_targets_fast; D.nt = sc->nt; D.tlist = g.tlist; D.ntl = g.ntl; D.tstride = g.Lw.tstride;
             D.sv = g.sv; D.spec = g.spec; D.t0rec = g.t0rec; D.rstride = g.Lw.rstride;
             D.PR = sc->d_prisms; D.np = sc->np; D.nr = nr;
@@ -1939,26 +1897,100 @@ std::vector<int> host_target_bounds(const rp_scene* sc, const double* tr, int64_
     return ub;
 }
 
+// An upper bound of each trace's illuminated-facet count: the facets of the
+// culling tiles whose bounding sphere is not wholly outside the aperture
+// cone.  The test is the culling kernel's (tile_outside) with a margin of
+// 1e-6 rad instead of 1e-9, so every tile the device keeps is counted here
+// and the bound holds whatever the last-ulp differences of acos and asin
+// between host and device.  It sizes the per-trace facet buffers (the
+// illuminated list, the facet-pair records, the surface phasors) to the
+// aperture's footprint instead of the whole store.  With wb, also a bound
+// of each trace's target-window width for planning: k_tsetup32's window of a
+// target spans (xmax - xmin) + kb (dmax - dmin) bins over the illuminated
+// facets' bounding box, at most diag (1 + max(n, c1/c2)) / dr for the
+// box's diagonal, here the diagonal of the kept tiles' box (plus margin).
+std::vector<int64_t> host_facet_bounds(const rp_scene* sc, const double* tr, int64_t ns,
+                                       std::vector<int>* wb = nullptr) {
+    const int64_t nf = sc->nf;
+    std::vector<int64_t> fb(ns, nf);
+    if (wb) wb->assign(ns, sc->nr);
+    const std::vector<double>& ts = sc->h_tiles_sorted;
+    const int64_t ntl = (int64_t)ts.size() / 4;
+    if (nf == 0 || ntl * RP_CULL_TILE < nf) return fb;
+    const double ap = sc->dp.ap_rad;
+    const double kw = (1.0 + std::max(sc->dp.nidx, sc->dp.c1_over_c2)) / sc->dp.dr;
+    auto count = [&](int64_t s) {
+        const double* r = tr + 9 * s;
+        int64_t c = 0;
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int64_t t = 0; t < ntl; ++t) {
+            const double* q = &ts[4 * t];
+            const double vx = q[0] - r[0], vy = q[1] - r[1], vz = q[2] - r[2];
+            const double d = std::sqrt(vx * vx + vy * vy + vz * vz);
+            bool outside = false;
+            if (d > q[3]) {
+                const double cs = std::max(-1.0, std::min(1.0, -(vx * r[3] + vy * r[4] + vz * r[5]) / d));
+                outside = std::acos(cs) - std::asin(q[3] / d) > ap + 1e-6;
+            }
+            if (!outside) {
+                c += std::min<int64_t>(RP_CULL_TILE, nf - t * RP_CULL_TILE);
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = std::min(lo[a], q[a] - q[3]);
+                    hi[a] = std::max(hi[a], q[a] + q[3]);
+                }
+            }
+        }
+        fb[s] = c;
+        if (wb && c > 0) {
+            double d2 = 0.0;
+            for (int a = 0; a < 3; ++a) d2 += (hi[a] - lo[a]) * (hi[a] - lo[a]);
+            const double w = std::ceil(std::sqrt(d2) * kw) + 8.0;
+            (*wb)[s] = (int)std::min<double>((double)sc->nr, std::max(1.0, w));
+        }
+    };
+    const int64_t work = ns * ntl;
+    const int nth = (int)std::min<int64_t>(std::min<int64_t>(ns, 16), std::max<int64_t>(1, work / 50000));
+    if (nth <= 1) {
+        for (int64_t s = 0; s < ns; ++s) count(s);
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nth; ++t)
+            th.emplace_back([&, t] {
+                for (int64_t s = t; s < ns; s += nth) count(s);
+            });
+        for (auto& x : th) x.join();
+    }
+    return fb;
+}
+
 // Size the next segment of a scene's traces starting at s0: up to 64 traces
-// whose scratch (target windows bounded by nr) fits the budget.
-void next_segment(const rp_scene* sc, const std::vector<int>& ub, int64_t s0, int64_t ns, int* nb_out,
-                  int64_t* tmax_out, size_t* bytes_out) {
+// whose scratch (target windows bounded by nr, facet buffers by the traces'
+// facet bounds fb) fits the budget.
+void next_segment(const rp_scene* sc, const std::vector<int>& ub, const std::vector<int64_t>& fb,
+                  const std::vector<int>& wb, int64_t s0, int64_t ns, int* nb_out, int64_t* tmax_out,
+                  int64_t* fmax_out, size_t* bytes_out) {
     int nb = 0;
-    int64_t tmax = 0;
+    int64_t tmax = 0, fmax = 0;
+    int wmax = 1;
     size_t bytes = 0;
     for (;;) {
         if (s0 + nb >= ns) break;
         const int64_t t2 = std::max<int64_t>(tmax, ub[s0 + nb]);
-        const FastLayout L = fast_layout(sc, nb + 1, t2, sc->nr);
+        const int64_t f2 = std::max<int64_t>(fmax, fb[s0 + nb]);
+        const int w2 = std::max(wmax, wb[s0 + nb]);
+        const FastLayout L = fast_layout(sc, nb + 1, t2, w2, f2);
         const size_t b2 = seg_setup_bytes(sc, L) + seg_pair_bytes(sc, L);
         if (nb > 0 && b2 > kFastBudget) break;
         tmax = t2;
+        fmax = f2;
+        wmax = w2;
         bytes = b2;
         ++nb;
         if (nb >= 64) break;
     }
     *nb_out = nb;
     *tmax_out = tmax;
+    *fmax_out = fmax;
     *bytes_out = bytes;
 }
 
@@ -1977,12 +2009,14 @@ int check_scene(const rp_scene* sc) {
 // target of the scene).
 size_t rp_fast_plan_bytes(const rp_scene* sc, const double* h_traces, int64_t ns) {
     std::vector<int> ub = h_traces ? host_target_bounds(sc, h_traces, ns) : std::vector<int>(ns, (int)sc->nt);
+    std::vector<int> wb(ns, sc->nr);
+    std::vector<int64_t> fb = h_traces ? host_facet_bounds(sc, h_traces, ns, &wb) : std::vector<int64_t>(ns, sc->nf);
     size_t peak = 0, wave = 0;
     for (int64_t s0 = 0; s0 < ns;) {
         int nb;
-        int64_t tmax;
+        int64_t tmax, fmax;
         size_t bytes;
-        next_segment(sc, ub, s0, ns, &nb, &tmax, &bytes);
+        next_segment(sc, ub, fb, wb, s0, ns, &nb, &tmax, &fmax, &bytes);
         if (wave > 0 && (sc->dp.specular || wave + bytes > kFastBudget)) {     // specular: one segment a wave
             peak = std::max(peak, wave);
             wave = 0;
@@ -2017,11 +2051,13 @@ int rp_fast_batch(const rp_job* jobs, int njobs, rp_workspace* ws, cudaStream_t 
         const int64_t ns = jobs[j].ns;
         const int nr = sc->nr;
         std::vector<int> ub = host_target_bounds(sc, tr[j].data(), ns);
+        std::vector<int> wb;
+        std::vector<int64_t> fb = host_facet_bounds(sc, tr[j].data(), ns, &wb);
         for (int64_t s0 = 0; s0 < ns;) {
             int nb;
-            int64_t tmax;
+            int64_t tmax, fmax;
             size_t bytes;
-            next_segment(sc, ub, s0, ns, &nb, &tmax, &bytes);
+            next_segment(sc, ub, fb, wb, s0, ns, &nb, &tmax, &fmax, &bytes);
             // a specular segment runs in a wave of its own (k_pairs32s is a
             // single-batch kernel)
             const bool alone = sc->dp.specular || (!wave.empty() && wave[0].sc->dp.specular);
@@ -2037,13 +2073,14 @@ int rp_fast_batch(const rp_job* jobs, int njobs, rp_workspace* ws, cudaStream_t 
             g.s0 = s0;
             g.nb = nb;
             g.tmax = tmax;
+            g.fmax = fmax;
             g.d_out = jobs[j].d_out;
             g.out64 = 0;
             g.h_counts = jobs[j].counts;
             g.deg = kc[j].deg;
             g.coef = kc[j].coef;
             g.coefr = kc[j].coefr;
-            g.Lw = fast_layout(sc, nb, tmax, nr);
+            g.Lw = fast_layout(sc, nb, tmax, nr, fmax);
             wave.push_back(g);
             wave_bytes += bytes;
             s0 += nb;
@@ -2069,17 +2106,19 @@ int rp_fast_run(rp_scene* sc, rp_workspace* ws, const double* d_traces, int64_t 
     RP_CUDA(cudaMemcpyAsync(tr.data(), d_traces, sizeof(double) * 9 * ns, cudaMemcpyDeviceToHost, st));
     RP_CUDA(cudaStreamSynchronize(st));
     std::vector<int> ub = host_target_bounds(sc, tr.data(), ns);
+    std::vector<int> wb;
+    std::vector<int64_t> fb = host_facet_bounds(sc, tr.data(), ns, &wb);
     const SceneConst kc = scene_const(sc);
     for (int64_t s0 = 0; s0 < ns;) {
         int nb;
-        int64_t tmax;
+        int64_t tmax, fmax;
         size_t bytes;
-        next_segment(sc, ub, s0, ns, &nb, &tmax, &bytes);
+        next_segment(sc, ub, fb, wb, s0, ns, &nb, &tmax, &fmax, &bytes);
         std::vector<Seg> w(1);
         Seg& g = w[0];
-        g.sc = sc; g.trb = d_traces + 9 * s0; g.s0 = s0; g.nb = nb; g.tmax = tmax;
+        g.sc = sc; g.trb = d_traces + 9 * s0; g.s0 = s0; g.nb = nb; g.tmax = tmax; g.fmax = fmax;
         g.d_out = d_out; g.out64 = 1; g.h_counts = h_counts; g.deg = kc.deg; g.coef = kc.coef; g.coefr = kc.coefr;
-        g.Lw = fast_layout(sc, nb, tmax, sc->nr);
+        g.Lw = fast_layout(sc, nb, tmax, sc->nr, fmax);
         rc = run_wave(w, ws, st);
         if (rc) return rc;
         s0 += nb;

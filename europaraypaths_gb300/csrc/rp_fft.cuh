@@ -214,24 +214,47 @@ __device__ __forceinline__ Cplx<T> tw_sfu(int j, float step) {   // e^{-i j step
     return Cplx<T>{(T)cs, (T)-sn};
 }
 
+// The two radix-4 DIF stages of spans L and L/4 on one group's 16 elements
+// in registers: x[i] = a[base + i S], S = L / 16, b = base mod S.
 template <class T>
-__device__ __forceinline__ void block_dif_s(Cplx<T>* a, int n) {
-    const int m = fft_log2(n);
-    int L = n, lL = m;
+__device__ __forceinline__ void dif16_regs(Cplx<T> (&x)[16], int b, int L) {
+    const int S = L >> 4;
+    const float st1 = 6.28318530717958647f / (float)L, st2 = 4.f * st1;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r4_dif_reg(x[i], x[i + 4], x[i + 8], x[i + 12], tw_sfu<T>(b + i * S, st1));
+    const Cplx<T> w = tw_sfu<T>(b, st2);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) r4_dif_reg(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3], w);
+}
+
+// The two radix-4 DIT stages of spans L and 4L on one group's 16 elements in
+// registers: x[i] = a[base + i S], S = L / 4, b = base mod S.
+template <class T>
+__device__ __forceinline__ void dit16_regs(Cplx<T> (&x)[16], int b, int L) {
+    const int S = L >> 2;
+    const float st1 = 6.28318530717958647f / (float)L, st2 = 0.25f * st1;
+    const Cplx<T> w = tw_sfu<T>(b, st1);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) r4_dit_reg(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3], w);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) r4_dit_reg(x[k], x[k + 4], x[k + 8], x[k + 12], tw_sfu<T>(b + k * S, st2));
+}
+
+// DIF stages from span L0 down (L0 = n: the whole transform; L0 = n / 16:
+// all but the first fused pass, which a caller ran on its own registers).
+// Ends with a barrier.
+template <class T>
+__device__ __forceinline__ void block_dif_s_from(Cplx<T>* a, int n, int L0) {
+    int L = L0, lL = fft_log2(L0);
     for (; L >= 16; L >>= 4, lL -= 4) {
         const int lS = lL - 4, S = 1 << lS;
-        const float st1 = 6.28318530717958647f / (float)L, st2 = 4.f * st1;
         for (int g = threadIdx.x; g < (n >> 4); g += blockDim.x) {
             const int b = g & (S - 1);
             const int base = (g >> lS) * L + b;
             Cplx<T> x[16];
 #pragma unroll
             for (int i = 0; i < 16; ++i) x[i] = a[swz(base + i * S)];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) r4_dif_reg(x[i], x[i + 4], x[i + 8], x[i + 12], tw_sfu<T>(b + i * S, st1));
-            const Cplx<T> w = tw_sfu<T>(b, st2);
-#pragma unroll
-            for (int c = 0; c < 4; ++c) r4_dif_reg(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3], w);
+            dif16_regs(x, b, L);
 #pragma unroll
             for (int i = 0; i < 16; ++i) a[swz(base + i * S)] = x[i];
         }
@@ -261,7 +284,14 @@ __device__ __forceinline__ void block_dif_s(Cplx<T>* a, int n) {
 }
 
 template <class T>
-__device__ __forceinline__ void block_dit_s(Cplx<T>* a, int n) {
+__device__ __forceinline__ void block_dif_s(Cplx<T>* a, int n) { block_dif_s_from(a, n, n); }
+
+// DIT stages up to the fused passes of span <= Lmax (Lmax = n / 4: the whole
+// transform; Lmax = n / 16: all but the last fused pass, spans n / 4 and n,
+// which a caller runs on its own registers).  Ends with a barrier when it
+// ran any stage.
+template <class T>
+__device__ __forceinline__ void block_dit_s_upto(Cplx<T>* a, int n, int Lmax) {
     const int m = fft_log2(n);
     int L, lL;
     if (m & 1) {
@@ -289,24 +319,22 @@ __device__ __forceinline__ void block_dit_s(Cplx<T>* a, int n) {
         L <<= 2;
         lL += 2;
     }
-    for (; L <= n / 4; L <<= 4, lL += 4) {
+    for (; L <= Lmax; L <<= 4, lL += 4) {
         const int lS = lL - 2, S = 1 << lS;
-        const float st1 = 6.28318530717958647f / (float)L, st2 = 0.25f * st1;
         for (int g = threadIdx.x; g < (n >> 4); g += blockDim.x) {
             const int b = g & (S - 1);
             const int base = (g >> lS) * (4 * L) + b;
             Cplx<T> x[16];
 #pragma unroll
             for (int i = 0; i < 16; ++i) x[i] = a[swz(base + i * S)];
-            const Cplx<T> w = tw_sfu<T>(b, st1);
-#pragma unroll
-            for (int c = 0; c < 4; ++c) r4_dit_reg(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3], w);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) r4_dit_reg(x[k], x[k + 4], x[k + 8], x[k + 12], tw_sfu<T>(b + k * S, st2));
+            dit16_regs(x, b, L);
 #pragma unroll
             for (int i = 0; i < 16; ++i) a[swz(base + i * S)] = x[i];
         }
         __syncthreads();
     }
 }
+
+template <class T>
+__device__ __forceinline__ void block_dit_s(Cplx<T>* a, int n) { block_dit_s_upto(a, n, n / 4); }
 #endif

@@ -20,6 +20,11 @@
 // Fixed-point scale headroom for deterministic integer accumulation.
 #define RP_FIX_BITS 60
 
+// Polls of an mbarrier before a pair kernel's wait for a staged chunk gives
+// up (RP_ERR_TIMEOUT), and the short limit of the stalled-copy test mode.
+#define RP_SPIN_LIMIT (1 << 22)
+#define RP_SPIN_LIMIT_TEST 4096
+
 void rp_set_error(const char* fmt, ...);
 #define RP_CULL_TILE 1024   // facets per compaction tile and per culling sphere
 
@@ -127,6 +132,7 @@ struct rp_scene {
     // ---- fast store: spatially sorted facets
     int64_t* d_order = nullptr;          // sorted position -> original index
     double* d_tiles_sorted = nullptr;    // per RP_CULL_TILE sorted facets: bounding sphere (x, y, z, r)
+    std::vector<double> h_tiles_sorted;  // the same on the host (per-trace facet bounds)
     double* d_tiles_file = nullptr;      // the same for the input-order store
     double* d_sorted = nullptr;          // FP64 SoA [12][nf] in sorted order
     // ---- per-scene spectral tables
@@ -151,6 +157,9 @@ struct rp_scene {
     int ortho = 0;                       // every facet frame (n, u, v) orthonormal to 1e-5
     int pair_variant = 0;                // 0 auto (polynomial sinc where accurate), 1 special-function sinc
     int pair_cfg = 1;                    // pair-kernel (ILP, blocks/SM) configuration (1: 2 x 2)
+    int spin_limit = RP_SPIN_LIMIT;      // polls of a pair kernel's chunk wait before it gives up
+    int stall_copies = 0;                // test mode (RP_TEST_STALL_COPIES): the pair kernels issue
+                                         // no bulk copy, so their first wait runs out (short limit)
     // ---- the scene's own workspace (rp_simulate / rp_simulate_device)
     rp_workspace ws;
     cudaStream_t own_stream = nullptr;

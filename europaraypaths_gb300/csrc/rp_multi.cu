@@ -43,23 +43,25 @@ k_pairs32m(const PairJob* __restrict__ jobs, const unsigned int* __restrict__ st
         const int part = li % RP_PARTS;
         const int tb = (li / RP_PARTS) % A.tblocks;
         const int s = li / (RP_PARTS * A.tblocks);
+        bool ok;
         if (ortho) {
             switch (deg) {
-                case 3: pair_item<3, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
-                case 4: pair_item<4, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
-                case 5: pair_item<5, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
-                case 6: pair_item<6, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
-                default: pair_item<0, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                case 3: ok = pair_item<3, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                case 4: ok = pair_item<4, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                case 5: ok = pair_item<5, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                case 6: ok = pair_item<6, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                default: ok = pair_item<0, ILP, true, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
             }
         } else {
             switch (deg) {
-                case 3: pair_item<3, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
-                case 4: pair_item<4, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
-                case 5: pair_item<5, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
-                case 6: pair_item<6, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
-                default: pair_item<0, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                case 3: ok = pair_item<3, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                case 4: ok = pair_item<4, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                case 5: ok = pair_item<5, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                case 6: ok = pair_item<6, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
+                default: ok = pair_item<0, ILP, false, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase); break;
             }
         }
+        if (!ok) break;
     }
     RP_PAIR_SMEM_END
 }
@@ -87,7 +89,7 @@ k_pairs32mk(const __grid_constant__ PairJobTable T, unsigned int* work) {
         const int part = item % RP_PARTS;
         const int tb = (item / RP_PARTS) % A.tblocks;
         const int s = item / (RP_PARTS * A.tblocks);
-        pair_item<NT, ILP, ORTHO, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase);
+        if (!pair_item<NT, ILP, ORTHO, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase)) break;
     }
     RP_PAIR_SMEM_END
 }

@@ -22,7 +22,6 @@
 #define RP_WIN_WIDE 24        // the default-mode and ttype-0 kernels' window: a 256-facet chunk of
                               // 2.5 m facets at 12.5 m bins spans up to ~14 bins for one target
 #define RP_PARTS 4            // facet-range splits per (trace, target block)
-#define RP_SPIN_LIMIT (1 << 22)
 
 namespace rpk {
 
@@ -122,9 +121,10 @@ __device__ __forceinline__ void tma_bulk_g2s(void* dst, const void* src, uint32_
         : "memory");
 }
 
-// Bounded wait on an mbarrier phase; returns false if the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
-    for (int it = 0; it < RP_SPIN_LIMIT; ++it) {
+// Bounded wait on an mbarrier phase: at most `limit` polls; returns false if
+// the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, int limit) {
+    for (int it = 0; it < limit; ++it) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
@@ -152,12 +152,14 @@ struct PairArgs {
     const double* PR;   // prisms (alpha, box) FP64 SoA
     int64_t np;
     const int* bt0;
-    C32* T;             // [RP_PARTS][nb][tstride][Wt]
+    C32* T;             // [RP_PARTS][nb][tstride][Wt] row elements, each {high, low} (two C32)
     int Wt;
     int nb;
     int tblocks;        // target blocks per trace
     unsigned int* work; // work counter
     unsigned int* err;  // error flags: [0] window overflow, [1] wait timeout
+    int spin_limit;     // polls of a chunk's mbarrier before the wait gives up
+    int stall_copies;   // test mode: no bulk copy is issued, so every wait runs out
     // constants
     float nr_f;
     int nr;
@@ -492,8 +494,38 @@ static __device__ __noinline__ float prism_factor(float4 ra, double cx, double c
     return exp2f(-ealpha * (float)tot - 2.f * 1.44269504f * (float)ex);
 }
 
+// Knuth's TwoSum: s = fl(a + b) and its exact rounding error e (a + b = s + e
+// exactly); the _rn intrinsics keep the compiler from contracting or
+// reordering it.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fadd_rn(s, -a);
+    e = __fadd_rn(__fadd_rn(a, -__fadd_rn(s, -bb)), __fadd_rn(b, -bb));
+}
+
+// Compensated (Kahan-Babuska) accumulation into a target row element: the
+// element is {high, low}, one 16-byte word (two C32 at Trow[2 o],
+// Trow[2 o + 1]); each add rounds into the high part and its exact rounding
+// error goes into the low part, so high + low carries the sum of every flush
+// to about FP32 precision of the sum, however many chunks flush into it.
+// Readers take high + low.
+__device__ __forceinline__ float4 comp_add(float4 t, float vre, float vim) {
+    float s, e;
+    two_sum(t.x, vre, s, e);
+    t.x = s;
+    t.z = __fadd_rn(t.z, e);
+    two_sum(t.y, vim, s, e);
+    t.y = s;
+    t.w = __fadd_rn(t.w, e);
+    return t;
+}
+__device__ __forceinline__ void comp_add_row(C32* Trow, int o, float vre, float vim) {
+    float4* p = reinterpret_cast<float4*>(Trow) + o;
+    *p = comp_add(*p, vre, vim);
+}
+
 // Add one phasor into the thread's window (or, outside it, directly into the
-// thread's own trace row).  Bin and weight follow the reference's two-bin
+// thread's own trace row, compensated).  Bin and weight follow the reference's two-bin
 // split: b = (short)x (truncation), w = x - b (radar_kernels.cu:736-760).
 // floor(xr) comes from rounding xr - 1/2 with the 1.5 * 2^23 magic number
 // (an exact half rounds either way; the split is continuous there, so both
@@ -529,19 +561,13 @@ static __device__ __noinline__ void bin_add_edge(int b, float w, float vre, floa
     }
     const int o0 = b - b0;
     if (o0 >= 0 && o0 < Wt) {
-        C32 t0 = Trow[o0];
-        t0.x = fmaf(vre, w0, t0.x);
-        t0.y = fmaf(vim, w0, t0.y);
-        Trow[o0] = t0;
+        comp_add_row(Trow, o0, vre * w0, vim * w0);
     } else {
         atomicOr(err, 1u);
     }
     if (two) {
         if (o0 + 1 >= 0 && o0 + 1 < Wt) {
-            C32 t1 = Trow[o0 + 1];
-            t1.x = fmaf(vre, w, t1.x);
-            t1.y = fmaf(vim, w, t1.y);
-            Trow[o0 + 1] = t1;
+            comp_add_row(Trow, o0 + 1, vre * w, vim * w);
         } else {
             atomicOr(err, 1u);
         }
@@ -685,43 +711,41 @@ __device__ __forceinline__ void bin_add1(float xr, float vre, float vim, int blo
     }
     const int o = b - b0;
     if (o >= 0 && o < A.Wt) {
-        C32 t0 = Trow[o];
-        t0.x += vre;
-        t0.y += vim;
-        Trow[o] = t0;
+        comp_add_row(Trow, o, vre, vim);
     } else {
         atomicOr(A.err, 1u);
     }
 }
 
 // Flush a thread's bin window into its target's row: each non-zero bin adds
-// to the row element it covers (outside the row: the window-overflow flag).
-// In groups of 8 bins, every row load of a group is issued before its first
-// add, so the read-modify-writes overlap instead of waiting on one another.
+// to the row element it covers, compensated (comp_add: the rounding error of
+// the add goes into the element's low part); outside the row: the
+// window-overflow flag.  In groups of 8 bins, every row load of a group
+// (high and low parts) is issued before its first add, so the
+// read-modify-writes overlap instead of waiting on one another.
 template <int W>
 __device__ __forceinline__ void flush_window(const float2* win, int tid, int blo, int b0, C32* Trow, int Wt,
                                              unsigned int* err) {
     static_assert(W % 8 == 0, "windows flush in groups of 8 bins");
+    float4* const R = reinterpret_cast<float4*>(Trow);
 #pragma unroll
     for (int g = 0; g < W; g += 8) {
         float2 v[8];
-        C32 t[8];
+        float4 t[8];
 #pragma unroll
         for (int w = 0; w < 8; ++w) v[w] = win[(g + w) * RP_PAIR_THREADS + tid];
 #pragma unroll
         for (int w = 0; w < 8; ++w) {
             const int o = blo + g + w - b0;
             const bool nz = v[w].x != 0.f || v[w].y != 0.f;
-            t[w] = (nz && o >= 0 && o < Wt) ? Trow[o] : C32{0.f, 0.f};
+            t[w] = (nz && o >= 0 && o < Wt) ? R[o] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
         for (int w = 0; w < 8; ++w) {
             if (v[w].x != 0.f || v[w].y != 0.f) {
                 const int o = blo + g + w - b0;
                 if (o >= 0 && o < Wt) {
-                    t[w].x += v[w].x;
-                    t[w].y += v[w].y;
-                    Trow[o] = t[w];
+                    R[o] = comp_add(t[w], v[w].x, v[w].y);
                 } else {
                     atomicOr(err, 1u);
                 }
@@ -731,13 +755,8 @@ __device__ __forceinline__ void flush_window(const float2* win, int tid, int blo
 }
 
 // ------------------------------------------------ double-float anchors --
-// Error-free transformations (Knuth TwoSum, FMA TwoProduct); the _rn
-// intrinsics keep the compiler from contracting or reordering them.
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-    s = __fadd_rn(a, b);
-    const float bb = __fadd_rn(s, -a);
-    e = __fadd_rn(__fadd_rn(a, -__fadd_rn(s, -bb)), __fadd_rn(b, -bb));
-}
+// Error-free transformation (FMA TwoProduct; TwoSum is above); the _rn
+// intrinsics keep the compiler from contracting it.
 __device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
     p = __fmul_rn(a, b);
     e = __fmaf_rn(a, b, -p);
@@ -812,8 +831,28 @@ __host__ __device__ constexpr size_t pair_smem_bytes(int W) { return pair_meta_o
 static_assert(RP_PAIR_SPEC_OFF % 16 == 0, "FacetSpec chunks are staged by bulk copies");
 static_assert(pair_smem_bytes(RP_WIN_WIDE) % 16 == 0, "FacetT0 chunks are staged by bulk copies");
 
+// A wait on a chunk's staged copy that ran out ends the block's work.  The
+// thread whose wait ran out skips the chunk (it never reads the unfilled
+// buffer); the chunk's trailing barrier tells every thread (a reduction in
+// place of the plain barrier, so the common path keeps one barrier per
+// chunk); then thread 0 raises the timeout flag (RP_ERR_TIMEOUT on the host)
+// and waits, again bounded, for the copies the block still has in flight,
+// and the block stops taking work.
+__device__ __forceinline__ void abort_block(const PairArgs& A, uint64_t* bars, const uint32_t* phase, int buf,
+                                            bool got, bool next_issued) {
+    if (threadIdx.x == 0) {
+        atomicOr(A.err + 1, 1u);
+        if (!A.stall_copies) {
+            if (!got) mbar_wait(&bars[buf], phase[buf], A.spin_limit);
+            if (next_issued) mbar_wait(&bars[buf ^ 1], phase[buf ^ 1], A.spin_limit);
+        }
+    }
+}
+
+// One work item of the pair kernels; false when a chunk's wait ran out (the
+// kernel then stops taking items).
 template <int NT, int ILP, bool ORTHO, bool SPEC, int W, class PA>
-__device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, uint64_t* bars, uint32_t* phase) {
+__device__ __forceinline__ bool pair_item(const PA& A, int s, int tb, int part, uint64_t* bars, uint32_t* phase) {
     static_assert(!SPEC || W == RP_WIN, "the specular layout holds two RP_WIN windows");
     // every hot shared array is derived here from the shared symbol itself
     FacetPair* srec = reinterpret_cast<FacetPair*>(pair_smem);                     // [2][RP_CHUNK_PAIRS]
@@ -829,11 +868,11 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
     const int tid = threadIdx.x;
     const int nq = A.ntl[s];
     const int n = A.nill[s];
-    if (tb * RP_PAIR_THREADS >= nq || n == 0) return;
+    if (tb * RP_PAIR_THREADS >= nq || n == 0) return true;
     const int nchunks = (n + RP_CHUNK - 1) / RP_CHUNK;
     const int k0 = (int)((int64_t)nchunks * part / RP_PARTS);
     const int k1 = (int)((int64_t)nchunks * (part + 1) / RP_PARTS);
-    if (k0 >= k1) return;
+    if (k0 >= k1) return true;
     const int q = tb * RP_PAIR_THREADS + tid;
     const bool active = q < nq;
     float tnx = 0, tny = 0, tnz = 1;
@@ -854,14 +893,14 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         tnx = (float)A.TG[3 * A.nt + ti]; tny = (float)A.TG[4 * A.nt + ti];
         tnz = (float)A.TG[5 * A.nt + ti];
         b0 = A.bt0[(size_t)s * A.tstride + q];
-        Trow = A.T + (((size_t)part * A.nb + s) * A.tstride + q) * A.Wt;
-        if constexpr (SPEC) Trow2 = A.T2 + (((size_t)part * A.nb + s) * A.tstride + q) * A.Wt;
+        Trow = A.T + 2 * ((((size_t)part * A.nb + s) * A.tstride + q) * A.Wt);
+        if constexpr (SPEC) Trow2 = A.T2 + 2 * ((((size_t)part * A.nb + s) * A.tstride + q) * A.Wt);
     }
     const FacetPair* rbase = A.rec + (size_t)s * (A.rstride / 2);
     const ChunkMeta* mbase = A.meta + (size_t)s * A.mstride;
     // prologue: stage chunk k0 and its metadata (whole pairs: an odd count
     // ends with a padded pair)
-    if (tid == 0) {
+    if (tid == 0 && !A.stall_copies) {
         int cnt = min(RP_CHUNK, n - k0 * RP_CHUNK);
         uint32_t bytes = (uint32_t)(((cnt + 1) >> 1) * sizeof(FacetPair));
         const uint32_t sbytes = SPEC ? (uint32_t)(((cnt + 1) >> 1) * sizeof(FacetSpec)) : 0u;
@@ -875,7 +914,7 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
         const int buf = (k - k0) & 1;
         // prefetch the next chunk into the other buffer (its readers
         // finished at the trailing __syncthreads of the previous step)
-        if (tid == 0 && k + 1 < k1) {
+        if (tid == 0 && k + 1 < k1 && !A.stall_copies) {
             int cnt = min(RP_CHUNK, n - (k + 1) * RP_CHUNK);
             uint32_t bytes = (uint32_t)(((cnt + 1) >> 1) * sizeof(FacetPair));
             const uint32_t sbytes = SPEC ? (uint32_t)(((cnt + 1) >> 1) * sizeof(FacetSpec)) : 0u;
@@ -889,16 +928,14 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
                              &bars[buf ^ 1]);
         }
         const ChunkMeta* mp = smeta + buf;
-        if (!mbar_wait(&bars[buf], phase[buf])) {
-            if (tid == 0) atomicOr(A.err + 1, 1u);
-        }
-        phase[buf] ^= 1u;
+        const bool got = mbar_wait(&bars[buf], phase[buf], A.spin_limit);
+        const bool live = active && got;
         const FacetPair* R = srec + buf * RP_CHUNK_PAIRS;
         const FacetSpec* RS = SPEC ? sspec + buf * RP_CHUNK_PAIRS : nullptr;
         Anchor an;
         int blo = 0;
         bool fits = true;
-        if (active) {
+        if (live) {
             // anchors of this (chunk, target) in double-float FP32
             const float4 th = s_tq[tid], tl = s_tq[RP_PAIR_THREADS + tid];
             const float cfx = mp->cfx, cfy = mp->cfy, cfz = mp->cfz;
@@ -928,7 +965,7 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
             an.eaT0 = fmaf(A.ealpha, Th, A.eks);
         }
         const bool all_fit = __all_sync(0xffffffffu, fits);
-        if (active) {
+        if (live) {
             for (int w = 0; w < W; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
             if constexpr (SPEC)
                 for (int w = 0; w < W; ++w) win2[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
@@ -1018,8 +1055,15 @@ __device__ __forceinline__ void pair_item(const PA& A, int s, int tb, int part, 
             flush_window<W>(win, tid, blo, b0, Trow, A.Wt, A.err);
             if constexpr (SPEC) flush_window<W>(win2, tid, blo, b0, Trow2, A.Wt, A.err);
         }
-        __syncthreads();   // everyone done with buffer `buf` before it is refilled
+        // everyone done with buffer `buf` before it is refilled; a wait that
+        // ran out anywhere in the block ends its work
+        if (__syncthreads_or(!got)) {
+            abort_block(A, bars, phase, buf, got, k + 1 < k1);
+            return false;
+        }
+        phase[buf] ^= 1u;
     }
+    return true;
 }
 
 // --------------------------------------------------- ttype-0 targets --
@@ -1112,7 +1156,7 @@ static_assert(pair_t0spec_off(RP_WIN_WIDE) % 16 == 0, "staged by bulk copies");
 // the double-float anchors are pair_item's; the anchors use c1/c2 in place
 // of n and a positive phase, and every phasor goes to one bin.
 template <int NT, int ILP, bool ORTHO, bool SPEC, int W>
-__device__ __forceinline__ void pair_item_t0(const PairArgs& A, int s, int tb, int part, uint64_t* bars,
+__device__ __forceinline__ bool pair_item_t0(const PairArgs& A, int s, int tb, int part, uint64_t* bars,
                                              uint32_t* phase) {
     FacetPair* srec = reinterpret_cast<FacetPair*>(pair_smem);
     float2* win = reinterpret_cast<float2*>(pair_smem + pair_win_off());
@@ -1124,11 +1168,11 @@ __device__ __forceinline__ void pair_item_t0(const PairArgs& A, int s, int tb, i
     const int qs = A.tq0[s];
     const int nq = A.ntl[s] - qs;
     const int n = A.nill[s];
-    if (tb * RP_PAIR_THREADS >= nq || n == 0) return;
+    if (tb * RP_PAIR_THREADS >= nq || n == 0) return true;
     const int nchunks = (n + RP_CHUNK - 1) / RP_CHUNK;
     const int k0 = (int)((int64_t)nchunks * part / RP_PARTS);
     const int k1 = (int)((int64_t)nchunks * (part + 1) / RP_PARTS);
-    if (k0 >= k1) return;
+    if (k0 >= k1) return true;
     const int ql = tb * RP_PAIR_THREADS + tid;
     const bool active = ql < nq;
     const int q = qs + ql;
@@ -1147,7 +1191,7 @@ __device__ __forceinline__ void pair_item_t0(const PairArgs& A, int s, int tb, i
         tnx = (float)A.TG[3 * A.nt + ti]; tny = (float)A.TG[4 * A.nt + ti];
         tnz = (float)A.TG[5 * A.nt + ti];
         b0 = A.bt0[(size_t)s * A.tstride + q];
-        Trow = A.T + (((size_t)part * A.nb + s) * A.tstride + q) * A.Wt;
+        Trow = A.T + 2 * ((((size_t)part * A.nb + s) * A.tstride + q) * A.Wt);
     }
     const size_t pbase = (size_t)s * (A.rstride / 2);
     const FacetPair* rbase = A.rec + pbase;
@@ -1164,22 +1208,20 @@ __device__ __forceinline__ void pair_item_t0(const PairArgs& A, int s, int tb, i
         if (SPEC)
             tma_bulk_g2s(sspec + b * RP_CHUNK_PAIRS, A.spec + pbase + (size_t)k * RP_CHUNK_PAIRS, sb, &bars[b]);
     };
-    if (tid == 0) stage(k0, 0);
+    if (tid == 0 && !A.stall_copies) stage(k0, 0);
     for (int k = k0; k < k1; ++k) {
         const int buf = (k - k0) & 1;
-        if (tid == 0 && k + 1 < k1) stage(k + 1, buf ^ 1);
+        if (tid == 0 && k + 1 < k1 && !A.stall_copies) stage(k + 1, buf ^ 1);
         const ChunkMeta* mp = smeta + buf;
-        if (!mbar_wait(&bars[buf], phase[buf])) {
-            if (tid == 0) atomicOr(A.err + 1, 1u);
-        }
-        phase[buf] ^= 1u;
+        const bool got = mbar_wait(&bars[buf], phase[buf], A.spin_limit);
+        const bool live = active && got;
         const FacetPair* R = srec + buf * RP_CHUNK_PAIRS;
         const FacetT0* R0 = st0 + buf * RP_CHUNK_PAIRS;
         const FacetSpec* RS = SPEC ? sspec + buf * RP_CHUNK_PAIRS : nullptr;
         Anchor an;
         int blo = 0;
         bool fits = true;
-        if (active) {
+        if (live) {
             const float4 th = s_tq[tid], tl = s_tq[RP_PAIR_THREADS + tid];
             const float cfx = mp->cfx, cfy = mp->cfy, cfz = mp->cfz;
             float Th, Tl, Qh;
@@ -1202,7 +1244,7 @@ __device__ __forceinline__ void pair_item_t0(const PairArgs& A, int s, int tb, i
             an.eaT0 = fmaf(A.ealpha, Th, A.eks);
         }
         const bool all_fit = __all_sync(0xffffffffu, fits);
-        if (active) {
+        if (live) {
             for (int w = 0; w < W; ++w) win[w * RP_PAIR_THREADS + tid] = make_float2(0.f, 0.f);
             const int cnt = min(RP_CHUNK, n - k * RP_CHUNK);
             const int npairs = (cnt + 1) >> 1;
@@ -1258,8 +1300,13 @@ __device__ __forceinline__ void pair_item_t0(const PairArgs& A, int s, int tb, i
             }
             flush_window<W>(win, tid, blo, b0, Trow, A.Wt, A.err);
         }
-        __syncthreads();
+        if (__syncthreads_or(!got)) {
+            abort_block(A, bars, phase, buf, got, k + 1 < k1);
+            return false;
+        }
+        phase[buf] ^= 1u;
     }
+    return true;
 }
 
 #define RP_PAIR_SMEM_DECL                                                                       \
@@ -1307,8 +1354,9 @@ int launch_pairs_t0(int deg, bool ortho, bool spec, const PairArgs& P, int64_t i
 #define RP_DS_GROUPS 128      // fixed facet-chunk groups per trace (ordered partial sums)
 struct DirectArgs {
     const double* F;        // sorted facet store, SoA [12][nf]
-    int64_t nf;             // its stride, also the stride of idx and sv
-    const int* idx;         // [nb][nf] illuminated facets (store order)
+    int64_t nf;             // its stride
+    int64_t fstride;        // per-trace stride of idx and sv (the segment's facet capacity)
+    const int* idx;         // [nb][fstride] illuminated facets (store order)
     const int* nill;
     const double* traces;   // [nb][9]
     const double* TG;       // fast target store [7][nt]
@@ -1316,7 +1364,7 @@ struct DirectArgs {
     const int* tlist;       // [nb][tstride] in-aperture targets (all ttype 0 in this mode)
     const int* ntl;
     int64_t tstride;
-    const C32* sv;          // [nb][nf] surface phasors fRe exp(+j 4 pi_F Itd / lam)
+    const C32* sv;          // [nb][fstride] surface phasors fRe exp(+j 4 pi_F Itd / lam)
     const FacetSpec* spec;  // [nb][rstride / 2]
     const FacetT0* t0rec;   // [nb][rstride / 2]
     int64_t rstride;

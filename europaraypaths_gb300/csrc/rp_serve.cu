@@ -1,11 +1,17 @@
 // rp_serve.cu -- the resident request loop (rp_server_*, rp_submit, rp_poll).
 //
-// Worker threads, each with its own CUDA stream and rp_workspace, take
-// requests from one FIFO queue under a device-memory budget.  A free worker
-// takes the queue head and, while they fit, the following fast-form requests
-// (up to max_batch) and runs them as one rp_simulate_batch call: continuous
-// batching over the resident scenes.  Host side only; the kernels are those
-// of the two forms.
+// Worker threads, each with its own CUDA stream and rp_workspace, serve
+// requests from one FIFO queue under a device-memory budget.  A request is
+// cut into steps of at most step_traces traces (the whole request when the
+// step is 0).  Each worker call takes the next step of up to max_batch
+// requests that are already running (round robin), then admits queued
+// requests in FIFO order while they fit the budget and the active-request
+// limit, and runs all the fast-form steps it took as one rp_simulate_batch
+// call: continuous batching at step granularity.  A request that arrives
+// while others run joins at the next call of any worker; short requests
+// finish without waiting for long ones; several workers' calls overlap on
+// the device.  Queued requests older than max_wait_ms are shed
+// (RP_ERR_TIMEOUT).  Host side only; the kernels are those of the two forms.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -27,7 +33,7 @@ double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-enum { Q_QUEUED = 0, Q_RUNNING = 1, Q_DONE = 2 };
+enum { Q_QUEUED = 0, Q_ACTIVE = 1, Q_DONE = 2 };
 
 struct SrvReq {
     int64_t id = 0;
@@ -43,11 +49,26 @@ struct SrvReq {
     int state = Q_QUEUED;
     int rc = RP_OK;
     std::string err;
+    // step scheduling (guarded by the server mutex)
+    int64_t step = 0;       // traces per step
+    int64_t next = 0;       // first trace not yet handed to a worker
+    int64_t finished = 0;   // traces whose step completed (or was dropped after a failure)
+    int running = 0;        // steps of this request in worker calls now
 };
 
 using ReqP = std::shared_ptr<SrvReq>;
 
 bool batchable(const SrvReq& r) { return (r.form & 0xff) == RP_FORM_FAST_F32 && !(r.form & RP_OUT_COMPLEX128); }
+
+size_t out_elem_bytes(const SrvReq& r) { return (r.form & RP_OUT_COMPLEX128) ? 16 : 8; }
+
+// One step of a request in a worker call: traces [c0, c0 + len).
+struct Step {
+    ReqP r;
+    int64_t c0 = 0, len = 0;
+    int rc = RP_OK;
+    std::string err;
+};
 
 }  // namespace
 
@@ -55,47 +76,57 @@ struct rp_server {
     int device = 0;
     int64_t budget = 0;
     int max_batch = 1;
+    int64_t step_traces = 0;   // 0: whole requests
+    int max_active = 0;        // 0: no limit but the budget
+    int max_wait_ms = 0;       // 0: no bound on the queue wait
     bool fake = false;
     rp_executor ex{};
     std::mutex mu;
     std::condition_variable cv;
     std::deque<ReqP> q;
+    std::vector<ReqP> active;
+    size_t rr = 0;             // round-robin cursor over active
     std::unordered_map<int64_t, ReqP> reqs;
     int64_t next_id = 1;
     int64_t in_flight = 0;
-    int running = 0;
+    int running = 0;           // worker calls in progress
     bool stop = false;
     std::vector<std::thread> threads;
     // statistics
     std::vector<double> lat_ms, wait_ms;
-    int64_t completed = 0, failed = 0, rejected = 0, cancelled = 0, calls = 0, max_in_call = 0;
+    int64_t completed = 0, failed = 0, rejected = 0, cancelled = 0, shed = 0, calls = 0, steps = 0;
+    int64_t max_in_call = 0, max_active_seen = 0, max_calls_running = 0;
     double pairs = 0, t_first = -1, t_last = 0;
 };
 
 namespace {
 
-// Run one worker call on the GPU: per-request device buffers, one
-// rp_simulate_batch for batchable requests (rp_simulate_ws otherwise), and
-// on a batch failure each request again alone so that errors stay with their
-// own request.
-void gpu_call(std::vector<ReqP>& batch, rp_workspace* ws, cudaStream_t st) {
-    const size_t n = batch.size();
+// Run the steps of one worker call on the GPU: per-step device buffers, one
+// rp_simulate_batch over the steps when they are all fast-form (and more
+// than one), else rp_simulate_ws per step; on a batch failure every step
+// runs again alone, so an error stays with its own request.  Each step's
+// radargram rows and counts land in its request's host output at the step's
+// trace offset.
+void gpu_call(std::vector<Step>& steps, rp_workspace* ws, cudaStream_t st) {
+    const size_t n = steps.size();
     std::vector<double*> d_tr(n, nullptr);
     std::vector<void*> d_out(n, nullptr);
     std::vector<size_t> out_bytes(n, 0);
+    bool all_batch = n > 1;
     auto fail_all = [&](int rc) {
         char buf[1024];
         rp_last_error(buf, sizeof(buf));
-        for (auto& r : batch) { r->rc = rc; r->err = buf; }
+        for (auto& s : steps) { s.rc = rc; s.err = buf; }
     };
     for (size_t i = 0; i < n; ++i) {
-        SrvReq& r = *batch[i];
-        r.counts.assign(2 * (size_t)r.ns, 0);
-        out_bytes[i] = (size_t)r.ns * r.sc->nr * ((r.form & RP_OUT_COMPLEX128) ? 16 : 8);
-        cudaError_t e = cudaMallocAsync((void**)&d_tr[i], sizeof(double) * 9 * r.ns, st);
+        Step& s = steps[i];
+        all_batch = all_batch && batchable(*s.r);
+        out_bytes[i] = (size_t)s.len * s.r->sc->nr * out_elem_bytes(*s.r);
+        cudaError_t e = cudaMallocAsync((void**)&d_tr[i], sizeof(double) * 9 * s.len, st);
         if (e == cudaSuccess) e = cudaMallocAsync(&d_out[i], out_bytes[i], st);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(d_tr[i], r.tr.data(), sizeof(double) * 9 * r.ns, cudaMemcpyHostToDevice, st);
+            e = cudaMemcpyAsync(d_tr[i], s.r->tr.data() + 9 * s.c0, sizeof(double) * 9 * s.len,
+                                cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) {
             fail_all(rp_cuda_fail(e, "server buffers"));
             goto cleanup;
@@ -103,27 +134,30 @@ void gpu_call(std::vector<ReqP>& batch, rp_workspace* ws, cudaStream_t st) {
     }
     {
         int rc = RP_OK;
-        if (n > 1) {
+        if (all_batch) {
             std::vector<rp_job> jobs(n);
             for (size_t i = 0; i < n; ++i)
-                jobs[i] = rp_job{batch[i]->sc, d_tr[i], batch[i]->ns, d_out[i], batch[i]->counts.data()};
+                jobs[i] = rp_job{steps[i].r->sc, d_tr[i], steps[i].len, d_out[i],
+                                 steps[i].r->counts.data() + 2 * steps[i].c0};
             rc = rp_simulate_batch(jobs.data(), (int)n, ws, st);
         }
         for (size_t i = 0; i < n; ++i) {
-            SrvReq& r = *batch[i];
+            Step& s = steps[i];
             int rci = rc;
-            if (n == 1 || rc != RP_OK)
-                rci = rp_simulate_ws(r.sc, ws, d_tr[i], r.ns, r.form, d_out[i], r.counts.data(), st);
+            if (!all_batch || rc != RP_OK)
+                rci = rp_simulate_ws(s.r->sc, ws, d_tr[i], s.len, s.r->form, d_out[i],
+                                     s.r->counts.data() + 2 * s.c0, st);
             if (rci == RP_OK) {
-                cudaError_t e = cudaMemcpyAsync(r.out, d_out[i], out_bytes[i], cudaMemcpyDeviceToHost, st);
+                char* dst = static_cast<char*>(s.r->out) + (size_t)s.c0 * s.r->sc->nr * out_elem_bytes(*s.r);
+                cudaError_t e = cudaMemcpyAsync(dst, d_out[i], out_bytes[i], cudaMemcpyDeviceToHost, st);
                 if (e == cudaSuccess) e = cudaStreamSynchronize(st);
                 if (e != cudaSuccess) rci = rp_cuda_fail(e, "server output copy");
             }
-            r.rc = rci;
+            s.rc = rci;
             if (rci != RP_OK) {
                 char buf[1024];
                 rp_last_error(buf, sizeof(buf));
-                r.err = buf;
+                s.err = buf;
             }
         }
     }
@@ -135,12 +169,97 @@ cleanup:
     cudaStreamSynchronize(st);
 }
 
-void fake_call(rp_server* S, std::vector<ReqP>& batch) {
-    for (auto& r : batch) {
-        r->counts.assign(2 * (size_t)r->ns, 0);
-        r->rc = S->ex.run(S->ex.user, r->sc, r->tr.data(), r->ns, r->form, r->out, r->counts.data());
-        if (r->rc != RP_OK) r->err = "executor failed";
+// Bytes of one output row of a request: nr x (8 or 16), from the scene, or
+// from the executor's bins() when an executor stands in for the GPU.
+size_t row_bytes(const rp_server* S, const SrvReq& r);
+
+void fake_call(rp_server* S, std::vector<Step>& steps) {
+    for (auto& s : steps) {
+        SrvReq& r = *s.r;
+        char* dst = static_cast<char*>(r.out) + (size_t)s.c0 * row_bytes(S, r);
+        s.rc = S->ex.run(S->ex.user, r.sc, r.tr.data() + 9 * s.c0, s.len, r.form, dst, r.counts.data() + 2 * s.c0);
+        if (s.rc != RP_OK) s.err = "executor failed";
     }
+}
+
+size_t row_bytes(const rp_server* S, const SrvReq& r) {
+    const int64_t nr = S->fake ? (S->ex.bins ? S->ex.bins(S->ex.user, r.sc) : 0) : r.sc->nr;
+    return (size_t)nr * out_elem_bytes(r);
+}
+
+// Finish a request whose traces are all done (caller holds the lock).
+void finish(rp_server* S, const ReqP& r, double t) {
+    r->t_end = t;
+    r->state = Q_DONE;
+    S->in_flight -= r->fp;
+    if (r->rc == RP_OK) {
+        ++S->completed;
+        S->lat_ms.push_back(1e3 * (r->t_end - r->t_submit));
+        S->wait_ms.push_back(1e3 * (r->t_start - r->t_submit));
+        for (int64_t k = 0; k < r->ns; ++k)
+            S->pairs += (double)r->counts[2 * k] * (1.0 + 2.0 * (double)r->counts[2 * k + 1]);
+        S->t_last = std::max(S->t_last, t);
+        if (r->user_counts) std::copy(r->counts.begin(), r->counts.end(), r->user_counts);
+    } else {
+        ++S->failed;
+    }
+    S->active.erase(std::find(S->active.begin(), S->active.end(), r));
+}
+
+// Take the steps of one worker call (caller holds the lock): shed queued
+// requests past the wait bound, then the next step of up to max_batch
+// running requests (round robin), then queued requests in FIFO order while
+// they fit the budget and the active limit.  A plain-form or complex128
+// step runs alone; fast-form steps are grouped.
+std::vector<Step> take_steps(rp_server* S, double t) {
+    std::vector<Step> out;
+    if (S->max_wait_ms > 0) {
+        while (!S->q.empty() && 1e3 * (t - S->q.front()->t_submit) > (double)S->max_wait_ms) {
+            ReqP r = S->q.front();
+            S->q.pop_front();
+            r->state = Q_DONE;
+            r->rc = RP_ERR_TIMEOUT;
+            r->err = "request waited in the queue longer than the server's bound";
+            r->t_end = t;
+            ++S->shed;
+        }
+    }
+    const int maxa = S->max_active > 0 ? S->max_active : INT32_MAX;
+    auto take = [&](const ReqP& r) -> bool {     // false: the call is full
+        if (!out.empty() && (!batchable(*out[0].r) || !batchable(*r))) return false;
+        Step s;
+        s.r = r;
+        s.c0 = r->next;
+        s.len = std::min(r->step, r->ns - r->next);
+        r->next += s.len;
+        ++r->running;
+        out.push_back(s);
+        return (int)out.size() < S->max_batch && batchable(*r);
+    };
+    bool room = true;
+    const size_t na = S->active.size();
+    const size_t start = na ? S->rr % na : 0;
+    for (size_t k = 0; k < na && room; ++k) {
+        const size_t idx = (start + k) % na;
+        const ReqP& r = S->active[idx];
+        if (r->next >= r->ns || r->rc != RP_OK) continue;
+        if (!out.empty() && (!batchable(*out[0].r) || !batchable(*r))) continue;
+        room = take(r);
+        S->rr = idx + 1;     // the next call starts after the last request served
+    }
+    while (room && !S->q.empty() && (int)S->active.size() < maxa &&
+           S->in_flight + S->q.front()->fp <= S->budget) {
+        ReqP r = S->q.front();
+        if (!out.empty() && (!batchable(*out[0].r) || !batchable(*r))) break;
+        S->q.pop_front();
+        S->in_flight += r->fp;
+        r->state = Q_ACTIVE;
+        r->t_start = t;
+        S->active.push_back(r);
+        room = take(r);
+    }
+    S->max_active_seen = std::max<int64_t>(S->max_active_seen, (int64_t)S->active.size());
+    return out;
 }
 
 void worker_main(rp_server* S) {
@@ -156,59 +275,48 @@ void worker_main(rp_server* S) {
         if (setup_rc != RP_OK) rp_last_error(setup_err, sizeof(setup_err));
     }
     for (;;) {
-        std::vector<ReqP> batch;
+        std::vector<Step> steps;
         {
             std::unique_lock<std::mutex> lk(S->mu);
-            S->cv.wait(lk, [&] {
-                return (S->stop && S->q.empty()) ||
-                       (!S->q.empty() && S->in_flight + S->q.front()->fp <= S->budget);
-            });
-            if (S->q.empty()) break;
-            const double t = now_s();
-            auto take = [&](const ReqP& r) {
-                S->q.pop_front();
-                S->in_flight += r->fp;
-                r->state = Q_RUNNING;
-                r->t_start = t;
-                batch.push_back(r);
-            };
-            ReqP h = S->q.front();
-            take(h);
-            if (batchable(*h))
-                while (!S->q.empty() && (int)batch.size() < S->max_batch) {
-                    ReqP nx = S->q.front();
-                    if (!batchable(*nx) || S->in_flight + nx->fp > S->budget) break;
-                    take(nx);
-                }
+            bool quit = false;
+            for (;;) {
+                if (S->stop && S->q.empty() && S->active.empty()) { quit = true; break; }
+                const int64_t shed0 = S->shed;
+                steps = take_steps(S, now_s());
+                if (S->shed != shed0) S->cv.notify_all();      // shed requests are finished
+                if (!steps.empty()) break;
+                // with a queue-wait bound, wake up now and then to shed
+                if (S->max_wait_ms > 0) S->cv.wait_for(lk, std::chrono::milliseconds(std::max(1, S->max_wait_ms / 4)));
+                else S->cv.wait(lk);
+            }
+            if (quit) break;
             ++S->running;
             ++S->calls;
-            S->max_in_call = std::max<int64_t>(S->max_in_call, (int64_t)batch.size());
+            S->steps += (int64_t)steps.size();
+            S->max_in_call = std::max<int64_t>(S->max_in_call, (int64_t)steps.size());
+            S->max_calls_running = std::max<int64_t>(S->max_calls_running, (int64_t)S->running);
         }
         if (setup_rc != RP_OK) {
-            for (auto& r : batch) { r->rc = setup_rc; r->err = setup_err; }
+            for (auto& s : steps) { s.rc = setup_rc; s.err = setup_err; }
         } else if (S->fake) {
-            fake_call(S, batch);
+            fake_call(S, steps);
         } else {
-            gpu_call(batch, ws, st);
+            gpu_call(steps, ws, st);
         }
         {
             std::lock_guard<std::mutex> lk(S->mu);
             const double t = now_s();
-            for (auto& r : batch) {
-                r->t_end = t;
-                r->state = Q_DONE;
-                S->in_flight -= r->fp;
-                if (r->rc == RP_OK) {
-                    ++S->completed;
-                    S->lat_ms.push_back(1e3 * (r->t_end - r->t_submit));
-                    S->wait_ms.push_back(1e3 * (r->t_start - r->t_submit));
-                    for (int64_t k = 0; k < r->ns; ++k)
-                        S->pairs += (double)r->counts[2 * k] * (1.0 + 2.0 * (double)r->counts[2 * k + 1]);
-                    S->t_last = std::max(S->t_last, t);
-                    if (r->user_counts) std::copy(r->counts.begin(), r->counts.end(), r->user_counts);
-                } else {
-                    ++S->failed;
+            for (auto& s : steps) {
+                const ReqP& r = s.r;
+                --r->running;
+                r->finished += s.len;
+                if (s.rc != RP_OK && r->rc == RP_OK) {
+                    r->rc = s.rc;
+                    r->err = s.err;
+                    r->finished += r->ns - r->next;    // the rest of the request is dropped
+                    r->next = r->ns;
                 }
+                if (r->finished >= r->ns && r->running == 0 && r->state == Q_ACTIVE) finish(S, r, t);
             }
             --S->running;
         }
@@ -255,10 +363,31 @@ extern "C" int rp_server_create(int device, int workers, int64_t mem_budget, int
     return RP_OK;
 }
 
+extern "C" int rp_server_configure(rp_server* S, int64_t step_traces, int max_active, int max_wait_ms) {
+    if (!S || step_traces < 0 || max_active < 0 || max_wait_ms < 0) {
+        rp_set_error("rp_server_configure: bad argument");
+        return RP_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (!S->reqs.empty() || !S->q.empty() || !S->active.empty()) {
+        rp_set_error("rp_server_configure: requests were already submitted");
+        return RP_ERR_ARG;
+    }
+    if (S->fake && step_traces > 0 && !S->ex.bins) {
+        rp_set_error("rp_server_configure: steps need the executor's bins()");
+        return RP_ERR_ARG;
+    }
+    S->step_traces = step_traces;
+    S->max_active = max_active;
+    S->max_wait_ms = max_wait_ms;
+    S->cv.notify_all();
+    return RP_OK;
+}
+
 extern "C" int rp_server_drain(rp_server* S, int timeout_ms) {
     if (!S) { rp_set_error("rp_server_drain: null server"); return RP_ERR_ARG; }
     std::unique_lock<std::mutex> lk(S->mu);
-    auto idle = [&] { return S->q.empty() && S->running == 0; };
+    auto idle = [&] { return S->q.empty() && S->active.empty() && S->running == 0; };
     if (timeout_ms < 0) {
         S->cv.wait(lk, idle);
     } else if (!S->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), idle)) {
@@ -298,13 +427,25 @@ extern "C" int rp_submit(rp_server* S, rp_scene* sc, const double* traces, int64
     r->form = form;
     r->out = out;
     r->user_counts = counts;
+    r->counts.assign(2 * (size_t)ns, 0);
+    int64_t step;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        step = S->step_traces > 0 ? std::min<int64_t>(S->step_traces, ns) : ns;
+    }
+    r->step = step;
+    // footprint: the largest step's scratch plus its trace table and output
     if (S->fake) {
-        r->fp = S->ex.footprint(S->ex.user, sc, ns, form);
+        r->fp = S->ex.footprint(S->ex.user, sc, step, form);
     } else {
         int64_t scratch = 0;
-        int rc = rp_query_footprint_traces(sc, traces, ns, form, &scratch);
-        if (rc) return rc;
-        r->fp = scratch + ns * (72 + (int64_t)sc->nr * ((form & RP_OUT_COMPLEX128) ? 16 : 8));
+        for (int64_t c0 = 0; c0 < ns; c0 += step) {
+            int64_t b = 0;
+            int rc = rp_query_footprint_traces(sc, traces + 9 * c0, std::min(step, ns - c0), form, &b);
+            if (rc) return rc;
+            scratch = std::max(scratch, b);
+        }
+        r->fp = scratch + step * (72 + (int64_t)sc->nr * ((form & RP_OUT_COMPLEX128) ? 16 : 8));
     }
     std::lock_guard<std::mutex> lk(S->mu);
     if (r->fp > S->budget) {
@@ -370,10 +511,11 @@ extern "C" int rp_server_stats(rp_server* S, double* stats, int n) {
     for (double v : S->wait_ms) wait += v;
     if (!S->lat_ms.empty()) { mean /= (double)S->lat_ms.size(); wait /= (double)S->wait_ms.size(); }
     const double wall = (S->t_first >= 0 && S->t_last > S->t_first) ? S->t_last - S->t_first : 0.0;
-    const double v[13] = {(double)S->completed, (double)S->failed, (double)S->rejected, (double)S->cancelled,
+    const double v[18] = {(double)S->completed, (double)S->failed, (double)S->rejected, (double)S->cancelled,
                           percentile(S->lat_ms, 50), percentile(S->lat_ms, 99), mean, wait, S->pairs,
                           wall > 0 ? S->pairs / wall : 0.0, (double)S->calls, (double)S->max_in_call,
-                          (double)S->in_flight};
-    for (int i = 0; i < n; ++i) stats[i] = i < 13 ? v[i] : 0.0;
+                          (double)S->in_flight, (double)S->shed, (double)S->steps, (double)S->max_active_seen,
+                          (double)S->max_calls_running, percentile(S->lat_ms, 90)};
+    for (int i = 0; i < n; ++i) stats[i] = i < 18 ? v[i] : 0.0;
     return RP_OK;
 }

@@ -30,7 +30,7 @@ k_pairs32s(const __grid_constant__ PairArgs A) {
         const int part = item % RP_PARTS;
         const int tb = (item / RP_PARTS) % A.tblocks;
         const int s = item / (RP_PARTS * A.tblocks);
-        pair_item<NT, ILP, false, true, RP_WIN>(A, s, tb, part, bars, phase);
+        if (!pair_item<NT, ILP, false, true, RP_WIN>(A, s, tb, part, bars, phase)) break;
     }
     RP_PAIR_SMEM_END
 }
@@ -76,7 +76,7 @@ k_pairs32t0(const __grid_constant__ PairArgs A) {
         const int part = item % RP_PARTS;
         const int tb = (item / RP_PARTS) % A.tblocks;
         const int s = item / (RP_PARTS * A.tblocks);
-        pair_item_t0<NT, 2, ORTHO, SPEC, RP_WIN_WIDE>(A, s, tb, part, bars, phase);
+        if (!pair_item_t0<NT, 2, ORTHO, SPEC, RP_WIN_WIDE>(A, s, tb, part, bars, phase)) break;
     }
     RP_PAIR_SMEM_END
 }

@@ -141,32 +141,34 @@ def large_scene(seed=2, n_facets_side=2000, n_targets_side=200, ns=2000):
     return {"name": "large_scene", "params": p, "facets": facets, "targets": targets}
 
 
-def flyby(seed=5, n_facets_side=8000, n_targets_side=400, ns=10000):
+def flyby(seed=5, n_facets_side=8000, fs=2.5, target_spacing=50.0, trace_spacing=2.0):
     """The flyby-scale scene (64M facets, two rough layers, 10,000 traces at
     25 km, 60 MHz / 10 MHz sampled at 24 MHz into 16384 bins).
 
     * surface: 8000x8000 facets at 2.5 m (20 km square), fractal heights
       (Hurst 0.75, RMS 8 m);
     * two rough interfaces 1 km and 3 km deep (RMS 10 m, l = 200 m), each
-      sampled as a 400x400 target grid at 50 m (320k targets, ttype 1);
-    * 10,000 traces along x at 25 km altitude, 2 m spacing, aperture 3 deg;
+      sampled as a target grid at 50 m (2 x 400x400 = 320k targets, ttype 1);
+    * traces along x at 25 km altitude every 2 m across the scene (10,000),
+      aperture 3 deg;
     * eps 3.15 above the first interface, sigma 1e-6.  The permittivities
       below the interfaces (3.2, 6.0) have no counterpart in the reference's
       physics (targets carry no Fresnel term) and are not used.
-    Sizes can be reduced for tests; the facet spacing scales so the scene
-    keeps its 20 km side."""
-    fs = 2.5 * 8000 / n_facets_side
+    A smaller ``n_facets_side`` keeps the spacings and band and shrinks the
+    square (2000 facets: 5 km, 4M facets, 2 x 100x100 targets, 2,500 traces;
+    the aperture footprint still fits inside)."""
     side = n_facets_side * fs
-    p = base_params(60e6, 10e6, 24e6, 16384, 3.0, 3.15, 1e-6, 8.0, fs, 25e3, ns, side / ns, 7.3)
+    ns = int(round(side / trace_spacing))
+    p = base_params(60e6, 10e6, 24e6, 16384, 3.0, 3.15, 1e-6, 8.0, fs, 25e3, ns, trace_spacing, 7.3)
     dom = {"fs": fs, "nx": n_facets_side, "ny": n_facets_side, "ox": -side / 2, "oy": -side / 2}
     h = fractal_field(n_facets_side, n_facets_side, fs, 8.0, 0.75, seed)
     facets = ss.surface_arrays_blocked(dom, h)
     del h
-    tfs = side / n_targets_side
-    tdom = {"fs": tfs, "nx": n_targets_side, "ny": n_targets_side, "ox": -side / 2, "oy": -side / 2}
+    n_targets_side = max(1, int(round(side / target_spacing)))
+    tdom = {"fs": target_spacing, "nx": n_targets_side, "ny": n_targets_side, "ox": -side / 2, "oy": -side / 2}
     layers = []
     for k, depth in enumerate((1000.0, 3000.0)):
-        th = gaussian_field(n_targets_side, n_targets_side, tfs, 10.0, 200.0, seed * 1000 + k)
+        th = gaussian_field(n_targets_side, n_targets_side, target_spacing, 10.0, 200.0, seed * 1000 + k)
         layers.append(ss.target_arrays(tdom, "flat", zoffset=-depth, heights=th))
     targets = np.concatenate(layers, axis=1)
     return {"name": "flyby", "params": p, "facets": facets, "targets": targets}

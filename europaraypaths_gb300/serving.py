@@ -31,7 +31,9 @@ RP_PENDING = 1
 RP_ERR_BUDGET = -7
 RP_ERR_CANCELLED = -10
 STAT_KEYS = ("completed", "failed", "rejected", "cancelled", "p50_ms", "p99_ms", "mean_ms", "mean_wait_ms",
-             "pairs", "pairs_per_s", "worker_calls", "max_batch_seen", "in_flight_bytes")
+             "pairs", "pairs_per_s", "worker_calls", "max_batch_seen", "in_flight_bytes", "shed", "steps",
+             "max_active_seen", "max_calls_running", "p90_ms")
+RP_ERR_TIMEOUT = -8
 
 
 class BudgetError(RuntimeError):
@@ -40,6 +42,10 @@ class BudgetError(RuntimeError):
 
 class CancelledError(RuntimeError):
     """The request was cancelled before it started."""
+
+
+class ShedError(RuntimeError):
+    """The request waited in the queue longer than the server's bound."""
 
 
 class Request:
@@ -75,6 +81,8 @@ class Request:
             self._finish(rc)
         if self.status == RP_ERR_CANCELLED:
             raise CancelledError(f"request {self.id} cancelled")
+        if self.status == RP_ERR_TIMEOUT:
+            raise ShedError(f"request {self.id} shed: {self.error_text}")
         if self.status != 0:
             raise RuntimeError(f"request {self.id} failed ({_abi.ERRORS.get(self.status, self.status)}): "
                                f"{self.error_text}")
@@ -84,10 +92,11 @@ class Request:
 _RUN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
                         ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64))
 _FOOT = ctypes.CFUNCTYPE(ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int)
+_BINS = ctypes.CFUNCTYPE(ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p)
 
 
 class _Executor(ctypes.Structure):
-    _fields_ = [("run", _RUN), ("footprint", _FOOT), ("user", ctypes.c_void_p)]
+    _fields_ = [("run", _RUN), ("footprint", _FOOT), ("user", ctypes.c_void_p), ("bins", _BINS)]
 
 
 class Server:
@@ -95,7 +104,13 @@ class Server:
 
     FORMS = {"plain": 0, "fast": 1}
 
-    def __init__(self, workers=3, mem_budget=None, device=0, max_batch=8, executor=None):
+    def __init__(self, workers=3, mem_budget=None, device=0, max_batch=8, executor=None, step_traces=0,
+                 max_active=0, max_wait=None):
+        """``step_traces`` > 0 cuts requests into steps of that many traces,
+        scheduled round robin across the active requests (continuous batching
+        at step granularity); ``max_active`` bounds the requests active at
+        once (0: the memory budget alone); ``max_wait`` (seconds) sheds
+        queued requests that waited longer (``ShedError``)."""
         self.device = device
         self.scenes = {}          # sid -> (handle, nr, owned Scene or None)
         self._next_sid = 1
@@ -117,11 +132,17 @@ class Server:
             def foot(_user, scene, ns, form):
                 return int(executor.footprint(int(scene or 0), ns, form))
 
-            self._ex = _Executor(_RUN(run), _FOOT(foot), None)
+            def bins(_user, scene):
+                return int(self.scenes[int(scene or 0)][1])
+
+            self._ex = _Executor(_RUN(run), _FOOT(foot), None, _BINS(bins))
             exp = ctypes.byref(self._ex)
         self._h = ctypes.c_void_p()
         _abi.check("rp_server_create", _abi.lib().rp_server_create(
             int(device), int(workers), int(mem_budget or 0), int(max_batch), exp, ctypes.byref(self._h)))
+        if step_traces or max_active or max_wait:
+            _abi.check("rp_server_configure", _abi.lib().rp_server_configure(
+                self._h, int(step_traces), int(max_active), int(round(1000 * (max_wait or 0)))))
 
     # ---------------------------------------------------------------- scenes
     def add_scene(self, params, facets=None, targets=None, prisms=None):
@@ -176,7 +197,7 @@ class Server:
         _abi.check("rp_server_stats", _abi.lib().rp_server_stats(self._h, buf, len(STAT_KEYS)))
         d = dict(zip(STAT_KEYS, list(buf)))
         for k in ("completed", "failed", "rejected", "cancelled", "worker_calls", "max_batch_seen",
-                  "in_flight_bytes"):
+                  "in_flight_bytes", "shed", "steps", "max_active_seen", "max_calls_running"):
             d[k] = int(d[k])
         return d
 

@@ -226,17 +226,22 @@ int rp_autotune_query(int multi, int degree, int* cfg);
  *
  * Requests name a resident scene and carry a host trace table (copied at
  * submit) and a caller-owned host output (ns x nr complex64, written before
- * the request completes).  A request is admitted when a worker is free and its
- * device footprint (rp_query_footprint plus its trace table and output) fits
- * the memory budget next to everything running; requests wait in FIFO order.
- * A free worker takes the queue head and, for fast-form requests, every
- * following queued fast-form request that also fits (up to max_batch), and
- * runs them as one rp_simulate_batch call on its own stream and workspace --
- * continuous batching: requests arriving while others run are admitted as
- * workers and memory free up, and their work overlaps on the device.  A
- * request's result does not depend on what it was batched or overlapped with.
- * The queue is internally locked; every function may be called from any
- * thread.
+ * the request completes).  A request is cut into steps of at most
+ * step_traces traces (rp_server_configure; by default the whole request is
+ * one step).  A request is admitted (becomes active) when its device
+ * footprint (the scratch of its largest step plus that step's trace table
+ * and output) fits the memory budget next to every active request, and the
+ * active limit allows; requests wait in FIFO order.  Each worker call takes
+ * the next step of up to max_batch active requests (round robin), then
+ * admits queued requests that fit and takes their first step, and runs the
+ * fast-form steps it took as one rp_simulate_batch call on its own stream
+ * and workspace -- continuous batching at step granularity: requests
+ * arriving while others run join at the next call of any worker, short
+ * requests finish without waiting for long ones, and the workers' calls
+ * overlap on the device.  Plain-form and complex128 steps run one per call.
+ * A request's result does not depend on what it was batched or overlapped
+ * with.  The queue is internally locked; every function may be called from
+ * any thread.
  */
 typedef struct rp_server rp_server;
 
@@ -248,12 +253,21 @@ typedef struct rp_executor {
                int64_t* counts);
     int64_t (*footprint)(void* user, rp_scene* scene, int64_t ns, int form);
     void* user;
+    /* range bins of a scene (its output row length); may be NULL when
+     * requests run whole (no step_traces) */
+    int64_t (*bins)(void* user, rp_scene* scene);
 } rp_executor;
 
 /* workers >= 1; mem_budget <= 0: 60% of the device's free memory;
  * max_batch >= 1 requests per worker call; ex may be NULL. */
 int rp_server_create(int device, int workers, int64_t mem_budget, int max_batch, const rp_executor* ex,
                      rp_server** out);
+/* Scheduling options, before the first rp_submit: step_traces > 0 cuts
+ * requests into steps of that many traces (0: whole requests); max_active
+ * > 0 bounds the requests active at once (0: the budget alone); max_wait_ms
+ * > 0 sheds queued requests that waited longer, finishing them with
+ * RP_ERR_TIMEOUT (0: no bound).  RP_ERR_ARG after a submit. */
+int rp_server_configure(rp_server* srv, int64_t step_traces, int max_active, int max_wait_ms);
 /* Drains the queue, then stops the workers. */
 int rp_server_destroy(rp_server* srv);
 /* Queue a request; *ticket identifies it.  RP_ERR_BUDGET when its footprint
@@ -264,13 +278,15 @@ int rp_submit(rp_server* srv, rp_scene* scene, const double* traces, int64_t ns,
  * (RP_OK, an error, RP_ERR_CANCELLED) and the ticket is released.
  * timeout_ms: 0 polls, < 0 waits until the request finishes. */
 int rp_poll(rp_server* srv, int64_t ticket, int timeout_ms);
-/* Cancel a request that has not started (RP_ERR_ARG if it has). */
+/* Cancel a request that is still queued (RP_ERR_ARG once it is active). */
 int rp_cancel(rp_server* srv, int64_t ticket);
 /* Wait until nothing is queued or running (timeout_ms < 0: no limit). */
 int rp_server_drain(rp_server* srv, int timeout_ms);
 /* stats[0..n): completed, failed, rejected, cancelled, p50 ms, p99 ms,
  * mean ms (submit to completion), mean queue wait ms, pairs, pairs/s (first
- * submit to last completion), worker calls, largest batch, requests in flight. */
+ * submit to last completion), worker calls, largest batch (steps in one
+ * call), footprint in flight (bytes), shed (queue-wait bound), steps run,
+ * most requests active at once, most worker calls running at once, p90 ms. */
 int rp_server_stats(rp_server* srv, double* stats, int n);
 
 /* Number of kernel launches issued by this thread's last rp_simulate*. */

@@ -1,8 +1,10 @@
 """Golden vectors of the reference's azimuth focusing (simple_focusing.py:
 full_focus_at_center 115-185, focus_rdrgrm 310-404) on small seeded
-radargrams.  Run here, where the reference sources are present:
+radargrams.  Run where the reference sources are present, with the path of
+their src/PYTHON directory as the argument (or REFERENCE_ROOT set to the
+checkout root); there is no default:
 
-    python tests/golden/make_focus_golden.py /root/reference/src/PYTHON
+    python tests/golden/make_focus_golden.py <reference checkout>/src/PYTHON
 
 Writes tests/golden/focus_small.npz (parameters and outputs; the input
 radargrams are regenerated from their seed by inputs()).  matplotlib is not
@@ -63,4 +65,9 @@ def main(ref_dir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src/PYTHON")
+    if len(sys.argv) > 1:
+        main(sys.argv[1])
+    elif os.environ.get("REFERENCE_ROOT"):
+        main(os.path.join(os.environ["REFERENCE_ROOT"], "src", "PYTHON"))
+    else:
+        sys.exit("usage: make_focus_golden.py <reference checkout>/src/PYTHON  (or set REFERENCE_ROOT)")

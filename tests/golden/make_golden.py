@@ -1,8 +1,11 @@
 """Generate golden fixtures from the reference's own Python entry points.
 
-Runs only where the reference checkout is available (REFERENCE_ROOT, default
-the read-only mount used when this was generated); the fixtures it writes are
-committed next to this script and are all the tests read.
+Runs only where a reference checkout is available: its root is the first
+argument or the REFERENCE_ROOT environment variable (there is no default).
+The fixtures it writes are committed next to this script and are all the
+tests read.
+
+    python tests/golden/make_golden.py <reference checkout root>
 
 Fixtures:
   params_<platform>_<media>.json   gen_params(...) for each preset
@@ -20,10 +23,15 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("REFERENCE_ROOT", "/root/reference")
+def reference_root():
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE_ROOT")
+    if not ref:
+        sys.exit("usage: make_golden.py <reference checkout root>  (or set REFERENCE_ROOT)")
+    return ref
 
 
 def main():
+    REF = reference_root()
     sys.path.insert(0, os.path.join(REF, "src", "PYTHON"))
     import param_gen as pg
     import simple_surfaces as ss

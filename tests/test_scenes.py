@@ -20,12 +20,13 @@ def test_blocked_surface_is_bit_identical(ny, nx, rows):
 
 def test_flyby_reduced_shapes_and_bands():
     from europaraypaths_gb300 import param_gen, scenes
-    sc = scenes.flyby(n_facets_side=200, n_targets_side=20, ns=50)
+    sc = scenes.flyby(n_facets_side=200)             # 500 m square at 2.5 m
     p = param_gen.to_rp_params(sc["params"])
     assert sc["facets"].shape == (12, 200 * 200)
-    assert sc["targets"].shape == (7, 2 * 20 * 20)
+    assert sc["targets"].shape == (7, 2 * 10 * 10)
     assert p.nr == 16384 and abs(p.frequency - 60e6) < 1 and abs(p.bandwidth - 10e6) < 1
+    assert p.ns == 250 and abs(p.sdx - 2.0) < 1e-12
     z = sc["targets"][2]
-    assert (np.abs(z[:400] + 1000.0) < 60).all() and (np.abs(z[400:] + 3000.0) < 60).all()
+    assert (np.abs(z[:100] + 1000.0) < 60).all() and (np.abs(z[100:] + 3000.0) < 60).all()
     side = sc["facets"][0].max() - sc["facets"][0].min()
-    assert abs(side - (20000.0 - 100.0)) < 1e-6
+    assert abs(side - (500.0 - 2.5)) < 1e-6

@@ -181,14 +181,89 @@ def test_adopted_scene_survives_close():
     assert sid in srv.scenes
 
 
+def test_steps_round_robin_results():
+    # requests cut into 2-trace steps: every step lands at its offset, and
+    # one call takes steps of several requests
+    eng = FakeEngine(delay=0.01)
+    srv, sid = _server(eng, nr=5, workers=1, mem_budget=10 ** 6, max_batch=4, step_traces=2)
+    a = srv.submit(sid, _traces(7, 100))
+    b = srv.submit(sid, _traces(3, 200))
+    c = srv.submit(sid, _traces(1, 300))
+    for r, n, base in ((a, 7, 100), (b, 3, 200), (c, 1, 300)):
+        out = r.result(timeout=10)
+        assert out.shape == (n, 5)
+        assert np.array_equal(out[:, 1].real, base + np.arange(n))
+        assert np.array_equal(r.counts, np.ones((n, 2)))
+    st = srv.stats()
+    assert st["steps"] == 4 + 2 + 1 and st["max_batch_seen"] >= 2 and st["completed"] == 3
+    srv.close()
+
+
+def test_short_request_not_blocked_by_long_one():
+    # step-level scheduling: a 1-trace request that arrives while a 30-trace
+    # request runs finishes long before it
+    eng = FakeEngine(delay=0.02)
+    srv, sid = _server(eng, workers=1, mem_budget=10 ** 6, max_batch=2, step_traces=1)
+    t0 = time.perf_counter()
+    big = srv.submit(sid, _traces(30, 0))
+    time.sleep(0.05)
+    small = srv.submit(sid, _traces(1, 1000))
+    small.result(timeout=10)
+    t_small = time.perf_counter() - t0
+    big.result(timeout=10)
+    t_big = time.perf_counter() - t0
+    assert t_small < 0.5 * t_big
+    srv.close()
+
+
+def test_active_limit_and_queue_wait_bound():
+    from europaraypaths_gb300.serving import ShedError
+    eng = FakeEngine(delay=0.05)
+    srv, sid = _server(eng, workers=2, mem_budget=10 ** 6, max_batch=4, step_traces=1, max_active=1,
+                       max_wait=0.15)
+    first = srv.submit(sid, _traces(8, 0))          # ~0.4 s of steps
+    time.sleep(0.02)
+    late = [srv.submit(sid, _traces(1, 100 + k)) for k in range(3)]
+    assert first.result(timeout=10).shape == (8, 4)
+    for r in late:
+        with pytest.raises(ShedError):
+            r.result(timeout=10)
+    st = srv.stats()
+    assert st["shed"] == 3 and st["max_active_seen"] == 1 and st["completed"] == 1
+    srv.close()
+
+
+def test_step_failure_drops_the_rest_of_its_request_only():
+    eng = FakeEngine(delay=0.005, fail_on_base=2.0)
+    srv, sid = _server(eng, workers=2, mem_budget=10 ** 6, max_batch=4, step_traces=2)
+    bad = srv.submit(sid, _traces(6, 0))           # steps at 0, 2 (fails), 4
+    good = srv.submit(sid, _traces(4, 50))
+    with pytest.raises(RuntimeError, match="failed"):
+        bad.result(timeout=10)
+    assert np.array_equal(good.result(timeout=10)[:, 1].real, 50 + np.arange(4))
+    st = srv.stats()
+    assert st["failed"] == 1 and st["completed"] == 1
+    srv.close()
+
+
+def test_configure_after_submit_refused():
+    from europaraypaths_gb300 import _abi
+    eng = FakeEngine(delay=0.2)
+    srv, sid = _server(eng, workers=1, mem_budget=10 ** 6)
+    srv.submit(sid, _traces(1, 0))
+    assert _abi.lib().rp_server_configure(srv._h, 2, 0, 0) == -1
+    srv.close()
+
+
 @pytest.mark.gpu
-def test_gpu_same_alone_and_mixed(built_lib):
+@pytest.mark.parametrize("step", [0, 2])
+def test_gpu_same_alone_and_mixed(built_lib, step):
     from europaraypaths_gb300 import param_gen, simulator, traces as tr_mod
     from europaraypaths_gb300.serving import Server
     from europaraypaths_gb300 import scenes as scn
     scs = [tiny_scene(nside=40, ntside=4, ns=6),
            tiny_scene(nside=30, ntside=3, ns=5, eps_2=4.0, rx_window_m=scn.rx_window_for_bins(1024, 4e6))]
-    srv = Server(workers=3, mem_budget=2 << 30)
+    srv = Server(workers=3, mem_budget=2 << 30, step_traces=step)
     sids = [srv.add_scene(sc["params"], sc["facets"], sc["targets"]) for sc in scs]
     jobs = []
     for k in range(12):
