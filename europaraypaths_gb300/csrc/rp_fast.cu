@@ -661,8 +661,10 @@ __device__ __forceinline__ Cplx<float> trace_at(const C32* __restrict__ T, size_
 // DIF of the zero-padded target trace into a (n values): the first fused
 // pass reads its 16 inputs straight from the target's rows (only the window
 // is non-zero), the rest run in place.  Ends with a barrier.
+// With to_edge, the stages of the edge block are left to the caller's edge
+// pass.
 __device__ __forceinline__ void dif_trace(Cplx<float>* a, const C32* __restrict__ T, size_t pstride, size_t qbase,
-                                          int b0, int Wt, int nr, int n) {
+                                          int b0, int Wt, int nr, int n, bool to_edge) {
     const int S = n >> 4;
     for (int g = threadIdx.x; g < S; g += RP_CONV_THREADS) {
         Cplx<float> x[16];
@@ -673,7 +675,33 @@ __device__ __forceinline__ void dif_trace(Cplx<float>* a, const C32* __restrict_
         for (int i = 0; i < 16; ++i) a[swz(g + i * S)] = x[i];
     }
     __syncthreads();
-    block_dif_s_from(a, n, n >> 4);
+    if (to_edge) block_dif_s_mid(a, n, n >> 4);
+    else block_dif_s_from(a, n, n >> 4);
+}
+
+// One pass over contiguous edge blocks of B elements of src: the last DIF
+// stages, then op(k0, x) (the pointwise product, the first DIT stages and the
+// stores, for elements k0 .. k0 + B - 1); no barrier.
+template <int B, class Op>
+__device__ __forceinline__ void edge_pass(const Cplx<float>* src, int n, Op op) {
+    for (int blk = threadIdx.x; blk < n / B; blk += RP_CONV_THREADS) {
+        Cplx<float> x[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) x[i] = src[swz(blk * B + i)];
+        dif_edge<float, B>(x);
+        op(blk * B, x);
+    }
+}
+
+// The edge pass for the block size of length n (16, 2, 4 or 8).
+template <class Op>
+__device__ __forceinline__ void edge_pass_n(const Cplx<float>* src, int n, Op op) {
+    switch (edge_block(n)) {
+        case 16: edge_pass<16>(src, n, op); break;
+        case 8: edge_pass<8>(src, n, op); break;
+        case 4: edge_pass<4>(src, n, op); break;
+        default: edge_pass<2>(src, n, op); break;
+    }
 }
 
 // Shared-memory range compression (nr a power of two >= 32).  One work item =
@@ -690,8 +718,13 @@ __device__ __forceinline__ void dif_trace(Cplx<float>* a, const C32* __restrict_
 // takeEveryOtherComplex) is linear in u and the same for every target, so it
 // runs once per trace on the sum (k_trace_m32).  The transforms are the
 // in-place stages of rp_fft.cuh with the elements at swizzled positions, and
-// three pass boundaries are crossed in registers instead of shared memory:
+// five pass boundaries are crossed in registers instead of shared memory:
 //  * the first DIF pass of X reads the target's rows directly;
+//  * the last DIF stages of X, the product with the chirp spectrum and the
+//    first DIT stages of Ptarg's transform act on the same contiguous edge
+//    blocks (rp_fft.cuh: edge_block), so they run as one edge pass; so do
+//    the last DIF stages of DIF(pad Ptarg), the spectra's product and the
+//    first DIT stages of u's transform;
 //  * Ptarg is a shift by nr/2 = 4 S of the first transform's natural-order
 //    output, S = n / 16, and the first DIF pass of the second transform reads
 //    elements g + i S (i < 8 non-zero) -- exactly the registers x[i + 4] that
@@ -772,25 +805,28 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
         for (int q = q0; q < q1; ++q) {
             const int b0 = bt0[(size_t)s * tstride + q];
             const size_t qbase = ((size_t)s * tstride + q) * Wt;
-            // ---- X = DIF(pad T); W = X * C2 (mode 1: X parks in the slot)
-            if constexpr (MODE == 1) {
-                dif_trace(W, T, pstride, qbase, b0, Wt, nr, n2);
-                #pragma unroll 8
-                for (int k = tid; k < n2; k += RP_CONV_THREADS) {
-                    const Cplx<float> v = W[swz(k)];
-                    X[swz(k)] = v;
-                    W[swz(k)] = c_mul(v, C2s[k]);
+            // ---- X = DIF(pad T) up to its edge block (mode 1: in W's
+            // shared memory), then one edge pass: the last DIF stages, X
+            // stored (mode 1: parked in the slot), W = X * C2 and the first
+            // DIT stages of Ptarg's transform
+            Cplx<float>* const D1 = (MODE == 1) ? W : X;
+            dif_trace(D1, T, pstride, qbase, b0, Wt, nr, n2, true);
+            edge_pass_n(D1, n2, [&](int k0, auto& x) {
+                constexpr int B = sizeof(x) / sizeof(x[0]);
+#pragma unroll
+                for (int i = 0; i < B; ++i) {
+                    X[swz(k0 + i)] = x[i];
+                    x[i] = c_mul(x[i], C2s[k0 + i]);
                 }
-            } else {
-                dif_trace(X, T, pstride, qbase, b0, Wt, nr, n2);
-                #pragma unroll 8
-                for (int k = tid; k < n2; k += RP_CONV_THREADS) W[swz(k)] = c_mul(X[swz(k)], C2s[k]);
-            }
+                dit_edge<float, B>(x);
+#pragma unroll
+                for (int i = 0; i < B; ++i) W[swz(k0 + i)] = x[i];
+            });
             __syncthreads();
-            // ---- Ptarg: every DIT stage but the last fused pass, then that
+            // ---- Ptarg: the DIT passes up to span n/16, then the last fused
             // pass, the shift by nr/2 with the 1/2nr scale and zero padding,
             // and the first DIF pass of DIF(pad Ptarg), in registers
-            block_dit_s_upto(W, n2, n2 >> 4);
+            block_dit_s_mid(W, n2, n2 >> 4);
             for (int g = tid; g < S; g += RP_CONV_THREADS) {
                 Cplx<float> x[16];
 #pragma unroll
@@ -805,29 +841,26 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
                 for (int i = 0; i < 16; ++i) W[swz(g + i * S)] = x[i];
             }
             __syncthreads();
-            block_dif_s_from(W, n2, n2 >> 4);
-            // ---- the spectra's product, scaled
-            if constexpr (SPEC) {
-                // Psour = s T2, the outbound leg's own trace: mode 1 parks
-                // DIF(Ptarg) in the slot and transforms T2 in shared memory
-                if constexpr (MODE == 1) {
-                    #pragma unroll 8
-                    for (int k = tid; k < n2; k += RP_CONV_THREADS) X[swz(k)] = W[swz(k)];
-                    __syncthreads();
-                    dif_trace(W, T2, pstride, qbase, b0, Wt, nr, n2);
-                } else {
-                    dif_trace(X, T2, pstride, qbase, b0, Wt, nr, n2);
+            // specular mode: Psour = s T2, the outbound leg's own trace, whose
+            // transform replaces X (X's DIF(pad T) is no longer needed)
+            if constexpr (SPEC) dif_trace(X, T2, pstride, qbase, b0, Wt, nr, n2, false);
+            block_dif_s_mid(W, n2, n2 >> 4);
+            // ---- one edge pass: DIF(pad Ptarg)'s last stages, the spectra's
+            // product (scaled) and the first DIT stages of u's transform
+            edge_pass_n(W, n2, [&](int k0, auto& x) {
+                constexpr int B = sizeof(x) / sizeof(x[0]);
+#pragma unroll
+                for (int i = 0; i < B; ++i) {
+                    const Cplx<float> v = c_mul(X[swz(k0 + i)], x[i]);
+                    x[i] = Cplx<float>{v.x * sc, v.y * sc};
                 }
-            }
-            #pragma unroll 8
-            for (int k = tid; k < n2; k += RP_CONV_THREADS) {
-                // the operand order of the product is the same in every mode
-                const Cplx<float> v = (SPEC && MODE == 1) ? c_mul(W[swz(k)], X[swz(k)]) : c_mul(X[swz(k)], W[swz(k)]);
-                W[swz(k)] = Cplx<float>{v.x * sc, v.y * sc};
-            }
+                dit_edge<float, B>(x);
+#pragma unroll
+                for (int i = 0; i < B; ++i) W[swz(k0 + i)] = x[i];
+            });
             __syncthreads();
             // ---- u = DIT(...): the last fused pass adds into the sums
-            block_dit_s_upto(W, n2, n2 >> 4);
+            block_dit_s_mid(W, n2, n2 >> 4);
             for (int g = tid; g < S; g += RP_CONV_THREADS) {
                 Cplx<float> x[16];
 #pragma unroll
@@ -1535,11 +1568,12 @@ int zero_pairs(const std::vector<Seg*>& ps, unsigned int* d_work, unsigned int* 
 }
 
 // Choose the pair configuration of a wave: the tuned one, or probe every
-// candidate (four for one segment, two for the specular kernel, eight for a
-// multi-segment wave: the multi-job kernel and per-segment launches in each
-// configuration); each probe is a full launch on this wave's items, outputs
-// re-zeroed after.  Tuned per kind: single kernel (0), multi-segment (1) or
-// specular (2), and sinc degree.
+// candidate (four for one segment, two for the specular kernel, ten for a
+// multi-segment wave: the multi-job kernel, per-segment launches and the
+// per-kind kernels); each probe is a full launch on this wave's items,
+// outputs re-zeroed after, and every candidate is probed twice (the best of
+// its two times counts).  Tuned per kind: single kernel (0), multi-segment
+// (1) or specular (2), and sinc degree.
 int choose_cfg(const std::vector<Seg*>& ps, const PairJob* d_jobs, const PairJob* h_jobs,
                const unsigned int* d_start, unsigned int* d_work, unsigned int* seg_work, int sms, cudaStream_t st,
                rp_workspace* ws, bool par, int* cfg_out) {
@@ -1558,22 +1592,28 @@ int choose_cfg(const std::vector<Seg*>& ps, const PairJob* d_jobs, const PairJob
     cudaEvent_t e0, e1;
     RP_CUDA(cudaEventCreate(&e0));
     RP_CUDA(cudaEventCreate(&e1));
-    float best = 1e30f;
-    int bestc = spec ? (ps[0]->sc->pair_cfg & 1) : (ps[0]->sc->pair_cfg & 3);
-    for (int k = 0; k < ncfg; ++k) {
-        int rc = zero_pairs(ps, d_work, seg_work, st);
-        if (rc) return rc;
-        RP_CUDA(cudaEventRecord(e0, st));
-        rc = launch_pairs(ps, d_jobs, h_jobs, d_start, d_work, seg_work, k, sms, st, ws, par);
-        if (rc) return rc;
-        RP_CUDA(cudaEventRecord(e1, st));
-        RP_CUDA(cudaEventSynchronize(e1));
+    // two rounds (forward, then backward), each configuration's best time:
+    // one probe per configuration let a noisy probe decide for the process
+    std::vector<float> tbest(ncfg, 1e30f);
+    int rc = RP_OK;
+    for (int r = 0; r < 2 * ncfg && rc == RP_OK; ++r) {
+        const int k = r < ncfg ? r : 2 * ncfg - 1 - r;
+        rc = zero_pairs(ps, d_work, seg_work, st);
+        cudaError_t e = rc ? cudaSuccess : cudaEventRecord(e0, st);
+        if (!rc && e == cudaSuccess) rc = launch_pairs(ps, d_jobs, h_jobs, d_start, d_work, seg_work, k, sms, st, ws, par);
+        if (!rc && e == cudaSuccess) e = cudaEventRecord(e1, st);
+        if (!rc && e == cudaSuccess) e = cudaEventSynchronize(e1);
         float ms = 0.f;
-        RP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        if (ms < best) { best = ms; bestc = k; }
+        if (!rc && e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (!rc && e != cudaSuccess) rc = rp_cuda_fail(e, "autotune probe");
+        if (!rc) tbest[k] = std::min(tbest[k], ms);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (rc) return rc;
+    int bestc = spec ? (ps[0]->sc->pair_cfg & 1) : (ps[0]->sc->pair_cfg & 3);
+    for (int k = 0; k < ncfg; ++k)
+        if (tbest[k] < tbest[bestc]) bestc = k;
     tuned_store(multi, deg, bestc);
     *cfg_out = bestc;
     return zero_pairs(ps, d_work, seg_work, st);

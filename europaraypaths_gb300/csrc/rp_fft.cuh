@@ -337,4 +337,108 @@ __device__ __forceinline__ void block_dit_s_upto(Cplx<T>* a, int n, int Lmax) {
 
 template <class T>
 __device__ __forceinline__ void block_dit_s(Cplx<T>* a, int n) { block_dit_s_upto(a, n, n / 4); }
+
+// ---- the edge block: the last DIF stages and the first DIT stages of a
+// length-n transform both act within contiguous blocks of B elements, B =
+// 16, 2, 4, 8 for log2 n = 0, 1, 2, 3 mod 4 (the last fused DIF pass at span
+// 16 and the first fused DIT pass at span 4; the radix-2 stage; the lone
+// radix-4 stage at span 4; the radix-4 stage at span 8 with the radix-2
+// stage).  So a pointwise product between a forward and an inverse
+// transform can sit between them in registers: one pass over the data
+// instead of three.  The stage arithmetic is the same as block_dif_s /
+// block_dit_s.
+__host__ __device__ __forceinline__ int edge_block(int n) {
+    const int r = fft_log2(n) & 3;
+    return r == 0 ? 16 : (r == 1 ? 2 : (r == 2 ? 4 : 8));
+}
+
+template <class T, int B>
+__device__ __forceinline__ void dif_edge(Cplx<T> (&x)[B]) {
+    if constexpr (B == 16) {
+        dif16_regs(x, 0, 16);
+    } else if constexpr (B == 8) {
+        const float st = 6.28318530717958647f / 8.f;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) r4_dif_reg(x[j], x[j + 2], x[j + 4], x[j + 6], tw_sfu<T>(j, st));
+#pragma unroll
+        for (int p = 0; p < 8; p += 2) {
+            const Cplx<T> a = x[p], b = x[p + 1];
+            x[p] = c_add(a, b);
+            x[p + 1] = c_sub(a, b);
+        }
+    } else if constexpr (B == 4) {
+        r4_dif_reg(x[0], x[1], x[2], x[3], tw_sfu<T>(0, 6.28318530717958647f / 4.f));
+    } else {
+        const Cplx<T> a = x[0], b = x[1];
+        x[0] = c_add(a, b);
+        x[1] = c_sub(a, b);
+    }
+}
+
+template <class T, int B>
+__device__ __forceinline__ void dit_edge(Cplx<T> (&x)[B]) {
+    if constexpr (B == 16) {
+        dit16_regs(x, 0, 4);
+    } else if constexpr (B == 8) {
+#pragma unroll
+        for (int p = 0; p < 8; p += 2) {
+            const Cplx<T> a = x[p], b = x[p + 1];
+            x[p] = c_add(a, b);
+            x[p + 1] = c_sub(a, b);
+        }
+        const float st = 6.28318530717958647f / 8.f;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) r4_dit_reg(x[j], x[j + 2], x[j + 4], x[j + 6], tw_sfu<T>(j, st));
+    } else if constexpr (B == 4) {
+        r4_dit_reg(x[0], x[1], x[2], x[3], tw_sfu<T>(0, 6.28318530717958647f / 4.f));
+    } else {
+        const Cplx<T> a = x[0], b = x[1];
+        x[0] = c_add(a, b);
+        x[1] = c_sub(a, b);
+    }
+}
+
+// DIF fused passes of spans L0, L0 / 16, ... > 16: the passes between a
+// transform's first pass (span n, run by the caller) and its edge block.
+// Ends with a barrier when it ran a pass.
+template <class T>
+__device__ __forceinline__ void block_dif_s_mid(Cplx<T>* a, int n, int L0) {
+    for (int L = L0, lL = fft_log2(L0); L > 16; L >>= 4, lL -= 4) {
+        const int lS = lL - 4, S = 1 << lS;
+        for (int g = threadIdx.x; g < (n >> 4); g += blockDim.x) {
+            const int b = g & (S - 1);
+            const int base = (g >> lS) * L + b;
+            Cplx<T> x[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) x[i] = a[swz(base + i * S)];
+            dif16_regs(x, b, L);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) a[swz(base + i * S)] = x[i];
+        }
+        __syncthreads();
+    }
+}
+
+// DIT fused passes of spans between the edge block's (exclusive) and Lmax
+// (inclusive): from 64, 8, 16, 32 for edge blocks 16, 2, 4, 8.  Ends with a
+// barrier when it ran a pass.
+template <class T>
+__device__ __forceinline__ void block_dit_s_mid(Cplx<T>* a, int n, int Lmax) {
+    const int B = edge_block(n);
+    const int L0 = B == 16 ? 64 : 4 * B;
+    for (int L = L0, lL = fft_log2(L0); L <= Lmax; L <<= 4, lL += 4) {
+        const int lS = lL - 2, S = 1 << lS;
+        for (int g = threadIdx.x; g < (n >> 4); g += blockDim.x) {
+            const int b = g & (S - 1);
+            const int base = (g >> lS) * (4 * L) + b;
+            Cplx<T> x[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) x[i] = a[swz(base + i * S)];
+            dit16_regs(x, b, L);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) a[swz(base + i * S)] = x[i];
+        }
+        __syncthreads();
+    }
+}
 #endif
