@@ -704,42 +704,88 @@ __device__ __forceinline__ void edge_pass_n(const Cplx<float>* src, int n, Op op
     }
 }
 
-// Shared-memory range compression (nr a power of two >= 32).  One work item =
+// The item's sum U of the targets' product spectra.  The inverse transform
+// that turns X * DIF(pad Ptarg) into u is linear, so the product spectra are
+// summed over the item's targets (in target order) and transformed once per
+// item.  U holds element k at swz(k), like X and W: in shared memory (mode
+// 0) or in the item's partial row in global memory (modes 1 and 2).
+// spec_add: one target's last DIF stages of DIF(pad Ptarg) (in W) and its
+// product with X, added into U (each element by the thread that owns its
+// edge block).
+template <int B>
+__device__ __forceinline__ void spec_add(const Cplx<float>* W, const Cplx<float>* X, Cplx<float>* U, int n) {
+    for (int blk = threadIdx.x; blk < n / B; blk += RP_CONV_THREADS) {
+        Cplx<float> x[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) x[i] = W[swz(blk * B + i)];
+        dif_edge<float, B>(x);
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            const int k = swz(blk * B + i);
+            const Cplx<float> v = c_mul(X[k], x[i]);
+            Cplx<float> o = U[k];
+            o.x += v.x;
+            o.y += v.y;
+            U[k] = o;
+        }
+    }
+}
+
+// U, scaled by sc, through the first DIT stages into W (the rest of u's
+// inverse transform follows).
+template <int B>
+__device__ __forceinline__ void spec_to_w(Cplx<float>* W, const Cplx<float>* U, int n, float sc) {
+    for (int blk = threadIdx.x; blk < n / B; blk += RP_CONV_THREADS) {
+        Cplx<float> x[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            const Cplx<float> o = U[swz(blk * B + i)];
+            x[i] = Cplx<float>{o.x * sc, o.y * sc};
+        }
+        dit_edge<float, B>(x);
+#pragma unroll
+        for (int i = 0; i < B; ++i) W[swz(blk * B + i)] = x[i];
+    }
+}
+
+// Shared-memory range compression (nr a power of two >= 16).  One work item =
 // RP_CONV_SPLIT consecutive targets of one trace; their contributions are
 // summed in target order and written as one partial trace.  Per target (n =
 // 2nr values in X and W):
 //   X = DIF(pad T)                         T = sum of the facet-range parts
 //   W = DIT(X * C2)[nr/2 ..] / 2nr         Ptarg (convolvePhasorChirpLinear)
-//   W = DIT(X * DIF(pad Ptarg)) * s / 2nr  u = Psour (*) Ptarg, Psour = s T
-//                                          (specular: X = DIF(pad T2) first)
-//                                          (length N = 2nr - 1: the N-point
-//                                          circular product has no wrap)
-// The rest of the chain (cropSpectrum, the inverse N-point DFT,
-// takeEveryOtherComplex) is linear in u and the same for every target, so it
-// runs once per trace on the sum (k_trace_m32).  The transforms are the
-// in-place stages of rp_fft.cuh with the elements at swizzled positions, and
-// five pass boundaries are crossed in registers instead of shared memory:
+//   U += X * DIF(pad Ptarg)                the product spectrum of u = Psour (*)
+//                                          Ptarg, Psour = s T (specular: X =
+//                                          DIF(pad T2) first); length N =
+//                                          2nr - 1, so the N-point circular
+//                                          product has no wrap
+// and per item u = DIT(U) * s / 2nr: the inverse transform is linear, so the
+// targets' product spectra are summed and transformed once (3 transforms a
+// target instead of 4).  The rest of the chain (cropSpectrum, the inverse
+// N-point DFT, takeEveryOtherComplex) is linear in u and the same for every
+// target, so it runs once per trace on the sum (k_trace_m32).  The
+// transforms are the in-place stages of rp_fft.cuh with the elements at
+// swizzled positions, and four pass boundaries are crossed in registers
+// instead of shared memory:
 //  * the first DIF pass of X reads the target's rows directly;
 //  * the last DIF stages of X, the product with the chirp spectrum and the
 //    first DIT stages of Ptarg's transform act on the same contiguous edge
-//    blocks (rp_fft.cuh: edge_block), so they run as one edge pass; so do
-//    the last DIF stages of DIF(pad Ptarg), the spectra's product and the
-//    first DIT stages of u's transform;
+//    blocks (rp_fft.cuh: edge_block), so they run as one edge pass;
 //  * Ptarg is a shift by nr/2 = 4 S of the first transform's natural-order
 //    output, S = n / 16, and the first DIF pass of the second transform reads
 //    elements g + i S (i < 8 non-zero) -- exactly the registers x[i + 4] that
 //    the last DIT pass of the first transform leaves in the same thread -- so
 //    the two passes and the shift run back to back in registers;
-//  * the last DIT pass of the product transform adds its outputs u[g + i S]
-//    straight into the item's sums.
+//  * the last DIF stages of DIF(pad Ptarg) and the spectra's product run in
+//    the edge pass that adds into U (spec_add).
 // Persistent over the items of one or more batches (job j owns items
-// [start[j], start[j + 1])); twiddles come from the SFU.  MODE 0: X and W in
-// shared memory (nr <= 4096), the sums in registers (thread g owns elements
-// g + i S).  MODE 1 (nr = 8192): every transform in one n-value buffer of
-// shared memory; X waits in this block's slot of the global scratch between
-// its two uses.  MODE 2: X and W in the slot (nr >= 16384).  Modes 1 and 2
-// sum the targets in the item's partial row in global memory (same element,
-// same target order as mode 0, so every mode gives the same sums).
+// [start[j], start[j + 1])); twiddles come from the SFU.  MODE 0: X, W and U
+// in shared memory (nr <= 4096; 192 KiB at nr = 4096).  MODE 1 (nr = 8192): every
+// transform in one n-value buffer of shared memory; X waits in this block's
+// slot of the global scratch between its two uses.  MODE 2: X and W in the
+// slot (nr >= 16384).  Modes 1 and 2 keep U in the item's partial row in
+// global memory (same element, same target order as mode 0, so every mode
+// gives the same sums), which then receives u.
 template <int MODE, bool SPEC>
 __global__ void __launch_bounds__(RP_CONV_THREADS, 1)
 k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ start, int njobs,
@@ -795,13 +841,13 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
         if (q0 >= nq) continue;
         const int q1 = min(q0 + RP_CONV_SPLIT, nq);
         C32* const out = part + ((size_t)s * nsplit + sp) * n2;
-        float accr[16], acci[16];               // MODE 0: u at g + i S, g = tid
-#pragma unroll
-        for (int i = 0; i < 16; ++i) { accr[i] = 0.f; acci[i] = 0.f; }
-        if (MODE != 0)
-            for (int j = tid; j < N; j += RP_CONV_THREADS) out[j] = C32{0.f, 0.f};
+        // U: the summed product spectra (spec_add); mode 0 in shared memory
+        // after X and W, else the item's partial row, which then receives u
+        Cplx<float>* const U = (MODE == 0) ? sbase + 2 * n2 : reinterpret_cast<Cplx<float>*>(out);
+        for (int j = tid; j < n2; j += RP_CONV_THREADS) U[j] = Cplx<float>{0.f, 0.f};
         const float inv = 1.f / (float)n2;
         const float sc = sig_scale / (float)n2;
+        const int EB = edge_block(n2);
         for (int q = q0; q < q1; ++q) {
             const int b0 = bt0[(size_t)s * tstride + q];
             const size_t qbase = ((size_t)s * tstride + q) * Wt;
@@ -845,51 +891,35 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
             // transform replaces X (X's DIF(pad T) is no longer needed)
             if constexpr (SPEC) dif_trace(X, T2, pstride, qbase, b0, Wt, nr, n2, false);
             block_dif_s_mid(W, n2, n2 >> 4);
-            // ---- one edge pass: DIF(pad Ptarg)'s last stages, the spectra's
-            // product (scaled) and the first DIT stages of u's transform
-            edge_pass_n(W, n2, [&](int k0, auto& x) {
-                constexpr int B = sizeof(x) / sizeof(x[0]);
-#pragma unroll
-                for (int i = 0; i < B; ++i) {
-                    const Cplx<float> v = c_mul(X[swz(k0 + i)], x[i]);
-                    x[i] = Cplx<float>{v.x * sc, v.y * sc};
-                }
-                dit_edge<float, B>(x);
-#pragma unroll
-                for (int i = 0; i < B; ++i) W[swz(k0 + i)] = x[i];
-            });
-            __syncthreads();
-            // ---- u = DIT(...): the last fused pass adds into the sums
-            block_dit_s_mid(W, n2, n2 >> 4);
-            for (int g = tid; g < S; g += RP_CONV_THREADS) {
-                Cplx<float> x[16];
-#pragma unroll
-                for (int i = 0; i < 16; ++i) x[i] = W[swz(g + i * S)];
-                dit16_regs(x, g, n2 >> 2);
-                if (MODE == 0) {
-#pragma unroll
-                    for (int i = 0; i < 16; ++i)
-                        if (g + i * S < N) { accr[i] += x[i].x; acci[i] += x[i].y; }
-                } else {
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        const int j = g + i * S;
-                        if (j < N) {
-                            C32 o = out[j];
-                            o.x += x[i].x;
-                            o.y += x[i].y;
-                            out[j] = o;
-                        }
-                    }
-                }
+            // ---- DIF(pad Ptarg)'s last stages and the spectra's product,
+            // added into the item's sum
+            switch (EB) {
+                case 16: spec_add<16>(W, X, U, n2); break;
+                case 8: spec_add<8>(W, X, U, n2); break;
+                case 4: spec_add<4>(W, X, U, n2); break;
+                default: spec_add<2>(W, X, U, n2); break;
             }
-            __syncthreads();
+            __syncthreads();    // X and W are read above; the next target overwrites them
         }
-        if (MODE == 0 && tid < S) {
+        // ---- the item's u = s / 2nr DIT(sum of the product spectra); the
+        // last fused pass writes the N values in natural order
+        switch (EB) {
+            case 16: spec_to_w<16>(W, U, n2, sc); break;
+            case 8: spec_to_w<8>(W, U, n2, sc); break;
+            case 4: spec_to_w<4>(W, U, n2, sc); break;
+            default: spec_to_w<2>(W, U, n2, sc); break;
+        }
+        __syncthreads();
+        block_dit_s_mid(W, n2, n2 >> 4);
+        for (int g = tid; g < S; g += RP_CONV_THREADS) {
+            Cplx<float> x[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) x[i] = W[swz(g + i * S)];
+            dit16_regs(x, g, n2 >> 2);
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
-                const int j = tid + i * S;
-                if (j < N) out[j] = C32{accr[i], acci[i]};
+                const int j = g + i * S;
+                if (j < N) out[j] = C32{x[i].x, x[i].y};
             }
         }
     }
@@ -1523,7 +1553,14 @@ int launch_pairs(const std::vector<Seg*>& ps, const PairJob* d_jobs, const PairJ
                  const unsigned int* d_start, unsigned int* d_work, unsigned int* seg_work, int cfg, int sms,
                  cudaStream_t st, rp_workspace* ws, bool par) {
     if (ps.size() > 1 && cfg >= 8) {
-        if (int rc = launch_pairs_multik(cfg - 8, h_jobs, (int)ps.size(), seg_work, sms, st)) return rc;
+        // the (sinc degree, frame kind) groups' launches run concurrently on
+        // the auxiliary streams, so one group's tail overlaps another's work
+        if (par) ws->fork(st);
+        const int rc = par ? launch_pairs_multik(cfg - 8, h_jobs, (int)ps.size(), seg_work, sms, st, ws->aux,
+                                                 rp_workspace::kAux)
+                           : launch_pairs_multik(cfg - 8, h_jobs, (int)ps.size(), seg_work, sms, st);
+        if (par) ws->join(st);
+        if (rc) return rc;
         RP_LAUNCHED();
         return RP_OK;
     }
@@ -1735,8 +1772,8 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
             hc[m].push_back(seg_conv_args(*g));
             hcs[m].push_back(hcs[m].back() + (unsigned)(g->nb * g->nsplit));
             max_nr[m] = std::max(max_nr[m], g->sc->nr);
-            // shared memory: X and W (mode 0), X (mode 1), nothing (mode 2)
-            const size_t sx = m == 0 ? (size_t)(4 * g->sc->nr) : (m == 1 ? (size_t)(2 * g->sc->nr) : 0);
+            // shared memory: X, W and U (mode 0), the working buffer (mode 1), nothing (mode 2)
+            const size_t sx = m == 0 ? (size_t)(6 * g->sc->nr) : (m == 1 ? (size_t)(2 * g->sc->nr) : 0);
             csm[m] = std::max(csm[m], sx * sizeof(Cplx<float>));
         }
     }

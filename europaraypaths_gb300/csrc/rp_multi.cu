@@ -114,9 +114,11 @@ void (*pick_mk(int deg, bool ortho))(const PairJobTable, unsigned int*) {
     }
 }
 
-int launch_pairs_multik(int cfg, const PairJob* h_jobs, int njobs, unsigned int* work, int sms, cudaStream_t st) {
+int launch_pairs_multik(int cfg, const PairJob* h_jobs, int njobs, unsigned int* work, int sms, cudaStream_t st,
+                        const cudaStream_t* aux, int naux) {
     const size_t smem = pair_smem_bytes(RP_WIN_WIDE);
     std::vector<char> done(njobs, 0);
+    int nl = 0;     // launches so far (stream round robin)
     for (int a = 0; a < njobs; ++a) {
         if (done[a]) continue;
         const int deg = h_jobs[a].deg;
@@ -138,8 +140,10 @@ int launch_pairs_multik(int cfg, const PairJob* h_jobs, int njobs, unsigned int*
             }
             if (n > 0 && (n == RP_MAXJ || b == njobs)) {
                 T.njobs = n;
-                mk<<<dim3((unsigned)(std::max(occ, 1) * sms), (unsigned)n), RP_PAIR_THREADS, smem, st>>>(T, work);
+                const cudaStream_t ls = naux > 0 ? aux[nl % naux] : st;
+                mk<<<dim3((unsigned)(std::max(occ, 1) * sms), (unsigned)n), RP_PAIR_THREADS, smem, ls>>>(T, work);
                 RP_CUDA(cudaGetLastError());
+                ++nl;
                 n = 0;
             }
         }

@@ -1335,8 +1335,13 @@ int launch_pairs_multi(int cfg, const PairJob* d_jobs, const unsigned int* d_sta
 
 // Launches of the per-kind multi-job kernels k_pairs32mk (rp_multi.cu), one
 // per (sinc degree, frame kind) group of h_jobs (host copies); work[j] is
-// job j's counter; cfg 0: 3 facet pairs per step, 1: 4.
-int launch_pairs_multik(int cfg, const PairJob* h_jobs, int njobs, unsigned int* work, int sms, cudaStream_t st);
+// job j's counter; cfg 0: 3 facet pairs per step, 1: 4.  With naux > 0 the
+// launches go round robin to the streams aux[0 .. naux), so the groups run
+// concurrently and one group's tail is filled by another's blocks (the
+// caller forks those streams from its own and joins them back); else all
+// on st.
+int launch_pairs_multik(int cfg, const PairJob* h_jobs, int njobs, unsigned int* work, int sms, cudaStream_t st,
+                        const cudaStream_t* aux = nullptr, int naux = 0);
 
 // Launch of the specular-mode pair kernel k_pairs32s (rp_spec.cu) of sinc
 // degree deg in configuration cfg (0 or 1) over items work items.
