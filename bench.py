@@ -505,6 +505,71 @@ def run_focus(Nr=4096, Na=2000):
     return line
 
 
+class CompletionClock:
+    """Records when each submitted request finishes, so that the latency
+    tail can be set against the requests' sizes.  A thread polls the pending
+    requests every millisecond (``done()`` is a zero-wait poll); callers read
+    the results only after ``finish()``, so no request is polled from two
+    threads."""
+
+    def __init__(self):
+        self.pending, self.done = [], []
+        self.lock = threading.Lock()
+        self.stop = False
+        self.thread = threading.Thread(target=self._run, daemon=True)
+        self.thread.start()
+
+    def add(self, req):
+        with self.lock:
+            self.pending.append((req, time.perf_counter()))
+
+    def _run(self):
+        while not self.stop:
+            with self.lock:
+                keep = []
+                for req, t0 in self.pending:
+                    if req.done():
+                        self.done.append((req, 1e3 * (time.perf_counter() - t0)))
+                    else:
+                        keep.append((req, t0))
+                self.pending = keep
+            time.sleep(0.001)
+
+    def finish(self, timeout):
+        t_end = time.perf_counter() + timeout
+        while time.perf_counter() < t_end:
+            with self.lock:
+                if not self.pending:
+                    break
+            time.sleep(0.01)
+        self.stop = True
+        self.thread.join()
+
+    def tail(self):
+        """Latency against request size over the requests that completed:
+        the rank correlation of latency with pairs, and the mean pairs and
+        traces of the slowest 1% and 10% of requests against all of them."""
+        from europaraypaths_gb300 import opcount
+        ok = [(opcount.pairs(r.counts), r.counts.shape[0], lat) for r, lat in self.done if r.status == 0]
+        if len(ok) < 10:
+            return None
+        pairs = np.array([a for a, _, _ in ok], np.float64)
+        ntr = np.array([b for _, b, _ in ok], np.float64)
+        lat = np.array([c for _, _, c in ok], np.float64)
+        rho = float(np.corrcoef(np.argsort(np.argsort(pairs)), np.argsort(np.argsort(lat)))[0, 1])
+        order = np.argsort(lat)
+        k1, k10 = max(1, len(ok) // 100), max(1, len(ok) // 10)
+        return {"requests": len(ok), "spearman_latency_vs_pairs": rho,
+                "mean_pairs": float(pairs.mean()), "mean_traces": float(ntr.mean()),
+                "slowest_1pct": {"mean_pairs": float(pairs[order[-k1:]].mean()),
+                                 "mean_traces": float(ntr[order[-k1:]].mean()),
+                                 "mean_ms": float(lat[order[-k1:]].mean())},
+                "slowest_10pct": {"mean_pairs": float(pairs[order[-k10:]].mean()),
+                                  "mean_traces": float(ntr[order[-k10:]].mean()),
+                                  "mean_ms": float(lat[order[-k10:]].mean())},
+                "note": "submit-to-completion on the host, 1 ms polling"}
+
+
 def run_serving(args, objs, tracks, plain_value):
     """The serving loop: Poisson arrivals of flyby requests over the resident
     scenes (a scene drawn uniformly, 1-8 consecutive interior traces), served
@@ -516,6 +581,7 @@ def run_serving(args, objs, tracks, plain_value):
     n_req = int(args.serve_rate * args.serve_seconds)
     gaps = rng.exponential(1.0 / args.serve_rate, n_req)
     reqs = []
+    clock = CompletionClock()
     t_start = time.perf_counter()
     t_next = t_start
     for g in gaps:
@@ -527,10 +593,14 @@ def run_serving(args, objs, tracks, plain_value):
         ns = tracks[i].shape[0]
         n = int(rng.integers(1, 9))
         lo = ns // 4 + int(rng.integers(0, max(ns // 2 - n, 1)))
-        reqs.append(srv.submit(sids[i], tracks[i][lo:lo + n]))
+        r = srv.submit(sids[i], tracks[i][lo:lo + n])
+        reqs.append(r)
+        clock.add(r)
+    clock.finish(600)
     for r in reqs:
         r.result(timeout=600)
     st = srv.stats()
+    st["latency_vs_size"] = clock.tail()
     srv.close(keep_scenes=True)
     st.update({"requests": n_req, "rate_req_s": args.serve_rate, "arrival_window_s": args.serve_seconds,
                "workers": 4, "request": "uniform scene of the uneven-scenes workload, 1-8 interior traces",
@@ -556,6 +626,7 @@ def run_serving_flybys(args, objs, tracks, plain_value):
     n_req = int(args.serve_rate * args.flyby_serve_seconds)
     gaps = rng.exponential(1.0 / args.serve_rate, n_req)
     reqs, offered_traces = [], 0
+    clock = CompletionClock()
     t_start = time.perf_counter()
     t_next = t_start
     for g in gaps:
@@ -568,8 +639,10 @@ def run_serving_flybys(args, objs, tracks, plain_value):
         n = min(int(rng.integers(50, 2001)), ns)
         lo = int(rng.integers(0, ns - n + 1))
         reqs.append((n, srv.submit(sids[i], tracks[i][lo:lo + n])))
+        clock.add(reqs[-1][1])
         offered_traces += n
     t_arrivals = time.perf_counter() - t_start
+    clock.finish(900)
     served_traces, shed = 0, 0
     for n, r in reqs:
         try:
@@ -579,6 +652,7 @@ def run_serving_flybys(args, objs, tracks, plain_value):
             shed += 1
     t_done = time.perf_counter() - t_start
     st = srv.stats()
+    st["latency_vs_size"] = clock.tail()
     srv.close(keep_scenes=True)
     st.update({"requests": n_req, "rate_req_s": args.serve_rate, "arrival_window_s": t_arrivals,
                "drained_after_s": t_done, "workers": 4, "step_traces": 16, "max_active": 16,

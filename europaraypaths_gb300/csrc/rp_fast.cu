@@ -45,6 +45,7 @@
 #define RP_CONV_SPLIT 64       // targets per range-compression work item (fixed:
                                // a trace's sum order never depends on the batch)
 #define RP_CONV_THREADS 512
+#define RP_CONV_CHUNK 16384    // mode 2: elements of the shared-memory buffer (128 KiB)
 
 using namespace rpk;
 
@@ -693,10 +694,11 @@ __device__ __forceinline__ void edge_pass(const Cplx<float>* src, int n, Op op) 
     }
 }
 
-// The edge pass for the block size of length n (16, 2, 4 or 8).
+// The edge pass for the block size of length n (16, 2, 4 or 8), or eb when
+// src holds sub-blocks of a longer transform.
 template <class Op>
-__device__ __forceinline__ void edge_pass_n(const Cplx<float>* src, int n, Op op) {
-    switch (edge_block(n)) {
+__device__ __forceinline__ void edge_pass_n(const Cplx<float>* src, int n, Op op, int eb = 0) {
+    switch (eb ? eb : edge_block(n)) {
         case 16: edge_pass<16>(src, n, op); break;
         case 8: edge_pass<8>(src, n, op); break;
         case 4: edge_pass<4>(src, n, op); break;
@@ -848,9 +850,82 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
         const float inv = 1.f / (float)n2;
         const float sc = sig_scale / (float)n2;
         const int EB = edge_block(n2);
+        const int SB = n2 >> 4;                 // mode 2: sub-block of the inner stages
+        const bool blocked = MODE == 2 && SB <= RP_CONV_CHUNK;
         for (int q = q0; q < q1; ++q) {
             const int b0 = bt0[(size_t)s * tstride + q];
             const size_t qbase = ((size_t)s * tstride + q) * Wt;
+            if (blocked) {
+                // ---- mode 2 by sub-blocks: the stages of spans <= n / 16
+                // act within contiguous sub-blocks of SB = n / 16 elements,
+                // so they run in shared memory, RP_CONV_CHUNK elements at a
+                // time; only the outer fused passes (spans n, n / 4) go to
+                // the global slot.  P1: the first DIF pass from the rows
+                for (int g = tid; g < S; g += RP_CONV_THREADS) {
+                    Cplx<float> x[16];
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) x[i] = trace_at(T, pstride, qbase, g + i * S, b0, Wt, nr);
+                    dif16_regs(x, g, n2);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) W[swz(g + i * S)] = x[i];
+                }
+                __syncthreads();
+                // P2, per chunk: the rest of DIF(pad T), X stored, the
+                // product with C2, the DIT stages of spans <= SB
+                for (int c0 = 0; c0 < n2; c0 += RP_CONV_CHUNK) {
+                    for (int k = tid; k < RP_CONV_CHUNK; k += RP_CONV_THREADS) sbase[k] = W[c0 + k];
+                    __syncthreads();
+                    block_dif_s_mid(sbase, RP_CONV_CHUNK, SB);
+                    Cplx<float>* const Xc = X + c0;
+                    const Cplx<float>* const Cc = C2s + c0;
+                    edge_pass_n(sbase, RP_CONV_CHUNK, [&](int k0, auto& x) {
+                        constexpr int B = sizeof(x) / sizeof(x[0]);
+#pragma unroll
+                        for (int i = 0; i < B; ++i) {
+                            Xc[swz(k0 + i)] = x[i];
+                            x[i] = c_mul(x[i], Cc[k0 + i]);
+                        }
+                        dit_edge<float, B>(x);
+#pragma unroll
+                        for (int i = 0; i < B; ++i) sbase[swz(k0 + i)] = x[i];
+                    }, EB);
+                    __syncthreads();
+                    block_dit_s_mid(sbase, RP_CONV_CHUNK, SB >> 2, EB);
+                    for (int k = tid; k < RP_CONV_CHUNK; k += RP_CONV_THREADS) W[c0 + k] = sbase[k];
+                    __syncthreads();
+                }
+                // P3: the last DIT pass, the shift, the first DIF pass (global)
+                for (int g = tid; g < S; g += RP_CONV_THREADS) {
+                    Cplx<float> x[16];
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) x[i] = W[swz(g + i * S)];
+                    dit16_regs(x, g, n2 >> 2);
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) x[i] = Cplx<float>{x[i + 4].x * inv, x[i + 4].y * inv};
+#pragma unroll
+                    for (int i = 8; i < 16; ++i) x[i] = Cplx<float>{0.f, 0.f};
+                    dif16_regs(x, g, n2);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) W[swz(g + i * S)] = x[i];
+                }
+                __syncthreads();
+                if constexpr (SPEC) dif_trace(X, T2, pstride, qbase, b0, Wt, nr, n2, false);
+                // P4, per chunk: the rest of DIF(pad Ptarg) and the product
+                // with X, added into U
+                for (int c0 = 0; c0 < n2; c0 += RP_CONV_CHUNK) {
+                    for (int k = tid; k < RP_CONV_CHUNK; k += RP_CONV_THREADS) sbase[k] = W[c0 + k];
+                    __syncthreads();
+                    block_dif_s_mid(sbase, RP_CONV_CHUNK, SB);
+                    switch (EB) {
+                        case 16: spec_add<16>(sbase, X + c0, U + c0, RP_CONV_CHUNK); break;
+                        case 8: spec_add<8>(sbase, X + c0, U + c0, RP_CONV_CHUNK); break;
+                        case 4: spec_add<4>(sbase, X + c0, U + c0, RP_CONV_CHUNK); break;
+                        default: spec_add<2>(sbase, X + c0, U + c0, RP_CONV_CHUNK); break;
+                    }
+                    __syncthreads();
+                }
+                continue;
+            }
             // ---- X = DIF(pad T) up to its edge block (mode 1: in W's
             // shared memory), then one edge pass: the last DIF stages, X
             // stored (mode 1: parked in the slot), W = X * C2 and the first
@@ -903,14 +978,29 @@ k_conv32s(const ConvArgs* __restrict__ jobs, const unsigned int* __restrict__ st
         }
         // ---- the item's u = s / 2nr DIT(sum of the product spectra); the
         // last fused pass writes the N values in natural order
-        switch (EB) {
-            case 16: spec_to_w<16>(W, U, n2, sc); break;
-            case 8: spec_to_w<8>(W, U, n2, sc); break;
-            case 4: spec_to_w<4>(W, U, n2, sc); break;
-            default: spec_to_w<2>(W, U, n2, sc); break;
+        if (blocked) {
+            for (int c0 = 0; c0 < n2; c0 += RP_CONV_CHUNK) {
+                switch (EB) {
+                    case 16: spec_to_w<16>(sbase, U + c0, RP_CONV_CHUNK, sc); break;
+                    case 8: spec_to_w<8>(sbase, U + c0, RP_CONV_CHUNK, sc); break;
+                    case 4: spec_to_w<4>(sbase, U + c0, RP_CONV_CHUNK, sc); break;
+                    default: spec_to_w<2>(sbase, U + c0, RP_CONV_CHUNK, sc); break;
+                }
+                __syncthreads();
+                block_dit_s_mid(sbase, RP_CONV_CHUNK, SB >> 2, EB);
+                for (int k = tid; k < RP_CONV_CHUNK; k += RP_CONV_THREADS) W[c0 + k] = sbase[k];
+                __syncthreads();
+            }
+        } else {
+            switch (EB) {
+                case 16: spec_to_w<16>(W, U, n2, sc); break;
+                case 8: spec_to_w<8>(W, U, n2, sc); break;
+                case 4: spec_to_w<4>(W, U, n2, sc); break;
+                default: spec_to_w<2>(W, U, n2, sc); break;
+            }
+            __syncthreads();
+            block_dit_s_mid(W, n2, n2 >> 4);
         }
-        __syncthreads();
-        block_dit_s_mid(W, n2, n2 >> 4);
         for (int g = tid; g < S; g += RP_CONV_THREADS) {
             Cplx<float> x[16];
 #pragma unroll
@@ -1772,8 +1862,9 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
             hc[m].push_back(seg_conv_args(*g));
             hcs[m].push_back(hcs[m].back() + (unsigned)(g->nb * g->nsplit));
             max_nr[m] = std::max(max_nr[m], g->sc->nr);
-            // shared memory: X, W and U (mode 0), the working buffer (mode 1), nothing (mode 2)
-            const size_t sx = m == 0 ? (size_t)(6 * g->sc->nr) : (m == 1 ? (size_t)(2 * g->sc->nr) : 0);
+            // shared memory: X, W and U (mode 0), the working buffer (mode 1), the
+            // sub-block buffer (mode 2)
+            const size_t sx = m == 0 ? (size_t)(6 * g->sc->nr) : (m == 1 ? (size_t)(2 * g->sc->nr) : RP_CONV_CHUNK);
             csm[m] = std::max(csm[m], sx * sizeof(Cplx<float>));
         }
     }

@@ -420,11 +420,12 @@ __device__ __forceinline__ void block_dif_s_mid(Cplx<T>* a, int n, int L0) {
 }
 
 // DIT fused passes of spans between the edge block's (exclusive) and Lmax
-// (inclusive): from 64, 8, 16, 32 for edge blocks 16, 2, 4, 8.  Ends with a
-// barrier when it ran a pass.
+// (inclusive): from 64, 8, 16, 32 for edge blocks 16, 2, 4, 8.  B: the edge
+// block of the whole transform when a holds only sub-blocks of it (0: that
+// of length n).  Ends with a barrier when it ran a pass.
 template <class T>
-__device__ __forceinline__ void block_dit_s_mid(Cplx<T>* a, int n, int Lmax) {
-    const int B = edge_block(n);
+__device__ __forceinline__ void block_dit_s_mid(Cplx<T>* a, int n, int Lmax, int B = 0) {
+    if (B == 0) B = edge_block(n);
     const int L0 = B == 16 ? 64 : 4 * B;
     for (int L = L0, lL = fft_log2(L0); L <= Lmax; L <<= 4, lL += 4) {
         const int lS = lL - 2, S = 1 << lS;

@@ -89,11 +89,13 @@ def test_fast_polynomial_sinc_regimes(built_lib, oracle, nside):
     check(got, ref)
 
 
-@pytest.mark.parametrize("nr", [4096, 8192, 16384, 6000])
+@pytest.mark.parametrize("nr", [4096, 8192, 16384, 32768, 6000])
 def test_fast_vhf_band(built_lib, oracle, nr):
-    # compression storage modes: 4096 bins all in shared memory, 8192 the
-    # product spectrum in global scratch, 16384 both buffers in global
-    # scratch, 6000 (not a power of two) the Bluestein kernel
+    # compression storage modes: 4096 bins all in shared memory, 8192 one
+    # transform buffer in shared memory with X parked in global scratch,
+    # 16384 and 32768 the transforms in global scratch with their inner
+    # stages (sub-blocks of 2048 and 4096 values) in shared memory, 6000 (not
+    # a power of two) the Bluestein kernel
     sc = vhf_scene(nr)
     got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle)
     assert got.shape[1] == nr

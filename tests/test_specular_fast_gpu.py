@@ -97,10 +97,11 @@ def test_fast_specular_non_pow2_bins(built_lib, oracle):
     assert got.shape[1] == 250
 
 
-@pytest.mark.parametrize("nr", [4096, 8192])
+@pytest.mark.parametrize("nr", [4096, 8192, 16384])
 def test_fast_specular_vhf_band(built_lib, oracle, nr):
     # 60 MHz, 2.5 m facets: degree-6 gain polynomial, reradiation arguments up
-    # to pi/2; 8192 bins: the product spectrum in global scratch
+    # to pi/2; 8192 bins: one transform buffer in shared memory, 16384: the
+    # transforms in global scratch by shared-memory sub-blocks
     from helpers import vhf_scene
     sc = vhf_scene(nr)
     sc["params"].update({"specular": True, "rerad_funct": 0})
