@@ -7,8 +7,12 @@ surface, Hurst 0.8, RMS 5 m), a rough interface 1.5 km deep sampled as
 9 MHz / 1 MHz chirp sampled at 4 MHz into 4096 range bins, aperture 3 deg.
 All inputs are seeded synthetic data (no public dataset is involved).
 
-A step is one call over a batch of consecutive flyby traces (default 8); the
-K timed steps walk along the track.  ``value`` is pairs/s with the scene and
+A step is one call over a batch of consecutive flyby traces (default 40); the
+K timed steps walk along the track.  A call's pair-kernel work items are
+traces x target blocks x 4 facet parts, taken by a persistent grid of 304
+blocks; at 40 traces (5760 items, 18.95 rounds of the grid) the last round
+is nearly full, where 8 traces (1152 items, 3.79 rounds) leave a fifth of
+the grid idle in theirs.  ``value`` is pairs/s with the scene and
 trace tables already resident on the device (pairs = sum over traces of
 N_ill * (1 + 2 N_t), counted exactly by the kernels); ``e2e`` is the same
 metric through the public C ABI call ``rp_simulate`` with pinned host trace
@@ -712,7 +716,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--traces-per-step", type=int, default=8)
+    ap.add_argument("--traces-per-step", type=int, default=40,
+                    help="traces per call: 40 x 36 target blocks x 4 facet parts = 5760 pair-kernel items, "
+                         "18.95 rounds of the 304-block persistent grid")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--plain-traces", type=int, default=1, help="traces for the plain FP64 form (0 = skip)")
     ap.add_argument("--cpu-targets", type=int, default=48, help="target cap of the CPU baseline sample")
@@ -845,9 +851,9 @@ def main():
                 "achieved": fp32_rate / 1e12, "peak": fp32_peak / 1e12,
                 "unit": "T FP32 lane-operations/s",
                 "frac": fp32_rate / fp32_peak if fp32_peak else None,
-                # DRAM read+write of one launch from the committed ncu capture (2 traces: 276.2 + 36.2
+                # DRAM read+write of one launch from the committed ncu capture (2 traces: 340.4 + 82.4
                 # MB), scaled by the traces per launch; the kernel is compute-bound (DRAM < 0.1 % of peak)
-                "traffic": 312.4e6 * tps / 2.0,
+                "traffic": 422.8e6 * tps / 2.0,
                 "traffic_unit": "bytes per launch (ncu, profiles/k_pairs32_large_scene.md, scaled)",
                 "peak_source": (f"nominal {opcount.FP32_FMA_PER_CLK_PER_SM} FP32 lanes/clk/SM x {n_sm} SMs x "
                                 f"{sm_mhz:.0f} MHz median SM clock under load; MEASURED_PEAKS.json holds HBM "

@@ -59,7 +59,9 @@ int rp_cuda_fail(cudaError_t e, const char* what) {
 int rp_allow_dyn_smem(const void* fn, size_t bytes) {
     static std::mutex mu;
     static std::map<std::pair<int, const void*>, size_t> cur;
-    if (bytes <= (48u << 10)) return RP_OK;
+    // the 48 KiB allowed without the attribute covers static and dynamic
+    // shared memory together, so any dynamic size sets it
+    if (bytes == 0) return RP_OK;
     int dev = 0;
     RP_CUDA(cudaGetDevice(&dev));
     std::lock_guard<std::mutex> lk(mu);

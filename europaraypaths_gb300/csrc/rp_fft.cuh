@@ -246,6 +246,7 @@ __device__ __forceinline__ void dit16_regs(Cplx<T> (&x)[16], int b, int L) {
 template <class T>
 __device__ __forceinline__ void block_dif_s_from(Cplx<T>* a, int n, int L0) {
     int L = L0, lL = fft_log2(L0);
+#pragma unroll
     for (; L >= 16; L >>= 4, lL -= 4) {
         const int lS = lL - 4, S = 1 << lS;
         for (int g = threadIdx.x; g < (n >> 4); g += blockDim.x) {
@@ -319,6 +320,7 @@ __device__ __forceinline__ void block_dit_s_upto(Cplx<T>* a, int n, int Lmax) {
         L <<= 2;
         lL += 2;
     }
+#pragma unroll
     for (; L <= Lmax; L <<= 4, lL += 4) {
         const int lS = lL - 2, S = 1 << lS;
         for (int g = threadIdx.x; g < (n >> 4); g += blockDim.x) {
@@ -403,6 +405,7 @@ __device__ __forceinline__ void dit_edge(Cplx<T> (&x)[B]) {
 // Ends with a barrier when it ran a pass.
 template <class T>
 __device__ __forceinline__ void block_dif_s_mid(Cplx<T>* a, int n, int L0) {
+#pragma unroll
     for (int L = L0, lL = fft_log2(L0); L > 16; L >>= 4, lL -= 4) {
         const int lS = lL - 4, S = 1 << lS;
         for (int g = threadIdx.x; g < (n >> 4); g += blockDim.x) {
@@ -427,6 +430,7 @@ template <class T>
 __device__ __forceinline__ void block_dit_s_mid(Cplx<T>* a, int n, int Lmax, int B = 0) {
     if (B == 0) B = edge_block(n);
     const int L0 = B == 16 ? 64 : 4 * B;
+#pragma unroll
     for (int L = L0, lL = fft_log2(L0); L <= Lmax; L <<= 4, lL += 4) {
         const int lS = lL - 2, S = 1 << lS;
         for (int g = threadIdx.x; g < (n >> 4); g += blockDim.x) {

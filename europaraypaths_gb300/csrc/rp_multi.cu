@@ -114,38 +114,53 @@ void (*pick_mk(int deg, bool ortho))(const PairJobTable, unsigned int*) {
     }
 }
 
+// Estimated duration of one work item of a job: its facet-part capacity
+// times the targets of a full target block (host bounds of the wave).
+static double item_cost(const PairJob& j) {
+    const double tpb = (double)std::min<int64_t>(j.a.tstride, RP_PAIR_THREADS);
+    return (double)j.a.rstride / RP_PARTS * tpb;
+}
+
 int launch_pairs_multik(int cfg, const PairJob* h_jobs, int njobs, unsigned int* work, int sms, cudaStream_t st,
                         const cudaStream_t* aux, int naux) {
     const size_t smem = pair_smem_bytes(RP_WIN_WIDE);
-    std::vector<char> done(njobs, 0);
+    // the (sinc degree, frame kind) groups, each's jobs by decreasing item
+    // cost: a launch's blocks take its jobs in order, so the launch ends on
+    // the jobs with the shortest items, not on a large scene's last items;
+    // the groups with the most work are launched first
+    struct Kind { int deg; bool ortho; double work; std::vector<int> jobs; };
+    std::vector<Kind> kinds;
+    for (int b = 0; b < njobs; ++b) {
+        const int deg = h_jobs[b].deg;
+        const bool ortho = h_jobs[b].ortho != 0;
+        size_t k = 0;
+        while (k < kinds.size() && !(kinds[k].deg == deg && kinds[k].ortho == ortho)) ++k;
+        if (k == kinds.size()) kinds.push_back(Kind{deg, ortho, 0.0, {}});
+        kinds[k].jobs.push_back(b);
+        kinds[k].work += item_cost(h_jobs[b]) * (double)h_jobs[b].a.nb * h_jobs[b].a.tblocks;
+    }
+    std::stable_sort(kinds.begin(), kinds.end(), [](const Kind& x, const Kind& y) { return x.work > y.work; });
     int nl = 0;     // launches so far (stream round robin)
-    for (int a = 0; a < njobs; ++a) {
-        if (done[a]) continue;
-        const int deg = h_jobs[a].deg;
-        const bool ortho = h_jobs[a].ortho != 0;
-        auto mk = (cfg & 1) ? pick_mk<4>(deg, ortho) : pick_mk<3>(deg, ortho);
+    for (Kind& K : kinds) {
+        std::stable_sort(K.jobs.begin(), K.jobs.end(),
+                         [&](int x, int y) { return item_cost(h_jobs[x]) > item_cost(h_jobs[y]); });
+        auto mk = (cfg & 1) ? pick_mk<4>(K.deg, K.ortho) : pick_mk<3>(K.deg, K.ortho);
         if (int rc = rp_allow_dyn_smem((const void*)mk, smem)) return rc;
         int occ = 0;
         RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mk, RP_PAIR_THREADS, smem));
-        // the jobs of this kind, RP_MAXJ per launch
-        PairJobTable T;
-        int n = 0;
-        for (int b = a; b <= njobs; ++b) {
-            const bool take = b < njobs && !done[b] && h_jobs[b].deg == deg && (h_jobs[b].ortho != 0) == ortho;
-            if (take) {
-                T.job[n] = h_jobs[b];
-                T.wi[n] = b;
-                done[b] = 1;
-                ++n;
+        // the kind's jobs, RP_MAXJ per launch
+        for (size_t j0 = 0; j0 < K.jobs.size(); j0 += RP_MAXJ) {
+            PairJobTable T;
+            const int n = (int)std::min<size_t>(RP_MAXJ, K.jobs.size() - j0);
+            for (int i = 0; i < n; ++i) {
+                T.job[i] = h_jobs[K.jobs[j0 + i]];
+                T.wi[i] = K.jobs[j0 + i];
             }
-            if (n > 0 && (n == RP_MAXJ || b == njobs)) {
-                T.njobs = n;
-                const cudaStream_t ls = naux > 0 ? aux[nl % naux] : st;
-                mk<<<dim3((unsigned)(std::max(occ, 1) * sms), (unsigned)n), RP_PAIR_THREADS, smem, ls>>>(T, work);
-                RP_CUDA(cudaGetLastError());
-                ++nl;
-                n = 0;
-            }
+            T.njobs = n;
+            const cudaStream_t ls = naux > 0 ? aux[nl % naux] : st;
+            mk<<<dim3((unsigned)(std::max(occ, 1) * sms), (unsigned)n), RP_PAIR_THREADS, smem, ls>>>(T, work);
+            RP_CUDA(cudaGetLastError());
+            ++nl;
         }
     }
     return RP_OK;

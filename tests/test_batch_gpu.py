@@ -26,6 +26,8 @@ def _scenes():
         tiny_scene(nside=148, ntside=3, ns=2),                                       # fs 13.5 m: degree-6 sinc
         tiny_scene(nside=30, ntside=4, ns=4, rx_window_m=scenes.rx_window_for_bins(512, 4e6),
                    rx_window_offset_m=24200.0),                                      # 512 bins
+        tiny_scene(nside=30, ntside=3, ns=2,
+                   rx_window_m=scenes.rx_window_for_bins(8192, 4e6)),                # 8192 bins (mode 1)
     ]
 
 
