@@ -353,7 +353,22 @@ static int build_tables(rp_scene* s) {
         const double tres = s->dp.specular ? p.rng_res : 2 * p.rng_res;
         std::vector<Cplx<double>> c2(n2), h(M, Cplx<double>{0, 0});
         for (int i = 0; i < n2; ++i) c2[i] = Cplx<double>{host_sinc((double)(i - nr / 2) * p.dr / tres), 0.0};
-        host_dif(c2.data(), n2, f, lM);
+        if (n2 == 2 * RP_CONV_CHUNK) {
+            // the compression runs these transforms by halves: DIF_n's first
+            // (span-n radix-2) stage, then DIF of each half of length nr
+            for (int e = 0; e < nr; ++e) {
+                const Cplx<double> a = c2[e], b = c2[e + nr];
+                const Cplx<double> d{a.x - b.x, a.y - b.y};
+                const double ang = -2.0 * RP_PI * e / n2;
+                const double cw = std::cos(ang), sw = std::sin(ang);
+                c2[e] = Cplx<double>{a.x + b.x, a.y + b.y};
+                c2[e + nr] = Cplx<double>{d.x * cw - d.y * sw, d.x * sw + d.y * cw};
+            }
+            host_dif(c2.data(), nr, f, lM);
+            host_dif(c2.data() + nr, nr, f, lM);
+        } else {
+            host_dif(c2.data(), n2, f, lM);
+        }
         // cropSpectrum followed by the inverse N-point DFT is a circular
         // convolution with h[n] = (1/N) sum_{min(k,N-k) <= K} e^{2 pi i k n / N}
         // = sin(pi (2K+1) n / N) / (N sin(pi n / N)) (the Dirichlet kernel of

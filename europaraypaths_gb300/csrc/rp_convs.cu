@@ -121,6 +121,50 @@ __device__ __forceinline__ void spec_to_w(Cplx<float>* W, const Cplx<float>* U, 
     }
 }
 
+// W^e = e^{-2 pi i e / n} for 0 <= e < n / 2, from the SFU at angles of
+// at most pi / 2 (W^e = -i W^{e - n/4} above n / 4).
+__device__ __forceinline__ Cplx<float> tw_half(int e, int n) {
+    const int q = n >> 2;
+    const bool hi = e >= q;
+    const Cplx<float> w = tw_sfu<float>(hi ? e - q : e, 6.28318530717958647f / (float)n);
+    return hi ? Cplx<float>{w.y, -w.x} : w;
+}
+
+// The first fused DIF pass of one half of a length-n transform whose input
+// has its upper half zero (a zero-padded trace): half 0 transforms x, half 1
+// x W^e (the span-n radix-2 stage of DIF_n is then a plain split), each as a
+// length-H = n / 2 transform.  get(e) gives x[e], e < H.  Into a (swizzled).
+template <class Get>
+__device__ __forceinline__ void half_first_pass(Cplx<float>* a, int H, int h, Get get) {
+    const int SH = H >> 4;
+    for (int g = threadIdx.x; g < SH; g += RP_CONV_THREADS) {
+        Cplx<float> x[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int e = g + i * SH;
+            const Cplx<float> v = get(e);
+            x[i] = h ? c_mul(v, tw_half(e, 2 * H)) : v;
+        }
+        dif16_regs(x, g, H);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) a[swz(g + i * SH)] = x[i];
+    }
+}
+
+// The last fused DIT pass of a length-H transform: natural-order outputs,
+// unscaled, into dst (swizzled; dst may be a).
+__device__ __forceinline__ void half_last_dit(const Cplx<float>* a, Cplx<float>* dst, int H) {
+    const int SH = H >> 4;
+    for (int g = threadIdx.x; g < SH; g += RP_CONV_THREADS) {
+        Cplx<float> x[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) x[i] = a[swz(g + i * SH)];
+        dit16_regs(x, g, H >> 2);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) dst[swz(g + i * SH)] = x[i];
+    }
+}
+
 // One work item of k_conv32s (below).  NC: the transform length 2nr
 // as a compile-time constant for the common lengths (0: the job's, at run
 // time), so the passes' strides, twiddle steps and loop trip counts fold.
@@ -160,9 +204,94 @@ __device__ __forceinline__ void conv_item(const ConvArgs& A, unsigned int item, 
     const int EB = edge_block(n2);
     const int SB = n2 >> 4;                 // mode 2: sub-block of the inner stages
     const bool blocked = MODE == 2 && SB <= RP_CONV_CHUNK;
+    // mode 2 at 2nr = 2 RP_CONV_CHUNK runs by halves (below); its spectra
+    // (the chirp's C2s included) are in the halves' order
+    constexpr bool HALVES = MODE == 2 && NC == 2 * RP_CONV_CHUNK;
+    constexpr int HH = RP_CONV_CHUNK;       // the half length
+    const int EBH = edge_block(HH);
     for (int q = q0; q < q1; ++q) {
         const int b0 = bt0[(size_t)s * tstride + q];
         const size_t qbase = ((size_t)s * tstride + q) * Wt;
+        if constexpr (HALVES) {
+            // ---- mode 2 at 2nr = 2 RP_CONV_CHUNK, by halves.  The input
+            // of every forward transform is a zero-padded trace, so DIF_n's
+            // first (span-n radix-2) stage splits it into x and x W^e, two
+            // independent length-H transforms run whole in shared memory;
+            // the spectra live in that split order ([DIF_H(x); DIF_H(x
+            // W^e)], the chirp's C2s included).  The inverse joins the two
+            // halves' DIT_H outputs a, b as y[e] = a[e] + W^-e b[e], y[e +
+            // H] = a[e] - W^-e b[e]; Ptarg needs y[nr/2 .. 3nr/2) only.
+            // Global slot: X (halves at 0 and H), then Wa (H values).
+            Cplx<float>* const Wa = gbase + n2;
+            const C32* __restrict__ Tr = T;
+            for (int h = 0; h < 2; ++h) {
+                half_first_pass(sbase, HH, h, [&](int e) { return trace_at(Tr, pstride, qbase, e, b0, Wt, nr); });
+                __syncthreads();
+                block_dif_s_mid(sbase, HH, HH >> 4);
+                Cplx<float>* const Xh = X + h * HH;
+                const Cplx<float>* const Ch = C2s + h * HH;
+                edge_pass_n(sbase, HH, [&](int k0, auto& x) {
+                    constexpr int B = sizeof(x) / sizeof(x[0]);
+#pragma unroll
+                    for (int i = 0; i < B; ++i) {
+                        Xh[swz(k0 + i)] = x[i];
+                        x[i] = c_mul(x[i], Ch[k0 + i]);
+                    }
+                    dit_edge<float, B>(x);
+#pragma unroll
+                    for (int i = 0; i < B; ++i) sbase[swz(k0 + i)] = x[i];
+                });
+                __syncthreads();
+                block_dit_s_mid(sbase, HH, HH >> 4);
+                half_last_dit(sbase, h == 0 ? Wa : sbase, HH);     // a to the slot, b in place
+                __syncthreads();
+            }
+            // Ptarg[k] = y[k + nr/2] / n: Ptarg[e] = a[e+Q] + W^-(e+Q) b[e+Q],
+            // Ptarg[e+Q] = a[e] - W^-e b[e] (Q = H / 2), into sbase and Wa
+            for (int e = tid; e < (HH >> 1); e += RP_CONV_THREADS) {
+                const int e1 = e + (HH >> 1);
+                const Cplx<float> a0 = Wa[swz(e)], a1 = Wa[swz(e1)];
+                const Cplx<float> t0 = c_mulc(sbase[swz(e)], tw_half(e, n2));
+                const Cplx<float> t1 = c_mulc(sbase[swz(e1)], tw_half(e1, n2));
+                const Cplx<float> lo{(a1.x + t1.x) * inv, (a1.y + t1.y) * inv};
+                const Cplx<float> hi{(a0.x - t0.x) * inv, (a0.y - t0.y) * inv};
+                sbase[swz(e)] = lo;
+                sbase[swz(e1)] = hi;
+                Wa[swz(e)] = lo;
+                Wa[swz(e1)] = hi;
+            }
+            __syncthreads();
+            if constexpr (SPEC) {
+                // Psour = s T2: its transform's halves replace X
+                const C32* __restrict__ T2r = T2;
+                for (int h = 0; h < 2; ++h) {
+                    half_first_pass(sbase, HH, h,
+                                    [&](int e) { return trace_at(T2r, pstride, qbase, e, b0, Wt, nr); });
+                    __syncthreads();
+                    block_dif_s_from(sbase, HH, HH >> 4);
+                    for (int k = tid; k < HH; k += RP_CONV_THREADS) X[h * HH + k] = sbase[k];
+                    __syncthreads();
+                }
+            }
+            // DIF(pad Ptarg) by halves, each's product with X added into U
+            for (int h = 0; h < 2; ++h) {
+                if (SPEC || h == 1) {
+                    half_first_pass(sbase, HH, h, [&](int e) { return Wa[swz(e)]; });
+                    __syncthreads();
+                    block_dif_s_mid(sbase, HH, HH >> 4);
+                } else {
+                    block_dif_s_mid(sbase, HH, HH);
+                }
+                switch (EBH) {
+                    case 16: spec_add<16>(sbase, X + h * HH, U + h * HH, HH); break;
+                    case 8: spec_add<8>(sbase, X + h * HH, U + h * HH, HH); break;
+                    case 4: spec_add<4>(sbase, X + h * HH, U + h * HH, HH); break;
+                    default: spec_add<2>(sbase, X + h * HH, U + h * HH, HH); break;
+                }
+                __syncthreads();
+            }
+            continue;
+        }
         if (blocked) {
             // ---- mode 2 by sub-blocks: the stages of spans <= n / 16
             // act within contiguous sub-blocks of SB = n / 16 elements,
@@ -286,6 +415,32 @@ __device__ __forceinline__ void conv_item(const ConvArgs& A, unsigned int item, 
     }
     // ---- the item's u = s / 2nr DIT(sum of the product spectra); the
     // last fused pass writes the N values in natural order
+    if constexpr (HALVES) {
+        // u = s / 2nr DIT(U) by halves: DIT_H of each half of U, then the
+        // join y[e] = a[e] + W^-e b[e], y[e + H] = a[e] - W^-e b[e] into
+        // the item's row (which held U: both halves are read before it is
+        // written)
+        Cplx<float>* const Wa = gbase + n2;
+        for (int h = 0; h < 2; ++h) {
+            for (int k = tid; k < HH; k += RP_CONV_THREADS) {
+                const Cplx<float> o = U[h * HH + k];
+                sbase[k] = Cplx<float>{o.x * sc, o.y * sc};
+            }
+            __syncthreads();
+            block_dit_s(sbase, HH);
+            if (h == 0) {
+                for (int k = tid; k < HH; k += RP_CONV_THREADS) Wa[k] = sbase[k];
+                __syncthreads();
+            }
+        }
+        for (int e = tid; e < HH; e += RP_CONV_THREADS) {
+            const Cplx<float> a = Wa[swz(e)];
+            const Cplx<float> t = c_mulc(sbase[swz(e)], tw_half(e, n2));
+            out[e] = C32{a.x + t.x, a.y + t.y};
+            if (e + HH < N) out[e + HH] = C32{a.x - t.x, a.y - t.y};
+        }
+        return;
+    }
     if (blocked) {
         for (int c0 = 0; c0 < n2; c0 += RP_CONV_CHUNK) {
             switch (EB) {

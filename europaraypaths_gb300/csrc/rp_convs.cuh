@@ -3,12 +3,12 @@
 #pragma once
 
 #include "rp_fft.cuh"
+#include "rp_internal.h"
 #include "rp_pair.cuh"
 
 #define RP_CONV_SPLIT 64       // targets per range-compression work item (fixed:
                                // a trace's sum order never depends on the batch)
 #define RP_CONV_THREADS 512
-#define RP_CONV_CHUNK 16384    // mode 2: elements of the shared-memory buffer (128 KiB)
 
 namespace rpk {
 

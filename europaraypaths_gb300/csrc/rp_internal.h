@@ -22,6 +22,11 @@
 
 // Polls of an mbarrier before a pair kernel's wait for a staged chunk gives
 // up (RP_ERR_TIMEOUT), and the short limit of the stalled-copy test mode.
+// Elements of the range compression's shared-memory transform buffer (128
+// KiB): mode 2 runs its sub-blocks, or at 2nr = 2 RP_CONV_CHUNK its two
+// halves, in it (rp_convs.cu); the chirp spectrum of such a scene is stored
+// in the halves' order.
+#define RP_CONV_CHUNK 16384
 #define RP_SPIN_LIMIT (1 << 22)
 #define RP_SPIN_LIMIT_TEST 4096
 
