@@ -99,6 +99,11 @@ _SIGS = {
                           ctypes.c_void_p], ctypes.c_int),
     "rp_server_destroy": ([ctypes.c_void_p], ctypes.c_int),
     "rp_server_configure": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "rp_graph_create": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                         ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "rp_graph_launch": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rp_graph_check": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rp_graph_destroy": ([ctypes.c_void_p], ctypes.c_int),
     "rp_submit": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rp_poll": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int], ctypes.c_int),

@@ -642,6 +642,132 @@ extern "C" int rp_simulate_device(rp_scene* s, const double* d_traces, int64_t n
     return run_form(s, &s->ws, d_traces, ns, form, d_out, counts, st);
 }
 
+// ------------------------------------------------------------ graphs --
+// A fast-form call recorded as a CUDA graph (rp_graph_create): planned from
+// the host copy of its traces, its target windows sized by host bounds, run
+// once eagerly (which reserves the buffers and tunes the pair kernel), then
+// run again under stream capture into a graph that replays the whole call --
+// setup, pair stage, compression, tails -- with one launch.  The graph owns
+// its workspace (device buffers, auxiliary streams, the pinned staging of its
+// job tables and of the flags and counts it reads back).
+struct rp_graph {
+    rp_scene* s = nullptr;
+    rp_workspace ws;
+    cudaStream_t st = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t ns = 0;
+    std::vector<double> h_traces;
+};
+
+static void graph_release(rp_graph* g) {
+    if (!g) return;
+    cudaSetDevice(g->ws.device);
+    cudaDeviceSynchronize();
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    g->ws.arena.release();
+    g->ws.arena2.release();
+    if (g->ws.aux_ready) {
+        for (int k = 0; k < rp_workspace::kAux; ++k) {
+            cudaStreamDestroy(g->ws.aux[k]);
+            cudaEventDestroy(g->ws.ev_join[k]);
+        }
+        cudaEventDestroy(g->ws.ev_fork);
+    }
+    if (g->ws.pin) cudaFreeHost(g->ws.pin);
+    if (g->st) cudaStreamDestroy(g->st);
+    delete g;
+}
+
+extern "C" int rp_graph_create(rp_scene* s, const double* h_traces, const double* d_traces, int64_t ns,
+                               void* d_out, rp_graph** out) {
+    if (!s || !h_traces || !d_traces || !d_out || !out || ns <= 0) {
+        rp_set_error("rp_graph_create: bad argument");
+        return RP_ERR_ARG;
+    }
+    *out = nullptr;
+    RP_CUDA(cudaSetDevice(s->device));
+    rp_graph* g = new rp_graph();
+    g->s = s;
+    g->ns = ns;
+    g->ws.device = s->device;
+    g->h_traces.assign(h_traces, h_traces + 9 * ns);
+    int rc = RP_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking);
+    const size_t pin_bytes = ((size_t)4 << 20) + 16 * (size_t)ns;
+    if (e == cudaSuccess) e = cudaHostAlloc((void**)&g->ws.pin, pin_bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) rc = rp_cuda_fail(e, "rp_graph_create");
+    g->ws.pin_cap = pin_bytes;
+    g->ws.plan_traces = g->h_traces.data();
+    const int timing = g_timer.enabled;
+    if (!rc) {
+        // the eager call: buffers, tuning, and every check of a plain call
+        g->ws.graph_mode = 1;
+        g_timer.enabled = 0;
+        rc = rp_fast_run(s, &g->ws, d_traces, ns, d_out, 0, nullptr, g->st);
+        if (!rc && (e = cudaStreamSynchronize(g->st)) != cudaSuccess) rc = rp_cuda_fail(e, "rp_graph_create");
+    }
+    if (!rc) {
+        g->ws.graph_mode = 2;
+        g->ws.pin_off = 0;
+        g->ws.graph_rb.clear();
+        e = cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            rc = rp_cuda_fail(e, "rp_graph_create: begin capture");
+        } else {
+            rc = rp_fast_run(s, &g->ws, d_traces, ns, d_out, 0, nullptr, g->st);
+            e = cudaStreamEndCapture(g->st, &g->graph);
+            if (!rc && e != cudaSuccess) rc = rp_cuda_fail(e, "rp_graph_create: end capture");
+        }
+        if (!rc && (e = cudaGraphInstantiate(&g->exec, g->graph, 0)) != cudaSuccess)
+            rc = rp_cuda_fail(e, "rp_graph_create: instantiate");
+    }
+    g_timer.enabled = timing;
+    if (rc) {
+        cudaGetLastError();
+        graph_release(g);
+        return rc;
+    }
+    *out = g;
+    return RP_OK;
+}
+
+extern "C" int rp_graph_launch(rp_graph* g, void* stream) {
+    if (!g || !g->exec) { rp_set_error("rp_graph_launch: null graph"); return RP_ERR_ARG; }
+    RP_CUDA(cudaSetDevice(g->ws.device));
+    RP_CUDA(cudaGraphLaunch(g->exec, stream ? (cudaStream_t)stream : g->st));
+    return RP_OK;
+}
+
+extern "C" int rp_graph_check(const rp_graph* g, int64_t* counts) {
+    if (!g) { rp_set_error("rp_graph_check: null graph"); return RP_ERR_ARG; }
+    for (const rp_workspace::Readback& r : g->ws.graph_rb) {
+        if (r.misc[6]) {
+            rp_set_error("fast form: an illuminated-facet or target list exceeded its capacity (a replay's "
+                         "traces outgrew the bounds the graph was planned with)");
+            return RP_ERR_INTERNAL;
+        }
+        if (r.misc[3]) { rp_set_error("fast form: a shared-memory stage wait timed out"); return RP_ERR_TIMEOUT; }
+        if (r.misc[2]) {
+            rp_set_error("fast form: a pair fell outside its target's bin window (a replay's traces outgrew "
+                         "the bounds the graph was planned with)");
+            return RP_ERR_INTERNAL;
+        }
+        if (counts)
+            for (int k = 0; k < r.nb; ++k) {
+                counts[2 * (r.s0 + k)] = r.cnt[k];
+                counts[2 * (r.s0 + k) + 1] = r.cnt[r.nb + k];
+            }
+    }
+    return RP_OK;
+}
+
+extern "C" int rp_graph_destroy(rp_graph* g) {
+    graph_release(g);
+    return RP_OK;
+}
+
 int rp_workspace::ensure_aux() {
     if (aux_ready) return RP_OK;
     for (int k = 0; k < kAux; ++k) {

@@ -247,20 +247,31 @@ __device__ __forceinline__ void conv_item(const ConvArgs& A, unsigned int item, 
                 __syncthreads();
             }
             // Ptarg[k] = y[k + nr/2] / n: Ptarg[e] = a[e+Q] + W^-(e+Q) b[e+Q],
-            // Ptarg[e+Q] = a[e] - W^-e b[e] (Q = H / 2), into sbase and Wa
-            for (int e = tid; e < (HH >> 1); e += RP_CONV_THREADS) {
-                const int e1 = e + (HH >> 1);
-                const Cplx<float> a0 = Wa[swz(e)], a1 = Wa[swz(e1)];
-                const Cplx<float> t0 = c_mulc(sbase[swz(e)], tw_half(e, n2));
-                const Cplx<float> t1 = c_mulc(sbase[swz(e1)], tw_half(e1, n2));
-                const Cplx<float> lo{(a1.x + t1.x) * inv, (a1.y + t1.y) * inv};
-                const Cplx<float> hi{(a0.x - t0.x) * inv, (a0.y - t0.y) * inv};
-                sbase[swz(e)] = lo;
-                sbase[swz(e1)] = hi;
-                Wa[swz(e)] = lo;
-                Wa[swz(e1)] = hi;
+            // Ptarg[e+Q] = a[e] - W^-e b[e] (Q = H / 2 = 8 SH), to Wa, and
+            // in the same registers the first DIF pass of half 0 of
+            // DIF(pad Ptarg): group g's elements g + i SH are the pairs' e
+            // (i < 8) and e + Q (i >= 8), e = g + i SH
+            {
+                constexpr int SH = HH >> 4, Q = HH >> 1;
+                for (int g = tid; g < SH; g += RP_CONV_THREADS) {
+                    Cplx<float> x[16];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int e = g + i * SH, e1 = e + Q;
+                        const Cplx<float> a0 = Wa[swz(e)], a1 = Wa[swz(e1)];
+                        const Cplx<float> t0 = c_mulc(sbase[swz(e)], tw_half(e, n2));
+                        const Cplx<float> t1 = c_mulc(sbase[swz(e1)], tw_half(e1, n2));
+                        x[i] = Cplx<float>{(a1.x + t1.x) * inv, (a1.y + t1.y) * inv};
+                        x[i + 8] = Cplx<float>{(a0.x - t0.x) * inv, (a0.y - t0.y) * inv};
+                    }
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) Wa[swz(g + i * SH)] = x[i];
+                    dif16_regs(x, g, HH);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) sbase[swz(g + i * SH)] = x[i];
+                }
+                __syncthreads();
             }
-            __syncthreads();
             if constexpr (SPEC) {
                 // Psour = s T2: its transform's halves replace X
                 const C32* __restrict__ T2r = T2;
@@ -278,10 +289,8 @@ __device__ __forceinline__ void conv_item(const ConvArgs& A, unsigned int item, 
                 if (SPEC || h == 1) {
                     half_first_pass(sbase, HH, h, [&](int e) { return Wa[swz(e)]; });
                     __syncthreads();
-                    block_dif_s_mid(sbase, HH, HH >> 4);
-                } else {
-                    block_dif_s_mid(sbase, HH, HH);
                 }
+                block_dif_s_mid(sbase, HH, HH >> 4);
                 switch (EBH) {
                     case 16: spec_add<16>(sbase, X + h * HH, U + h * HH, HH); break;
                     case 8: spec_add<8>(sbase, X + h * HH, U + h * HH, HH); break;

@@ -31,6 +31,7 @@
 // regenerates it, sim.cu:851-856).
 #include <algorithm>
 #include <climits>
+#include <cstring>
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -956,6 +957,7 @@ struct Seg {
     int nb = 0;
     int64_t tmax = 0;
     int64_t fmax = 0;              // illuminated-facet capacity per trace (host bound)
+    int wmax = 0;                  // target-window width, host bound over the segment's traces
     void* d_out = nullptr;
     int out64 = 0;
     int64_t* h_counts = nullptr;
@@ -1277,6 +1279,11 @@ int choose_cfg(const std::vector<Seg*>& ps, const PairJob* d_jobs, const PairJob
     }
     int c = tuned_lookup(multi, deg);
     if (c >= 0) { *cfg_out = c; return RP_OK; }
+    if (ws->graph_mode == 2) {      // no probes under capture (the warm-up call tuned)
+        const int d = ps[0]->sc->pair_cfg;
+        *cfg_out = spec ? (d & 1) : (multi == 1 ? d : (d & 3));
+        return RP_OK;
+    }
     cudaEvent_t e0, e1;
     RP_CUDA(cudaEventCreate(&e0));
     RP_CUDA(cudaEventCreate(&e1));
@@ -1311,9 +1318,14 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     const int nseg = (int)segs.size();
     const int sms = segs[0].sc->sm_count;
     // ---- setup stage for every segment
+    const bool capturing = ws->graph_mode == 2;
     {
         size_t need = 0;
         for (Seg& g : segs) need += seg_setup_bytes(g.sc, g.Lw);
+        if (capturing && need > ws->arena.cap) {
+            rp_set_error("graph capture: the setup buffers outgrew the warm-up call's");
+            return RP_ERR_INTERNAL;
+        }
         int rc = ws->arena.reserve(need);
         if (rc) return rc;
     }
@@ -1331,23 +1343,28 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         for (Seg& g : segs) seg_setup(g, a, st);
     }
     RP_CUDA(cudaGetLastError());
-    std::vector<int> h_misc(8 * (size_t)nseg);
-    for (int i = 0; i < nseg; ++i)
-        RP_CUDA(cudaMemcpyAsync(&h_misc[8 * i], segs[i].misc, sizeof(int) * 8, cudaMemcpyDeviceToHost, st));
-    g_timer.mark(1, st);
-    RP_CUDA(cudaStreamSynchronize(st));
-    g_timer.collect(0, 1);
-    for (int i = 0; i < nseg; ++i)
-        if (h_misc[8 * i + 6]) {
-            rp_set_error("fast form: an illuminated-facet or target list exceeded its capacity");
-            return RP_ERR_INTERNAL;
-        }
+    std::vector<int> h_misc(8 * (size_t)nseg, 0);
+    if (!capturing) {
+        for (int i = 0; i < nseg; ++i)
+            RP_CUDA(cudaMemcpyAsync(&h_misc[8 * i], segs[i].misc, sizeof(int) * 8, cudaMemcpyDeviceToHost, st));
+        g_timer.mark(1, st);
+        RP_CUDA(cudaStreamSynchronize(st));
+        g_timer.collect(0, 1);
+        for (int i = 0; i < nseg; ++i)
+            if (h_misc[8 * i + 6]) {
+                rp_set_error("fast form: an illuminated-facet or target list exceeded its capacity");
+                return RP_ERR_INTERNAL;
+            }
+    }
     // ---- pair-stage buffers and job tables
     std::vector<Seg*> ps, cs[3];
     size_t gslot[3] = {0, 0, 0};
     for (int i = 0; i < nseg; ++i) {
         Seg& g = segs[i];
-        g.Wt = std::max(1, std::min(g.sc->nr, (h_misc[8 * i] + 3) & ~3));
+        // the measured widest target window, or in graph mode the host bound
+        // (a replay's traces are not known when the buffers are laid out)
+        const int wt = ws->graph_mode ? g.wmax : h_misc[8 * i];
+        g.Wt = std::max(1, std::min(g.sc->nr, (wt + 3) & ~3));
         g.L = fast_layout(g.sc, g.nb, g.tmax, g.Wt, g.fmax);
         g.cmode = conv_mode(g.sc);
         g.nsplit = (int)conv_splits(g.L.tstride);
@@ -1386,6 +1403,10 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
         size_t need = 4096 + 1024 * (cg.size() + 1) + (ps.size() + ncs) * (sizeof(PairJob) + sizeof(ConvArgs) + 64)
                       + gscr_n * sizeof(C32);
         for (Seg& g : segs) need += seg_pair_bytes(g.sc, g.L);
+        if (capturing && need > ws->arena2.cap) {
+            rp_set_error("graph capture: the pair-stage buffers outgrew the warm-up call's");
+            return RP_ERR_INTERNAL;
+        }
         int rc = ws->arena2.reserve(need);
         if (rc) return rc;
     }
@@ -1449,15 +1470,30 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
             csm[k] = std::max(csm[k], sx * sizeof(Cplx<float>));
         }
     }
+    // host-to-device copies of the job tables; under capture from pinned
+    // staging that lives as long as the graph (its copy nodes read it at
+    // every replay)
+    auto upload = [&](void* dst, const void* src, size_t bytes) -> int {
+        if (!capturing) {
+            RP_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+            return RP_OK;
+        }
+        void* h = ws->pin_take(bytes);
+        if (!h) {
+            rp_set_error("graph capture: pinned staging of %zu bytes exhausted", ws->pin_cap);
+            return RP_ERR_BUDGET;
+        }
+        std::memcpy(h, src, bytes);
+        RP_CUDA(cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, st));
+        return RP_OK;
+    };
     if (!hp.empty()) {
-        RP_CUDA(cudaMemcpyAsync(d_pjobs, hp.data(), sizeof(PairJob) * hp.size(), cudaMemcpyHostToDevice, st));
-        RP_CUDA(cudaMemcpyAsync(d_pstart, hps.data(), sizeof(unsigned int) * hps.size(), cudaMemcpyHostToDevice, st));
+        if (int rc = upload(d_pjobs, hp.data(), sizeof(PairJob) * hp.size())) return rc;
+        if (int rc = upload(d_pstart, hps.data(), sizeof(unsigned int) * hps.size())) return rc;
     }
     for (size_t k = 0; k < cg.size(); ++k) {
-        RP_CUDA(cudaMemcpyAsync(d_cjobs[k], hc[k].data(), sizeof(ConvArgs) * hc[k].size(), cudaMemcpyHostToDevice,
-                                st));
-        RP_CUDA(cudaMemcpyAsync(d_cstart[k], hcs[k].data(), sizeof(unsigned int) * hcs[k].size(),
-                                cudaMemcpyHostToDevice, st));
+        if (int rc = upload(d_cjobs[k], hc[k].data(), sizeof(ConvArgs) * hc[k].size())) return rc;
+        if (int rc = upload(d_cstart[k], hcs[k].data(), sizeof(unsigned int) * hcs[k].size())) return rc;
     }
     // ---- pair stage: one launch for the wave
     if (!ps.empty()) {
@@ -1593,6 +1629,24 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     }
     RP_CUDA(cudaGetLastError());    // before the join's event calls
     if (par) ws->join(st);
+    if (capturing) {
+        // flags and counts into pinned memory, read by rp_graph_check after
+        // the replay has finished
+        for (int i = 0; i < nseg; ++i) {
+            int* hm = static_cast<int*>(ws->pin_take(sizeof(int) * 8));
+            int* hc2 = static_cast<int*>(ws->pin_take(sizeof(int) * 2 * (size_t)segs[i].nb));
+            if (!hm || !hc2) {
+                rp_set_error("graph capture: pinned staging of %zu bytes exhausted", ws->pin_cap);
+                return RP_ERR_BUDGET;
+            }
+            RP_CUDA(cudaMemcpyAsync(hm, segs[i].misc, sizeof(int) * 8, cudaMemcpyDeviceToHost, st));
+            RP_CUDA(cudaMemcpyAsync(hc2, segs[i].nill, sizeof(int) * segs[i].nb, cudaMemcpyDeviceToHost, st));
+            RP_CUDA(cudaMemcpyAsync(hc2 + segs[i].nb, segs[i].ntl, sizeof(int) * segs[i].nb, cudaMemcpyDeviceToHost,
+                                    st));
+            ws->graph_rb.push_back(rp_workspace::Readback{hm, hc2, segs[i].nb, segs[i].s0});
+        }
+        return RP_OK;
+    }
     g_timer.mark(4, st);
     std::vector<std::vector<int>> cnt(nseg);
     for (int i = 0; i < nseg; ++i)
@@ -1795,16 +1849,25 @@ size_t rp_fast_scratch(const rp_scene* sc, int64_t ns) { return rp_fast_plan_byt
 int rp_fast_batch(const rp_job* jobs, int njobs, rp_workspace* ws, cudaStream_t st) {
     std::vector<SceneConst> kc(njobs);
     std::vector<std::vector<double>> tr(njobs);
+    // graph mode plans a single job from the host copy of its traces (no
+    // device readback: the call may be under stream capture)
+    const bool host_plan = ws->graph_mode && ws->plan_traces;
+    if (host_plan && njobs != 1) {
+        rp_set_error("graph capture: one job per call");
+        return RP_ERR_UNSUPPORTED;
+    }
     for (int j = 0; j < njobs; ++j) {
         int rc = check_scene(jobs[j].scene);
         if (rc) return rc;
         kc[j] = scene_const(jobs[j].scene);
         tr[j].resize(9 * (size_t)jobs[j].ns);
-        if (jobs[j].ns)
+        if (host_plan)
+            std::copy(ws->plan_traces, ws->plan_traces + 9 * jobs[j].ns, tr[j].begin());
+        else if (jobs[j].ns)
             RP_CUDA(cudaMemcpyAsync(tr[j].data(), jobs[j].d_traces, sizeof(double) * 9 * jobs[j].ns,
                                     cudaMemcpyDeviceToHost, st));
     }
-    RP_CUDA(cudaStreamSynchronize(st));
+    if (!host_plan) RP_CUDA(cudaStreamSynchronize(st));
     std::vector<Seg> wave;
     size_t wave_bytes = 0;
     for (int j = 0; j < njobs; ++j) {
@@ -1842,6 +1905,7 @@ int rp_fast_batch(const rp_job* jobs, int njobs, rp_workspace* ws, cudaStream_t 
             g.coef = kc[j].coef;
             g.coefr = kc[j].coefr;
             g.Lw = fast_layout(sc, nb, tmax, nr, fmax);
+            for (int64_t k = s0; k < s0 + nb; ++k) g.wmax = std::max(g.wmax, wb[k]);
             wave.push_back(g);
             wave_bytes += bytes;
             s0 += nb;

@@ -266,8 +266,9 @@ __device__ __forceinline__ void sinc_sfu(float u, float& num, float& den) {
 // Two (facet, target) evaluations of the target leg (compTargetRays,
 // compRefrEnergyIn, accumulateTarget; geometry_kernels.cu:272-350, 520-554,
 // radar_kernels.cu:767-830): the two facets of pair record r against one
-// target, in packed two-lane FP32.  Returns per lane the phasor and x - blo,
-// the bin coordinate relative to the window start.
+// target, in packed two-lane FP32.  Returns per lane the phasor's amplitude,
+// the cosine and sine of its phase, and x - blo, the bin coordinate relative
+// to the window start (pair_eval2 below forms the phasor itself).
 //
 // The two directivities facet_G(Tth, Tph) and facet_G(TargetTh, Tph)
 // (radar_kernels.cu:658-677) need sinc(pik/pi * sin(th) cos(ph)) and
@@ -285,8 +286,8 @@ __device__ __forceinline__ void sinc_sfu(float u, float& num, float& den) {
 // cosine; the fast path skips it when the chunk keeps |phase| below 84 pi
 // (sin/cos.approx hold their accuracy over +-100 pi radians).
 template <int NT, bool ORTHO, bool RED = true>
-__device__ __forceinline__ void pair_eval2(const FacetPair& r, const Anchor& an, const PairArgs& A, f2& xr,
-                                           f2& vre, f2& vim) {
+__device__ __forceinline__ void pair_eval2_core(const FacetPair& r, const Anchor& an, const PairArgs& A, f2& xr,
+                                                f2& amp_out, f2& cs, f2& sn) {
     const f2 ONE = bc(1.f), M1 = bc(-1.f);
     const f2 dx = fld<F_DX>(r), dy = fld<F_DY>(r), dz = fld<F_DZ>(r);
     // m = -2 D: Ttd^2 - T0^2 = |a|^2 - 2 D.a as one chain from |a|^2; the
@@ -356,12 +357,20 @@ __device__ __forceinline__ void pair_eval2(const FacetPair& r, const Anchor& an,
         const f2 k = mul2(ph, bc(0.159154943091895336f));
         ph = fma2(make_float2(rintf(k.x), rintf(k.y)), bc(-6.28318530717958647f), ph);
     }
-    f2 sn, cs;
     __sincosf(ph.x, &sn.x, &cs.x);
     __sincosf(ph.y, &sn.y, &cs.y);
+    amp_out = amp;
+    xr = fma2(bc(A.kb), dT, add2(fld<F_XI>(r), bc(an.xbase)));
+}
+
+// pair_eval2_core with the phasor formed: vre + i vim = amp e^{i ph}.
+template <int NT, bool ORTHO, bool RED = true>
+__device__ __forceinline__ void pair_eval2(const FacetPair& r, const Anchor& an, const PairArgs& A, f2& xr,
+                                           f2& vre, f2& vim) {
+    f2 amp, cs, sn;
+    pair_eval2_core<NT, ORTHO, RED>(r, an, A, xr, amp, cs, sn);
     vre = mul2(amp, cs);
     vim = mul2(amp, sn);
-    xr = fma2(bc(A.kb), dT, add2(fld<F_XI>(r), bc(an.xbase)));
 }
 
 // pair_eval2 for specular mode (general frames): also returns per lane the
@@ -609,6 +618,41 @@ __device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo,
 // fall inside the window and the trace (pair_item checks that per chunk and
 // warp): no range tests, no edge path, lane 0 before lane 1.  The clamp only
 // keeps a (never expected) stray bin inside the window.
+// bin_add_fast2 from the phasor's amplitude and direction: the split
+// weights take the amplitude (amp w and amp - amp w, one product fewer than
+// forming the phasor first), then multiply cos and sin.
+template <int W>
+__device__ __forceinline__ void bin_add_fast2a(f2 xr, f2 amp, f2 cs, f2 sn, float2* win, int tid) {
+    const int f0 = floor_i(xr.x), f1 = floor_i(xr.y);
+    const f2 w = fma2(make_float2((float)f0, (float)f1), bc(-1.f), xr);
+    const f2 a1 = mul2(amp, w);
+    const f2 a0 = add2(amp, neg2(a1));
+    {
+        const unsigned sl = min((unsigned)f0, (unsigned)(W - 2));
+        float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
+        float2* p1 = p0 + RP_PAIR_THREADS;
+        float2 v0 = *p0, v1 = *p1;
+        v0.x = fmaf(cs.x, a0.x, v0.x);
+        v0.y = fmaf(sn.x, a0.x, v0.y);
+        v1.x = fmaf(cs.x, a1.x, v1.x);
+        v1.y = fmaf(sn.x, a1.x, v1.y);
+        *p0 = v0;
+        *p1 = v1;
+    }
+    {
+        const unsigned sl = min((unsigned)f1, (unsigned)(W - 2));
+        float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
+        float2* p1 = p0 + RP_PAIR_THREADS;
+        float2 v0 = *p0, v1 = *p1;
+        v0.x = fmaf(cs.y, a0.y, v0.x);
+        v0.y = fmaf(sn.y, a0.y, v0.y);
+        v1.x = fmaf(cs.y, a1.y, v1.x);
+        v1.y = fmaf(sn.y, a1.y, v1.y);
+        *p0 = v0;
+        *p1 = v1;
+    }
+}
+
 template <int W>
 __device__ __forceinline__ void bin_add_fast2(f2 xr, f2 vre, f2 vim, float2* win, int tid) {
     const int f0 = floor_i(xr.x), f1 = floor_i(xr.y);
@@ -1016,20 +1060,20 @@ __device__ __forceinline__ bool pair_item(const PA& A, int s, int tb, int part, 
                 // gives the same sums
                 if (ILP > 1)
                 for (; jp + ILP <= npairs; jp += ILP) {
-                    f2 x[ILP], re[ILP], im[ILP];
+                    f2 x[ILP], am[ILP], cs[ILP], sn[ILP];
 #pragma unroll
                     for (int i = 0; i < ILP; ++i) {
                         const FacetPair r0 = R[jp + i];
-                        pair_eval2<NT, ORTHO, false>(r0, an, A, x[i], re[i], im[i]);
+                        pair_eval2_core<NT, ORTHO, false>(r0, an, A, x[i], am[i], cs[i], sn[i]);
                     }
 #pragma unroll
-                    for (int i = 0; i < ILP; ++i) bin_add_fast2<W>(x[i], re[i], im[i], win, tid);
+                    for (int i = 0; i < ILP; ++i) bin_add_fast2a<W>(x[i], am[i], cs[i], sn[i], win, tid);
                 }
                 for (; jp < npairs; ++jp) {
                     const FacetPair r0 = R[jp];
-                    f2 x0, re0, im0;
-                    pair_eval2<NT, ORTHO, false>(r0, an, A, x0, re0, im0);
-                    bin_add_fast2<W>(x0, re0, im0, win, tid);
+                    f2 x0, am0, cs0, sn0;
+                    pair_eval2_core<NT, ORTHO, false>(r0, an, A, x0, am0, cs0, sn0);
+                    bin_add_fast2a<W>(x0, am0, cs0, sn0, win, tid);
                 }
             } else {
                 for (; jp < npairs; ++jp) {

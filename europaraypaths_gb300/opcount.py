@@ -18,15 +18,16 @@ launch, divided by the evaluations of that launch); a higher sinc degree
 adds 4 FP32 lane operations per degree, general (non-orthonormal) frames
 about 10:
 
-* FP32 lane operations: 58.4 -- 53 from packed two-lane instructions (one
+* FP32 lane operations: 57.4 -- 52 from packed two-lane instructions (one
   lane per evaluation: anchor distance and Ttd - T0, three direction dot
   products, the four squared sinc arguments, four degree-3 polynomials and
-  their product, the attenuation exponent, amplitude, phase, phasor, bin
-  coordinate and split weights) and 5.4 scalar (the two-bin window update
-  and the phase scaling of the special-function sine and cosine).
+  their product, the attenuation exponent, amplitude, phase, bin coordinate
+  and the amplitude-weighted split weights) and 5.4 scalar (the two-bin
+  window update from the phase's cosine and sine, and the phase scaling of
+  the special-function sine and cosine).
 * MUFU (special-function) instructions: 6 -- rsqrt (1/Ttd), rcp (dT), rcp
   (the in-plane split), ex2, sin and cos of the phase.
-* All thread instructions: 54.0 -- a packed instruction issues once for two
+* All thread instructions: 53.5 -- a packed instruction issues once for two
   evaluations; plus 4 shared-memory record loads and 4 window accesses per
   evaluation, the floor conversion pair, address arithmetic and the loop.
 """
@@ -45,9 +46,9 @@ REF_SFU_PER_TARGET_LEG = 25
 REF_FMA_PER_SURFACE_LEG = 120
 REF_SFU_PER_SURFACE_LEG = 20
 
-FP32_OPS_PER_EVAL = 58.4
+FP32_OPS_PER_EVAL = 57.4
 MUFU_PER_EVAL = 6
-INSTR_PER_EVAL = 54.0
+INSTR_PER_EVAL = 53.5
 EVALS_PER_TARGET_PAIR_METRIC = 0.5     # one evaluation covers two metric pairs
 
 # Nominal special-function throughput of a Blackwell SM (results per clock).

@@ -147,6 +147,25 @@ class Scene:
                                            ctypes.c_void_p(d_out.data_ptr()), cp, sp)
         _abi.check("rp_simulate_device", rc)
 
+    def capture(self, traces, d_traces, d_out):
+        """Record one fast-form call as a CUDA graph (rp_graph_create):
+        ``traces`` (ns, 9) float64 on the host plan it; ``d_traces`` (ns, 9)
+        float64 and ``d_out`` (ns, nr) complex64 torch CUDA tensors are the
+        buffers every replay reads and writes.  The inputs must hold the
+        traces when this is called (the call runs once eagerly first).
+        Returns a :class:`Graph`."""
+        import torch
+        tr = np.ascontiguousarray(traces, dtype=np.float64).reshape(-1, 9)
+        ns = tr.shape[0]
+        if tuple(d_traces.shape) != (ns, 9) or tuple(d_out.shape) != (ns, self.nr):
+            raise ValueError("capture: d_traces must be (ns, 9) and d_out (ns, nr)")
+        torch.cuda.current_stream(d_traces.device).synchronize()     # inputs written before the eager run
+        g = ctypes.c_void_p()
+        rc = _abi.lib().rp_graph_create(self._h, tr.ctypes.data, ctypes.c_void_p(d_traces.data_ptr()), ns,
+                                        ctypes.c_void_p(d_out.data_ptr()), ctypes.byref(g))
+        _abi.check("rp_graph_create", rc)
+        return Graph(g.value, ns, (self, d_traces, d_out))
+
     def simulate_host_ptrs(self, traces_ptr, ns, out_ptr, form="fast", stream=None, counts=None):
         """rp_simulate on raw host pointers (e.g. pinned torch tensors); runs
         on ``stream`` (default: torch's current stream on the scene's device)."""
@@ -156,6 +175,42 @@ class Scene:
         rc = _abi.lib().rp_simulate(self._h, ctypes.c_void_p(traces_ptr), int(ns), f,
                                     ctypes.c_void_p(out_ptr), 0, cp, sp)
         _abi.check("rp_simulate", rc)
+
+
+class Graph:
+    """A captured fast-form call (Scene.capture): launch() replays the whole
+    call on a stream with one graph launch; check() after the replay has
+    finished returns the counts (ns, 2) or raises the status a direct call
+    would have raised."""
+
+    def __init__(self, handle, ns, keep):
+        self._h = handle
+        self.ns = ns
+        self._keep = keep          # the scene and the device buffers the graph uses
+
+    def launch(self, stream=None):
+        dev = self._keep[1].device.index
+        _abi.check("rp_graph_launch", _abi.lib().rp_graph_launch(ctypes.c_void_p(self._h), stream_handle(stream, dev)))
+
+    def check(self, stream=None):
+        """Waits for ``stream`` (default: torch's current stream), then reads
+        the replay's flags and counts."""
+        import torch
+        (stream if stream is not None else torch.cuda.current_stream(self._keep[1].device)).synchronize()
+        counts = np.zeros((self.ns, 2), np.int64)
+        _abi.check("rp_graph_check", _abi.lib().rp_graph_check(ctypes.c_void_p(self._h), counts.ctypes.data))
+        return counts
+
+    def close(self):
+        if self._h:
+            _abi.lib().rp_graph_destroy(ctypes.c_void_p(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def set_timing(enable=True):

@@ -205,6 +205,37 @@ typedef struct rp_job {
  * live on the workspace's device. */
 int rp_simulate_batch(const rp_job* jobs, int njobs, rp_workspace* ws, void* stream);
 
+/*
+ * CUDA-graph capture of a whole fast-form call.  The reference runs every
+ * trace as a host-driven sequence of launches and syncs (sim.cu:615-1008);
+ * here one call -- setup, pair stage, compression and tails of every
+ * segment, on the caller's stream and the workspace's auxiliary streams --
+ * is recorded once and replayed with one graph launch.
+ *   rp_graph_create  plans the call from h_traces (host ns x 9, the layout of
+ *                    d_traces) with target windows sized by host bounds,
+ *                    runs it once eagerly on d_traces / d_out (device
+ *                    buffers the graph keeps), then records it.  The graph
+ *                    owns its workspace.
+ *   rp_graph_launch  replays it on `stream` (NULL: the graph's own stream):
+ *                    the results of whatever traces d_traces then holds go
+ *                    to d_out.  Replays on one graph must be ordered.
+ *   rp_graph_check   after the replay has completed: the status a plain call
+ *                    would have returned (a replay whose traces need more
+ *                    illuminated-facet or target capacity, or wider target
+ *                    windows, than the traces the graph was planned with
+ *                    reports RP_ERR_INTERNAL and its output is not valid),
+ *                    and the counts (ns x 2: N_ill, N_t) when counts is not
+ *                    NULL.
+ * Results equal rp_simulate_device's fast form bit for bit.  Fast form,
+ * complex64 output only.
+ */
+typedef struct rp_graph rp_graph;
+int rp_graph_create(rp_scene* s, const double* h_traces, const double* d_traces, int64_t ns, void* d_out,
+                    rp_graph** out);
+int rp_graph_launch(rp_graph* g, void* stream);
+int rp_graph_check(const rp_graph* g, int64_t* counts);
+int rp_graph_destroy(rp_graph* g);
+
 /* Pair-kernel autotuner.  With tuning on (the default unless RP_PAIR_CFG
  * fixes a configuration), the first pair launch of each kind (single-scene
  * kernel per sinc degree, or the multi-scene kernel) times the kernel's
