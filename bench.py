@@ -725,7 +725,7 @@ def main():
     ap.add_argument("--ref-targets", type=int, default=24, help="target cap per --impl reference step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=64, help="scenes of the batched workload (0 = skip)")
-    ap.add_argument("--batch-traces", type=int, default=2, help="interior traces per scene per batched step")
+    ap.add_argument("--batch-traces", type=int, default=8, help="interior traces per scene per batched step")
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--serve-seconds", type=float, default=15.0, help="serving-loop arrivals window (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson request rate, requests/s")
@@ -945,6 +945,16 @@ def main():
                 try:
                     line["batch"] = run_batch(args, objs, tracks, stream)
                     line["batch"]["setup_s"] = t_build
+                    # the pair stage against the headline's (pairs per ms of
+                    # the pair stage on both sides)
+                    b = line["batch"]
+                    bp = b["pairs_per_step"] / (b["stage_ms_per_step"]["pairs_ms"] / 1e3)
+                    rs = line["roofline"]
+                    hp = line["value"] * line["ms_per_step"] / (rs["stage_ms"]["pairs_ms"] / args.steps)
+                    b["pair_stage"] = {"pairs_per_s": bp, "headline_pair_stage_pairs_per_s": hp,
+                                       "over_headline": bp / hp,
+                                       "note": "headline at its traces per call; the batch's 60 MHz "
+                                               "evaluations (degree-6 sinc) cost 17% more instructions"}
                 except Exception as e:       # reported in the line; the headline stands
                     line["batch"] = {"error": f"{type(e).__name__}: {e}"}
             plain = line.get("plain_form", {}).get("value")
