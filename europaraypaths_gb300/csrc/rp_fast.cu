@@ -835,7 +835,9 @@ FastLayout fast_layout(const rp_scene* sc, int nb, int64_t tstride, int Wt, int6
     return L;
 }
 
-const size_t kFastBudget = (size_t)32 << 30;
+// Scratch of one wave (the segments whose pair stage shares one launch):
+// the 64-scene uneven batch at 8 traces per scene fits one wave.
+const size_t kFastBudget = (size_t)64 << 30;
 
 
 // Pair-kernel instantiation: sinc degree x frame kind x (ILP facet pairs per
