@@ -851,9 +851,9 @@ def main():
                 "achieved": fp32_rate / 1e12, "peak": fp32_peak / 1e12,
                 "unit": "T FP32 lane-operations/s",
                 "frac": fp32_rate / fp32_peak if fp32_peak else None,
-                # DRAM read+write of one launch from the committed ncu capture (2 traces: 340.4 + 82.4
+                # DRAM read+write of one launch from the committed ncu capture (2 traces: 353.9 + 82.5
                 # MB), scaled by the traces per launch; the kernel is compute-bound (DRAM < 0.1 % of peak)
-                "traffic": 422.8e6 * tps / 2.0,
+                "traffic": 436.4e6 * tps / 2.0,
                 "traffic_unit": "bytes per launch (ncu, profiles/k_pairs32_large_scene.md, scaled)",
                 "peak_source": (f"nominal {opcount.FP32_FMA_PER_CLK_PER_SM} FP32 lanes/clk/SM x {n_sm} SMs x "
                                 f"{sm_mhz:.0f} MHz median SM clock under load; MEASURED_PEAKS.json holds HBM "
