@@ -59,7 +59,7 @@ __device__ __forceinline__ void edge_pass(const Cplx<float>* src, int n, Op op) 
     for (int blk = threadIdx.x; blk < n / B; blk += RP_CONV_THREADS) {
         Cplx<float> x[B];
 #pragma unroll
-        for (int i = 0; i < B; ++i) x[i] = src[swz(blk * B + i)];
+        for (int i = 0; i < B; i += 2) ld_pair(src, blk * B + i, x[i], x[i + 1]);
         dif_edge<float, B>(x);
         op(blk * B, x);
     }
@@ -90,16 +90,15 @@ __device__ __forceinline__ void spec_add(const Cplx<float>* W, const Cplx<float>
     for (int blk = threadIdx.x; blk < n / B; blk += RP_CONV_THREADS) {
         Cplx<float> x[B];
 #pragma unroll
-        for (int i = 0; i < B; ++i) x[i] = W[swz(blk * B + i)];
+        for (int i = 0; i < B; i += 2) ld_pair(W, blk * B + i, x[i], x[i + 1]);
         dif_edge<float, B>(x);
 #pragma unroll
-        for (int i = 0; i < B; ++i) {
-            const int k = swz(blk * B + i);
-            const Cplx<float> v = c_mul(X[k], x[i]);
-            Cplx<float> o = U[k];
-            o.x += v.x;
-            o.y += v.y;
-            U[k] = o;
+        for (int i = 0; i < B; i += 2) {
+            Cplx<float> a0, a1, o0, o1;
+            ld_pair(X, blk * B + i, a0, a1);
+            ld_pair(U, blk * B + i, o0, o1);
+            const Cplx<float> v0 = c_mul(a0, x[i]), v1 = c_mul(a1, x[i + 1]);
+            st_pair(U, blk * B + i, Cplx<float>{o0.x + v0.x, o0.y + v0.y}, Cplx<float>{o1.x + v1.x, o1.y + v1.y});
         }
     }
 }
@@ -111,13 +110,15 @@ __device__ __forceinline__ void spec_to_w(Cplx<float>* W, const Cplx<float>* U, 
     for (int blk = threadIdx.x; blk < n / B; blk += RP_CONV_THREADS) {
         Cplx<float> x[B];
 #pragma unroll
-        for (int i = 0; i < B; ++i) {
-            const Cplx<float> o = U[swz(blk * B + i)];
-            x[i] = Cplx<float>{o.x * sc, o.y * sc};
+        for (int i = 0; i < B; i += 2) {
+            Cplx<float> o0, o1;
+            ld_pair(U, blk * B + i, o0, o1);
+            x[i] = Cplx<float>{o0.x * sc, o0.y * sc};
+            x[i + 1] = Cplx<float>{o1.x * sc, o1.y * sc};
         }
         dit_edge<float, B>(x);
 #pragma unroll
-        for (int i = 0; i < B; ++i) W[swz(blk * B + i)] = x[i];
+        for (int i = 0; i < B; i += 2) st_pair(W, blk * B + i, x[i], x[i + 1]);
     }
 }
 
@@ -233,13 +234,15 @@ __device__ __forceinline__ void conv_item(const ConvArgs& A, unsigned int item, 
                 edge_pass_n(sbase, HH, [&](int k0, auto& x) {
                     constexpr int B = sizeof(x) / sizeof(x[0]);
 #pragma unroll
-                    for (int i = 0; i < B; ++i) {
-                        Xh[swz(k0 + i)] = x[i];
-                        x[i] = c_mul(x[i], Ch[k0 + i]);
+                    for (int i = 0; i < B; i += 2) {
+                        st_pair(Xh, k0 + i, x[i], x[i + 1]);
+                        const float4 c = *reinterpret_cast<const float4*>(Ch + k0 + i);
+                        x[i] = c_mul(x[i], Cplx<float>{c.x, c.y});
+                        x[i + 1] = c_mul(x[i + 1], Cplx<float>{c.z, c.w});
                     }
                     dit_edge<float, B>(x);
 #pragma unroll
-                    for (int i = 0; i < B; ++i) sbase[swz(k0 + i)] = x[i];
+                    for (int i = 0; i < B; i += 2) st_pair(sbase, k0 + i, x[i], x[i + 1]);
                 });
                 __syncthreads();
                 block_dit_s_mid(sbase, HH, HH >> 4);
@@ -327,13 +330,15 @@ __device__ __forceinline__ void conv_item(const ConvArgs& A, unsigned int item, 
                 edge_pass_n(sbase, RP_CONV_CHUNK, [&](int k0, auto& x) {
                     constexpr int B = sizeof(x) / sizeof(x[0]);
 #pragma unroll
-                    for (int i = 0; i < B; ++i) {
-                        Xc[swz(k0 + i)] = x[i];
-                        x[i] = c_mul(x[i], Cc[k0 + i]);
+                    for (int i = 0; i < B; i += 2) {
+                        st_pair(Xc, k0 + i, x[i], x[i + 1]);
+                        const float4 c = *reinterpret_cast<const float4*>(Cc + k0 + i);
+                        x[i] = c_mul(x[i], Cplx<float>{c.x, c.y});
+                        x[i + 1] = c_mul(x[i + 1], Cplx<float>{c.z, c.w});
                     }
                     dit_edge<float, B>(x);
 #pragma unroll
-                    for (int i = 0; i < B; ++i) sbase[swz(k0 + i)] = x[i];
+                    for (int i = 0; i < B; i += 2) st_pair(sbase, k0 + i, x[i], x[i + 1]);
                 }, EB);
                 __syncthreads();
                 block_dit_s_mid(sbase, RP_CONV_CHUNK, SB >> 2, EB);
@@ -381,13 +386,15 @@ __device__ __forceinline__ void conv_item(const ConvArgs& A, unsigned int item, 
         edge_pass_n(D1, n2, [&](int k0, auto& x) {
             constexpr int B = sizeof(x) / sizeof(x[0]);
 #pragma unroll
-            for (int i = 0; i < B; ++i) {
-                X[swz(k0 + i)] = x[i];
-                x[i] = c_mul(x[i], C2s[k0 + i]);
+            for (int i = 0; i < B; i += 2) {
+                st_pair(X, k0 + i, x[i], x[i + 1]);
+                const float4 c = *reinterpret_cast<const float4*>(C2s + k0 + i);
+                x[i] = c_mul(x[i], Cplx<float>{c.x, c.y});
+                x[i + 1] = c_mul(x[i + 1], Cplx<float>{c.z, c.w});
             }
             dit_edge<float, B>(x);
 #pragma unroll
-            for (int i = 0; i < B; ++i) W[swz(k0 + i)] = x[i];
+            for (int i = 0; i < B; i += 2) st_pair(W, k0 + i, x[i], x[i + 1]);
         });
         __syncthreads();
         // ---- Ptarg: the DIT passes up to span n/16, then the last fused

@@ -198,14 +198,29 @@ __device__ __forceinline__ void r4_dit_reg(Cplx<T>& x0, Cplx<T>& x1, Cplx<T>& x2
 #endif
 
 #ifdef __CUDACC__
-// Bank-conflict-free variants for the compression kernel.  Element e of a
-// shared array lives at swz(e) = e ^ ((e >> 5) & 31): a permutation inside
-// each row of 32 complex values, so every access pattern of the stages below
-// (consecutive elements, or one element per row at any power-of-two stride)
-// reaches 32 distinct bank pairs.  Twiddles e^{-2 pi i j / L} come from the
-// special-function unit (__sincosf, |angle| <= pi / 2, absolute error below
-// 1e-6) instead of a table.
-__device__ __forceinline__ int swz(int e) { return e ^ ((e >> 5) & 31); }
+// Swizzled variants for the compression kernel.  Element e of a shared
+// array lives at swz(e) = e ^ (2 ((e >> 5) & 15)): a permutation inside each
+// row of 32 complex values that XORs the column with twice the row index.
+// The fused passes whose groups stride 2 or 4 elements (lanes in 8 or 4
+// consecutive rows) then reach 16 distinct bank pairs per half-warp, and
+// the permutation keeps each even-odd pair of elements adjacent (the XOR
+// value is even), so a pair moves as one 16-byte access (ld_pair /
+// st_pair).  Twiddles e^{-2 pi i j / L} come from the special-function unit
+// (__sincosf, |angle| <= pi / 2, absolute error below 1e-6) instead of a
+// table.
+__device__ __forceinline__ int swz(int e) { return e ^ ((e >> 4) & 30); }
+
+// Elements e and e + 1 (e even) of a swizzled array, 16-byte aligned when a is.
+template <class T>
+__device__ __forceinline__ void ld_pair(const Cplx<T>* a, int e, Cplx<T>& x0, Cplx<T>& x1) {
+    const float4 v = *reinterpret_cast<const float4*>(a + swz(e));
+    x0 = Cplx<T>{v.x, v.y};
+    x1 = Cplx<T>{v.z, v.w};
+}
+template <class T>
+__device__ __forceinline__ void st_pair(Cplx<T>* a, int e, Cplx<T> x0, Cplx<T> x1) {
+    *reinterpret_cast<float4*>(a + swz(e)) = make_float4(x0.x, x0.y, x1.x, x1.y);
+}
 
 template <class T>
 __device__ __forceinline__ Cplx<T> tw_sfu(int j, float step) {   // e^{-i j step}
