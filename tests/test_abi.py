@@ -94,6 +94,16 @@ def test_scene_create_rejects_bad_arguments(built_lib):
     assert built_lib.rp_simulate(None, None, 1, 1, None, 0, None, None) == -1
 
 
+def test_graph_calls_reject_bad_arguments(built_lib):
+    # argument checks come before any device work, so they run without a GPU
+    g = ctypes.c_void_p()
+    assert built_lib.rp_graph_create(None, None, None, 1, None, ctypes.byref(g)) == -1
+    assert "rp_graph_create" in _abi.last_error()
+    assert built_lib.rp_graph_launch(None, None) == -1
+    assert built_lib.rp_graph_check(None, None) == -1
+    assert built_lib.rp_graph_destroy(None) == 0
+
+
 @pytest.mark.parametrize("over,ttype", [({"convolution": False}, 1), ({"convolution_linear": False}, 1),
                                         ({"specular": True, "convolution": False}, 1),
                                         ({"specular": True, "convolution_linear": False}, 1)])
