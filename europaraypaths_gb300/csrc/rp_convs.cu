@@ -58,8 +58,7 @@ template <int B, class Op>
 __device__ __forceinline__ void edge_pass(const Cplx<float>* src, int n, Op op) {
     for (int blk = threadIdx.x; blk < n / B; blk += RP_CONV_THREADS) {
         Cplx<float> x[B];
-#pragma unroll
-        for (int i = 0; i < B; i += 2) ld_pair(src, blk * B + i, x[i], x[i + 1]);
+        ld_pairs<B>(src, blk * B, x);
         dif_edge<float, B>(x);
         op(blk * B, x);
     }
@@ -88,18 +87,17 @@ __device__ __forceinline__ void edge_pass_n(const Cplx<float>* src, int n, Op op
 template <int B>
 __device__ __forceinline__ void spec_add(const Cplx<float>* W, const Cplx<float>* X, Cplx<float>* U, int n) {
     for (int blk = threadIdx.x; blk < n / B; blk += RP_CONV_THREADS) {
-        Cplx<float> x[B];
-#pragma unroll
-        for (int i = 0; i < B; i += 2) ld_pair(W, blk * B + i, x[i], x[i + 1]);
+        Cplx<float> x[B], a[B], o[B];
+        ld_pairs<B>(W, blk * B, x);
         dif_edge<float, B>(x);
+        ld_pairs<B>(X, blk * B, a);
+        ld_pairs<B>(U, blk * B, o);
 #pragma unroll
-        for (int i = 0; i < B; i += 2) {
-            Cplx<float> a0, a1, o0, o1;
-            ld_pair(X, blk * B + i, a0, a1);
-            ld_pair(U, blk * B + i, o0, o1);
-            const Cplx<float> v0 = c_mul(a0, x[i]), v1 = c_mul(a1, x[i + 1]);
-            st_pair(U, blk * B + i, Cplx<float>{o0.x + v0.x, o0.y + v0.y}, Cplx<float>{o1.x + v1.x, o1.y + v1.y});
+        for (int i = 0; i < B; ++i) {
+            const Cplx<float> v = c_mul(a[i], x[i]);
+            o[i] = Cplx<float>{o[i].x + v.x, o[i].y + v.y};
         }
+        st_pairs<B>(U, blk * B, o);
     }
 }
 
@@ -109,16 +107,11 @@ template <int B>
 __device__ __forceinline__ void spec_to_w(Cplx<float>* W, const Cplx<float>* U, int n, float sc) {
     for (int blk = threadIdx.x; blk < n / B; blk += RP_CONV_THREADS) {
         Cplx<float> x[B];
+        ld_pairs<B>(U, blk * B, x);
 #pragma unroll
-        for (int i = 0; i < B; i += 2) {
-            Cplx<float> o0, o1;
-            ld_pair(U, blk * B + i, o0, o1);
-            x[i] = Cplx<float>{o0.x * sc, o0.y * sc};
-            x[i + 1] = Cplx<float>{o1.x * sc, o1.y * sc};
-        }
+        for (int i = 0; i < B; ++i) x[i] = Cplx<float>{x[i].x * sc, x[i].y * sc};
         dit_edge<float, B>(x);
-#pragma unroll
-        for (int i = 0; i < B; i += 2) st_pair(W, blk * B + i, x[i], x[i + 1]);
+        st_pairs<B>(W, blk * B, x);
     }
 }
 
@@ -233,16 +226,15 @@ __device__ __forceinline__ void conv_item(const ConvArgs& A, unsigned int item, 
                 const Cplx<float>* const Ch = C2s + h * HH;
                 edge_pass_n(sbase, HH, [&](int k0, auto& x) {
                     constexpr int B = sizeof(x) / sizeof(x[0]);
+                    st_pairs<B>(Xh, k0, x);
 #pragma unroll
                     for (int i = 0; i < B; i += 2) {
-                        st_pair(Xh, k0 + i, x[i], x[i + 1]);
                         const float4 c = *reinterpret_cast<const float4*>(Ch + k0 + i);
                         x[i] = c_mul(x[i], Cplx<float>{c.x, c.y});
                         x[i + 1] = c_mul(x[i + 1], Cplx<float>{c.z, c.w});
                     }
                     dit_edge<float, B>(x);
-#pragma unroll
-                    for (int i = 0; i < B; i += 2) st_pair(sbase, k0 + i, x[i], x[i + 1]);
+                    st_pairs<B>(sbase, k0, x);
                 });
                 __syncthreads();
                 block_dit_s_mid(sbase, HH, HH >> 4);
@@ -329,16 +321,15 @@ __device__ __forceinline__ void conv_item(const ConvArgs& A, unsigned int item, 
                 const Cplx<float>* const Cc = C2s + c0;
                 edge_pass_n(sbase, RP_CONV_CHUNK, [&](int k0, auto& x) {
                     constexpr int B = sizeof(x) / sizeof(x[0]);
+                    st_pairs<B>(Xc, k0, x);
 #pragma unroll
                     for (int i = 0; i < B; i += 2) {
-                        st_pair(Xc, k0 + i, x[i], x[i + 1]);
                         const float4 c = *reinterpret_cast<const float4*>(Cc + k0 + i);
                         x[i] = c_mul(x[i], Cplx<float>{c.x, c.y});
                         x[i + 1] = c_mul(x[i + 1], Cplx<float>{c.z, c.w});
                     }
                     dit_edge<float, B>(x);
-#pragma unroll
-                    for (int i = 0; i < B; i += 2) st_pair(sbase, k0 + i, x[i], x[i + 1]);
+                    st_pairs<B>(sbase, k0, x);
                 }, EB);
                 __syncthreads();
                 block_dit_s_mid(sbase, RP_CONV_CHUNK, SB >> 2, EB);
@@ -385,16 +376,15 @@ __device__ __forceinline__ void conv_item(const ConvArgs& A, unsigned int item, 
         dif_trace(D1, T, pstride, qbase, b0, Wt, nr, n2, true);
         edge_pass_n(D1, n2, [&](int k0, auto& x) {
             constexpr int B = sizeof(x) / sizeof(x[0]);
+            st_pairs<B>(X, k0, x);
 #pragma unroll
             for (int i = 0; i < B; i += 2) {
-                st_pair(X, k0 + i, x[i], x[i + 1]);
                 const float4 c = *reinterpret_cast<const float4*>(C2s + k0 + i);
                 x[i] = c_mul(x[i], Cplx<float>{c.x, c.y});
                 x[i + 1] = c_mul(x[i + 1], Cplx<float>{c.z, c.w});
             }
             dit_edge<float, B>(x);
-#pragma unroll
-            for (int i = 0; i < B; i += 2) st_pair(W, k0 + i, x[i], x[i + 1]);
+            st_pairs<B>(W, k0, x);
         });
         __syncthreads();
         // ---- Ptarg: the DIT passes up to span n/16, then the last fused

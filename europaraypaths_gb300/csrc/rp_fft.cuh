@@ -222,6 +222,36 @@ __device__ __forceinline__ void st_pair(Cplx<T>* a, int e, Cplx<T> x0, Cplx<T> x
     *reinterpret_cast<float4*>(a + swz(e)) = make_float4(x0.x, x0.y, x1.x, x1.y);
 }
 
+// The B elements k0 .. k0 + B - 1 (a block of B, k0 = blk B) as B / 2 pair
+// accesses.  For B = 4 the lanes whose block index has bit 2 set take their
+// second pair first: a quarter-warp's eight 16-byte accesses then cover all
+// eight bank groups (in order, blocks 2 chunks apart would meet pairwise).
+template <int B, class T>
+__device__ __forceinline__ void ld_pairs(const Cplx<T>* a, int k0, Cplx<T> (&x)[B]) {
+    if constexpr (B == 4) {
+        const bool r = (k0 >> 4) & 1;
+        Cplx<T> p0, p1, q0, q1;
+        ld_pair(a, k0 + (r ? 2 : 0), p0, p1);
+        ld_pair(a, k0 + (r ? 0 : 2), q0, q1);
+        x[0] = r ? q0 : p0; x[1] = r ? q1 : p1;
+        x[2] = r ? p0 : q0; x[3] = r ? p1 : q1;
+    } else {
+#pragma unroll
+        for (int i = 0; i < B; i += 2) ld_pair(a, k0 + i, x[i], x[i + 1]);
+    }
+}
+template <int B, class T>
+__device__ __forceinline__ void st_pairs(Cplx<T>* a, int k0, const Cplx<T> (&x)[B]) {
+    if constexpr (B == 4) {
+        const bool r = (k0 >> 4) & 1;
+        st_pair(a, k0 + (r ? 2 : 0), r ? x[2] : x[0], r ? x[3] : x[1]);
+        st_pair(a, k0 + (r ? 0 : 2), r ? x[0] : x[2], r ? x[1] : x[3]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < B; i += 2) st_pair(a, k0 + i, x[i], x[i + 1]);
+    }
+}
+
 template <class T>
 __device__ __forceinline__ Cplx<T> tw_sfu(int j, float step) {   // e^{-i j step}
     float sn, cs;
