@@ -64,6 +64,29 @@ __device__ T block_reduce(T v, Op op, T* sh) {
     return r;
 }
 
+// Block-wide maxima of N floats at once: one shared-memory round and two
+// barriers for all of them (sh: N x 32 floats).  Minima are maxima of the
+// negated values.
+template <int N>
+__device__ __forceinline__ void block_max_n(float (&v)[N], float* sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] = fmaxf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < N; ++k) sh[k * 32 + wid] = v[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        float r = sh[k * 32];
+        for (int w = 1; w < nw; ++w) r = fmaxf(r, sh[k * 32 + w]);
+        v[k] = r;
+    }
+    __syncthreads();
+}
+
 struct MinOp { __device__ double operator()(double a, double b) const { return fmin(a, b); } };
 struct MaxOp { __device__ double operator()(double a, double b) const { return fmax(a, b); } };
 struct MinOpF { __device__ float operator()(float a, float b) const { return fminf(a, b); } };
@@ -91,8 +114,7 @@ k_facets32(const double* __restrict__ F, int64_t nf, int64_t fstride, const int*
            int64_t mstride, float* __restrict__ sx_o, C32* __restrict__ sv_o,
            unsigned long long* __restrict__ vmax, double* __restrict__ org,
            const int64_t* __restrict__ order, FacetSpec* __restrict__ spec, FacetT0* __restrict__ t0rec) {
-    __shared__ double shd[32];
-    __shared__ float shf[32];
+    __shared__ float shf[6 * 32];
     const int s = blockIdx.y;
     const int n = nill[s];
     const int k = blockIdx.x;
@@ -106,21 +128,29 @@ k_facets32(const double* __restrict__ F, int64_t nf, int64_t fstride, const int*
         i = idx[(size_t)s * fstride + j];
         fx = F[i]; fy = F[nf + i]; fz = F[2 * nf + i];
     }
-    // chunk bounding box and centre (FP64)
-    double mnx = block_reduce(ok ? fx : 1e300, MinOp(), shd);
-    double mny = block_reduce(ok ? fy : 1e300, MinOp(), shd);
-    double mnz = block_reduce(ok ? fz : 1e300, MinOp(), shd);
-    double mxx = block_reduce(ok ? fx : -1e300, MaxOp(), shd);
-    double mxy = block_reduce(ok ? fy : -1e300, MaxOp(), shd);
-    double mxz = block_reduce(ok ? fz : -1e300, MaxOp(), shd);
-    // the trace origin is its first illuminated facet; the chunk centre is
-    // the origin plus the FP32 rounding of (bounding-box centre - origin), so
-    // its offset cf from the origin is exact in FP32
+    // the trace origin is its first illuminated facet.  The chunk's bounding
+    // box comes from the facets' FP32 offsets from the origin (one combined
+    // reduction: FP64 minima and maxima would run on the narrow FP64 pipe),
+    // widened by the offsets' rounding so that it holds every facet.  The
+    // chunk centre is the origin plus the box centre cf, an FP32 offset, so
+    // cf is exact in FP32 by construction.
     const int64_t i0 = idx[(size_t)s * fstride];
     const double ox = F[i0], oy = F[nf + i0], oz = F[2 * nf + i0];
-    const float cfx = (float)(0.5 * (mnx + mxx) - ox), cfy = (float)(0.5 * (mny + mxy) - oy),
-                cfz = (float)(0.5 * (mnz + mxz) - oz);
+    float bx[6];
+    {
+        const float qx = (float)(fx - ox), qy = (float)(fy - oy), qz = (float)(fz - oz);
+        bx[0] = ok ? -qx : -3e38f; bx[1] = ok ? -qy : -3e38f; bx[2] = ok ? -qz : -3e38f;
+        bx[3] = ok ? qx : -3e38f; bx[4] = ok ? qy : -3e38f; bx[5] = ok ? qz : -3e38f;
+    }
+    block_max_n<6>(bx, shf);
+    const float qmnx = -bx[0], qmny = -bx[1], qmnz = -bx[2], qmxx = bx[3], qmxy = bx[4], qmxz = bx[5];
+    const float cfx = 0.5f * (qmnx + qmxx), cfy = 0.5f * (qmny + qmxy), cfz = 0.5f * (qmnz + qmxz);
     const double cx = ox + (double)cfx, cy = oy + (double)cfy, cz = oz + (double)cfz;
+    // |FP32 rounding of an offset q| <= |q| 2^-24: widen by 2^-23 of the extent and 1 micrometre
+    auto lo_edge = [](double o, float q) { return o + (double)q - (fabs((double)q) * 0x1p-23 + 1e-6); };
+    auto hi_edge = [](double o, float q) { return o + (double)q + (fabs((double)q) * 0x1p-23 + 1e-6); };
+    const double mnx = lo_edge(ox, qmnx), mny = lo_edge(oy, qmny), mnz = lo_edge(oz, qmnz);
+    const double mxx = hi_edge(ox, qmxx), mxy = hi_edge(oy, qmxy), mxz = hi_edge(oz, qmxz);
     if (k == 0 && threadIdx.x == 0) {
         org[4 * s] = ox; org[4 * s + 1] = oy; org[4 * s + 2] = oz; org[4 * s + 3] = 0.0;
     }
@@ -284,12 +314,13 @@ k_facets32(const double* __restrict__ F, int64_t nf, int64_t fstride, const int*
                 t0rec[((size_t)s * rstride + j) / 2].v = make_float4(t0a, pok ? pa : 0.f, t0d, pok ? pdd : t0d);
         }
     }
-    // the surface amplitude maximum of the trace: one atomic per chunk
-    const float bmax = block_reduce(amax, MaxOpF(), shf);
+    // the surface amplitude maximum of the trace (one atomic per chunk), the
+    // chunk's radius and its range of xI, in one combined reduction
+    float mx4[4] = {amax, ok ? rr : 0.f, ok ? -xI : -3e38f, ok ? xI : -3e38f};
+    block_max_n<4>(mx4, shf);
+    const float bmax = mx4[0];
     if (threadIdx.x == 0 && bmax > 0.f) atomic_max_pos(vmax + s, (double)bmax);
-    float R = block_reduce(ok ? rr : 0.f, MaxOpF(), shf);
-    float xmn = block_reduce(ok ? xI : 3e38f, MinOpF(), shf);
-    float xmx = block_reduce(ok ? xI : -3e38f, MaxOpF(), shf);
+    const float R = mx4[1], xmn = -mx4[2], xmx = mx4[3];
     if (threadIdx.x == 0) {
         ChunkMeta m;
         m.cx = cx; m.cy = cy; m.cz = cz;
