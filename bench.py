@@ -353,6 +353,58 @@ def run_direct(args, sc, track, stream):
     return out
 
 
+def run_graph(args, scene, track):
+    """One-trace calls, each followed by a sync: a direct
+    rp_simulate_device call (host planning from the trace, two host syncs,
+    the launches) against the replay of the same call captured as a CUDA
+    graph (rp_graph_*).  Wall-clock per call on the host; the replay's
+    radargram must equal the direct call's bit for bit.  On the headline
+    scene (trace 1000, ~20 ms of device work a call) and on the small plain
+    scene (200x200 facets, 1600 targets, 2048 bins: a call short enough
+    for the host's share to show)."""
+    from europaraypaths_gb300 import scenes, simulator
+    out = {"large_scene": _graph_case(args.graph_calls, scene, track[1000:1001])}
+    sp = scenes.small_plain()
+    with simulator.Scene(sp["params"], sp["facets"], sp["targets"]) as small:
+        tr = small.default_traces()
+        out["small_scene"] = _graph_case(args.graph_calls * 5, small, tr[50:51])
+    return out
+
+
+def _graph_case(n, scene, trace):
+    import torch
+    tr = np.ascontiguousarray(trace)
+    d_tr = torch.from_numpy(tr).cuda()
+    ref = torch.empty((1, scene.nr), dtype=torch.complex64, device="cuda")
+    cur = torch.cuda.current_stream()
+    for _ in range(3):
+        scene.simulate_device(d_tr, ref)
+        cur.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n):
+        scene.simulate_device(d_tr, ref)
+        cur.synchronize()
+    direct = (time.perf_counter() - t0) / n
+    out = torch.empty_like(ref)
+    g = scene.capture(tr, d_tr, out)
+    try:
+        for _ in range(3):
+            g.launch()
+            cur.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n):
+            g.launch()
+            cur.synchronize()
+        replay = (time.perf_counter() - t0) / n
+        g.check()
+        same = bool(torch.equal(torch.view_as_real(out), torch.view_as_real(ref)))
+    finally:
+        g.close()
+    return {"traces_per_call": 1, "calls": n, "direct_ms_per_call": 1e3 * direct,
+            "replay_ms_per_call": 1e3 * replay, "direct_over_replay": direct / replay,
+            "bitwise_equal": same, "note": "host wall clock per call, each call followed by a stream sync"}
+
+
 def run_flyby(args, stream):
     """The flyby-scale scene: 64M facets (8000x8000 at 2.5 m), two rough
     layers (320k targets), 10,000 traces at 25 km, 60 MHz / 10 MHz sampled
@@ -735,6 +787,8 @@ def main():
                     help="queue-wait bound (s) of that serving run; older queued requests are shed")
     ap.add_argument("--no-io", dest="io", action="store_false", help="skip the host file-I/O measurement")
     ap.add_argument("--no-focus", dest="focus", action="store_false", help="skip the azimuth-focusing measurement")
+    ap.add_argument("--graph-calls", type=int, default=20,
+                    help="one-trace calls timed direct and as graph replays (0 = skip)")
     ap.add_argument("--spec-traces", type=int, default=4,
                     help="traces per step of the specular-mode and ttype-0 runs (0 = skip)")
     ap.add_argument("--spec-steps", type=int, default=3)
@@ -923,6 +977,11 @@ def main():
                 line["direct"] = run_direct(args, sc, track, stream)
             except Exception as e:
                 line["direct"] = {"error": f"{type(e).__name__}: {e}"}
+        if args.graph_calls > 0 and world == 1:
+            try:
+                line["graph"] = run_graph(args, scene, track)
+            except Exception as e:
+                line["graph"] = {"error": f"{type(e).__name__}: {e}"}
         if args.flyby_traces > 0 and world == 1:
             try:
                 line["flyby"] = run_flyby(args, stream)
