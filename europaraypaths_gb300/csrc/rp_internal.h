@@ -179,7 +179,8 @@ struct rp_scene {
     // ---- tuning
     int ortho = 0;                       // every facet frame (n, u, v) orthonormal to 1e-5
     int pair_variant = 0;                // 0 auto (polynomial sinc where accurate), 1 special-function sinc
-    int pair_cfg = 1;                    // pair-kernel (ILP, blocks/SM) configuration (1: 2 x 2)
+    int pair_cfg = 3;                    // pair-kernel configuration without tuning, and the tuner's
+                                         // default (3: 4 facet pairs per step x 2 blocks per SM)
     int spin_limit = RP_SPIN_LIMIT;      // polls of a pair kernel's chunk wait before it gives up
     int stall_copies = 0;                // test mode (RP_TEST_STALL_COPIES): the pair kernels issue
                                          // no bulk copy, so their first wait runs out (short limit)
