@@ -1251,9 +1251,22 @@ int launch_pairs(const std::vector<Seg*>& ps, const PairJob* d_jobs, const PairJ
         return RP_OK;
     }
     if (ps.size() > 1 && cfg >= 4) {
-        if (par) ws->fork(st);
+        // segments by decreasing work (items x facet-part capacity x targets
+        // per block), dealt round robin to the auxiliary streams: each
+        // stream's last launches are its short ones
+        std::vector<size_t> order(ps.size());
+        std::vector<double> work(ps.size());
         for (size_t i = 0; i < ps.size(); ++i) {
-            const cudaStream_t ss = par ? ws->aux[i % rp_workspace::kAux] : st;
+            const Seg& g = *ps[i];
+            const double tb = (double)((g.L.tstride + RP_PAIR_THREADS - 1) / RP_PAIR_THREADS);
+            work[i] = (double)g.nb * tb * (double)g.L.rstride * (double)std::min<int64_t>(g.L.tstride, RP_PAIR_THREADS);
+            order[i] = i;
+        }
+        std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return work[a] > work[b]; });
+        if (par) ws->fork(st);
+        for (size_t k = 0; k < order.size(); ++k) {
+            const size_t i = order[k];
+            const cudaStream_t ss = par ? ws->aux[k % rp_workspace::kAux] : st;
             if (int rc = launch_pairs_one(*ps[i], seg_work + i, cfg - 4, sms, ss)) return rc;
             RP_LAUNCHED();
         }
