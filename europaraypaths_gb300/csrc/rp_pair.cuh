@@ -614,112 +614,70 @@ __device__ __forceinline__ void bin_add(float xr, float vre, float vim, int blo,
     }
 }
 
+// Both lanes' bins, floor(x), without the conversion unit: x + 1.5 2^23
+// rounded down lies in [2^23, 2^24), where the FP32 grid is the integers, so
+// it is 1.5 2^23 + floor(x) exactly for |x| < 2^22, and its bit pattern is
+// 0x4B400000 + floor(x).  fl = floor(x) as floats (exact); s0, s1 = the
+// slots, floor(x) clamped to [0, HI] by one unsigned min.  Anything else
+// (x < 0, |x| >= 2^22, NaN) lands in slot HI, and no slot leaves the window.
+template <unsigned HI>
+__device__ __forceinline__ void floor_slots2(f2 x, f2& fl, unsigned& s0, unsigned& s1) {
+    const f2 M = bc(12582912.f);
+    const f2 t = __fadd2_rd(x, M);
+    fl = add2(t, neg2(M));
+    s0 = min(__float_as_uint(t.x) - 0x4B400000u, HI);
+    s1 = min(__float_as_uint(t.y) - 0x4B400000u, HI);
+}
+
+// Adds (v0 += a0 (c, s), v1 += a1 (c, s)) to the window bins of slot sl and
+// sl + 1 of the thread whose column starts at wt = win + tid.
+__device__ __forceinline__ void win_add2(float2* wt, unsigned sl, float c, float s, float a0, float a1) {
+    float2* p0 = wt + sl * RP_PAIR_THREADS;
+    float2* p1 = p0 + RP_PAIR_THREADS;
+    float2 v0 = *p0, v1 = *p1;
+    v0.x = fmaf(c, a0, v0.x);
+    v0.y = fmaf(s, a0, v0.y);
+    v1.x = fmaf(c, a1, v1.x);
+    v1.y = fmaf(s, a1, v1.y);
+    *p0 = v0;
+    *p1 = v1;
+}
+
 // bin_add for the two lanes of a pair evaluation in a chunk whose pairs all
 // fall inside the window and the trace (pair_item checks that per chunk and
 // warp): no range tests, no edge path, lane 0 before lane 1.  The clamp only
-// keeps a (never expected) stray bin inside the window.
-// bin_add_fast2 from the phasor's amplitude and direction: the split
-// weights take the amplitude (amp w and amp - amp w, one product fewer than
-// forming the phasor first), then multiply cos and sin.
+// keeps a (never expected) stray bin inside the window.  The phasor comes as
+// its amplitude and direction: the split weights take the amplitude (amp w
+// and amp - amp w, one product fewer than forming the phasor first), then
+// multiply cos and sin.
 template <int W>
 __device__ __forceinline__ void bin_add_fast2a(f2 xr, f2 amp, f2 cs, f2 sn, float2* win, int tid) {
     const int f0 = floor_i(xr.x), f1 = floor_i(xr.y);
+    const unsigned s0 = min((unsigned)f0, (unsigned)(W - 2)), s1 = min((unsigned)f1, (unsigned)(W - 2));
     const f2 w = fma2(make_float2((float)f0, (float)f1), bc(-1.f), xr);
     const f2 a1 = mul2(amp, w);
     const f2 a0 = add2(amp, neg2(a1));
-    {
-        const unsigned sl = min((unsigned)f0, (unsigned)(W - 2));
-        float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
-        float2* p1 = p0 + RP_PAIR_THREADS;
-        float2 v0 = *p0, v1 = *p1;
-        v0.x = fmaf(cs.x, a0.x, v0.x);
-        v0.y = fmaf(sn.x, a0.x, v0.y);
-        v1.x = fmaf(cs.x, a1.x, v1.x);
-        v1.y = fmaf(sn.x, a1.x, v1.y);
-        *p0 = v0;
-        *p1 = v1;
-    }
-    {
-        const unsigned sl = min((unsigned)f1, (unsigned)(W - 2));
-        float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
-        float2* p1 = p0 + RP_PAIR_THREADS;
-        float2 v0 = *p0, v1 = *p1;
-        v0.x = fmaf(cs.y, a0.y, v0.x);
-        v0.y = fmaf(sn.y, a0.y, v0.y);
-        v1.x = fmaf(cs.y, a1.y, v1.x);
-        v1.y = fmaf(sn.y, a1.y, v1.y);
-        *p0 = v0;
-        *p1 = v1;
-    }
+    float2* const wt = win + tid;
+    win_add2(wt, s0, cs.x, sn.x, a0.x, a1.x);
+    win_add2(wt, s1, cs.y, sn.y, a0.y, a1.y);
 }
 
-template <int W>
-__device__ __forceinline__ void bin_add_fast2(f2 xr, f2 vre, f2 vim, float2* win, int tid) {
-    const int f0 = floor_i(xr.x), f1 = floor_i(xr.y);
-    const f2 w = fma2(make_float2((float)f0, (float)f1), bc(-1.f), xr);
-    const f2 w0 = fma2(w, bc(-1.f), bc(1.f));
-    {
-        const unsigned sl = min((unsigned)f0, (unsigned)(W - 2));
-        float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
-        float2* p1 = p0 + RP_PAIR_THREADS;
-        float2 v0 = *p0, v1 = *p1;
-        v0.x = fmaf(vre.x, w0.x, v0.x);
-        v0.y = fmaf(vim.x, w0.x, v0.y);
-        v1.x = fmaf(vre.x, w.x, v1.x);
-        v1.y = fmaf(vim.x, w.x, v1.y);
-        *p0 = v0;
-        *p1 = v1;
-    }
-    {
-        const unsigned sl = min((unsigned)f1, (unsigned)(W - 2));
-        float2* p0 = &win[sl * RP_PAIR_THREADS + tid];
-        float2* p1 = p0 + RP_PAIR_THREADS;
-        float2 v0 = *p0, v1 = *p1;
-        v0.x = fmaf(vre.y, w0.y, v0.x);
-        v0.y = fmaf(vim.y, w0.y, v0.y);
-        v1.x = fmaf(vre.y, w.y, v1.x);
-        v1.y = fmaf(vim.y, w.y, v1.y);
-        *p0 = v0;
-        *p1 = v1;
-    }
-}
-
-// bin_add_fast2 for specular mode: the same bins and split weights, the
-// inbound phasor times g1 into win and the outbound one times g2 into win2.
+// The same bins and split weights in specular mode: the inbound phasor
+// times g1 into win and the outbound one times g2 into win2.
 __device__ __forceinline__ void bin_add_fast2s(f2 xr, f2 vre, f2 vim, f2 g1, f2 g2, float2* win, float2* win2,
                                                int tid) {
-    const int f0 = floor_i(xr.x), f1 = floor_i(xr.y);
-    const f2 w = fma2(make_float2((float)f0, (float)f1), bc(-1.f), xr);
+    f2 fl;
+    unsigned s0, s1;
+    floor_slots2<RP_WIN - 2>(xr, fl, s0, s1);
+    const f2 w = fma2(fl, bc(-1.f), xr);
     const f2 w0 = fma2(w, bc(-1.f), bc(1.f));
     const f2 ar = mul2(vre, g1), ai = mul2(vim, g1), br = mul2(vre, g2), bi = mul2(vim, g2);
-    const unsigned s0 = min((unsigned)f0, (unsigned)(RP_WIN - 2));
-    const unsigned s1 = min((unsigned)f1, (unsigned)(RP_WIN - 2));
-    float2* const W[2] = {win, win2};
-    const float re0[2] = {ar.x, br.x}, im0[2] = {ai.x, bi.x}, re1[2] = {ar.y, br.y}, im1[2] = {ai.y, bi.y};
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        float2* p0 = &W[h][s0 * RP_PAIR_THREADS + tid];
-        float2* p1 = p0 + RP_PAIR_THREADS;
-        float2 v0 = *p0, v1 = *p1;
-        v0.x = fmaf(re0[h], w0.x, v0.x);
-        v0.y = fmaf(im0[h], w0.x, v0.y);
-        v1.x = fmaf(re0[h], w.x, v1.x);
-        v1.y = fmaf(im0[h], w.x, v1.y);
-        *p0 = v0;
-        *p1 = v1;
-    }
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        float2* p0 = &W[h][s1 * RP_PAIR_THREADS + tid];
-        float2* p1 = p0 + RP_PAIR_THREADS;
-        float2 v0 = *p0, v1 = *p1;
-        v0.x = fmaf(re1[h], w0.y, v0.x);
-        v0.y = fmaf(im1[h], w0.y, v0.y);
-        v1.x = fmaf(re1[h], w.y, v1.x);
-        v1.y = fmaf(im1[h], w.y, v1.y);
-        *p0 = v0;
-        *p1 = v1;
-    }
+    float2* const wt = win + tid;
+    float2* const wt2 = win2 + tid;
+    win_add2(wt, s0, ar.x, ai.x, w0.x, w.x);
+    win_add2(wt2, s0, br.x, bi.x, w0.x, w.x);
+    win_add2(wt, s1, ar.y, ai.y, w0.y, w.y);
+    win_add2(wt2, s1, br.y, bi.y, w0.y, w.y);
 }
 
 // One ttype-0 phasor into the thread's window, or (outside it) its target
