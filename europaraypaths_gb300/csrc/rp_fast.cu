@@ -571,24 +571,59 @@ __global__ void k_t0_conv32(const C32* __restrict__ sum0, int nr, const C32* __r
 
 // Single-batch pair kernel: the batch's constants live in the parameter
 // bank.  Persistent: blocks take (trace, target block, part) items from a
-// work counter until all are done.
-template <int NT, int ILP, int MINB, bool ORTHO>
+// work counter until all are done.  SUB: the wave's parts are split further
+// (2^lparts parts, pair_sub), an instance of its own so that the common
+// kernel keeps its compile-time part count.
+template <int NT, int ILP, int MINB, bool ORTHO, bool SUB = false>
 __global__ void __launch_bounds__(RP_PAIR_THREADS, MINB)
 k_pairs32(const __grid_constant__ PairArgs A) {
     RP_PAIR_SMEM_DECL
-    const unsigned int items = (unsigned)A.nb * A.tblocks * RP_PARTS;
+    const int lp = SUB ? A.lparts : RP_LPARTS;
+    const unsigned int items = ((unsigned)A.nb * A.tblocks) << lp;
     for (;;) {
         if (tid == 0) s_item = atomicAdd(A.work, 1u);
         __syncthreads();
         const unsigned int item = s_item;
         __syncthreads();
         if (item >= items) break;
-        const int part = item % RP_PARTS;
-        const int tb = (item / RP_PARTS) % A.tblocks;
-        const int s = item / (RP_PARTS * A.tblocks);
-        if (!pair_item<NT, ILP, ORTHO, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase)) break;
+        if constexpr (SUB) {
+            const int part = item & ((1u << lp) - 1u);
+            const int tb = (item >> lp) % A.tblocks;
+            const int s = (item >> lp) / A.tblocks;
+            if (!pair_item<NT, ILP, ORTHO, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase, lp)) break;
+        } else {
+            const int part = item % RP_PARTS;
+            const int tb = (item / RP_PARTS) % A.tblocks;
+            const int s = item / (RP_PARTS * A.tblocks);
+            if (!pair_item<NT, ILP, ORTHO, false, RP_WIN_WIDE>(A, s, tb, part, bars, phase)) break;
+        }
     }
     RP_PAIR_SMEM_END
+}
+
+// Folds a wave's facet sub-parts back into its RP_PARTS parts: part p's row
+// element becomes the compensated sum of sub-parts p sub ... p sub + sub - 1
+// (in that order) at part p's place, so the compression reads RP_PARTS
+// parts as always.  A thread owns one element of every part and reads all
+// its sub-parts before it writes, so the fold runs in place.
+__global__ void k_fold_parts(float4* __restrict__ T, int64_t slot, int sub) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < slot;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        float4 out[RP_PARTS];
+#pragma unroll
+        for (int p = 0; p < RP_PARTS; ++p) {
+            float4 acc = T[(int64_t)p * sub * slot + e];
+            for (int j = 1; j < sub; ++j) {
+                const float4 u = T[((int64_t)p * sub + j) * slot + e];
+                acc = comp_add(acc, u.x, u.y);
+                acc.z = __fadd_rn(acc.z, u.z);
+                acc.w = __fadd_rn(acc.w, u.w);
+            }
+            out[p] = acc;
+        }
+#pragma unroll
+        for (int p = 0; p < RP_PARTS; ++p) T[(int64_t)p * slot + e] = out[p];
+    }
 }
 
 // ---------------------------------------------------------- compression --
@@ -891,7 +926,16 @@ void (*pick_cfg(int cfg, bool ortho))(const PairArgs) {
     }
 }
 
-void (*pick_pair_kernel(int deg, int cfg, bool ortho))(const PairArgs) {
+void (*pick_pair_kernel(int deg, int cfg, bool ortho, bool sub = false))(const PairArgs) {
+    if (sub) {      // split parts: the default shape (4 facet pairs per step, 2 blocks per SM)
+        switch (deg) {
+            case 3: return ortho ? k_pairs32<3, 4, 2, true, true> : k_pairs32<3, 4, 2, false, true>;
+            case 4: return ortho ? k_pairs32<4, 4, 2, true, true> : k_pairs32<4, 4, 2, false, true>;
+            case 5: return ortho ? k_pairs32<5, 4, 2, true, true> : k_pairs32<5, 4, 2, false, true>;
+            case 6: return ortho ? k_pairs32<6, 4, 2, true, true> : k_pairs32<6, 4, 2, false, true>;
+            default: return ortho ? k_pairs32<0, 4, 2, true, true> : k_pairs32<0, 4, 2, false, true>;
+        }
+    }
     switch (deg) {
         case 3: return pick_cfg<3>(cfg, ortho);
         case 4: return pick_cfg<4>(cfg, ortho);
@@ -1011,8 +1055,9 @@ struct Seg {
     int cmode = 0;          // compression storage mode (conv_mode)
     bool pairs = false;
     C32* T = nullptr; C32* Z = nullptr; C32* cscr = nullptr; C32* part = nullptr;
+    int sub = 1;            // facet sub-splits per part (pair_sub)
     // row elements of T (and T2); each is {high, low}, two C32
-    int64_t row_elems() const { return (int64_t)RP_PARTS * nb * L.tstride * Wt; }
+    int64_t row_elems() const { return (int64_t)RP_PARTS * sub * nb * L.tstride * Wt; }
     C32* T2 = nullptr;      // specular mode: outbound-leg parts
     C32* sum0 = nullptr; C32* r0 = nullptr; C32* t0scr = nullptr;   // ttype-0 targets
     double2* t0part = nullptr;
@@ -1137,6 +1182,8 @@ PairArgs seg_pair_args(const Seg& g) {
     P.TG = sc->d_targets_fast; P.nt = sc->nt; P.PR = sc->d_prisms; P.np = sc->np;
     P.bt0 = g.bt0; P.T = g.T; P.Wt = g.Wt; P.nb = g.nb;
     P.tblocks = (int)((g.L.tstride + RP_PAIR_THREADS - 1) / RP_PAIR_THREADS);
+    P.lparts = RP_LPARTS;
+    for (int k = g.sub; k > 1; k >>= 1) ++P.lparts;
     P.work = reinterpret_cast<unsigned int*>(g.misc + 1);
     P.err = reinterpret_cast<unsigned int*>(g.misc + 2);
     P.spin_limit = sc->spin_limit;
@@ -1217,11 +1264,11 @@ int launch_pairs_one(const Seg& g, unsigned int* work, int cfg, int sms, cudaStr
     const size_t pair_smem = pair_smem_bytes(RP_WIN_WIDE);
     PairArgs P = seg_pair_args(g);
     P.work = work;
-    void (*pk)(const PairArgs) = pick_pair_kernel(g.deg, cfg, g.sc->ortho != 0);
+    void (*pk)(const PairArgs) = pick_pair_kernel(g.deg, cfg, g.sc->ortho != 0, g.sub > 1);
     if (int rc = rp_allow_dyn_smem((const void*)pk, pair_smem)) return rc;
     int occ = 0;
     RP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk, RP_PAIR_THREADS, pair_smem));
-    const int64_t items = (int64_t)g.nb * P.tblocks * RP_PARTS;
+    const int64_t items = ((int64_t)g.nb * P.tblocks) << P.lparts;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(occ, 1) * sms, items));
     pk<<<grid, RP_PAIR_THREADS, pair_smem, st>>>(P);
     return RP_OK;
@@ -1310,6 +1357,40 @@ int zero_pairs(const std::vector<Seg*>& ps, unsigned int* d_work, unsigned int* 
 // outputs re-zeroed after, and every candidate is probed twice (the best of
 // its two times counts).  Tuned per kind: single kernel (0), multi-segment
 // (1) or specular (2), and sinc degree.
+// Facet sub-splits per part for a wave of one segment (default mode,
+// ttype-1 targets only).  A small call's items, traces x target blocks x
+// RP_PARTS, can leave most of the pair kernel's resident blocks idle (one
+// trace of a 36-block scene: 144 items for 304 blocks); splitting each
+// part's facet range sub ways, into rows of their own that k_fold_parts
+// adds back into the parts, spreads the call over them.  sub doubles while
+// the items still fit one round of the slots, each sub-part keeps at least
+// two chunks of facets and the extra rows stay under 256 MiB.
+const int64_t kSubBytes = (int64_t)256 << 20;
+
+int pair_sub(const Seg& g, int slots) {
+    const rp_scene* sc = g.sc;
+    const FastLayout& L = g.L;
+    if (sc->dp.specular || sc->nt1 < sc->nt) return 1;
+    const int64_t tblocks = (L.tstride + RP_PAIR_THREADS - 1) / RP_PAIR_THREADS;
+    const int64_t items = (int64_t)L.nb * tblocks * RP_PARTS;
+    const int64_t part_bytes = (int64_t)2 * RP_PARTS * L.nb * L.tstride * L.Wt * (int64_t)sizeof(C32);
+    int sub = 1;
+    while (sub < 32 && items * sub * 2 <= slots && L.mstride >= (int64_t)RP_PARTS * sub * 4 &&
+           part_bytes * (2 * sub - 1) <= kSubBytes)
+        sub *= 2;
+    return sub;
+}
+
+// Upper bound of pair_sub's extra row bytes for a one-segment call laid out
+// as L, whose window width is a bound of the one the call will measure.
+int64_t pair_sub_bound_bytes(const rp_scene* sc, const FastLayout& L, int slots) {
+    if (sc->dp.specular || sc->nt1 < sc->nt) return 0;
+    const int64_t tblocks = (L.tstride + RP_PAIR_THREADS - 1) / RP_PAIR_THREADS;
+    if ((int64_t)L.nb * tblocks * RP_PARTS * 2 > slots || L.mstride < (int64_t)RP_PARTS * 4) return 0;
+    const int64_t part_bytes = (int64_t)2 * RP_PARTS * L.nb * L.tstride * L.Wt * (int64_t)sizeof(C32);
+    return std::min<int64_t>(kSubBytes, part_bytes * 31);
+}
+
 int choose_cfg(const std::vector<Seg*>& ps, const PairJob* d_jobs, const PairJob* h_jobs,
                const unsigned int* d_start, unsigned int* d_work, unsigned int* seg_work, int sms, cudaStream_t st,
                rp_workspace* ws, bool par, int* cfg_out) {
@@ -1325,7 +1406,10 @@ int choose_cfg(const std::vector<Seg*>& ps, const PairJob* d_jobs, const PairJob
     }
     int c = tuned_lookup(multi, deg);
     if (c >= 0) { *cfg_out = c; return RP_OK; }
-    if (ws->graph_mode == 2) {      // no probes under capture (the warm-up call tuned)
+    // no probes under capture (the warm-up call tuned), nor for a wave of
+    // split parts (one kernel shape whatever the configuration; tuning
+    // waits for a call that can tell the configurations apart)
+    if (ws->graph_mode == 2 || (multi == 0 && ps[0]->sub > 1)) {
         const int d = ps[0]->sc->pair_cfg;
         *cfg_out = spec ? (d & 1) : (multi == 1 ? d : (d & 3));
         return RP_OK;
@@ -1428,6 +1512,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
             gslot[g.cmode] = std::max(gslot[g.cmode], conv_gslot(g.sc));
         }
     }
+    if (nseg == 1 && ps.size() == 1) ps[0]->sub = pair_sub(*ps[0], 2 * sms);
     // one global compression scratch region per wave, shared by the mode-1
     // and mode-2 launches (they run one after the other on one stream)
     const size_t gscr_n = (size_t)sms * std::max(gslot[1], gslot[2]);
@@ -1453,7 +1538,8 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     {
         size_t need = 4096 + 1024 * (cg.size() + 1) + (ps.size() + ncs) * (sizeof(PairJob) + sizeof(ConvArgs) + 64)
                       + gscr_n * sizeof(C32);
-        for (Seg& g : segs) need += seg_pair_bytes(g.sc, g.L);
+        for (Seg& g : segs)
+            need += seg_pair_bytes(g.sc, g.L) + (size_t)(g.sub - 1) * 2 * RP_PARTS * g.nb * g.L.tstride * g.Wt * sizeof(C32);
         if (capturing && need > ws->arena2.cap) {
             rp_set_error("graph capture: the pair-stage buffers outgrew the warm-up call's");
             return RP_ERR_INTERNAL;
@@ -1464,8 +1550,8 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
     Arena& b = ws->arena2;
     b.reset();
     for (Seg& g : segs) {
-        g.T = b.take<C32>((size_t)2 * RP_PARTS * g.nb * g.L.tstride * g.Wt);
-        g.T2 = g.sc->dp.specular ? b.take<C32>((size_t)2 * RP_PARTS * g.nb * g.L.tstride * g.Wt) : nullptr;
+        g.T = b.take<C32>((size_t)2 * g.row_elems());
+        g.T2 = g.sc->dp.specular ? b.take<C32>((size_t)2 * g.row_elems()) : nullptr;
         g.dpart = g.sc->dp.cmode == 2 ? b.take<double2>((size_t)g.nb * RP_DS_GROUPS * g.sc->nr) : nullptr;
         if (g.t0rec) {
             g.sum0 = b.take<C32>((size_t)g.nb * g.sc->nr);
@@ -1564,6 +1650,13 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
             const int64_t items = (int64_t)g.nb * P0.tblocks * RP_PARTS;
             rc = launch_pairs_t0(g.deg, g.sc->ortho != 0, g.sc->dp.specular != 0, P0, items, sms, st);
             if (rc) return rc;
+            RP_LAUNCHED();
+        }
+        for (Seg* g : ps) {
+            if (g->sub == 1) continue;
+            const int64_t slot = (int64_t)g->nb * g->L.tstride * g->Wt;
+            const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((slot + 255) / 256, (int64_t)8 * sms));
+            k_fold_parts<<<grid, 256, 0, st>>>(reinterpret_cast<float4*>(g->T), slot, g->sub);
             RP_LAUNCHED();
         }
     } else {
@@ -1834,7 +1927,7 @@ std::vector<int64_t> host_facet_bounds(const rp_scene* sc, const double* tr, int
 // facet bounds fb) fits the budget.
 void next_segment(const rp_scene* sc, const std::vector<int>& ub, const std::vector<int64_t>& fb,
                   const std::vector<int>& wb, int64_t s0, int64_t ns, int* nb_out, int64_t* tmax_out,
-                  int64_t* fmax_out, size_t* bytes_out) {
+                  int64_t* fmax_out, size_t* bytes_out, int* wmax_out = nullptr) {
     int nb = 0;
     int64_t tmax = 0, fmax = 0;
     int wmax = 1;
@@ -1858,6 +1951,7 @@ void next_segment(const rp_scene* sc, const std::vector<int>& ub, const std::vec
     *tmax_out = tmax;
     *fmax_out = fmax;
     *bytes_out = bytes;
+    if (wmax_out) *wmax_out = wmax;
 }
 
 int check_scene(const rp_scene* sc) {
@@ -1878,15 +1972,20 @@ size_t rp_fast_plan_bytes(const rp_scene* sc, const double* h_traces, int64_t ns
     std::vector<int> wb(ns, sc->nr);
     std::vector<int64_t> fb = h_traces ? host_facet_bounds(sc, h_traces, ns, &wb) : std::vector<int64_t>(ns, sc->nf);
     size_t peak = 0, wave = 0;
-    for (int64_t s0 = 0; s0 < ns;) {
-        int nb;
+    int nseg = 0;
+    for (int64_t s0 = 0; s0 < ns; ++nseg) {
+        int nb, wmax = 1;
         int64_t tmax, fmax;
         size_t bytes;
-        next_segment(sc, ub, fb, wb, s0, ns, &nb, &tmax, &fmax, &bytes);
+        next_segment(sc, ub, fb, wb, s0, ns, &nb, &tmax, &fmax, &bytes, &wmax);
         if (wave > 0 && (sc->dp.specular || wave + bytes > kFastBudget)) {     // specular: one segment a wave
             peak = std::max(peak, wave);
             wave = 0;
         }
+        // a call of one segment may split its facet parts (pair_sub): the
+        // extra rows, bounded with the segment's window bound
+        if (s0 == 0 && nb >= ns)
+            bytes += (size_t)pair_sub_bound_bytes(sc, fast_layout(sc, nb, tmax, wmax, fmax), 2 * sc->sm_count);
         wave += bytes;
         s0 += nb;
     }

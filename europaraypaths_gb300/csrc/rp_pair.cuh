@@ -22,6 +22,7 @@
 #define RP_WIN_WIDE 24        // the default-mode and ttype-0 kernels' window: a 256-facet chunk of
                               // 2.5 m facets at 12.5 m bins spans up to ~14 bins for one target
 #define RP_PARTS 4            // facet-range splits per (trace, target block)
+#define RP_LPARTS 2           // log2 RP_PARTS
 
 namespace rpk {
 
@@ -152,7 +153,7 @@ struct PairArgs {
     const double* PR;   // prisms (alpha, box) FP64 SoA
     int64_t np;
     const int* bt0;
-    C32* T;             // [RP_PARTS][nb][tstride][Wt] row elements, each {high, low} (two C32)
+    C32* T;             // [2^lparts][nb][tstride][Wt] row elements, each {high, low} (two C32)
     int Wt;
     int nb;
     int tblocks;        // target blocks per trace
@@ -193,6 +194,9 @@ struct PairArgs {
     int rf;                 // rerad_funct: 0 none, 1-3 angle threshold, 4 Gaussian
     float rcos;             // threshold on cos(TargetTh) for rf 1-3
     float rgl;              // rf 4: -0.5 log2(e) / (pi_F/180)^2
+    // log2 of the facet-range parts per (trace, target block): log2 RP_PARTS,
+    // more in a wave whose parts are split further (k_pairs32's SUB instance)
+    int lparts;
 };
 
 // A job of the multi-job pair kernel: a batch's arguments and its sinc
@@ -854,7 +858,8 @@ __device__ __forceinline__ void abort_block(const PairArgs& A, uint64_t* bars, c
 // One work item of the pair kernels; false when a chunk's wait ran out (the
 // kernel then stops taking items).
 template <int NT, int ILP, bool ORTHO, bool SPEC, int W, class PA>
-__device__ __forceinline__ bool pair_item(const PA& A, int s, int tb, int part, uint64_t* bars, uint32_t* phase) {
+__device__ __forceinline__ bool pair_item(const PA& A, int s, int tb, int part, uint64_t* bars, uint32_t* phase,
+                                          int lparts = RP_LPARTS) {
     static_assert(!SPEC || W == RP_WIN, "the specular layout holds two RP_WIN windows");
     // every hot shared array is derived here from the shared symbol itself
     FacetPair* srec = reinterpret_cast<FacetPair*>(pair_smem);                     // [2][RP_CHUNK_PAIRS]
@@ -872,8 +877,9 @@ __device__ __forceinline__ bool pair_item(const PA& A, int s, int tb, int part, 
     const int n = A.nill[s];
     if (tb * RP_PAIR_THREADS >= nq || n == 0) return true;
     const int nchunks = (n + RP_CHUNK - 1) / RP_CHUNK;
-    const int k0 = (int)((int64_t)nchunks * part / RP_PARTS);
-    const int k1 = (int)((int64_t)nchunks * (part + 1) / RP_PARTS);
+    const int64_t np = (int64_t)1 << lparts;
+    const int k0 = (int)((int64_t)nchunks * part / np);
+    const int k1 = (int)((int64_t)nchunks * (part + 1) / np);
     if (k0 >= k1) return true;
     const int q = tb * RP_PAIR_THREADS + tid;
     const bool active = q < nq;
