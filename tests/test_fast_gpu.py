@@ -155,3 +155,29 @@ def test_fast_narrow_aperture_tile_culling(built_lib, oracle):
     got, ref, cnt, rcnt = fast_vs_oracle(sc, oracle)
     assert np.array_equal(cnt, rcnt) and 0 < cnt[:, 0].max() < 40000 // 4
     check(got, ref)
+
+
+def test_fast_split_parts_small_call(built_lib, oracle):
+    # one trace of the small plain scene fills a few target blocks, so its
+    # facet parts are split further (k_pairs32's split instance) and folded
+    # back before the compression: one launch more than the same trace
+    # inside a 40-trace call, the same result to FP32 summation order, and
+    # within the bar against the oracle
+    from europaraypaths_gb300 import scenes, simulator, traces as tr_mod, param_gen
+    sc = scenes.small_plain()
+    p = param_gen.to_rp_params(sc["params"])
+    tr = tr_mod.linear_track(p)
+    scene = simulator.Scene(sc["params"], sc["facets"], sc["targets"])
+    try:
+        scene.simulate(tr[30:70], form="fast")      # warm-up: the first call may tune
+        many = scene.simulate(tr[30:70], form="fast")
+        n_many = simulator.last_launch_count()
+        one = scene.simulate(tr[50:51], form="fast")
+        n_one = simulator.last_launch_count()
+    finally:
+        scene.close()
+    assert n_one == n_many + 1, (n_one, n_many)
+    assert rel_l2(one[0], many[20]) <= 1e-6, rel_l2(one[0], many[20])
+    assert np.array_equal(peak_bins(one), peak_bins(many[20:21]))
+    ref, _ = oracle.simulate(scene.params, sc["facets"], sc["targets"], tr[50:51])
+    check(one, ref)
