@@ -1364,8 +1364,8 @@ int zero_pairs(const std::vector<Seg*>& ps, unsigned int* d_work, unsigned int* 
 // part's facet range sub ways, into rows of their own that k_fold_parts
 // adds back into the parts, spreads the call over them.  sub doubles while
 // the items still fit one round of the slots, each sub-part keeps at least
-// two chunks of facets and the extra rows stay under 256 MiB.
-const int64_t kSubBytes = (int64_t)256 << 20;
+// two chunks of facets and the extra rows stay under 1 GiB.
+const int64_t kSubBytes = (int64_t)1 << 30;
 
 int pair_sub(const Seg& g, int slots) {
     const rp_scene* sc = g.sc;
