@@ -241,6 +241,26 @@ def run_batch(args, objs, tracks, stream):
     torch.cuda.synchronize()
     ts = time.perf_counter() - t0
     ws.close()
+    # the first timed step's call recorded as one CUDA graph
+    # (rp_graph_create_batch) and replayed on the same device buffers
+    g = simulator.capture_batch([(o, d_tr[1][i].cpu().numpy()) for i, o in enumerate(objs)], d_tr[1], d_out[1])
+    try:
+        ref = [torch.view_as_real(o).clone() for o in d_out[1]]      # the capture's eager batch call
+        for o in d_out[1]:
+            o.fill_(complex(float("nan"), float("nan")))
+        torch.cuda.synchronize()
+        g.launch(stream)
+        stream.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps - 1):
+            g.launch(stream)
+        stream.synchronize()
+        tg = (time.perf_counter() - t0) / (steps - 1)
+        g.check(stream)
+        same = all(torch.equal(a.view(torch.int32), torch.view_as_real(b).view(torch.int32))
+                   for a, b in zip(ref, d_out[1]))
+    finally:
+        g.close()
     bands = {}
     for o in objs:
         key = f"{o.params.frequency / 1e6:g} MHz/{o.nr} bins"
@@ -250,6 +270,9 @@ def run_batch(args, objs, tracks, stream):
             "gpu_launches_per_step": launches / (steps - 1), "stage_ms_per_step": stage,
             "one_scene_per_call": {"value": pairs / ts, "ms_per_step": 1e3 * ts / (steps - 1)},
             "batched_over_one_at_a_time": ts / tb,
+            "graph": {"replay_ms_per_call": 1e3 * tg, "direct_ms_per_call": 1e3 * tb / (steps - 1),
+                      "bitwise_equal": bool(same),
+                      "note": "the whole batch call as one CUDA graph (rp_graph_create_batch), host wall clock"},
             "tuned_multi_cfg": simulator.autotune_query(True),
             "mix": bands}
 

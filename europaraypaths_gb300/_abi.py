@@ -94,6 +94,7 @@ _SIGS = {
                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rp_simulate_batch": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rp_autotune": ([ctypes.c_int], ctypes.c_int),
+    "rp_split_parts": ([ctypes.c_int], ctypes.c_int),
     "rp_autotune_query": ([ctypes.c_int, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
     "rp_server_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p,
                           ctypes.c_void_p], ctypes.c_int),
@@ -101,6 +102,8 @@ _SIGS = {
     "rp_server_configure": ([ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "rp_graph_create": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                          ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "rp_graph_create_batch": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)],
+                              ctypes.c_int),
     "rp_graph_launch": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rp_graph_check": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rp_graph_destroy": ([ctypes.c_void_p], ctypes.c_int),

@@ -643,21 +643,21 @@ extern "C" int rp_simulate_device(rp_scene* s, const double* d_traces, int64_t n
 }
 
 // ------------------------------------------------------------ graphs --
-// A fast-form call recorded as a CUDA graph (rp_graph_create): planned from
-// the host copy of its traces, its target windows sized by host bounds, run
+// A fast-form call (rp_graph_create) or batch (rp_graph_create_batch)
+// recorded as a CUDA graph: planned from the host copy of its traces, its
+// target windows sized by host bounds, run
 // once eagerly (which reserves the buffers and tunes the pair kernel), then
 // run again under stream capture into a graph that replays the whole call --
 // setup, pair stage, compression, tails -- with one launch.  The graph owns
 // its workspace (device buffers, auxiliary streams, the pinned staging of its
 // job tables and of the flags and counts it reads back).
 struct rp_graph {
-    rp_scene* s = nullptr;
     rp_workspace ws;
     cudaStream_t st = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    int64_t ns = 0;
-    std::vector<double> h_traces;
+    int64_t ns = 0;                                 // traces over all jobs
+    std::vector<std::vector<double>> h_traces;      // per job: the host traces it was planned with
 };
 
 static void graph_release(rp_graph* g) {
@@ -680,6 +680,40 @@ static void graph_release(rp_graph* g) {
     delete g;
 }
 
+// Records jobs (planned from g's host trace copies) on g's stream: the eager
+// call first (buffers, tuning and every check of a plain call), then the same
+// call under stream capture, instantiated.
+static int graph_record(rp_graph* g, const std::vector<rp_job>& jobs, int64_t ns_total) {
+    int rc = RP_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking);
+    const size_t pin_bytes = ((size_t)4 << 20) + 16 * (size_t)ns_total + 4096 * jobs.size();
+    if (e == cudaSuccess) e = cudaHostAlloc((void**)&g->ws.pin, pin_bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) return rp_cuda_fail(e, "rp_graph_create");
+    g->ws.pin_cap = pin_bytes;
+    const int timing = g_timer.enabled;
+    g->ws.graph_mode = 1;
+    g_timer.enabled = 0;
+    rc = rp_fast_batch(jobs.data(), (int)jobs.size(), &g->ws, g->st);
+    if (!rc && (e = cudaStreamSynchronize(g->st)) != cudaSuccess) rc = rp_cuda_fail(e, "rp_graph_create");
+    if (!rc) {
+        g->ws.graph_mode = 2;
+        g->ws.pin_off = 0;
+        g->ws.graph_rb.clear();
+        e = cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            rc = rp_cuda_fail(e, "rp_graph_create: begin capture");
+        } else {
+            rc = rp_fast_batch(jobs.data(), (int)jobs.size(), &g->ws, g->st);
+            e = cudaStreamEndCapture(g->st, &g->graph);
+            if (!rc && e != cudaSuccess) rc = rp_cuda_fail(e, "rp_graph_create: end capture");
+        }
+        if (!rc && (e = cudaGraphInstantiate(&g->exec, g->graph, 0)) != cudaSuccess)
+            rc = rp_cuda_fail(e, "rp_graph_create: instantiate");
+    }
+    g_timer.enabled = timing;
+    return rc;
+}
+
 extern "C" int rp_graph_create(rp_scene* s, const double* h_traces, const double* d_traces, int64_t ns,
                                void* d_out, rp_graph** out) {
     if (!s || !h_traces || !d_traces || !d_out || !out || ns <= 0) {
@@ -689,41 +723,48 @@ extern "C" int rp_graph_create(rp_scene* s, const double* h_traces, const double
     *out = nullptr;
     RP_CUDA(cudaSetDevice(s->device));
     rp_graph* g = new rp_graph();
-    g->s = s;
     g->ns = ns;
     g->ws.device = s->device;
-    g->h_traces.assign(h_traces, h_traces + 9 * ns);
-    int rc = RP_OK;
-    cudaError_t e = cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking);
-    const size_t pin_bytes = ((size_t)4 << 20) + 16 * (size_t)ns;
-    if (e == cudaSuccess) e = cudaHostAlloc((void**)&g->ws.pin, pin_bytes, cudaHostAllocDefault);
-    if (e != cudaSuccess) rc = rp_cuda_fail(e, "rp_graph_create");
-    g->ws.pin_cap = pin_bytes;
-    g->ws.plan_traces = g->h_traces.data();
-    const int timing = g_timer.enabled;
-    if (!rc) {
-        // the eager call: buffers, tuning, and every check of a plain call
-        g->ws.graph_mode = 1;
-        g_timer.enabled = 0;
-        rc = rp_fast_run(s, &g->ws, d_traces, ns, d_out, 0, nullptr, g->st);
-        if (!rc && (e = cudaStreamSynchronize(g->st)) != cudaSuccess) rc = rp_cuda_fail(e, "rp_graph_create");
+    g->h_traces.assign(1, std::vector<double>(h_traces, h_traces + 9 * ns));
+    g->ws.plan_traces = g->h_traces[0].data();
+    const int rc = graph_record(g, std::vector<rp_job>{rp_job{s, d_traces, ns, d_out, nullptr}}, ns);
+    if (rc) {
+        cudaGetLastError();
+        graph_release(g);
+        return rc;
     }
-    if (!rc) {
-        g->ws.graph_mode = 2;
-        g->ws.pin_off = 0;
-        g->ws.graph_rb.clear();
-        e = cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal);
-        if (e != cudaSuccess) {
-            rc = rp_cuda_fail(e, "rp_graph_create: begin capture");
-        } else {
-            rc = rp_fast_run(s, &g->ws, d_traces, ns, d_out, 0, nullptr, g->st);
-            e = cudaStreamEndCapture(g->st, &g->graph);
-            if (!rc && e != cudaSuccess) rc = rp_cuda_fail(e, "rp_graph_create: end capture");
+    *out = g;
+    return RP_OK;
+}
+
+extern "C" int rp_graph_create_batch(const rp_job* jobs, int njobs, const double* const* h_traces,
+                                     rp_graph** out) {
+    if (!jobs || njobs <= 0 || !h_traces || !out) {
+        rp_set_error("rp_graph_create_batch: bad argument");
+        return RP_ERR_ARG;
+    }
+    *out = nullptr;
+    int64_t ns_total = 0;
+    for (int j = 0; j < njobs; ++j) {
+        const rp_job& b = jobs[j];
+        if (!b.scene || b.ns <= 0 || !b.d_traces || !b.d_out || !h_traces[j] ||
+            b.scene->device != jobs[0].scene->device) {
+            rp_set_error("rp_graph_create_batch: job %d: bad scene, trace tables, output or device", j);
+            return RP_ERR_ARG;
         }
-        if (!rc && (e = cudaGraphInstantiate(&g->exec, g->graph, 0)) != cudaSuccess)
-            rc = rp_cuda_fail(e, "rp_graph_create: instantiate");
+        ns_total += b.ns;
     }
-    g_timer.enabled = timing;
+    RP_CUDA(cudaSetDevice(jobs[0].scene->device));
+    rp_graph* g = new rp_graph();
+    g->ns = ns_total;
+    g->ws.device = jobs[0].scene->device;
+    std::vector<rp_job> js(jobs, jobs + njobs);
+    for (int j = 0; j < njobs; ++j) {
+        js[j].counts = nullptr;         // rp_graph_check reports the counts
+        g->h_traces.emplace_back(h_traces[j], h_traces[j] + 9 * jobs[j].ns);
+    }
+    for (const std::vector<double>& h : g->h_traces) g->ws.plan_jobs.push_back(h.data());
+    const int rc = graph_record(g, js, ns_total);
     if (rc) {
         cudaGetLastError();
         graph_release(g);

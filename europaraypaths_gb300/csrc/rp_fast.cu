@@ -34,6 +34,7 @@
 #include <cstring>
 #include <cmath>
 #include <map>
+#include <atomic>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -1056,6 +1057,7 @@ struct Seg {
     bool pairs = false;
     C32* T = nullptr; C32* Z = nullptr; C32* cscr = nullptr; C32* part = nullptr;
     int sub = 1;            // facet sub-splits per part (pair_sub)
+    int64_t cbase = 0;      // first trace of the segment's job over all jobs of the call
     // row elements of T (and T2); each is {high, low}, two C32
     int64_t row_elems() const { return (int64_t)RP_PARTS * sub * nb * L.tstride * Wt; }
     C32* T2 = nullptr;      // specular mode: outbound-leg parts
@@ -1366,14 +1368,19 @@ int zero_pairs(const std::vector<Seg*>& ps, unsigned int* d_work, unsigned int* 
 // the items still fit one round of the slots, each sub-part keeps at least
 // two chunks of facets and the extra rows stay under 1 GiB.
 const int64_t kSubBytes = (int64_t)1 << 30;
+std::atomic<int> g_split_parts{1};      // rp_split_parts
 
 int pair_sub(const Seg& g, int slots) {
     const rp_scene* sc = g.sc;
     const FastLayout& L = g.L;
-    if (sc->dp.specular || sc->nt1 < sc->nt) return 1;
+    if (!g_split_parts.load() || sc->dp.specular || sc->nt1 < sc->nt) return 1;
     const int64_t tblocks = (L.tstride + RP_PAIR_THREADS - 1) / RP_PAIR_THREADS;
     const int64_t items = (int64_t)L.nb * tblocks * RP_PARTS;
-    const int64_t part_bytes = (int64_t)2 * RP_PARTS * L.nb * L.tstride * L.Wt * (int64_t)sizeof(C32);
+    // the row cap takes the host bound of the window width where the call
+    // has one (the width a graph replay lays out), so that a direct call and
+    // a replay of the same traces split alike and sum in the same order
+    const int64_t wb = std::max<int64_t>(L.Wt, std::max(1, std::min(sc->nr, (g.wmax + 3) & ~3)));
+    const int64_t part_bytes = (int64_t)2 * RP_PARTS * L.nb * L.tstride * wb * (int64_t)sizeof(C32);
     int sub = 1;
     while (sub < 32 && items * sub * 2 <= slots && L.mstride >= (int64_t)RP_PARTS * sub * 4 &&
            part_bytes * (2 * sub - 1) <= kSubBytes)
@@ -1384,7 +1391,7 @@ int pair_sub(const Seg& g, int slots) {
 // Upper bound of pair_sub's extra row bytes for a one-segment call laid out
 // as L, whose window width is a bound of the one the call will measure.
 int64_t pair_sub_bound_bytes(const rp_scene* sc, const FastLayout& L, int slots) {
-    if (sc->dp.specular || sc->nt1 < sc->nt) return 0;
+    if (!g_split_parts.load() || sc->dp.specular || sc->nt1 < sc->nt) return 0;
     const int64_t tblocks = (L.tstride + RP_PAIR_THREADS - 1) / RP_PAIR_THREADS;
     if ((int64_t)L.nb * tblocks * RP_PARTS * 2 > slots || L.mstride < (int64_t)RP_PARTS * 4) return 0;
     const int64_t part_bytes = (int64_t)2 * RP_PARTS * L.nb * L.tstride * L.Wt * (int64_t)sizeof(C32);
@@ -1787,7 +1794,7 @@ int run_wave(std::vector<Seg>& segs, rp_workspace* ws, cudaStream_t st) {
             RP_CUDA(cudaMemcpyAsync(hc2, segs[i].nill, sizeof(int) * segs[i].nb, cudaMemcpyDeviceToHost, st));
             RP_CUDA(cudaMemcpyAsync(hc2 + segs[i].nb, segs[i].ntl, sizeof(int) * segs[i].nb, cudaMemcpyDeviceToHost,
                                     st));
-            ws->graph_rb.push_back(rp_workspace::Readback{hm, hc2, segs[i].nb, segs[i].s0});
+            ws->graph_rb.push_back(rp_workspace::Readback{hm, hc2, segs[i].nb, segs[i].cbase + segs[i].s0});
         }
         return RP_OK;
     }
@@ -1999,20 +2006,22 @@ size_t rp_fast_scratch(const rp_scene* sc, int64_t ns) { return rp_fast_plan_byt
 int rp_fast_batch(const rp_job* jobs, int njobs, rp_workspace* ws, cudaStream_t st) {
     std::vector<SceneConst> kc(njobs);
     std::vector<std::vector<double>> tr(njobs);
-    // graph mode plans a single job from the host copy of its traces (no
-    // device readback: the call may be under stream capture)
-    const bool host_plan = ws->graph_mode && ws->plan_traces;
-    if (host_plan && njobs != 1) {
-        rp_set_error("graph capture: one job per call");
-        return RP_ERR_UNSUPPORTED;
+    // graph mode plans from the host copies of the jobs' traces (no device
+    // readback: the call may be under stream capture)
+    const bool host_plan = ws->graph_mode && (ws->plan_traces || !ws->plan_jobs.empty());
+    if (host_plan && (ws->plan_jobs.empty() ? njobs != 1 : (int)ws->plan_jobs.size() != njobs)) {
+        rp_set_error("graph capture: the planned traces do not match the call's jobs");
+        return RP_ERR_INTERNAL;
     }
     for (int j = 0; j < njobs; ++j) {
         int rc = check_scene(jobs[j].scene);
         if (rc) return rc;
         kc[j] = scene_const(jobs[j].scene);
         tr[j].resize(9 * (size_t)jobs[j].ns);
-        if (host_plan)
-            std::copy(ws->plan_traces, ws->plan_traces + 9 * jobs[j].ns, tr[j].begin());
+        if (host_plan) {
+            const double* h = ws->plan_jobs.empty() ? ws->plan_traces : ws->plan_jobs[j];
+            std::copy(h, h + 9 * jobs[j].ns, tr[j].begin());
+        }
         else if (jobs[j].ns)
             RP_CUDA(cudaMemcpyAsync(tr[j].data(), jobs[j].d_traces, sizeof(double) * 9 * jobs[j].ns,
                                     cudaMemcpyDeviceToHost, st));
@@ -2020,6 +2029,7 @@ int rp_fast_batch(const rp_job* jobs, int njobs, rp_workspace* ws, cudaStream_t 
     if (!host_plan) RP_CUDA(cudaStreamSynchronize(st));
     std::vector<Seg> wave;
     size_t wave_bytes = 0;
+    int64_t cbase = 0;      // the job's first trace over all jobs (graph readback)
     for (int j = 0; j < njobs; ++j) {
         rp_scene* sc = jobs[j].scene;
         const int64_t ns = jobs[j].ns;
@@ -2056,10 +2066,12 @@ int rp_fast_batch(const rp_job* jobs, int njobs, rp_workspace* ws, cudaStream_t 
             g.coefr = kc[j].coefr;
             g.Lw = fast_layout(sc, nb, tmax, nr, fmax);
             for (int64_t k = s0; k < s0 + nb; ++k) g.wmax = std::max(g.wmax, wb[k]);
+            g.cbase = cbase;
             wave.push_back(g);
             wave_bytes += bytes;
             s0 += nb;
         }
+        cbase += ns;
     }
     if (!wave.empty()) {
         int rc = run_wave(wave, ws, st);
@@ -2098,6 +2110,11 @@ int rp_fast_run(rp_scene* sc, rp_workspace* ws, const double* d_traces, int64_t 
         if (rc) return rc;
         s0 += nb;
     }
+    return RP_OK;
+}
+
+extern "C" int rp_split_parts(int enable) {
+    g_split_parts.store(enable ? 1 : 0);
     return RP_OK;
 }
 

@@ -115,16 +115,18 @@ struct rp_workspace {
     void fork(cudaStream_t st);                         // aux streams wait for st
     void join(cudaStream_t st);                         // st waits for the aux streams
     // ---- graph capture (rp_graph_*).  graph_mode 1: an eager call planned
-    // from plan_traces (host [ns][9]) with target windows from host bounds;
+    // from plan_traces (host [ns][9]; a batch: plan_jobs, one per job) with
+    // target windows from host bounds;
     // 2: the same call under stream capture -- no host syncs or readbacks,
     // no tuning probes, job tables staged in the pinned arena, and each
     // segment's flags and counts copied into it (graph_rb) for
     // rp_graph_check after the replay.
     int graph_mode = 0;
     const double* plan_traces = nullptr;
+    std::vector<const double*> plan_jobs;
     char* pin = nullptr;            // pinned host arena (graph mode 2)
     size_t pin_cap = 0, pin_off = 0;
-    struct Readback { const int* misc; const int* cnt; int nb; int64_t s0; };
+    struct Readback { const int* misc; const int* cnt; int nb; int64_t s0; };   // s0: first trace, over all jobs
     std::vector<Readback> graph_rb;
     void* pin_take(size_t bytes) {                      // nullptr when full
         const size_t a = (pin_off + 255) & ~size_t(255);

@@ -164,7 +164,7 @@ class Scene:
         rc = _abi.lib().rp_graph_create(self._h, tr.ctypes.data, ctypes.c_void_p(d_traces.data_ptr()), ns,
                                         ctypes.c_void_p(d_out.data_ptr()), ctypes.byref(g))
         _abi.check("rp_graph_create", rc)
-        return Graph(g.value, ns, (self, d_traces, d_out))
+        return Graph(g.value, ns, (self, d_traces, d_out), d_traces.device)
 
     def simulate_host_ptrs(self, traces_ptr, ns, out_ptr, form="fast", stream=None, counts=None):
         """rp_simulate on raw host pointers (e.g. pinned torch tensors); runs
@@ -178,25 +178,27 @@ class Scene:
 
 
 class Graph:
-    """A captured fast-form call (Scene.capture): launch() replays the whole
-    call on a stream with one graph launch; check() after the replay has
-    finished returns the counts (ns, 2) or raises the status a direct call
-    would have raised."""
+    """A captured fast-form call (Scene.capture) or batch (capture_batch):
+    launch() replays the whole call on a stream with one graph launch; check()
+    after the replay has finished returns the counts (ns, 2; a batch's jobs
+    stacked in job order) or raises the status a direct call would have
+    raised."""
 
-    def __init__(self, handle, ns, keep):
+    def __init__(self, handle, ns, keep, device):
         self._h = handle
         self.ns = ns
-        self._keep = keep          # the scene and the device buffers the graph uses
+        self._keep = keep          # the scenes and the device buffers the graph uses
+        self.device = device
 
     def launch(self, stream=None):
-        dev = self._keep[1].device.index
-        _abi.check("rp_graph_launch", _abi.lib().rp_graph_launch(ctypes.c_void_p(self._h), stream_handle(stream, dev)))
+        _abi.check("rp_graph_launch", _abi.lib().rp_graph_launch(ctypes.c_void_p(self._h),
+                                                                 stream_handle(stream, self.device.index)))
 
     def check(self, stream=None):
         """Waits for ``stream`` (default: torch's current stream), then reads
         the replay's flags and counts."""
         import torch
-        (stream if stream is not None else torch.cuda.current_stream(self._keep[1].device)).synchronize()
+        (stream if stream is not None else torch.cuda.current_stream(self.device)).synchronize()
         counts = np.zeros((self.ns, 2), np.int64)
         _abi.check("rp_graph_check", _abi.lib().rp_graph_check(ctypes.c_void_p(self._h), counts.ctypes.data))
         return counts
@@ -295,6 +297,41 @@ def simulate_batch(jobs, workspace=None, stream=None, return_counts=False):
     _abi.check("rp_simulate_batch", rc)
     outs = [o.cpu().numpy() for o in d_out]
     return (outs, counts) if return_counts else outs
+
+
+def capture_batch(jobs, d_traces, d_outs):
+    """Record one simulate_batch call as a CUDA graph (rp_graph_create_batch).
+
+    ``jobs``: (Scene, traces (ns, 9) float64 on the host) pairs that plan the
+    call; ``d_traces[j]`` (ns_j, 9) float64 and ``d_outs[j]`` (ns_j, nr_j)
+    complex64 torch CUDA tensors are the buffers every replay reads and
+    writes, and must hold the traces when this is called (the call runs once
+    eagerly first).  Returns a :class:`Graph`; its check() stacks the jobs'
+    counts in job order."""
+    import torch
+    if not jobs or len(jobs) != len(d_traces) or len(jobs) != len(d_outs):
+        raise ValueError("capture_batch: one trace buffer and one output buffer per job")
+    arr = (_abi.RpJob * len(jobs))()
+    hs = []
+    for j, ((sc, tr), dt, do) in enumerate(zip(jobs, d_traces, d_outs)):
+        tr = np.ascontiguousarray(tr, dtype=np.float64).reshape(-1, 9)
+        ns = tr.shape[0]
+        if tuple(dt.shape) != (ns, 9) or tuple(do.shape) != (ns, sc.nr):
+            raise ValueError(f"capture_batch: job {j}: d_traces must be (ns, 9) and d_out (ns, nr)")
+        hs.append(tr)
+        arr[j] = _abi.RpJob(sc.handle, dt.data_ptr(), ns, do.data_ptr(), None)
+    ptrs = (ctypes.c_void_p * len(hs))(*[h.ctypes.data for h in hs])
+    torch.cuda.current_stream(d_traces[0].device).synchronize()     # inputs written before the eager run
+    g = ctypes.c_void_p()
+    rc = _abi.lib().rp_graph_create_batch(arr, len(jobs), ptrs, ctypes.byref(g))
+    _abi.check("rp_graph_create_batch", rc)
+    return Graph(g.value, sum(h.shape[0] for h in hs), (jobs, d_traces, d_outs, hs), d_traces[0].device)
+
+
+def split_parts(enable=True):
+    """Split the facet parts of small calls (rp_split_parts; on by default).
+    Off: every trace's result is bitwise independent of the call's shape."""
+    _abi.lib().rp_split_parts(1 if enable else 0)
 
 
 def autotune(enable=True):

@@ -201,8 +201,9 @@ typedef struct rp_job {
  * persistent kernel launch (a job table over all scenes' work items), range
  * compression in one launch per bin-count class.  No counterpart in the
  * reference, which runs one scene per process (sim.cu:615-1008); each
- * trace's result is bitwise the one rp_simulate_ws gives.  Every scene must
- * live on the workspace's device. */
+ * trace's result is bitwise the one rp_simulate_ws gives, unless the lone
+ * call splits its facet parts (rp_split_parts).  Every scene must live on
+ * the workspace's device. */
 int rp_simulate_batch(const rp_job* jobs, int njobs, rp_workspace* ws, void* stream);
 
 /*
@@ -232,6 +233,12 @@ int rp_simulate_batch(const rp_job* jobs, int njobs, rp_workspace* ws, void* str
 typedef struct rp_graph rp_graph;
 int rp_graph_create(rp_scene* s, const double* h_traces, const double* d_traces, int64_t ns, void* d_out,
                     rp_graph** out);
+/* A whole rp_simulate_batch call recorded as one graph: h_traces[j] is job
+ * j's trace table on the host (jobs[j].ns x 9, the layout of
+ * jobs[j].d_traces); jobs[j].counts is ignored (rp_graph_check writes the
+ * counts of every job in job order, sum of ns x 2).  Every scene must live on
+ * one device.  Replays equal direct rp_simulate_batch calls bit for bit. */
+int rp_graph_create_batch(const rp_job* jobs, int njobs, const double* const* h_traces, rp_graph** out);
 int rp_graph_launch(rp_graph* g, void* stream);
 int rp_graph_check(const rp_graph* g, int64_t* counts);
 int rp_graph_destroy(rp_graph* g);
@@ -243,6 +250,19 @@ int rp_graph_destroy(rp_graph* g);
  * sample of its work items and keeps the fastest for the process.  The
  * configurations give bitwise identical results. */
 int rp_autotune(int enable);
+
+/* Split facet parts (on by default).  A fast-form call of one segment whose
+ * pair-stage work items (traces x target blocks x 4 facet parts) fill at most
+ * half of the pair kernel's resident blocks -- one trace of a small scene, a
+ * small serving request -- splits each part's facet range further and folds
+ * the split rows back, compensated and in fixed order, before the range
+ * compression.  Calls of the same traces give identical results either way
+ * to FP32 rounding of each part's compensated sum: a split call can differ
+ * from the same trace computed in a larger call or a batch in the last bit
+ * (where a part's sum falls within its compensation error of a rounding
+ * boundary).  Off: every trace's result is bitwise independent of the call's
+ * shape, and small calls leave most of the GPU idle. */
+int rp_split_parts(int enable);
 /* The tuned configuration for (kind, degree), or -1 when not tuned yet.
  * multi: 0 the single-batch kernel (configurations 0-3), 1 multi-segment
  * waves (degree ignored; 0-3 the multi-scene kernel, 4-7 one single-batch

@@ -34,3 +34,13 @@ def oracle():
     from oracle import loader
     loader.lib()
     return loader
+
+
+@pytest.fixture
+def no_split_parts(built_lib):
+    """Split facet parts off for the test (rp_split_parts): a lone small call
+    then sums its parts in the same grouping as any larger call, so results
+    compare bitwise across call shapes."""
+    built_lib.rp_split_parts(0)
+    yield
+    built_lib.rp_split_parts(1)

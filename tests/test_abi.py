@@ -102,6 +102,14 @@ def test_graph_calls_reject_bad_arguments(built_lib):
     assert built_lib.rp_graph_launch(None, None) == -1
     assert built_lib.rp_graph_check(None, None) == -1
     assert built_lib.rp_graph_destroy(None) == 0
+    assert built_lib.rp_graph_create_batch(None, 1, None, ctypes.byref(g)) == -1
+    assert "rp_graph_create_batch" in _abi.last_error()
+    jobs = (_abi.RpJob * 1)()
+    ptrs = (ctypes.c_void_p * 1)()
+    assert built_lib.rp_graph_create_batch(jobs, 0, ptrs, ctypes.byref(g)) == -1
+    assert built_lib.rp_graph_create_batch(jobs, 1, ptrs, ctypes.byref(g)) == -1     # no scene
+    assert "job 0" in _abi.last_error()
+    assert built_lib.rp_split_parts(0) == 0 and built_lib.rp_split_parts(1) == 0
 
 
 @pytest.mark.parametrize("over,ttype", [({"convolution": False}, 1), ({"convolution_linear": False}, 1),

@@ -1,6 +1,7 @@
 """Many scenes in one call (rp_simulate_batch): the pair stage of every scene
 in one persistent launch.  Each job's radargram is bitwise the one the scene
-gives alone, and within the fast form's tolerance of the FP64 oracle; the
+gives alone (split facet parts off, so that no lone call regroups its part
+sums), and within the fast form's tolerance of the FP64 oracle; the
 pair-kernel configurations the autotuner chooses between give bitwise equal
 results; a scene with more traces than one segment (multi-job kernel) equals
 its traces run one at a time."""
@@ -35,7 +36,7 @@ def _bits(a):
     return np.ascontiguousarray(a).view(np.uint32)
 
 
-def test_batch_equals_single_and_oracle(built_lib, oracle):
+def test_batch_equals_single_and_oracle(built_lib, oracle, no_split_parts):
     from europaraypaths_gb300 import simulator, traces as tr_mod
     scs = _scenes()
     scenes = [simulator.Scene(s["params"], s["facets"], s["targets"]) for s in scs]
@@ -83,7 +84,7 @@ def test_batch_per_segment_launches_bitwise(built_lib):
             assert np.array_equal(_bits(a), _bits(b))
 
 
-def test_many_segments_multi_kernel(built_lib):
+def test_many_segments_multi_kernel(built_lib, no_split_parts):
     # 70 traces = two segments of one scene in one wave: the multi-job kernel
     from europaraypaths_gb300 import simulator, traces as tr_mod
     s = tiny_scene(nside=24, ntside=3, ns=70)

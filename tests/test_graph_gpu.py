@@ -3,7 +3,9 @@ ABI): the replay of the recorded call equals a direct rp_simulate_device call
 bit for bit -- on the traces the graph was planned with, and on other traces
 written into the same device buffer (the planned traces in reverse order, so
 the graph's capacities and windows still hold) -- with the same counts, on a
-single-segment and a multi-segment call, and replays repeat exactly."""
+single-segment and a multi-segment call, and replays repeat exactly; a whole
+batch of scenes (rp_graph_create_batch) replays the direct batch call bit for
+bit."""
 import numpy as np
 import pytest
 
@@ -77,3 +79,35 @@ def test_graph_multi_segment_call(built_lib):
             assert torch.equal(_bits(out), _bits(ref))
         finally:
             g.close()
+
+
+def test_graph_batch_equals_direct_batch(built_lib):
+    # one rp_simulate_batch call over three scenes (9 MHz at 2048 and 1024
+    # bins, 60 MHz at 4096 bins: a multi-segment wave, compression job tables
+    # of two length classes) recorded as one graph
+    import torch
+    from europaraypaths_gb300 import simulator, scenes as scn
+    scs = [tiny_scene(nside=40, ntside=4, ns=5),
+           tiny_scene(nside=30, ntside=3, ns=3, eps_2=4.0, rx_window_m=scn.rx_window_for_bins(1024, 4e6)),
+           vhf_scene(4096, n_side=120, ns=4)]
+    scenes = [simulator.Scene(s["params"], s["facets"], s["targets"]) for s in scs]
+    try:
+        trs = [np.ascontiguousarray(sc.default_traces()) for sc in scenes]
+        ref, cnt = simulator.simulate_batch(list(zip(scenes, trs)), return_counts=True)
+        d_tr = [torch.from_numpy(t).cuda() for t in trs]
+        d_out = [torch.zeros((t.shape[0], sc.nr), dtype=torch.complex64, device="cuda")
+                 for t, sc in zip(trs, scenes)]
+        g = simulator.capture_batch(list(zip(scenes, trs)), d_tr, d_out)
+        try:
+            for _ in range(2):
+                for o in d_out:
+                    o.fill_(complex(float("nan"), float("nan")))
+                g.launch()
+                assert np.array_equal(g.check(), np.concatenate(cnt))
+                for o, r in zip(d_out, ref):
+                    assert np.array_equal(o.cpu().numpy().view(np.uint32), np.ascontiguousarray(r).view(np.uint32))
+        finally:
+            g.close()
+    finally:
+        for sc in scenes:
+            sc.close()

@@ -1,6 +1,7 @@
 """Request loop: admission by device footprint, FIFO order, failure isolation,
 latency statistics (CPU, fake engine), and on the GPU that every request's
-radargram is bitwise the same alone and in a concurrent mix."""
+radargram is bitwise the same alone and in a concurrent mix (split facet
+parts off, so that a lone small call sums its parts as a larger one does)."""
 import threading
 import time
 
@@ -257,7 +258,7 @@ def test_configure_after_submit_refused():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("step", [0, 2])
-def test_gpu_same_alone_and_mixed(built_lib, step):
+def test_gpu_same_alone_and_mixed(built_lib, step, no_split_parts):
     from europaraypaths_gb300 import param_gen, simulator, traces as tr_mod
     from europaraypaths_gb300.serving import Server
     from europaraypaths_gb300 import scenes as scn
