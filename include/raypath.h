@@ -261,7 +261,8 @@ int rp_autotune(int enable);
  * from the same trace computed in a larger call or a batch in the last bit
  * (where a part's sum falls within its compensation error of a rounding
  * boundary).  Off: every trace's result is bitwise independent of the call's
- * shape, and small calls leave most of the GPU idle. */
+ * shape, and small calls leave most of the GPU idle.  Read when a call is
+ * planned: a graph keeps the choice it was recorded with. */
 int rp_split_parts(int enable);
 /* The tuned configuration for (kind, degree), or -1 when not tuned yet.
  * multi: 0 the single-batch kernel (configurations 0-3), 1 multi-segment
