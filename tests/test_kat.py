@@ -72,6 +72,16 @@ def _subsurface(h, d):
     return prm, fac, tg, Pr, phase
 
 
+# The reference's plots band these scenes at 0-5 % (power) and the phase is
+# compared in degrees.  The oracle's measured errors on the scenes below are
+# at most 1.7 % in power (fresnel 0.7-1.2 %, image 0.05-1.5 %, subsurface
+# target 0.28-1.7 %) and 4.5 degrees in phase (0.4 degrees at 5 km depth), so
+# the bars are tightened to 2.5 % and 6 degrees; the GPU forms agree with the
+# oracle to ~1e-7 and are held to the same bars.
+POWER_TOL = 2.5
+PHASE_TOL = 6.0
+
+
 def _check_power(out, Pr, tol_pct):
     Pnum = float(np.max(np.abs(out) ** 2))
     err = abs(Pnum - Pr) / Pr * 100
@@ -94,21 +104,21 @@ def _oracle_run(oracle, prm, fac, tg):
 @pytest.mark.parametrize("h", [200e3, 50e3])
 def test_kat_fresnel_zone_oracle(oracle, h):
     prm, fac, tg, Pr = _fresnel(h)
-    _check_power(_oracle_run(oracle, prm, fac, tg), Pr, 5.0)
+    _check_power(_oracle_run(oracle, prm, fac, tg), Pr, POWER_TOL)
 
 
 @pytest.mark.parametrize("h", [100e3, 25e3])
 def test_kat_image_theory_oracle(oracle, h):
     prm, fac, tg, Pr = _image(h)
-    _check_power(_oracle_run(oracle, prm, fac, tg), Pr, 5.0)
+    _check_power(_oracle_run(oracle, prm, fac, tg), Pr, POWER_TOL)
 
 
 @pytest.mark.parametrize("h,d", [(300e3, 250.0), (19e3, 250.0), (100e3, 5000.0)])
 def test_kat_subsurface_target_oracle(oracle, h, d):
     prm, fac, tg, Pr, ph = _subsurface(h, d)
     out = _oracle_run(oracle, prm, fac, tg)
-    _check_power(out, Pr, 5.0)
-    _check_phase(out, ph, 10.0)
+    _check_power(out, Pr, POWER_TOL)
+    _check_phase(out, ph, PHASE_TOL)
 
 
 # ------------------------------------------------------------------ GPU --
@@ -122,9 +132,9 @@ def _gpu_run(prm, fac, tg, form):
 @pytest.mark.parametrize("form", ["fast", "plain"])
 def test_kat_fresnel_and_image_gpu(built_lib, form):
     prm, fac, tg, Pr = _fresnel(125e3)
-    _check_power(_gpu_run(prm, fac, tg, form), Pr, 5.0)
+    _check_power(_gpu_run(prm, fac, tg, form), Pr, POWER_TOL)
     prm, fac, tg, Pr = _image(50e3)
-    _check_power(_gpu_run(prm, fac, tg, form), Pr, 5.0)
+    _check_power(_gpu_run(prm, fac, tg, form), Pr, POWER_TOL)
 
 
 @pytest.mark.gpu
@@ -133,8 +143,8 @@ def test_kat_subsurface_target_gpu(built_lib, form):
     for h, d in ((300e3, 250.0), (19e3, 5000.0)):
         prm, fac, tg, Pr, ph = _subsurface(h, d)
         out = _gpu_run(prm, fac, tg, form)
-        _check_power(out, Pr, 5.0)
-        _check_phase(out, ph, 10.0)
+        _check_power(out, Pr, POWER_TOL)
+        _check_phase(out, ph, PHASE_TOL)
 
 
 @pytest.mark.gpu
