@@ -112,10 +112,7 @@ __device__ __forceinline__ void fix_add(long long* p, double v, double scale) {
     atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)(long long)llrint(v * scale));
 }
 
-// Positive doubles order like their bit patterns: atomicMin/Max on bits.
-__device__ __forceinline__ void atomic_min_pos(unsigned long long* p, double v) {
-    atomicMin(p, (unsigned long long)__double_as_longlong(v));
-}
+// Positive doubles order like their bit patterns: atomicMax on bits.
 __device__ __forceinline__ void atomic_max_pos(unsigned long long* p, double v) {
     atomicMax(p, (unsigned long long)__double_as_longlong(v));
 }
@@ -238,8 +235,3 @@ __host__ __device__ __forceinline__ double rp_incoherent_turns(uint64_t seed, do
     return (double)(rp_mix64(key ^ (uint64_t)facet) >> 40) * (1.0 / 16777216.0);
 }
 
-__host__ __device__ __forceinline__ int ilog2(int n) {
-    int l = 0;
-    while ((1 << l) < n) ++l;
-    return l;
-}
